@@ -1,0 +1,301 @@
+"""Benchmark: visual observation Jacobian evaluations per second on the
+2,000-keyframe VI bundle-adjustment workload, plus BA time-to-cost-tolerance.
+
+One step = one robustified tangent-space linearization (residual + landmark,
+store-pose and observer-pose Jacobian blocks + Huber corrector + cost) of every
+visual observation of the workload, the evaluation half of one LM iteration.
+
+  value  : device-resident throughput of the evaluation kernel (mixed path:
+           FP32 Jacobians), CUDA events on the launching stream, L2 flushed
+           (256 MiB write) before every timed launch.
+  e2e    : the same metric through the C ABI with pinned HOST buffers: state
+           upload (mba_write_state), linearization, and the residuals and
+           Jacobians read back in the caller's order (mba_linearize_visual).
+  ba     : time-to-cost-tolerance of the device LM (plain FP64 vs mixed) on the
+           same map, 20 iterations, block-Jacobi PCG (<= 100 its, tol 1e-6).
+
+--impl reference times the CPU restatement of the reference's evaluation
+(oracle/, all host threads) on the same map.  Multi-GPU runs are independent
+replicas (the workload does not shard here): value is summed over ranks.
+"""
+import argparse
+import ctypes
+import json
+import os
+import statistics
+import subprocess
+import sys
+import threading
+import time
+
+ROOT = os.path.dirname(os.path.abspath(__file__))
+sys.path.insert(0, ROOT)
+
+METRIC = "obs Jacobian evals/s"
+WORKLOAD = "C2: plain method on GPU, 2,000 keyframes, 200k landmarks, ~1.6M observations, 2 cameras (radtan + equidistant)"
+
+
+def _dist():
+    ws = int(os.environ.get("WORLD_SIZE", "1"))
+    rank = int(os.environ.get("RANK", "0"))
+    local = int(os.environ.get("LOCAL_RANK", "0"))
+    return ws, rank, local
+
+
+class ClockSampler:
+    """nvidia-smi clocks / throttle reasons sampled during the timed region."""
+
+    def __init__(self, index):
+        self.index = index
+        self.samples = []
+        self.proc = None
+
+    def __enter__(self):
+        q = ("index,clocks.sm,clocks.max.sm,power.draw,clocks_event_reasons.active,"
+             "clocks_event_reasons.hw_slowdown,clocks_event_reasons.hw_thermal_slowdown,"
+             "clocks_event_reasons.sw_thermal_slowdown,clocks_event_reasons.sw_power_cap")
+        try:
+            self.proc = subprocess.Popen(["nvidia-smi", f"--id={self.index}", f"--query-gpu={q}",
+                                          "--format=csv,noheader,nounits", "-lms", "200"],
+                                         stdout=subprocess.PIPE, stderr=subprocess.DEVNULL, text=True)
+            self.reader = threading.Thread(target=self._read, daemon=True)
+            self.reader.start()
+        except OSError:
+            self.proc = None
+        return self
+
+    def _read(self):
+        for line in self.proc.stdout:
+            parts = [p.strip() for p in line.split(",")]
+            if len(parts) >= 9:
+                self.samples.append(parts)
+
+    def __exit__(self, *a):
+        if self.proc:
+            time.sleep(0.25)
+            self.proc.terminate()
+            try:
+                self.proc.wait(timeout=5)
+            except subprocess.TimeoutExpired:
+                self.proc.kill()
+
+    def summary(self):
+        if not self.samples:
+            return {"sm_mhz": None, "sm_max_mhz": None, "reasons": ["unsampled"]}
+        sm = [float(s[1]) for s in self.samples if s[1].replace(".", "").isdigit()]
+        mx = [float(s[2]) for s in self.samples if s[2].replace(".", "").isdigit()]
+        names = ["hw_slowdown", "hw_thermal_slowdown", "sw_thermal_slowdown", "sw_power_cap"]
+        reasons = sorted({names[i] for s in self.samples for i in range(4) if "Active" in s[5 + i]})
+        return {"sm_mhz": statistics.median(sm) if sm else None, "sm_max_mhz": max(mx) if mx else None,
+                "reasons": reasons, "samples": len(self.samples)}
+
+
+def _peaks():
+    try:
+        return json.load(open(os.path.join(ROOT, "MEASURED_PEAKS.json"))), "measured"
+    except OSError:
+        return {"hbm_gbs": 6800.0, "bf16_tflops": 1900.0}, "fallback"
+
+
+def _traffic_summary():
+    try:
+        return json.load(open(os.path.join(ROOT, "profiles", "visual_linearize_c2_traffic.json")))
+    except OSError:
+        return None
+
+
+def _make_map(args):
+    from maplab_gb300 import synth
+    return synth.generate(args.config)
+
+
+def run_reference(args):
+    ws, rank, local = _dist()
+    if rank != 0:
+        return
+    sys.path.insert(0, os.path.join(ROOT, "tests"))
+    import oracle_lib
+    m = _make_map(args)
+    n = m.desc.num_observations
+    threads = os.cpu_count() or 1
+    o = oracle_lib.OracleProblem(m.desc, threads=threads)
+    sample = min(n, args.cpu_sample)
+    for _ in range(args.warmup):
+        o.time_visual(threads, sample, 1)
+    t = [o.time_visual(threads, sample, 1) for _ in range(args.steps)]
+    sec = sum(t) / len(t)
+    v = sample / sec
+    line = {
+        "impl": "reference", "metric": METRIC, "value": v, "unit": "evals/s", "n_gpus": ws, "steps": args.steps,
+        "warmup": args.warmup, "ms_per_step": sec * 1e3, "higher_is_better": True, "scaling": "weak",
+        "vs_baseline": None, "dtype": "f64", "data": "synthetic (seeded generator restating vi-map-generator-6dof)",
+        "config": {"workload": WORKLOAD, "observations": n, "sample_per_step": sample},
+        "cpu_baseline": {"value": v, "unit": "evals/s", "cores": threads, "kind": "port",
+                         "sample": f"{sample} observations per step of the {n}-observation workload"},
+        "e2e": {"value": v, "unit": "evals/s", "h2d_bytes_per_step": 0, "d2h_bytes_per_step": 0},
+    }
+    print(json.dumps(line), flush=True)
+
+
+def run_ours(args):
+    import numpy as np
+    import torch
+    from maplab_gb300 import _native as N
+    from maplab_gb300 import ba
+
+    ws, rank, local = _dist()
+    if ws > 1:
+        import torch.distributed as dist
+        dist.init_process_group("nccl", device_id=torch.device("cuda", local))
+    torch.cuda.set_device(local)
+
+    def barrier():
+        if ws > 1:
+            import torch.distributed as dist
+            dist.barrier()
+        torch.cuda.synchronize()
+
+    def max_over_ranks(x):
+        if ws == 1:
+            return x
+        import torch.distributed as dist
+        t = torch.tensor([x], dtype=torch.float64, device="cuda")
+        dist.all_reduce(t, op=dist.ReduceOp.MAX)
+        return float(t.item())
+
+    m = _make_map(args)
+    d = m.desc
+    n, nl, nk = d.num_observations, d.num_landmarks, d.num_keyframes
+    g = ba.BundleAdjuster(d, device=local)
+
+    # ---- value: device-resident kernel throughput (mixed FP32 Jacobians)
+    g.time_visual_kernel(mode=1, iters=max(args.warmup, 3))
+    with ClockSampler(local) as clk:
+        barrier()
+        t0 = time.perf_counter()
+        ms32 = g.time_visual_kernel(mode=1, iters=args.steps)
+        barrier()
+        wall = time.perf_counter() - t0
+    ms32 = max_over_ranks(ms32)
+    ms64 = max_over_ranks(g.time_visual_kernel(mode=0, iters=max(3, args.steps // 2)))
+    value = ws * n / (ms32 * 1e-3)
+
+    # ---- e2e through the C ABI with pinned host buffers
+    st = g.read_state()
+    pin = lambda a: torch.from_numpy(np.ascontiguousarray(a)).pin_memory()
+    h_kx, h_kv, h_kbg, h_kba, h_lp = (pin(st[k]) for k in ("kf_q_IM_p_MI", "kf_v_M", "kf_b_g", "kf_b_a", "lm_p_B"))
+    out = [torch.empty((n, c), dtype=torch.float64).pin_memory() for c in (2, 6, 12, 12)]
+    P = lambda t: ctypes.cast(t.data_ptr(), N.c_double_p)
+    lib = ba.lib()
+
+    def e2e_step():
+        assert lib.mba_write_state(g.handle, P(h_kx), P(h_kv), P(h_kbg), P(h_kba), P(h_lp)) == 0
+        assert lib.mba_linearize_visual(g.handle, N.MBA_PRECISION_MIXED, *[P(o) for o in out]) == 0
+
+    for _ in range(args.warmup):
+        e2e_step()
+    barrier()
+    t0 = time.perf_counter()
+    for _ in range(args.steps):
+        e2e_step()
+    barrier()
+    e2e_sec = max_over_ranks((time.perf_counter() - t0) / args.steps)
+    h2d = 8 * (16 * nk + 3 * nl)
+    d2h = 8 * 32 * n
+
+    # ---- roofline of the evaluation kernel
+    peaks, peak_kind = _peaks()
+    alg_bytes = 40 * n + 24 * nl + 56 * nk + 128 * n
+    achieved = alg_bytes / (ms32 * 1e-3) / 1e9
+    tr = _traffic_summary()
+    roof = {"bound": "hbm", "achieved": achieved, "peak": peaks["hbm_gbs"], "unit": "GB/s",
+            "frac": achieved / peaks["hbm_gbs"], "peak_kind": peak_kind,
+            "traffic": (tr["dram_bytes_per_launch"] if tr else None),
+            "algorithmic_bytes_per_launch": alg_bytes}
+
+    # ---- BA time-to-cost-tolerance: plain FP64 vs mixed (rank-local)
+    ba_info = None
+    if args.solve:
+        ba_info = {}
+        opts64 = ba.default_options(max_num_iterations=20, max_linear_iterations=100, linear_tolerance=1e-6,
+                                    check_tolerances=0)
+        g64 = ba.BundleAdjuster(d, device=local)
+        s64 = g64.solve(opts64)
+        g64.close()
+        target = s64["final_cost"] * (1 + 1e-6)
+        opts32 = ba.default_options(max_num_iterations=40, max_linear_iterations=100, linear_tolerance=1e-6,
+                                    check_tolerances=0, precision=N.MBA_PRECISION_MIXED, stop_cost=target)
+        g32 = ba.BundleAdjuster(d, device=local)
+        s32 = g32.solve(opts32)
+        g32.close()
+        ba_info = {"fp64_20_iters_s": s64["total_time_ms"] / 1e3, "fp64_final_cost": s64["final_cost"],
+                   "fp64_initial_cost": s64["initial_cost"], "fp64_pcg_iterations": s64["linear_iterations"],
+                   "mixed_time_to_cost_tol_s": (s32["time_to_stop_cost_ms"] / 1e3
+                                                if s32["time_to_stop_cost_ms"] >= 0 else None),
+                   "mixed_final_cost": s32["final_cost"], "mixed_iterations": s32["num_iterations"] - 1,
+                   "cost_tolerance": "1e-6 relative to the FP64 path's 20-iteration cost"}
+
+    # ---- CPU baseline (rank 0, N=1 only): the oracle on the host cores
+    cpu = None
+    if rank == 0 and ws == 1 and not args.skip_cpu:
+        sys.path.insert(0, os.path.join(ROOT, "tests"))
+        import oracle_lib
+        threads = os.cpu_count() or 1
+        o = oracle_lib.OracleProblem(d, threads=threads)
+        sample = min(n, args.cpu_sample)
+        o.time_visual(threads, sample, 1)
+        reps = max(1, int(10.0 / max(1e-3, o.time_visual(threads, sample, 1))))
+        sec = o.time_visual(threads, sample, min(reps, 200))
+        cpu = {"value": sample / sec, "unit": "evals/s", "cores": threads, "kind": "port",
+               "sample": f"{sample} of {n} observations per pass, {min(reps, 200)} passes (about 10 s)"}
+
+    if rank == 0:
+        line = {
+            "metric": METRIC, "value": value, "unit": "evals/s", "n_gpus": ws, "steps": args.steps,
+            "warmup": args.warmup, "ms_per_step": ms32, "higher_is_better": True, "scaling": "weak",
+            "vs_baseline": None, "dtype": "f32",
+            "data": "synthetic (seeded generator restating test/vi-map-generator-6dof; no public dataset)",
+            "config": {"workload": WORKLOAD, "observations": n, "landmarks": nl, "keyframes": nk,
+                       "precision": "mixed: FP32 Jacobians/residuals, FP64 inputs and cost",
+                       "l2": "256 MiB write before every timed launch (L2 flushed)",
+                       "fp64_kernel_ms": ms64, "fp64_evals_per_s": ws * n / (ms64 * 1e-3),
+                       "timed_wall_s": wall, "parallelism": f"replicas x{ws}"},
+            "e2e": {"value": ws * n / e2e_sec, "unit": "evals/s", "h2d_bytes_per_step": h2d, "d2h_bytes_per_step": d2h},
+            "roofline": roof,
+            "cpu_baseline": cpu,
+            "clocks": clk.summary(),
+            "gpu_launches": args.steps,
+            "ba_time_to_cost_tol": ba_info,
+        }
+        print(json.dumps(line), flush=True)
+    g.close()
+    if ws > 1:
+        import torch.distributed as dist
+        dist.destroy_process_group()
+
+
+def main():
+    ap = argparse.ArgumentParser()
+    ap.add_argument("--gpus", type=int, default=1)
+    ap.add_argument("--steps", type=int, default=20)
+    ap.add_argument("--warmup", type=int, default=5)
+    ap.add_argument("--impl", default="ours", choices=["ours", "reference"])
+    ap.add_argument("--config", default="c2")
+    ap.add_argument("--cpu-sample", type=int, default=400_000)
+    ap.add_argument("--solve", type=int, default=1)
+    ap.add_argument("--skip-cpu", action="store_true")
+    args = ap.parse_args()
+    if args.warmup < 3:
+        args.warmup = 3
+    from maplab_gb300 import build
+    build.build()
+    if args.impl == "reference":
+        subprocess.check_call(["make", "-s", "-C", os.path.join(ROOT, "oracle")])
+        run_reference(args)
+    else:
+        subprocess.check_call(["make", "-s", "-C", os.path.join(ROOT, "oracle")])
+        run_ours(args)
+
+
+if __name__ == "__main__":
+    main()

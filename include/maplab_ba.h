@@ -1,0 +1,277 @@
+/*
+ * maplab_ba.h — C ABI of the GB300 visual-inertial bundle-adjustment back-end.
+ *
+ * Plain C types only (no Eigen, no Ceres, no torch).  All arrays are
+ * structure-of-arrays, row-major, FP64 unless stated.  Quaternions are stored
+ * xyzw and interpreted as JPL (passive), exactly like maplab's
+ * OptimizationStateBuffer.  Poses are 7-vectors [q_xyzw, p].
+ *
+ * The entry points replace three reference interfaces:
+ *   1. map_optimization::VIMapOptimizer::optimize
+ *        algorithms/map-optimization/include/map-optimization/vi-map-optimizer.h:21-39
+ *        algorithms/map-optimization/src/vi-map-optimizer.cc:34-78
+ *      and map_optimization::solve (src/solver.cc:14-44)      -> mba_create + mba_solve
+ *   2. ceres::CostFunction::Evaluate of VisualReprojectionError and
+ *      InertialErrorTerm
+ *        algorithms/ceres-error-terms/include/ceres-error-terms/visual-error-term-inl.h:12-379
+ *        algorithms/ceres-error-terms/src/inertial-error-term.cc:77-286
+ *                                         -> mba_evaluate_visual / mba_evaluate_inertial
+ *   3. ceres_error_terms::ProblemInformation + OptimizationStateBuffer
+ *        algorithms/ceres-error-terms/include/ceres-error-terms/problem-information.h:18-140
+ *        algorithms/map-optimization/src/optimization-state-buffer.cc:42-264
+ *                                         -> mba_problem_desc, mba_read_state / mba_write_state
+ *
+ * Errors are returned as mba_status codes; no entry point aborts the process.
+ * One handle per host thread; every handle owns one CUDA stream.
+ */
+#ifndef MAPLAB_BA_H_
+#define MAPLAB_BA_H_
+
+#include <stddef.h>
+#include <stdint.h>
+
+#ifdef __cplusplus
+extern "C" {
+#endif
+
+#define MBA_ABI_VERSION 1
+
+typedef enum mba_status {
+  MBA_OK = 0,
+  MBA_ERR_INVALID_ARG = 1,
+  MBA_ERR_OUT_OF_RANGE_INDEX = 2,
+  MBA_ERR_NON_FINITE = 3,
+  MBA_ERR_NOT_SPD = 4,
+  MBA_ERR_CUDA = 5,
+  MBA_ERR_TIMEOUT = 6,
+  MBA_ERR_CANCELLED = 7,
+  MBA_ERR_NO_DEVICE = 8,
+  MBA_ERR_UNORDERED_IMU = 9
+} mba_status;
+
+/* ceres_error_terms::LandmarkErrorType (ceres-error-terms/common.h:14). */
+enum { MBA_LOCAL_KEYFRAME = 0, MBA_LOCAL_MISSION = 1, MBA_GLOBAL = 2 };
+
+/* aslam::Distortion::Type subset: pinhole + {none, radtan, equidistant}. */
+enum { MBA_DISTORTION_NONE = 0, MBA_DISTORTION_RADTAN = 1, MBA_DISTORTION_EQUIDISTANT = 2 };
+
+/* Per-keyframe fix flags (kf_flags).  They restate the Ceres parameter-block
+ * constness and local parameterizations chosen by the problem builder:
+ * ba_fix_vertices / ba_fix_velocity / ba_fix_gyro_bias / ba_fix_accel_bias
+ * (map-optimization/src/vi-optimization-builder.cc:36-47) and the gauge fix of
+ * the first vertex of a mission cluster (src/optimization-problem.cc:19-75). */
+enum {
+  MBA_KF_POSE_CONSTANT = 1u << 0,       /* whole 7-dof pose block constant */
+  MBA_KF_GAUGE_ROLL_PITCH = 1u << 1,    /* JplRollPitchQuaternionParameterization + position fixed */
+  MBA_KF_VELOCITY_CONSTANT = 1u << 2,
+  MBA_KF_GYRO_BIAS_CONSTANT = 1u << 3,
+  MBA_KF_ACCEL_BIAS_CONSTANT = 1u << 4,
+  MBA_KF_POSITION_CONSTANT = 1u << 5,   /* SubsetParameterization(3,{0,1,2}) on the position */
+  MBA_KF_ROTATION_CONSTANT = 1u << 6    /* FixedRotationDoF::kAll: rotation constant */
+};
+
+typedef struct mba_camera {
+  double intrinsics[4];   /* fu, fv, cu, cv */
+  double distortion[4];   /* radtan: k1 k2 p1 p2; equidistant: k1 k2 k3 k4 */
+  int32_t distortion_type;/* MBA_DISTORTION_* */
+  int32_t width, height;  /* image size in pixels (isKeypointVisible) */
+  int32_t pad_;
+  double q_CI_p_CI[7];    /* extrinsics: JPL q_C_I, then p_C_I */
+} mba_camera;
+
+typedef struct mba_problem_desc {
+  int64_t num_keyframes;
+  int64_t num_landmarks;
+  int64_t num_observations;
+  int64_t num_cameras;
+  int64_t num_missions;
+  int64_t num_imu_edges;      /* 0 => purely visual problem */
+  int64_t num_imu_samples;    /* total samples over all edges */
+
+  /* Visual observations (one VisualReprojectionError each). */
+  const double* obs_uv;       /* [N_obs][2] distorted keypoint measurement */
+  const double* obs_sigma;    /* [N_obs] keypoint uncertainty in px (> 0) */
+  const int32_t* obs_landmark;/* [N_obs] */
+  const int32_t* obs_keyframe;/* [N_obs] observer vertex */
+  const int32_t* obs_camera;  /* [N_obs] */
+
+  /* Landmarks: p_B expressed in the IMU frame of their store vertex. */
+  const double* lm_p_B;             /* [N_lm][3] */
+  const int32_t* lm_store_keyframe; /* [N_lm] */
+  const uint8_t* lm_constant;       /* [N_lm] or NULL (ba_fix_landmark_positions) */
+
+  /* Keyframes (vertices). */
+  const double* kf_q_IM_p_MI; /* [N_kf][7] */
+  const double* kf_v_M;       /* [N_kf][3] */
+  const double* kf_b_g;       /* [N_kf][3] */
+  const double* kf_b_a;       /* [N_kf][3] */
+  const int32_t* kf_mission;  /* [N_kf] */
+  const uint32_t* kf_flags;   /* [N_kf] MBA_KF_* bits, or NULL */
+
+  /* Missions: baseframe pose q_G_M (JPL) | p_G_M; always constant here. */
+  const double* mission_q_GM_p_GM; /* [N_mis][7] */
+
+  const mba_camera* cameras;  /* [N_cam]; intrinsics/extrinsics constant */
+
+  /* Inertial edges (one InertialErrorTerm each). Samples of edge e are
+   * imu_*[edge_sample_offset[e] .. edge_sample_offset[e+1]). */
+  const int32_t* edge_from;          /* [N_e] */
+  const int32_t* edge_to;            /* [N_e] */
+  const int64_t* edge_sample_offset; /* [N_e + 1] */
+  const int64_t* imu_timestamp_ns;   /* [N_s] */
+  const double* imu_acc_gyro;        /* [N_s][6]: acc xyz, gyro xyz */
+  double gyro_noise_sigma, gyro_bias_sigma, acc_noise_sigma, acc_bias_sigma;
+  double gravity_magnitude;
+
+  /* Robust loss on visual terms (optimization-terms-addition.cc:189-198):
+   * HuberLoss(delta * sigma) with delta = 3 (local) or 10 (global).
+   * use_huber = 0 disables the loss (plain least squares). */
+  int32_t use_huber;
+  int32_t pad_;
+  double huber_delta_local;
+  double huber_delta_global;
+} mba_problem_desc;
+
+/* Subset of ceres::Solver::Options used by map_optimization
+ * (include/map-optimization/solver-options.h:26-75), same names and defaults
+ * as the ba_* gflags (src/solver-options.cc:3-52). */
+enum { MBA_LINEAR_SOLVER_PCG = 0, MBA_LINEAR_SOLVER_DENSE_SCHUR = 1 };
+enum { MBA_PRECOND_BLOCK_JACOBI = 0, MBA_PRECOND_LEARNED = 1 };
+enum { MBA_PRECISION_FP64 = 0, MBA_PRECISION_MIXED = 1 };
+
+typedef struct mba_solver_options {
+  int32_t max_num_iterations;          /* ba_num_iterations = 30 */
+  int32_t jacobi_scaling;              /* ba_use_jacobi_scaling = 1 */
+  double initial_trust_region_radius;  /* 1e5 */
+  double max_trust_region_radius;      /* 1e20 */
+  double min_trust_region_radius;      /* 1e-32 */
+  double function_tolerance;           /* 1e-12 */
+  double gradient_tolerance;           /* 1e-10 */
+  double parameter_tolerance;          /* 1e-8 */
+  double min_relative_decrease;        /* 1e-3 (Ceres default) */
+  double min_lm_diagonal;              /* 1e-6 (Ceres default) */
+  double max_lm_diagonal;              /* 1e32 (Ceres default) */
+  int32_t linear_solver;               /* MBA_LINEAR_SOLVER_* */
+  int32_t max_linear_iterations;       /* PCG cap (100) */
+  double linear_tolerance;             /* PCG relative residual tolerance (1e-6) */
+  int32_t precision;                   /* MBA_PRECISION_* */
+  int32_t preconditioner;              /* MBA_PRECOND_* */
+  int32_t use_cuda_graph;              /* capture each LM iteration as a graph */
+  int32_t check_tolerances;            /* 1: stop on function/gradient/parameter tolerance */
+  double stop_cost;                    /* >0: stop as soon as cost <= stop_cost */
+} mba_solver_options;
+
+/* Mirrors the columns of ceres::IterationSummary printed by maplab's
+ * OutlierRejectionCallback (outlier-rejection-solver.h:29-68). */
+typedef struct mba_iteration_summary {
+  int32_t iteration;
+  int32_t step_is_successful;
+  int32_t linear_solver_iterations;
+  int32_t pad_;
+  double cost;
+  double cost_change;
+  double gradient_max_norm;
+  double step_norm;
+  double relative_decrease;
+  double trust_region_radius;
+  double iteration_time_ms;
+} mba_iteration_summary;
+
+typedef struct mba_summary {
+  int32_t num_iterations;         /* entries written to `iterations` */
+  int32_t num_successful_steps;
+  int32_t termination;            /* 0 max iterations, 1 function tol, 2 gradient tol,
+                                     3 parameter tol, 4 min radius, 5 cancelled, 6 stop_cost */
+  int32_t total_linear_iterations;
+  double initial_cost;
+  double final_cost;
+  double total_time_ms;
+  double time_to_stop_cost_ms;    /* -1 if stop_cost was not reached */
+  int32_t max_iterations_capacity;/* caller sets: length of `iterations` */
+  int32_t pad_;
+  mba_iteration_summary* iterations; /* caller-owned, may be NULL */
+} mba_summary;
+
+typedef struct mba_handle mba_handle;
+
+/* Library / ABI version (MBA_ABI_VERSION). */
+int32_t mba_abi_version(void);
+
+/* Fills opts with the maplab ba_* flag defaults (solver-options.cc:3-52). */
+void mba_default_solver_options(mba_solver_options* opts);
+
+/* Text for a status code. */
+const char* mba_status_string(mba_status s);
+
+/* Validates the descriptor (indices in range, sigmas > 0, quaternions unit
+ * within 1e-5 like assertValidQuaternion, IMU timestamps ordered), copies all
+ * arrays to device memory and builds the Schur pattern.  Caller arrays are not
+ * retained.  Replaces constructOptimizationProblem + OptimizationStateBuffer::
+ * importStatesOfMissions (vi-optimization-builder.cc:154-374,
+ * optimization-state-buffer.cc:153-264). */
+mba_status mba_create(const mba_problem_desc* desc, int32_t device, mba_handle** out);
+
+void mba_destroy(mba_handle* h);
+
+/* Batched ceres::CostFunction::Evaluate of every VisualReprojectionError at the
+ * current state (visual-error-term-inl.h:12-379).  residuals: [N_obs][2] or
+ * NULL.  jacobians: NULL or an array of 9 pointers (landmark p [N][2x3],
+ * landmark-base pose [N][2x7], landmark-mission baseframe [N][2x7],
+ * observer-mission baseframe [N][2x7], observer pose [N][2x7], q_C_I [N][2x4],
+ * p_C_I [N][2x3], intrinsics [N][2x4], distortion [N][2x4]), each NULL to
+ * skip, in the ambient row-major layout Ceres receives.  Host pointers.  The
+ * raw (un-robustified) residual is returned, as Evaluate does. */
+mba_status mba_evaluate_visual(mba_handle* h, double* residuals, double* const* jacobians);
+
+/* Batched InertialErrorTerm::Evaluate (inertial-error-term.cc:77-286).
+ * residuals: [N_e][15] or NULL; jacobians: NULL or 8 pointers (pose_from
+ * [N][15x7], b_g_from [N][15x3], v_from, b_a_from, pose_to, b_g_to, v_to,
+ * b_a_to), each NULL to skip.  Host pointers. */
+mba_status mba_evaluate_inertial(mba_handle* h, double* residuals, double* const* jacobians);
+
+/* Tangent-space (post local-parameterization) Jacobians the solver uses, with
+ * the Huber correction applied, for parity tests of the solver path.
+ * precision MBA_PRECISION_FP64 or MBA_PRECISION_MIXED (FP32 Jacobians).
+ * Outputs (host, FP64, may be NULL): r [N][2], J_landmark [N][2x3],
+ * J_store [N][2x6], J_observer [N][2x6]. */
+mba_status mba_linearize_visual(mba_handle* h, int32_t precision, double* r,
+                                double* J_landmark, double* J_store, double* J_observer);
+
+/* Ceres-style total cost 0.5 * sum rho(|r|^2) at the current state. */
+mba_status mba_cost(mba_handle* h, int32_t precision, double* cost);
+
+/* Runs Levenberg-Marquardt on the device (ceres::Solve with the options of
+ * solver-options.h:26-75).  The state stays on the device; read it back with
+ * mba_read_state.  summary may be NULL. */
+mba_status mba_solve(mba_handle* h, const mba_solver_options* opts, mba_summary* summary);
+
+/* OptimizationStateBuffer analogue: copy the optimized state out / in.
+ * Any pointer may be NULL.  Shapes as in mba_problem_desc. */
+mba_status mba_read_state(mba_handle* h, double* kf_q_IM_p_MI, double* kf_v_M,
+                          double* kf_b_g, double* kf_b_a, double* lm_p_B);
+mba_status mba_write_state(mba_handle* h, const double* kf_q_IM_p_MI, const double* kf_v_M,
+                           const double* kf_b_g, const double* kf_b_a, const double* lm_p_B);
+
+/* Thread-safe request to stop after the current LM iteration (the SIGINT
+ * handler of ceres-error-terms/src/ceres-signal-handler.cc:12-56). */
+void mba_cancel(mba_handle* h);
+
+/* Timing of the visual evaluation kernel alone over `iters` launches with
+ * the inputs resident on the device (CUDA events on the handle's stream).
+ * mode 0: FP64 tangent linearization, 1: FP32 tangent linearization.
+ * Writes the mean milliseconds per launch. */
+mba_status mba_time_visual_kernel(mba_handle* h, int32_t mode, int32_t iters, double* ms_per_launch);
+
+/* Problem statistics (for reports): sizes of the reduced camera system. */
+typedef struct mba_problem_stats {
+  int64_t num_keyframes, num_landmarks, num_observations, num_imu_edges;
+  int64_t num_schur_pose_blocks;   /* off-diagonal 6x6 pose-pose blocks (both triangles) */
+  int64_t device_bytes;            /* bytes held on the device by the handle */
+} mba_problem_stats;
+mba_status mba_get_stats(mba_handle* h, mba_problem_stats* stats);
+
+#ifdef __cplusplus
+}
+#endif
+
+#endif /* MAPLAB_BA_H_ */

@@ -1,0 +1,310 @@
+"""ctypes mirrors of include/maplab_ba.h and include/maplab_ba_synth.h.
+
+The structures below follow the C declarations field by field; ctypes applies
+the platform C alignment rules, so the layouts match on x86_64 and aarch64.
+"""
+import ctypes
+import os
+
+import numpy as np
+
+_HERE = os.path.dirname(os.path.abspath(__file__))
+BUILD_DIR = os.path.join(_HERE, "_build")
+
+c_double_p = ctypes.POINTER(ctypes.c_double)
+c_int32_p = ctypes.POINTER(ctypes.c_int32)
+c_int64_p = ctypes.POINTER(ctypes.c_int64)
+c_uint8_p = ctypes.POINTER(ctypes.c_uint8)
+c_uint32_p = ctypes.POINTER(ctypes.c_uint32)
+
+# mba_status
+MBA_OK = 0
+MBA_ERR_INVALID_ARG = 1
+MBA_ERR_OUT_OF_RANGE_INDEX = 2
+MBA_ERR_NON_FINITE = 3
+MBA_ERR_NOT_SPD = 4
+MBA_ERR_CUDA = 5
+MBA_ERR_TIMEOUT = 6
+MBA_ERR_CANCELLED = 7
+MBA_ERR_NO_DEVICE = 8
+MBA_ERR_UNORDERED_IMU = 9
+
+MBA_LOCAL_KEYFRAME, MBA_LOCAL_MISSION, MBA_GLOBAL = 0, 1, 2
+MBA_DISTORTION_NONE, MBA_DISTORTION_RADTAN, MBA_DISTORTION_EQUIDISTANT = 0, 1, 2
+
+MBA_KF_POSE_CONSTANT = 1 << 0
+MBA_KF_GAUGE_ROLL_PITCH = 1 << 1
+MBA_KF_VELOCITY_CONSTANT = 1 << 2
+MBA_KF_GYRO_BIAS_CONSTANT = 1 << 3
+MBA_KF_ACCEL_BIAS_CONSTANT = 1 << 4
+MBA_KF_POSITION_CONSTANT = 1 << 5
+MBA_KF_ROTATION_CONSTANT = 1 << 6
+
+MBA_LINEAR_SOLVER_PCG, MBA_LINEAR_SOLVER_DENSE_SCHUR = 0, 1
+MBA_PRECOND_BLOCK_JACOBI, MBA_PRECOND_LEARNED = 0, 1
+MBA_PRECISION_FP64, MBA_PRECISION_MIXED = 0, 1
+
+MBA_SYNTH_LANDMARKS_BOX, MBA_SYNTH_LANDMARKS_FRUSTUM = 0, 1
+MBA_SYNTH_TRACK_UNIFORM, MBA_SYNTH_TRACK_GEOMETRIC, MBA_SYNTH_TRACK_POWER_LAW = 0, 1, 2
+
+
+class Camera(ctypes.Structure):
+    _fields_ = [
+        ("intrinsics", ctypes.c_double * 4),
+        ("distortion", ctypes.c_double * 4),
+        ("distortion_type", ctypes.c_int32),
+        ("width", ctypes.c_int32),
+        ("height", ctypes.c_int32),
+        ("pad_", ctypes.c_int32),
+        ("q_CI_p_CI", ctypes.c_double * 7),
+    ]
+
+
+class ProblemDesc(ctypes.Structure):
+    _fields_ = [
+        ("num_keyframes", ctypes.c_int64),
+        ("num_landmarks", ctypes.c_int64),
+        ("num_observations", ctypes.c_int64),
+        ("num_cameras", ctypes.c_int64),
+        ("num_missions", ctypes.c_int64),
+        ("num_imu_edges", ctypes.c_int64),
+        ("num_imu_samples", ctypes.c_int64),
+        ("obs_uv", c_double_p),
+        ("obs_sigma", c_double_p),
+        ("obs_landmark", c_int32_p),
+        ("obs_keyframe", c_int32_p),
+        ("obs_camera", c_int32_p),
+        ("lm_p_B", c_double_p),
+        ("lm_store_keyframe", c_int32_p),
+        ("lm_constant", c_uint8_p),
+        ("kf_q_IM_p_MI", c_double_p),
+        ("kf_v_M", c_double_p),
+        ("kf_b_g", c_double_p),
+        ("kf_b_a", c_double_p),
+        ("kf_mission", c_int32_p),
+        ("kf_flags", c_uint32_p),
+        ("mission_q_GM_p_GM", c_double_p),
+        ("cameras", ctypes.POINTER(Camera)),
+        ("edge_from", c_int32_p),
+        ("edge_to", c_int32_p),
+        ("edge_sample_offset", c_int64_p),
+        ("imu_timestamp_ns", c_int64_p),
+        ("imu_acc_gyro", c_double_p),
+        ("gyro_noise_sigma", ctypes.c_double),
+        ("gyro_bias_sigma", ctypes.c_double),
+        ("acc_noise_sigma", ctypes.c_double),
+        ("acc_bias_sigma", ctypes.c_double),
+        ("gravity_magnitude", ctypes.c_double),
+        ("use_huber", ctypes.c_int32),
+        ("pad_", ctypes.c_int32),
+        ("huber_delta_local", ctypes.c_double),
+        ("huber_delta_global", ctypes.c_double),
+    ]
+
+
+class SolverOptions(ctypes.Structure):
+    _fields_ = [
+        ("max_num_iterations", ctypes.c_int32),
+        ("jacobi_scaling", ctypes.c_int32),
+        ("initial_trust_region_radius", ctypes.c_double),
+        ("max_trust_region_radius", ctypes.c_double),
+        ("min_trust_region_radius", ctypes.c_double),
+        ("function_tolerance", ctypes.c_double),
+        ("gradient_tolerance", ctypes.c_double),
+        ("parameter_tolerance", ctypes.c_double),
+        ("min_relative_decrease", ctypes.c_double),
+        ("min_lm_diagonal", ctypes.c_double),
+        ("max_lm_diagonal", ctypes.c_double),
+        ("linear_solver", ctypes.c_int32),
+        ("max_linear_iterations", ctypes.c_int32),
+        ("linear_tolerance", ctypes.c_double),
+        ("precision", ctypes.c_int32),
+        ("preconditioner", ctypes.c_int32),
+        ("use_cuda_graph", ctypes.c_int32),
+        ("check_tolerances", ctypes.c_int32),
+        ("stop_cost", ctypes.c_double),
+    ]
+
+
+class IterationSummary(ctypes.Structure):
+    _fields_ = [
+        ("iteration", ctypes.c_int32),
+        ("step_is_successful", ctypes.c_int32),
+        ("linear_solver_iterations", ctypes.c_int32),
+        ("pad_", ctypes.c_int32),
+        ("cost", ctypes.c_double),
+        ("cost_change", ctypes.c_double),
+        ("gradient_max_norm", ctypes.c_double),
+        ("step_norm", ctypes.c_double),
+        ("relative_decrease", ctypes.c_double),
+        ("trust_region_radius", ctypes.c_double),
+        ("iteration_time_ms", ctypes.c_double),
+    ]
+
+
+class Summary(ctypes.Structure):
+    _fields_ = [
+        ("num_iterations", ctypes.c_int32),
+        ("num_successful_steps", ctypes.c_int32),
+        ("termination", ctypes.c_int32),
+        ("total_linear_iterations", ctypes.c_int32),
+        ("initial_cost", ctypes.c_double),
+        ("final_cost", ctypes.c_double),
+        ("total_time_ms", ctypes.c_double),
+        ("time_to_stop_cost_ms", ctypes.c_double),
+        ("max_iterations_capacity", ctypes.c_int32),
+        ("pad_", ctypes.c_int32),
+        ("iterations", ctypes.POINTER(IterationSummary)),
+    ]
+
+
+class ProblemStats(ctypes.Structure):
+    _fields_ = [
+        ("num_keyframes", ctypes.c_int64),
+        ("num_landmarks", ctypes.c_int64),
+        ("num_observations", ctypes.c_int64),
+        ("num_imu_edges", ctypes.c_int64),
+        ("num_schur_pose_blocks", ctypes.c_int64),
+        ("device_bytes", ctypes.c_int64),
+    ]
+
+
+class SynthConfig(ctypes.Structure):
+    _fields_ = [
+        ("seed", ctypes.c_uint64),
+        ("num_missions", ctypes.c_int32),
+        ("keyframes_per_mission", ctypes.c_int32),
+        ("kf_min", ctypes.c_int32),
+        ("kf_max", ctypes.c_int32),
+        ("landmarks_per_keyframe", ctypes.c_int32),
+        ("num_landmarks", ctypes.c_int64),
+        ("landmark_mode", ctypes.c_int32),
+        ("track_model", ctypes.c_int32),
+        ("track_min", ctypes.c_int32),
+        ("track_max", ctypes.c_int32),
+        ("track_mean", ctypes.c_double),
+        ("track_alpha", ctypes.c_double),
+        ("num_cameras", ctypes.c_int32),
+        ("camera_per_mission", ctypes.c_int32),
+        ("camera0_distortion", ctypes.c_int32),
+        ("camera1_distortion", ctypes.c_int32),
+        ("radius_m", ctypes.c_double),
+        ("box_half_xy", ctypes.c_double),
+        ("box_half_z", ctypes.c_double),
+        ("keyframes_per_lap", ctypes.c_double),
+        ("kf_rate_hz", ctypes.c_double),
+        ("imu_rate_hz", ctypes.c_double),
+        ("pixel_sigma", ctypes.c_double),
+        ("acc_noise", ctypes.c_double),
+        ("gyro_noise", ctypes.c_double),
+        ("acc_bias_rw", ctypes.c_double),
+        ("gyro_bias_rw", ctypes.c_double),
+        ("rot_perturb", ctypes.c_double),
+        ("pos_perturb", ctypes.c_double),
+        ("lm_perturb", ctypes.c_double),
+        ("vel_perturb", ctypes.c_double),
+        ("shared_landmark_fraction", ctypes.c_double),
+        ("include_inertial", ctypes.c_int32),
+        ("co_registered", ctypes.c_int32),
+    ]
+
+
+def ptr(a, ctype=ctypes.c_double):
+    """Pointer to a contiguous numpy array (None for None)."""
+    if a is None:
+        return None
+    assert a.flags["C_CONTIGUOUS"], "array must be C-contiguous"
+    return a.ctypes.data_as(ctypes.POINTER(ctype))
+
+
+def _declare(lib, name, restype, argtypes):
+    f = getattr(lib, name)
+    f.restype = restype
+    f.argtypes = argtypes
+    return f
+
+
+def load_synth():
+    path = os.path.join(BUILD_DIR, "libmba_synth.so")
+    if not os.path.exists(path):
+        raise RuntimeError(f"{path} is missing: run __graft_entry__.build() first")
+    lib = ctypes.CDLL(path)
+    _declare(lib, "mba_synth_default_config", None, [ctypes.POINTER(SynthConfig)])
+    _declare(lib, "mba_synth_generate", ctypes.c_int, [ctypes.POINTER(SynthConfig), ctypes.POINTER(ctypes.c_void_p)])
+    _declare(lib, "mba_synth_free", None, [ctypes.c_void_p])
+    _declare(lib, "mba_synth_describe", ctypes.c_int, [ctypes.c_void_p, ctypes.POINTER(ProblemDesc)])
+    _declare(lib, "mba_synth_ground_truth", ctypes.c_int, [ctypes.c_void_p] + [c_double_p] * 5)
+    return lib
+
+
+def load_ba():
+    """Loads the CUDA back-end (libmaplab_ba.so); raises if it is not built."""
+    path = os.path.join(BUILD_DIR, "libmaplab_ba.so")
+    if not os.path.exists(path):
+        raise RuntimeError(f"{path} is missing: the CUDA back-end is not built (run __graft_entry__.build())")
+    lib = ctypes.CDLL(path)
+    vp = ctypes.c_void_p
+    _declare(lib, "mba_abi_version", ctypes.c_int32, [])
+    _declare(lib, "mba_default_solver_options", None, [ctypes.POINTER(SolverOptions)])
+    _declare(lib, "mba_status_string", ctypes.c_char_p, [ctypes.c_int])
+    _declare(lib, "mba_create", ctypes.c_int, [ctypes.POINTER(ProblemDesc), ctypes.c_int32, ctypes.POINTER(vp)])
+    _declare(lib, "mba_destroy", None, [vp])
+    _declare(lib, "mba_evaluate_visual", ctypes.c_int, [vp, c_double_p, ctypes.POINTER(c_double_p)])
+    _declare(lib, "mba_evaluate_inertial", ctypes.c_int, [vp, c_double_p, ctypes.POINTER(c_double_p)])
+    _declare(lib, "mba_linearize_visual", ctypes.c_int, [vp, ctypes.c_int32] + [c_double_p] * 4)
+    _declare(lib, "mba_cost", ctypes.c_int, [vp, ctypes.c_int32, c_double_p])
+    _declare(lib, "mba_solve", ctypes.c_int, [vp, ctypes.POINTER(SolverOptions), ctypes.POINTER(Summary)])
+    _declare(lib, "mba_read_state", ctypes.c_int, [vp] + [c_double_p] * 5)
+    _declare(lib, "mba_write_state", ctypes.c_int, [vp] + [c_double_p] * 5)
+    _declare(lib, "mba_cancel", None, [vp])
+    _declare(lib, "mba_time_visual_kernel", ctypes.c_int, [vp, ctypes.c_int32, ctypes.c_int32, c_double_p])
+    _declare(lib, "mba_get_stats", ctypes.c_int, [vp, ctypes.POINTER(ProblemStats)])
+    return lib
+
+
+def default_solver_options(lib=None):
+    """ba_* flag defaults (solver-options.cc:3-52) without needing the CUDA library."""
+    o = SolverOptions()
+    o.max_num_iterations = 30
+    o.jacobi_scaling = 1
+    o.initial_trust_region_radius = 1e5
+    o.max_trust_region_radius = 1e20
+    o.min_trust_region_radius = 1e-32
+    o.function_tolerance = 1e-12
+    o.gradient_tolerance = 1e-10
+    o.parameter_tolerance = 1e-8
+    o.min_relative_decrease = 1e-3
+    o.min_lm_diagonal = 1e-6
+    o.max_lm_diagonal = 1e32
+    o.linear_solver = MBA_LINEAR_SOLVER_PCG
+    o.max_linear_iterations = 100
+    o.linear_tolerance = 1e-6
+    o.precision = MBA_PRECISION_FP64
+    o.preconditioner = MBA_PRECOND_BLOCK_JACOBI
+    o.use_cuda_graph = 1
+    o.check_tolerances = 1
+    o.stop_cost = 0.0
+    return o
+
+
+def make_summary(capacity=64):
+    s = Summary()
+    its = (IterationSummary * capacity)()
+    s.max_iterations_capacity = capacity
+    s.iterations = ctypes.cast(its, ctypes.POINTER(IterationSummary))
+    s._its = its  # keep alive
+    return s
+
+
+def summary_dict(s):
+    n = min(s.num_iterations, s.max_iterations_capacity)
+    its = []
+    for i in range(n):
+        it = s.iterations[i]
+        its.append({"iteration": it.iteration, "ok": bool(it.step_is_successful), "cost": it.cost,
+                    "lin_iters": it.linear_solver_iterations, "radius": it.trust_region_radius,
+                    "relative_decrease": it.relative_decrease, "time_ms": it.iteration_time_ms})
+    return {"num_iterations": s.num_iterations, "successful": s.num_successful_steps,
+            "termination": s.termination, "linear_iterations": s.total_linear_iterations,
+            "initial_cost": s.initial_cost, "final_cost": s.final_cost, "total_time_ms": s.total_time_ms,
+            "time_to_stop_cost_ms": s.time_to_stop_cost_ms, "iterations": its}

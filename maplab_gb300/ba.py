@@ -1,0 +1,138 @@
+"""Python front-end over the C ABI (libmaplab_ba.so).
+
+``BundleAdjuster`` mirrors the reference's optimizer entry points: create from
+a problem description (constructOptimizationProblem + state import), evaluate
+the cost terms like ceres::CostFunction::Evaluate, solve like
+VIMapOptimizer::optimize / map_optimization::solve, and read the state back
+like OptimizationStateBuffer::copyAllStatesBackToMap.  Every call goes through
+the CUDA library; there is no CPU fallback.
+"""
+import ctypes
+
+import numpy as np
+
+from . import _native as N
+
+
+class BAError(RuntimeError):
+    def __init__(self, status, what):
+        self.status = status
+        super().__init__(f"{what} failed: status {status}")
+
+
+_LIB = None
+
+
+def lib():
+    global _LIB
+    if _LIB is None:
+        _LIB = N.load_ba()
+    return _LIB
+
+
+def _check(st, what):
+    if st != N.MBA_OK:
+        raise BAError(st, what)
+
+
+VISUAL_BLOCK_SIZES = [6, 14, 14, 14, 14, 8, 6, 8, 8]
+INERTIAL_BLOCK_SIZES = [105, 45, 45, 45, 105, 45, 45, 45]
+
+
+def default_options(**kw):
+    o = N.SolverOptions()
+    lib().mba_default_solver_options(ctypes.byref(o))
+    for k, v in kw.items():
+        setattr(o, k, v)
+    return o
+
+
+class BundleAdjuster:
+    def __init__(self, desc, device=0):
+        self._lib = lib()
+        self.desc = desc
+        h = ctypes.c_void_p()
+        _check(self._lib.mba_create(ctypes.byref(desc), device, ctypes.byref(h)), "mba_create")
+        self._h = h
+
+    def close(self):
+        if getattr(self, "_h", None):
+            self._lib.mba_destroy(self._h)
+            self._h = None
+
+    def __del__(self):
+        self.close()
+
+    def __enter__(self):
+        return self
+
+    def __exit__(self, *a):
+        self.close()
+
+    @property
+    def handle(self):
+        return self._h
+
+    def evaluate_visual(self, blocks=range(9)):
+        n = self.desc.num_observations
+        r = np.zeros((n, 2))
+        J = [np.zeros((n, VISUAL_BLOCK_SIZES[b])) if b in blocks else None for b in range(9)]
+        arr = (N.c_double_p * 9)(*[N.ptr(j) if j is not None else None for j in J])
+        _check(self._lib.mba_evaluate_visual(self._h, N.ptr(r), arr), "mba_evaluate_visual")
+        return r, J
+
+    def evaluate_inertial(self, blocks=range(8)):
+        n = self.desc.num_imu_edges
+        r = np.zeros((n, 15))
+        J = [np.zeros((n, INERTIAL_BLOCK_SIZES[b])) if b in blocks else None for b in range(8)]
+        arr = (N.c_double_p * 8)(*[N.ptr(j) if j is not None else None for j in J])
+        _check(self._lib.mba_evaluate_inertial(self._h, N.ptr(r), arr), "mba_evaluate_inertial")
+        return r, J
+
+    def linearize_visual(self, precision=N.MBA_PRECISION_FP64):
+        n = self.desc.num_observations
+        r = np.zeros((n, 2)); Jl = np.zeros((n, 6)); Js = np.zeros((n, 12)); Jo = np.zeros((n, 12))
+        _check(self._lib.mba_linearize_visual(self._h, precision, N.ptr(r), N.ptr(Jl), N.ptr(Js), N.ptr(Jo)),
+               "mba_linearize_visual")
+        return r, Jl, Js, Jo
+
+    def cost(self):
+        c = ctypes.c_double()
+        _check(self._lib.mba_cost(self._h, 0, ctypes.byref(c)), "mba_cost")
+        return c.value
+
+    def solve(self, opts=None, capacity=256):
+        if opts is None:
+            opts = default_options()
+        s = N.make_summary(capacity)
+        _check(self._lib.mba_solve(self._h, ctypes.byref(opts), ctypes.byref(s)), "mba_solve")
+        return N.summary_dict(s)
+
+    def read_state(self):
+        d = self.desc
+        kx = np.zeros((d.num_keyframes, 7)); kv = np.zeros((d.num_keyframes, 3))
+        kbg = np.zeros((d.num_keyframes, 3)); kba = np.zeros((d.num_keyframes, 3))
+        lp = np.zeros((d.num_landmarks, 3))
+        _check(self._lib.mba_read_state(self._h, N.ptr(kx), N.ptr(kv), N.ptr(kbg), N.ptr(kba), N.ptr(lp)),
+               "mba_read_state")
+        return dict(kf_q_IM_p_MI=kx, kf_v_M=kv, kf_b_g=kbg, kf_b_a=kba, lm_p_B=lp)
+
+    def write_state(self, st):
+        g = lambda k: N.ptr(np.ascontiguousarray(st[k], dtype=np.float64)) if st.get(k) is not None else None
+        keep = {k: np.ascontiguousarray(v, dtype=np.float64) for k, v in st.items() if v is not None}
+        _check(self._lib.mba_write_state(self._h, *[N.ptr(keep[k]) if k in keep else None for k in
+                                                      ("kf_q_IM_p_MI", "kf_v_M", "kf_b_g", "kf_b_a", "lm_p_B")]),
+               "mba_write_state")
+
+    def time_visual_kernel(self, mode=1, iters=20):
+        ms = ctypes.c_double()
+        _check(self._lib.mba_time_visual_kernel(self._h, mode, iters, ctypes.byref(ms)), "mba_time_visual_kernel")
+        return ms.value
+
+    def stats(self):
+        s = N.ProblemStats()
+        _check(self._lib.mba_get_stats(self._h, ctypes.byref(s)), "mba_get_stats")
+        return {f: getattr(s, f) for f, _ in s._fields_}
+
+    def cancel(self):
+        self._lib.mba_cancel(self._h)

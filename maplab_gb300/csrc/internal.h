@@ -1,0 +1,87 @@
+// Internal declarations shared by the CUDA translation units of libmaplab_ba.
+#pragma once
+
+#include <cuda_runtime.h>
+#include <stdint.h>
+
+#include "../../include/maplab_ba.h"
+#include "device_math.cuh"
+
+namespace mba {
+
+// Device-resident problem (plain pointers; passed by value to kernels).
+// Observations are sorted by landmark (contiguous per landmark).
+struct DevProblem {
+  int64_t nkf, nlm, nobs, ncam, nmis, nedge, nsamp;
+  // observations
+  const double2* obs_uv;
+  const double* obs_sinv;   // 1 / sigma
+  const double* obs_huber;  // Huber scale a = delta * sigma, 0 = no loss
+  const int32_t* obs_lm;
+  const int32_t* obs_kf;
+  const int32_t* obs_store;
+  const uint8_t* obs_cam;
+  const uint8_t* obs_type;
+  const int64_t* obs_perm;  // sorted index -> caller index
+  // landmarks
+  double* lm_p;             // [nlm][4] (x, y, z, pad)
+  const int64_t* lm_obs_off;// [nlm+1]
+  const uint8_t* lm_active;
+  // keyframes
+  double* kf_state;         // [nkf][16] = q(4) p(3) v(3) b_g(3) b_a(3)
+  const int32_t* kf_mis;
+  const uint32_t* kf_flags;
+  const uint16_t* kf_mask;  // bit d set = tangent dim d active (theta, p, v, b_g, b_a)
+  const double* mis;        // [nmis][8] = q_G_M(4) p_G_M(3) pad
+  const DevCamera* cams;
+  // inertial edges
+  const int32_t* e_from;
+  const int32_t* e_to;
+  const int64_t* e_off;
+  const int64_t* imu_ts;
+  const double* imu;        // [nsamp][6]
+  double gyro_noise2, gyro_bias2, acc_noise2, acc_bias2, gravity;
+};
+
+template <typename T>
+struct VisualLin {
+  T* r;   // [2][nobs]
+  T* Jl;  // [6][nobs]
+  T* Js;  // [12][nobs]  store pose tangent (theta, p)
+  T* Jo;  // [12][nobs]  observer pose tangent
+};
+
+template <typename T>
+struct InertialLin {
+  T* r;   // [nedge][15]
+  T* Jf;  // [nedge][225] from-keyframe tangent (theta, p, v, b_g, b_a)
+  T* Jt;  // [nedge][225] to-keyframe tangent
+};
+
+// Launchers (kernels_eval.cu).
+cudaError_t launch_visual_ambient(const DevProblem& P, double* res, double* const* jac_dev, cudaStream_t s);
+template <typename T>
+cudaError_t launch_visual_linearize(const DevProblem& P, VisualLin<T> out, double* cost_accum, cudaStream_t s);
+cudaError_t launch_visual_cost(const DevProblem& P, const double* kf_state, const double* lm_p, double* cost_accum,
+                               int* nonfinite, cudaStream_t s);
+// Inertial: full evaluation at `kf_state`; writes tangent linearization (if
+// lin.r) and/or the ambient blocks (if amb_res / amb_jac), accumulates cost.
+cudaError_t launch_inertial(const DevProblem& P, const double* kf_state, InertialLin<double> lin, double* amb_res,
+                            double* const* amb_jac, double* cost_accum, int* status, cudaStream_t s);
+template <typename T>
+cudaError_t launch_visual_linearize_gated(const DevProblem& P, VisualLin<T> out, double* cost_accum, const int* run_if,
+                                          const int* skip_if, cudaStream_t s);
+cudaError_t launch_visual_cost_gated(const DevProblem& P, const double* kf_state, const double* lm_p,
+                                     double* cost_accum, int* nonfinite, const int* skip_if, cudaStream_t s);
+cudaError_t launch_inertial_gated(const DevProblem& P, const double* kf_state, InertialLin<double> lin,
+                                  double* cost_accum, int* status, const int* skip_if, cudaStream_t s);
+template <typename T>
+cudaError_t launch_gather_visual(const DevProblem& P, VisualLin<T> v, double* r, double* Jl, double* Js, double* Jo,
+                                 cudaStream_t s);
+// to_device = 1: host-layout device arrays -> kf_state / lm_p; 0: the reverse.
+cudaError_t launch_pack_state(const DevProblem& P, const double* kx, const double* kv, const double* kbg,
+                              const double* kba, const double* lp, int to_device, cudaStream_t s);
+cudaError_t launch_inertial_f32(const DevProblem& P, const InertialLin<double>& src, InertialLin<float> dst,
+                                cudaStream_t s);
+
+}  // namespace mba

@@ -1,0 +1,980 @@
+// Evaluation kernels: visual reprojection terms (one thread per observation,
+// SoA in/out) and inertial terms (one warp per IMU edge, RK4 preintegration in
+// shared memory).
+//
+// Visual: VisualReprojectionError::Evaluate
+//   (algorithms/ceres-error-terms/include/ceres-error-terms/visual-error-term-inl.h:12-379)
+// Inertial: InertialErrorTerm::Evaluate / IntegrateStateAndCovariance
+//   (algorithms/ceres-error-terms/src/inertial-error-term.cc:9-286) with
+//   ImuIntegratorRK4::integrate
+//   (algorithms/imu-integrator-rk4/include/imu-integrator/imu-integrator-inl.h:17-334).
+#include <cuda_runtime.h>
+
+#include "internal.h"
+
+namespace mba {
+
+namespace {
+
+constexpr int kBlock = 256;
+
+__device__ __forceinline__ double warp_sum(double v) {
+#pragma unroll
+  for (int o = 16; o > 0; o >>= 1) v += __shfl_xor_sync(0xffffffffu, v, o);
+  return v;
+}
+
+// Block-wide sum of v, one atomicAdd per block into *acc.
+__device__ __forceinline__ void block_accumulate(double v, double* acc) {
+  __shared__ double red[32];
+  v = warp_sum(v);
+  const int lane = threadIdx.x & 31, w = threadIdx.x >> 5;
+  if (lane == 0) red[w] = v;
+  __syncthreads();
+  if (w == 0) {
+    v = (lane < (int)(blockDim.x >> 5)) ? red[lane] : 0.0;
+    v = warp_sum(v);
+    if (lane == 0 && v != 0.0) atomicAdd(acc, v);
+  }
+}
+
+__device__ __forceinline__ bool gated(const int* run_if, const int* skip_if) {
+  if (skip_if && *skip_if) return true;
+  if (run_if && !*run_if) return true;
+  return false;
+}
+
+template <typename T>
+__device__ __forceinline__ void load_q(const double* s, T* q) {
+  const double2 a = *reinterpret_cast<const double2*>(s);
+  const double2 b = *reinterpret_cast<const double2*>(s + 2);
+  q[0] = T(a.x); q[1] = T(a.y); q[2] = T(b.x); q[3] = T(b.y);
+}
+
+// Rotation-tangent basis of keyframe k: Ceres applies the local
+// parameterization Jacobian on top of the ambient 4-column quaternion block;
+// with the 4*Jq^T lift of the error terms this gives J_theta * B where
+// B = |q|^2 I for JplQuaternionParameterization and
+// B = -|q|^2 (R_I_M R_M_G)[:, 0:2] for JplRollPitchQuaternionParameterization
+// (quaternion-param-jpl.cc:144-164).  Masked tangent dims are zero columns.
+template <typename T>
+__device__ __forceinline__ void rot_basis(const DevProblem& P, int k, const T* q, const M3<T>& R_I_M, M3<T>& B) {
+  const uint16_t m = P.kf_mask[k];
+  const T n2 = q[0] * q[0] + q[1] * q[1] + q[2] * q[2] + q[3] * q[3];
+  if (P.kf_flags[k] & MBA_KF_GAUGE_ROLL_PITCH) {
+    T qg[4];
+    load_q(P.mis + 8 * P.kf_mis[k], qg);
+    M3<T> R_G_M;
+    jplR(qg, R_G_M);
+    // R_I_M * R_M_G = R_I_M * R_G_M^T
+    M3<T> A;
+#pragma unroll
+    for (int i = 0; i < 3; ++i)
+#pragma unroll
+      for (int j = 0; j < 3; ++j)
+        A.m[3 * i + j] = R_I_M.m[3 * i] * R_G_M.m[3 * j] + R_I_M.m[3 * i + 1] * R_G_M.m[3 * j + 1] +
+                         R_I_M.m[3 * i + 2] * R_G_M.m[3 * j + 2];
+#pragma unroll
+    for (int i = 0; i < 3; ++i) {
+      B.m[3 * i + 0] = (m & 1) ? -n2 * A.m[3 * i + 0] : T(0);
+      B.m[3 * i + 1] = (m & 2) ? -n2 * A.m[3 * i + 1] : T(0);
+      B.m[3 * i + 2] = T(0);
+    }
+  } else {
+#pragma unroll
+    for (int i = 0; i < 9; ++i) B.m[i] = T(0);
+    B.m[0] = (m & 1) ? n2 : T(0);
+    B.m[4] = (m & 2) ? n2 : T(0);
+    B.m[8] = (m & 4) ? n2 : T(0);
+  }
+}
+
+// ------------------------------------------------------------------ visual
+// Tangent-space, Huber-corrected linearization of every observation.
+template <typename T>
+__global__ void __launch_bounds__(kBlock) k_visual_linearize(DevProblem P, VisualLin<T> out, double* cost_accum,
+                                                             const int* run_if, const int* skip_if) {
+  if (gated(run_if, skip_if)) return;
+  const int64_t i = blockIdx.x * (int64_t)blockDim.x + threadIdx.x;
+  double cost = 0.0;
+  if (i < P.nobs) {
+    const int64_t N = P.nobs;
+    const int lm = P.obs_lm[i];
+    const int kf = P.obs_kf[i];
+    const int st = P.obs_store[i];
+    const int type = P.obs_type[i];
+    const DevCamera& cam = P.cams[P.obs_cam[i]];
+    const double2 uv = P.obs_uv[i];
+    const T sinv = T(P.obs_sinv[i]);
+    const double ha = P.obs_huber[i];
+    const double2 l01 = *reinterpret_cast<const double2*>(P.lm_p + 4 * (int64_t)lm);
+    const double l2 = P.lm_p[4 * (int64_t)lm + 2];
+    const T pB[3] = {T(l01.x), T(l01.y), T(l2)};
+    T qCI[4] = {T(cam.q_CI[0]), T(cam.q_CI[1]), T(cam.q_CI[2]), T(cam.q_CI[3])};
+    M3<T> RCI;
+    jplR(qCI, RCI);
+    T pI[3];
+    M3<T> RIM, RBLM, RMG, RGLM;
+    T qst[4], qob[4], pLMB[3], pMI[3];
+    if (type == MBA_LOCAL_KEYFRAME) {
+      pI[0] = pB[0]; pI[1] = pB[1]; pI[2] = pB[2];
+    } else {
+      const double* xs = P.kf_state + 16 * (int64_t)st;
+      const double* xo = P.kf_state + 16 * (int64_t)kf;
+      load_q(xs, qst);
+      load_q(xo, qob);
+      pLMB[0] = T(xs[4]); pLMB[1] = T(xs[5]); pLMB[2] = T(xs[6]);
+      pMI[0] = T(xo[4]); pMI[1] = T(xo[5]); pMI[2] = T(xo[6]);
+      jplR(qst, RBLM);
+      jplR(qob, RIM);
+      T pM[3];
+      mtv3(RBLM, pB, pM);  // R_LM_B p_B
+      pM[0] += pLMB[0]; pM[1] += pLMB[1]; pM[2] += pLMB[2];
+      if (type == MBA_GLOBAL) {
+        const double* ml = P.mis + 8 * P.kf_mis[st];
+        const double* mo = P.mis + 8 * P.kf_mis[kf];
+        T qgl[4], qgm[4];
+        load_q(ml, qgl);
+        load_q(mo, qgm);
+        jplR(qgl, RGLM);
+        M3<T> RGM;
+        jplR(qgm, RGM);
+        T pG[3];
+        mv3(RGLM, pM, pG);
+        pG[0] += T(ml[4]) - T(mo[4]); pG[1] += T(ml[5]) - T(mo[5]); pG[2] += T(ml[6]) - T(mo[6]);
+        mtv3(RGM, pG, pM);  // R_M_G (p_G - p_G_M)
+#pragma unroll
+        for (int a = 0; a < 3; ++a)
+#pragma unroll
+          for (int b = 0; b < 3; ++b) RMG.m[3 * a + b] = RGM.m[3 * b + a];
+      }
+      T d[3] = {pM[0] - pMI[0], pM[1] - pMI[1], pM[2] - pMI[2]};
+      mv3(RIM, d, pI);
+    }
+    T pC[3];
+    mv3(RCI, pI, pC);
+    pC[0] += T(cam.p_CI[0]); pC[1] += T(cam.p_CI[1]); pC[2] += T(cam.p_CI[2]);
+    T kp[2], Jkp[6];
+    const bool failed = project<T>(cam, pC, kp, Jkp);
+    T r[2], Jl[6], Js[12], Jo[12];
+#pragma unroll
+    for (int a = 0; a < 12; ++a) { Js[a] = T(0); Jo[a] = T(0); }
+    if (failed) {
+      r[0] = r[1] = T(0);
+#pragma unroll
+      for (int a = 0; a < 6; ++a) Jl[a] = T(0);
+    } else {
+      r[0] = (kp[0] - T(uv.x)) * sinv;
+      r[1] = (kp[1] - T(uv.y)) * sinv;
+      T A[6];
+      m23x33(Jkp, RCI, A);  // Jkp * R_C_I
+      if (type == MBA_LOCAL_KEYFRAME) {
+#pragma unroll
+        for (int a = 0; a < 6; ++a) Jl[a] = A[a] * sinv;
+      } else {
+        T B[6], Cp[6];
+        m23x33(A, RIM, B);  // Jkp R_C_I R_I_M  (= -J_p_M_I)
+        if (type == MBA_LOCAL_MISSION) {
+#pragma unroll
+          for (int a = 0; a < 6; ++a) Cp[a] = B[a];
+        } else {
+          T D[6];
+          m23x33(B, RMG, D);   // J_p_G_LM
+          m23x33(D, RGLM, Cp); // J_p_LM_B
+        }
+        // J_p_B = J_p_LM_B * R_LM_B  (R_LM_B = R_B_LM^T)
+        T JpB[6];
+#pragma unroll
+        for (int rr = 0; rr < 2; ++rr)
+#pragma unroll
+          for (int c = 0; c < 3; ++c)
+            JpB[3 * rr + c] = Cp[3 * rr] * RBLM.m[3 * c] + Cp[3 * rr + 1] * RBLM.m[3 * c + 1] + Cp[3 * rr + 2] * RBLM.m[3 * c + 2];
+        T Jqs[6], Jqo[6];
+        m23xskew(JpB, pB, Jqs);  // -J_q_B_LM
+        m23xskew(A, pI, Jqo);    // J_q_I_M
+        M3<T> Bs, Bo;
+        rot_basis<T>(P, st, qst, RBLM, Bs);
+        rot_basis<T>(P, kf, qob, RIM, Bo);
+        const uint16_t ms = P.kf_mask[st], mo = P.kf_mask[kf];
+#pragma unroll
+        for (int rr = 0; rr < 2; ++rr) {
+#pragma unroll
+          for (int c = 0; c < 3; ++c) {
+            Js[6 * rr + c] = -(Jqs[3 * rr] * Bs.m[c] + Jqs[3 * rr + 1] * Bs.m[3 + c] + Jqs[3 * rr + 2] * Bs.m[6 + c]) * sinv;
+            Jo[6 * rr + c] = (Jqo[3 * rr] * Bo.m[c] + Jqo[3 * rr + 1] * Bo.m[3 + c] + Jqo[3 * rr + 2] * Bo.m[6 + c]) * sinv;
+            Js[6 * rr + 3 + c] = (ms & (8u << c)) ? Cp[3 * rr + c] * sinv : T(0);
+            Jo[6 * rr + 3 + c] = (mo & (8u << c)) ? -B[3 * rr + c] * sinv : T(0);
+          }
+        }
+#pragma unroll
+        for (int a = 0; a < 6; ++a) Jl[a] = JpB[a] * sinv;
+      }
+      if (!P.lm_active[lm]) {
+#pragma unroll
+        for (int a = 0; a < 6; ++a) Jl[a] = T(0);
+      }
+    }
+    const T s = r[0] * r[0] + r[1] * r[1];
+    if (ha > 0.0) {
+      T rho0, sq1, rs, as;
+      huber_corrector<T>(T(ha), s, &rho0, &sq1, &rs, &as);
+      cost = 0.5 * double(rho0);
+      // J' = sq1 (J - as r (r^T J)), r' = rs r
+#pragma unroll
+      for (int c = 0; c < 3; ++c) {
+        const T t = r[0] * Jl[c] + r[1] * Jl[3 + c];
+        Jl[c] = sq1 * (Jl[c] - as * r[0] * t);
+        Jl[3 + c] = sq1 * (Jl[3 + c] - as * r[1] * t);
+      }
+#pragma unroll
+      for (int c = 0; c < 6; ++c) {
+        const T t = r[0] * Js[c] + r[1] * Js[6 + c];
+        Js[c] = sq1 * (Js[c] - as * r[0] * t);
+        Js[6 + c] = sq1 * (Js[6 + c] - as * r[1] * t);
+        const T u = r[0] * Jo[c] + r[1] * Jo[6 + c];
+        Jo[c] = sq1 * (Jo[c] - as * r[0] * u);
+        Jo[6 + c] = sq1 * (Jo[6 + c] - as * r[1] * u);
+      }
+      r[0] *= rs;
+      r[1] *= rs;
+    } else {
+      cost = 0.5 * double(s);
+    }
+    out.r[i] = r[0];
+    out.r[N + i] = r[1];
+#pragma unroll
+    for (int a = 0; a < 6; ++a) out.Jl[a * N + i] = Jl[a];
+#pragma unroll
+    for (int a = 0; a < 12; ++a) out.Js[a * N + i] = Js[a];
+#pragma unroll
+    for (int a = 0; a < 12; ++a) out.Jo[a * N + i] = Jo[a];
+  }
+  if (cost_accum) block_accumulate(cost, cost_accum);
+}
+
+// FP64 residual-only cost at an arbitrary state (candidate evaluation).
+__global__ void __launch_bounds__(kBlock) k_visual_cost(DevProblem P, const double* kf_state, const double* lm_p,
+                                                        double* cost_accum, int* nonfinite, const int* skip_if) {
+  if (gated(nullptr, skip_if)) return;
+  const int64_t i = blockIdx.x * (int64_t)blockDim.x + threadIdx.x;
+  double cost = 0.0;
+  if (i < P.nobs) {
+    const int lm = P.obs_lm[i], kf = P.obs_kf[i], st = P.obs_store[i], type = P.obs_type[i];
+    const DevCamera& cam = P.cams[P.obs_cam[i]];
+    const double pB[3] = {lm_p[4 * (int64_t)lm], lm_p[4 * (int64_t)lm + 1], lm_p[4 * (int64_t)lm + 2]};
+    M3<double> RCI;
+    jplR(cam.q_CI, RCI);
+    double pI[3];
+    if (type == MBA_LOCAL_KEYFRAME) {
+      pI[0] = pB[0]; pI[1] = pB[1]; pI[2] = pB[2];
+    } else {
+      const double* xs = kf_state + 16 * (int64_t)st;
+      const double* xo = kf_state + 16 * (int64_t)kf;
+      M3<double> RBLM, RIM;
+      jplR(xs, RBLM);
+      jplR(xo, RIM);
+      double pM[3];
+      mtv3(RBLM, pB, pM);
+      pM[0] += xs[4]; pM[1] += xs[5]; pM[2] += xs[6];
+      if (type == MBA_GLOBAL) {
+        const double* ml = P.mis + 8 * P.kf_mis[st];
+        const double* mo = P.mis + 8 * P.kf_mis[kf];
+        M3<double> RGLM, RGM;
+        jplR(ml, RGLM);
+        jplR(mo, RGM);
+        double pG[3];
+        mv3(RGLM, pM, pG);
+        pG[0] += ml[4] - mo[4]; pG[1] += ml[5] - mo[5]; pG[2] += ml[6] - mo[6];
+        mtv3(RGM, pG, pM);
+      }
+      const double d[3] = {pM[0] - xo[4], pM[1] - xo[5], pM[2] - xo[6]};
+      mv3(RIM, d, pI);
+    }
+    double pC[3];
+    mv3(RCI, pI, pC);
+    pC[0] += cam.p_CI[0]; pC[1] += cam.p_CI[1]; pC[2] += cam.p_CI[2];
+    double kp[2];
+    const bool failed = project<double>(cam, pC, kp, nullptr);
+    if (!failed) {
+      const double2 uv = P.obs_uv[i];
+      const double sinv = P.obs_sinv[i];
+      const double r0 = (kp[0] - uv.x) * sinv, r1 = (kp[1] - uv.y) * sinv;
+      const double s = r0 * r0 + r1 * r1;
+      const double a = P.obs_huber[i];
+      if (a > 0.0 && s > a * a) cost = 0.5 * (2.0 * a * sqrt(s) - a * a);
+      else cost = 0.5 * s;
+      if (!isfinite(cost) && nonfinite) *nonfinite = 1;
+    }
+  }
+  block_accumulate(cost, cost_accum);
+}
+
+// Distortion-parameter Jacobian at the undistorted normalized point
+// (distortion-radtan.cc:67-91, distortion-equidistant.cc:109-142).
+__device__ void dist_param_jac(int dtype, const double* pt, double* J) {
+  if (dtype == MBA_DISTORTION_RADTAN) {
+    const double y0 = pt[0], y1 = pt[1], r2 = y0 * y0 + y1 * y1, r4 = r2 * r2;
+    J[0] = y0 * r2; J[1] = y0 * r4; J[2] = 2.0 * y0 * y1; J[3] = r2 + 2.0 * y0 * y0;
+    J[4] = y1 * r2; J[5] = y1 * r4; J[6] = r2 + 2.0 * y1 * y1; J[7] = 2.0 * y0 * y1;
+  } else if (dtype == MBA_DISTORTION_EQUIDISTANT) {
+    const double x = pt[0], y = pt[1];
+    const double r = sqrt(x * x + y * y);
+    const double th = atan(r);
+    if (r < 1e-10) {
+      for (int a = 0; a < 8; ++a) J[a] = 0.0;
+      return;
+    }
+    const double t3 = pow(th, 3.0), t5 = pow(th, 5.0), t7 = pow(th, 7.0), t9 = pow(th, 9.0);
+    J[0] = x * t3 / r; J[1] = x * t5 / r; J[2] = x * t7 / r; J[3] = x * t9 / r;
+    J[4] = y * t3 / r; J[5] = y * t5 / r; J[6] = y * t7 / r; J[7] = y * t9 / r;
+  } else {
+    for (int a = 0; a < 8; ++a) J[a] = 0.0;
+  }
+}
+
+struct AmbientOut {
+  double* res;
+  double* J[9];
+};
+
+// Writes [A_q * 4 Jq^T * s | A_p * s] as a 2x7 row-major block.
+__device__ __forceinline__ void write_pose_block(const double* Aq, const double* Ap, const double* q, double s,
+                                                 double* out) {
+  double Jq[12];
+  dqdtheta(q, Jq);
+#pragma unroll
+  for (int rr = 0; rr < 2; ++rr) {
+#pragma unroll
+    for (int c = 0; c < 4; ++c)
+      out[7 * rr + c] = (Aq[3 * rr] * 4.0 * Jq[3 * c] + Aq[3 * rr + 1] * 4.0 * Jq[3 * c + 1] + Aq[3 * rr + 2] * 4.0 * Jq[3 * c + 2]) * s;
+#pragma unroll
+    for (int c = 0; c < 3; ++c) out[7 * rr + 4 + c] = Ap[3 * rr + c] * s;
+  }
+}
+
+// Ambient (Ceres-facing) evaluation of every observation: residual and all
+// nine Jacobian blocks exactly as VisualReprojectionError::Evaluate writes
+// them.  Outputs are in the caller's observation order.
+__global__ void __launch_bounds__(128) k_visual_ambient(DevProblem P, AmbientOut o) {
+  const int64_t i = blockIdx.x * (int64_t)blockDim.x + threadIdx.x;
+  if (i >= P.nobs) return;
+  const int64_t oi = P.obs_perm[i];
+  const int lm = P.obs_lm[i], kf = P.obs_kf[i], st = P.obs_store[i], type = P.obs_type[i];
+  const DevCamera& cam = P.cams[P.obs_cam[i]];
+  const double sinv = P.obs_sinv[i];
+  const double* pB = P.lm_p + 4 * (int64_t)lm;
+  const double* xs = P.kf_state + 16 * (int64_t)st;
+  const double* xo = P.kf_state + 16 * (int64_t)kf;
+  const double* ml = P.mis + 8 * P.kf_mis[st];
+  const double* mo = P.mis + 8 * P.kf_mis[kf];
+  M3<double> RCI, RBLM, RIM, RGLM, RGM, RMG;
+  jplR(cam.q_CI, RCI);
+  double pI[3], pG[3] = {0, 0, 0};
+  if (type == MBA_LOCAL_KEYFRAME) {
+    pI[0] = pB[0]; pI[1] = pB[1]; pI[2] = pB[2];
+  } else {
+    jplR(xs, RBLM);
+    jplR(xo, RIM);
+    double pM[3];
+    mtv3(RBLM, pB, pM);
+    pM[0] += xs[4]; pM[1] += xs[5]; pM[2] += xs[6];
+    if (type == MBA_GLOBAL) {
+      jplR(ml, RGLM);
+      jplR(mo, RGM);
+      mv3(RGLM, pM, pG);
+      pG[0] += ml[4]; pG[1] += ml[5]; pG[2] += ml[6];
+      const double d[3] = {pG[0] - mo[4], pG[1] - mo[5], pG[2] - mo[6]};
+      mtv3(RGM, d, pM);
+      for (int a = 0; a < 3; ++a)
+        for (int b = 0; b < 3; ++b) RMG.m[3 * a + b] = RGM.m[3 * b + a];
+    }
+    const double d[3] = {pM[0] - xo[4], pM[1] - xo[5], pM[2] - xo[6]};
+    mv3(RIM, d, pI);
+  }
+  double pC[3];
+  mv3(RCI, pI, pC);
+  pC[0] += cam.p_CI[0]; pC[1] += cam.p_CI[1]; pC[2] += cam.p_CI[2];
+  double kp[2], Jkp[6];
+  const bool failed = project<double>(cam, pC, kp, Jkp);
+  double* r = o.res ? o.res + 2 * oi : nullptr;
+  if (r) {
+    if (failed) { r[0] = r[1] = 0.0; }
+    else { const double2 uv = P.obs_uv[i]; r[0] = (kp[0] - uv.x) * sinv; r[1] = (kp[1] - uv.y) * sinv; }
+  }
+  const int sz[9] = {6, 14, 14, 14, 14, 8, 6, 8, 8};
+  if (failed) {
+    for (int b = 0; b < 9; ++b)
+      if (o.J[b]) for (int a = 0; a < sz[b]; ++a) o.J[b][sz[b] * oi + a] = 0.0;
+    return;
+  }
+  double A[6];
+  m23x33(Jkp, RCI, A);  // Jkp * R_C_I
+  double JpB[6], JpMI[6] = {0}, JpLMB[6] = {0}, JpGLM[6] = {0}, JpGM[6] = {0};
+  double JqBLM[6] = {0}, JqGLM[6] = {0}, JqGM[6] = {0}, JqIM[6] = {0};
+  if (type == MBA_LOCAL_KEYFRAME) {
+    for (int a = 0; a < 6; ++a) JpB[a] = A[a];
+  } else {
+    double B[6];
+    m23x33(A, RIM, B);
+    for (int a = 0; a < 6; ++a) JpMI[a] = -B[a];
+    if (type == MBA_LOCAL_MISSION) {
+      for (int a = 0; a < 6; ++a) JpLMB[a] = B[a];
+    } else {
+      double D[6];
+      m23x33(JpMI, RMG, D);  // J_p_G_M
+      for (int a = 0; a < 6; ++a) { JpGM[a] = D[a]; JpGLM[a] = -D[a]; }
+      m23x33(JpGLM, RGLM, JpLMB);
+      m23xskew(JpGLM, pG, JqGLM);
+      m23xskew(JpGM, pG, JqGM);
+    }
+    for (int rr = 0; rr < 2; ++rr)
+      for (int c = 0; c < 3; ++c)
+        JpB[3 * rr + c] = JpLMB[3 * rr] * RBLM.m[3 * c] + JpLMB[3 * rr + 1] * RBLM.m[3 * c + 1] + JpLMB[3 * rr + 2] * RBLM.m[3 * c + 2];
+    m23xskew(JpB, pB, JqBLM);
+    for (int a = 0; a < 6; ++a) JqBLM[a] = -JqBLM[a];
+    m23xskew(A, pI, JqIM);
+  }
+  if (o.J[0]) for (int a = 0; a < 6; ++a) o.J[0][6 * oi + a] = JpB[a] * sinv;
+  const bool dummy_base = type == MBA_LOCAL_KEYFRAME;
+  const bool dummy_mis = type != MBA_GLOBAL;
+  if (o.J[1]) { if (dummy_base) for (int a = 0; a < 14; ++a) o.J[1][14 * oi + a] = 0.0; else write_pose_block(JqBLM, JpLMB, xs, sinv, o.J[1] + 14 * oi); }
+  if (o.J[2]) { if (dummy_mis) for (int a = 0; a < 14; ++a) o.J[2][14 * oi + a] = 0.0; else write_pose_block(JqGLM, JpGLM, ml, sinv, o.J[2] + 14 * oi); }
+  if (o.J[3]) { if (dummy_mis) for (int a = 0; a < 14; ++a) o.J[3][14 * oi + a] = 0.0; else write_pose_block(JqGM, JpGM, mo, sinv, o.J[3] + 14 * oi); }
+  if (o.J[4]) { if (dummy_base) for (int a = 0; a < 14; ++a) o.J[4][14 * oi + a] = 0.0; else write_pose_block(JqIM, JpMI, xo, sinv, o.J[4] + 14 * oi); }
+  if (o.J[5]) {
+    double RpI[3], S[6], Jq[12];
+    mv3(RCI, pI, RpI);
+    // J_p_C_wrt_q_C_I = skew(R_C_I p_I); Jkp * skew(v)
+    m23xskew(Jkp, RpI, S);
+    dqdtheta(cam.q_CI, Jq);
+    for (int rr = 0; rr < 2; ++rr)
+      for (int c = 0; c < 4; ++c)
+        o.J[5][8 * oi + 4 * rr + c] = (S[3 * rr] * 4.0 * Jq[3 * c] + S[3 * rr + 1] * 4.0 * Jq[3 * c + 1] + S[3 * rr + 2] * 4.0 * Jq[3 * c + 2]) * sinv;
+  }
+  if (o.J[6]) for (int a = 0; a < 6; ++a) o.J[6][6 * oi + a] = Jkp[a] * sinv;
+  if (o.J[7] || o.J[8]) {
+    // Distorted normalized point for the intrinsics Jacobian, undistorted one
+    // for the distortion-parameter Jacobian (camera-pinhole.cc:98-157).
+    const double un[2] = {pC[0] / pC[2], pC[1] / pC[2]};
+    double dn[2] = {un[0], un[1]}, Jd[4];
+    distort<double>(cam.dtype, cam.dist, dn, Jd);
+    if (o.J[7]) {
+      double* J = o.J[7] + 8 * oi;
+      J[0] = dn[0] * sinv; J[1] = 0.0; J[2] = sinv; J[3] = 0.0;
+      J[4] = 0.0; J[5] = dn[1] * sinv; J[6] = 0.0; J[7] = sinv;
+    }
+    if (o.J[8]) {
+      double Jp[8];
+      dist_param_jac(cam.dtype, un, Jp);
+      for (int a = 0; a < 4; ++a) {
+        o.J[8][8 * oi + a] = Jp[a] * cam.intr[0] * sinv;
+        o.J[8][8 * oi + 4 + a] = Jp[4 + a] * cam.intr[1] * sinv;
+      }
+    }
+  }
+}
+
+// ------------------------------------------------------------------ inertial
+constexpr int kWarpsPerBlockI = 2;
+
+struct InertialSmem {
+  double phiacc[225], Qacc[225], Pi[225], Ti[225], cd[225], td[225], sumcd[225], sumtd[225], tmp[225];
+  double s0[16], si[16], dk[16], sumd[16], nxt[16];
+  double F[27];  // F00, F60, F69 (row-major 3x3 each) of the current derivative evaluation
+};
+
+// getStateDerivativeRungeKutta (imu-integrator-inl.h:170-207), lane 0.
+__device__ void state_derivative(double g, const double* rd, const double* s, double* d) {
+  double q[4] = {s[0], s[1], s[2], s[3]};
+  normalize4(q);
+  M3<double> BRG;
+  jplR(q, BRG);
+  const double* w = rd + 3;
+  for (int a = 0; a < 16; ++a) d[a] = 0.0;
+  d[0] = 0.5 * (w[2] * q[1] - w[1] * q[2] + w[0] * q[3]);
+  d[1] = 0.5 * (-w[2] * q[0] + w[0] * q[2] + w[1] * q[3]);
+  d[2] = 0.5 * (w[1] * q[0] - w[0] * q[1] + w[2] * q[3]);
+  d[3] = 0.5 * (-w[0] * q[0] - w[1] * q[1] - w[2] * q[2]);
+  double a[3];
+  mtv3(BRG, rd, a);  // G_R_B * acc
+  d[7] = a[0]; d[8] = a[1]; d[9] = a[2] - g;
+  d[13] = s[7]; d[14] = s[8]; d[15] = s[9];
+}
+
+// phi_cont blocks (imu-integrator-inl.h:223-252) for state s, lane 0.
+__device__ void phi_cont_blocks(const double* rd, const double* s, double* F) {
+  double q[4] = {s[0], s[1], s[2], s[3]};
+  normalize4(q);
+  M3<double> BRG;
+  jplR(q, BRG);
+  const double* w = rd + 3;
+  const double* a = rd;
+  // F00 = -[w]x
+  F[0] = 0.0;   F[1] = w[2];  F[2] = -w[1];
+  F[3] = -w[2]; F[4] = 0.0;   F[5] = w[0];
+  F[6] = w[1];  F[7] = -w[0]; F[8] = 0.0;
+  // F69 = -G_R_B ; F60 = -G_R_B [a]x
+  for (int i = 0; i < 3; ++i)
+    for (int j = 0; j < 3; ++j) F[18 + 3 * i + j] = -BRG.m[3 * j + i];
+  const double ax[9] = {0.0, -a[2], a[1], a[2], 0.0, -a[0], -a[1], a[0], 0.0};
+  for (int i = 0; i < 3; ++i)
+    for (int j = 0; j < 3; ++j)
+      F[9 + 3 * i + j] = F[18 + 3 * i] * ax[j] + F[18 + 3 * i + 1] * ax[3 + j] + F[18 + 3 * i + 2] * ax[6 + j];
+}
+
+// getCovarianceTransitionDerivativesRungeKutta (imu-integrator-inl.h:209-296),
+// warp-cooperative.  Writes cd (225) and td (225; rows 3-5, 9-11 zero).
+__device__ void cov_trans_derivative(const DevProblem& P, InertialSmem& S, const double* Pm, const double* Tm,
+                                     int lane) {
+  const double* F = S.F;
+  // td and PC rows 0-2, 6-8, 12-14 (135 entries each); other rows zero.
+  for (int e = lane; e < 225; e += 32) { S.td[e] = 0.0; S.tmp[e] = 0.0; }
+  __syncwarp();
+  for (int e = lane; e < 135; e += 32) {
+    const int blk = e / 45, rr = (e % 45) / 15, c = e % 15;
+    double tv, pv;
+    if (blk == 0) {
+      tv = F[3 * rr] * Tm[c] + F[3 * rr + 1] * Tm[15 + c] + F[3 * rr + 2] * Tm[30 + c] - Tm[(3 + rr) * 15 + c];
+      pv = F[3 * rr] * Pm[c] + F[3 * rr + 1] * Pm[15 + c] + F[3 * rr + 2] * Pm[30 + c] - Pm[(3 + rr) * 15 + c];
+      S.td[rr * 15 + c] = tv;
+      S.tmp[rr * 15 + c] = pv;
+    } else if (blk == 1) {
+      tv = (F[9 + 3 * rr] * Tm[c] + F[9 + 3 * rr + 1] * Tm[15 + c] + F[9 + 3 * rr + 2] * Tm[30 + c]) +
+           (F[18 + 3 * rr] * Tm[135 + c] + F[18 + 3 * rr + 1] * Tm[150 + c] + F[18 + 3 * rr + 2] * Tm[165 + c]);
+      pv = (F[9 + 3 * rr] * Pm[c] + F[9 + 3 * rr + 1] * Pm[15 + c] + F[9 + 3 * rr + 2] * Pm[30 + c]) +
+           (F[18 + 3 * rr] * Pm[135 + c] + F[18 + 3 * rr + 1] * Pm[150 + c] + F[18 + 3 * rr + 2] * Pm[165 + c]);
+      S.td[(6 + rr) * 15 + c] = tv;
+      S.tmp[(6 + rr) * 15 + c] = pv;
+    } else {
+      S.td[(12 + rr) * 15 + c] = Tm[(6 + rr) * 15 + c];
+      S.tmp[(12 + rr) * 15 + c] = Pm[(6 + rr) * 15 + c];
+    }
+  }
+  __syncwarp();
+  for (int e = lane; e < 225; e += 32) {
+    const int rr = e / 15, c = e % 15;
+    double v = S.tmp[e] + S.tmp[c * 15 + rr];
+    if (rr == c) {
+      if (rr < 3) v += P.gyro_noise2;
+      else if (rr < 6) v += P.gyro_bias2;
+      else if (rr < 9) v += P.acc_noise2;
+      else if (rr < 12) v += P.acc_bias2;
+    }
+    S.cd[e] = v;
+  }
+  __syncwarp();
+}
+
+struct InertialAmb {
+  double* res;
+  double* J[8];
+};
+
+__global__ void __launch_bounds__(32 * kWarpsPerBlockI) k_inertial(DevProblem P, const double* kf_state,
+                                                                   InertialLin<double> lin, InertialAmb amb,
+                                                                   double* cost_accum, int* status,
+                                                                   const int* skip_if) {
+  if (gated(nullptr, skip_if)) return;
+  extern __shared__ __align__(16) unsigned char smem_raw[];
+  InertialSmem& S = reinterpret_cast<InertialSmem*>(smem_raw)[threadIdx.x >> 5];
+  const int lane = threadIdx.x & 31;
+  const int64_t e = blockIdx.x * (int64_t)kWarpsPerBlockI + (threadIdx.x >> 5);
+  if (e >= P.nedge) return;
+  const int f = P.e_from[e], t = P.e_to[e];
+  const int64_t o0 = P.e_off[e];
+  const int ns = (int)(P.e_off[e + 1] - o0);
+  const double* xf = kf_state + 16 * (int64_t)f;
+  const double* xt = kf_state + 16 * (int64_t)t;
+  // begin state in integrator layout: q(4) b_g(3) v(3) b_a(3) p(3)
+  if (lane == 0) {
+    for (int a = 0; a < 4; ++a) S.s0[a] = xf[a];
+    for (int a = 0; a < 3; ++a) {
+      S.s0[4 + a] = xf[10 + a];
+      S.s0[7 + a] = xf[7 + a];
+      S.s0[10 + a] = xf[13 + a];
+      S.s0[13 + a] = xf[4 + a];
+    }
+    for (int a = 0; a < 16; ++a) S.nxt[a] = S.s0[a];
+  }
+  for (int a = lane; a < 225; a += 32) {
+    S.Qacc[a] = 0.0;
+    S.phiacc[a] = (a % 16 == 0) ? 1.0 : 0.0;
+  }
+  __syncwarp();
+  bool unordered = false;
+  for (int k = 0; k + 1 < ns; ++k) {
+    const int64_t a0 = o0 + k;
+    const double dt = (double)(P.imu_ts[a0 + 1] - P.imu_ts[a0]) * 1e-9;
+    if (P.imu_ts[a0 + 1] < P.imu_ts[a0]) unordered = true;
+    // de-biased readings (inertial-error-term.cc:49-57)
+    double rd[12];
+    for (int a = 0; a < 3; ++a) {
+      rd[a] = P.imu[6 * a0 + a] - S.s0[10 + a];
+      rd[3 + a] = P.imu[6 * a0 + 3 + a] - S.s0[4 + a];
+      rd[6 + a] = P.imu[6 * (a0 + 1) + a] - S.s0[10 + a];
+      rd[9 + a] = P.imu[6 * (a0 + 1) + 3 + a] - S.s0[4 + a];
+    }
+    double r23[6];
+    if (dt < 2.220446049250313e-16) {
+      for (int a = 0; a < 6; ++a) r23[a] = rd[a];
+    } else {
+      for (int a = 0; a < 6; ++a) r23[a] = rd[a] + (rd[6 + a] - rd[a]) * ((0.5 * dt) / dt);
+    }
+    const double* rk[4] = {rd, r23, r23, rd + 6};
+    const double cst[4] = {0.5, 0.5, 1.0, 0.0};
+    const double wsum[4] = {1.0, 2.0, 2.0, 1.0};
+    // RK4 on the state and on (cov, transition), stage by stage.
+    for (int a = lane; a < 225; a += 32) {
+      S.Pi[a] = 0.0;
+      S.Ti[a] = (a % 16 == 0) ? 1.0 : 0.0;
+      S.sumcd[a] = 0.0;
+      S.sumtd[a] = 0.0;
+    }
+    if (lane == 0) {
+      for (int a = 0; a < 16; ++a) { S.si[a] = S.s0[a]; S.sumd[a] = 0.0; }
+    }
+    __syncwarp();
+    for (int stg = 0; stg < 4; ++stg) {
+      if (lane == 0) {
+        state_derivative(P.gravity, rk[stg], S.si, S.dk);
+        phi_cont_blocks(rk[stg], S.si, S.F);
+      }
+      __syncwarp();
+      cov_trans_derivative(P, S, S.Pi, S.Ti, lane);
+      // accumulate RK sums, form next intermediates
+      for (int a = lane; a < 225; a += 32) {
+        S.sumcd[a] += wsum[stg] * S.cd[a];
+        S.sumtd[a] += wsum[stg] * S.td[a];
+      }
+      __syncwarp();
+      if (stg < 3) {
+        for (int a = lane; a < 225; a += 32) {
+          S.Pi[a] = cst[stg] * dt * S.cd[a];
+          S.Ti[a] = ((a % 16 == 0) ? 1.0 : 0.0) + cst[stg] * dt * S.td[a];
+        }
+      }
+      if (lane == 0) {
+        for (int a = 0; a < 16; ++a) {
+          S.sumd[a] += wsum[stg] * S.dk[a];
+          if (stg < 3) S.si[a] = S.s0[a] + cst[stg] * dt * S.dk[a];
+        }
+      }
+      __syncwarp();
+    }
+    // next state, per-step phi (in sumtd) and Q (in sumcd)
+    if (lane == 0) {
+      for (int a = 0; a < 16; ++a) S.nxt[a] = S.s0[a] + dt * S.sumd[a] / 6.0;
+    }
+    for (int a = lane; a < 225; a += 32) {
+      const int rr = a / 15;
+      const bool upd = (rr < 3) || (rr >= 6 && rr < 9) || (rr >= 12);
+      S.sumcd[a] = dt * S.sumcd[a] / 6.0;
+      S.sumtd[a] = ((a % 16 == 0) ? 1.0 : 0.0) + (upd ? dt * S.sumtd[a] / 6.0 : 0.0);
+    }
+    __syncwarp();
+    // Q_acc = phi Q_acc phi^T + Q ; phi_acc = phi phi_acc
+    for (int a = lane; a < 225; a += 32) {
+      const int rr = a / 15, c = a % 15;
+      double v = 0.0;
+      for (int m = 0; m < 15; ++m) v += S.sumtd[rr * 15 + m] * S.Qacc[m * 15 + c];
+      S.tmp[a] = v;
+    }
+    __syncwarp();
+    for (int a = lane; a < 225; a += 32) {
+      const int rr = a / 15, c = a % 15;
+      double v = 0.0;
+      for (int m = 0; m < 15; ++m) v += S.tmp[rr * 15 + m] * S.sumtd[c * 15 + m];
+      S.Pi[a] = v + S.sumcd[a];
+    }
+    __syncwarp();
+    for (int a = lane; a < 225; a += 32) {
+      const int rr = a / 15, c = a % 15;
+      double v = 0.0;
+      for (int m = 0; m < 15; ++m) v += S.sumtd[rr * 15 + m] * S.phiacc[m * 15 + c];
+      S.tmp[a] = v;
+    }
+    __syncwarp();
+    for (int a = lane; a < 225; a += 32) {
+      S.Qacc[a] = S.Pi[a];
+      S.phiacc[a] = S.tmp[a];
+    }
+    if (lane == 0) for (int a = 0; a < 16; ++a) S.s0[a] = S.nxt[a];
+    __syncwarp();
+  }
+  // Cholesky of Q_acc (lane 0) into Ti (lower), then L^-1 into Pi.
+  __shared__ int spd_fail[kWarpsPerBlockI];
+  if (lane == 0) {
+    int fail = 0;
+    double* L = S.Ti;
+    for (int a = 0; a < 225; ++a) L[a] = 0.0;
+    for (int j = 0; j < 15 && !fail; ++j) {
+      double d = S.Qacc[j * 15 + j];
+      for (int k = 0; k < j; ++k) d -= L[j * 15 + k] * L[j * 15 + k];
+      if (!(d > 0.0)) { fail = 1; break; }
+      const double ljj = sqrt(d);
+      L[j * 15 + j] = ljj;
+      for (int i = j + 1; i < 15; ++i) {
+        double s = S.Qacc[i * 15 + j];
+        for (int k = 0; k < j; ++k) s -= L[i * 15 + k] * L[j * 15 + k];
+        L[i * 15 + j] = s / ljj;
+      }
+    }
+    spd_fail[threadIdx.x >> 5] = fail;
+  }
+  __syncwarp();
+  const int fail = spd_fail[threadIdx.x >> 5];
+  if (fail || unordered) {
+    if (lane == 0 && status) atomicMax(status, unordered ? (int)MBA_ERR_UNORDERED_IMU : (int)MBA_ERR_NOT_SPD);
+    return;
+  }
+  // Linv column c by forward substitution (lanes 0..14).
+  if (lane < 15) {
+    const double* L = S.Ti;
+    double* X = S.Pi;
+    for (int i = 0; i < 15; ++i) {
+      double s = (i == lane) ? 1.0 : 0.0;
+      for (int k = 0; k < i; ++k) s -= L[i * 15 + k] * X[k * 15 + lane];
+      X[i * 15 + lane] = s / L[i * 15 + i];
+    }
+  }
+  __syncwarp();
+  // M = Linv * phi_acc  (into tmp)
+  for (int a = lane; a < 225; a += 32) {
+    const int rr = a / 15, c = a % 15;
+    double v = 0.0;
+    for (int m = 0; m <= rr; ++m) v += S.Pi[rr * 15 + m] * S.phiacc[m * 15 + c];
+    S.tmp[a] = v;
+  }
+  // raw residual (lane 0) into sumd[0..14]
+  if (lane == 0) {
+    const double* qi = S.s0;  // end state
+    const double n2 = qi[0] * qi[0] + qi[1] * qi[1] + qi[2] * qi[2] + qi[3] * qi[3];
+    double qinv[4] = {0, 0, 0, 0};
+    if (n2 > 0.0) { qinv[0] = -qi[0] / n2; qinv[1] = -qi[1] / n2; qinv[2] = -qi[2] / n2; qinv[3] = qi[3] / n2; }
+    double dq[4];
+    qprod_pos(xt, qinv, dq);
+    double* rr = S.sumd;
+    rr[0] = 2.0 * dq[0]; rr[1] = 2.0 * dq[1]; rr[2] = 2.0 * dq[2];
+    for (int a = 0; a < 3; ++a) {
+      rr[3 + a] = xt[10 + a] - S.s0[4 + a];   // b_g
+      rr[6 + a] = xt[7 + a] - S.s0[7 + a];    // v
+      rr[9 + a] = xt[13 + a] - S.s0[10 + a];  // b_a
+      rr[12 + a] = xt[4 + a] - S.s0[13 + a];  // p
+    }
+  }
+  __syncwarp();
+  // whitened residual r = Linv * r_raw (lanes 0..14) into dk
+  double rw = 0.0;
+  if (lane < 15) {
+    for (int m = 0; m <= lane; ++m) rw += S.Pi[lane * 15 + m] * S.sumd[m];
+    S.dk[lane] = rw;
+  }
+  const double sq = warp_sum(lane < 15 ? rw * rw : 0.0);
+  if (lane == 0 && cost_accum) atomicAdd(cost_accum, 0.5 * sq);
+  __syncwarp();
+  // Tangent outputs: KF order theta(0-2) p(3-5) v(6-8) b_g(9-11) b_a(12-14);
+  // error-state order theta(0-2) b_g(3-5) v(6-8) b_a(9-11) p(12-14).
+  if (lin.r) {
+    if (lane < 15) lin.r[15 * e + lane] = S.dk[lane];
+    // rotation bases
+    double qf[4] = {xf[0], xf[1], xf[2], xf[3]}, qt[4] = {xt[0], xt[1], xt[2], xt[3]};
+    M3<double> Rf, Rt, Bf, Bt;
+    jplR(qf, Rf);
+    jplR(qt, Rt);
+    rot_basis<double>(P, f, qf, Rf, Bf);
+    rot_basis<double>(P, t, qt, Rt, Bt);
+    const uint16_t mf = P.kf_mask[f], mt = P.kf_mask[t];
+    const int src[15] = {0, 1, 2, 12, 13, 14, 6, 7, 8, 3, 4, 5, 9, 10, 11};
+    for (int a = lane; a < 225; a += 32) {
+      const int rr = a / 15, c = a % 15;
+      double vf, vt;
+      if (c < 3) {
+        vf = -(S.tmp[rr * 15 + 0] * Bf.m[c] + S.tmp[rr * 15 + 1] * Bf.m[3 + c] + S.tmp[rr * 15 + 2] * Bf.m[6 + c]);
+        vt = S.Pi[rr * 15 + 0] * Bt.m[c] + S.Pi[rr * 15 + 1] * Bt.m[3 + c] + S.Pi[rr * 15 + 2] * Bt.m[6 + c];
+      } else {
+        vf = (mf & (1u << c)) ? -S.tmp[rr * 15 + src[c]] : 0.0;
+        vt = (mt & (1u << c)) ? S.Pi[rr * 15 + src[c]] : 0.0;
+      }
+      lin.Jf[225 * e + a] = vf;
+      lin.Jt[225 * e + a] = vt;
+    }
+  }
+  if (amb.res && lane < 15) amb.res[15 * e + lane] = S.dk[lane];
+  // Ambient blocks (inertial-error-term.cc:188-283).
+  if (amb.J[0] || amb.J[4]) {
+    double Jqf[12], Jqt[12];
+    dqdtheta(xf, Jqf);
+    dqdtheta(xt, Jqt);
+    for (int a = lane; a < 105; a += 32) {
+      const int rr = a / 7, c = a % 7;
+      if (amb.J[0]) {
+        double v;
+        if (c < 4) v = -4.0 * (S.tmp[rr * 15] * Jqf[3 * c] + S.tmp[rr * 15 + 1] * Jqf[3 * c + 1] + S.tmp[rr * 15 + 2] * Jqf[3 * c + 2]);
+        else v = -S.tmp[rr * 15 + 12 + (c - 4)];
+        amb.J[0][105 * e + a] = v;
+      }
+      if (amb.J[4]) {
+        double v;
+        if (c < 4) v = 4.0 * (S.Pi[rr * 15] * Jqt[3 * c] + S.Pi[rr * 15 + 1] * Jqt[3 * c + 1] + S.Pi[rr * 15 + 2] * Jqt[3 * c + 2]);
+        else v = S.Pi[rr * 15 + 12 + (c - 4)];
+        amb.J[4][105 * e + a] = v;
+      }
+    }
+  }
+  for (int b = 0; b < 3; ++b) {
+    // b_g (err cols 3-5), v (6-8), b_a (9-11)
+    const int col0 = (b == 0) ? 3 : (b == 1 ? 6 : 9);
+    for (int a = lane; a < 45; a += 32) {
+      const int rr = a / 3, c = a % 3;
+      if (amb.J[1 + b]) amb.J[1 + b][45 * e + a] = -S.tmp[rr * 15 + col0 + c];
+      if (amb.J[5 + b]) amb.J[5 + b][45 * e + a] = S.Pi[rr * 15 + col0 + c];
+    }
+  }
+}
+
+__global__ void k_convert_f32(const double* a, float* b, int64_t n) {
+  const int64_t i = blockIdx.x * (int64_t)blockDim.x + threadIdx.x;
+  if (i < n) b[i] = (float)a[i];
+}
+
+}  // namespace
+
+cudaError_t launch_visual_ambient(const DevProblem& P, double* res, double* const* jac_dev, cudaStream_t s) {
+  if (P.nobs == 0) return cudaSuccess;
+  AmbientOut o;
+  o.res = res;
+  for (int b = 0; b < 9; ++b) o.J[b] = jac_dev ? jac_dev[b] : nullptr;
+  const int64_t blocks = (P.nobs + 127) / 128;
+  k_visual_ambient<<<(unsigned)blocks, 128, 0, s>>>(P, o);
+  return cudaGetLastError();
+}
+
+template <typename T>
+cudaError_t launch_visual_linearize_gated(const DevProblem& P, VisualLin<T> out, double* cost_accum, const int* run_if,
+                                          const int* skip_if, cudaStream_t s) {
+  if (P.nobs == 0) return cudaSuccess;
+  const int64_t blocks = (P.nobs + kBlock - 1) / kBlock;
+  k_visual_linearize<T><<<(unsigned)blocks, kBlock, 0, s>>>(P, out, cost_accum, run_if, skip_if);
+  return cudaGetLastError();
+}
+template <typename T>
+cudaError_t launch_visual_linearize(const DevProblem& P, VisualLin<T> out, double* cost_accum, cudaStream_t s) {
+  return launch_visual_linearize_gated<T>(P, out, cost_accum, nullptr, nullptr, s);
+}
+template cudaError_t launch_visual_linearize<double>(const DevProblem&, VisualLin<double>, double*, cudaStream_t);
+template cudaError_t launch_visual_linearize<float>(const DevProblem&, VisualLin<float>, double*, cudaStream_t);
+template cudaError_t launch_visual_linearize_gated<double>(const DevProblem&, VisualLin<double>, double*, const int*,
+                                                           const int*, cudaStream_t);
+template cudaError_t launch_visual_linearize_gated<float>(const DevProblem&, VisualLin<float>, double*, const int*,
+                                                          const int*, cudaStream_t);
+
+cudaError_t launch_visual_cost_gated(const DevProblem& P, const double* kf_state, const double* lm_p,
+                                     double* cost_accum, int* nonfinite, const int* skip_if, cudaStream_t s) {
+  if (P.nobs == 0) return cudaSuccess;
+  const int64_t blocks = (P.nobs + kBlock - 1) / kBlock;
+  k_visual_cost<<<(unsigned)blocks, kBlock, 0, s>>>(P, kf_state, lm_p, cost_accum, nonfinite, skip_if);
+  return cudaGetLastError();
+}
+cudaError_t launch_visual_cost(const DevProblem& P, const double* kf_state, const double* lm_p, double* cost_accum,
+                               int* nonfinite, cudaStream_t s) {
+  return launch_visual_cost_gated(P, kf_state, lm_p, cost_accum, nonfinite, nullptr, s);
+}
+
+static cudaError_t launch_inertial_impl(const DevProblem& P, const double* kf_state, InertialLin<double> lin,
+                                        double* amb_res, double* const* amb_jac, double* cost_accum, int* status,
+                                        const int* skip_if, cudaStream_t s) {
+  if (P.nedge == 0) return cudaSuccess;
+  // 2 x 17 KB of shared memory per block: below the 48 KB default, so no
+  // attribute call is needed (none may happen inside graph capture).
+  const size_t smem = sizeof(InertialSmem) * kWarpsPerBlockI;
+  static_assert(sizeof(InertialSmem) * kWarpsPerBlockI <= 48 * 1024, "inertial smem above the default limit");
+  InertialAmb amb;
+  amb.res = amb_res;
+  for (int b = 0; b < 8; ++b) amb.J[b] = amb_jac ? amb_jac[b] : nullptr;
+  const int64_t blocks = (P.nedge + kWarpsPerBlockI - 1) / kWarpsPerBlockI;
+  k_inertial<<<(unsigned)blocks, 32 * kWarpsPerBlockI, smem, s>>>(P, kf_state, lin, amb, cost_accum, status, skip_if);
+  return cudaGetLastError();
+}
+cudaError_t launch_inertial(const DevProblem& P, const double* kf_state, InertialLin<double> lin, double* amb_res,
+                            double* const* amb_jac, double* cost_accum, int* status, cudaStream_t s) {
+  return launch_inertial_impl(P, kf_state, lin, amb_res, amb_jac, cost_accum, status, nullptr, s);
+}
+cudaError_t launch_inertial_gated(const DevProblem& P, const double* kf_state, InertialLin<double> lin,
+                                  double* cost_accum, int* status, const int* skip_if, cudaStream_t s) {
+  return launch_inertial_impl(P, kf_state, lin, nullptr, nullptr, cost_accum, status, skip_if, s);
+}
+
+cudaError_t launch_inertial_f32(const DevProblem& P, const InertialLin<double>& src, InertialLin<float> dst,
+                                cudaStream_t s) {
+  if (P.nedge == 0) return cudaSuccess;
+  const int64_t n1 = 15 * P.nedge, n2 = 225 * P.nedge;
+  k_convert_f32<<<(unsigned)((n1 + 255) / 256), 256, 0, s>>>(src.r, dst.r, n1);
+  k_convert_f32<<<(unsigned)((n2 + 255) / 256), 256, 0, s>>>(src.Jf, dst.Jf, n2);
+  k_convert_f32<<<(unsigned)((n2 + 255) / 256), 256, 0, s>>>(src.Jt, dst.Jt, n2);
+  return cudaGetLastError();
+}
+
+namespace {
+template <typename T>
+__global__ void k_gather_visual(int64_t N, const int64_t* perm, VisualLin<T> v, double* r, double* Jl, double* Js,
+                                double* Jo) {
+  const int64_t i = blockIdx.x * (int64_t)blockDim.x + threadIdx.x;
+  if (i >= N) return;
+  const int64_t o = perm[i];
+  if (r) for (int c = 0; c < 2; ++c) r[2 * o + c] = (double)v.r[c * N + i];
+  if (Jl) for (int c = 0; c < 6; ++c) Jl[6 * o + c] = (double)v.Jl[c * N + i];
+  if (Js) for (int c = 0; c < 12; ++c) Js[12 * o + c] = (double)v.Js[c * N + i];
+  if (Jo) for (int c = 0; c < 12; ++c) Jo[12 * o + c] = (double)v.Jo[c * N + i];
+}
+
+__global__ void k_pack_state(int64_t NK, int64_t NL, double* kf_state, double* lm_p, const double* kx, const double* kv,
+                             const double* kbg, const double* kba, const double* lp, int to_device) {
+  const int64_t i = blockIdx.x * (int64_t)blockDim.x + threadIdx.x;
+  if (i < NK) {
+    double* x = kf_state + 16 * i;
+    if (to_device) {
+      if (kx) for (int a = 0; a < 7; ++a) x[a] = kx[7 * i + a];
+      for (int a = 0; a < 3; ++a) {
+        if (kv) x[7 + a] = kv[3 * i + a];
+        if (kbg) x[10 + a] = kbg[3 * i + a];
+        if (kba) x[13 + a] = kba[3 * i + a];
+      }
+    } else {
+      if (kx) for (int a = 0; a < 7; ++a) const_cast<double*>(kx)[7 * i + a] = x[a];
+      for (int a = 0; a < 3; ++a) {
+        if (kv) const_cast<double*>(kv)[3 * i + a] = x[7 + a];
+        if (kbg) const_cast<double*>(kbg)[3 * i + a] = x[10 + a];
+        if (kba) const_cast<double*>(kba)[3 * i + a] = x[13 + a];
+      }
+    }
+  } else if (i < NK + NL && lp) {
+    const int64_t l = i - NK;
+    for (int a = 0; a < 3; ++a) {
+      if (to_device) lm_p[4 * l + a] = lp[3 * l + a];
+      else const_cast<double*>(lp)[3 * l + a] = lm_p[4 * l + a];
+    }
+  }
+}
+}  // namespace
+
+template <typename T>
+cudaError_t launch_gather_visual(const DevProblem& P, VisualLin<T> v, double* r, double* Jl, double* Js, double* Jo,
+                                 cudaStream_t s) {
+  if (P.nobs == 0) return cudaSuccess;
+  k_gather_visual<T><<<(unsigned)((P.nobs + 255) / 256), 256, 0, s>>>(P.nobs, P.obs_perm, v, r, Jl, Js, Jo);
+  return cudaGetLastError();
+}
+template cudaError_t launch_gather_visual<double>(const DevProblem&, VisualLin<double>, double*, double*, double*,
+                                                  double*, cudaStream_t);
+template cudaError_t launch_gather_visual<float>(const DevProblem&, VisualLin<float>, double*, double*, double*,
+                                                 double*, cudaStream_t);
+
+cudaError_t launch_pack_state(const DevProblem& P, const double* kx, const double* kv, const double* kbg,
+                              const double* kba, const double* lp, int to_device, cudaStream_t s) {
+  const int64_t n = P.nkf + P.nlm;
+  k_pack_state<<<(unsigned)((n + 255) / 256), 256, 0, s>>>(P.nkf, P.nlm, P.kf_state, P.lm_p, kx, kv, kbg, kba, lp,
+                                                            to_device);
+  return cudaGetLastError();
+}
+
+}  // namespace mba

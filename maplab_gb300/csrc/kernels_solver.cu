@@ -1,0 +1,892 @@
+// Device-resident Levenberg-Marquardt with Schur elimination of the
+// landmarks and block-Jacobi PCG on the reduced camera system.
+//
+// Restates the solver behaviour maplab configures in
+// algorithms/map-optimization/include/map-optimization/solver-options.h:26-75
+// (Ceres trust-region LM, Jacobi scaling, SPARSE_SCHUR / ITERATIVE_SCHUR
+// linear solvers): Jacobi scaling s = 1 / (1 + sqrt(diag(J^T J))) from the
+// first Jacobian, LM diagonal clamp(diag, 1e-6, 1e32) / radius, model cost
+// change -J d . (r + J d / 2), step acceptance at relative decrease > 1e-3,
+// radius update radius / max(1/3, 1 - (2 rho - 1)^3) on success and
+// radius / 2^k on failure.  Every per-iteration decision runs on the device
+// (one thread), so an LM iteration is a fixed kernel sequence that is
+// captured once as a CUDA graph.
+#include <cuda_runtime.h>
+
+#include "solver.h"
+
+namespace mba {
+
+namespace {
+
+constexpr int kB = 256;
+
+__device__ __forceinline__ double wsum(double v) {
+#pragma unroll
+  for (int o = 16; o > 0; o >>= 1) v += __shfl_xor_sync(0xffffffffu, v, o);
+  return v;
+}
+
+__device__ __forceinline__ void block_add(double v, double* acc) {
+  __shared__ double red[32];
+  v = wsum(v);
+  const int lane = threadIdx.x & 31, w = threadIdx.x >> 5;
+  __syncthreads();
+  if (lane == 0) red[w] = v;
+  __syncthreads();
+  if (w == 0) {
+    v = (lane < (int)(blockDim.x >> 5)) ? red[lane] : 0.0;
+    v = wsum(v);
+    if (lane == 0 && v != 0.0) atomicAdd(acc, v);
+  }
+}
+
+__device__ __forceinline__ bool gated(const int* run_if, const int* skip_if) {
+  if (skip_if && *skip_if) return true;
+  if (run_if && !*run_if) return true;
+  return false;
+}
+
+template <typename T>
+__device__ __forceinline__ void atomic_add(T* a, T v) {
+  atomicAdd(a, v);
+}
+
+// ------------------------------------------------------------ assembly
+template <typename T>
+__global__ void __launch_bounds__(kB) k_zero(T* a, int64_t n, const int* run_if, const int* skip_if) {
+  if (gated(run_if, skip_if)) return;
+  for (int64_t i = blockIdx.x * (int64_t)blockDim.x + threadIdx.x; i < n; i += (int64_t)gridDim.x * blockDim.x)
+    a[i] = T(0);
+}
+
+// One thread per landmark: H_ll, g_l, slot blocks W and the direct
+// camera-camera terms of its observations.
+template <typename T>
+__global__ void __launch_bounds__(kB) k_assemble_lm(DevProblem P, SchurPattern S, VisualLin<T> v, LinearSystem<T> L,
+                                                    const int* run_if, const int* skip_if) {
+  if (gated(run_if, skip_if)) return;
+  const int64_t l = blockIdx.x * (int64_t)blockDim.x + threadIdx.x;
+  if (l >= P.nlm) return;
+  const int64_t N = P.nobs, NS = S.nslot, NL = P.nlm;
+  const int64_t s0 = S.lm_slot_off[l];
+  const int st = S.slot_kf[s0];
+  T H[9], g[3], Wst[18], Dst[36], gst[6];
+#pragma unroll
+  for (int a = 0; a < 9; ++a) H[a] = T(0);
+#pragma unroll
+  for (int a = 0; a < 3; ++a) g[a] = T(0);
+#pragma unroll
+  for (int a = 0; a < 18; ++a) Wst[a] = T(0);
+#pragma unroll
+  for (int a = 0; a < 36; ++a) Dst[a] = T(0);
+#pragma unroll
+  for (int a = 0; a < 6; ++a) gst[a] = T(0);
+  bool any_cam = false;
+  for (int64_t i = P.lm_obs_off[l]; i < P.lm_obs_off[l + 1]; ++i) {
+    T r[2] = {v.r[i], v.r[N + i]};
+    T Jl[6];
+#pragma unroll
+    for (int a = 0; a < 6; ++a) Jl[a] = v.Jl[a * N + i];
+#pragma unroll
+    for (int a = 0; a < 3; ++a) {
+#pragma unroll
+      for (int b = 0; b < 3; ++b) H[3 * a + b] += Jl[a] * Jl[b] + Jl[3 + a] * Jl[3 + b];
+      g[a] += Jl[a] * r[0] + Jl[3 + a] * r[1];
+    }
+    const int slot = S.obs_slot[i];
+    if (slot < 0) continue;
+    any_cam = true;
+    T Js[12], Jo[12];
+#pragma unroll
+    for (int a = 0; a < 12; ++a) { Js[a] = v.Js[a * N + i]; Jo[a] = v.Jo[a * N + i]; }
+    const int ob = P.obs_kf[i];
+#pragma unroll
+    for (int x = 0; x < 3; ++x)
+#pragma unroll
+      for (int c = 0; c < 6; ++c) {
+        Wst[6 * x + c] += Jl[x] * Js[c] + Jl[3 + x] * Js[6 + c];
+        L.Wslot[(6 * x + c) * NS + slot] = Jl[x] * Jo[c] + Jl[3 + x] * Jo[6 + c];
+      }
+#pragma unroll
+    for (int a = 0; a < 6; ++a) {
+      gst[a] += Js[a] * r[0] + Js[6 + a] * r[1];
+      atomic_add(&L.gc[15 * (int64_t)ob + a], Jo[a] * r[0] + Jo[6 + a] * r[1]);
+#pragma unroll
+      for (int b = 0; b < 6; ++b) {
+        Dst[6 * a + b] += Js[a] * Js[b] + Js[6 + a] * Js[6 + b];
+        atomic_add(&L.Dbase[225 * (int64_t)ob + 15 * a + b], Jo[a] * Jo[b] + Jo[6 + a] * Jo[6 + b]);
+      }
+    }
+    const int blk = S.obs_pblk[i];
+    T* Pb = L.Pbase + 36 * (int64_t)blk;
+    if (st < ob) {
+#pragma unroll
+      for (int a = 0; a < 6; ++a)
+#pragma unroll
+        for (int b = 0; b < 6; ++b) atomic_add(&Pb[6 * a + b], Js[a] * Jo[b] + Js[6 + a] * Jo[6 + b]);
+    } else {
+#pragma unroll
+      for (int a = 0; a < 6; ++a)
+#pragma unroll
+        for (int b = 0; b < 6; ++b) atomic_add(&Pb[6 * a + b], Jo[a] * Js[b] + Jo[6 + a] * Js[6 + b]);
+    }
+  }
+#pragma unroll
+  for (int a = 0; a < 9; ++a) L.Hll[a * NL + l] = H[a];
+#pragma unroll
+  for (int a = 0; a < 3; ++a) L.gl[a * NL + l] = g[a];
+#pragma unroll
+  for (int a = 0; a < 18; ++a) L.Wslot[a * NS + s0] = Wst[a];
+  if (any_cam) {
+#pragma unroll
+    for (int a = 0; a < 6; ++a) {
+      atomic_add(&L.gc[15 * (int64_t)st + a], gst[a]);
+#pragma unroll
+      for (int b = 0; b < 6; ++b) atomic_add(&L.Dbase[225 * (int64_t)st + 15 * a + b], Dst[6 * a + b]);
+    }
+  }
+}
+
+// One warp per inertial edge.
+template <typename T>
+__global__ void __launch_bounds__(128) k_assemble_inertial(DevProblem P, InertialLin<T> in, LinearSystem<T> L,
+                                                           const int* run_if, const int* skip_if) {
+  if (gated(run_if, skip_if)) return;
+  const int64_t e = (blockIdx.x * (int64_t)blockDim.x + threadIdx.x) >> 5;
+  const int lane = threadIdx.x & 31;
+  if (e >= P.nedge) return;
+  const int f = P.e_from[e], t = P.e_to[e];
+  const T* Jf = in.Jf + 225 * e;
+  const T* Jt = in.Jt + 225 * e;
+  const T* r = in.r + 15 * e;
+  for (int a = lane; a < 225; a += 32) {
+    const int rr = a / 15, c = a % 15;
+    T dff = T(0), dtt = T(0), eft = T(0);
+#pragma unroll
+    for (int m = 0; m < 15; ++m) {
+      dff += Jf[15 * m + rr] * Jf[15 * m + c];
+      dtt += Jt[15 * m + rr] * Jt[15 * m + c];
+      eft += Jf[15 * m + rr] * Jt[15 * m + c];
+    }
+    atomic_add(&L.Dbase[225 * (int64_t)f + a], dff);
+    atomic_add(&L.Dbase[225 * (int64_t)t + a], dtt);
+    L.Ebase[225 * e + a] = eft;
+  }
+  if (lane < 15) {
+    T gf = T(0), gt = T(0);
+#pragma unroll
+    for (int m = 0; m < 15; ++m) { gf += Jf[15 * m + lane] * r[m]; gt += Jt[15 * m + lane] * r[m]; }
+    atomic_add(&L.gc[15 * (int64_t)f + lane], gf);
+    atomic_add(&L.gc[15 * (int64_t)t + lane], gt);
+  }
+}
+
+// Jacobi scaling from the unscaled diagonal of J^T J.
+template <typename T>
+__global__ void k_scale(DevProblem P, LinearSystem<T> L, ScaleVectors sc, int jacobi) {
+  const int64_t i = blockIdx.x * (int64_t)blockDim.x + threadIdx.x;
+  const int64_t nk = 15 * P.nkf, nl = 3 * P.nlm;
+  if (i < nk) {
+    const int64_t k = i / 15, d = i % 15;
+    const double h = (double)L.Dbase[225 * k + 16 * d];
+    sc.skf[i] = jacobi ? 1.0 / (1.0 + sqrt(h > 0.0 ? h : 0.0)) : 1.0;
+  } else if (i < nk + nl) {
+    const int64_t j = i - nk, a = j / P.nlm, l = j % P.nlm;
+    const double h = (double)L.Hll[(4 * a) * P.nlm + l];
+    sc.slm[j] = jacobi ? 1.0 / (1.0 + sqrt(h > 0.0 ? h : 0.0)) : 1.0;
+  }
+}
+
+__device__ __forceinline__ double lm_damp(double s, double h, const LmParams& prm, double radius) {
+  double d = s * s * h;
+  d = d < prm.min_lm_diagonal ? prm.min_lm_diagonal : (d > prm.max_lm_diagonal ? prm.max_lm_diagonal : d);
+  return d / radius;
+}
+
+// Scaled, damped keyframe system: SD, SE, SP (upper), rhs = -s g.
+template <typename T>
+__global__ void __launch_bounds__(kB) k_build_system(SolverLaunch<T> s) {
+  LmControl* ctl = s.ctl;
+  if (ctl->terminated) return;
+  const int64_t nkf = s.P.nkf, ne = s.P.nedge, npu = s.S.npu;
+  const int64_t n1 = nkf * 225, n2 = n1 + ne * 225, n3 = n2 + npu * 36, n4 = n3 + nkf * 15;
+  const double radius = ctl->radius;
+  const int64_t tid = blockIdx.x * (int64_t)blockDim.x + threadIdx.x;
+  if (tid == 0) {
+    ctl->accepted = 0;
+    ctl->status = 0;
+    ctl->model_change = 0.0;
+    ctl->cost_cand = 0.0;
+    ctl->step_norm2 = 0.0;
+    ctl->x_norm2 = 0.0;
+    ctl->nonfinite = 0;
+    ctl->inertial_status = 0;
+    ctl->pcg_done = 0;
+    ctl->pcg_iters = 0;
+    ctl->pcg_rz0 = 0.0;
+    ctl->pcg_bnorm2 = 0.0;
+    for (int a = 0; a < 3; ++a) { ctl->pcg_pq[a] = 0.0; ctl->pcg_rr[a] = 0.0; ctl->pcg_rz[a] = 0.0; }
+  }
+  for (int64_t i = tid; i < n4; i += (int64_t)gridDim.x * blockDim.x) {
+    if (i < n1) {
+      const int64_t k = i / 225, e = i % 225, a = e / 15, b = e % 15;
+      const double sa = s.sc.skf[15 * k + a], sb = s.sc.skf[15 * k + b];
+      const double h = (double)s.L.Dbase[i];
+      double v = sa * h * sb;
+      if (a == b) v += lm_damp(sa, h, s.prm, radius);
+      s.L.SD[i] = T(v);
+    } else if (i < n2) {
+      const int64_t j = i - n1, e = j / 225, q = j % 225, a = q / 15, b = q % 15;
+      s.L.SE[j] = T(s.sc.skf[15 * (int64_t)s.P.e_from[e] + a] * (double)s.L.Ebase[j] * s.sc.skf[15 * (int64_t)s.P.e_to[e] + b]);
+    } else if (i < n3) {
+      const int64_t j = i - n2, b = j / 36, q = j % 36, a = q / 6, c = q % 6;
+      s.L.SP[j] = T(s.sc.skf[15 * (int64_t)s.S.pu_i[b] + a] * (double)s.L.Pbase[j] * s.sc.skf[15 * (int64_t)s.S.pu_j[b] + c]);
+    } else {
+      const int64_t j = i - n3;
+      s.L.rhs[j] = T(-s.sc.skf[j] * (double)s.L.gc[j]);
+    }
+  }
+}
+
+__device__ bool inv3d(const double* A, double* B) {
+  const double det = A[0] * (A[4] * A[8] - A[5] * A[7]) - A[1] * (A[3] * A[8] - A[5] * A[6]) +
+                     A[2] * (A[3] * A[7] - A[4] * A[6]);
+  if (!(fabs(det) > 0.0) || !isfinite(det)) return false;
+  const double id = 1.0 / det;
+  B[0] = (A[4] * A[8] - A[5] * A[7]) * id; B[1] = (A[2] * A[7] - A[1] * A[8]) * id; B[2] = (A[1] * A[5] - A[2] * A[4]) * id;
+  B[3] = (A[5] * A[6] - A[3] * A[8]) * id; B[4] = (A[0] * A[8] - A[2] * A[6]) * id; B[5] = (A[2] * A[3] - A[0] * A[5]) * id;
+  B[6] = (A[3] * A[7] - A[4] * A[6]) * id; B[7] = (A[1] * A[6] - A[0] * A[7]) * id; B[8] = (A[0] * A[4] - A[1] * A[3]) * id;
+  return true;
+}
+
+// Landmark elimination, part 1: V = (s H s + D)^-1 and rhs += W^T V g.
+template <typename T>
+__global__ void __launch_bounds__(kB) k_schur_lm(SolverLaunch<T> s) {
+  if (s.ctl->terminated) return;
+  const int64_t l = blockIdx.x * (int64_t)blockDim.x + threadIdx.x;
+  const int64_t NL = s.P.nlm, NS = s.S.nslot;
+  if (l >= NL) return;
+  double V[9] = {0, 0, 0, 0, 0, 0, 0, 0, 0};
+  if (s.P.lm_active[l]) {
+    const double radius = s.ctl->radius;
+    double sl[3], Hs[9];
+    for (int a = 0; a < 3; ++a) sl[a] = s.sc.slm[a * NL + l];
+    for (int a = 0; a < 3; ++a)
+      for (int b = 0; b < 3; ++b) Hs[3 * a + b] = sl[a] * (double)s.L.Hll[(3 * a + b) * NL + l] * sl[b];
+    for (int a = 0; a < 3; ++a) Hs[4 * a] += lm_damp(sl[a], (double)s.L.Hll[(4 * a) * NL + l], s.prm, radius);
+    if (!inv3d(Hs, V)) {
+      atomicExch(&s.ctl->status, (int)MBA_ERR_NOT_SPD);
+      for (int a = 0; a < 9; ++a) V[a] = 0.0;
+    }
+    double gs[3], Vg[3];
+    for (int a = 0; a < 3; ++a) gs[a] = sl[a] * (double)s.L.gl[a * NL + l];
+    for (int a = 0; a < 3; ++a) Vg[a] = V[3 * a] * gs[0] + V[3 * a + 1] * gs[1] + V[3 * a + 2] * gs[2];
+    for (int64_t sl_i = s.S.lm_slot_off[l]; sl_i < s.S.lm_slot_off[l + 1]; ++sl_i) {
+      const int64_t k = s.S.slot_kf[sl_i];
+      for (int c = 0; c < 6; ++c) {
+        const double sk = s.sc.skf[15 * k + c];
+        double acc = 0.0;
+        for (int x = 0; x < 3; ++x) acc += sl[x] * (double)s.L.Wslot[(6 * x + c) * NS + sl_i] * sk * Vg[x];
+        if (acc != 0.0) atomic_add(&s.L.rhs[15 * k + c], T(acc));
+      }
+    }
+  }
+  for (int a = 0; a < 9; ++a) s.L.V[a * NL + l] = T(V[a]);
+}
+
+// Landmark elimination, part 2: U = V Ws per slot (Ws = scaled W).
+template <typename T>
+__global__ void __launch_bounds__(kB) k_schur_slot(SolverLaunch<T> s) {
+  if (s.ctl->terminated) return;
+  const int64_t i = blockIdx.x * (int64_t)blockDim.x + threadIdx.x;
+  const int64_t NS = s.S.nslot, NL = s.P.nlm;
+  if (i >= NS) return;
+  const int64_t l = s.S.slot_lm[i], k = s.S.slot_kf[i];
+  T Ws[18];
+  for (int x = 0; x < 3; ++x) {
+    const double sl = s.sc.slm[x * NL + l];
+    for (int c = 0; c < 6; ++c) Ws[6 * x + c] = T(sl * (double)s.L.Wslot[(6 * x + c) * NS + i] * s.sc.skf[15 * k + c]);
+  }
+  T V[9];
+  for (int a = 0; a < 9; ++a) V[a] = s.L.V[a * NL + l];
+  for (int x = 0; x < 3; ++x)
+    for (int c = 0; c < 6; ++c)
+      s.L.U[(6 * x + c) * NS + i] = V[3 * x] * Ws[c] + V[3 * x + 1] * Ws[6 + c] + V[3 * x + 2] * Ws[12 + c];
+}
+
+// Landmark elimination, part 3: S(k_a, k_b) -= Ws_a^T U_b for every slot pair.
+template <typename T>
+__global__ void __launch_bounds__(kB) k_schur_pairs(SolverLaunch<T> s) {
+  if (s.ctl->terminated) return;
+  const int64_t pidx = blockIdx.x * (int64_t)blockDim.x + threadIdx.x;
+  if (pidx >= s.S.npair) return;
+  const int64_t NS = s.S.nslot, NL = s.P.nlm;
+  const int64_t a = s.S.pair_a[pidx], b = s.S.pair_b[pidx];
+  const int tgt = s.S.pair_t[pidx];
+  const int64_t l = s.S.slot_lm[a], ka = s.S.slot_kf[a], kb = s.S.slot_kf[b];
+  T Wa[18], Ub[18];
+  for (int x = 0; x < 3; ++x) {
+    const double sl = s.sc.slm[x * NL + l];
+    for (int c = 0; c < 6; ++c) {
+      Wa[6 * x + c] = T(sl * (double)s.L.Wslot[(6 * x + c) * NS + a] * s.sc.skf[15 * ka + c]);
+      Ub[6 * x + c] = s.L.U[(6 * x + c) * NS + b];
+    }
+  }
+  T M[36];
+#pragma unroll
+  for (int r = 0; r < 6; ++r)
+#pragma unroll
+    for (int c = 0; c < 6; ++c) M[6 * r + c] = Wa[r] * Ub[c] + Wa[6 + r] * Ub[6 + c] + Wa[12 + r] * Ub[12 + c];
+  if (tgt < 0) {
+    T* D = s.L.SD + 225 * (int64_t)(-tgt - 1);
+    if (a == b) {
+#pragma unroll
+      for (int r = 0; r < 6; ++r)
+#pragma unroll
+        for (int c = 0; c < 6; ++c) atomic_add(&D[15 * r + c], -M[6 * r + c]);
+    } else {
+#pragma unroll
+      for (int r = 0; r < 6; ++r)
+#pragma unroll
+        for (int c = 0; c < 6; ++c) atomic_add(&D[15 * r + c], -(M[6 * r + c] + M[6 * c + r]));
+    }
+  } else {
+    T* B = s.L.SP + 36 * (int64_t)tgt;
+    if (ka < kb) {
+#pragma unroll
+      for (int r = 0; r < 6; ++r)
+#pragma unroll
+        for (int c = 0; c < 6; ++c) atomic_add(&B[6 * r + c], -M[6 * r + c]);
+    } else {
+#pragma unroll
+      for (int r = 0; r < 6; ++r)
+#pragma unroll
+        for (int c = 0; c < 6; ++c) atomic_add(&B[6 * r + c], -M[6 * c + r]);
+    }
+  }
+}
+
+// Masked tangent dims -> identity rows; mirror SP to the lower orientation.
+template <typename T>
+__global__ void __launch_bounds__(kB) k_finalize_system(SolverLaunch<T> s) {
+  if (s.ctl->terminated) return;
+  const int64_t nkf = s.P.nkf, ne = s.P.nedge, npu = s.S.npu;
+  const int64_t n1 = nkf * 225, n2 = n1 + ne * 225, n3 = n2 + npu * 36, n4 = n3 + nkf * 15;
+  for (int64_t i = blockIdx.x * (int64_t)blockDim.x + threadIdx.x; i < n4; i += (int64_t)gridDim.x * blockDim.x) {
+    if (i < n1) {
+      const int64_t k = i / 225, e = i % 225, a = e / 15, b = e % 15;
+      const uint16_t m = s.P.kf_mask[k];
+      if (!((m >> a) & 1) || !((m >> b) & 1)) s.L.SD[i] = (a == b) ? T(1) : T(0);
+    } else if (i < n2) {
+      const int64_t j = i - n1, e = j / 225, q = j % 225, a = q / 15, b = q % 15;
+      if (!((s.P.kf_mask[s.P.e_from[e]] >> a) & 1) || !((s.P.kf_mask[s.P.e_to[e]] >> b) & 1)) s.L.SE[j] = T(0);
+    } else if (i < n3) {
+      const int64_t j = i - n2, b = j / 36, q = j % 36, a = q / 6, c = q % 6;
+      T v = s.L.SP[j];
+      if (!((s.P.kf_mask[s.S.pu_i[b]] >> a) & 1) || !((s.P.kf_mask[s.S.pu_j[b]] >> c) & 1)) {
+        v = T(0);
+        s.L.SP[j] = v;
+      }
+      s.L.SP[36 * (npu + b) + 6 * c + a] = v;
+    } else {
+      const int64_t j = i - n3, k = j / 15, d = j % 15;
+      if (!((s.P.kf_mask[k] >> d) & 1)) s.L.rhs[j] = T(0);
+    }
+  }
+}
+
+// Block-Jacobi preconditioner: FP64 Cholesky inverse of each 15x15 SD block.
+template <typename T>
+__global__ void __launch_bounds__(64) k_block_jacobi(SolverLaunch<T> s) {
+  if (s.ctl->terminated) return;
+  const int64_t k = blockIdx.x * (int64_t)blockDim.x + threadIdx.x;
+  if (k >= s.P.nkf) return;
+  double L[120];  // packed lower triangle
+  const T* A = s.L.SD + 225 * k;
+  int fail = 0;
+  for (int j = 0; j < 15 && !fail; ++j) {
+    double d = (double)A[16 * j];
+    for (int q = 0; q < j; ++q) d -= L[j * (j + 1) / 2 + q] * L[j * (j + 1) / 2 + q];
+    if (!(d > 0.0)) { fail = 1; break; }
+    const double ljj = sqrt(d);
+    L[j * (j + 1) / 2 + j] = ljj;
+    for (int i = j + 1; i < 15; ++i) {
+      double v = 0.5 * ((double)A[15 * i + j] + (double)A[15 * j + i]);
+      for (int q = 0; q < j; ++q) v -= L[i * (i + 1) / 2 + q] * L[j * (j + 1) / 2 + q];
+      L[i * (i + 1) / 2 + j] = v / ljj;
+    }
+  }
+  double* M = s.L.Minv + 225 * k;
+  if (fail) {
+    atomicExch(&s.ctl->status, (int)MBA_ERR_NOT_SPD);
+    for (int a = 0; a < 225; ++a) M[a] = (a % 16 == 0) ? 1.0 : 0.0;
+    return;
+  }
+  // Linv (lower) in place of a local 15x15, then M = Linv^T Linv.
+  double X[225];
+  for (int c = 0; c < 15; ++c)
+    for (int i = 0; i < 15; ++i) {
+      double v = (i == c) ? 1.0 : 0.0;
+      for (int q = c; q < i; ++q) v -= L[i * (i + 1) / 2 + q] * X[15 * q + c];
+      X[15 * i + c] = (i < c) ? 0.0 : v / L[i * (i + 1) / 2 + i];
+    }
+  for (int a = 0; a < 15; ++a)
+    for (int b = a; b < 15; ++b) {
+      double v = 0.0;
+      for (int q = b; q < 15; ++q) v += X[15 * q + a] * X[15 * q + b];
+      M[15 * a + b] = v;
+      M[15 * b + a] = v;
+    }
+}
+
+// ------------------------------------------------------------ PCG
+template <typename T>
+__global__ void __launch_bounds__(kB) k_pcg_init(SolverLaunch<T> s) {
+  if (s.ctl->terminated) return;
+  const int64_t i = blockIdx.x * (int64_t)blockDim.x + threadIdx.x;
+  const int64_t n = 15 * s.P.nkf;
+  double rz = 0.0, rr = 0.0;
+  if (i < n) {
+    const int64_t k = i / 15, a = i % 15;
+    const double* M = s.L.Minv + 225 * k;
+    double z = 0.0;
+    for (int b = 0; b < 15; ++b) z += M[15 * a + b] * (double)s.L.rhs[15 * k + b];
+    const double r = (double)s.L.rhs[i];
+    s.L.x[i] = T(0);
+    s.L.r[i] = T(r);
+    s.L.z[i] = T(z);
+    s.L.p[i] = T(z);
+    rz = r * z;
+    rr = r * r;
+  }
+  block_add(rz, &s.ctl->pcg_rz0);
+  block_add(rr, &s.ctl->pcg_bnorm2);
+}
+
+// q = S p and pq += p.q ; one warp per keyframe row.
+template <typename T>
+__global__ void __launch_bounds__(128) k_pcg_spmv(SolverLaunch<T> s, int it) {
+  LmControl* ctl = s.ctl;
+  if (ctl->terminated || ctl->pcg_done || ctl->status) return;
+  if (!(ctl->pcg_bnorm2 > 0.0)) {
+    if (threadIdx.x == 0 && blockIdx.x == 0) { ctl->pcg_done = 1; ctl->pcg_iters = 0; }
+    return;
+  }
+  const int64_t k = (blockIdx.x * (int64_t)blockDim.x + threadIdx.x) >> 5;
+  const int lane = threadIdx.x & 31;
+  double pq = 0.0;
+  if (k < s.P.nkf) {
+    const T* p = s.L.p;
+    double acc[6] = {0, 0, 0, 0, 0, 0};
+    for (int64_t e = s.S.row_off[k] + lane; e < s.S.row_off[k + 1]; e += 32) {
+      const int64_t j = s.S.row_col[e];
+      const T* B = s.L.SP + 36 * (int64_t)s.S.row_blk[e];
+      T pj[6];
+#pragma unroll
+      for (int c = 0; c < 6; ++c) pj[c] = p[15 * j + c];
+#pragma unroll
+      for (int r = 0; r < 6; ++r) {
+        T v = T(0);
+#pragma unroll
+        for (int c = 0; c < 6; ++c) v += B[6 * r + c] * pj[c];
+        acc[r] += (double)v;
+      }
+    }
+#pragma unroll
+    for (int r = 0; r < 6; ++r) acc[r] = wsum(acc[r]);
+    if (lane < 15) {
+      const T* D = s.L.SD + 225 * k;
+      double y = 0.0;
+#pragma unroll
+      for (int c = 0; c < 15; ++c) y += (double)(D[15 * lane + c] * p[15 * k + c]);
+      if (lane < 6) y += acc[lane];
+      for (int64_t e = s.S.kfe_off[k]; e < s.S.kfe_off[k + 1]; ++e) {
+        const int code = s.S.kfe[e];
+        if (code > 0) {
+          const int64_t ed = code - 1;
+          const T* E = s.L.SE + 225 * ed;
+          const int64_t t = s.P.e_to[ed];
+          for (int c = 0; c < 15; ++c) y += (double)(E[15 * lane + c] * p[15 * t + c]);
+        } else {
+          const int64_t ed = -code - 1;
+          const T* E = s.L.SE + 225 * ed;
+          const int64_t f = s.P.e_from[ed];
+          for (int c = 0; c < 15; ++c) y += (double)(E[15 * c + lane] * p[15 * f + c]);
+        }
+      }
+      s.L.q[15 * k + lane] = T(y);
+      pq = y * (double)p[15 * k + lane];
+    }
+  }
+  block_add(pq, &ctl->pcg_pq[it % 3]);
+}
+
+// x += alpha p ; r -= alpha q ; z = M r ; rr, rz dots.  16 threads per keyframe.
+template <typename T>
+__global__ void __launch_bounds__(kB) k_pcg_update(SolverLaunch<T> s, int it) {
+  LmControl* ctl = s.ctl;
+  if (ctl->terminated || ctl->pcg_done || ctl->status) return;
+  __shared__ double rsh[kB];
+  const int64_t k = (blockIdx.x * (int64_t)blockDim.x + threadIdx.x) >> 4;
+  const int a = threadIdx.x & 15;
+  const double rzprev = it == 0 ? ctl->pcg_rz0 : ctl->pcg_rz[(it + 2) % 3];
+  const double alpha = rzprev / ctl->pcg_pq[it % 3];
+  double rr = 0.0, rz = 0.0;
+  double rnew = 0.0;
+  const bool act = (k < s.P.nkf) && a < 15;
+  if (act) {
+    const int64_t i = 15 * k + a;
+    s.L.x[i] = T((double)s.L.x[i] + alpha * (double)s.L.p[i]);
+    rnew = (double)s.L.r[i] - alpha * (double)s.L.q[i];
+    s.L.r[i] = T(rnew);
+  }
+  rsh[threadIdx.x] = rnew;
+  __syncthreads();
+  if (act) {
+    const double* M = s.L.Minv + 225 * k;
+    const int base = threadIdx.x & ~15;
+    double z = 0.0;
+#pragma unroll
+    for (int b = 0; b < 15; ++b) z += M[15 * a + b] * rsh[base + b];
+    s.L.z[15 * k + a] = T(z);
+    rr = rnew * rnew;
+    rz = rnew * z;
+  }
+  if (blockIdx.x == 0 && threadIdx.x == 0) ctl->pcg_pq[(it + 1) % 3] = 0.0;
+  block_add(rr, &ctl->pcg_rr[it % 3]);
+  block_add(rz, &ctl->pcg_rz[it % 3]);
+}
+
+// Convergence test and p = z + beta p.
+template <typename T>
+__global__ void __launch_bounds__(kB) k_pcg_pupdate(SolverLaunch<T> s, int it, int last) {
+  LmControl* ctl = s.ctl;
+  if (ctl->terminated || ctl->pcg_done || ctl->status) return;
+  const double tol = s.prm.linear_tolerance;
+  const bool conv = ctl->pcg_rr[it % 3] <= tol * tol * ctl->pcg_bnorm2;
+  const int64_t i = blockIdx.x * (int64_t)blockDim.x + threadIdx.x;
+  if (conv || last) {
+    if (i == 0) { ctl->pcg_done = 1; ctl->pcg_iters = it + 1; }
+    return;
+  }
+  const double rzprev = it == 0 ? ctl->pcg_rz0 : ctl->pcg_rz[(it + 2) % 3];
+  const double beta = ctl->pcg_rz[it % 3] / rzprev;
+  if (i < 15 * s.P.nkf) s.L.p[i] = T((double)s.L.z[i] + beta * (double)s.L.p[i]);
+  if (i == 0) {
+    ctl->pcg_rr[(it + 1) % 3] = 0.0;
+    ctl->pcg_rz[(it + 1) % 3] = 0.0;
+  }
+}
+
+// ------------------------------------------------------------ step
+// Back substitution: dl = V (-g_s - sum_a Ws_a x_{k_a}).
+template <typename T>
+__global__ void __launch_bounds__(kB) k_backsub(SolverLaunch<T> s) {
+  if (s.ctl->terminated) return;
+  const int64_t l = blockIdx.x * (int64_t)blockDim.x + threadIdx.x;
+  const int64_t NL = s.P.nlm, NS = s.S.nslot;
+  if (l >= NL) return;
+  double t[3];
+  double sl[3];
+  for (int a = 0; a < 3; ++a) { sl[a] = s.sc.slm[a * NL + l]; t[a] = -sl[a] * (double)s.L.gl[a * NL + l]; }
+  for (int64_t i = s.S.lm_slot_off[l]; i < s.S.lm_slot_off[l + 1]; ++i) {
+    const int64_t k = s.S.slot_kf[i];
+    for (int x = 0; x < 3; ++x) {
+      double acc = 0.0;
+      for (int c = 0; c < 6; ++c) acc += (double)s.L.Wslot[(6 * x + c) * NS + i] * s.sc.skf[15 * k + c] * (double)s.L.x[15 * k + c];
+      t[x] -= sl[x] * acc;
+    }
+  }
+  for (int a = 0; a < 3; ++a) {
+    double v = 0.0;
+    for (int b = 0; b < 3; ++b) v += (double)s.L.V[(3 * a + b) * NL + l] * t[b];
+    s.L.dl[a * NL + l] = s.P.lm_active[l] ? v : 0.0;
+  }
+}
+
+// Model cost change -u.(r + u/2) with u = J du (unscaled J, unscaled step).
+template <typename T>
+__global__ void __launch_bounds__(kB) k_model_visual(SolverLaunch<T> s) {
+  if (s.ctl->terminated) return;
+  const int64_t i = blockIdx.x * (int64_t)blockDim.x + threadIdx.x;
+  const int64_t N = s.P.nobs, NL = s.P.nlm;
+  double m = 0.0;
+  if (i < N) {
+    const int64_t l = s.P.obs_lm[i];
+    double u[2] = {0.0, 0.0};
+    for (int rr = 0; rr < 2; ++rr)
+      for (int a = 0; a < 3; ++a)
+        u[rr] += (double)s.vis.Jl[(3 * rr + a) * N + i] * s.sc.slm[a * NL + l] * s.L.dl[a * NL + l];
+    if (s.P.obs_type[i] != MBA_LOCAL_KEYFRAME) {
+      const int64_t ks = s.P.obs_store[i], ko = s.P.obs_kf[i];
+      for (int rr = 0; rr < 2; ++rr)
+        for (int c = 0; c < 6; ++c)
+          u[rr] += (double)s.vis.Js[(6 * rr + c) * N + i] * s.sc.skf[15 * ks + c] * (double)s.L.x[15 * ks + c] +
+                   (double)s.vis.Jo[(6 * rr + c) * N + i] * s.sc.skf[15 * ko + c] * (double)s.L.x[15 * ko + c];
+    }
+    m = -(u[0] * ((double)s.vis.r[i] + u[0] / 2.0) + u[1] * ((double)s.vis.r[N + i] + u[1] / 2.0));
+  }
+  block_add(m, &s.ctl->model_change);
+}
+
+template <typename T>
+__global__ void __launch_bounds__(128) k_model_inertial(SolverLaunch<T> s) {
+  if (s.ctl->terminated) return;
+  const int64_t e = (blockIdx.x * (int64_t)blockDim.x + threadIdx.x) >> 5;
+  const int lane = threadIdx.x & 31;
+  double m = 0.0;
+  if (e < s.P.nedge && lane < 15) {
+    const int64_t f = s.P.e_from[e], t = s.P.e_to[e];
+    double u = 0.0;
+    for (int c = 0; c < 15; ++c)
+      u += (double)s.ine.Jf[225 * e + 15 * lane + c] * s.sc.skf[15 * f + c] * (double)s.L.x[15 * f + c] +
+           (double)s.ine.Jt[225 * e + 15 * lane + c] * s.sc.skf[15 * t + c] * (double)s.L.x[15 * t + c];
+    m = -u * ((double)s.ine.r[15 * e + lane] + u / 2.0);
+  }
+  block_add(m, &s.ctl->model_change);
+}
+
+// Retraction x_cand = Plus(x, s * dx) in FP64 (JplPoseParameterization,
+// JplRollPitchQuaternionParameterization for the gauge keyframe).
+template <typename T>
+__global__ void __launch_bounds__(kB) k_retract(SolverLaunch<T> s) {
+  if (s.ctl->terminated) return;
+  const int64_t i = blockIdx.x * (int64_t)blockDim.x + threadIdx.x;
+  double sn = 0.0, xn = 0.0;
+  if (i < s.P.nkf) {
+    const int64_t k = i;
+    const uint16_t m = s.P.kf_mask[k];
+    const double* x = s.P.kf_state + 16 * k;
+    double* o = s.kf_cand + 16 * k;
+    double d[15];
+    for (int a = 0; a < 15; ++a) d[a] = ((m >> a) & 1) ? s.sc.skf[15 * k + a] * (double)s.L.x[15 * k + a] : 0.0;
+    double q[4] = {x[0], x[1], x[2], x[3]};
+    if (s.P.kf_flags[k] & MBA_KF_GAUGE_ROLL_PITCH) {
+      if (m & 3) jpl_rollpitch_plus(s.P.mis + 8 * s.P.kf_mis[k], x, d, q);
+    } else if (m & 7) {
+      jpl_plus(x, d, q);
+    }
+    for (int a = 0; a < 4; ++a) o[a] = q[a];
+    for (int a = 0; a < 12; ++a) o[4 + a] = x[4 + a] + d[3 + a];
+    const bool pose_var = (m & 0x3f) != 0;
+    if (pose_var)
+      for (int a = 0; a < 7; ++a) { sn += (o[a] - x[a]) * (o[a] - x[a]); xn += x[a] * x[a]; }
+    for (int blk = 0; blk < 3; ++blk)
+      if ((m >> (6 + 3 * blk)) & 7)
+        for (int a = 0; a < 3; ++a) { const double dd = o[7 + 3 * blk + a] - x[7 + 3 * blk + a]; sn += dd * dd; xn += x[7 + 3 * blk + a] * x[7 + 3 * blk + a]; }
+  } else if (i < s.P.nkf + s.P.nlm) {
+    const int64_t l = i - s.P.nkf, NL = s.P.nlm;
+    const double* x = s.P.lm_p + 4 * l;
+    double* o = s.lm_cand + 4 * l;
+    const bool act = s.P.lm_active[l];
+    for (int a = 0; a < 3; ++a) {
+      const double d = act ? s.sc.slm[a * NL + l] * s.L.dl[a * NL + l] : 0.0;
+      o[a] = x[a] + d;
+      if (act) { sn += d * d; xn += x[a] * x[a]; }
+    }
+    o[3] = 0.0;
+  }
+  block_add(sn, &s.ctl->step_norm2);
+  block_add(xn, &s.ctl->x_norm2);
+}
+
+// The LM decision (single thread).
+__global__ void k_decide(LmControl* ctl, LmParams prm, mba_iteration_summary* log) {
+  if (ctl->terminated) return;
+  const int it = ++ctl->iteration;
+  const double mcc = ctl->model_change;
+  const double cost = ctl->cost;
+  double new_cost = ctl->cost_cand;
+  if (ctl->nonfinite || ctl->inertial_status || !isfinite(new_cost)) new_cost = INFINITY;
+  const bool valid = ctl->status == 0 && mcc > 0.0 && isfinite(mcc);
+  int ok = 0;
+  double rel = 0.0;
+  const double step_norm = sqrt(ctl->step_norm2), x_norm = sqrt(ctl->x_norm2);
+  if (valid) {
+    rel = (cost - new_cost) / mcc;
+    ok = isfinite(new_cost) && rel > prm.min_relative_decrease;
+    if (prm.check_tolerances && step_norm <= prm.parameter_tolerance * (x_norm + prm.parameter_tolerance)) {
+      ctl->terminated = 1;
+      ctl->termination = 3;
+    } else if (prm.check_tolerances && fabs(cost - new_cost) <= prm.function_tolerance * cost) {
+      ctl->terminated = 1;
+      ctl->termination = 1;
+    }
+  }
+  if (ok) {
+    ctl->cost = new_cost;
+    ctl->num_successful++;
+    if (!ctl->terminated) {
+      double r = ctl->radius / fmax(1.0 / 3.0, 1.0 - pow(2.0 * rel - 1.0, 3.0));
+      ctl->radius = fmin(r, prm.max_radius);
+      ctl->decrease_factor = 2.0;
+    }
+  } else if (!ctl->terminated) {
+    ctl->radius /= ctl->decrease_factor;
+    ctl->decrease_factor *= 2.0;
+  }
+  ctl->accepted = ok;
+  ctl->total_pcg += ctl->pcg_iters;
+  if (prm.stop_cost > 0.0 && ctl->cost <= prm.stop_cost && ctl->stop_iteration < 0) {
+    ctl->stop_iteration = it;
+    if (!ctl->terminated) { ctl->terminated = 1; ctl->termination = 6; }
+  }
+  if (!ctl->terminated && ctl->radius < prm.min_radius) { ctl->terminated = 1; ctl->termination = 4; }
+  if (!ctl->terminated && it >= prm.max_num_iterations) { ctl->terminated = 1; ctl->termination = 0; }
+  if (log && it <= prm.max_num_iterations) {
+    mba_iteration_summary& e = log[it];
+    e.iteration = it;
+    e.step_is_successful = ok;
+    e.linear_solver_iterations = ctl->pcg_iters;
+    e.cost = ctl->cost;
+    e.cost_change = valid ? cost - new_cost : 0.0;
+    e.gradient_max_norm = 0.0;
+    e.step_norm = step_norm;
+    e.relative_decrease = rel;
+    e.trust_region_radius = ctl->radius;
+    e.iteration_time_ms = 0.0;
+  }
+}
+
+// Accepted step: candidate state and inertial linearization become current.
+template <typename T>
+__global__ void __launch_bounds__(kB) k_accept(SolverLaunch<T> s, InertialLin<double> cand, InertialLin<double> cur) {
+  if (!s.ctl->accepted) return;
+  const int64_t nk = 16 * s.P.nkf, nl = 4 * s.P.nlm, ne1 = 15 * s.P.nedge, ne2 = 225 * s.P.nedge;
+  const int64_t total = nk + nl + ne1 + 2 * ne2;
+  for (int64_t i = blockIdx.x * (int64_t)blockDim.x + threadIdx.x; i < total; i += (int64_t)gridDim.x * blockDim.x) {
+    if (i < nk) s.P.kf_state[i] = s.kf_cand[i];
+    else if (i < nk + nl) s.P.lm_p[i - nk] = s.lm_cand[i - nk];
+    else if (i < nk + nl + ne1) {
+      const int64_t j = i - nk - nl;
+      cur.r[j] = cand.r[j];
+      s.ine.r[j] = T(cand.r[j]);
+    } else if (i < nk + nl + ne1 + ne2) {
+      const int64_t j = i - nk - nl - ne1;
+      cur.Jf[j] = cand.Jf[j];
+      s.ine.Jf[j] = T(cand.Jf[j]);
+    } else {
+      const int64_t j = i - nk - nl - ne1 - ne2;
+      cur.Jt[j] = cand.Jt[j];
+      s.ine.Jt[j] = T(cand.Jt[j]);
+    }
+  }
+}
+
+__global__ void k_init_control(LmControl* ctl, double radius) {
+  ctl->radius = radius;
+  ctl->decrease_factor = 2.0;
+  ctl->accepted = 0;
+  ctl->terminated = 0;
+  ctl->termination = 0;
+  ctl->iteration = 0;
+  ctl->num_successful = 0;
+  ctl->total_pcg = 0;
+  ctl->status = 0;
+  ctl->stop_iteration = -1;
+}
+
+template <typename T>
+__global__ void k_copy_cast(const double* a, T* b, int64_t n) {
+  const int64_t i = blockIdx.x * (int64_t)blockDim.x + threadIdx.x;
+  if (i < n) b[i] = T(a[i]);
+}
+
+inline unsigned nblk(int64_t n, int b) { return (unsigned)((n + b - 1) / b); }
+inline unsigned gridcap(int64_t n) {
+  const int64_t b = (n + kB - 1) / kB;
+  return (unsigned)(b < 152 * 16 ? (b < 1 ? 1 : b) : 152 * 16);
+}
+
+}  // namespace
+
+cudaError_t solver_init_control(LmControl* ctl, double radius, cudaStream_t st) {
+  k_init_control<<<1, 1, 0, st>>>(ctl, radius);
+  return cudaGetLastError();
+}
+
+template <typename T>
+cudaError_t solver_assemble(const SolverLaunch<T>& s, const int* gate, cudaStream_t st) {
+  const int* skip = gate ? &s.ctl->terminated : nullptr;
+  k_zero<T><<<gridcap(225 * s.P.nkf), kB, 0, st>>>(s.L.Dbase, 225 * s.P.nkf, gate, skip);
+  k_zero<T><<<gridcap(15 * s.P.nkf), kB, 0, st>>>(s.L.gc, 15 * s.P.nkf, gate, skip);
+  if (s.S.npu) k_zero<T><<<gridcap(36 * s.S.npu), kB, 0, st>>>(s.L.Pbase, 36 * s.S.npu, gate, skip);
+  if (s.P.nlm) k_assemble_lm<T><<<nblk(s.P.nlm, kB), kB, 0, st>>>(s.P, s.S, s.vis, s.L, gate, skip);
+  if (s.P.nedge) k_assemble_inertial<T><<<nblk(32 * s.P.nedge, 128), 128, 0, st>>>(s.P, s.ine, s.L, gate, skip);
+  return cudaGetLastError();
+}
+
+template <typename T>
+cudaError_t solver_compute_scale(const SolverLaunch<T>& s, int jacobi, cudaStream_t st) {
+  const int64_t n = 15 * s.P.nkf + 3 * s.P.nlm;
+  k_scale<T><<<nblk(n, kB), kB, 0, st>>>(s.P, s.L, s.sc, jacobi);
+  return cudaGetLastError();
+}
+
+template <typename T>
+cudaError_t solver_step(const SolverLaunch<T>& s, cudaStream_t st) {
+  const int64_t nsys = 225 * s.P.nkf + 225 * s.P.nedge + 36 * s.S.npu + 15 * s.P.nkf;
+  k_build_system<T><<<gridcap(nsys), kB, 0, st>>>(s);
+  if (s.P.nlm) k_schur_lm<T><<<nblk(s.P.nlm, kB), kB, 0, st>>>(s);
+  if (s.S.nslot) k_schur_slot<T><<<nblk(s.S.nslot, kB), kB, 0, st>>>(s);
+  if (s.S.npair) k_schur_pairs<T><<<nblk(s.S.npair, kB), kB, 0, st>>>(s);
+  k_finalize_system<T><<<gridcap(nsys), kB, 0, st>>>(s);
+  k_block_jacobi<T><<<nblk(s.P.nkf, 64), 64, 0, st>>>(s);
+  const int64_t n = 15 * s.P.nkf;
+  k_pcg_init<T><<<nblk(n, kB), kB, 0, st>>>(s);
+  const int maxit = s.prm.max_linear_iterations;
+  for (int it = 0; it < maxit; ++it) {
+    k_pcg_spmv<T><<<nblk(32 * s.P.nkf, 128), 128, 0, st>>>(s, it);
+    k_pcg_update<T><<<nblk(16 * s.P.nkf, kB), kB, 0, st>>>(s, it);
+    k_pcg_pupdate<T><<<nblk(n, kB), kB, 0, st>>>(s, it, it == maxit - 1);
+  }
+  if (s.P.nlm) k_backsub<T><<<nblk(s.P.nlm, kB), kB, 0, st>>>(s);
+  if (s.P.nobs) k_model_visual<T><<<nblk(s.P.nobs, kB), kB, 0, st>>>(s);
+  if (s.P.nedge) k_model_inertial<T><<<nblk(32 * s.P.nedge, 128), 128, 0, st>>>(s);
+  k_retract<T><<<nblk(s.P.nkf + s.P.nlm, kB), kB, 0, st>>>(s);
+  return cudaGetLastError();
+}
+
+template <typename T>
+cudaError_t solver_evaluate_candidate(const SolverLaunch<T>& s, InertialLin<double> ine_cand, cudaStream_t st) {
+  cudaError_t e = launch_visual_cost_gated(s.P, s.kf_cand, s.lm_cand, &s.ctl->cost_cand, &s.ctl->nonfinite,
+                                           &s.ctl->terminated, st);
+  if (e != cudaSuccess) return e;
+  return launch_inertial_gated(s.P, s.kf_cand, ine_cand, &s.ctl->cost_cand, &s.ctl->inertial_status,
+                               &s.ctl->terminated, st);
+}
+
+template <typename T>
+cudaError_t solver_decide_and_accept(const SolverLaunch<T>& s, InertialLin<double> ine_cand,
+                                     InertialLin<double> ine_cur, cudaStream_t st) {
+  k_decide<<<1, 1, 0, st>>>(s.ctl, s.prm, s.log);
+  const int64_t total = 16 * s.P.nkf + 4 * s.P.nlm + 465 * s.P.nedge;
+  k_accept<T><<<gridcap(total), kB, 0, st>>>(s, ine_cand, ine_cur);
+  return cudaGetLastError();
+}
+
+template <typename T>
+cudaError_t solver_relinearize(const SolverLaunch<T>& s, const InertialLin<double>& ine_cur, cudaStream_t st) {
+  (void)ine_cur;
+  cudaError_t e = launch_visual_linearize_gated<T>(s.P, s.vis, nullptr, &s.ctl->accepted, &s.ctl->terminated, st);
+  if (e != cudaSuccess) return e;
+  return solver_assemble<T>(s, &s.ctl->accepted, st);
+}
+
+template cudaError_t solver_assemble<double>(const SolverLaunch<double>&, const int*, cudaStream_t);
+template cudaError_t solver_assemble<float>(const SolverLaunch<float>&, const int*, cudaStream_t);
+template cudaError_t solver_compute_scale<double>(const SolverLaunch<double>&, int, cudaStream_t);
+template cudaError_t solver_compute_scale<float>(const SolverLaunch<float>&, int, cudaStream_t);
+template cudaError_t solver_step<double>(const SolverLaunch<double>&, cudaStream_t);
+template cudaError_t solver_step<float>(const SolverLaunch<float>&, cudaStream_t);
+template cudaError_t solver_evaluate_candidate<double>(const SolverLaunch<double>&, InertialLin<double>, cudaStream_t);
+template cudaError_t solver_evaluate_candidate<float>(const SolverLaunch<float>&, InertialLin<double>, cudaStream_t);
+template cudaError_t solver_decide_and_accept<double>(const SolverLaunch<double>&, InertialLin<double>,
+                                                      InertialLin<double>, cudaStream_t);
+template cudaError_t solver_decide_and_accept<float>(const SolverLaunch<float>&, InertialLin<double>,
+                                                     InertialLin<double>, cudaStream_t);
+template cudaError_t solver_relinearize<double>(const SolverLaunch<double>&, const InertialLin<double>&, cudaStream_t);
+template cudaError_t solver_relinearize<float>(const SolverLaunch<float>&, const InertialLin<double>&, cudaStream_t);
+
+}  // namespace mba

@@ -1,0 +1,116 @@
+"""Extracts golden vectors from the reference's own unit tests (read as text).
+
+Run in a container where the maplab source tree is mounted:
+
+    python tests/golden/make_golden.py /path/to/maplab
+
+It writes tests/golden/imu_integrator.json with the known-answer cases of
+algorithms/imu-integrator-rk4/test/test_imu_integrator_cov_phi_test.cc
+(ImuIntegratorPhiTest, ImuIntegratorCovarianceTest: expected 16-dim state,
+15x15 transition and 15x15 covariance at 1e-12) and the closed-form cases of
+test_imu_integrator_basic_test.cc (restated as inputs + expected outputs).
+The numbers are copied verbatim from the reference tests; nothing is
+recomputed here.
+"""
+import json
+import math
+import os
+import re
+import sys
+
+
+def _numbers_after(text, marker, count):
+    i = text.index(marker)
+    j = text.index("<<", i) + 2
+    k = text.index(";", j)
+    nums = re.findall(r"[-+]?\d+(?:\.\d*)?(?:[eE][-+]?\d+)?", text[j:k])
+    vals = [float(x) for x in nums]
+    assert len(vals) == count, (marker, len(vals))
+    return vals
+
+
+def _test_body(text, name):
+    i = text.index(name)
+    j = text.index("TEST_F", i + len(name)) if "TEST_F" in text[i + len(name):] else len(text)
+    return text[i:j]
+
+
+def main(root):
+    base = os.path.join(root, "algorithms", "imu-integrator-rk4", "test")
+    src = open(os.path.join(base, "test_imu_integrator_cov_phi_test.cc")).read()
+    phi_body = _test_body(src, "ImuIntegratorPhiTest")
+    cov_body = _test_body(src, "ImuIntegratorCovarianceTest")
+    s2 = math.sqrt(2.0) / 2.0
+    # Common inputs of both tests (cov_phi_test.cc:14-40 and :94-121).
+    readings = [0.3, 0.0, 9.81, 0.0, 0.2, 0.0, 0.3, 0.0, 9.81, 0.0, 0.2, 0.0]
+    state = [0.0, 0.0, -s2, s2, 0, 0, 0, 0.0, 2.5, 0.0, 0, 0, 0, 0, 0, 0]
+    cases = [
+        {
+            "name": "ImuIntegratorPhiTest",
+            "source": "algorithms/imu-integrator-rk4/test/test_imu_integrator_cov_phi_test.cc:13-90",
+            "gravity": 9.81, "sigmas": [0.0, 0.0, 0.0, 0.0], "dt": 1.2,
+            "state": state, "readings": readings, "tol": 1e-12,
+            "expected_state": _numbers_after(phi_body, "expected_state", 16),
+            "expected_phi": _numbers_after(phi_body, "expected_phi", 225),
+        },
+        {
+            "name": "ImuIntegratorCovarianceTest",
+            "source": "algorithms/imu-integrator-rk4/test/test_imu_integrator_cov_phi_test.cc:92-178",
+            "gravity": 9.81, "sigmas": [0.1, 0.2, 0.3, 0.4], "dt": 1.2,
+            "state": state, "readings": readings, "tol": 1e-12,
+            "expected_state": _numbers_after(cov_body, "expected_state", 16),
+            "expected_cov": _numbers_after(cov_body, "expected_cov", 225),
+        },
+    ]
+    # Closed-form cases of test_imu_integrator_basic_test.cc (inputs and the
+    # expected values stated by those tests).
+    a, v = 0.3, 2.5
+    basic = []
+    basic.append({"name": "ZeroReadingsZeroBiases", "source": "test_imu_integrator_basic_test.cc:13-28",
+                  "gravity": 0.0, "dt": 1.0, "state": [0, 0, 0, 1] + [0] * 12, "readings": [0.0] * 12,
+                  "expected_state": [0, 0, 0, 1] + [0] * 12, "tol": 1e-15, "cov_zero": True})
+    basic.append({"name": "JustNonzeroGravity", "source": "test_imu_integrator_basic_test.cc:30-60",
+                  "gravity": 1.0, "dt": 1.0, "state": [0, 0, 0, 1] + [0] * 12, "readings": [0.0] * 12,
+                  "expected_state": [0, 0, 0, 1, 0, 0, 0, 0, 0, -1.0, 0, 0, 0, 0, 0, -0.5], "tol": 1e-15,
+                  "cov_zero": True})
+    basic.append({"name": "ConstantForwardAcceleration", "source": "test_imu_integrator_basic_test.cc:62-95",
+                  "gravity": 9.81, "dt": 1.0, "state": [0, 0, 0, 1] + [0] * 12,
+                  "readings": [a, 0, 9.81, 0, 0, 0, a, 0, 9.81, 0, 0, 0],
+                  "expected_state": [0, 0, 0, 1, 0, 0, 0, a, 0, 0, 0, 0, 0, a / 2, 0, 0], "tol": 1e-15,
+                  "cov_zero": True})
+    dt = 1.8
+    basic.append({"name": "ConstForwardAccelInitialVelocity", "source": "test_imu_integrator_basic_test.cc:97-136",
+                  "gravity": 9.81, "dt": dt, "state": [0, 0, 0, 1, 0, 0, 0, v, 0, 0, 0, 0, 0, 0, 0, 0],
+                  "readings": [a, 0, 9.81, 0, 0, 0, a, 0, 9.81, 0, 0, 0],
+                  "expected_state": [0, 0, 0, 1, 0, 0, 0, v + a * dt, 0, 0, 0, 0, 0,
+                                     v * dt + a * dt * dt / 2, 0, 0], "tol": 1e-15, "cov_zero": True})
+    dt = 1.2
+    basic.append({"name": "ConstAccelAndVelocityWhenRotated", "source": "test_imu_integrator_basic_test.cc:138-181",
+                  "gravity": 9.81, "dt": dt, "state": [0, 0, s2, s2, 0, 0, 0, 0, v, 0, 0, 0, 0, 0, 0, 0],
+                  "readings": [a, 0, 9.81, 0, 0, 0, a, 0, 9.81, 0, 0, 0],
+                  "expected_state": [0, 0, s2, s2, 0, 0, 0, 0, v + a * dt, 0, 0, 0, 0, 0,
+                                     v * dt + a * dt * dt / 2, 0], "tol": 1e-15, "cov_zero": True})
+    w = math.pi / 180.0
+    basic.append({"name": "ConstantAngularVelocity", "source": "test_imu_integrator_basic_test.cc:183-226",
+                  "gravity": 9.81, "dt": 1.0, "state": [0, 0, 0, 1] + [0] * 12,
+                  "readings": [0, 0, 9.81, 0, 0, w, 0, 0, 9.81, 0, 0, w],
+                  "expected_quat": [0, 0, math.sin(w / 2), math.cos(w / 2)], "quat_tol": 1e-10})
+    basic.append({"name": "AngularVelocitySlope", "source": "test_imu_integrator_basic_test.cc:228-256",
+                  "gravity": 0.0, "dt": 1.0, "state": [0, 0, 0, 1] + [0] * 12,
+                  "readings": [0, 0, 0, 0, 0, w, 0, 0, 0, 0, 0, 0],
+                  "expected_quat": [0, 0, math.sin(w / 4), math.cos(w / 4)], "quat_tol": 1e-8})
+    dt = 3.0
+    basic.append({"name": "LinearAccelerationSlope", "source": "test_imu_integrator_basic_test.cc:258-288",
+                  "gravity": 9.81, "dt": dt, "state": [0, 0, 0, 1] + [0] * 12,
+                  "readings": [0.5, 0, 9.81, 0, 0, 0, 0, 0, 9.81, 0, 0, 0],
+                  "expected_velocity": [0.5 * dt / 2, 0, 0],
+                  "expected_position": [0.5 * dt * dt / 3, 0, 0], "tol": 1e-15})
+    out = {"generator": "tests/golden/make_golden.py", "cases": cases, "basic": basic}
+    here = os.path.dirname(os.path.abspath(__file__))
+    with open(os.path.join(here, "imu_integrator.json"), "w") as f:
+        json.dump(out, f, indent=1)
+    print("wrote", os.path.join(here, "imu_integrator.json"))
+
+
+if __name__ == "__main__":
+    main(sys.argv[1] if len(sys.argv) > 1 else "/root/reference")

@@ -1,0 +1,113 @@
+"""Device Levenberg-Marquardt against the oracle's restated LM.
+
+Bar (FP64 path): final cost within 1e-6 relative of the oracle after the same
+iteration count, per-iteration costs likewise.  The oracle solves the reduced
+camera system by dense Cholesky; the device by block-Jacobi PCG run to a tight
+tolerance (1e-10) so both compute the same LM steps.
+"""
+import numpy as np
+import pytest
+
+import oracle_lib as O
+from maplab_gb300 import _native as N
+from maplab_gb300 import ba, synth
+from problem_util import OwnedDesc, camera, unit_quat
+
+pytestmark = pytest.mark.gpu
+
+
+def _oracle_opts(iters):
+    o = N.default_solver_options()
+    o.max_num_iterations = iters
+    o.linear_solver = N.MBA_LINEAR_SOLVER_DENSE_SCHUR
+    o.check_tolerances = 0
+    return o
+
+
+def _gpu_opts(iters, **kw):
+    kw.setdefault("linear_tolerance", 1e-10)
+    kw.setdefault("max_linear_iterations", 500)
+    return ba.default_options(max_num_iterations=iters, check_tolerances=0, **kw)
+
+
+@pytest.fixture(scope="module")
+def c1_oracle_run():
+    m = synth.generate("c1")
+    o = O.OracleProblem(m.desc)
+    s = o.solve(_oracle_opts(10))
+    return m, s, o.read_state()
+
+
+def test_c1_fp64_final_cost_matches_oracle(c1_oracle_run):
+    m, so, st_o = c1_oracle_run
+    with ba.BundleAdjuster(m.desc) as g:
+        sg = g.solve(_gpu_opts(10))
+        st_g = g.read_state()
+    assert abs(sg["initial_cost"] - so["initial_cost"]) <= 1e-12 * so["initial_cost"]
+    assert abs(sg["final_cost"] - so["final_cost"]) <= 1e-6 * so["final_cost"], (sg["final_cost"], so["final_cost"])
+    for a, b in zip(sg["iterations"], so["iterations"]):
+        assert abs(a["cost"] - b["cost"]) <= 1e-6 * b["cost"], (a, b)
+        assert a["ok"] == b["ok"]
+    # the optimized states agree closely as well
+    np.testing.assert_allclose(st_g["kf_q_IM_p_MI"], st_o["kf_q_IM_p_MI"], atol=1e-6)
+    np.testing.assert_allclose(st_g["lm_p_B"], st_o["lm_p_B"], atol=1e-4)
+
+
+def test_c1_eager_and_graph_agree():
+    m = synth.generate("c1", keyframes_per_mission=40, num_landmarks=800)
+    with ba.BundleAdjuster(m.desc) as g:
+        s1 = g.solve(_gpu_opts(5, use_cuda_graph=1))
+    with ba.BundleAdjuster(m.desc) as g:
+        s2 = g.solve(_gpu_opts(5, use_cuda_graph=0))
+    assert s1["final_cost"] == s2["final_cost"] or abs(s1["final_cost"] - s2["final_cost"]) <= 1e-9 * s2["final_cost"]
+
+
+def test_c1_mixed_precision_reaches_fp64_cost(c1_oracle_run):
+    m, so, _ = c1_oracle_run
+    with ba.BundleAdjuster(m.desc) as g:
+        sg = g.solve(_gpu_opts(20, precision=N.MBA_PRECISION_MIXED, linear_tolerance=1e-6, max_linear_iterations=100))
+    # The mixed path's cost is reduced in FP64; after more iterations it
+    # reaches the FP64 path's 10-iteration cost within 1e-6 relative.
+    assert sg["final_cost"] <= so["final_cost"] * (1 + 1e-6), (sg["final_cost"], so["final_cost"])
+
+
+def test_visual_only_problem_matches_oracle():
+    m = synth.generate("c1", keyframes_per_mission=30, num_landmarks=600, include_inertial=0)
+    o = O.OracleProblem(m.desc)
+    so = o.solve(_oracle_opts(6))
+    with ba.BundleAdjuster(m.desc) as g:
+        sg = g.solve(_gpu_opts(6))
+    assert abs(sg["final_cost"] - so["final_cost"]) <= 1e-6 * so["final_cost"], (sg["final_cost"], so["final_cost"])
+
+
+def test_multi_mission_global_terms_match_oracle():
+    m = synth.generate("c4", num_missions=3, keyframes_per_mission=40, num_landmarks=1500,
+                       shared_landmark_fraction=0.3)
+    o = O.OracleProblem(m.desc)
+    so = o.solve(_oracle_opts(5))
+    with ba.BundleAdjuster(m.desc) as g:
+        sg = g.solve(_gpu_opts(5))
+    assert abs(sg["final_cost"] - so["final_cost"]) <= 1e-6 * so["final_cost"], (sg["final_cost"], so["final_cost"])
+
+
+def test_landmark_recovery_two_observers():
+    """test_visual_term_test.cc style ground-truth recovery on the device."""
+    cam = camera(q_CI=unit_quat(0.5, -0.5, 0.5, -0.5))
+    kx = np.array([[0, 0, 0, 1, 0, 0, 0], np.concatenate([unit_quat(0, 0, 0.05, 1), [0.0, 0.5, 0.0]])])
+    uv = [[353.02323456, 255.31784363], [437.32659405, 255.37958988]]  # projections of (6, 0.3, -0.2)
+    od = OwnedDesc(obs_uv=uv, obs_sigma=[0.7, 0.7], obs_landmark=[0, 0], obs_keyframe=[0, 1], obs_camera=[0, 0],
+                   lm_p_B=[[6.3, 0.1, 0.05]], lm_store_keyframe=[0], kf_q_IM_p_MI=kx,
+                   kf_flags=[N.MBA_KF_POSE_CONSTANT] * 2, cameras=[cam])
+    with ba.BundleAdjuster(od.desc) as g:
+        s = g.solve(_gpu_opts(30, function_tolerance=0.0, parameter_tolerance=0.0))
+        st = g.read_state()
+    assert s["final_cost"] < 1e-12
+    np.testing.assert_allclose(st["lm_p_B"][0], [6.0, 0.3, -0.2], atol=1e-6)
+
+
+def test_zero_iterations_returns_cost():
+    m = synth.generate("c1", keyframes_per_mission=20, num_landmarks=200)
+    o = O.OracleProblem(m.desc)
+    with ba.BundleAdjuster(m.desc) as g:
+        s = g.solve(_gpu_opts(0))
+    assert abs(s["final_cost"] - o.cost()) <= 1e-12 * o.cost()
