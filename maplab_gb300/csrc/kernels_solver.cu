@@ -456,7 +456,7 @@ __global__ void __launch_bounds__(kB) k_pcg_init(SolverLaunch<T> s) {
     s.L.x[i] = T(0);
     s.L.r[i] = T(r);
     s.L.z[i] = T(z);
-    s.L.p[i] = T(z);
+    s.L.p[i] = T(z);  // read with beta = 0 by the first product; must be finite
     rz = r * z;
     rr = r * r;
   }
@@ -464,32 +464,46 @@ __global__ void __launch_bounds__(kB) k_pcg_init(SolverLaunch<T> s) {
   block_add(rr, &s.ctl->pcg_bnorm2);
 }
 
-// q = S p and pq += p.q ; one warp per keyframe row.
+// Direction update fused into the product: p_new = z + beta p_old (beta = 0
+// at it = 0, where p_old = z), q = S p_new, pq += p_new.q.  p is double
+// buffered (pa -> pb) because neighbour rows read p_old while each warp writes
+// its own p_new.  At it > 0 the convergence test of the previous update runs
+// first.  One warp per keyframe row.
 template <typename T>
-__global__ void __launch_bounds__(128) k_pcg_spmv(SolverLaunch<T> s, int it) {
+__global__ void __launch_bounds__(128) k_pcg_spmv(SolverLaunch<T> s, int it, const T* pa, T* pb) {
   LmControl* ctl = s.ctl;
   if (ctl->terminated || ctl->pcg_done || ctl->status) return;
   if (!(ctl->pcg_bnorm2 > 0.0)) {
     if (threadIdx.x == 0 && blockIdx.x == 0) { ctl->pcg_done = 1; ctl->pcg_iters = 0; }
     return;
   }
+  double beta = 0.0;
+  if (it > 0) {
+    const double tol = s.prm.linear_tolerance;
+    if (ctl->pcg_rr[(it - 1) % 3] <= tol * tol * ctl->pcg_bnorm2) {
+      if (threadIdx.x == 0 && blockIdx.x == 0) { ctl->pcg_done = 1; ctl->pcg_iters = it; }
+      return;
+    }
+    const double rzprev = (it == 1) ? ctl->pcg_rz0 : ctl->pcg_rz[(it + 1) % 3];
+    beta = ctl->pcg_rz[(it - 1) % 3] / rzprev;
+  }
+  const T* z = s.L.z;
   const int64_t k = (blockIdx.x * (int64_t)blockDim.x + threadIdx.x) >> 5;
   const int lane = threadIdx.x & 31;
   double pq = 0.0;
   if (k < s.P.nkf) {
-    const T* p = s.L.p;
     double acc[6] = {0, 0, 0, 0, 0, 0};
     for (int64_t e = s.S.row_off[k] + lane; e < s.S.row_off[k + 1]; e += 32) {
       const int64_t j = s.S.row_col[e];
       const T* B = s.L.SP + 36 * (int64_t)s.S.row_blk[e];
-      T pj[6];
+      double pj[6];
 #pragma unroll
-      for (int c = 0; c < 6; ++c) pj[c] = p[15 * j + c];
+      for (int c = 0; c < 6; ++c) pj[c] = (double)z[15 * j + c] + beta * (double)pa[15 * j + c];
 #pragma unroll
       for (int r = 0; r < 6; ++r) {
         T v = T(0);
 #pragma unroll
-        for (int c = 0; c < 6; ++c) v += B[6 * r + c] * pj[c];
+        for (int c = 0; c < 6; ++c) v += B[6 * r + c] * T(pj[c]);
         acc[r] += (double)v;
       }
     }
@@ -499,24 +513,24 @@ __global__ void __launch_bounds__(128) k_pcg_spmv(SolverLaunch<T> s, int it) {
       const T* D = s.L.SD + 225 * k;
       double y = 0.0;
 #pragma unroll
-      for (int c = 0; c < 15; ++c) y += (double)(D[15 * lane + c] * p[15 * k + c]);
+      for (int c = 0; c < 15; ++c)
+        y += (double)(D[15 * lane + c] * T((double)z[15 * k + c] + beta * (double)pa[15 * k + c]));
       if (lane < 6) y += acc[lane];
       for (int64_t e = s.S.kfe_off[k]; e < s.S.kfe_off[k + 1]; ++e) {
         const int code = s.S.kfe[e];
-        if (code > 0) {
-          const int64_t ed = code - 1;
-          const T* E = s.L.SE + 225 * ed;
-          const int64_t t = s.P.e_to[ed];
-          for (int c = 0; c < 15; ++c) y += (double)(E[15 * lane + c] * p[15 * t + c]);
-        } else {
-          const int64_t ed = -code - 1;
-          const T* E = s.L.SE + 225 * ed;
-          const int64_t f = s.P.e_from[ed];
-          for (int c = 0; c < 15; ++c) y += (double)(E[15 * c + lane] * p[15 * f + c]);
+        const bool from = code > 0;
+        const int64_t ed = from ? code - 1 : -code - 1;
+        const T* E = s.L.SE + 225 * ed;
+        const int64_t o = from ? s.P.e_to[ed] : s.P.e_from[ed];
+        for (int c = 0; c < 15; ++c) {
+          const T pv = T((double)z[15 * o + c] + beta * (double)pa[15 * o + c]);
+          y += (double)((from ? E[15 * lane + c] : E[15 * c + lane]) * pv);
         }
       }
+      const double pk = (double)z[15 * k + lane] + beta * (double)pa[15 * k + lane];
+      pb[15 * k + lane] = T(pk);
       s.L.q[15 * k + lane] = T(y);
-      pq = y * (double)p[15 * k + lane];
+      pq = y * pk;
     }
   }
   block_add(pq, &ctl->pcg_pq[it % 3]);
@@ -524,7 +538,7 @@ __global__ void __launch_bounds__(128) k_pcg_spmv(SolverLaunch<T> s, int it) {
 
 // x += alpha p ; r -= alpha q ; z = M r ; rr, rz dots.  16 threads per keyframe.
 template <typename T>
-__global__ void __launch_bounds__(kB) k_pcg_update(SolverLaunch<T> s, int it) {
+__global__ void __launch_bounds__(kB) k_pcg_update(SolverLaunch<T> s, int it, const T* p, int last) {
   LmControl* ctl = s.ctl;
   if (ctl->terminated || ctl->pcg_done || ctl->status) return;
   __shared__ double rsh[kB];
@@ -537,7 +551,7 @@ __global__ void __launch_bounds__(kB) k_pcg_update(SolverLaunch<T> s, int it) {
   const bool act = (k < s.P.nkf) && a < 15;
   if (act) {
     const int64_t i = 15 * k + a;
-    s.L.x[i] = T((double)s.L.x[i] + alpha * (double)s.L.p[i]);
+    s.L.x[i] = T((double)s.L.x[i] + alpha * (double)p[i]);
     rnew = (double)s.L.r[i] - alpha * (double)s.L.q[i];
     s.L.r[i] = T(rnew);
   }
@@ -553,30 +567,14 @@ __global__ void __launch_bounds__(kB) k_pcg_update(SolverLaunch<T> s, int it) {
     rr = rnew * rnew;
     rz = rnew * z;
   }
-  if (blockIdx.x == 0 && threadIdx.x == 0) ctl->pcg_pq[(it + 1) % 3] = 0.0;
-  block_add(rr, &ctl->pcg_rr[it % 3]);
-  block_add(rz, &ctl->pcg_rz[it % 3]);
-}
-
-// Convergence test and p = z + beta p.
-template <typename T>
-__global__ void __launch_bounds__(kB) k_pcg_pupdate(SolverLaunch<T> s, int it, int last) {
-  LmControl* ctl = s.ctl;
-  if (ctl->terminated || ctl->pcg_done || ctl->status) return;
-  const double tol = s.prm.linear_tolerance;
-  const bool conv = ctl->pcg_rr[it % 3] <= tol * tol * ctl->pcg_bnorm2;
-  const int64_t i = blockIdx.x * (int64_t)blockDim.x + threadIdx.x;
-  if (conv || last) {
-    if (i == 0) { ctl->pcg_done = 1; ctl->pcg_iters = it + 1; }
-    return;
-  }
-  const double rzprev = it == 0 ? ctl->pcg_rz0 : ctl->pcg_rz[(it + 2) % 3];
-  const double beta = ctl->pcg_rz[it % 3] / rzprev;
-  if (i < 15 * s.P.nkf) s.L.p[i] = T((double)s.L.z[i] + beta * (double)s.L.p[i]);
-  if (i == 0) {
+  if (blockIdx.x == 0 && threadIdx.x == 0) {
+    ctl->pcg_pq[(it + 1) % 3] = 0.0;
     ctl->pcg_rr[(it + 1) % 3] = 0.0;
     ctl->pcg_rz[(it + 1) % 3] = 0.0;
+    if (last) ctl->pcg_iters = it + 1;
   }
+  block_add(rr, &ctl->pcg_rr[it % 3]);
+  block_add(rz, &ctl->pcg_rz[it % 3]);
 }
 
 // ------------------------------------------------------------ step
@@ -837,9 +835,10 @@ cudaError_t solver_step(const SolverLaunch<T>& s, cudaStream_t st) {
   k_pcg_init<T><<<nblk(n, kB), kB, 0, st>>>(s);
   const int maxit = s.prm.max_linear_iterations;
   for (int it = 0; it < maxit; ++it) {
-    k_pcg_spmv<T><<<nblk(32 * s.P.nkf, 128), 128, 0, st>>>(s, it);
-    k_pcg_update<T><<<nblk(16 * s.P.nkf, kB), kB, 0, st>>>(s, it);
-    k_pcg_pupdate<T><<<nblk(n, kB), kB, 0, st>>>(s, it, it == maxit - 1);
+    T* pa = (it & 1) ? s.L.q2 : s.L.p;
+    T* pb = (it & 1) ? s.L.p : s.L.q2;
+    k_pcg_spmv<T><<<nblk(32 * s.P.nkf, 128), 128, 0, st>>>(s, it, pa, pb);
+    k_pcg_update<T><<<nblk(16 * s.P.nkf, kB), kB, 0, st>>>(s, it, pb, it == maxit - 1);
   }
   if (s.P.nlm) k_backsub<T><<<nblk(s.P.nlm, kB), kB, 0, st>>>(s);
   if (s.P.nobs) k_model_visual<T><<<nblk(s.P.nobs, kB), kB, 0, st>>>(s);

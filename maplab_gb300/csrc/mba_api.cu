@@ -185,6 +185,7 @@ mba_status ensure_solver_buffers(mba_handle* h, SolverBuffers<T>& b) {
   L.z = A.alloc<T>(15 * NK);
   L.p = A.alloc<T>(15 * NK);
   L.q = A.alloc<T>(15 * NK);
+  L.q2 = A.alloc<T>(15 * NK);
   L.dl = A.alloc<double>(3 * NL);
   if (A.err != cudaSuccess) return MBA_ERR_CUDA;
   b.ready = true;

@@ -87,7 +87,7 @@ struct LinearSystem {
   T* V;      // [9][nlm]
   T* U;      // [18][nslot]
   double* Minv;  // [nkf][225]
-  T *x, *r, *z, *p, *q;  // [nkf*15]
+  T *x, *r, *z, *p, *q, *q2;  // [nkf*15]; p and q2 double-buffer the PCG direction
   double* dl;    // [3][nlm] scaled landmark step
 };
 
