@@ -270,6 +270,50 @@ typedef struct mba_problem_stats {
 } mba_problem_stats;
 mba_status mba_get_stats(mba_handle* h, mba_problem_stats* stats);
 
+/* Visual observations and the state they depend on, all in DEVICE memory
+ * owned by the caller, laid out as in mba_problem_desc (state arrays in the
+ * caller's layout: kf_q_IM_p_MI [N_kf][7], lm_p_B [N_lm][3], ...). */
+typedef struct mba_visual_batch_device {
+  int64_t num_observations;
+  int64_t num_landmarks, num_keyframes, num_missions, num_cameras;
+  const double* obs_uv;            /* [N_obs][2] */
+  const double* obs_sigma;         /* [N_obs] */
+  const int32_t* obs_landmark;     /* [N_obs] */
+  const int32_t* obs_keyframe;     /* [N_obs] */
+  const int32_t* obs_camera;       /* [N_obs] */
+  const int32_t* lm_store_keyframe;/* [N_lm] */
+  const double* lm_p_B;            /* [N_lm][3] */
+  const double* kf_q_IM_p_MI;      /* [N_kf][7] */
+  const int32_t* kf_mission;       /* [N_kf] */
+  const double* mission_q_GM_p_GM; /* [N_mis][7] */
+  const mba_camera* cameras;       /* [N_cam] */
+  int32_t use_huber;
+  int32_t pad_;
+  double huber_delta_local, huber_delta_global;
+} mba_visual_batch_device;
+
+/* Robustified visual cost 0.5 * sum rho(|r|^2) of a batch, computed without
+ * allocating any memory.  This entry point has no counterpart in the
+ * reference; it serves callers that may not allocate device memory while
+ * running: a real-time visual-inertial estimator thread must not block on the
+ * device-wide synchronization of cudaMalloc/cudaFree or fail on an
+ * out-of-memory error mid-mission, and an application whose device memory is
+ * owned by another allocator's pool cannot have it fragmented by foreign
+ * cudaMalloc calls.  The caller passes device pointers for every input and
+ * for the output (*cost_out_device, one double).  Intermediates live in a
+ * fixed 512 KiB file-scope device array that each GPU loading the library
+ * keeps until the process exits; batches above 16,777,216 observations are
+ * rejected with MBA_ERR_INVALID_ARG.  All calls share that array, so calls
+ * that overlap on the GPU (other streams or threads) race; serialize them.
+ * The first call on a device looks up the array's device address with that
+ * device current; make that first call before any stream capture.  Runs on
+ * `stream` (a cudaStream_t, NULL = legacy default stream) and returns after
+ * the stream has finished the evaluation.  Out-of-range indices are skipped
+ * on the device and reported as MBA_ERR_OUT_OF_RANGE_INDEX; non-finite costs
+ * as MBA_ERR_NON_FINITE. */
+mba_status mba_visual_cost_noalloc(const mba_visual_batch_device* batch, int32_t device, void* stream,
+                                   double* cost_out_device);
+
 #ifdef __cplusplus
 }
 #endif

@@ -169,6 +169,31 @@ class ProblemStats(ctypes.Structure):
     ]
 
 
+class VisualBatchDevice(ctypes.Structure):
+    _fields_ = [
+        ("num_observations", ctypes.c_int64),
+        ("num_landmarks", ctypes.c_int64),
+        ("num_keyframes", ctypes.c_int64),
+        ("num_missions", ctypes.c_int64),
+        ("num_cameras", ctypes.c_int64),
+        ("obs_uv", ctypes.c_void_p),
+        ("obs_sigma", ctypes.c_void_p),
+        ("obs_landmark", ctypes.c_void_p),
+        ("obs_keyframe", ctypes.c_void_p),
+        ("obs_camera", ctypes.c_void_p),
+        ("lm_store_keyframe", ctypes.c_void_p),
+        ("lm_p_B", ctypes.c_void_p),
+        ("kf_q_IM_p_MI", ctypes.c_void_p),
+        ("kf_mission", ctypes.c_void_p),
+        ("mission_q_GM_p_GM", ctypes.c_void_p),
+        ("cameras", ctypes.c_void_p),
+        ("use_huber", ctypes.c_int32),
+        ("pad_", ctypes.c_int32),
+        ("huber_delta_local", ctypes.c_double),
+        ("huber_delta_global", ctypes.c_double),
+    ]
+
+
 class SynthConfig(ctypes.Structure):
     _fields_ = [
         ("seed", ctypes.c_uint64),
@@ -259,6 +284,8 @@ def load_ba():
     _declare(lib, "mba_cancel", None, [vp])
     _declare(lib, "mba_time_visual_kernel", ctypes.c_int, [vp, ctypes.c_int32, ctypes.c_int32, c_double_p])
     _declare(lib, "mba_get_stats", ctypes.c_int, [vp, ctypes.POINTER(ProblemStats)])
+    _declare(lib, "mba_visual_cost_noalloc", ctypes.c_int,
+             [ctypes.POINTER(VisualBatchDevice), ctypes.c_int32, vp, vp])
     return lib
 
 

@@ -46,7 +46,7 @@ def test_synth_library_exports_every_declared_symbol():
 STRUCTS = {
     "mba_camera": N.Camera, "mba_problem_desc": N.ProblemDesc, "mba_solver_options": N.SolverOptions,
     "mba_iteration_summary": N.IterationSummary, "mba_summary": N.Summary, "mba_problem_stats": N.ProblemStats,
-    "mba_synth_config": N.SynthConfig,
+    "mba_synth_config": N.SynthConfig, "mba_visual_batch_device": N.VisualBatchDevice,
 }
 
 
