@@ -97,14 +97,27 @@ __device__ __forceinline__ void m23xskew(const T* A, const T* v, T* C) {
 }
 
 // ---------------------------------------------------------------- camera
-struct DevCamera {
-  double intr[4];
-  double dist[4];
+template <typename S>
+struct DevCameraT {
+  S intr[4];
+  S dist[4];
   int32_t dtype;
   int32_t width, height, pad;
-  double q_CI[4];
-  double p_CI[3];
-  double pad2;
+  S q_CI[4];
+  S p_CI[3];
+  S pad2;
+};
+using DevCamera = DevCameraT<double>;
+
+template <typename T>
+struct Vec2;
+template <>
+struct Vec2<double> {
+  using type = double2;
+};
+template <>
+struct Vec2<float> {
+  using type = float2;
 };
 
 template <typename T>
@@ -183,8 +196,8 @@ __device__ __forceinline__ void distort(int dtype, const T* k, T* pt, T* J) {
 // term fails (visual-error-term-inl.h:159-166): POINT_BEHIND_CAMERA,
 // PROJECTION_INVALID (camera-pinhole-inl.h:47-65), depth < 0.05, or
 // |kp|^2 > 1e10.  KEYPOINT_OUTSIDE_IMAGE_BOX is not a failure.
-template <typename T>
-__device__ __forceinline__ bool project(const DevCamera& c, const T* p, T* kp, T* Jkp) {
+template <typename T, typename S>
+__device__ __forceinline__ bool project(const DevCameraT<S>& c, const T* p, T* kp, T* Jkp) {
   const T fu = T(c.intr[0]), fv = T(c.intr[1]), cu = T(c.intr[2]), cv = T(c.intr[3]);
   const T x = p[0], y = p[1], z = p[2];
   const T rz = T(1) / z;

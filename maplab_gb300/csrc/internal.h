@@ -41,6 +41,30 @@ struct DevProblem {
   const int64_t* imu_ts;
   const double* imu;        // [nsamp][6]
   double gyro_noise2, gyro_bias2, acc_noise2, acc_bias2, gravity;
+  // FP32 mirrors read by the FP32 evaluation kernel (no FP64 instruction in
+  // that kernel: GB300's FP64 pipe is narrow).  The state mirrors are
+  // refreshed whenever the FP64 state changes.
+  const float2* obs_uv_f;
+  const float* obs_sinv_f;
+  const float* obs_huber_f;
+  float* lm_p_f;            // [nlm][4]
+  float* kf_pose_f;         // [nkf][8] = q(4) p(3) pad
+  const float* mis_f;       // [nmis][8]
+  const DevCameraT<float>* cams_f;
+};
+
+// Typed view of the inputs of the evaluation kernel (FP64 arrays for the
+// FP64 kernel, the FP32 mirrors for the FP32 kernel).
+template <typename T>
+struct VisualInputs {
+  const typename Vec2<T>::type* uv;
+  const T* sinv;
+  const T* huber;
+  const T* lm_p;       // stride 4
+  const T* kf;         // pose q(4) p(3), stride kf_stride
+  int kf_stride;
+  const T* mis;        // stride 8
+  const DevCameraT<T>* cams;
 };
 
 template <typename T>

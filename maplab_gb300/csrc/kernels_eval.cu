@@ -57,13 +57,15 @@ __device__ __forceinline__ void load_q(const double* s, T* q) {
 // B = |q|^2 I for JplQuaternionParameterization and
 // B = -|q|^2 (R_I_M R_M_G)[:, 0:2] for JplRollPitchQuaternionParameterization
 // (quaternion-param-jpl.cc:144-164).  Masked tangent dims are zero columns.
-template <typename T>
-__device__ __forceinline__ void rot_basis(const DevProblem& P, int k, const T* q, const M3<T>& R_I_M, M3<T>& B) {
+template <typename T, typename S>
+__device__ __forceinline__ void rot_basis(const DevProblem& P, const S* mis, int k, const T* q, const M3<T>& R_I_M,
+                                          M3<T>& B) {
   const uint16_t m = P.kf_mask[k];
   const T n2 = q[0] * q[0] + q[1] * q[1] + q[2] * q[2] + q[3] * q[3];
   if (P.kf_flags[k] & MBA_KF_GAUGE_ROLL_PITCH) {
     T qg[4];
-    load_q(P.mis + 8 * P.kf_mis[k], qg);
+    const S* mq = mis + 8 * P.kf_mis[k];
+    qg[0] = T(mq[0]); qg[1] = T(mq[1]); qg[2] = T(mq[2]); qg[3] = T(mq[3]);
     M3<T> R_G_M;
     jplR(qg, R_G_M);
     // R_I_M * R_M_G = R_I_M * R_G_M^T
@@ -90,10 +92,13 @@ __device__ __forceinline__ void rot_basis(const DevProblem& P, int k, const T* q
 }
 
 // ------------------------------------------------------------------ visual
-// Tangent-space, Huber-corrected linearization of every observation.
-template <typename T>
-__global__ void __launch_bounds__(kBlock) k_visual_linearize(DevProblem P, VisualLin<T> out, double* cost_accum,
-                                                             const int* run_if, const int* skip_if) {
+// Tangent-space, Huber-corrected linearization of every observation.  kCost
+// adds the FP64 cost reduction (FP64 path only): the FP32 instantiation reads
+// the FP32 mirrors and executes no FP64 instruction.
+template <typename T, bool kCost>
+__global__ void __launch_bounds__(kBlock) k_visual_linearize(DevProblem P, VisualInputs<T> in, VisualLin<T> out,
+                                                             double* cost_accum, const int* run_if,
+                                                             const int* skip_if) {
   if (gated(run_if, skip_if)) return;
   const int64_t i = blockIdx.x * (int64_t)blockDim.x + threadIdx.x;
   double cost = 0.0;
@@ -103,45 +108,40 @@ __global__ void __launch_bounds__(kBlock) k_visual_linearize(DevProblem P, Visua
     const int kf = P.obs_kf[i];
     const int st = P.obs_store[i];
     const int type = P.obs_type[i];
-    const DevCamera& cam = P.cams[P.obs_cam[i]];
-    const double2 uv = P.obs_uv[i];
-    const T sinv = T(P.obs_sinv[i]);
-    const double ha = P.obs_huber[i];
-    const double2 l01 = *reinterpret_cast<const double2*>(P.lm_p + 4 * (int64_t)lm);
-    const double l2 = P.lm_p[4 * (int64_t)lm + 2];
-    const T pB[3] = {T(l01.x), T(l01.y), T(l2)};
-    T qCI[4] = {T(cam.q_CI[0]), T(cam.q_CI[1]), T(cam.q_CI[2]), T(cam.q_CI[3])};
+    const DevCameraT<T>& cam = in.cams[P.obs_cam[i]];
+    const auto uv = in.uv[i];
+    const T sinv = in.sinv[i];
+    const T ha = in.huber[i];
+    const T* lp = in.lm_p + 4 * (int64_t)lm;
+    const T pB[3] = {lp[0], lp[1], lp[2]};
     M3<T> RCI;
-    jplR(qCI, RCI);
+    jplR(cam.q_CI, RCI);
     T pI[3];
     M3<T> RIM, RBLM, RMG, RGLM;
     T qst[4], qob[4], pLMB[3], pMI[3];
     if (type == MBA_LOCAL_KEYFRAME) {
       pI[0] = pB[0]; pI[1] = pB[1]; pI[2] = pB[2];
     } else {
-      const double* xs = P.kf_state + 16 * (int64_t)st;
-      const double* xo = P.kf_state + 16 * (int64_t)kf;
-      load_q(xs, qst);
-      load_q(xo, qob);
-      pLMB[0] = T(xs[4]); pLMB[1] = T(xs[5]); pLMB[2] = T(xs[6]);
-      pMI[0] = T(xo[4]); pMI[1] = T(xo[5]); pMI[2] = T(xo[6]);
+      const T* xs = in.kf + (int64_t)in.kf_stride * st;
+      const T* xo = in.kf + (int64_t)in.kf_stride * kf;
+#pragma unroll
+      for (int a = 0; a < 4; ++a) { qst[a] = xs[a]; qob[a] = xo[a]; }
+      pLMB[0] = xs[4]; pLMB[1] = xs[5]; pLMB[2] = xs[6];
+      pMI[0] = xo[4]; pMI[1] = xo[5]; pMI[2] = xo[6];
       jplR(qst, RBLM);
       jplR(qob, RIM);
       T pM[3];
       mtv3(RBLM, pB, pM);  // R_LM_B p_B
       pM[0] += pLMB[0]; pM[1] += pLMB[1]; pM[2] += pLMB[2];
       if (type == MBA_GLOBAL) {
-        const double* ml = P.mis + 8 * P.kf_mis[st];
-        const double* mo = P.mis + 8 * P.kf_mis[kf];
-        T qgl[4], qgm[4];
-        load_q(ml, qgl);
-        load_q(mo, qgm);
-        jplR(qgl, RGLM);
+        const T* ml = in.mis + 8 * P.kf_mis[st];
+        const T* mo = in.mis + 8 * P.kf_mis[kf];
+        jplR(ml, RGLM);
         M3<T> RGM;
-        jplR(qgm, RGM);
+        jplR(mo, RGM);
         T pG[3];
         mv3(RGLM, pM, pG);
-        pG[0] += T(ml[4]) - T(mo[4]); pG[1] += T(ml[5]) - T(mo[5]); pG[2] += T(ml[6]) - T(mo[6]);
+        pG[0] += ml[4] - mo[4]; pG[1] += ml[5] - mo[5]; pG[2] += ml[6] - mo[6];
         mtv3(RGM, pG, pM);  // R_M_G (p_G - p_G_M)
 #pragma unroll
         for (int a = 0; a < 3; ++a)
@@ -153,7 +153,7 @@ __global__ void __launch_bounds__(kBlock) k_visual_linearize(DevProblem P, Visua
     }
     T pC[3];
     mv3(RCI, pI, pC);
-    pC[0] += T(cam.p_CI[0]); pC[1] += T(cam.p_CI[1]); pC[2] += T(cam.p_CI[2]);
+    pC[0] += cam.p_CI[0]; pC[1] += cam.p_CI[1]; pC[2] += cam.p_CI[2];
     T kp[2], Jkp[6];
     const bool failed = project<T>(cam, pC, kp, Jkp);
     T r[2], Jl[6], Js[12], Jo[12];
@@ -164,8 +164,8 @@ __global__ void __launch_bounds__(kBlock) k_visual_linearize(DevProblem P, Visua
 #pragma unroll
       for (int a = 0; a < 6; ++a) Jl[a] = T(0);
     } else {
-      r[0] = (kp[0] - T(uv.x)) * sinv;
-      r[1] = (kp[1] - T(uv.y)) * sinv;
+      r[0] = (kp[0] - uv.x) * sinv;
+      r[1] = (kp[1] - uv.y) * sinv;
       T A[6];
       m23x33(Jkp, RCI, A);  // Jkp * R_C_I
       if (type == MBA_LOCAL_KEYFRAME) {
@@ -193,8 +193,8 @@ __global__ void __launch_bounds__(kBlock) k_visual_linearize(DevProblem P, Visua
         m23xskew(JpB, pB, Jqs);  // -J_q_B_LM
         m23xskew(A, pI, Jqo);    // J_q_I_M
         M3<T> Bs, Bo;
-        rot_basis<T>(P, st, qst, RBLM, Bs);
-        rot_basis<T>(P, kf, qob, RIM, Bo);
+        rot_basis<T>(P, in.mis, st, qst, RBLM, Bs);
+        rot_basis<T>(P, in.mis, kf, qob, RIM, Bo);
         const uint16_t ms = P.kf_mask[st], mo = P.kf_mask[kf];
 #pragma unroll
         for (int rr = 0; rr < 2; ++rr) {
@@ -215,10 +215,10 @@ __global__ void __launch_bounds__(kBlock) k_visual_linearize(DevProblem P, Visua
       }
     }
     const T s = r[0] * r[0] + r[1] * r[1];
-    if (ha > 0.0) {
+    if (ha > T(0)) {
       T rho0, sq1, rs, as;
-      huber_corrector<T>(T(ha), s, &rho0, &sq1, &rs, &as);
-      cost = 0.5 * double(rho0);
+      huber_corrector<T>(ha, s, &rho0, &sq1, &rs, &as);
+      if (kCost) cost = 0.5 * double(rho0);
       // J' = sq1 (J - as r (r^T J)), r' = rs r
 #pragma unroll
       for (int c = 0; c < 3; ++c) {
@@ -237,7 +237,7 @@ __global__ void __launch_bounds__(kBlock) k_visual_linearize(DevProblem P, Visua
       }
       r[0] *= rs;
       r[1] *= rs;
-    } else {
+    } else if (kCost) {
       cost = 0.5 * double(s);
     }
     out.r[i] = r[0];
@@ -249,7 +249,7 @@ __global__ void __launch_bounds__(kBlock) k_visual_linearize(DevProblem P, Visua
 #pragma unroll
     for (int a = 0; a < 12; ++a) out.Jo[a * N + i] = Jo[a];
   }
-  if (cost_accum) block_accumulate(cost, cost_accum);
+  if (kCost) block_accumulate(cost, cost_accum);
 }
 
 // FP64 residual-only cost at an arbitrary state (candidate evaluation).
@@ -781,8 +781,8 @@ __global__ void __launch_bounds__(32 * kWarpsPerBlockI) k_inertial(DevProblem P,
     M3<double> Rf, Rt, Bf, Bt;
     jplR(qf, Rf);
     jplR(qt, Rt);
-    rot_basis<double>(P, f, qf, Rf, Bf);
-    rot_basis<double>(P, t, qt, Rt, Bt);
+    rot_basis<double>(P, P.mis, f, qf, Rf, Bf);
+    rot_basis<double>(P, P.mis, t, qt, Rt, Bt);
     const uint16_t mf = P.kf_mask[f], mt = P.kf_mask[t];
     const int src[15] = {0, 1, 2, 12, 13, 14, 6, 7, 8, 3, 4, 5, 9, 10, 11};
     for (int a = lane; a < 225; a += 32) {
@@ -850,11 +850,27 @@ cudaError_t launch_visual_ambient(const DevProblem& P, double* res, double* cons
 }
 
 template <typename T>
+VisualInputs<T> visual_inputs(const DevProblem& P) {
+  VisualInputs<T> in;
+  if constexpr (sizeof(T) == 8) {
+    in.uv = P.obs_uv; in.sinv = P.obs_sinv; in.huber = P.obs_huber; in.lm_p = P.lm_p;
+    in.kf = P.kf_state; in.kf_stride = 16; in.mis = P.mis; in.cams = P.cams;
+  } else {
+    in.uv = P.obs_uv_f; in.sinv = P.obs_sinv_f; in.huber = P.obs_huber_f; in.lm_p = P.lm_p_f;
+    in.kf = P.kf_pose_f; in.kf_stride = 8; in.mis = P.mis_f; in.cams = P.cams_f;
+  }
+  return in;
+}
+
+template <typename T>
 cudaError_t launch_visual_linearize_gated(const DevProblem& P, VisualLin<T> out, double* cost_accum, const int* run_if,
                                           const int* skip_if, cudaStream_t s) {
   if (P.nobs == 0) return cudaSuccess;
   const int64_t blocks = (P.nobs + kBlock - 1) / kBlock;
-  k_visual_linearize<T><<<(unsigned)blocks, kBlock, 0, s>>>(P, out, cost_accum, run_if, skip_if);
+  if (cost_accum)
+    k_visual_linearize<T, true><<<(unsigned)blocks, kBlock, 0, s>>>(P, visual_inputs<T>(P), out, cost_accum, run_if, skip_if);
+  else
+    k_visual_linearize<T, false><<<(unsigned)blocks, kBlock, 0, s>>>(P, visual_inputs<T>(P), out, nullptr, run_if, skip_if);
   return cudaGetLastError();
 }
 template <typename T>
@@ -927,13 +943,18 @@ __global__ void k_gather_visual(int64_t N, const int64_t* perm, VisualLin<T> v, 
   if (Jo) for (int c = 0; c < 12; ++c) Jo[12 * o + c] = (double)v.Jo[c * N + i];
 }
 
-__global__ void k_pack_state(int64_t NK, int64_t NL, double* kf_state, double* lm_p, const double* kx, const double* kv,
-                             const double* kbg, const double* kba, const double* lp, int to_device) {
+__global__ void k_pack_state(int64_t NK, int64_t NL, double* kf_state, double* lm_p, float* kf_pose_f, float* lm_p_f,
+                             const double* kx, const double* kv, const double* kbg, const double* kba, const double* lp,
+                             int to_device) {
   const int64_t i = blockIdx.x * (int64_t)blockDim.x + threadIdx.x;
   if (i < NK) {
     double* x = kf_state + 16 * i;
     if (to_device) {
-      if (kx) for (int a = 0; a < 7; ++a) x[a] = kx[7 * i + a];
+      if (kx)
+        for (int a = 0; a < 7; ++a) {
+          x[a] = kx[7 * i + a];
+          kf_pose_f[8 * i + a] = (float)kx[7 * i + a];
+        }
       for (int a = 0; a < 3; ++a) {
         if (kv) x[7 + a] = kv[3 * i + a];
         if (kbg) x[10 + a] = kbg[3 * i + a];
@@ -950,8 +971,12 @@ __global__ void k_pack_state(int64_t NK, int64_t NL, double* kf_state, double* l
   } else if (i < NK + NL && lp) {
     const int64_t l = i - NK;
     for (int a = 0; a < 3; ++a) {
-      if (to_device) lm_p[4 * l + a] = lp[3 * l + a];
-      else const_cast<double*>(lp)[3 * l + a] = lm_p[4 * l + a];
+      if (to_device) {
+        lm_p[4 * l + a] = lp[3 * l + a];
+        lm_p_f[4 * l + a] = (float)lp[3 * l + a];
+      } else {
+        const_cast<double*>(lp)[3 * l + a] = lm_p[4 * l + a];
+      }
     }
   }
 }
@@ -972,8 +997,8 @@ template cudaError_t launch_gather_visual<float>(const DevProblem&, VisualLin<fl
 cudaError_t launch_pack_state(const DevProblem& P, const double* kx, const double* kv, const double* kbg,
                               const double* kba, const double* lp, int to_device, cudaStream_t s) {
   const int64_t n = P.nkf + P.nlm;
-  k_pack_state<<<(unsigned)((n + 255) / 256), 256, 0, s>>>(P.nkf, P.nlm, P.kf_state, P.lm_p, kx, kv, kbg, kba, lp,
-                                                            to_device);
+  k_pack_state<<<(unsigned)((n + 255) / 256), 256, 0, s>>>(P.nkf, P.nlm, P.kf_state, P.lm_p, P.kf_pose_f, P.lm_p_f,
+                                                            kx, kv, kbg, kba, lp, to_device);
   return cudaGetLastError();
 }
 

@@ -417,10 +417,10 @@ __global__ void __launch_bounds__(64) k_block_jacobi(SolverLaunch<T> s) {
       L[i * (i + 1) / 2 + j] = v / ljj;
     }
   }
-  double* M = s.L.Minv + 225 * k;
+  T* M = s.L.Minv + 225 * k;
   if (fail) {
     atomicExch(&s.ctl->status, (int)MBA_ERR_NOT_SPD);
-    for (int a = 0; a < 225; ++a) M[a] = (a % 16 == 0) ? 1.0 : 0.0;
+    for (int a = 0; a < 225; ++a) M[a] = (a % 16 == 0) ? T(1) : T(0);
     return;
   }
   // Linv (lower) in place of a local 15x15, then M = Linv^T Linv.
@@ -435,8 +435,8 @@ __global__ void __launch_bounds__(64) k_block_jacobi(SolverLaunch<T> s) {
     for (int b = a; b < 15; ++b) {
       double v = 0.0;
       for (int q = b; q < 15; ++q) v += X[15 * q + a] * X[15 * q + b];
-      M[15 * a + b] = v;
-      M[15 * b + a] = v;
+      M[15 * a + b] = T(v);
+      M[15 * b + a] = T(v);
     }
 }
 
@@ -449,9 +449,9 @@ __global__ void __launch_bounds__(kB) k_pcg_init(SolverLaunch<T> s) {
   double rz = 0.0, rr = 0.0;
   if (i < n) {
     const int64_t k = i / 15, a = i % 15;
-    const double* M = s.L.Minv + 225 * k;
+    const T* M = s.L.Minv + 225 * k;
     double z = 0.0;
-    for (int b = 0; b < 15; ++b) z += M[15 * a + b] * (double)s.L.rhs[15 * k + b];
+    for (int b = 0; b < 15; ++b) z += (double)M[15 * a + b] * (double)s.L.rhs[15 * k + b];
     const double r = (double)s.L.rhs[i];
     s.L.x[i] = T(0);
     s.L.r[i] = T(r);
@@ -487,50 +487,59 @@ __global__ void __launch_bounds__(128) k_pcg_spmv(SolverLaunch<T> s, int it, con
     const double rzprev = (it == 1) ? ctl->pcg_rz0 : ctl->pcg_rz[(it + 1) % 3];
     beta = ctl->pcg_rz[(it - 1) % 3] / rzprev;
   }
+  const T tb = T(beta);
   const T* z = s.L.z;
   const int64_t k = (blockIdx.x * (int64_t)blockDim.x + threadIdx.x) >> 5;
   const int lane = threadIdx.x & 31;
+  const int w = threadIdx.x >> 5;
+  __shared__ T red[4][32];
   double pq = 0.0;
   if (k < s.P.nkf) {
-    double acc[6] = {0, 0, 0, 0, 0, 0};
-    for (int64_t e = s.S.row_off[k] + lane; e < s.S.row_off[k + 1]; e += 32) {
-      const int64_t j = s.S.row_col[e];
-      const T* B = s.L.SP + 36 * (int64_t)s.S.row_blk[e];
-      double pj[6];
+    // Pose-pose blocks of row k: 5 blocks per warp step, 6 lanes per block,
+    // lane r of a block owns output row r (6 contiguous values of the block).
+    T acc = T(0);
+    const int sub = lane / 6, r = lane - 6 * (lane / 6);
+    if (sub < 5) {
+      const int64_t e1 = s.S.row_off[k + 1];
+      for (int64_t e = s.S.row_off[k] + sub; e < e1; e += 5) {
+        const int64_t j = s.S.row_col[e];
+        const T* B = s.L.SP + 36 * (int64_t)s.S.row_blk[e] + 6 * r;
+        const T* zj = z + 15 * j;
+        const T* pj = pa + 15 * j;
 #pragma unroll
-      for (int c = 0; c < 6; ++c) pj[c] = (double)z[15 * j + c] + beta * (double)pa[15 * j + c];
-#pragma unroll
-      for (int r = 0; r < 6; ++r) {
-        T v = T(0);
-#pragma unroll
-        for (int c = 0; c < 6; ++c) v += B[6 * r + c] * T(pj[c]);
-        acc[r] += (double)v;
+        for (int c = 0; c < 6; ++c) acc += B[c] * (zj[c] + tb * pj[c]);
       }
     }
-#pragma unroll
-    for (int r = 0; r < 6; ++r) acc[r] = wsum(acc[r]);
+    red[w][lane] = acc;
+    __syncwarp();
     if (lane < 15) {
-      const T* D = s.L.SD + 225 * k;
-      double y = 0.0;
+      const T* D = s.L.SD + 225 * k + 15 * lane;
+      const T* zk = z + 15 * k;
+      const T* pk_old = pa + 15 * k;
+      T y = T(0);
 #pragma unroll
-      for (int c = 0; c < 15; ++c)
-        y += (double)(D[15 * lane + c] * T((double)z[15 * k + c] + beta * (double)pa[15 * k + c]));
-      if (lane < 6) y += acc[lane];
+      for (int c = 0; c < 15; ++c) y += D[c] * (zk[c] + tb * pk_old[c]);
+      if (lane < 6) y += red[w][lane] + red[w][lane + 6] + red[w][lane + 12] + red[w][lane + 18] + red[w][lane + 24];
       for (int64_t e = s.S.kfe_off[k]; e < s.S.kfe_off[k + 1]; ++e) {
         const int code = s.S.kfe[e];
         const bool from = code > 0;
         const int64_t ed = from ? code - 1 : -code - 1;
         const T* E = s.L.SE + 225 * ed;
         const int64_t o = from ? s.P.e_to[ed] : s.P.e_from[ed];
-        for (int c = 0; c < 15; ++c) {
-          const T pv = T((double)z[15 * o + c] + beta * (double)pa[15 * o + c]);
-          y += (double)((from ? E[15 * lane + c] : E[15 * c + lane]) * pv);
+        const T* zo = z + 15 * o;
+        const T* po = pa + 15 * o;
+        if (from) {
+#pragma unroll
+          for (int c = 0; c < 15; ++c) y += E[15 * lane + c] * (zo[c] + tb * po[c]);
+        } else {
+#pragma unroll
+          for (int c = 0; c < 15; ++c) y += E[15 * c + lane] * (zo[c] + tb * po[c]);
         }
       }
-      const double pk = (double)z[15 * k + lane] + beta * (double)pa[15 * k + lane];
-      pb[15 * k + lane] = T(pk);
-      s.L.q[15 * k + lane] = T(y);
-      pq = y * pk;
+      const T pk = zk[lane] + tb * pk_old[lane];
+      pb[15 * k + lane] = pk;
+      s.L.q[15 * k + lane] = y;
+      pq = (double)y * (double)pk;
     }
   }
   block_add(pq, &ctl->pcg_pq[it % 3]);
@@ -541,31 +550,31 @@ template <typename T>
 __global__ void __launch_bounds__(kB) k_pcg_update(SolverLaunch<T> s, int it, const T* p, int last) {
   LmControl* ctl = s.ctl;
   if (ctl->terminated || ctl->pcg_done || ctl->status) return;
-  __shared__ double rsh[kB];
+  __shared__ T rsh[kB];
   const int64_t k = (blockIdx.x * (int64_t)blockDim.x + threadIdx.x) >> 4;
   const int a = threadIdx.x & 15;
   const double rzprev = it == 0 ? ctl->pcg_rz0 : ctl->pcg_rz[(it + 2) % 3];
-  const double alpha = rzprev / ctl->pcg_pq[it % 3];
+  const T alpha = T(rzprev / ctl->pcg_pq[it % 3]);
   double rr = 0.0, rz = 0.0;
-  double rnew = 0.0;
+  T rnew = T(0);
   const bool act = (k < s.P.nkf) && a < 15;
   if (act) {
     const int64_t i = 15 * k + a;
-    s.L.x[i] = T((double)s.L.x[i] + alpha * (double)p[i]);
-    rnew = (double)s.L.r[i] - alpha * (double)s.L.q[i];
-    s.L.r[i] = T(rnew);
+    s.L.x[i] = s.L.x[i] + alpha * p[i];
+    rnew = s.L.r[i] - alpha * s.L.q[i];
+    s.L.r[i] = rnew;
   }
   rsh[threadIdx.x] = rnew;
   __syncthreads();
   if (act) {
-    const double* M = s.L.Minv + 225 * k;
+    const T* M = s.L.Minv + 225 * k + 15 * a;
     const int base = threadIdx.x & ~15;
-    double z = 0.0;
+    T z = T(0);
 #pragma unroll
-    for (int b = 0; b < 15; ++b) z += M[15 * a + b] * rsh[base + b];
-    s.L.z[15 * k + a] = T(z);
-    rr = rnew * rnew;
-    rz = rnew * z;
+    for (int b = 0; b < 15; ++b) z += M[b] * rsh[base + b];
+    s.L.z[15 * k + a] = z;
+    rr = (double)rnew * (double)rnew;
+    rz = (double)rnew * (double)z;
   }
   if (blockIdx.x == 0 && threadIdx.x == 0) {
     ctl->pcg_pq[(it + 1) % 3] = 0.0;
@@ -754,9 +763,15 @@ __global__ void __launch_bounds__(kB) k_accept(SolverLaunch<T> s, InertialLin<do
   const int64_t nk = 16 * s.P.nkf, nl = 4 * s.P.nlm, ne1 = 15 * s.P.nedge, ne2 = 225 * s.P.nedge;
   const int64_t total = nk + nl + ne1 + 2 * ne2;
   for (int64_t i = blockIdx.x * (int64_t)blockDim.x + threadIdx.x; i < total; i += (int64_t)gridDim.x * blockDim.x) {
-    if (i < nk) s.P.kf_state[i] = s.kf_cand[i];
-    else if (i < nk + nl) s.P.lm_p[i - nk] = s.lm_cand[i - nk];
-    else if (i < nk + nl + ne1) {
+    if (i < nk) {
+      const double v = s.kf_cand[i];
+      s.P.kf_state[i] = v;
+      if ((i & 15) < 7) s.P.kf_pose_f[8 * (i >> 4) + (i & 15)] = (float)v;  // FP32 mirror
+    } else if (i < nk + nl) {
+      const double v = s.lm_cand[i - nk];
+      s.P.lm_p[i - nk] = v;
+      s.P.lm_p_f[i - nk] = (float)v;
+    } else if (i < nk + nl + ne1) {
       const int64_t j = i - nk - nl;
       cur.r[j] = cand.r[j];
       s.ine.r[j] = T(cand.r[j]);

@@ -179,7 +179,7 @@ mba_status ensure_solver_buffers(mba_handle* h, SolverBuffers<T>& b) {
   L.rhs = A.alloc<T>(15 * NK);
   L.V = A.alloc<T>(9 * NL);
   L.U = A.alloc<T>(18 * NS);
-  L.Minv = A.alloc<double>(225 * NK);
+  L.Minv = A.alloc<T>(225 * NK);
   L.x = A.alloc<T>(15 * NK);
   L.r = A.alloc<T>(15 * NK);
   L.z = A.alloc<T>(15 * NK);
@@ -708,6 +708,37 @@ mba_status mba_create(const mba_problem_desc* d, int32_t device, mba_handle** ou
   P.e_off = A.upload(e_off, st);
   P.imu_ts = A.upload(ts, st);
   P.imu = A.upload(imu, st);
+  {
+    // FP32 mirrors for the FP32 evaluation kernel.
+    std::vector<float> uvf(2 * N), sinvf(N), hubf(N), lmf(4 * NL, 0.f), kff(8 * NK, 0.f), misf(8 * NM, 0.f);
+    for (int64_t a = 0; a < 2 * N; ++a) uvf[a] = (float)uv[a];
+    for (int64_t a = 0; a < N; ++a) { sinvf[a] = (float)sinv[a]; hubf[a] = (float)hub[a]; }
+    for (int64_t a = 0; a < 4 * NL; ++a) lmf[a] = (float)lm_p[a];
+    for (int64_t k = 0; k < NK; ++k) for (int a = 0; a < 7; ++a) kff[8 * k + a] = (float)kf_state[16 * k + a];
+    for (int64_t a = 0; a < 8 * NM; ++a) misf[a] = (float)mis[a];
+    std::vector<DevCameraT<float>> camf(NC);
+    for (int64_t c = 0; c < NC; ++c) {
+      DevCameraT<float>& o = camf[c];
+      std::memset(&o, 0, sizeof(o));
+      for (int a = 0; a < 4; ++a) {
+        o.intr[a] = (float)cams[c].intr[a];
+        o.dist[a] = (float)cams[c].dist[a];
+        o.q_CI[a] = (float)cams[c].q_CI[a];
+      }
+      for (int a = 0; a < 3; ++a) o.p_CI[a] = (float)cams[c].p_CI[a];
+      o.dtype = cams[c].dtype;
+      o.width = cams[c].width;
+      o.height = cams[c].height;
+    }
+    P.obs_uv_f = reinterpret_cast<const float2*>(A.upload(uvf, st));
+    P.obs_sinv_f = A.upload(sinvf, st);
+    P.obs_huber_f = A.upload(hubf, st);
+    P.lm_p_f = A.upload(lmf, st);
+    P.kf_pose_f = A.upload(kff, st);
+    P.mis_f = A.upload(misf, st);
+    P.cams_f = A.upload(camf, st);
+    if (cudaStreamSynchronize(st) != cudaSuccess) A.err = cudaErrorUnknown;  // host vectors die here
+  }
   P.gyro_noise2 = d->gyro_noise_sigma * d->gyro_noise_sigma;
   P.gyro_bias2 = d->gyro_bias_sigma * d->gyro_bias_sigma;
   P.acc_noise2 = d->acc_noise_sigma * d->acc_noise_sigma;

@@ -86,7 +86,7 @@ struct LinearSystem {
   T* rhs;    // [nkf*15]
   T* V;      // [9][nlm]
   T* U;      // [18][nslot]
-  double* Minv;  // [nkf][225]
+  T* Minv;       // [nkf][225] block-Jacobi inverses (factorized and inverted in FP64)
   T *x, *r, *z, *p, *q, *q2;  // [nkf*15]; p and q2 double-buffer the PCG direction
   double* dl;    // [3][nlm] scaled landmark step
 };
