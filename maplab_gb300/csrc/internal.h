@@ -41,6 +41,9 @@ struct DevProblem {
   const int64_t* imu_ts;
   const double* imu;        // [nsamp][6]
   double gyro_noise2, gyro_bias2, acc_noise2, acc_bias2, gravity;
+  // Inertial scratch: dt per step, end state per edge, RK4 stage inputs
+  // (15 values x 4 stages per step, FP64 or FP32).
+  double* ine_scratch;
   // FP32 mirrors read by the FP32 evaluation kernel (no FP64 instruction in
   // that kernel: GB300's FP64 pipe is narrow).  The state mirrors are
   // refreshed whenever the FP64 state changes.
@@ -98,13 +101,19 @@ cudaError_t launch_visual_linearize_gated(const DevProblem& P, VisualLin<T> out,
 cudaError_t launch_visual_cost_gated(const DevProblem& P, const double* kf_state, const double* lm_p,
                                      double* cost_accum, int* nonfinite, const int* skip_if, cudaStream_t s);
 cudaError_t launch_inertial_gated(const DevProblem& P, const double* kf_state, InertialLin<double> lin,
-                                  double* cost_accum, int* status, const int* skip_if, cudaStream_t s);
+                                  double* cost_accum, int* status, const int* skip_if, cudaStream_t s,
+                                  bool f32 = false);
 template <typename T>
 cudaError_t launch_gather_visual(const DevProblem& P, VisualLin<T> v, double* r, double* Jl, double* Js, double* Jo,
                                  cudaStream_t s);
 // to_device = 1: host-layout device arrays -> kf_state / lm_p; 0: the reverse.
 cudaError_t launch_pack_state(const DevProblem& P, const double* kx, const double* kv, const double* kbg,
                               const double* kba, const double* lp, int to_device, cudaStream_t s);
+// kernels_inertial.cu: f32_matrices selects FP32 propagation of Phi and Q
+// (mixed path); the state, Cholesky, residual and Jacobians stay FP64.
+cudaError_t launch_inertial_v2(const DevProblem& P, const double* kf_state, bool f32_matrices, InertialLin<double> lin,
+                               double* amb_res, double* const* amb_jac, double* cost_accum, int* status,
+                               const int* skip_if, cudaStream_t s);
 cudaError_t launch_inertial_f32(const DevProblem& P, const InertialLin<double>& src, InertialLin<float> dst,
                                 cudaStream_t s);
 

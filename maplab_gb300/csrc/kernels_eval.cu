@@ -1,6 +1,5 @@
 // Evaluation kernels: visual reprojection terms (one thread per observation,
-// SoA in/out) and inertial terms (one warp per IMU edge, RK4 preintegration in
-// shared memory).
+// SoA in/out); the inertial launchers route to kernels_inertial.cu.
 //
 // Visual: VisualReprojectionError::Evaluate
 //   (algorithms/ceres-error-terms/include/ceres-error-terms/visual-error-term-inl.h:12-379)
@@ -474,364 +473,6 @@ __global__ void __launch_bounds__(128) k_visual_ambient(DevProblem P, AmbientOut
   }
 }
 
-// ------------------------------------------------------------------ inertial
-constexpr int kWarpsPerBlockI = 2;
-
-struct InertialSmem {
-  double phiacc[225], Qacc[225], Pi[225], Ti[225], cd[225], td[225], sumcd[225], sumtd[225], tmp[225];
-  double s0[16], si[16], dk[16], sumd[16], nxt[16];
-  double F[27];  // F00, F60, F69 (row-major 3x3 each) of the current derivative evaluation
-};
-
-// getStateDerivativeRungeKutta (imu-integrator-inl.h:170-207), lane 0.
-__device__ void state_derivative(double g, const double* rd, const double* s, double* d) {
-  double q[4] = {s[0], s[1], s[2], s[3]};
-  normalize4(q);
-  M3<double> BRG;
-  jplR(q, BRG);
-  const double* w = rd + 3;
-  for (int a = 0; a < 16; ++a) d[a] = 0.0;
-  d[0] = 0.5 * (w[2] * q[1] - w[1] * q[2] + w[0] * q[3]);
-  d[1] = 0.5 * (-w[2] * q[0] + w[0] * q[2] + w[1] * q[3]);
-  d[2] = 0.5 * (w[1] * q[0] - w[0] * q[1] + w[2] * q[3]);
-  d[3] = 0.5 * (-w[0] * q[0] - w[1] * q[1] - w[2] * q[2]);
-  double a[3];
-  mtv3(BRG, rd, a);  // G_R_B * acc
-  d[7] = a[0]; d[8] = a[1]; d[9] = a[2] - g;
-  d[13] = s[7]; d[14] = s[8]; d[15] = s[9];
-}
-
-// phi_cont blocks (imu-integrator-inl.h:223-252) for state s, lane 0.
-__device__ void phi_cont_blocks(const double* rd, const double* s, double* F) {
-  double q[4] = {s[0], s[1], s[2], s[3]};
-  normalize4(q);
-  M3<double> BRG;
-  jplR(q, BRG);
-  const double* w = rd + 3;
-  const double* a = rd;
-  // F00 = -[w]x
-  F[0] = 0.0;   F[1] = w[2];  F[2] = -w[1];
-  F[3] = -w[2]; F[4] = 0.0;   F[5] = w[0];
-  F[6] = w[1];  F[7] = -w[0]; F[8] = 0.0;
-  // F69 = -G_R_B ; F60 = -G_R_B [a]x
-  for (int i = 0; i < 3; ++i)
-    for (int j = 0; j < 3; ++j) F[18 + 3 * i + j] = -BRG.m[3 * j + i];
-  const double ax[9] = {0.0, -a[2], a[1], a[2], 0.0, -a[0], -a[1], a[0], 0.0};
-  for (int i = 0; i < 3; ++i)
-    for (int j = 0; j < 3; ++j)
-      F[9 + 3 * i + j] = F[18 + 3 * i] * ax[j] + F[18 + 3 * i + 1] * ax[3 + j] + F[18 + 3 * i + 2] * ax[6 + j];
-}
-
-// getCovarianceTransitionDerivativesRungeKutta (imu-integrator-inl.h:209-296),
-// warp-cooperative.  Writes cd (225) and td (225; rows 3-5, 9-11 zero).
-__device__ void cov_trans_derivative(const DevProblem& P, InertialSmem& S, const double* Pm, const double* Tm,
-                                     int lane) {
-  const double* F = S.F;
-  // td and PC rows 0-2, 6-8, 12-14 (135 entries each); other rows zero.
-  for (int e = lane; e < 225; e += 32) { S.td[e] = 0.0; S.tmp[e] = 0.0; }
-  __syncwarp();
-  for (int e = lane; e < 135; e += 32) {
-    const int blk = e / 45, rr = (e % 45) / 15, c = e % 15;
-    double tv, pv;
-    if (blk == 0) {
-      tv = F[3 * rr] * Tm[c] + F[3 * rr + 1] * Tm[15 + c] + F[3 * rr + 2] * Tm[30 + c] - Tm[(3 + rr) * 15 + c];
-      pv = F[3 * rr] * Pm[c] + F[3 * rr + 1] * Pm[15 + c] + F[3 * rr + 2] * Pm[30 + c] - Pm[(3 + rr) * 15 + c];
-      S.td[rr * 15 + c] = tv;
-      S.tmp[rr * 15 + c] = pv;
-    } else if (blk == 1) {
-      tv = (F[9 + 3 * rr] * Tm[c] + F[9 + 3 * rr + 1] * Tm[15 + c] + F[9 + 3 * rr + 2] * Tm[30 + c]) +
-           (F[18 + 3 * rr] * Tm[135 + c] + F[18 + 3 * rr + 1] * Tm[150 + c] + F[18 + 3 * rr + 2] * Tm[165 + c]);
-      pv = (F[9 + 3 * rr] * Pm[c] + F[9 + 3 * rr + 1] * Pm[15 + c] + F[9 + 3 * rr + 2] * Pm[30 + c]) +
-           (F[18 + 3 * rr] * Pm[135 + c] + F[18 + 3 * rr + 1] * Pm[150 + c] + F[18 + 3 * rr + 2] * Pm[165 + c]);
-      S.td[(6 + rr) * 15 + c] = tv;
-      S.tmp[(6 + rr) * 15 + c] = pv;
-    } else {
-      S.td[(12 + rr) * 15 + c] = Tm[(6 + rr) * 15 + c];
-      S.tmp[(12 + rr) * 15 + c] = Pm[(6 + rr) * 15 + c];
-    }
-  }
-  __syncwarp();
-  for (int e = lane; e < 225; e += 32) {
-    const int rr = e / 15, c = e % 15;
-    double v = S.tmp[e] + S.tmp[c * 15 + rr];
-    if (rr == c) {
-      if (rr < 3) v += P.gyro_noise2;
-      else if (rr < 6) v += P.gyro_bias2;
-      else if (rr < 9) v += P.acc_noise2;
-      else if (rr < 12) v += P.acc_bias2;
-    }
-    S.cd[e] = v;
-  }
-  __syncwarp();
-}
-
-struct InertialAmb {
-  double* res;
-  double* J[8];
-};
-
-__global__ void __launch_bounds__(32 * kWarpsPerBlockI) k_inertial(DevProblem P, const double* kf_state,
-                                                                   InertialLin<double> lin, InertialAmb amb,
-                                                                   double* cost_accum, int* status,
-                                                                   const int* skip_if) {
-  if (gated(nullptr, skip_if)) return;
-  extern __shared__ __align__(16) unsigned char smem_raw[];
-  InertialSmem& S = reinterpret_cast<InertialSmem*>(smem_raw)[threadIdx.x >> 5];
-  const int lane = threadIdx.x & 31;
-  const int64_t e = blockIdx.x * (int64_t)kWarpsPerBlockI + (threadIdx.x >> 5);
-  if (e >= P.nedge) return;
-  const int f = P.e_from[e], t = P.e_to[e];
-  const int64_t o0 = P.e_off[e];
-  const int ns = (int)(P.e_off[e + 1] - o0);
-  const double* xf = kf_state + 16 * (int64_t)f;
-  const double* xt = kf_state + 16 * (int64_t)t;
-  // begin state in integrator layout: q(4) b_g(3) v(3) b_a(3) p(3)
-  if (lane == 0) {
-    for (int a = 0; a < 4; ++a) S.s0[a] = xf[a];
-    for (int a = 0; a < 3; ++a) {
-      S.s0[4 + a] = xf[10 + a];
-      S.s0[7 + a] = xf[7 + a];
-      S.s0[10 + a] = xf[13 + a];
-      S.s0[13 + a] = xf[4 + a];
-    }
-    for (int a = 0; a < 16; ++a) S.nxt[a] = S.s0[a];
-  }
-  for (int a = lane; a < 225; a += 32) {
-    S.Qacc[a] = 0.0;
-    S.phiacc[a] = (a % 16 == 0) ? 1.0 : 0.0;
-  }
-  __syncwarp();
-  bool unordered = false;
-  for (int k = 0; k + 1 < ns; ++k) {
-    const int64_t a0 = o0 + k;
-    const double dt = (double)(P.imu_ts[a0 + 1] - P.imu_ts[a0]) * 1e-9;
-    if (P.imu_ts[a0 + 1] < P.imu_ts[a0]) unordered = true;
-    // de-biased readings (inertial-error-term.cc:49-57)
-    double rd[12];
-    for (int a = 0; a < 3; ++a) {
-      rd[a] = P.imu[6 * a0 + a] - S.s0[10 + a];
-      rd[3 + a] = P.imu[6 * a0 + 3 + a] - S.s0[4 + a];
-      rd[6 + a] = P.imu[6 * (a0 + 1) + a] - S.s0[10 + a];
-      rd[9 + a] = P.imu[6 * (a0 + 1) + 3 + a] - S.s0[4 + a];
-    }
-    double r23[6];
-    if (dt < 2.220446049250313e-16) {
-      for (int a = 0; a < 6; ++a) r23[a] = rd[a];
-    } else {
-      for (int a = 0; a < 6; ++a) r23[a] = rd[a] + (rd[6 + a] - rd[a]) * ((0.5 * dt) / dt);
-    }
-    const double* rk[4] = {rd, r23, r23, rd + 6};
-    const double cst[4] = {0.5, 0.5, 1.0, 0.0};
-    const double wsum[4] = {1.0, 2.0, 2.0, 1.0};
-    // RK4 on the state and on (cov, transition), stage by stage.
-    for (int a = lane; a < 225; a += 32) {
-      S.Pi[a] = 0.0;
-      S.Ti[a] = (a % 16 == 0) ? 1.0 : 0.0;
-      S.sumcd[a] = 0.0;
-      S.sumtd[a] = 0.0;
-    }
-    if (lane == 0) {
-      for (int a = 0; a < 16; ++a) { S.si[a] = S.s0[a]; S.sumd[a] = 0.0; }
-    }
-    __syncwarp();
-    for (int stg = 0; stg < 4; ++stg) {
-      if (lane == 0) {
-        state_derivative(P.gravity, rk[stg], S.si, S.dk);
-        phi_cont_blocks(rk[stg], S.si, S.F);
-      }
-      __syncwarp();
-      cov_trans_derivative(P, S, S.Pi, S.Ti, lane);
-      // accumulate RK sums, form next intermediates
-      for (int a = lane; a < 225; a += 32) {
-        S.sumcd[a] += wsum[stg] * S.cd[a];
-        S.sumtd[a] += wsum[stg] * S.td[a];
-      }
-      __syncwarp();
-      if (stg < 3) {
-        for (int a = lane; a < 225; a += 32) {
-          S.Pi[a] = cst[stg] * dt * S.cd[a];
-          S.Ti[a] = ((a % 16 == 0) ? 1.0 : 0.0) + cst[stg] * dt * S.td[a];
-        }
-      }
-      if (lane == 0) {
-        for (int a = 0; a < 16; ++a) {
-          S.sumd[a] += wsum[stg] * S.dk[a];
-          if (stg < 3) S.si[a] = S.s0[a] + cst[stg] * dt * S.dk[a];
-        }
-      }
-      __syncwarp();
-    }
-    // next state, per-step phi (in sumtd) and Q (in sumcd)
-    if (lane == 0) {
-      for (int a = 0; a < 16; ++a) S.nxt[a] = S.s0[a] + dt * S.sumd[a] / 6.0;
-    }
-    for (int a = lane; a < 225; a += 32) {
-      const int rr = a / 15;
-      const bool upd = (rr < 3) || (rr >= 6 && rr < 9) || (rr >= 12);
-      S.sumcd[a] = dt * S.sumcd[a] / 6.0;
-      S.sumtd[a] = ((a % 16 == 0) ? 1.0 : 0.0) + (upd ? dt * S.sumtd[a] / 6.0 : 0.0);
-    }
-    __syncwarp();
-    // Q_acc = phi Q_acc phi^T + Q ; phi_acc = phi phi_acc
-    for (int a = lane; a < 225; a += 32) {
-      const int rr = a / 15, c = a % 15;
-      double v = 0.0;
-      for (int m = 0; m < 15; ++m) v += S.sumtd[rr * 15 + m] * S.Qacc[m * 15 + c];
-      S.tmp[a] = v;
-    }
-    __syncwarp();
-    for (int a = lane; a < 225; a += 32) {
-      const int rr = a / 15, c = a % 15;
-      double v = 0.0;
-      for (int m = 0; m < 15; ++m) v += S.tmp[rr * 15 + m] * S.sumtd[c * 15 + m];
-      S.Pi[a] = v + S.sumcd[a];
-    }
-    __syncwarp();
-    for (int a = lane; a < 225; a += 32) {
-      const int rr = a / 15, c = a % 15;
-      double v = 0.0;
-      for (int m = 0; m < 15; ++m) v += S.sumtd[rr * 15 + m] * S.phiacc[m * 15 + c];
-      S.tmp[a] = v;
-    }
-    __syncwarp();
-    for (int a = lane; a < 225; a += 32) {
-      S.Qacc[a] = S.Pi[a];
-      S.phiacc[a] = S.tmp[a];
-    }
-    if (lane == 0) for (int a = 0; a < 16; ++a) S.s0[a] = S.nxt[a];
-    __syncwarp();
-  }
-  // Cholesky of Q_acc (lane 0) into Ti (lower), then L^-1 into Pi.
-  __shared__ int spd_fail[kWarpsPerBlockI];
-  if (lane == 0) {
-    int fail = 0;
-    double* L = S.Ti;
-    for (int a = 0; a < 225; ++a) L[a] = 0.0;
-    for (int j = 0; j < 15 && !fail; ++j) {
-      double d = S.Qacc[j * 15 + j];
-      for (int k = 0; k < j; ++k) d -= L[j * 15 + k] * L[j * 15 + k];
-      if (!(d > 0.0)) { fail = 1; break; }
-      const double ljj = sqrt(d);
-      L[j * 15 + j] = ljj;
-      for (int i = j + 1; i < 15; ++i) {
-        double s = S.Qacc[i * 15 + j];
-        for (int k = 0; k < j; ++k) s -= L[i * 15 + k] * L[j * 15 + k];
-        L[i * 15 + j] = s / ljj;
-      }
-    }
-    spd_fail[threadIdx.x >> 5] = fail;
-  }
-  __syncwarp();
-  const int fail = spd_fail[threadIdx.x >> 5];
-  if (fail || unordered) {
-    if (lane == 0 && status) atomicMax(status, unordered ? (int)MBA_ERR_UNORDERED_IMU : (int)MBA_ERR_NOT_SPD);
-    return;
-  }
-  // Linv column c by forward substitution (lanes 0..14).
-  if (lane < 15) {
-    const double* L = S.Ti;
-    double* X = S.Pi;
-    for (int i = 0; i < 15; ++i) {
-      double s = (i == lane) ? 1.0 : 0.0;
-      for (int k = 0; k < i; ++k) s -= L[i * 15 + k] * X[k * 15 + lane];
-      X[i * 15 + lane] = s / L[i * 15 + i];
-    }
-  }
-  __syncwarp();
-  // M = Linv * phi_acc  (into tmp)
-  for (int a = lane; a < 225; a += 32) {
-    const int rr = a / 15, c = a % 15;
-    double v = 0.0;
-    for (int m = 0; m <= rr; ++m) v += S.Pi[rr * 15 + m] * S.phiacc[m * 15 + c];
-    S.tmp[a] = v;
-  }
-  // raw residual (lane 0) into sumd[0..14]
-  if (lane == 0) {
-    const double* qi = S.s0;  // end state
-    const double n2 = qi[0] * qi[0] + qi[1] * qi[1] + qi[2] * qi[2] + qi[3] * qi[3];
-    double qinv[4] = {0, 0, 0, 0};
-    if (n2 > 0.0) { qinv[0] = -qi[0] / n2; qinv[1] = -qi[1] / n2; qinv[2] = -qi[2] / n2; qinv[3] = qi[3] / n2; }
-    double dq[4];
-    qprod_pos(xt, qinv, dq);
-    double* rr = S.sumd;
-    rr[0] = 2.0 * dq[0]; rr[1] = 2.0 * dq[1]; rr[2] = 2.0 * dq[2];
-    for (int a = 0; a < 3; ++a) {
-      rr[3 + a] = xt[10 + a] - S.s0[4 + a];   // b_g
-      rr[6 + a] = xt[7 + a] - S.s0[7 + a];    // v
-      rr[9 + a] = xt[13 + a] - S.s0[10 + a];  // b_a
-      rr[12 + a] = xt[4 + a] - S.s0[13 + a];  // p
-    }
-  }
-  __syncwarp();
-  // whitened residual r = Linv * r_raw (lanes 0..14) into dk
-  double rw = 0.0;
-  if (lane < 15) {
-    for (int m = 0; m <= lane; ++m) rw += S.Pi[lane * 15 + m] * S.sumd[m];
-    S.dk[lane] = rw;
-  }
-  const double sq = warp_sum(lane < 15 ? rw * rw : 0.0);
-  if (lane == 0 && cost_accum) atomicAdd(cost_accum, 0.5 * sq);
-  __syncwarp();
-  // Tangent outputs: KF order theta(0-2) p(3-5) v(6-8) b_g(9-11) b_a(12-14);
-  // error-state order theta(0-2) b_g(3-5) v(6-8) b_a(9-11) p(12-14).
-  if (lin.r) {
-    if (lane < 15) lin.r[15 * e + lane] = S.dk[lane];
-    // rotation bases
-    double qf[4] = {xf[0], xf[1], xf[2], xf[3]}, qt[4] = {xt[0], xt[1], xt[2], xt[3]};
-    M3<double> Rf, Rt, Bf, Bt;
-    jplR(qf, Rf);
-    jplR(qt, Rt);
-    rot_basis<double>(P, P.mis, f, qf, Rf, Bf);
-    rot_basis<double>(P, P.mis, t, qt, Rt, Bt);
-    const uint16_t mf = P.kf_mask[f], mt = P.kf_mask[t];
-    const int src[15] = {0, 1, 2, 12, 13, 14, 6, 7, 8, 3, 4, 5, 9, 10, 11};
-    for (int a = lane; a < 225; a += 32) {
-      const int rr = a / 15, c = a % 15;
-      double vf, vt;
-      if (c < 3) {
-        vf = -(S.tmp[rr * 15 + 0] * Bf.m[c] + S.tmp[rr * 15 + 1] * Bf.m[3 + c] + S.tmp[rr * 15 + 2] * Bf.m[6 + c]);
-        vt = S.Pi[rr * 15 + 0] * Bt.m[c] + S.Pi[rr * 15 + 1] * Bt.m[3 + c] + S.Pi[rr * 15 + 2] * Bt.m[6 + c];
-      } else {
-        vf = (mf & (1u << c)) ? -S.tmp[rr * 15 + src[c]] : 0.0;
-        vt = (mt & (1u << c)) ? S.Pi[rr * 15 + src[c]] : 0.0;
-      }
-      lin.Jf[225 * e + a] = vf;
-      lin.Jt[225 * e + a] = vt;
-    }
-  }
-  if (amb.res && lane < 15) amb.res[15 * e + lane] = S.dk[lane];
-  // Ambient blocks (inertial-error-term.cc:188-283).
-  if (amb.J[0] || amb.J[4]) {
-    double Jqf[12], Jqt[12];
-    dqdtheta(xf, Jqf);
-    dqdtheta(xt, Jqt);
-    for (int a = lane; a < 105; a += 32) {
-      const int rr = a / 7, c = a % 7;
-      if (amb.J[0]) {
-        double v;
-        if (c < 4) v = -4.0 * (S.tmp[rr * 15] * Jqf[3 * c] + S.tmp[rr * 15 + 1] * Jqf[3 * c + 1] + S.tmp[rr * 15 + 2] * Jqf[3 * c + 2]);
-        else v = -S.tmp[rr * 15 + 12 + (c - 4)];
-        amb.J[0][105 * e + a] = v;
-      }
-      if (amb.J[4]) {
-        double v;
-        if (c < 4) v = 4.0 * (S.Pi[rr * 15] * Jqt[3 * c] + S.Pi[rr * 15 + 1] * Jqt[3 * c + 1] + S.Pi[rr * 15 + 2] * Jqt[3 * c + 2]);
-        else v = S.Pi[rr * 15 + 12 + (c - 4)];
-        amb.J[4][105 * e + a] = v;
-      }
-    }
-  }
-  for (int b = 0; b < 3; ++b) {
-    // b_g (err cols 3-5), v (6-8), b_a (9-11)
-    const int col0 = (b == 0) ? 3 : (b == 1 ? 6 : 9);
-    for (int a = lane; a < 45; a += 32) {
-      const int rr = a / 3, c = a % 3;
-      if (amb.J[1 + b]) amb.J[1 + b][45 * e + a] = -S.tmp[rr * 15 + col0 + c];
-      if (amb.J[5 + b]) amb.J[5 + b][45 * e + a] = S.Pi[rr * 15 + col0 + c];
-    }
-  }
-}
-
 __global__ void k_convert_f32(const double* a, float* b, int64_t n) {
   const int64_t i = blockIdx.x * (int64_t)blockDim.x + threadIdx.x;
   if (i < n) b[i] = (float)a[i];
@@ -898,26 +539,16 @@ cudaError_t launch_visual_cost(const DevProblem& P, const double* kf_state, cons
 
 static cudaError_t launch_inertial_impl(const DevProblem& P, const double* kf_state, InertialLin<double> lin,
                                         double* amb_res, double* const* amb_jac, double* cost_accum, int* status,
-                                        const int* skip_if, cudaStream_t s) {
-  if (P.nedge == 0) return cudaSuccess;
-  // 2 x 17 KB of shared memory per block: below the 48 KB default, so no
-  // attribute call is needed (none may happen inside graph capture).
-  const size_t smem = sizeof(InertialSmem) * kWarpsPerBlockI;
-  static_assert(sizeof(InertialSmem) * kWarpsPerBlockI <= 48 * 1024, "inertial smem above the default limit");
-  InertialAmb amb;
-  amb.res = amb_res;
-  for (int b = 0; b < 8; ++b) amb.J[b] = amb_jac ? amb_jac[b] : nullptr;
-  const int64_t blocks = (P.nedge + kWarpsPerBlockI - 1) / kWarpsPerBlockI;
-  k_inertial<<<(unsigned)blocks, 32 * kWarpsPerBlockI, smem, s>>>(P, kf_state, lin, amb, cost_accum, status, skip_if);
-  return cudaGetLastError();
+                                        const int* skip_if, cudaStream_t s, bool f32 = false) {
+  return launch_inertial_v2(P, kf_state, f32, lin, amb_res, amb_jac, cost_accum, status, skip_if, s);
 }
 cudaError_t launch_inertial(const DevProblem& P, const double* kf_state, InertialLin<double> lin, double* amb_res,
                             double* const* amb_jac, double* cost_accum, int* status, cudaStream_t s) {
   return launch_inertial_impl(P, kf_state, lin, amb_res, amb_jac, cost_accum, status, nullptr, s);
 }
 cudaError_t launch_inertial_gated(const DevProblem& P, const double* kf_state, InertialLin<double> lin,
-                                  double* cost_accum, int* status, const int* skip_if, cudaStream_t s) {
-  return launch_inertial_impl(P, kf_state, lin, nullptr, nullptr, cost_accum, status, skip_if, s);
+                                  double* cost_accum, int* status, const int* skip_if, cudaStream_t s, bool f32) {
+  return launch_inertial_impl(P, kf_state, lin, nullptr, nullptr, cost_accum, status, skip_if, s, f32);
 }
 
 cudaError_t launch_inertial_f32(const DevProblem& P, const InertialLin<double>& src, InertialLin<float> dst,

@@ -867,8 +867,9 @@ cudaError_t solver_evaluate_candidate(const SolverLaunch<T>& s, InertialLin<doub
   cudaError_t e = launch_visual_cost_gated(s.P, s.kf_cand, s.lm_cand, &s.ctl->cost_cand, &s.ctl->nonfinite,
                                            &s.ctl->terminated, st);
   if (e != cudaSuccess) return e;
+  // Mixed path: Phi / Q propagated in FP32 (state, Cholesky, residual FP64).
   return launch_inertial_gated(s.P, s.kf_cand, ine_cand, &s.ctl->cost_cand, &s.ctl->inertial_status,
-                               &s.ctl->terminated, st);
+                               &s.ctl->terminated, st, sizeof(T) == 4);
 }
 
 template <typename T>

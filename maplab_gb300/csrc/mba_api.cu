@@ -284,7 +284,9 @@ mba_status run_solve(mba_handle* h, const mba_solver_options& o, mba_summary* su
   if (e == cudaSuccess) e = cudaMemsetAsync(&h->ctl->cost, 0, sizeof(double), st);
   if (e == cudaSuccess) e = cudaMemsetAsync(h->iscratch, 0, 2 * sizeof(int), st);
   if (e == cudaSuccess) e = launch_visual_cost(h->P, h->P.kf_state, h->P.lm_p, &h->ctl->cost, h->iscratch, st);
-  if (e == cudaSuccess) e = launch_inertial(h->P, h->P.kf_state, h->ine_cur, nullptr, nullptr, &h->ctl->cost, h->iscratch + 1, st);
+  if (e == cudaSuccess)
+    e = launch_inertial_gated(h->P, h->P.kf_state, h->ine_cur, &h->ctl->cost, h->iscratch + 1, nullptr, st,
+                              sizeof(T) == 4);
   if constexpr (sizeof(T) == 4) {
     if (e == cudaSuccess) e = launch_inertial_f32(h->P, h->ine_cur, b.ine, st);
   } else {
@@ -763,6 +765,9 @@ mba_status mba_create(const mba_problem_desc* d, int32_t device, mba_handle** ou
   S.row_blk = A.upload(row_blk, st);
   S.kfe_off = A.upload(kfe_off, st);
   S.kfe = A.upload(kfe, st);
+  // Inertial scratch (kernels_inertial.cu): dt per step, end state per edge,
+  // 4 RK4 stages x 15 values per step.
+  P.ine_scratch = A.alloc<double>((NSMP - NE) + 16 * NE + 60 * (NSMP - NE) + 1);
   h->scratch = A.alloc<double>(4);
   h->iscratch = A.alloc<int>(4);
   if (A.err != cudaSuccess || cudaStreamSynchronize(st) != cudaSuccess) {
