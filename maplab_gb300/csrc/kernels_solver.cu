@@ -182,7 +182,8 @@ __global__ void __launch_bounds__(128) k_assemble_inertial(DevProblem P, Inertia
   }
 }
 
-// Jacobi scaling from the unscaled diagonal of J^T J.
+// Jacobi scaling from the unscaled diagonal of J^T J (first linearization
+// only); FP64 and T copies of the scale vectors.
 template <typename T>
 __global__ void k_scale(DevProblem P, LinearSystem<T> L, ScaleVectors sc, int jacobi) {
   const int64_t i = blockIdx.x * (int64_t)blockDim.x + threadIdx.x;
@@ -191,27 +192,66 @@ __global__ void k_scale(DevProblem P, LinearSystem<T> L, ScaleVectors sc, int ja
     const int64_t k = i / 15, d = i % 15;
     const double h = (double)L.Dbase[225 * k + 16 * d];
     sc.skf[i] = jacobi ? 1.0 / (1.0 + sqrt(h > 0.0 ? h : 0.0)) : 1.0;
+    L.skf[i] = T(sc.skf[i]);
   } else if (i < nk + nl) {
     const int64_t j = i - nk, a = j / P.nlm, l = j % P.nlm;
     const double h = (double)L.Hll[(4 * a) * P.nlm + l];
     sc.slm[j] = jacobi ? 1.0 / (1.0 + sqrt(h > 0.0 ? h : 0.0)) : 1.0;
+    L.slm[j] = T(sc.slm[j]);
   }
 }
 
-__device__ __forceinline__ double lm_damp(double s, double h, const LmParams& prm, double radius) {
-  double d = s * s * h;
-  d = d < prm.min_lm_diagonal ? prm.min_lm_diagonal : (d > prm.max_lm_diagonal ? prm.max_lm_diagonal : d);
+// Applies the Jacobi scaling in place to the assembled normal equations:
+// H_ll, g_l, W slots, D, P, E blocks and g_c (J s instead of J).
+template <typename T>
+__global__ void __launch_bounds__(kB) k_scale_inplace(DevProblem P, SchurPattern S, LinearSystem<T> L,
+                                                      const int* run_if, const int* skip_if) {
+  if (gated(run_if, skip_if)) return;
+  const int64_t NL = P.nlm, NS = S.nslot, NK = P.nkf, NE = P.nedge, NPU = S.npu;
+  const int64_t n1 = 9 * NL, n2 = n1 + 3 * NL, n3 = n2 + 18 * NS, n4 = n3 + 225 * NK, n5 = n4 + 36 * NPU,
+                n6 = n5 + 225 * NE, n7 = n6 + 15 * NK;
+  for (int64_t i = blockIdx.x * (int64_t)blockDim.x + threadIdx.x; i < n7; i += (int64_t)gridDim.x * blockDim.x) {
+    if (i < n1) {
+      const int64_t q = i / NL, l = i % NL;
+      L.Hll[i] *= L.slm[(q / 3) * NL + l] * L.slm[(q % 3) * NL + l];
+    } else if (i < n2) {
+      const int64_t j = i - n1, l = j % NL;
+      L.gl[j] *= L.slm[j];
+      (void)l;
+    } else if (i < n3) {
+      const int64_t j = i - n2, q = j / NS, sl = j % NS;
+      L.Wslot[j] *= L.slm[(q / 6) * NL + S.slot_lm[sl]] * L.skf[15 * (int64_t)S.slot_kf[sl] + q % 6];
+    } else if (i < n4) {
+      const int64_t j = i - n3, k = j / 225, e = j % 225;
+      L.Dbase[j] *= L.skf[15 * k + e / 15] * L.skf[15 * k + e % 15];
+    } else if (i < n5) {
+      const int64_t j = i - n4, b = j / 36, e = j % 36;
+      L.Pbase[j] *= L.skf[15 * (int64_t)S.pu_i[b] + e / 6] * L.skf[15 * (int64_t)S.pu_j[b] + e % 6];
+    } else if (i < n6) {
+      const int64_t j = i - n5, ed = j / 225, e = j % 225;
+      L.Ebase[j] *= L.skf[15 * (int64_t)P.e_from[ed] + e / 15] * L.skf[15 * (int64_t)P.e_to[ed] + e % 15];
+    } else {
+      const int64_t j = i - n6;
+      L.gc[j] *= L.skf[j];
+    }
+  }
+}
+
+template <typename T>
+__device__ __forceinline__ T lm_damp_t(T h, T mn, T mx, T radius) {
+  T d = h < mn ? mn : (h > mx ? mx : h);
   return d / radius;
 }
 
-// Scaled, damped keyframe system: SD, SE, SP (upper), rhs = -s g.
+// Damped keyframe system from the scaled blocks: SD = D + diag, SE, SP, rhs = -g.
 template <typename T>
 __global__ void __launch_bounds__(kB) k_build_system(SolverLaunch<T> s) {
   LmControl* ctl = s.ctl;
   if (ctl->terminated) return;
   const int64_t nkf = s.P.nkf, ne = s.P.nedge, npu = s.S.npu;
   const int64_t n1 = nkf * 225, n2 = n1 + ne * 225, n3 = n2 + npu * 36, n4 = n3 + nkf * 15;
-  const double radius = ctl->radius;
+  const T radius = T(ctl->radius);
+  const T mn = T(s.prm.min_lm_diagonal), mx = T(s.prm.max_lm_diagonal);
   const int64_t tid = blockIdx.x * (int64_t)blockDim.x + threadIdx.x;
   if (tid == 0) {
     ctl->accepted = 0;
@@ -230,139 +270,161 @@ __global__ void __launch_bounds__(kB) k_build_system(SolverLaunch<T> s) {
   }
   for (int64_t i = tid; i < n4; i += (int64_t)gridDim.x * blockDim.x) {
     if (i < n1) {
-      const int64_t k = i / 225, e = i % 225, a = e / 15, b = e % 15;
-      const double sa = s.sc.skf[15 * k + a], sb = s.sc.skf[15 * k + b];
-      const double h = (double)s.L.Dbase[i];
-      double v = sa * h * sb;
-      if (a == b) v += lm_damp(sa, h, s.prm, radius);
-      s.L.SD[i] = T(v);
+      const int64_t e = i % 225, a = e / 15, b = e % 15;
+      const T h = s.L.Dbase[i];
+      s.L.SD[i] = (a == b) ? h + lm_damp_t(h, mn, mx, radius) : h;
     } else if (i < n2) {
-      const int64_t j = i - n1, e = j / 225, q = j % 225, a = q / 15, b = q % 15;
-      s.L.SE[j] = T(s.sc.skf[15 * (int64_t)s.P.e_from[e] + a] * (double)s.L.Ebase[j] * s.sc.skf[15 * (int64_t)s.P.e_to[e] + b]);
+      s.L.SE[i - n1] = s.L.Ebase[i - n1];
     } else if (i < n3) {
-      const int64_t j = i - n2, b = j / 36, q = j % 36, a = q / 6, c = q % 6;
-      s.L.SP[j] = T(s.sc.skf[15 * (int64_t)s.S.pu_i[b] + a] * (double)s.L.Pbase[j] * s.sc.skf[15 * (int64_t)s.S.pu_j[b] + c]);
+      s.L.SP[i - n2] = s.L.Pbase[i - n2];
     } else {
-      const int64_t j = i - n3;
-      s.L.rhs[j] = T(-s.sc.skf[j] * (double)s.L.gc[j]);
+      s.L.rhs[i - n3] = -s.L.gc[i - n3];
     }
   }
 }
 
-__device__ bool inv3d(const double* A, double* B) {
-  const double det = A[0] * (A[4] * A[8] - A[5] * A[7]) - A[1] * (A[3] * A[8] - A[5] * A[6]) +
-                     A[2] * (A[3] * A[7] - A[4] * A[6]);
-  if (!(fabs(det) > 0.0) || !isfinite(det)) return false;
-  const double id = 1.0 / det;
-  B[0] = (A[4] * A[8] - A[5] * A[7]) * id; B[1] = (A[2] * A[7] - A[1] * A[8]) * id; B[2] = (A[1] * A[5] - A[2] * A[4]) * id;
-  B[3] = (A[5] * A[6] - A[3] * A[8]) * id; B[4] = (A[0] * A[8] - A[2] * A[6]) * id; B[5] = (A[2] * A[3] - A[0] * A[5]) * id;
-  B[6] = (A[3] * A[7] - A[4] * A[6]) * id; B[7] = (A[1] * A[6] - A[0] * A[7]) * id; B[8] = (A[0] * A[4] - A[1] * A[3]) * id;
+template <typename T>
+__device__ __forceinline__ bool inv3t(const T* A, T* B) {
+  const T c0 = A[4] * A[8] - A[5] * A[7], c1 = A[5] * A[6] - A[3] * A[8], c2 = A[3] * A[7] - A[4] * A[6];
+  const T det = A[0] * c0 + A[1] * c1 + A[2] * c2;
+  if (!(det != T(0)) || !isfinite((double)det)) return false;
+  const T id = T(1) / det;
+  B[0] = c0 * id; B[1] = (A[2] * A[7] - A[1] * A[8]) * id; B[2] = (A[1] * A[5] - A[2] * A[4]) * id;
+  B[3] = c1 * id; B[4] = (A[0] * A[8] - A[2] * A[6]) * id; B[5] = (A[2] * A[3] - A[0] * A[5]) * id;
+  B[6] = c2 * id; B[7] = (A[1] * A[6] - A[0] * A[7]) * id; B[8] = (A[0] * A[4] - A[1] * A[3]) * id;
   return true;
 }
 
-// Landmark elimination, part 1: V = (s H s + D)^-1 and rhs += W^T V g.
+// Landmark elimination, part 1: V = (H + D)^-1 and rhs += W^T V g (scaled blocks).
 template <typename T>
 __global__ void __launch_bounds__(kB) k_schur_lm(SolverLaunch<T> s) {
   if (s.ctl->terminated) return;
   const int64_t l = blockIdx.x * (int64_t)blockDim.x + threadIdx.x;
   const int64_t NL = s.P.nlm, NS = s.S.nslot;
   if (l >= NL) return;
-  double V[9] = {0, 0, 0, 0, 0, 0, 0, 0, 0};
+  T V[9] = {T(0), T(0), T(0), T(0), T(0), T(0), T(0), T(0), T(0)};
   if (s.P.lm_active[l]) {
-    const double radius = s.ctl->radius;
-    double sl[3], Hs[9];
-    for (int a = 0; a < 3; ++a) sl[a] = s.sc.slm[a * NL + l];
-    for (int a = 0; a < 3; ++a)
-      for (int b = 0; b < 3; ++b) Hs[3 * a + b] = sl[a] * (double)s.L.Hll[(3 * a + b) * NL + l] * sl[b];
-    for (int a = 0; a < 3; ++a) Hs[4 * a] += lm_damp(sl[a], (double)s.L.Hll[(4 * a) * NL + l], s.prm, radius);
-    if (!inv3d(Hs, V)) {
+    const T radius = T(s.ctl->radius), mn = T(s.prm.min_lm_diagonal), mx = T(s.prm.max_lm_diagonal);
+    // The 3x3 inverse runs in FP64 in both paths: poorly constrained landmarks
+    // (short baselines) make these blocks ill-conditioned.
+    double Hs[9], Vd[9];
+#pragma unroll
+    for (int a = 0; a < 9; ++a) Hs[a] = (double)s.L.Hll[a * NL + l];
+#pragma unroll
+    for (int a = 0; a < 3; ++a) Hs[4 * a] += (double)lm_damp_t(T(Hs[4 * a]), mn, mx, radius);
+    if (!inv3t(Hs, Vd)) {
       atomicExch(&s.ctl->status, (int)MBA_ERR_NOT_SPD);
-      for (int a = 0; a < 9; ++a) V[a] = 0.0;
+#pragma unroll
+      for (int a = 0; a < 9; ++a) Vd[a] = 0.0;
     }
-    double gs[3], Vg[3];
-    for (int a = 0; a < 3; ++a) gs[a] = sl[a] * (double)s.L.gl[a * NL + l];
-    for (int a = 0; a < 3; ++a) Vg[a] = V[3 * a] * gs[0] + V[3 * a + 1] * gs[1] + V[3 * a + 2] * gs[2];
-    for (int64_t sl_i = s.S.lm_slot_off[l]; sl_i < s.S.lm_slot_off[l + 1]; ++sl_i) {
-      const int64_t k = s.S.slot_kf[sl_i];
+#pragma unroll
+    for (int a = 0; a < 9; ++a) V[a] = T(Vd[a]);
+    T g[3], Vg[3];
+#pragma unroll
+    for (int a = 0; a < 3; ++a) g[a] = s.L.gl[a * NL + l];
+#pragma unroll
+    for (int a = 0; a < 3; ++a) Vg[a] = V[3 * a] * g[0] + V[3 * a + 1] * g[1] + V[3 * a + 2] * g[2];
+    for (int64_t si = s.S.lm_slot_off[l]; si < s.S.lm_slot_off[l + 1]; ++si) {
+      const int64_t k = s.S.slot_kf[si];
+#pragma unroll
       for (int c = 0; c < 6; ++c) {
-        const double sk = s.sc.skf[15 * k + c];
-        double acc = 0.0;
-        for (int x = 0; x < 3; ++x) acc += sl[x] * (double)s.L.Wslot[(6 * x + c) * NS + sl_i] * sk * Vg[x];
-        if (acc != 0.0) atomic_add(&s.L.rhs[15 * k + c], T(acc));
+        const T acc = s.L.Wslot[c * NS + si] * Vg[0] + s.L.Wslot[(6 + c) * NS + si] * Vg[1] +
+                      s.L.Wslot[(12 + c) * NS + si] * Vg[2];
+        if (acc != T(0)) atomic_add(&s.L.rhs[15 * k + c], acc);
       }
     }
   }
-  for (int a = 0; a < 9; ++a) s.L.V[a * NL + l] = T(V[a]);
+#pragma unroll
+  for (int a = 0; a < 9; ++a) s.L.V[a * NL + l] = V[a];
 }
 
-// Landmark elimination, part 2: U = V Ws per slot (Ws = scaled W).
+// Landmark elimination, part 2: U = V W per slot.
 template <typename T>
 __global__ void __launch_bounds__(kB) k_schur_slot(SolverLaunch<T> s) {
   if (s.ctl->terminated) return;
   const int64_t i = blockIdx.x * (int64_t)blockDim.x + threadIdx.x;
   const int64_t NS = s.S.nslot, NL = s.P.nlm;
   if (i >= NS) return;
-  const int64_t l = s.S.slot_lm[i], k = s.S.slot_kf[i];
-  T Ws[18];
-  for (int x = 0; x < 3; ++x) {
-    const double sl = s.sc.slm[x * NL + l];
-    for (int c = 0; c < 6; ++c) Ws[6 * x + c] = T(sl * (double)s.L.Wslot[(6 * x + c) * NS + i] * s.sc.skf[15 * k + c]);
-  }
-  T V[9];
+  const int64_t l = s.S.slot_lm[i];
+  T W[18], V[9];
+#pragma unroll
+  for (int a = 0; a < 18; ++a) W[a] = s.L.Wslot[a * NS + i];
+#pragma unroll
   for (int a = 0; a < 9; ++a) V[a] = s.L.V[a * NL + l];
+#pragma unroll
   for (int x = 0; x < 3; ++x)
+#pragma unroll
     for (int c = 0; c < 6; ++c)
-      s.L.U[(6 * x + c) * NS + i] = V[3 * x] * Ws[c] + V[3 * x + 1] * Ws[6 + c] + V[3 * x + 2] * Ws[12 + c];
+      s.L.U[(6 * x + c) * NS + i] = V[3 * x] * W[c] + V[3 * x + 1] * W[6 + c] + V[3 * x + 2] * W[12 + c];
 }
 
-// Landmark elimination, part 3: S(k_a, k_b) -= Ws_a^T U_b for every slot pair.
+// Adds -M (6x6, row-major), -(M + M^T) (sym) or -M^T (tr) into a 6x6 block
+// with leading dimension ld.
 template <typename T>
-__global__ void __launch_bounds__(kB) k_schur_pairs(SolverLaunch<T> s) {
-  if (s.ctl->terminated) return;
-  const int64_t pidx = blockIdx.x * (int64_t)blockDim.x + threadIdx.x;
-  if (pidx >= s.S.npair) return;
-  const int64_t NS = s.S.nslot, NL = s.P.nlm;
-  const int64_t a = s.S.pair_a[pidx], b = s.S.pair_b[pidx];
-  const int tgt = s.S.pair_t[pidx];
-  const int64_t l = s.S.slot_lm[a], ka = s.S.slot_kf[a], kb = s.S.slot_kf[b];
-  T Wa[18], Ub[18];
-  for (int x = 0; x < 3; ++x) {
-    const double sl = s.sc.slm[x * NL + l];
-    for (int c = 0; c < 6; ++c) {
-      Wa[6 * x + c] = T(sl * (double)s.L.Wslot[(6 * x + c) * NS + a] * s.sc.skf[15 * ka + c]);
-      Ub[6 * x + c] = s.L.U[(6 * x + c) * NS + b];
-    }
-  }
-  T M[36];
+__device__ __forceinline__ void sub_block(T* dst, int ld, const T* M, bool sym, bool tr) {
 #pragma unroll
   for (int r = 0; r < 6; ++r)
 #pragma unroll
-    for (int c = 0; c < 6; ++c) M[6 * r + c] = Wa[r] * Ub[c] + Wa[6 + r] * Ub[6 + c] + Wa[12 + r] * Ub[12 + c];
-  if (tgt < 0) {
-    T* D = s.L.SD + 225 * (int64_t)(-tgt - 1);
-    if (a == b) {
-#pragma unroll
-      for (int r = 0; r < 6; ++r)
-#pragma unroll
-        for (int c = 0; c < 6; ++c) atomic_add(&D[15 * r + c], -M[6 * r + c]);
-    } else {
-#pragma unroll
-      for (int r = 0; r < 6; ++r)
-#pragma unroll
-        for (int c = 0; c < 6; ++c) atomic_add(&D[15 * r + c], -(M[6 * r + c] + M[6 * c + r]));
+    for (int c = 0; c < 6; ++c) {
+      const T v = sym ? M[6 * r + c] + M[6 * c + r] : (tr ? M[6 * c + r] : M[6 * r + c]);
+      atomic_add(&dst[ld * r + c], -v);
     }
-  } else {
-    T* B = s.L.SP + 36 * (int64_t)tgt;
-    if (ka < kb) {
+}
+
+// Landmark elimination, part 3: S(k_a, k_b) -= W_a^T U_b for every slot pair.
+// One block per pair group: the group's pairs accumulate into a shared-memory
+// copy of the (at most kSchurGroupTargets) S blocks they touch, which is added
+// to S once at the end, so contended updates stay on chip.  Pairs of a
+// landmark too large for any group (pair_loc < 0) update S directly.
+constexpr int kSchurThreads = 256;
+
+template <typename T>
+__global__ void __launch_bounds__(kSchurThreads) k_schur_pairs(SolverLaunch<T> s) {
+  extern __shared__ __align__(16) unsigned char schur_smem[];
+  T* acc = reinterpret_cast<T*>(schur_smem);
+  if (s.ctl->terminated) return;
+  const int64_t g = blockIdx.x;
+  const int64_t p0 = s.S.grp_pair_off[g], p1 = s.S.grp_pair_off[g + 1];
+  const int64_t t0 = s.S.grp_tgt_off[g];
+  const int nacc = 36 * (int)(s.S.grp_tgt_off[g + 1] - t0);
+  for (int i = threadIdx.x; i < nacc; i += blockDim.x) acc[i] = T(0);
+  __syncthreads();
+  const int64_t NS = s.S.nslot;
+  for (int64_t pidx = p0 + threadIdx.x; pidx < p1; pidx += blockDim.x) {
+    const int64_t a = s.S.pair_a[pidx], b = s.S.pair_b[pidx];
+    const int tgt = s.S.pair_t[pidx], loc = s.S.pair_loc[pidx];
+    T Wa[18], Ub[18];
 #pragma unroll
-      for (int r = 0; r < 6; ++r)
+    for (int q = 0; q < 18; ++q) {
+      Wa[q] = s.L.Wslot[q * NS + a];
+      Ub[q] = s.L.U[q * NS + b];
+    }
+    T M[36];
 #pragma unroll
-        for (int c = 0; c < 6; ++c) atomic_add(&B[6 * r + c], -M[6 * r + c]);
+    for (int r = 0; r < 6; ++r)
+#pragma unroll
+      for (int c = 0; c < 6; ++c) M[6 * r + c] = Wa[r] * Ub[c] + Wa[6 + r] * Ub[6 + c] + Wa[12 + r] * Ub[12 + c];
+    // Orientation of M in the target: diagonal blocks take M (a == b) or
+    // M + M^T; upper blocks (k_a < k_b) take M, else M^T.
+    const bool sym = tgt < 0 && a != b;
+    const bool tr = tgt >= 0 && s.S.slot_kf[a] > s.S.slot_kf[b];
+    if (loc >= 0) {
+      sub_block(acc + 36 * loc, 6, M, sym, tr);
+    } else if (tgt < 0) {
+      sub_block(s.L.SD + 225 * (int64_t)(-tgt - 1), 15, M, sym, tr);
     } else {
-#pragma unroll
-      for (int r = 0; r < 6; ++r)
-#pragma unroll
-        for (int c = 0; c < 6; ++c) atomic_add(&B[6 * r + c], -M[6 * c + r]);
+      sub_block(s.L.SP + 36 * (int64_t)tgt, 6, M, sym, tr);
+    }
+  }
+  __syncthreads();
+  for (int i = threadIdx.x; i < nacc; i += blockDim.x) {
+    const T v = acc[i];
+    if (v == T(0)) continue;
+    const int code = s.S.grp_tgt[t0 + i / 36], e = i % 36;
+    if (code < 0) {
+      atomic_add(&s.L.SD[225 * (int64_t)(-code - 1) + 15 * (e / 6) + e % 6], v);
+    } else {
+      atomic_add(&s.L.SP[36 * (int64_t)code + e], v);
     }
   }
 }
@@ -587,32 +649,41 @@ __global__ void __launch_bounds__(kB) k_pcg_update(SolverLaunch<T> s, int it, co
 }
 
 // ------------------------------------------------------------ step
-// Back substitution: dl = V (-g_s - sum_a Ws_a x_{k_a}).
+// Back substitution: dl = V (-g - sum_a W_a x_{k_a}) (scaled system).
 template <typename T>
 __global__ void __launch_bounds__(kB) k_backsub(SolverLaunch<T> s) {
   if (s.ctl->terminated) return;
   const int64_t l = blockIdx.x * (int64_t)blockDim.x + threadIdx.x;
   const int64_t NL = s.P.nlm, NS = s.S.nslot;
   if (l >= NL) return;
-  double t[3];
-  double sl[3];
-  for (int a = 0; a < 3; ++a) { sl[a] = s.sc.slm[a * NL + l]; t[a] = -sl[a] * (double)s.L.gl[a * NL + l]; }
+  T t[3];
+#pragma unroll
+  for (int a = 0; a < 3; ++a) t[a] = -s.L.gl[a * NL + l];
   for (int64_t i = s.S.lm_slot_off[l]; i < s.S.lm_slot_off[l + 1]; ++i) {
-    const int64_t k = s.S.slot_kf[i];
+    const T* xk = s.L.x + 15 * (int64_t)s.S.slot_kf[i];
+    T xv[6];
+#pragma unroll
+    for (int c = 0; c < 6; ++c) xv[c] = xk[c];
+#pragma unroll
     for (int x = 0; x < 3; ++x) {
-      double acc = 0.0;
-      for (int c = 0; c < 6; ++c) acc += (double)s.L.Wslot[(6 * x + c) * NS + i] * s.sc.skf[15 * k + c] * (double)s.L.x[15 * k + c];
-      t[x] -= sl[x] * acc;
+      T acc = T(0);
+#pragma unroll
+      for (int c = 0; c < 6; ++c) acc += s.L.Wslot[(6 * x + c) * NS + i] * xv[c];
+      t[x] -= acc;
     }
   }
+  const bool act = s.P.lm_active[l];
+#pragma unroll
   for (int a = 0; a < 3; ++a) {
-    double v = 0.0;
-    for (int b = 0; b < 3; ++b) v += (double)s.L.V[(3 * a + b) * NL + l] * t[b];
-    s.L.dl[a * NL + l] = s.P.lm_active[l] ? v : 0.0;
+    T v = T(0);
+#pragma unroll
+    for (int b = 0; b < 3; ++b) v += s.L.V[(3 * a + b) * NL + l] * t[b];
+    s.L.dl[a * NL + l] = act ? (double)v : 0.0;
   }
 }
 
-// Model cost change -u.(r + u/2) with u = J du (unscaled J, unscaled step).
+// Model cost change -u.(r + u/2) with u = J du (unscaled J, du = s dx);
+// u in T, the reduction in FP64.
 template <typename T>
 __global__ void __launch_bounds__(kB) k_model_visual(SolverLaunch<T> s) {
   if (s.ctl->terminated) return;
@@ -621,18 +692,30 @@ __global__ void __launch_bounds__(kB) k_model_visual(SolverLaunch<T> s) {
   double m = 0.0;
   if (i < N) {
     const int64_t l = s.P.obs_lm[i];
-    double u[2] = {0.0, 0.0};
+    T dl[3];
+#pragma unroll
+    for (int a = 0; a < 3; ++a) dl[a] = s.L.slm[a * NL + l] * T(s.L.dl[a * NL + l]);
+    T u[2] = {T(0), T(0)};
+#pragma unroll
     for (int rr = 0; rr < 2; ++rr)
-      for (int a = 0; a < 3; ++a)
-        u[rr] += (double)s.vis.Jl[(3 * rr + a) * N + i] * s.sc.slm[a * NL + l] * s.L.dl[a * NL + l];
+#pragma unroll
+      for (int a = 0; a < 3; ++a) u[rr] += s.vis.Jl[(3 * rr + a) * N + i] * dl[a];
     if (s.P.obs_type[i] != MBA_LOCAL_KEYFRAME) {
       const int64_t ks = s.P.obs_store[i], ko = s.P.obs_kf[i];
+      T xs[6], xo[6];
+#pragma unroll
+      for (int c = 0; c < 6; ++c) {
+        xs[c] = s.L.skf[15 * ks + c] * s.L.x[15 * ks + c];
+        xo[c] = s.L.skf[15 * ko + c] * s.L.x[15 * ko + c];
+      }
+#pragma unroll
       for (int rr = 0; rr < 2; ++rr)
+#pragma unroll
         for (int c = 0; c < 6; ++c)
-          u[rr] += (double)s.vis.Js[(6 * rr + c) * N + i] * s.sc.skf[15 * ks + c] * (double)s.L.x[15 * ks + c] +
-                   (double)s.vis.Jo[(6 * rr + c) * N + i] * s.sc.skf[15 * ko + c] * (double)s.L.x[15 * ko + c];
+          u[rr] += s.vis.Js[(6 * rr + c) * N + i] * xs[c] + s.vis.Jo[(6 * rr + c) * N + i] * xo[c];
     }
-    m = -(u[0] * ((double)s.vis.r[i] + u[0] / 2.0) + u[1] * ((double)s.vis.r[N + i] + u[1] / 2.0));
+    const double u0 = (double)u[0], u1 = (double)u[1];
+    m = -(u0 * ((double)s.vis.r[i] + u0 / 2.0) + u1 * ((double)s.vis.r[N + i] + u1 / 2.0));
   }
   block_add(m, &s.ctl->model_change);
 }
@@ -645,11 +728,13 @@ __global__ void __launch_bounds__(128) k_model_inertial(SolverLaunch<T> s) {
   double m = 0.0;
   if (e < s.P.nedge && lane < 15) {
     const int64_t f = s.P.e_from[e], t = s.P.e_to[e];
-    double u = 0.0;
+    T u = T(0);
+#pragma unroll
     for (int c = 0; c < 15; ++c)
-      u += (double)s.ine.Jf[225 * e + 15 * lane + c] * s.sc.skf[15 * f + c] * (double)s.L.x[15 * f + c] +
-           (double)s.ine.Jt[225 * e + 15 * lane + c] * s.sc.skf[15 * t + c] * (double)s.L.x[15 * t + c];
-    m = -u * ((double)s.ine.r[15 * e + lane] + u / 2.0);
+      u += s.ine.Jf[225 * e + 15 * lane + c] * s.L.skf[15 * f + c] * s.L.x[15 * f + c] +
+           s.ine.Jt[225 * e + 15 * lane + c] * s.L.skf[15 * t + c] * s.L.x[15 * t + c];
+    const double ud = (double)u;
+    m = -ud * ((double)s.ine.r[15 * e + lane] + ud / 2.0);
   }
   block_add(m, &s.ctl->model_change);
 }
@@ -827,6 +912,12 @@ cudaError_t solver_assemble(const SolverLaunch<T>& s, const int* gate, cudaStrea
   if (s.S.npu) k_zero<T><<<gridcap(36 * s.S.npu), kB, 0, st>>>(s.L.Pbase, 36 * s.S.npu, gate, skip);
   if (s.P.nlm) k_assemble_lm<T><<<nblk(s.P.nlm, kB), kB, 0, st>>>(s.P, s.S, s.vis, s.L, gate, skip);
   if (s.P.nedge) k_assemble_inertial<T><<<nblk(32 * s.P.nedge, 128), 128, 0, st>>>(s.P, s.ine, s.L, gate, skip);
+  // Relinearizations inside the LM loop apply the (fixed) Jacobi scaling right
+  // away; the first assembly is scaled by solver_compute_scale.
+  if (gate) {
+    const int64_t n = 12 * s.P.nlm + 18 * s.S.nslot + 240 * s.P.nkf + 36 * s.S.npu + 225 * s.P.nedge;
+    k_scale_inplace<T><<<gridcap(n), kB, 0, st>>>(s.P, s.S, s.L, gate, skip);
+  }
   return cudaGetLastError();
 }
 
@@ -834,7 +925,17 @@ template <typename T>
 cudaError_t solver_compute_scale(const SolverLaunch<T>& s, int jacobi, cudaStream_t st) {
   const int64_t n = 15 * s.P.nkf + 3 * s.P.nlm;
   k_scale<T><<<nblk(n, kB), kB, 0, st>>>(s.P, s.L, s.sc, jacobi);
+  const int64_t m = 12 * s.P.nlm + 18 * s.S.nslot + 240 * s.P.nkf + 36 * s.S.npu + 225 * s.P.nedge;
+  k_scale_inplace<T><<<gridcap(m), kB, 0, st>>>(s.P, s.S, s.L, nullptr, nullptr);
   return cudaGetLastError();
+}
+
+template <typename T>
+cudaError_t solver_prepare(const SolverLaunch<T>& s) {
+  const size_t smem = sizeof(T) * 36 * (size_t)s.S.max_group_targets;
+  if (smem > 48 * 1024)
+    return cudaFuncSetAttribute(k_schur_pairs<T>, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)smem);
+  return cudaSuccess;
 }
 
 template <typename T>
@@ -843,7 +944,8 @@ cudaError_t solver_step(const SolverLaunch<T>& s, cudaStream_t st) {
   k_build_system<T><<<gridcap(nsys), kB, 0, st>>>(s);
   if (s.P.nlm) k_schur_lm<T><<<nblk(s.P.nlm, kB), kB, 0, st>>>(s);
   if (s.S.nslot) k_schur_slot<T><<<nblk(s.S.nslot, kB), kB, 0, st>>>(s);
-  if (s.S.npair) k_schur_pairs<T><<<nblk(s.S.npair, kB), kB, 0, st>>>(s);
+  if (s.S.ngroup)
+    k_schur_pairs<T><<<s.S.ngroup, kSchurThreads, sizeof(T) * 36 * (size_t)s.S.max_group_targets, st>>>(s);
   k_finalize_system<T><<<gridcap(nsys), kB, 0, st>>>(s);
   k_block_jacobi<T><<<nblk(s.P.nkf, 64), 64, 0, st>>>(s);
   const int64_t n = 15 * s.P.nkf;
@@ -893,6 +995,8 @@ template cudaError_t solver_assemble<double>(const SolverLaunch<double>&, const 
 template cudaError_t solver_assemble<float>(const SolverLaunch<float>&, const int*, cudaStream_t);
 template cudaError_t solver_compute_scale<double>(const SolverLaunch<double>&, int, cudaStream_t);
 template cudaError_t solver_compute_scale<float>(const SolverLaunch<float>&, int, cudaStream_t);
+template cudaError_t solver_prepare<double>(const SolverLaunch<double>&);
+template cudaError_t solver_prepare<float>(const SolverLaunch<float>&);
 template cudaError_t solver_step<double>(const SolverLaunch<double>&, cudaStream_t);
 template cudaError_t solver_step<float>(const SolverLaunch<float>&, cudaStream_t);
 template cudaError_t solver_evaluate_candidate<double>(const SolverLaunch<double>&, InertialLin<double>, cudaStream_t);

@@ -8,6 +8,9 @@
 
 namespace mba {
 
+// Distinct S blocks a pair group may touch (shared-memory accumulator size).
+constexpr int64_t kSchurGroupTargets = 256;
+
 // Static sparsity of the reduced camera system, built on the host at create.
 struct SchurPattern {
   int64_t nslot = 0;      // landmark slots: slot 0 = store keyframe, then one per non-keyframe observation
@@ -21,6 +24,12 @@ struct SchurPattern {
   int32_t* pair_a;        // [npair] global slot ids
   int32_t* pair_b;
   int32_t* pair_t;        // >= 0: upper block index; < 0: -(kf+1) diagonal block
+  int32_t* pair_loc;      // [npair] target id local to the pair's group, -1 = accumulate globally
+  int64_t ngroup = 0;     // pair groups (contiguous pair ranges, landmarks ordered by store keyframe)
+  int64_t max_group_targets = 0;
+  int64_t* grp_pair_off;  // [ngroup+1]
+  int64_t* grp_tgt_off;   // [ngroup+1]
+  int32_t* grp_tgt;       // group-local target id -> pair_t code
   int32_t* pu_i;          // [npu]
   int32_t* pu_j;
   int64_t* row_off;       // [nkf+1] full (both orientations) pose-pose rows
@@ -89,6 +98,8 @@ struct LinearSystem {
   T* Minv;       // [nkf][225] block-Jacobi inverses (factorized and inverted in FP64)
   T *x, *r, *z, *p, *q, *q2;  // [nkf*15]; p and q2 double-buffer the PCG direction
   double* dl;    // [3][nlm] scaled landmark step
+  T* skf;        // [nkf*15] Jacobi scale (T copy)
+  T* slm;        // [3][nlm]
 };
 
 struct ScaleVectors {
@@ -116,6 +127,10 @@ template <typename T>
 cudaError_t solver_assemble(const SolverLaunch<T>& s, const int* gate, cudaStream_t st);
 template <typename T>
 cudaError_t solver_compute_scale(const SolverLaunch<T>& s, int jacobi, cudaStream_t st);
+// Host-side kernel attributes; call before the first solver_step (not
+// during stream capture).
+template <typename T>
+cudaError_t solver_prepare(const SolverLaunch<T>& s);
 template <typename T>
 cudaError_t solver_step(const SolverLaunch<T>& s, cudaStream_t st);
 template <typename T>
