@@ -446,14 +446,21 @@ mba_status mba_synth_generate(const mba_synth_config* cfg, mba_synth_map** out) 
       M->obs_kf.push_back(K);
       M->obs_cam.push_back(c);
     }
-    // Loop-closure landmarks shared with another co-registered mission.
+    // Loop-closure landmarks shared with another co-registered mission.  The
+    // missions re-traverse the same path; mission m overlaps its ring
+    // neighbours m-1 and m+1, and the landmark is re-observed from the
+    // keyframes of that mission closest to the store keyframe within the same
+    // lap, so loop closures link corresponding trajectory segments.
     if (nm > 1 && cfg->co_registered && cfg->shared_landmark_fraction > 0 && rng.uniform() < cfg->shared_landmark_fraction) {
-      const int m2 = (m + 1 + (int)rng.below(nm - 1)) % nm;
+      const int m2 = nm == 2 ? 1 - m : (rng.below(2) ? (m + 1) % nm : (m + nm - 1) % nm);
       const int c2 = cfg->camera_per_mission ? m2 % cfg->num_cameras : c;
       const int64_t Kbest = [&]() {
+        const int64_t lap = (int64_t)std::llround(cfg->keyframes_per_lap);
+        const int64_t local = store - kf0[m];
+        const int64_t lo = std::max<int64_t>(0, local - lap / 2), hi = std::min<int64_t>(nk[m2], local + lap / 2 + 1);
         int64_t best = -1;
         double bd = 1e30;
-        for (int k = 0; k < nk[m2]; k += 1) {
+        for (int64_t k = lo; k < hi; ++k) {
           const int64_t K = kf0[m2] + k;
           double d = 0.0;
           for (int i = 0; i < 3; ++i) d += (kf_pG[K][i] - kf_pG[store][i]) * (kf_pG[K][i] - kf_pG[store][i]);
