@@ -52,6 +52,26 @@ __device__ __forceinline__ void atomic_add(T* a, T v) {
   atomicAdd(a, v);
 }
 
+// Loads the 18 values of one slot (slot-major W or U rows).
+__device__ __forceinline__ void load_slot(const float* p, float* v) {
+  const float2* q = reinterpret_cast<const float2*>(p);  // 72-byte rows: 8-byte aligned
+#pragma unroll
+  for (int i = 0; i < 9; ++i) {
+    const float2 t = q[i];
+    v[2 * i] = t.x;
+    v[2 * i + 1] = t.y;
+  }
+}
+__device__ __forceinline__ void load_slot(const double* p, double* v) {
+  const double2* q = reinterpret_cast<const double2*>(p);  // 144-byte rows: 16-byte aligned
+#pragma unroll
+  for (int i = 0; i < 9; ++i) {
+    const double2 t = q[i];
+    v[2 * i] = t.x;
+    v[2 * i + 1] = t.y;
+  }
+}
+
 // ------------------------------------------------------------ assembly
 template <typename T>
 __global__ void __launch_bounds__(kB) k_zero(T* a, int64_t n, const int* run_if, const int* skip_if) {
@@ -68,7 +88,7 @@ __global__ void __launch_bounds__(kB) k_assemble_lm(DevProblem P, SchurPattern S
   if (gated(run_if, skip_if)) return;
   const int64_t l = blockIdx.x * (int64_t)blockDim.x + threadIdx.x;
   if (l >= P.nlm) return;
-  const int64_t N = P.nobs, NS = S.nslot, NL = P.nlm;
+  const int64_t N = P.nobs, NL = P.nlm;
   const int64_t s0 = S.lm_slot_off[l];
   const int st = S.slot_kf[s0];
   T H[9], g[3], Wst[18], Dst[36], gst[6];
@@ -106,7 +126,7 @@ __global__ void __launch_bounds__(kB) k_assemble_lm(DevProblem P, SchurPattern S
 #pragma unroll
       for (int c = 0; c < 6; ++c) {
         Wst[6 * x + c] += Jl[x] * Js[c] + Jl[3 + x] * Js[6 + c];
-        L.Wslot[(6 * x + c) * NS + slot] = Jl[x] * Jo[c] + Jl[3 + x] * Jo[6 + c];
+        L.Wslot[18 * (int64_t)slot + 6 * x + c] = Jl[x] * Jo[c] + Jl[3 + x] * Jo[6 + c];
       }
 #pragma unroll
     for (int a = 0; a < 6; ++a) {
@@ -137,7 +157,7 @@ __global__ void __launch_bounds__(kB) k_assemble_lm(DevProblem P, SchurPattern S
 #pragma unroll
   for (int a = 0; a < 3; ++a) L.gl[a * NL + l] = g[a];
 #pragma unroll
-  for (int a = 0; a < 18; ++a) L.Wslot[a * NS + s0] = Wst[a];
+  for (int a = 0; a < 18; ++a) L.Wslot[18 * s0 + a] = Wst[a];
   if (any_cam) {
 #pragma unroll
     for (int a = 0; a < 6; ++a) {
@@ -219,7 +239,7 @@ __global__ void __launch_bounds__(kB) k_scale_inplace(DevProblem P, SchurPattern
       L.gl[j] *= L.slm[j];
       (void)l;
     } else if (i < n3) {
-      const int64_t j = i - n2, q = j / NS, sl = j % NS;
+      const int64_t j = i - n2, q = j % 18, sl = j / 18;
       L.Wslot[j] *= L.slm[(q / 6) * NL + S.slot_lm[sl]] * L.skf[15 * (int64_t)S.slot_kf[sl] + q % 6];
     } else if (i < n4) {
       const int64_t j = i - n3, k = j / 225, e = j % 225;
@@ -328,8 +348,8 @@ __global__ void __launch_bounds__(kB) k_schur_lm(SolverLaunch<T> s) {
       const int64_t k = s.S.slot_kf[si];
 #pragma unroll
       for (int c = 0; c < 6; ++c) {
-        const T acc = s.L.Wslot[c * NS + si] * Vg[0] + s.L.Wslot[(6 + c) * NS + si] * Vg[1] +
-                      s.L.Wslot[(12 + c) * NS + si] * Vg[2];
+        const T* w = s.L.Wslot + 18 * si;
+        const T acc = w[c] * Vg[0] + w[6 + c] * Vg[1] + w[12 + c] * Vg[2];
         if (acc != T(0)) atomic_add(&s.L.rhs[15 * k + c], acc);
       }
     }
@@ -347,85 +367,61 @@ __global__ void __launch_bounds__(kB) k_schur_slot(SolverLaunch<T> s) {
   if (i >= NS) return;
   const int64_t l = s.S.slot_lm[i];
   T W[18], V[9];
-#pragma unroll
-  for (int a = 0; a < 18; ++a) W[a] = s.L.Wslot[a * NS + i];
+  load_slot(s.L.Wslot + 18 * i, W);
 #pragma unroll
   for (int a = 0; a < 9; ++a) V[a] = s.L.V[a * NL + l];
 #pragma unroll
   for (int x = 0; x < 3; ++x)
 #pragma unroll
     for (int c = 0; c < 6; ++c)
-      s.L.U[(6 * x + c) * NS + i] = V[3 * x] * W[c] + V[3 * x + 1] * W[6 + c] + V[3 * x + 2] * W[12 + c];
-}
-
-// Adds -M (6x6, row-major), -(M + M^T) (sym) or -M^T (tr) into a 6x6 block
-// with leading dimension ld.
-template <typename T>
-__device__ __forceinline__ void sub_block(T* dst, int ld, const T* M, bool sym, bool tr) {
-#pragma unroll
-  for (int r = 0; r < 6; ++r)
-#pragma unroll
-    for (int c = 0; c < 6; ++c) {
-      const T v = sym ? M[6 * r + c] + M[6 * c + r] : (tr ? M[6 * c + r] : M[6 * r + c]);
-      atomic_add(&dst[ld * r + c], -v);
-    }
+      s.L.U[18 * i + 6 * x + c] = V[3 * x] * W[c] + V[3 * x + 1] * W[6 + c] + V[3 * x + 2] * W[12 + c];
 }
 
 // Landmark elimination, part 3: S(k_a, k_b) -= W_a^T U_b for every slot pair.
-// One block per pair group: the group's pairs accumulate into a shared-memory
-// copy of the (at most kSchurGroupTargets) S blocks they touch, which is added
-// to S once at the end, so contended updates stay on chip.  Pairs of a
-// landmark too large for any group (pair_loc < 0) update S directly.
-constexpr int kSchurThreads = 256;
-
+// Pairs are sorted by target block; one thread sums a chunk of one target's
+// pairs in registers and writes the block once (plain read-modify-write when
+// it owns the whole target, atomics otherwise).  Diagonal targets take
+// M + M^T for a != b; upper pairs are oriented so M lands untransposed.
 template <typename T>
-__global__ void __launch_bounds__(kSchurThreads) k_schur_pairs(SolverLaunch<T> s) {
-  extern __shared__ __align__(16) unsigned char schur_smem[];
-  T* acc = reinterpret_cast<T*>(schur_smem);
+__global__ void __launch_bounds__(kB) k_schur_pairs(SolverLaunch<T> s) {
   if (s.ctl->terminated) return;
-  const int64_t g = blockIdx.x;
-  const int64_t p0 = s.S.grp_pair_off[g], p1 = s.S.grp_pair_off[g + 1];
-  const int64_t t0 = s.S.grp_tgt_off[g];
-  const int nacc = 36 * (int)(s.S.grp_tgt_off[g + 1] - t0);
-  for (int i = threadIdx.x; i < nacc; i += blockDim.x) acc[i] = T(0);
-  __syncthreads();
-  const int64_t NS = s.S.nslot;
-  for (int64_t pidx = p0 + threadIdx.x; pidx < p1; pidx += blockDim.x) {
-    const int64_t a = s.S.pair_a[pidx], b = s.S.pair_b[pidx];
-    const int tgt = s.S.pair_t[pidx], loc = s.S.pair_loc[pidx];
-    T Wa[18], Ub[18];
+  const int64_t c = blockIdx.x * (int64_t)blockDim.x + threadIdx.x;
+  if (c >= s.S.nchunk) return;
+  const int32_t raw = s.S.chunk_tgt[c];
+  const bool whole = raw >= 0;
+  const int64_t tid = whole ? raw : ~raw;
+  const bool diag = tid < s.P.nkf;
+  T acc[36];
 #pragma unroll
-    for (int q = 0; q < 18; ++q) {
-      Wa[q] = s.L.Wslot[q * NS + a];
-      Ub[q] = s.L.U[q * NS + b];
-    }
-    T M[36];
+  for (int q = 0; q < 36; ++q) acc[q] = T(0);
+  const int64_t p1 = s.S.chunk_off[c + 1];
+  for (int64_t p = s.S.chunk_off[c]; p < p1; ++p) {
+    const int64_t a = s.S.pair_a[p], b = s.S.pair_b[p];
+    T Wa[18], Ub[18];
+    load_slot(s.L.Wslot + 18 * a, Wa);
+    load_slot(s.L.U + 18 * b, Ub);
+    const bool sym = diag && a != b;
 #pragma unroll
     for (int r = 0; r < 6; ++r)
 #pragma unroll
-      for (int c = 0; c < 6; ++c) M[6 * r + c] = Wa[r] * Ub[c] + Wa[6 + r] * Ub[6 + c] + Wa[12 + r] * Ub[12 + c];
-    // Orientation of M in the target: diagonal blocks take M (a == b) or
-    // M + M^T; upper blocks (k_a < k_b) take M, else M^T.
-    const bool sym = tgt < 0 && a != b;
-    const bool tr = tgt >= 0 && s.S.slot_kf[a] > s.S.slot_kf[b];
-    if (loc >= 0) {
-      sub_block(acc + 36 * loc, 6, M, sym, tr);
-    } else if (tgt < 0) {
-      sub_block(s.L.SD + 225 * (int64_t)(-tgt - 1), 15, M, sym, tr);
-    } else {
-      sub_block(s.L.SP + 36 * (int64_t)tgt, 6, M, sym, tr);
-    }
+      for (int q = 0; q < 6; ++q) {
+        const T m = Wa[r] * Ub[q] + Wa[6 + r] * Ub[6 + q] + Wa[12 + r] * Ub[12 + q];
+        acc[6 * r + q] += m;
+        if (sym) acc[6 * q + r] += m;
+      }
   }
-  __syncthreads();
-  for (int i = threadIdx.x; i < nacc; i += blockDim.x) {
-    const T v = acc[i];
-    if (v == T(0)) continue;
-    const int code = s.S.grp_tgt[t0 + i / 36], e = i % 36;
-    if (code < 0) {
-      atomic_add(&s.L.SD[225 * (int64_t)(-code - 1) + 15 * (e / 6) + e % 6], v);
-    } else {
-      atomic_add(&s.L.SP[36 * (int64_t)code + e], v);
-    }
+  T* dst = diag ? s.L.SD + 225 * tid : s.L.SP + 36 * (tid - s.P.nkf);
+  const int ld = diag ? 15 : 6;
+  if (whole) {
+#pragma unroll
+    for (int r = 0; r < 6; ++r)
+#pragma unroll
+      for (int q = 0; q < 6; ++q) dst[ld * r + q] -= acc[6 * r + q];
+  } else {
+#pragma unroll
+    for (int r = 0; r < 6; ++r)
+#pragma unroll
+      for (int q = 0; q < 6; ++q) atomic_add(&dst[ld * r + q], -acc[6 * r + q]);
   }
 }
 
@@ -668,7 +664,7 @@ __global__ void __launch_bounds__(kB) k_backsub(SolverLaunch<T> s) {
     for (int x = 0; x < 3; ++x) {
       T acc = T(0);
 #pragma unroll
-      for (int c = 0; c < 6; ++c) acc += s.L.Wslot[(6 * x + c) * NS + i] * xv[c];
+      for (int c = 0; c < 6; ++c) acc += s.L.Wslot[18 * i + 6 * x + c] * xv[c];
       t[x] -= acc;
     }
   }
@@ -931,21 +927,12 @@ cudaError_t solver_compute_scale(const SolverLaunch<T>& s, int jacobi, cudaStrea
 }
 
 template <typename T>
-cudaError_t solver_prepare(const SolverLaunch<T>& s) {
-  const size_t smem = sizeof(T) * 36 * (size_t)s.S.max_group_targets;
-  if (smem > 48 * 1024)
-    return cudaFuncSetAttribute(k_schur_pairs<T>, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)smem);
-  return cudaSuccess;
-}
-
-template <typename T>
 cudaError_t solver_step(const SolverLaunch<T>& s, cudaStream_t st) {
   const int64_t nsys = 225 * s.P.nkf + 225 * s.P.nedge + 36 * s.S.npu + 15 * s.P.nkf;
   k_build_system<T><<<gridcap(nsys), kB, 0, st>>>(s);
   if (s.P.nlm) k_schur_lm<T><<<nblk(s.P.nlm, kB), kB, 0, st>>>(s);
   if (s.S.nslot) k_schur_slot<T><<<nblk(s.S.nslot, kB), kB, 0, st>>>(s);
-  if (s.S.ngroup)
-    k_schur_pairs<T><<<s.S.ngroup, kSchurThreads, sizeof(T) * 36 * (size_t)s.S.max_group_targets, st>>>(s);
+  if (s.S.nchunk) k_schur_pairs<T><<<nblk(s.S.nchunk, kB), kB, 0, st>>>(s);
   k_finalize_system<T><<<gridcap(nsys), kB, 0, st>>>(s);
   k_block_jacobi<T><<<nblk(s.P.nkf, 64), 64, 0, st>>>(s);
   const int64_t n = 15 * s.P.nkf;
@@ -995,8 +982,6 @@ template cudaError_t solver_assemble<double>(const SolverLaunch<double>&, const 
 template cudaError_t solver_assemble<float>(const SolverLaunch<float>&, const int*, cudaStream_t);
 template cudaError_t solver_compute_scale<double>(const SolverLaunch<double>&, int, cudaStream_t);
 template cudaError_t solver_compute_scale<float>(const SolverLaunch<float>&, int, cudaStream_t);
-template cudaError_t solver_prepare<double>(const SolverLaunch<double>&);
-template cudaError_t solver_prepare<float>(const SolverLaunch<float>&);
 template cudaError_t solver_step<double>(const SolverLaunch<double>&, cudaStream_t);
 template cudaError_t solver_step<float>(const SolverLaunch<float>&, cudaStream_t);
 template cudaError_t solver_evaluate_candidate<double>(const SolverLaunch<double>&, InertialLin<double>, cudaStream_t);

@@ -16,7 +16,7 @@
 #include <cmath>
 #include <cstring>
 #include <new>
-#include <unordered_map>
+#include <numeric>
 #include <vector>
 
 #include "../../include/maplab_ba.h"
@@ -275,8 +275,7 @@ mba_status run_solve(mba_handle* h, const mba_solver_options& o, mba_summary* su
   if (ms != MBA_OK) return ms;
   SolverLaunch<T> s = make_launch<T>(h, b, o);
   cudaStream_t st = h->stream;
-  cudaError_t e = solver_prepare<T>(s);
-  if (e != cudaSuccess) return cuda_status(e);
+  cudaError_t e = cudaSuccess;
   cudaEvent_t ev0, ev1;
   cudaEventCreate(&ev0);
   cudaEventCreate(&ev1);
@@ -615,69 +614,67 @@ mba_status mba_create(const mba_problem_desc* d, int32_t device, mba_handle** ou
   PairMap pm(std::max<int64_t>(1024, N + NE));
   for (int64_t s = 0; s < N; ++s)
     if (otype[s] != MBA_LOCAL_KEYFRAME) obs_pblk[s] = pm.get(ost[s], okf[s]);
-  // Slot pairs, grouped: landmarks ordered by store keyframe and packed into
-  // groups whose pairs touch at most kSchurGroupTargets distinct S blocks, so
-  // one thread block accumulates a group in shared memory.  A landmark whose
-  // own pairs exceed the cap keeps its pairs in the group with local id -1
-  // (direct global accumulation).
-  std::vector<int32_t> pa, pb, pt, ploc;
-  std::vector<int64_t> grp_pair_off(1, 0), grp_tgt_off(1, 0);
-  std::vector<int32_t> grp_tgt;
-  pa.reserve(npair_est); pb.reserve(npair_est); pt.reserve(npair_est); ploc.reserve(npair_est);
+  // Slot pairs, sorted by the S block they update.  Targets are diagonal
+  // blocks (kf, kf) -> id kf, and upper blocks (i < j) -> id NK + block; an
+  // upper pair is oriented so slot_kf[a] < slot_kf[b] (W_a^T V W_b is
+  // transposed by swapping a and b, V being symmetric).  Targets are ordered
+  // by (i, j) so consecutive targets touch landmarks of nearby keyframes, and
+  // each target's pairs are cut into chunks of at most kSchurChunk pairs,
+  // one chunk per thread.
+  std::vector<int32_t> pa, pb;
+  std::vector<int32_t> chunk_tgt;
+  std::vector<int64_t> chunk_off;
   {
-    std::vector<int64_t> lm_order;
-    lm_order.reserve(NL);
-    for (int64_t l = 0; l < NL; ++l)
-      if (lm_active[l]) lm_order.push_back(l);
-    std::stable_sort(lm_order.begin(), lm_order.end(), [&](int64_t a, int64_t b) {
-      return d->lm_store_keyframe[a] < d->lm_store_keyframe[b];
-    });
-    std::vector<int32_t> lt;  // global targets of one landmark's pairs
-    std::unordered_map<int32_t, int32_t> local;  // target -> local id in the open group
-    auto close_group = [&]() {
-      if ((int64_t)pa.size() == grp_pair_off.back()) return;
-      grp_pair_off.push_back((int64_t)pa.size());
-      grp_tgt_off.push_back((int64_t)grp_tgt.size());
-      local.clear();
-    };
-    for (int64_t l : lm_order) {
-      lt.clear();
-      for (int64_t a = slot_off[l]; a < slot_off[l + 1]; ++a)
-        for (int64_t b = a; b < slot_off[l + 1]; ++b) {
-          const int32_t ka = slot_kf[a], kb = slot_kf[b];
-          lt.push_back(ka == kb ? -(ka + 1) : pm.get(ka, kb));
-        }
-      int32_t fresh = 0;
-      {
-        std::vector<int32_t> u(lt);
-        std::sort(u.begin(), u.end());
-        u.erase(std::unique(u.begin(), u.end()), u.end());
-        for (int32_t t : u) fresh += local.count(t) ? 0 : 1;
-        if ((int64_t)u.size() > kSchurGroupTargets) fresh = -1;  // too large for any group
-      }
-      if (fresh >= 0 && (int64_t)local.size() + fresh > kSchurGroupTargets) close_group();
-      size_t q = 0;
-      for (int64_t a = slot_off[l]; a < slot_off[l + 1]; ++a)
-        for (int64_t b = a; b < slot_off[l + 1]; ++b, ++q) {
-          const int32_t t = lt[q];
-          int32_t id = -1;
-          if (fresh >= 0) {
-            auto it = local.find(t);
-            if (it == local.end()) {
-              id = (int32_t)local.size();
-              local.emplace(t, id);
-              grp_tgt.push_back(t);
-            } else {
-              id = it->second;
-            }
+    std::vector<int32_t> ta, tb;
+    std::vector<int64_t> tt;
+    ta.reserve(npair_est); tb.reserve(npair_est); tt.reserve(npair_est);
+    for (int64_t l = 0; l < NL; ++l) {
+      if (!lm_active[l]) continue;
+      for (int64_t x = slot_off[l]; x < slot_off[l + 1]; ++x)
+        for (int64_t y = x; y < slot_off[l + 1]; ++y) {
+          const int32_t kx = slot_kf[x], ky = slot_kf[y];
+          if (kx == ky) {
+            ta.push_back((int32_t)x); tb.push_back((int32_t)y); tt.push_back(kx);
+          } else {
+            const int32_t blk = pm.get(kx, ky);
+            if (kx < ky) { ta.push_back((int32_t)x); tb.push_back((int32_t)y); }
+            else { ta.push_back((int32_t)y); tb.push_back((int32_t)x); }
+            tt.push_back(NK + blk);
           }
-          pa.push_back((int32_t)a);
-          pb.push_back((int32_t)b);
-          pt.push_back(t);
-          ploc.push_back(id);
         }
     }
-    close_group();
+    // Target order by (i, j); rank[target id] = position.
+    const int64_t ntgt = NK + pm.count;
+    std::vector<int64_t> order(ntgt);
+    std::iota(order.begin(), order.end(), 0);
+    auto key = [&](int64_t t) -> int64_t {
+      if (t < NK) return t * NK + t;
+      return (int64_t)pm.bi[t - NK] * NK + pm.bj[t - NK];
+    };
+    std::sort(order.begin(), order.end(), [&](int64_t x, int64_t y) { return key(x) < key(y); });
+    std::vector<int64_t> rank(ntgt), cnt(ntgt + 1, 0);
+    for (int64_t r = 0; r < ntgt; ++r) rank[order[r]] = r;
+    for (int64_t t : tt) cnt[rank[t] + 1]++;
+    for (int64_t r = 0; r < ntgt; ++r) cnt[r + 1] += cnt[r];
+    const int64_t np = (int64_t)tt.size();
+    pa.resize(np); pb.resize(np);
+    {
+      std::vector<int64_t> fill(cnt.begin(), cnt.end() - 1);
+      for (int64_t q = 0; q < np; ++q) {
+        const int64_t dst = fill[rank[tt[q]]]++;
+        pa[dst] = ta[q]; pb[dst] = tb[q];
+      }
+    }
+    chunk_off.push_back(0);
+    for (int64_t r = 0; r < ntgt; ++r) {
+      const int64_t b0 = cnt[r], b1 = cnt[r + 1];
+      if (b1 == b0) continue;
+      const bool whole = b1 - b0 <= kSchurChunk;
+      for (int64_t c0 = b0; c0 < b1; c0 += kSchurChunk) {
+        chunk_tgt.push_back(whole ? (int32_t)order[r] : ~(int32_t)order[r]);
+        chunk_off.push_back(std::min(b1, c0 + kSchurChunk));
+      }
+    }
   }
   const int64_t npu = pm.count;
   std::vector<int64_t> row_off(NK + 1, 0);
@@ -813,15 +810,9 @@ mba_status mba_create(const mba_problem_desc* d, int32_t device, mba_handle** ou
   S.obs_pblk = A.upload(obs_pblk, st);
   S.pair_a = A.upload(pa, st);
   S.pair_b = A.upload(pb, st);
-  S.pair_t = A.upload(pt, st);
-  S.pair_loc = A.upload(ploc, st);
-  S.ngroup = (int64_t)grp_pair_off.size() - 1;
-  S.grp_pair_off = A.upload(grp_pair_off, st);
-  S.grp_tgt_off = A.upload(grp_tgt_off, st);
-  S.grp_tgt = A.upload(grp_tgt, st);
-  S.max_group_targets = 0;
-  for (int64_t g = 0; g < S.ngroup; ++g)
-    S.max_group_targets = std::max<int64_t>(S.max_group_targets, grp_tgt_off[g + 1] - grp_tgt_off[g]);
+  S.nchunk = (int64_t)chunk_tgt.size();
+  S.chunk_tgt = A.upload(chunk_tgt, st);
+  S.chunk_off = A.upload(chunk_off, st);
   S.pu_i = A.upload(pm.bi, st);
   S.pu_j = A.upload(pm.bj, st);
   S.row_off = A.upload(row_off, st);

@@ -8,8 +8,9 @@
 
 namespace mba {
 
-// Distinct S blocks a pair group may touch (shared-memory accumulator size).
-constexpr int64_t kSchurGroupTargets = 256;
+// Slot pairs per thread of the Schur pair kernel (a target with more pairs
+// is split into several chunks that add atomically).
+constexpr int64_t kSchurChunk = 16;
 
 // Static sparsity of the reduced camera system, built on the host at create.
 struct SchurPattern {
@@ -21,15 +22,12 @@ struct SchurPattern {
   int32_t* slot_lm;       // [nslot]
   int32_t* obs_slot;      // [nobs] slot of the observer, -1 for kLocalKeyframe
   int32_t* obs_pblk;      // [nobs] upper block of (store, observer), -1 for kLocalKeyframe
-  int32_t* pair_a;        // [npair] global slot ids
+  int64_t nchunk = 0;     // pair chunks (contiguous pair ranges of one target)
+  int32_t* pair_a;        // [npair] global slot ids, sorted by target; slot_kf[a] <= slot_kf[b]
   int32_t* pair_b;
-  int32_t* pair_t;        // >= 0: upper block index; < 0: -(kf+1) diagonal block
-  int32_t* pair_loc;      // [npair] target id local to the pair's group, -1 = accumulate globally
-  int64_t ngroup = 0;     // pair groups (contiguous pair ranges, landmarks ordered by store keyframe)
-  int64_t max_group_targets = 0;
-  int64_t* grp_pair_off;  // [ngroup+1]
-  int64_t* grp_tgt_off;   // [ngroup+1]
-  int32_t* grp_tgt;       // group-local target id -> pair_t code
+  int32_t* chunk_tgt;     // [nchunk] target id (kf for diagonal, nkf + upper block);
+                          //   bitwise-not of it when the target spans several chunks
+  int64_t* chunk_off;     // [nchunk+1] pair range of each chunk
   int32_t* pu_i;          // [npu]
   int32_t* pu_j;
   int64_t* row_off;       // [nkf+1] full (both orientations) pose-pose rows
@@ -84,7 +82,7 @@ template <typename T>
 struct LinearSystem {
   T* Hll;    // [9][nlm]
   T* gl;     // [3][nlm]
-  T* Wslot;  // [18][nslot]
+  T* Wslot;  // [nslot][18] slot-major
   T* Dbase;  // [nkf][225]
   T* Pbase;  // [npu][36]
   T* Ebase;  // [nedge][225]
@@ -94,7 +92,7 @@ struct LinearSystem {
   T* SE;     // [nedge][225]
   T* rhs;    // [nkf*15]
   T* V;      // [9][nlm]
-  T* U;      // [18][nslot]
+  T* U;      // [nslot][18] slot-major
   T* Minv;       // [nkf][225] block-Jacobi inverses (factorized and inverted in FP64)
   T *x, *r, *z, *p, *q, *q2;  // [nkf*15]; p and q2 double-buffer the PCG direction
   double* dl;    // [3][nlm] scaled landmark step
@@ -127,10 +125,6 @@ template <typename T>
 cudaError_t solver_assemble(const SolverLaunch<T>& s, const int* gate, cudaStream_t st);
 template <typename T>
 cudaError_t solver_compute_scale(const SolverLaunch<T>& s, int jacobi, cudaStream_t st);
-// Host-side kernel attributes; call before the first solver_step (not
-// during stream capture).
-template <typename T>
-cudaError_t solver_prepare(const SolverLaunch<T>& s);
 template <typename T>
 cudaError_t solver_step(const SolverLaunch<T>& s, cudaStream_t st);
 template <typename T>
