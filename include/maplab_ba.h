@@ -136,7 +136,14 @@ typedef struct mba_problem_desc {
  * (include/map-optimization/solver-options.h:26-75), same names and defaults
  * as the ba_* gflags (src/solver-options.cc:3-52). */
 enum { MBA_LINEAR_SOLVER_PCG = 0, MBA_LINEAR_SOLVER_DENSE_SCHUR = 1 };
-enum { MBA_PRECOND_BLOCK_JACOBI = 0, MBA_PRECOND_LEARNED = 1 };
+/* Preconditioners of the reduced camera system's PCG: block-Jacobi (15x15
+ * keyframe blocks, the plain method); CHAIN: block-Jacobi corrected by the
+ * couplings between consecutive keyframes of each trajectory (a
+ * block-tridiagonal matrix solved by cyclic reduction, fixed coefficients);
+ * LEARNED: the same correction with coefficients predicted per keyframe by a
+ * graph network over the co-visibility graph.  CHAIN and LEARNED fall back to
+ * block-Jacobi for any LM iteration whose correction is not positive definite. */
+enum { MBA_PRECOND_BLOCK_JACOBI = 0, MBA_PRECOND_LEARNED = 1, MBA_PRECOND_CHAIN = 2 };
 enum { MBA_PRECISION_FP64 = 0, MBA_PRECISION_MIXED = 1 };
 
 typedef struct mba_solver_options {
@@ -159,6 +166,13 @@ typedef struct mba_solver_options {
   int32_t use_cuda_graph;              /* capture each LM iteration as a graph */
   int32_t check_tolerances;            /* 1: stop on function/gradient/parameter tolerance */
   double stop_cost;                    /* >0: stop as soon as cost <= stop_cost */
+  /* Outlier-landmark rejection (outlier-rejection-solver.cc): every n
+   * iterations the solve restarts after removing the landmarks seen at depth
+   * <= 0 (or, optionally, with a reprojection error above the threshold).
+   * ba_use_visual_outlier_rejection_solver = true, n = 3; 0 disables. */
+  int32_t reject_outliers_every_n_iters;     /* ba_outlier_rejection_reject_every_n_iters = 3 */
+  int32_t outlier_use_reprojection_error;    /* ba_outlier_rejection_use_reprojection_error = 0 */
+  double outlier_max_reprojection_error_px;  /* ba_outlier_rejection_max_reprojection_error_px = 50 */
 } mba_solver_options;
 
 /* Mirrors the columns of ceres::IterationSummary printed by maplab's
@@ -188,7 +202,7 @@ typedef struct mba_summary {
   double total_time_ms;
   double time_to_stop_cost_ms;    /* -1 if stop_cost was not reached */
   int32_t max_iterations_capacity;/* caller sets: length of `iterations` */
-  int32_t pad_;
+  int32_t num_rejected_landmarks; /* outlier landmarks removed during this solve */
   mba_iteration_summary* iterations; /* caller-owned, may be NULL */
 } mba_summary;
 
@@ -261,6 +275,29 @@ void mba_cancel(mba_handle* h);
  * mode 0: FP64 tangent linearization, 1: FP32 tangent linearization.
  * Writes the mean milliseconds per launch. */
 mba_status mba_time_visual_kernel(mba_handle* h, int32_t mode, int32_t iters, double* ms_per_launch);
+
+/* The damped reduced camera system of the current state, as one LM iteration
+ * builds it (the matrix Ceres's SchurEliminator forms internally for
+ * SPARSE_SCHUR / ITERATIVE_SCHUR, linear_solver/schur_eliminator.h; maplab has
+ * no interface to it, so this entry point has no reference counterpart).
+ * Jacobi-scaled like the solver's system, LM-damped with trust-region radius
+ * `radius`, fixed tangent dims as identity rows with zero right-hand side.
+ * Keyframe blocks are 15x15 in the order (theta, p, v, b_g, b_a).
+ * Host outputs, FP64, each may be NULL:
+ *   diag [N_kf][15][15];
+ *   upper_ij [N_pu][2] keyframe pairs (i < j) and upper [N_pu][6][6], the
+ *     pose-pose (theta, p) block of row i, column j,
+ *     N_pu = mba_problem_stats.num_schur_pose_blocks / 2;
+ *   inertial [N_edge][15][15], row = edge's from keyframe, column = to;
+ *   rhs [N_kf][15].
+ * precision MBA_PRECISION_FP64 or MBA_PRECISION_MIXED (FP32 system). */
+mba_status mba_reduced_system(mba_handle* h, int32_t precision, double radius, double* diag, int32_t* upper_ij,
+                              double* upper, double* inertial, double* rhs);
+
+/* Landmarks rejected as outliers by the solves run on this handle so far
+ * (Landmark::Quality::kBad in maplab): flags [N_lm] (1 = rejected, may be
+ * NULL) and their count.  Rejected landmarks stay out of later solves. */
+mba_status mba_rejected_landmarks(mba_handle* h, uint8_t* flags, int64_t* count);
 
 /* Problem statistics (for reports): sizes of the reduced camera system. */
 typedef struct mba_problem_stats {

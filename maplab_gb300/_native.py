@@ -41,7 +41,7 @@ MBA_KF_POSITION_CONSTANT = 1 << 5
 MBA_KF_ROTATION_CONSTANT = 1 << 6
 
 MBA_LINEAR_SOLVER_PCG, MBA_LINEAR_SOLVER_DENSE_SCHUR = 0, 1
-MBA_PRECOND_BLOCK_JACOBI, MBA_PRECOND_LEARNED = 0, 1
+MBA_PRECOND_BLOCK_JACOBI, MBA_PRECOND_LEARNED, MBA_PRECOND_CHAIN = 0, 1, 2
 MBA_PRECISION_FP64, MBA_PRECISION_MIXED = 0, 1
 
 MBA_SYNTH_LANDMARKS_BOX, MBA_SYNTH_LANDMARKS_FRUSTUM = 0, 1
@@ -123,6 +123,9 @@ class SolverOptions(ctypes.Structure):
         ("use_cuda_graph", ctypes.c_int32),
         ("check_tolerances", ctypes.c_int32),
         ("stop_cost", ctypes.c_double),
+        ("reject_outliers_every_n_iters", ctypes.c_int32),
+        ("outlier_use_reprojection_error", ctypes.c_int32),
+        ("outlier_max_reprojection_error_px", ctypes.c_double),
     ]
 
 
@@ -153,7 +156,7 @@ class Summary(ctypes.Structure):
         ("total_time_ms", ctypes.c_double),
         ("time_to_stop_cost_ms", ctypes.c_double),
         ("max_iterations_capacity", ctypes.c_int32),
-        ("pad_", ctypes.c_int32),
+        ("num_rejected_landmarks", ctypes.c_int32),
         ("iterations", ctypes.POINTER(IterationSummary)),
     ]
 
@@ -284,6 +287,10 @@ def load_ba():
     _declare(lib, "mba_cancel", None, [vp])
     _declare(lib, "mba_time_visual_kernel", ctypes.c_int, [vp, ctypes.c_int32, ctypes.c_int32, c_double_p])
     _declare(lib, "mba_get_stats", ctypes.c_int, [vp, ctypes.POINTER(ProblemStats)])
+    _declare(lib, "mba_rejected_landmarks", ctypes.c_int, [vp, ctypes.POINTER(ctypes.c_uint8), ctypes.POINTER(ctypes.c_int64)])
+    _declare(lib, "mba_reduced_system", ctypes.c_int,
+             [vp, ctypes.c_int32, ctypes.c_double, c_double_p, ctypes.POINTER(ctypes.c_int32), c_double_p,
+              c_double_p, c_double_p])
     _declare(lib, "mba_visual_cost_noalloc", ctypes.c_int,
              [ctypes.POINTER(VisualBatchDevice), ctypes.c_int32, vp, vp])
     return lib
@@ -311,6 +318,9 @@ def default_solver_options(lib=None):
     o.use_cuda_graph = 1
     o.check_tolerances = 1
     o.stop_cost = 0.0
+    o.reject_outliers_every_n_iters = 3
+    o.outlier_use_reprojection_error = 0
+    o.outlier_max_reprojection_error_px = 50.0
     return o
 
 
@@ -330,8 +340,10 @@ def summary_dict(s):
         it = s.iterations[i]
         its.append({"iteration": it.iteration, "ok": bool(it.step_is_successful), "cost": it.cost,
                     "lin_iters": it.linear_solver_iterations, "radius": it.trust_region_radius,
-                    "relative_decrease": it.relative_decrease, "time_ms": it.iteration_time_ms})
+                    "relative_decrease": it.relative_decrease, "time_ms": it.iteration_time_ms,
+                    "cost_change": it.cost_change, "step_norm": it.step_norm})
     return {"num_iterations": s.num_iterations, "successful": s.num_successful_steps,
             "termination": s.termination, "linear_iterations": s.total_linear_iterations,
             "initial_cost": s.initial_cost, "final_cost": s.final_cost, "total_time_ms": s.total_time_ms,
-            "time_to_stop_cost_ms": s.time_to_stop_cost_ms, "iterations": its}
+            "time_to_stop_cost_ms": s.time_to_stop_cost_ms, "rejected_landmarks": s.num_rejected_landmarks,
+            "iterations": its}

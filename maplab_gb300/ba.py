@@ -134,5 +134,29 @@ class BundleAdjuster:
         _check(self._lib.mba_get_stats(self._h, ctypes.byref(s)), "mba_get_stats")
         return {f: getattr(s, f) for f, _ in s._fields_}
 
+    def reduced_system(self, precision=N.MBA_PRECISION_FP64, radius=1e5):
+        """Damped, Jacobi-scaled reduced camera system at the current state:
+        dict of diag [N_kf,15,15], upper_ij [N_pu,2], upper [N_pu,6,6],
+        inertial [N_e,15,15] (with edge_from / edge_to) and rhs [N_kf,15]."""
+        st = self.stats()
+        nk, ne, npu = st["num_keyframes"], st["num_imu_edges"], st["num_schur_pose_blocks"] // 2
+        D = np.zeros((nk, 15, 15)); ij = np.zeros((npu, 2), dtype=np.int32); U = np.zeros((npu, 6, 6))
+        E = np.zeros((ne, 15, 15)); b = np.zeros((nk, 15))
+        _check(self._lib.mba_reduced_system(self._h, precision, radius, N.ptr(D),
+                                            ij.ctypes.data_as(ctypes.POINTER(ctypes.c_int32)), N.ptr(U), N.ptr(E),
+                                            N.ptr(b)), "mba_reduced_system")
+        d = self.desc
+        ef = np.ctypeslib.as_array(d.edge_from, (ne,)).copy() if ne else np.zeros(0, np.int32)
+        et = np.ctypeslib.as_array(d.edge_to, (ne,)).copy() if ne else np.zeros(0, np.int32)
+        return dict(diag=D, upper_ij=ij, upper=U, inertial=E, edge_from=ef, edge_to=et, rhs=b)
+
+    def rejected_landmarks(self):
+        """(flags [N_lm] bool, count) of the landmarks rejected as outliers."""
+        flags = np.zeros(self.desc.num_landmarks, dtype=np.uint8)
+        c = ctypes.c_int64()
+        _check(self._lib.mba_rejected_landmarks(self._h, flags.ctypes.data_as(ctypes.POINTER(ctypes.c_uint8)),
+                                                ctypes.byref(c)), "mba_rejected_landmarks")
+        return flags.astype(bool), c.value
+
     def cancel(self):
         self._lib.mba_cancel(self._h)

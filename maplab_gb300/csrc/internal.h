@@ -27,6 +27,7 @@ struct DevProblem {
   double* lm_p;             // [nlm][4] (x, y, z, pad)
   const int64_t* lm_obs_off;// [nlm+1]
   const uint8_t* lm_active;
+  int32_t* lm_off;          // [nlm] 1 = rejected as an outlier: its terms are out of the problem
   // keyframes
   double* kf_state;         // [nkf][16] = q(4) p(3) v(3) b_g(3) b_a(3)
   const int32_t* kf_mis;
@@ -116,5 +117,11 @@ cudaError_t launch_inertial_v2(const DevProblem& P, const double* kf_state, bool
                                const int* skip_if, cudaStream_t s);
 cudaError_t launch_inertial_f32(const DevProblem& P, const InertialLin<double>& src, InertialLin<float> dst,
                                 cudaStream_t s);
+// Outlier landmarks at the current state (outlier-rejection-solver.cc:28-103):
+// a landmark goes out of the problem when one of its observations has depth
+// <= 0 in the observing camera or, if use_reprojection, a reprojection error
+// above max_px.  Newly rejected landmarks are counted into *count.
+cudaError_t launch_find_outliers(const DevProblem& P, int use_reprojection, double max_px, int* count,
+                                 const int* skip_if, cudaStream_t s);
 
 }  // namespace mba

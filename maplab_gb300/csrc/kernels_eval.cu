@@ -154,7 +154,7 @@ __global__ void __launch_bounds__(kBlock) k_visual_linearize(DevProblem P, Visua
     mv3(RCI, pI, pC);
     pC[0] += cam.p_CI[0]; pC[1] += cam.p_CI[1]; pC[2] += cam.p_CI[2];
     T kp[2], Jkp[6];
-    const bool failed = project<T>(cam, pC, kp, Jkp);
+    const bool failed = project<T>(cam, pC, kp, Jkp) || P.lm_off[lm];
     T r[2], Jl[6], Js[12], Jo[12];
 #pragma unroll
     for (int a = 0; a < 12; ++a) { Js[a] = T(0); Jo[a] = T(0); }
@@ -252,46 +252,53 @@ __global__ void __launch_bounds__(kBlock) k_visual_linearize(DevProblem P, Visua
 }
 
 // FP64 residual-only cost at an arbitrary state (candidate evaluation).
+// Landmark of observation i in the observing camera frame (FP64), following
+// the frame chain of the visual term for its error type.
+__device__ void obs_point_C(const DevProblem& P, const double* kf_state, const double* lm_p, int64_t i, double* pC) {
+  const int lm = P.obs_lm[i], kf = P.obs_kf[i], st = P.obs_store[i], type = P.obs_type[i];
+  const DevCamera& cam = P.cams[P.obs_cam[i]];
+  const double pB[3] = {lm_p[4 * (int64_t)lm], lm_p[4 * (int64_t)lm + 1], lm_p[4 * (int64_t)lm + 2]};
+  M3<double> RCI;
+  jplR(cam.q_CI, RCI);
+  double pI[3];
+  if (type == MBA_LOCAL_KEYFRAME) {
+    pI[0] = pB[0]; pI[1] = pB[1]; pI[2] = pB[2];
+  } else {
+    const double* xs = kf_state + 16 * (int64_t)st;
+    const double* xo = kf_state + 16 * (int64_t)kf;
+    M3<double> RBLM, RIM;
+    jplR(xs, RBLM);
+    jplR(xo, RIM);
+    double pM[3];
+    mtv3(RBLM, pB, pM);
+    pM[0] += xs[4]; pM[1] += xs[5]; pM[2] += xs[6];
+    if (type == MBA_GLOBAL) {
+      const double* ml = P.mis + 8 * P.kf_mis[st];
+      const double* mo = P.mis + 8 * P.kf_mis[kf];
+      M3<double> RGLM, RGM;
+      jplR(ml, RGLM);
+      jplR(mo, RGM);
+      double pG[3];
+      mv3(RGLM, pM, pG);
+      pG[0] += ml[4] - mo[4]; pG[1] += ml[5] - mo[5]; pG[2] += ml[6] - mo[6];
+      mtv3(RGM, pG, pM);
+    }
+    const double d[3] = {pM[0] - xo[4], pM[1] - xo[5], pM[2] - xo[6]};
+    mv3(RIM, d, pI);
+  }
+  mv3(RCI, pI, pC);
+  pC[0] += cam.p_CI[0]; pC[1] += cam.p_CI[1]; pC[2] += cam.p_CI[2];
+}
+
 __global__ void __launch_bounds__(kBlock) k_visual_cost(DevProblem P, const double* kf_state, const double* lm_p,
                                                         double* cost_accum, int* nonfinite, const int* skip_if) {
   if (gated(nullptr, skip_if)) return;
   const int64_t i = blockIdx.x * (int64_t)blockDim.x + threadIdx.x;
   double cost = 0.0;
-  if (i < P.nobs) {
-    const int lm = P.obs_lm[i], kf = P.obs_kf[i], st = P.obs_store[i], type = P.obs_type[i];
+  if (i < P.nobs && !P.lm_off[P.obs_lm[i]]) {
     const DevCamera& cam = P.cams[P.obs_cam[i]];
-    const double pB[3] = {lm_p[4 * (int64_t)lm], lm_p[4 * (int64_t)lm + 1], lm_p[4 * (int64_t)lm + 2]};
-    M3<double> RCI;
-    jplR(cam.q_CI, RCI);
-    double pI[3];
-    if (type == MBA_LOCAL_KEYFRAME) {
-      pI[0] = pB[0]; pI[1] = pB[1]; pI[2] = pB[2];
-    } else {
-      const double* xs = kf_state + 16 * (int64_t)st;
-      const double* xo = kf_state + 16 * (int64_t)kf;
-      M3<double> RBLM, RIM;
-      jplR(xs, RBLM);
-      jplR(xo, RIM);
-      double pM[3];
-      mtv3(RBLM, pB, pM);
-      pM[0] += xs[4]; pM[1] += xs[5]; pM[2] += xs[6];
-      if (type == MBA_GLOBAL) {
-        const double* ml = P.mis + 8 * P.kf_mis[st];
-        const double* mo = P.mis + 8 * P.kf_mis[kf];
-        M3<double> RGLM, RGM;
-        jplR(ml, RGLM);
-        jplR(mo, RGM);
-        double pG[3];
-        mv3(RGLM, pM, pG);
-        pG[0] += ml[4] - mo[4]; pG[1] += ml[5] - mo[5]; pG[2] += ml[6] - mo[6];
-        mtv3(RGM, pG, pM);
-      }
-      const double d[3] = {pM[0] - xo[4], pM[1] - xo[5], pM[2] - xo[6]};
-      mv3(RIM, d, pI);
-    }
     double pC[3];
-    mv3(RCI, pI, pC);
-    pC[0] += cam.p_CI[0]; pC[1] += cam.p_CI[1]; pC[2] += cam.p_CI[2];
+    obs_point_C(P, kf_state, lm_p, i, pC);
     double kp[2];
     const bool failed = project<double>(cam, pC, kp, nullptr);
     if (!failed) {
@@ -306,6 +313,29 @@ __global__ void __launch_bounds__(kBlock) k_visual_cost(DevProblem P, const doub
     }
   }
   block_accumulate(cost, cost_accum);
+}
+
+// Outlier test per observation (outlier-rejection-solver.cc:28-103): depth
+// p_C.z <= 0, or (optionally) squared reprojection error in pixels above
+// max_px^2, marks the landmark.  Landmarks already out are skipped.
+__global__ void __launch_bounds__(kBlock) k_find_outliers(DevProblem P, int use_reprojection, double max_px2,
+                                                          int* count, const int* skip_if) {
+  if (gated(nullptr, skip_if)) return;
+  const int64_t i = blockIdx.x * (int64_t)blockDim.x + threadIdx.x;
+  if (i >= P.nobs) return;
+  const int lm = P.obs_lm[i];
+  if (P.lm_off[lm]) return;
+  double pC[3];
+  obs_point_C(P, P.kf_state, P.lm_p, i, pC);
+  bool out = !(pC[2] > 0.0);
+  if (!out && use_reprojection) {
+    double kp[2];
+    project<double>(P.cams[P.obs_cam[i]], pC, kp, nullptr);
+    const double2 uv = P.obs_uv[i];
+    const double e0 = kp[0] - uv.x, e1 = kp[1] - uv.y;
+    out = !(e0 * e0 + e1 * e1 <= max_px2);
+  }
+  if (out && atomicExch(&P.lm_off[lm], 1) == 0) atomicAdd(count, 1);
 }
 
 // Distortion-parameter Jacobian at the undistorted normalized point
@@ -524,6 +554,14 @@ template cudaError_t launch_visual_linearize_gated<double>(const DevProblem&, Vi
                                                            const int*, cudaStream_t);
 template cudaError_t launch_visual_linearize_gated<float>(const DevProblem&, VisualLin<float>, double*, const int*,
                                                           const int*, cudaStream_t);
+
+cudaError_t launch_find_outliers(const DevProblem& P, int use_reprojection, double max_px, int* count,
+                                 const int* skip_if, cudaStream_t s) {
+  if (P.nobs == 0) return cudaSuccess;
+  const int64_t blocks = (P.nobs + kBlock - 1) / kBlock;
+  k_find_outliers<<<(unsigned)blocks, kBlock, 0, s>>>(P, use_reprojection, max_px * max_px, count, skip_if);
+  return cudaGetLastError();
+}
 
 cudaError_t launch_visual_cost_gated(const DevProblem& P, const double* kf_state, const double* lm_p,
                                      double* cost_accum, int* nonfinite, const int* skip_if, cudaStream_t s) {

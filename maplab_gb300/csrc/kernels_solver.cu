@@ -278,12 +278,14 @@ __global__ void __launch_bounds__(kB) k_build_system(SolverLaunch<T> s) {
     ctl->status = 0;
     ctl->model_change = 0.0;
     ctl->cost_cand = 0.0;
+    ctl->cost_cand_ine = 0.0;
     ctl->step_norm2 = 0.0;
     ctl->x_norm2 = 0.0;
     ctl->nonfinite = 0;
     ctl->inertial_status = 0;
     ctl->pcg_done = 0;
     ctl->pcg_iters = 0;
+    ctl->chain_failed = 0;
     ctl->pcg_rz0 = 0.0;
     ctl->pcg_bnorm2 = 0.0;
     for (int a = 0; a < 3; ++a) { ctl->pcg_pq[a] = 0.0; ctl->pcg_rr[a] = 0.0; ctl->pcg_rz[a] = 0.0; }
@@ -499,23 +501,28 @@ __global__ void __launch_bounds__(64) k_block_jacobi(SolverLaunch<T> s) {
 }
 
 // ------------------------------------------------------------ PCG
+// x = 0, r = b, z = M b (block-Jacobi here; the chain sweeps write z and
+// rz0 afterwards when the chain preconditioner is active).
 template <typename T>
 __global__ void __launch_bounds__(kB) k_pcg_init(SolverLaunch<T> s) {
   if (s.ctl->terminated) return;
   const int64_t i = blockIdx.x * (int64_t)blockDim.x + threadIdx.x;
   const int64_t n = 15 * s.P.nkf;
+  const bool chain = s.precond != MBA_PRECOND_BLOCK_JACOBI && !s.ctl->chain_failed;
   double rz = 0.0, rr = 0.0;
   if (i < n) {
     const int64_t k = i / 15, a = i % 15;
-    const T* M = s.L.Minv + 225 * k;
-    double z = 0.0;
-    for (int b = 0; b < 15; ++b) z += (double)M[15 * a + b] * (double)s.L.rhs[15 * k + b];
     const double r = (double)s.L.rhs[i];
+    double z = 0.0;
+    if (!chain) {
+      const T* M = s.L.Minv + 225 * k;
+      for (int b = 0; b < 15; ++b) z += (double)M[15 * a + b] * (double)s.L.rhs[15 * k + b];
+      rz = r * z;
+    }
     s.L.x[i] = T(0);
     s.L.r[i] = T(r);
     s.L.z[i] = T(z);
-    s.L.p[i] = T(z);  // read with beta = 0 by the first product; must be finite
-    rz = r * z;
+    s.L.p[i] = T(0);  // read with beta = 0 by the first product; must be finite
     rr = r * r;
   }
   block_add(rz, &s.ctl->pcg_rz0);
@@ -616,6 +623,7 @@ __global__ void __launch_bounds__(kB) k_pcg_update(SolverLaunch<T> s, int it, co
   double rr = 0.0, rz = 0.0;
   T rnew = T(0);
   const bool act = (k < s.P.nkf) && a < 15;
+  const bool chain = s.precond != MBA_PRECOND_BLOCK_JACOBI && !ctl->chain_failed;
   if (act) {
     const int64_t i = 15 * k + a;
     s.L.x[i] = s.L.x[i] + alpha * p[i];
@@ -624,7 +632,8 @@ __global__ void __launch_bounds__(kB) k_pcg_update(SolverLaunch<T> s, int it, co
   }
   rsh[threadIdx.x] = rnew;
   __syncthreads();
-  if (act) {
+  if (act && chain) rr = (double)rnew * (double)rnew;  // z and r.z come from the chain sweeps
+  if (act && !chain) {
     const T* M = s.L.Minv + 225 * k + 15 * a;
     const int base = threadIdx.x & ~15;
     T z = T(0);
@@ -785,7 +794,7 @@ __global__ void k_decide(LmControl* ctl, LmParams prm, mba_iteration_summary* lo
   const int it = ++ctl->iteration;
   const double mcc = ctl->model_change;
   const double cost = ctl->cost;
-  double new_cost = ctl->cost_cand;
+  double new_cost = ctl->cost_cand + ctl->cost_cand_ine;
   if (ctl->nonfinite || ctl->inertial_status || !isfinite(new_cost)) new_cost = INFINITY;
   const bool valid = ctl->status == 0 && mcc > 0.0 && isfinite(mcc);
   int ok = 0;
@@ -804,6 +813,7 @@ __global__ void k_decide(LmControl* ctl, LmParams prm, mba_iteration_summary* lo
   }
   if (ok) {
     ctl->cost = new_cost;
+    ctl->cost_ine = ctl->cost_cand_ine;
     ctl->num_successful++;
     if (!ctl->terminated) {
       double r = ctl->radius / fmax(1.0 / 3.0, 1.0 - pow(2.0 * rel - 1.0, 3.0));
@@ -879,7 +889,13 @@ __global__ void k_init_control(LmControl* ctl, double radius) {
   ctl->total_pcg = 0;
   ctl->status = 0;
   ctl->stop_iteration = -1;
+  ctl->rejected = 0;
+  ctl->reject_count = 0;
+  ctl->cost_ine = 0.0;
+  ctl->cost_cand_ine = 0.0;
 }
+
+__global__ void k_add_inertial_cost(LmControl* ctl) { ctl->cost += ctl->cost_ine; }
 
 template <typename T>
 __global__ void k_copy_cast(const double* a, T* b, int64_t n) {
@@ -897,6 +913,11 @@ inline unsigned gridcap(int64_t n) {
 
 cudaError_t solver_init_control(LmControl* ctl, double radius, cudaStream_t st) {
   k_init_control<<<1, 1, 0, st>>>(ctl, radius);
+  return cudaGetLastError();
+}
+
+cudaError_t solver_add_inertial_cost(LmControl* ctl, cudaStream_t st) {
+  k_add_inertial_cost<<<1, 1, 0, st>>>(ctl);
   return cudaGetLastError();
 }
 
@@ -927,7 +948,7 @@ cudaError_t solver_compute_scale(const SolverLaunch<T>& s, int jacobi, cudaStrea
 }
 
 template <typename T>
-cudaError_t solver_step(const SolverLaunch<T>& s, cudaStream_t st) {
+cudaError_t solver_build_reduced(const SolverLaunch<T>& s, cudaStream_t st) {
   const int64_t nsys = 225 * s.P.nkf + 225 * s.P.nedge + 36 * s.S.npu + 15 * s.P.nkf;
   k_build_system<T><<<gridcap(nsys), kB, 0, st>>>(s);
   if (s.P.nlm) k_schur_lm<T><<<nblk(s.P.nlm, kB), kB, 0, st>>>(s);
@@ -935,14 +956,35 @@ cudaError_t solver_step(const SolverLaunch<T>& s, cudaStream_t st) {
   if (s.S.nchunk) k_schur_pairs<T><<<nblk(s.S.nchunk, kB), kB, 0, st>>>(s);
   k_finalize_system<T><<<gridcap(nsys), kB, 0, st>>>(s);
   k_block_jacobi<T><<<nblk(s.P.nkf, 64), 64, 0, st>>>(s);
+  if (s.precond != MBA_PRECOND_BLOCK_JACOBI) {
+    cudaError_t e = cudaGetLastError();
+    if (e != cudaSuccess) return e;
+    return chain_factor<T>(s, st);
+  }
+  return cudaGetLastError();
+}
+
+template <typename T>
+cudaError_t solver_step(const SolverLaunch<T>& s, cudaStream_t st) {
+  cudaError_t e = solver_build_reduced<T>(s, st);
+  if (e != cudaSuccess) return e;
   const int64_t n = 15 * s.P.nkf;
   k_pcg_init<T><<<nblk(n, kB), kB, 0, st>>>(s);
+  const bool chain = s.precond != MBA_PRECOND_BLOCK_JACOBI;
+  if (chain) {
+    e = chain_apply<T>(s, s.L.r, s.L.z, &s.ctl->pcg_rz0, st);
+    if (e != cudaSuccess) return e;
+  }
   const int maxit = s.prm.max_linear_iterations;
   for (int it = 0; it < maxit; ++it) {
     T* pa = (it & 1) ? s.L.q2 : s.L.p;
     T* pb = (it & 1) ? s.L.p : s.L.q2;
     k_pcg_spmv<T><<<nblk(32 * s.P.nkf, 128), 128, 0, st>>>(s, it, pa, pb);
     k_pcg_update<T><<<nblk(16 * s.P.nkf, kB), kB, 0, st>>>(s, it, pb, it == maxit - 1);
+    if (chain) {
+      e = chain_apply<T>(s, s.L.r, s.L.z, &s.ctl->pcg_rz[it % 3], st);
+      if (e != cudaSuccess) return e;
+    }
   }
   if (s.P.nlm) k_backsub<T><<<nblk(s.P.nlm, kB), kB, 0, st>>>(s);
   if (s.P.nobs) k_model_visual<T><<<nblk(s.P.nobs, kB), kB, 0, st>>>(s);
@@ -957,7 +999,7 @@ cudaError_t solver_evaluate_candidate(const SolverLaunch<T>& s, InertialLin<doub
                                            &s.ctl->terminated, st);
   if (e != cudaSuccess) return e;
   // Mixed path: Phi / Q propagated in FP32 (state, Cholesky, residual FP64).
-  return launch_inertial_gated(s.P, s.kf_cand, ine_cand, &s.ctl->cost_cand, &s.ctl->inertial_status,
+  return launch_inertial_gated(s.P, s.kf_cand, ine_cand, &s.ctl->cost_cand_ine, &s.ctl->inertial_status,
                                &s.ctl->terminated, st, sizeof(T) == 4);
 }
 
@@ -978,10 +1020,42 @@ cudaError_t solver_relinearize(const SolverLaunch<T>& s, const InertialLin<doubl
   return solver_assemble<T>(s, &s.ctl->accepted, st);
 }
 
+__global__ void k_restart_begin(LmControl* ctl) {
+  if (ctl->terminated) return;
+  ctl->cost = 0.0;
+}
+
+__global__ void k_restart_end(LmControl* ctl, const int* count) {
+  if (ctl->terminated) return;
+  ctl->cost += ctl->cost_ine;
+  ctl->decrease_factor = 2.0;
+  ctl->rejected += *count;
+}
+
+template <typename T>
+cudaError_t solver_reject_and_restart(const SolverLaunch<T>& s, int use_reprojection, double max_px, int jacobi,
+                                      cudaStream_t st) {
+  LmControl* c = s.ctl;
+  int* count = &c->reject_count;
+  cudaError_t e = cudaMemsetAsync(count, 0, sizeof(int), st);
+  if (e == cudaSuccess) e = launch_find_outliers(s.P, use_reprojection, max_px, count, &c->terminated, st);
+  if (e != cudaSuccess) return e;
+  k_restart_begin<<<1, 1, 0, st>>>(c);
+  e = launch_visual_cost_gated(s.P, s.P.kf_state, s.P.lm_p, &c->cost, nullptr, &c->terminated, st);
+  if (e != cudaSuccess) return e;
+  k_restart_end<<<1, 1, 0, st>>>(c, count);
+  e = launch_visual_linearize_gated<T>(s.P, s.vis, nullptr, nullptr, &c->terminated, st);
+  if (e == cudaSuccess) e = solver_assemble<T>(s, nullptr, st);
+  if (e == cudaSuccess) e = solver_compute_scale<T>(s, jacobi, st);
+  return e;
+}
+
 template cudaError_t solver_assemble<double>(const SolverLaunch<double>&, const int*, cudaStream_t);
 template cudaError_t solver_assemble<float>(const SolverLaunch<float>&, const int*, cudaStream_t);
 template cudaError_t solver_compute_scale<double>(const SolverLaunch<double>&, int, cudaStream_t);
 template cudaError_t solver_compute_scale<float>(const SolverLaunch<float>&, int, cudaStream_t);
+template cudaError_t solver_build_reduced<double>(const SolverLaunch<double>&, cudaStream_t);
+template cudaError_t solver_build_reduced<float>(const SolverLaunch<float>&, cudaStream_t);
 template cudaError_t solver_step<double>(const SolverLaunch<double>&, cudaStream_t);
 template cudaError_t solver_step<float>(const SolverLaunch<float>&, cudaStream_t);
 template cudaError_t solver_evaluate_candidate<double>(const SolverLaunch<double>&, InertialLin<double>, cudaStream_t);
@@ -992,5 +1066,7 @@ template cudaError_t solver_decide_and_accept<float>(const SolverLaunch<float>&,
                                                      InertialLin<double>, cudaStream_t);
 template cudaError_t solver_relinearize<double>(const SolverLaunch<double>&, const InertialLin<double>&, cudaStream_t);
 template cudaError_t solver_relinearize<float>(const SolverLaunch<float>&, const InertialLin<double>&, cudaStream_t);
+template cudaError_t solver_reject_and_restart<double>(const SolverLaunch<double>&, int, double, int, cudaStream_t);
+template cudaError_t solver_reject_and_restart<float>(const SolverLaunch<float>&, int, double, int, cudaStream_t);
 
 }  // namespace mba

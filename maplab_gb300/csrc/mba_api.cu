@@ -104,11 +104,24 @@ struct PairMap {
     bj.push_back(j);
     return count++;
   }
+  // Index of the (i, j) block, -1 if absent (no insertion).
+  int32_t find(int32_t i, int32_t j) const {
+    if (i > j) std::swap(i, j);
+    const uint64_t key = ((uint64_t)(uint32_t)i << 32) | (uint32_t)j;
+    uint64_t h = (key * 0x9E3779B97F4A7C15ull) & mask;
+    while (keys[h] != ~0ull) {
+      if (keys[h] == key) return vals[h];
+      h = (h + 1) & mask;
+    }
+    return -1;
+  }
 };
 
 template <typename T>
 struct SolverBuffers {
   bool ready = false;
+  bool chain_ready = false;
+  ChainSystem<T> C{};
   VisualLin<T> vis{};
   InertialLin<T> ine{};
   LinearSystem<T> L{};
@@ -195,6 +208,38 @@ mba_status ensure_solver_buffers(mba_handle* h, SolverBuffers<T>& b) {
   return MBA_OK;
 }
 
+// Chain-preconditioner factors (allocated on first use).  The FP64 arrays
+// double as the working-precision copies when T = double.
+template <typename T>
+mba_status ensure_chain_buffers(mba_handle* h, SolverBuffers<T>& b) {
+  if (b.chain_ready) return MBA_OK;
+  DeviceArena& A = h->arena;
+  const int64_t n = h->P.nkf;
+  ChainSystem<T>& C = b.C;
+  C.A = A.alloc<double>(225 * n);
+  C.B = A.alloc<double>(225 * n);
+  C.F64 = A.alloc<double>(225 * n);
+  C.CL64 = A.alloc<double>(225 * n);
+  C.CR64 = A.alloc<double>(225 * n);
+  C.XL64 = A.alloc<double>(225 * n);
+  C.XR64 = A.alloc<double>(225 * n);
+  if constexpr (sizeof(T) == 8) {
+    C.F = C.F64; C.CL = C.CL64; C.CR = C.CR64; C.XL = C.XL64; C.XR = C.XR64;
+  } else {
+    C.F = A.alloc<T>(225 * n);
+    C.CL = A.alloc<T>(225 * n);
+    C.CR = A.alloc<T>(225 * n);
+    C.XL = A.alloc<T>(225 * n);
+    C.XR = A.alloc<T>(225 * n);
+  }
+  C.w = A.alloc<T>(15 * n);
+  C.coef = A.alloc<double>(3 * n);
+  if (A.err != cudaSuccess) return MBA_ERR_CUDA;
+  if (chain_default_coef(C.coef, n, h->stream) != cudaSuccess) return MBA_ERR_CUDA;
+  b.chain_ready = true;
+  return MBA_OK;
+}
+
 mba_status ensure_common_solver(mba_handle* h, int capacity) {
   DeviceArena& A = h->arena;
   const DevProblem& P = h->P;
@@ -252,7 +297,35 @@ SolverLaunch<T> make_launch(mba_handle* h, SolverBuffers<T>& b, const mba_solver
   s.log = h->log;
   s.kf_cand = h->kf_cand;
   s.lm_cand = h->lm_cand;
+  s.C = b.C;
+  s.precond = (o.preconditioner == MBA_PRECOND_CHAIN || o.preconditioner == MBA_PRECOND_LEARNED) && b.chain_ready
+                  ? o.preconditioner : MBA_PRECOND_BLOCK_JACOBI;
   return s;
+}
+
+// Cost, inertial and visual linearization at the current state, assembly and
+// Jacobi scaling (the work before the first LM iteration).
+template <typename T>
+cudaError_t linearize_current(mba_handle* h, SolverBuffers<T>& b, SolverLaunch<T>& s, int jacobi, cudaStream_t st) {
+  cudaError_t e = cudaMemsetAsync(&h->ctl->cost, 0, sizeof(double), st);
+  if (e == cudaSuccess) e = cudaMemsetAsync(&h->ctl->cost_ine, 0, sizeof(double), st);
+  if (e == cudaSuccess) e = cudaMemsetAsync(h->iscratch, 0, 2 * sizeof(int), st);
+  if (e == cudaSuccess) e = launch_visual_cost(h->P, h->P.kf_state, h->P.lm_p, &h->ctl->cost, h->iscratch, st);
+  if (e == cudaSuccess)
+    e = launch_inertial_gated(h->P, h->P.kf_state, h->ine_cur, &h->ctl->cost_ine, h->iscratch + 1, nullptr, st,
+                              sizeof(T) == 4);
+  if (e == cudaSuccess) e = solver_add_inertial_cost(h->ctl, st);
+  if constexpr (sizeof(T) == 4) {
+    if (e == cudaSuccess) e = launch_inertial_f32(h->P, h->ine_cur, b.ine, st);
+  } else {
+    // FP64 path: the solver reads the current inertial linearization directly.
+    b.ine = h->ine_cur;
+    s.ine = b.ine;
+  }
+  if (e == cudaSuccess) e = launch_visual_linearize<T>(h->P, b.vis, nullptr, st);
+  if (e == cudaSuccess) e = solver_assemble<T>(s, nullptr, st);
+  if (e == cudaSuccess) e = solver_compute_scale<T>(s, jacobi, st);
+  return e;
 }
 
 // Records one LM iteration (graph body) on the stream.
@@ -273,6 +346,10 @@ mba_status run_solve(mba_handle* h, const mba_solver_options& o, mba_summary* su
   SolverBuffers<T>& b = buffers_of<T>(h);
   ms = ensure_solver_buffers<T>(h, b);
   if (ms != MBA_OK) return ms;
+  if (o.preconditioner == MBA_PRECOND_CHAIN || o.preconditioner == MBA_PRECOND_LEARNED) {
+    ms = ensure_chain_buffers<T>(h, b);
+    if (ms != MBA_OK) return ms;
+  }
   SolverLaunch<T> s = make_launch<T>(h, b, o);
   cudaStream_t st = h->stream;
   cudaError_t e = cudaSuccess;
@@ -284,22 +361,7 @@ mba_status run_solve(mba_handle* h, const mba_solver_options& o, mba_summary* su
   cudaEventRecord(ev0, st);
   // Initial evaluation: FP64 cost, inertial linearization, visual linearization, assembly, scaling.
   e = solver_init_control(h->ctl, o.initial_trust_region_radius, st);
-  if (e == cudaSuccess) e = cudaMemsetAsync(&h->ctl->cost, 0, sizeof(double), st);
-  if (e == cudaSuccess) e = cudaMemsetAsync(h->iscratch, 0, 2 * sizeof(int), st);
-  if (e == cudaSuccess) e = launch_visual_cost(h->P, h->P.kf_state, h->P.lm_p, &h->ctl->cost, h->iscratch, st);
-  if (e == cudaSuccess)
-    e = launch_inertial_gated(h->P, h->P.kf_state, h->ine_cur, &h->ctl->cost, h->iscratch + 1, nullptr, st,
-                              sizeof(T) == 4);
-  if constexpr (sizeof(T) == 4) {
-    if (e == cudaSuccess) e = launch_inertial_f32(h->P, h->ine_cur, b.ine, st);
-  } else {
-    // FP64 path: the solver reads the current inertial linearization directly.
-    b.ine = h->ine_cur;
-    s.ine = b.ine;
-  }
-  if (e == cudaSuccess) e = launch_visual_linearize<T>(h->P, b.vis, nullptr, st);
-  if (e == cudaSuccess) e = solver_assemble<T>(s, nullptr, st);
-  if (e == cudaSuccess) e = solver_compute_scale<T>(s, o.jacobi_scaling, st);
+  if (e == cudaSuccess) e = linearize_current<T>(h, b, s, o.jacobi_scaling, st);
   if (e != cudaSuccess) return MBA_ERR_CUDA;
   double initial_cost = 0.0;
   int flags[2] = {0, 0};
@@ -310,7 +372,7 @@ mba_status run_solve(mba_handle* h, const mba_solver_options& o, mba_summary* su
   if (flags[1]) return (mba_status)flags[1];
   if (flags[0] || !std::isfinite(initial_cost)) return MBA_ERR_NON_FINITE;
   // Capture one LM iteration as a graph (or launch it eagerly).
-  cudaGraphExec_t exec = nullptr;
+  cudaGraphExec_t exec = nullptr, restart = nullptr;
   if (o.use_cuda_graph) {
     cudaGraph_t graph = nullptr;
     e = cudaStreamBeginCapture(st, cudaStreamCaptureModeThreadLocal);
@@ -321,7 +383,22 @@ mba_status run_solve(mba_handle* h, const mba_solver_options& o, mba_summary* su
     }
     if (e == cudaSuccess) e = cudaGraphInstantiate(&exec, graph, 0);
     if (graph) cudaGraphDestroy(graph);
-    if (e != cudaSuccess) return MBA_ERR_CUDA;
+    graph = nullptr;
+    if (e == cudaSuccess && o.reject_outliers_every_n_iters > 0) {
+      e = cudaStreamBeginCapture(st, cudaStreamCaptureModeThreadLocal);
+      if (e == cudaSuccess) {
+        cudaError_t e2 = solver_reject_and_restart<T>(s, o.outlier_use_reprojection_error,
+                                                      o.outlier_max_reprojection_error_px, o.jacobi_scaling, st);
+        e = cudaStreamEndCapture(st, &graph);
+        if (e2 != cudaSuccess) e = e2;
+      }
+      if (e == cudaSuccess) e = cudaGraphInstantiate(&restart, graph, 0);
+      if (graph) cudaGraphDestroy(graph);
+    }
+    if (e != cudaSuccess) {
+      if (exec) cudaGraphExecDestroy(exec);
+      return MBA_ERR_CUDA;
+    }
   }
   const auto t0 = std::chrono::steady_clock::now();
   cudaEventRecord(ev0, st);
@@ -331,6 +408,15 @@ mba_status run_solve(mba_handle* h, const mba_solver_options& o, mba_summary* su
     if (h->cancel.load()) { result = MBA_ERR_CANCELLED; break; }
     e = exec ? cudaGraphLaunch(exec, st) : record_iteration<T>(h, s);
     if (e != cudaSuccess) break;
+    // maplab's outlier-rejection solver: every n iterations, drop outlier
+    // landmarks and restart (scaling, cost, linearization; radius kept).
+    const int nrej = o.reject_outliers_every_n_iters;
+    if (nrej > 0 && (it + 1) % nrej == 0 && it + 1 < o.max_num_iterations) {
+      e = restart ? cudaGraphLaunch(restart, st)
+                  : solver_reject_and_restart<T>(s, o.outlier_use_reprojection_error,
+                                                 o.outlier_max_reprojection_error_px, o.jacobi_scaling, st);
+      if (e != cudaSuccess) break;
+    }
     cudaEventRecord(evs[it], st);
     ++launched;
     // Poll for early termination every few iterations without stalling the queue.
@@ -344,6 +430,7 @@ mba_status run_solve(mba_handle* h, const mba_solver_options& o, mba_summary* su
   if (e == cudaSuccess) e = cudaStreamSynchronize(st);
   const double wall_ms = std::chrono::duration<double, std::milli>(std::chrono::steady_clock::now() - t0).count();
   if (exec) cudaGraphExecDestroy(exec);
+  if (restart) cudaGraphExecDestroy(restart);
   if (e != cudaSuccess) return MBA_ERR_CUDA;
   LmControl c;
   cudaMemcpy(&c, h->ctl, sizeof(c), cudaMemcpyDeviceToHost);
@@ -358,6 +445,7 @@ mba_status run_solve(mba_handle* h, const mba_solver_options& o, mba_summary* su
     sum->total_linear_iterations = c.total_pcg;
     sum->total_time_ms = wall_ms;
     sum->time_to_stop_cost_ms = -1.0;
+    sum->num_rejected_landmarks = c.rejected;
     if (c.stop_iteration > 0 && c.stop_iteration <= launched) {
       float ms = 0.f;
       cudaEventElapsedTime(&ms, ev0, evs[c.stop_iteration - 1]);
@@ -381,6 +469,50 @@ mba_status run_solve(mba_handle* h, const mba_solver_options& o, mba_summary* su
   cudaEventDestroy(ev0);
   cudaEventDestroy(ev1);
   return result;
+}
+
+
+template <typename T>
+static cudaError_t copy_out(double* dst, const T* src, int64_t n, cudaStream_t st) {
+  if (!dst || n == 0) return cudaSuccess;
+  std::vector<T> tmp(n);
+  cudaError_t e = cudaMemcpyAsync(tmp.data(), src, sizeof(T) * n, cudaMemcpyDeviceToHost, st);
+  if (e == cudaSuccess) e = cudaStreamSynchronize(st);
+  for (int64_t i = 0; i < n && e == cudaSuccess; ++i) dst[i] = (double)tmp[i];
+  return e;
+}
+
+template <typename T>
+mba_status reduced_system(mba_handle* h, double radius, double* diag, int32_t* upper_ij, double* upper,
+                          double* inertial, double* rhs) {
+  mba_status ms = ensure_common_solver(h, 2);
+  if (ms != MBA_OK) return ms;
+  SolverBuffers<T>& b = buffers_of<T>(h);
+  ms = ensure_solver_buffers<T>(h, b);
+  if (ms != MBA_OK) return ms;
+  mba_solver_options o;
+  mba_default_solver_options(&o);
+  SolverLaunch<T> s = make_launch<T>(h, b, o);
+  cudaStream_t st = h->stream;
+  cudaError_t e = solver_init_control(h->ctl, radius, st);
+  if (e == cudaSuccess) e = linearize_current<T>(h, b, s, o.jacobi_scaling, st);
+  if (e == cudaSuccess) e = solver_build_reduced<T>(s, st);
+  if (e == cudaSuccess) e = cudaStreamSynchronize(st);
+  const int64_t NK = h->P.nkf, NE = h->P.nedge, NPU = h->S.npu;
+  if (e == cudaSuccess) e = copy_out<T>(diag, b.L.SD, 225 * NK, st);
+  if (e == cudaSuccess) e = copy_out<T>(upper, b.L.SP, 36 * NPU, st);
+  if (e == cudaSuccess) e = copy_out<T>(inertial, b.L.SE, 225 * NE, st);
+  if (e == cudaSuccess) e = copy_out<T>(rhs, b.L.rhs, 15 * NK, st);
+  if (e == cudaSuccess && upper_ij && NPU) {
+    std::vector<int32_t> bi(NPU), bj(NPU);
+    e = cudaMemcpy(bi.data(), h->S.pu_i, sizeof(int32_t) * NPU, cudaMemcpyDeviceToHost);
+    if (e == cudaSuccess) e = cudaMemcpy(bj.data(), h->S.pu_j, sizeof(int32_t) * NPU, cudaMemcpyDeviceToHost);
+    for (int64_t q = 0; q < NPU && e == cudaSuccess; ++q) { upper_ij[2 * q] = bi[q]; upper_ij[2 * q + 1] = bj[q]; }
+  }
+  if (e != cudaSuccess) return MBA_ERR_CUDA;
+  int status = 0;
+  cudaMemcpy(&status, &h->ctl->status, sizeof(int), cudaMemcpyDeviceToHost);
+  return status ? (mba_status)status : MBA_OK;
 }
 
 void unpermute_soa(const std::vector<double>& sorted_soa, int64_t N, int comps, const std::vector<int64_t>& perm,
@@ -454,6 +586,9 @@ void mba_default_solver_options(mba_solver_options* o) {
   o->use_cuda_graph = 1;
   o->check_tolerances = 1;
   o->stop_cost = 0.0;
+  o->reject_outliers_every_n_iters = 3;
+  o->outlier_use_reprojection_error = 0;
+  o->outlier_max_reprojection_error_px = 50.0;
 }
 
 const char* mba_status_string(mba_status s) {
@@ -701,6 +836,50 @@ mba_status mba_create(const mba_problem_desc* d, int32_t device, mba_handle** ou
     }
   }
 
+  // ---- keyframe chains (chain preconditioner).  With inertial edges a chain
+  // follows from -> to; without, the keyframes of a mission in index order.
+  // All chains are laid end to end in one sequence of positions; position p
+  // couples to p - 1 only inside a chain (link_edge / link_blk give the
+  // blocks of that coupling, -1 where absent).
+  std::vector<int32_t> chain_perm, link_edge(NK, -1), link_blk(NK, -1);
+  chain_perm.reserve(NK);
+  {
+    std::vector<int32_t> next(NK, -1), next_e(NK, -1);
+    std::vector<char> has_prev(NK, 0), seen(NK, 0), start(NK, 0);
+    for (int64_t e = 0; e < NE; ++e) {
+      const int32_t f = d->edge_from[e], t = d->edge_to[e];
+      if (next[f] < 0 && !has_prev[t]) { next[f] = t; next_e[f] = (int32_t)e; has_prev[t] = 1; }
+    }
+    auto follow = [&](int32_t k) {
+      start[k] = 1;
+      while (k >= 0 && !seen[k]) {
+        seen[k] = 1;
+        chain_perm.push_back(k);
+        k = next[k];
+      }
+    };
+    if (NE > 0) {
+      for (int32_t k = 0; k < NK; ++k) if (!has_prev[k] && !seen[k]) follow(k);
+      for (int32_t k = 0; k < NK; ++k) if (!seen[k]) follow(k);
+    } else {
+      std::vector<int32_t> ord(NK);
+      std::iota(ord.begin(), ord.end(), 0);
+      std::stable_sort(ord.begin(), ord.end(), [&](int32_t a, int32_t b) { return d->kf_mission[a] < d->kf_mission[b]; });
+      for (int64_t q = 0; q < NK; ++q) {
+        const int32_t k = ord[q];
+        start[k] = (q == 0 || d->kf_mission[ord[q - 1]] != d->kf_mission[k]);
+        chain_perm.push_back(k);
+      }
+    }
+    for (int64_t q = 1; q < NK; ++q) {
+      const int32_t a = chain_perm[q - 1], b = chain_perm[q];
+      if (start[b]) continue;
+      if (NE > 0 && next[a] == b) link_edge[q] = next_e[a];  // SE[e] is the (a, b) block
+      const int32_t blk = pm.find(a, b);
+      if (blk >= 0) link_blk[q] = (b < a) ? blk : (int32_t)(npu + blk);  // SP block with rows b, columns a
+    }
+  }
+
   // ---- state and constants
   std::vector<double> kf_state(16 * NK), lm_p(4 * NL, 0.0), mis(8 * NM, 0.0);
   for (int64_t k = 0; k < NK; ++k) {
@@ -752,6 +931,8 @@ mba_status mba_create(const mba_problem_desc* d, int32_t device, mba_handle** ou
   P.lm_p = A.upload(lm_p, st);
   P.lm_obs_off = A.upload(off, st);
   P.lm_active = A.upload(lm_active, st);
+  P.lm_off = A.alloc<int32_t>(NL);
+  if (NL && P.lm_off) cudaMemsetAsync(P.lm_off, 0, sizeof(int32_t) * NL, st);
   P.kf_state = A.upload(kf_state, st);
   P.kf_mis = A.upload(kfm, st);
   P.kf_flags = A.upload(flags, st);
@@ -820,6 +1001,14 @@ mba_status mba_create(const mba_problem_desc* d, int32_t device, mba_handle** ou
   S.row_blk = A.upload(row_blk, st);
   S.kfe_off = A.upload(kfe_off, st);
   S.kfe = A.upload(kfe, st);
+  S.chain_perm = A.upload(chain_perm, st);
+  S.link_edge = A.upload(link_edge, st);
+  S.link_blk = A.upload(link_blk, st);
+  S.chain_levels = 0;
+  while (((int64_t)1 << S.chain_levels) < NK) ++S.chain_levels;
+  S.chain_tail = 0;
+  while (S.chain_tail < S.chain_levels && ((NK + ((int64_t)1 << S.chain_tail) - 1) >> S.chain_tail) > 128)
+    ++S.chain_tail;
   // Inertial scratch (kernels_inertial.cu): dt per step, end state per edge,
   // 4 RK4 stages x 15 values per step.
   P.ine_scratch = A.alloc<double>((NSMP - NE) + 16 * NE + 60 * (NSMP - NE) + 1);
@@ -1027,6 +1216,31 @@ mba_status mba_time_visual_kernel(mba_handle* h, int32_t mode, int32_t iters, do
   for (auto& x : ev) cudaEventDestroy(x);
   *ms_per_launch = total / iters;
   return cuda_status(e);
+}
+
+mba_status mba_reduced_system(mba_handle* h, int32_t precision, double radius, double* diag, int32_t* upper_ij,
+                              double* upper, double* inertial, double* rhs) {
+  if (!h || !(radius > 0.0)) return MBA_ERR_INVALID_ARG;
+  if (precision != MBA_PRECISION_FP64 && precision != MBA_PRECISION_MIXED) return MBA_ERR_INVALID_ARG;
+  cudaSetDevice(h->device);
+  if (precision == MBA_PRECISION_MIXED) return reduced_system<float>(h, radius, diag, upper_ij, upper, inertial, rhs);
+  return reduced_system<double>(h, radius, diag, upper_ij, upper, inertial, rhs);
+}
+
+mba_status mba_rejected_landmarks(mba_handle* h, uint8_t* flags, int64_t* count) {
+  if (!h) return MBA_ERR_INVALID_ARG;
+  cudaSetDevice(h->device);
+  const int64_t NL = h->P.nlm;
+  std::vector<int32_t> off(NL);
+  if (NL && cudaMemcpy(off.data(), h->P.lm_off, sizeof(int32_t) * NL, cudaMemcpyDeviceToHost) != cudaSuccess)
+    return MBA_ERR_CUDA;
+  int64_t c = 0;
+  for (int64_t l = 0; l < NL; ++l) {
+    c += off[l] != 0;
+    if (flags) flags[l] = off[l] != 0;
+  }
+  if (count) *count = c;
+  return MBA_OK;
 }
 
 mba_status mba_get_stats(mba_handle* h, mba_problem_stats* s) {

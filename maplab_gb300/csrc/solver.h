@@ -35,12 +35,23 @@ struct SchurPattern {
   int32_t* row_blk;       // [2 npu] block index into SP (upper b -> b, lower -> npu + b)
   int64_t* kfe_off;       // [nkf+1] incident inertial edges
   int32_t* kfe;           // +(e+1): keyframe is 'from' ; -(e+1): keyframe is 'to'
+  // Keyframe chains laid end to end (chain preconditioner): position -> kf,
+  // and the blocks coupling position p to p - 1 (-1 where absent):
+  // link_edge = inertial edge whose SE block is (kf(p-1), kf(p)); link_blk =
+  // SP block with rows kf(p), columns kf(p-1).
+  int32_t* chain_perm;    // [nkf]
+  int32_t* link_edge;     // [nkf]
+  int32_t* link_blk;      // [nkf]
+  int32_t chain_levels = 0;  // cyclic-reduction levels, 2^levels >= nkf
+  int32_t chain_tail = 0;    // first level handled by the single-block tail sweep
 };
 
 // Device control block of the LM loop (all scalars live on the device).
 struct LmControl {
   double cost;
-  double cost_cand;
+  double cost_cand;        // visual part of the candidate cost
+  double cost_ine;         // inertial part of `cost`
+  double cost_cand_ine;    // inertial part of the candidate cost
   double model_change;
   double radius;
   double decrease_factor;
@@ -63,7 +74,10 @@ struct LmControl {
   int32_t nonfinite;
   int32_t inertial_status;
   int32_t stop_iteration;  // iteration at which cost <= stop_cost (or -1)
-  int32_t pad_[2];
+  int32_t chain_failed;    // chain factorization hit a non-SPD pivot: PCG falls back to block-Jacobi
+  int32_t rejected;        // landmarks rejected as outliers during this solve
+  int32_t reject_count;    // landmarks rejected by the last outlier pass
+  int32_t pad_;
 };
 
 struct LmParams {
@@ -100,6 +114,24 @@ struct LinearSystem {
   T* slm;        // [3][nlm]
 };
 
+// Block cyclic reduction of the chain matrix T (block-tridiagonal in chain
+// positions): T_pp = S_kk + alpha_p diag(off-chain |S| row sums, pose rows),
+// T_{p,p-1} = gamma_ine,p E + gamma_vis,p P (inertial / visual coupling).
+// Position p (> 0) is eliminated at level ctz(p); position 0 last.
+template <typename T>
+struct ChainSystem {
+  double* A;     // [n][225] diagonal blocks of the current level
+  double* B;     // [n][225] coupling to the left neighbour of the current level
+  double* F64;   // [n][225] inverse of the eliminated diagonal block
+  double* CL64;  // [n][225] T(p, p - s) at elimination
+  double* CR64;  // [n][225] T(p, p + s)
+  double* XL64;  // [n][225] T(p - s, p) F(p)
+  double* XR64;  // [n][225] T(p + s, p) F(p)
+  T *F, *CL, *CR, *XL, *XR;  // working-precision copies read by the sweeps
+  T* w;          // [n*15] forward-sweep vector (position order)
+  double* coef;  // [n][3] gamma_ine, gamma_vis (link p -> p-1), alpha (node p)
+};
+
 struct ScaleVectors {
   double* skf;  // [nkf*15]
   double* slm;  // [3][nlm]
@@ -118,6 +150,8 @@ struct SolverLaunch {
   mba_iteration_summary* log;  // device [max_num_iterations + 1]
   double* kf_cand;             // [nkf][16]
   double* lm_cand;             // [nlm][4]
+  ChainSystem<T> C;
+  int32_t precond = 0;         // MBA_PRECOND_*
 };
 
 // kernels_solver.cu
@@ -125,6 +159,10 @@ template <typename T>
 cudaError_t solver_assemble(const SolverLaunch<T>& s, const int* gate, cudaStream_t st);
 template <typename T>
 cudaError_t solver_compute_scale(const SolverLaunch<T>& s, int jacobi, cudaStream_t st);
+// Damped reduced camera system (build + Schur + masks) and the block-Jacobi
+// inverses, at the radius held in the control block.
+template <typename T>
+cudaError_t solver_build_reduced(const SolverLaunch<T>& s, cudaStream_t st);
 template <typename T>
 cudaError_t solver_step(const SolverLaunch<T>& s, cudaStream_t st);
 template <typename T>
@@ -135,5 +173,23 @@ cudaError_t solver_decide_and_accept(const SolverLaunch<T>& s, InertialLin<doubl
 template <typename T>
 cudaError_t solver_relinearize(const SolverLaunch<T>& s, const InertialLin<double>& ine_cur, cudaStream_t st);
 cudaError_t solver_init_control(LmControl* ctl, double radius, cudaStream_t st);
+// cost += cost_ine (after the initial visual and inertial evaluations).
+cudaError_t solver_add_inertial_cost(LmControl* ctl, cudaStream_t st);
+// Outlier rejection and restart at the current state (the Ceres solve that
+// maplab restarts every n iterations): rejects outlier landmarks, recomputes
+// the cost, the visual linearization, the assembly and the Jacobi scaling;
+// keeps the trust-region radius and resets the decrease factor.
+template <typename T>
+cudaError_t solver_reject_and_restart(const SolverLaunch<T>& s, int use_reprojection, double max_px, int jacobi,
+                                      cudaStream_t st);
+
+// kernels_chain.cu: factorization of the chain matrix (after the reduced
+// system is built) and z = T^-1 r with the r.z dot added to *rz.
+template <typename T>
+cudaError_t chain_factor(const SolverLaunch<T>& s, cudaStream_t st);
+template <typename T>
+cudaError_t chain_apply(const SolverLaunch<T>& s, const T* r, T* z, double* rz, cudaStream_t st);
+// Fixed coefficients of the untrained chain preconditioner (gamma = 1, alpha = 0).
+cudaError_t chain_default_coef(double* coef, int64_t n, cudaStream_t st);
 
 }  // namespace mba

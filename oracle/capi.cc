@@ -14,6 +14,7 @@ void evaluateVisualAmbient(const Problem& p, double* res, double* const* jac);
 int evaluateInertialAmbient(const Problem& p, double* res, double* const* jac);
 struct Linearization;
 int solve(Problem& p, const mba_solver_options& o, mba_summary* sum);
+int reducedSystemDense(Problem& p, const mba_solver_options& o, double radius, double* A, double* b);
 }  // namespace oracle
 
 // Access helpers defined in solver.cc's translation unit are kept private; the
@@ -50,6 +51,9 @@ int oracle_linearize_visual(void* h, double* r, double* Jl, double* Js, double* 
 }
 int oracle_solve(void* h, const mba_solver_options* o, mba_summary* s) {
   return oracle::solve(*(oracle::Problem*)h, *o, s);
+}
+int oracle_reduced_system(void* h, const mba_solver_options* o, double radius, double* A, double* b) {
+  return oracle::reducedSystemDense(*(oracle::Problem*)h, *o, radius, A, b);
 }
 int oracle_read_state(void* h, double* kx, double* kv, double* kbg, double* kba, double* lp) {
   return oracle::oracleReadState((oracle::Problem*)h, kx, kv, kbg, kba, lp);

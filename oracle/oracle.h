@@ -148,6 +148,7 @@ int pinholeProject3(const mba_camera& cam, const double* p_C, double* kp,
 // q_C_I 4, p_C_I 3, intrinsics 4, distortion 4).  jacobians: 9 nullable
 // row-major ambient blocks (2x3, 2x7, 2x7, 2x7, 2x7, 2x4, 2x3, 2x4, 2x4).
 // Returns true like Evaluate; *failed tells whether the projection failed.
+void visualPointInCamera(const double* const* params, int type, double* p_C);
 bool visualEvaluate(const double* const* params, const double* measurement, double pixel_sigma,
                     int error_type, const mba_camera& cam, double* residual,
                     double** jacobians, bool* failed);

@@ -60,6 +60,7 @@ struct Problem {
   std::vector<int64_t> lm_obs_off, lm_obs_idx;
   std::vector<uint8_t> kf_mask;  // 15 per keyframe, 1 = active tangent dim
   std::vector<uint8_t> lm_mask;  // 1 = active landmark
+  std::vector<uint8_t> lm_off;   // 1 = rejected outlier: its terms are out of the problem
 };
 
 int createProblem(const mba_problem_desc* d, Problem** out) {
@@ -141,6 +142,7 @@ int createProblem(const mba_problem_desc* d, Problem** out) {
     if (f & MBA_KF_ACCEL_BIAS_CONSTANT) for (int i = 12; i < 15; ++i) m[i] = 0;
   }
   p->lm_mask.assign(p->nlm, 1);
+  p->lm_off.assign(p->nlm, 0);
   for (int64_t l = 0; l < p->nlm; ++l) if (p->lm_const[l] || p->lm_obs_off[l + 1] == p->lm_obs_off[l]) p->lm_mask[l] = 0;
   p->threads = std::max(1u, std::thread::hardware_concurrency());
   *out = p;
@@ -280,6 +282,7 @@ int linearize(const Problem& p, bool want_jac, Linearization* L) {
     auto workRange = [&](int t, int64_t b, int64_t e) {
       double acc = 0.0;
       for (int64_t i = b; i < e; ++i) {
+        if (p.lm_off[p.obs_lm[i]]) continue;  // rejected: zero residual and Jacobians
         const double* P[9];
         visualParams(p, i, P);
         double r[2], Jl[6], Js7[14], Jo7[14];
@@ -499,9 +502,12 @@ struct Scaled {
 
 // Solves (J^T J + D^2) d = -J^T r for the scaled Jacobian via Schur
 // elimination of the landmarks.
+// With dense_A / dense_b set, the reduced system (symmetric, n = 15 N_kf,
+// row-major) and its right-hand side are written there and nothing is solved.
 static StepResult computeStep(const Problem& p, const Linearization& L, const Scaled& sc,
                               const std::vector<double>& dkf, const std::vector<double>& dlm,
-                              const BlockSystem& pattern, int solver, int max_it, double tol) {
+                              const BlockSystem& pattern, int solver, int max_it, double tol,
+                              double* dense_A = nullptr, double* dense_b = nullptr) {
   StepResult out;
   const int64_t N = p.nkf;
   BlockSystem S = pattern;  // copies pattern + zeroed blocks
@@ -625,6 +631,21 @@ static StepResult computeStep(const Problem& p, const Linearization& L, const Sc
     for (int d = 0; d < 15; ++d)
       if (!p.kf_mask[15 * k + d]) bc[15 * k + d] = 0.0;
 
+  if (dense_A) {
+    const size_t n = 15 * N;
+    std::fill(dense_A, dense_A + n * n, 0.0);
+    for (size_t b = 0; b < S.bi.size(); ++b) {
+      const int64_t i = S.bi[b], j = S.bj[b];
+      const double* B = &S.blocks[225 * b];
+      for (int r = 0; r < 15; ++r)
+        for (int c = 0; c < 15; ++c) {
+          dense_A[(15 * i + r) * n + 15 * j + c] = B[15 * r + c];
+          dense_A[(15 * j + c) * n + 15 * i + r] = B[15 * r + c];
+        }
+    }
+    std::copy(bc.begin(), bc.end(), dense_b);
+    return out;
+  }
   std::vector<double> x(15 * N, 0.0);
   if (solver == MBA_LINEAR_SOLVER_DENSE_SCHUR) {
     const int n = (int)(15 * N);
@@ -759,6 +780,57 @@ static void plusState(const Problem& p, const std::vector<double>& dkf, const st
       for (int i = 0; i < 3; ++i) (*lp)[3 * l + i] += dlm[3 * l + i];
 }
 
+// Jacobi scaling 1 / (1 + |column|) and the column norms of the Jacobian.
+static void columnNorms(const Problem& p, const Linearization& L, std::vector<double>& nkf, std::vector<double>& nlm) {
+  nkf.assign(15 * p.nkf, 0.0);
+  nlm.assign(3 * p.nlm, 0.0);
+  for (int64_t i = 0; i < p.nobs; ++i) {
+    const int l = p.obs_lm[i];
+    for (int a = 0; a < 3; ++a) nlm[3 * l + a] += L.vJl[6 * i + a] * L.vJl[6 * i + a] + L.vJl[6 * i + 3 + a] * L.vJl[6 * i + 3 + a];
+    if (p.obs_type[i] == MBA_LOCAL_KEYFRAME) continue;
+    const int64_t ks = p.lm_store[l], ko = p.obs_kf[i];
+    for (int c = 0; c < 6; ++c) {
+      nkf[15 * ks + c] += L.vJs[12 * i + c] * L.vJs[12 * i + c] + L.vJs[12 * i + 6 + c] * L.vJs[12 * i + 6 + c];
+      nkf[15 * ko + c] += L.vJo[12 * i + c] * L.vJo[12 * i + c] + L.vJo[12 * i + 6 + c] * L.vJo[12 * i + 6 + c];
+    }
+  }
+  for (int64_t e = 0; e < p.nedge; ++e)
+    for (int c = 0; c < 15; ++c)
+      for (int r = 0; r < 15; ++r) {
+        nkf[15 * p.e_from[e] + c] += L.iJf[225 * e + 15 * r + c] * L.iJf[225 * e + 15 * r + c];
+        nkf[15 * p.e_to[e] + c] += L.iJt[225 * e + 15 * r + c] * L.iJt[225 * e + 15 * r + c];
+      }
+}
+
+// findOutlierLandmarks (outlier-rejection-solver.cc:28-103): a landmark is
+// an outlier if one of its observations has camera depth <= 0 or, with
+// use_reprojection_error, a squared pixel error above the threshold.
+// Returns the number of newly rejected landmarks.
+static int64_t rejectOutlierLandmarks(Problem& p, const mba_solver_options& o) {
+  int64_t n = 0;
+  const double max2 = o.outlier_max_reprojection_error_px * o.outlier_max_reprojection_error_px;
+  std::vector<uint8_t> out(p.nlm, 0);
+  for (int64_t i = 0; i < p.nobs; ++i) {
+    const int l = p.obs_lm[i];
+    if (p.lm_off[l] || out[l]) continue;
+    const double* P[9];
+    visualParams(p, i, P);
+    double pc[3];
+    visualPointInCamera(P, p.obs_type[i], pc);
+    bool bad = !(pc[2] > 0.0);
+    if (!bad && o.outlier_use_reprojection_error) {
+      double kp[2];
+      pinholeProject3(p.cams[p.obs_cam[i]], pc, kp, nullptr, nullptr, nullptr);
+      const double e0 = kp[0] - p.obs_uv[2 * i], e1 = kp[1] - p.obs_uv[2 * i + 1];
+      bad = !(e0 * e0 + e1 * e1 <= max2);
+    }
+    if (bad) out[l] = 1;
+  }
+  for (int64_t l = 0; l < p.nlm; ++l)
+    if (out[l]) { p.lm_off[l] = 1; ++n; }
+  return n;
+}
+
 int solve(Problem& p, const mba_solver_options& o, mba_summary* sum) {
   using clk = std::chrono::steady_clock;
   const auto t0 = clk::now();
@@ -768,26 +840,7 @@ int solve(Problem& p, const mba_solver_options& o, mba_summary* sum) {
   Scaled sc;
   sc.skf.assign(15 * p.nkf, 1.0);
   sc.slm.assign(3 * p.nlm, 1.0);
-  auto colnorms = [&](std::vector<double>& nkf, std::vector<double>& nlm) {
-    nkf.assign(15 * p.nkf, 0.0);
-    nlm.assign(3 * p.nlm, 0.0);
-    for (int64_t i = 0; i < p.nobs; ++i) {
-      const int l = p.obs_lm[i];
-      for (int a = 0; a < 3; ++a) nlm[3 * l + a] += L.vJl[6 * i + a] * L.vJl[6 * i + a] + L.vJl[6 * i + 3 + a] * L.vJl[6 * i + 3 + a];
-      if (p.obs_type[i] == MBA_LOCAL_KEYFRAME) continue;
-      const int64_t ks = p.lm_store[l], ko = p.obs_kf[i];
-      for (int c = 0; c < 6; ++c) {
-        nkf[15 * ks + c] += L.vJs[12 * i + c] * L.vJs[12 * i + c] + L.vJs[12 * i + 6 + c] * L.vJs[12 * i + 6 + c];
-        nkf[15 * ko + c] += L.vJo[12 * i + c] * L.vJo[12 * i + c] + L.vJo[12 * i + 6 + c] * L.vJo[12 * i + 6 + c];
-      }
-    }
-    for (int64_t e = 0; e < p.nedge; ++e)
-      for (int c = 0; c < 15; ++c)
-        for (int r = 0; r < 15; ++r) {
-          nkf[15 * p.e_from[e] + c] += L.iJf[225 * e + 15 * r + c] * L.iJf[225 * e + 15 * r + c];
-          nkf[15 * p.e_to[e] + c] += L.iJt[225 * e + 15 * r + c] * L.iJt[225 * e + 15 * r + c];
-        }
-  };
+  auto colnorms = [&](std::vector<double>& nkf, std::vector<double>& nlm) { columnNorms(p, L, nkf, nlm); };
   std::vector<double> nkf, nlm;
   colnorms(nkf, nlm);
   if (o.jacobi_scaling) {
@@ -823,8 +876,27 @@ int solve(Problem& p, const mba_solver_options& o, mba_summary* sum) {
   };
   record(0, true, 0, cost, 0.0, 0.0, 0.0);
   if (sum && o.stop_cost > 0 && cost <= o.stop_cost) { sum->termination = 6; sum->time_to_stop_cost_ms = 0.0; }
+  int64_t rejected = 0;
   for (int iter = 1; iter <= o.max_num_iterations; ++iter) {
     if (sum && sum->termination == 6) break;
+    // solveWithOutlierRejection (outlier-rejection-solver.cc:199-259): every
+    // n iterations the Ceres solve ends, outlier landmarks are removed and a
+    // new solve starts from the last trust-region radius (fresh evaluation,
+    // Jacobi scaling and decrease factor).
+    const int nrej = o.reject_outliers_every_n_iters;
+    if (nrej > 0 && iter > 1 && (iter - 1) % nrej == 0) {
+      rejected += rejectOutlierLandmarks(p, o);
+      st = linearize(p, true, &L);
+      if (st) return st;
+      cost = L.cost;
+      colnorms(nkf, nlm);
+      if (o.jacobi_scaling) {
+        for (size_t a = 0; a < nkf.size(); ++a) sc.skf[a] = 1.0 / (1.0 + std::sqrt(nkf[a]));
+        for (size_t a = 0; a < nlm.size(); ++a) sc.slm[a] = 1.0 / (1.0 + std::sqrt(nlm[a]));
+      }
+      decrease_factor = 2.0;
+      reuse_diag = false;
+    }
     // LM diagonal from the scaled Jacobian column norms.
     if (!reuse_diag) {
       colnorms(nkf, nlm);
@@ -930,8 +1002,35 @@ int solve(Problem& p, const mba_solver_options& o, mba_summary* sum) {
   if (sum) {
     sum->final_cost = cost;
     sum->total_time_ms = std::chrono::duration<double, std::milli>(clk::now() - t0).count();
+    sum->num_rejected_landmarks = (int32_t)rejected;
   }
   return MBA_OK;
+}
+
+// The damped, Jacobi-scaled reduced camera system of the first LM iteration
+// at trust-region radius `radius` (dense, row-major, n = 15 N_kf).
+int reducedSystemDense(Problem& p, const mba_solver_options& o, double radius, double* A, double* b) {
+  Linearization L;
+  int st = linearize(p, true, &L);
+  if (st) return st;
+  Scaled sc;
+  std::vector<double> nkf, nlm;
+  columnNorms(p, L, nkf, nlm);
+  sc.skf.assign(15 * p.nkf, 1.0);
+  sc.slm.assign(3 * p.nlm, 1.0);
+  if (o.jacobi_scaling) {
+    for (size_t a = 0; a < nkf.size(); ++a) sc.skf[a] = 1.0 / (1.0 + std::sqrt(nkf[a]));
+    for (size_t a = 0; a < nlm.size(); ++a) sc.slm[a] = 1.0 / (1.0 + std::sqrt(nlm[a]));
+  }
+  std::vector<double> dkf(15 * p.nkf), dlm(3 * p.nlm);
+  for (size_t a = 0; a < nkf.size(); ++a)
+    dkf[a] = std::min(std::max(nkf[a] * sc.skf[a] * sc.skf[a], o.min_lm_diagonal), o.max_lm_diagonal) / radius;
+  for (size_t a = 0; a < nlm.size(); ++a)
+    dlm[a] = std::min(std::max(nlm[a] * sc.slm[a] * sc.slm[a], o.min_lm_diagonal), o.max_lm_diagonal) / radius;
+  BlockSystem pattern;
+  buildPattern(p, &pattern);
+  StepResult r = computeStep(p, L, sc, dkf, dlm, pattern, MBA_LINEAR_SOLVER_DENSE_SCHUR, 1, 0.0, A, b);
+  return r.status;
 }
 
 int oracleLinearizeVisual(Problem* p, double* r, double* Jl, double* Js, double* Jo, double* cost) {

@@ -244,6 +244,40 @@ static void writePoseBlock(const double* Jkp, const double* Jth, const double* J
   }
 }
 
+// Landmark position in the observing camera frame (VIMap::getLandmark_p_C_fi,
+// map-structure/vi-map/src/vi-map.cc, as used by findOutlierLandmarks in
+// outlier-rejection-solver.cc:62-63): the frame chain of the visual term.
+void visualPointInCamera(const double* const* P, int type, double* p_C) {
+  const double* p_B = P[0];
+  double R[9], Rt[9], p_I[3], p_M[3], t[3];
+  if (type == MBA_LOCAL_KEYFRAME) {
+    for (int i = 0; i < 3; ++i) p_I[i] = p_B[i];
+  } else {
+    toRotationMatrixJPL(P[1], R);
+    mat3_transpose(R, Rt);
+    double p_LM[3];
+    mat3_vec(Rt, p_B, p_LM);
+    for (int i = 0; i < 3; ++i) p_LM[i] += P[1][4 + i];
+    if (type == MBA_LOCAL_MISSION) {
+      for (int i = 0; i < 3; ++i) p_M[i] = p_LM[i];
+    } else {
+      double p_G[3];
+      toRotationMatrixJPL(P[2], R);
+      mat3_vec(R, p_LM, p_G);
+      for (int i = 0; i < 3; ++i) t[i] = p_G[i] + P[2][4 + i] - P[3][4 + i];
+      toRotationMatrixJPL(P[3], R);
+      mat3_transpose(R, Rt);
+      mat3_vec(Rt, t, p_M);
+    }
+    toRotationMatrixJPL(P[4], R);
+    for (int i = 0; i < 3; ++i) t[i] = p_M[i] - P[4][4 + i];
+    mat3_vec(R, t, p_I);
+  }
+  toRotationMatrixJPL(P[5], R);
+  mat3_vec(R, p_I, p_C);
+  for (int i = 0; i < 3; ++i) p_C[i] += P[6][i];
+}
+
 bool visualEvaluate(const double* const* P, const double* meas, double pixel_sigma, int type,
                     const mba_camera& cam, double* residual, double** jac, bool* failed_out) {
   const double sinv = 1.0 / pixel_sigma;

@@ -36,6 +36,7 @@ def load():
         "oracle_linearize_visual": (ctypes.c_int, [vp, dp, dp, dp, dp, dp]),
         "oracle_solve": (ctypes.c_int, [vp, ctypes.POINTER(N.SolverOptions), ctypes.POINTER(N.Summary)]),
         "oracle_read_state": (ctypes.c_int, [vp, dp, dp, dp, dp, dp]),
+        "oracle_reduced_system": (ctypes.c_int, [vp, ctypes.POINTER(N.SolverOptions), ctypes.c_double, dp, dp]),
         "oracle_write_state": (ctypes.c_int, [vp, dp, dp, dp, dp, dp]),
         "oracle_time_visual": (ctypes.c_double, [vp, ctypes.c_int, ctypes.c_int64, ctypes.c_int]),
         "oracle_imu_integrate": (None, [dp, dp, dp, ctypes.c_double, dp, dp, dp]),
@@ -125,6 +126,16 @@ class OracleProblem:
         if st != 0:
             raise RuntimeError(f"oracle_solve failed: {st}")
         return N.summary_dict(s)
+
+    def reduced_system(self, opts, radius):
+        """Dense damped, Jacobi-scaled reduced camera system (A, b) of the
+        first LM iteration at trust-region radius `radius`."""
+        n = 15 * self.desc.num_keyframes
+        A = np.zeros((n, n)); b = np.zeros(n)
+        st = self.lib.oracle_reduced_system(self.h, ctypes.byref(opts), radius, N.ptr(A), N.ptr(b))
+        if st != 0:
+            raise RuntimeError(f"oracle_reduced_system failed: {st}")
+        return A, b
 
     def read_state(self):
         d = self.desc

@@ -139,3 +139,60 @@ def test_zero_iterations_returns_cost():
     with ba.BundleAdjuster(m.desc) as g:
         s = g.solve(_gpu_opts(0))
     assert abs(s["final_cost"] - o.cost()) <= 1e-12 * o.cost()
+
+
+def test_chain_preconditioner_matches_oracle_dense(c1_oracle_run):
+    """The chain-corrected preconditioner changes only how fast PCG converges:
+    run to 1e-10 it gives the oracle's exact-Schur LM trajectory, in far fewer
+    linear iterations than block-Jacobi."""
+    m, so, _ = c1_oracle_run
+    with ba.BundleAdjuster(m.desc) as g:
+        sc = g.solve(_gpu_opts(10, max_linear_iterations=6000, preconditioner=N.MBA_PRECOND_CHAIN))
+    with ba.BundleAdjuster(m.desc) as g:
+        sb = g.solve(_gpu_opts(10, max_linear_iterations=6000))
+    assert abs(sc["final_cost"] - so["final_cost"]) <= 1e-6 * so["final_cost"], (sc["final_cost"], so["final_cost"])
+    for a, b in zip(sc["iterations"], so["iterations"]):
+        assert abs(a["cost"] - b["cost"]) <= 1e-6 * b["cost"], (a, b)
+    assert sc["linear_iterations"] < 0.5 * sb["linear_iterations"], (sc["linear_iterations"], sb["linear_iterations"])
+
+
+def test_chain_preconditioner_mixed_reaches_fp64_cost():
+    m = synth.generate("c1")
+    with ba.BundleAdjuster(m.desc) as g:
+        s64 = g.solve(_gpu_opts(10, max_linear_iterations=100, linear_tolerance=1e-6))
+    target = s64["final_cost"] * (1 + 1e-6)
+    with ba.BundleAdjuster(m.desc) as g:
+        s = g.solve(_gpu_opts(30, max_linear_iterations=100, linear_tolerance=1e-6, stop_cost=target,
+                              precision=N.MBA_PRECISION_MIXED, preconditioner=N.MBA_PRECOND_CHAIN))
+    assert s["termination"] == 6, s
+    assert s["final_cost"] <= target
+
+
+def test_outlier_rejection_matches_oracle():
+    """maplab's outlier-rejection solve (every 3 iterations, depth <= 0):
+    ten landmarks flipped behind their store camera are rejected at the first
+    restart on both sides, the rejected sets agree, and the LM trajectories
+    (exact Schur vs PCG to 1e-10) match to 1e-6."""
+    m = synth.generate("c1")
+    lp = m.array("lm_p_B")
+    flipped = np.arange(0, 2000, 200)
+    lp[flipped] *= -3.0
+    oo = _oracle_opts(7)
+    oo.reject_outliers_every_n_iters = 3
+    so = O.OracleProblem(m.desc).solve(oo)
+    with ba.BundleAdjuster(m.desc) as g:
+        sg = g.solve(_gpu_opts(7, max_linear_iterations=6000, reject_outliers_every_n_iters=3))
+        flags, count = g.rejected_landmarks()
+    assert so["rejected_landmarks"] == sg["rejected_landmarks"] == count == len(flipped)
+    assert set(np.nonzero(flags)[0]) == set(flipped)
+    for a, b in zip(sg["iterations"], so["iterations"]):
+        assert abs(a["cost"] - b["cost"]) <= 1e-6 * b["cost"], (a, b)
+
+
+def test_outlier_rejection_off_keeps_all_landmarks():
+    m = synth.generate("c1")
+    m.array("lm_p_B")[:5] *= -3.0
+    with ba.BundleAdjuster(m.desc) as g:
+        s = g.solve(_gpu_opts(4, reject_outliers_every_n_iters=0))
+        _, count = g.rejected_landmarks()
+    assert s["rejected_landmarks"] == 0 and count == 0
