@@ -299,6 +299,44 @@ mba_status mba_reduced_system(mba_handle* h, int32_t precision, double radius, d
  * NULL) and their count.  Rejected landmarks stay out of later solves. */
 mba_status mba_rejected_landmarks(mba_handle* h, uint8_t* flags, int64_t* count);
 
+/* ---- Learned preconditioner (no reference counterpart: maplab's Ceres path
+ * uses SCHUR_JACOBI).  A 3-layer message-passing network (hidden 64, BF16
+ * weights, FP32 accumulation) over the co-visibility graph of the reduced
+ * camera system predicts, per keyframe, the coefficients of the chain
+ * correction to block-Jacobi (MBA_PRECOND_LEARNED).  The model is trained on
+ * the device on reduced systems this library builds. */
+typedef struct mba_gnn mba_gnn;
+int64_t mba_gnn_num_parameters(void);
+/* Randomly initialised model on `device` (head biased towards the plain chain). */
+mba_status mba_gnn_create(int32_t device, uint64_t seed, mba_gnn** out);
+void mba_gnn_destroy(mba_gnn* m);
+/* FP32 master parameters [mba_gnn_num_parameters()]; set resets the optimizer. */
+mba_status mba_gnn_get_parameters(mba_gnn* m, float* params);
+mba_status mba_gnn_set_parameters(mba_gnn* m, const float* params);
+/* Model used by MBA_PRECOND_LEARNED solves on this handle (NULL detaches; the
+ * caller keeps ownership).  Solves asking for LEARNED without a model fail
+ * with MBA_ERR_INVALID_ARG. */
+mba_status mba_set_preconditioner_model(mba_handle* h, mba_gnn* m);
+/* Training on the reduced system of the handle's current state (FP32 system,
+ * LM radius `radius`): `steps` Adam steps (learning rate lr) on the probe
+ * loss mean |T^-1 S w - w|^2 over nprobe normal probes w (T: the chain matrix
+ * with the model's coefficients).  losses [steps] receives the loss before
+ * each step (may be NULL). */
+mba_status mba_gnn_train(mba_handle* h, mba_gnn* m, double radius, int32_t nprobe, int32_t steps, float lr,
+                         uint64_t seed, double* losses);
+/* Loss and its gradient for given probes (host [nprobe][15 N_kf], or seeded
+ * draws if NULL) without updating the model: grad [num_parameters], loss,
+ * coef [N_kf][3] per chain position (gamma_ine, gamma_vis, alpha).  For
+ * gradient checks. */
+mba_status mba_gnn_gradient(mba_handle* h, mba_gnn* m, double radius, int32_t nprobe, const float* probes,
+                            uint64_t seed, float* grad, double* loss, double* coef);
+/* Keyframe chain order used by the chain preconditioner: perm [N_kf] chain
+ * position -> keyframe; link_edge [N_kf] inertial edge coupling position p to
+ * p - 1 (-1: none); link_blk [N_kf] index of the (kf(p), kf(p-1)) pose block
+ * among the 2 N_pu oriented blocks (upper j < N_pu, else the transpose of
+ * upper j - N_pu; -1: none).  Any pointer may be NULL. */
+mba_status mba_chain_structure(mba_handle* h, int32_t* perm, int32_t* link_edge, int32_t* link_blk);
+
 /* Problem statistics (for reports): sizes of the reduced camera system. */
 typedef struct mba_problem_stats {
   int64_t num_keyframes, num_landmarks, num_observations, num_imu_edges;

@@ -287,6 +287,19 @@ def load_ba():
     _declare(lib, "mba_cancel", None, [vp])
     _declare(lib, "mba_time_visual_kernel", ctypes.c_int, [vp, ctypes.c_int32, ctypes.c_int32, c_double_p])
     _declare(lib, "mba_get_stats", ctypes.c_int, [vp, ctypes.POINTER(ProblemStats)])
+    i32p = ctypes.POINTER(ctypes.c_int32)
+    f32p = ctypes.POINTER(ctypes.c_float)
+    _declare(lib, "mba_gnn_num_parameters", ctypes.c_int64, [])
+    _declare(lib, "mba_gnn_create", ctypes.c_int, [ctypes.c_int32, ctypes.c_uint64, ctypes.POINTER(vp)])
+    _declare(lib, "mba_gnn_destroy", None, [vp])
+    _declare(lib, "mba_gnn_get_parameters", ctypes.c_int, [vp, f32p])
+    _declare(lib, "mba_gnn_set_parameters", ctypes.c_int, [vp, f32p])
+    _declare(lib, "mba_set_preconditioner_model", ctypes.c_int, [vp, vp])
+    _declare(lib, "mba_gnn_train", ctypes.c_int, [vp, vp, ctypes.c_double, ctypes.c_int32, ctypes.c_int32,
+                                                  ctypes.c_float, ctypes.c_uint64, c_double_p])
+    _declare(lib, "mba_gnn_gradient", ctypes.c_int, [vp, vp, ctypes.c_double, ctypes.c_int32, f32p, ctypes.c_uint64,
+                                                     f32p, c_double_p, c_double_p])
+    _declare(lib, "mba_chain_structure", ctypes.c_int, [vp, i32p, i32p, i32p])
     _declare(lib, "mba_rejected_landmarks", ctypes.c_int, [vp, ctypes.POINTER(ctypes.c_uint8), ctypes.POINTER(ctypes.c_int64)])
     _declare(lib, "mba_reduced_system", ctypes.c_int,
              [vp, ctypes.c_int32, ctypes.c_double, c_double_p, ctypes.POINTER(ctypes.c_int32), c_double_p,

@@ -47,6 +47,58 @@ def default_options(**kw):
     return o
 
 
+class PreconditionerModel:
+    """Learned chain-preconditioner network (mba_gnn): FP32 master weights on
+    one device, BF16 copies used by the kernels."""
+
+    def __init__(self, device=0, seed=0):
+        self._lib = lib()
+        h = ctypes.c_void_p()
+        _check(self._lib.mba_gnn_create(device, seed, ctypes.byref(h)), "mba_gnn_create")
+        self._h = h
+        self.device = device
+
+    @staticmethod
+    def num_parameters():
+        return int(lib().mba_gnn_num_parameters())
+
+    @property
+    def handle(self):
+        return self._h
+
+    def close(self):
+        if self._h:
+            self._lib.mba_gnn_destroy(self._h)
+            self._h = None
+
+    def __del__(self):
+        try:
+            self.close()
+        except Exception:
+            pass
+
+    def parameters(self):
+        w = np.zeros(self.num_parameters(), dtype=np.float32)
+        _check(self._lib.mba_gnn_get_parameters(self._h, w.ctypes.data_as(ctypes.POINTER(ctypes.c_float))),
+               "mba_gnn_get_parameters")
+        return w
+
+    def set_parameters(self, w):
+        w = np.ascontiguousarray(w, dtype=np.float32)
+        assert w.size == self.num_parameters()
+        _check(self._lib.mba_gnn_set_parameters(self._h, w.ctypes.data_as(ctypes.POINTER(ctypes.c_float))),
+               "mba_gnn_set_parameters")
+
+    def save(self, path):
+        np.save(path, self.parameters())
+
+    @classmethod
+    def load(cls, path, device=0):
+        m = cls(device=device)
+        m.set_parameters(np.load(path))
+        return m
+
+
 class BundleAdjuster:
     def __init__(self, desc, device=0):
         self._lib = lib()
@@ -157,6 +209,42 @@ class BundleAdjuster:
         _check(self._lib.mba_rejected_landmarks(self._h, flags.ctypes.data_as(ctypes.POINTER(ctypes.c_uint8)),
                                                 ctypes.byref(c)), "mba_rejected_landmarks")
         return flags.astype(bool), c.value
+
+    def set_preconditioner_model(self, model):
+        _check(self._lib.mba_set_preconditioner_model(self._h, model.handle if model is not None else None),
+               "mba_set_preconditioner_model")
+        self._model = model
+
+    def train_preconditioner(self, model, radius=1e5, nprobe=4, steps=1, lr=1e-3, seed=0):
+        """Adam steps of the coefficient network on this state's reduced system;
+        returns the loss before each step."""
+        losses = np.zeros(max(steps, 1))
+        _check(self._lib.mba_gnn_train(self._h, model.handle, radius, nprobe, steps, lr, seed, N.ptr(losses)),
+               "mba_gnn_train")
+        return losses[:steps]
+
+    def preconditioner_gradient(self, model, radius=1e5, probes=None, nprobe=2, seed=0):
+        """(loss, gradient [num_parameters], coef [N_kf, 3] per chain position)."""
+        npar = model.num_parameters()
+        grad = np.zeros(npar, dtype=np.float32)
+        coef = np.zeros((self.desc.num_keyframes, 3))
+        loss = ctypes.c_double()
+        pr = None
+        if probes is not None:
+            probes = np.ascontiguousarray(probes, dtype=np.float32)
+            nprobe = probes.shape[0]
+            pr = probes.ctypes.data_as(ctypes.POINTER(ctypes.c_float))
+        _check(self._lib.mba_gnn_gradient(self._h, model.handle, radius, nprobe, pr, seed,
+                                          grad.ctypes.data_as(ctypes.POINTER(ctypes.c_float)), ctypes.byref(loss),
+                                          N.ptr(coef)), "mba_gnn_gradient")
+        return loss.value, grad, coef
+
+    def chain_structure(self):
+        n = self.desc.num_keyframes
+        perm = np.zeros(n, dtype=np.int32); le = np.zeros(n, dtype=np.int32); lb = np.zeros(n, dtype=np.int32)
+        p = lambda a: a.ctypes.data_as(ctypes.POINTER(ctypes.c_int32))
+        _check(self._lib.mba_chain_structure(self._h, p(perm), p(le), p(lb)), "mba_chain_structure")
+        return perm, le, lb
 
     def cancel(self):
         self._lib.mba_cancel(self._h)

@@ -159,7 +159,7 @@ __global__ void __launch_bounds__(32 * kCW) k_chain_init(SolverLaunch<T> s) {
   const T* D = s.L.SD + 225 * k;
   for (int idx = lane; idx < 225; idx += 32) A[idx] = (double)D[idx];
   // Diagonal compensation: alpha * sum of |S| over the off-chain pose blocks of row k.
-  if (al != 0.0) {
+  {
     const bool ll = p > 0 && (s.S.link_edge[p] >= 0 || s.S.link_blk[p] >= 0);
     const bool lr = p + 1 < n && (s.S.link_edge[p + 1] >= 0 || s.S.link_blk[p + 1] >= 0);
     const int64_t kl = ll ? s.S.chain_perm[p - 1] : -1, kr = lr ? s.S.chain_perm[p + 1] : -1;
@@ -180,7 +180,10 @@ __global__ void __launch_bounds__(32 * kCW) k_chain_init(SolverLaunch<T> s) {
       if (part + o < 5) c += t;
     }
     __syncwarp();
-    if (r < 6 && part == 0 && ((s.P.kf_mask[k] >> r) & 1)) A[16 * r] += al * c;
+    if (r < 6 && part == 0) {
+      s.C.comp[6 * p + r] = c;
+      if (al != 0.0 && ((s.P.kf_mask[k] >> r) & 1)) A[16 * r] += al * c;
+    }
   }
   const int32_t le = p > 0 ? s.S.link_edge[p] : -1, lb = p > 0 ? s.S.link_blk[p] : -1;
   for (int idx = lane; idx < 225; idx += 32) {

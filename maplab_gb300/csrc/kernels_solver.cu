@@ -958,6 +958,7 @@ cudaError_t solver_build_reduced(const SolverLaunch<T>& s, cudaStream_t st) {
   k_block_jacobi<T><<<nblk(s.P.nkf, 64), 64, 0, st>>>(s);
   if (s.precond != MBA_PRECOND_BLOCK_JACOBI) {
     cudaError_t e = cudaGetLastError();
+    if (e == cudaSuccess && s.precond == MBA_PRECOND_LEARNED) e = gnn_forward<T>(s, s.gg, s.gp, s.gw, st);
     if (e != cudaSuccess) return e;
     return chain_factor<T>(s, st);
   }

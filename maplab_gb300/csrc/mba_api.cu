@@ -8,6 +8,7 @@
 // descriptor already holds the JPL state arrays.  mba_solve replaces
 // map_optimization::solve (src/solver.cc:14-44), i.e. ceres::Solve with the
 // options of include/map-optimization/solver-options.h:26-75.
+#include <cuda_bf16.h>
 #include <cuda_runtime.h>
 
 #include <algorithm>
@@ -129,6 +130,13 @@ struct SolverBuffers {
 
 }  // namespace
 
+// Learned-preconditioner model: parameters and Adam state on one device.
+struct mba_gnn {
+  int device = 0;
+  DeviceArena arena;
+  GnnParams p{};
+};
+
 struct mba_handle {
   int device = 0;
   cudaStream_t stream = nullptr;
@@ -155,6 +163,11 @@ struct mba_handle {
   double* stage_state = nullptr;  // 16 NK + 3 NL
   double* stage_lin = nullptr;    // 32 N
   char* l2_flush = nullptr;       // buffer larger than L2 for timing hygiene
+  // learned preconditioner
+  GnnGraph gg{};
+  GnnWork gw{};
+  bool gw_ready = false;
+  mba_gnn* model = nullptr;
 };
 
 namespace {
@@ -234,9 +247,36 @@ mba_status ensure_chain_buffers(mba_handle* h, SolverBuffers<T>& b) {
   }
   C.w = A.alloc<T>(15 * n);
   C.coef = A.alloc<double>(3 * n);
+  C.comp = A.alloc<double>(6 * n);
   if (A.err != cudaSuccess) return MBA_ERR_CUDA;
   if (chain_default_coef(C.coef, n, h->stream) != cudaSuccess) return MBA_ERR_CUDA;
   b.chain_ready = true;
+  return MBA_OK;
+}
+
+mba_status ensure_gnn_work(mba_handle* h) {
+  if (h->gw_ready) return MBA_OK;
+  DeviceArena& A = h->arena;
+  const int64_t n = h->P.nkf, nnz = 2 * h->S.npu + 2 * h->P.nedge;
+  GnnWork& w = h->gw;
+  w.n = n;
+  w.wgt = A.alloc<float>(nnz + 1);
+  w.deg = A.alloc<float>(n);
+  w.h[0] = w.x = A.alloc<__nv_bfloat16>(n * kGnnIn);
+  for (int l = 0; l < kGnnLayers; ++l) {
+    w.h[l + 1] = A.alloc<__nv_bfloat16>(n * kGnnHidden);
+    w.m[l] = A.alloc<__nv_bfloat16>(n * (l == 0 ? kGnnIn : kGnnHidden));
+    w.z[l] = A.alloc<float>(n * kGnnHidden);
+  }
+  w.o = A.alloc<float>(n * kGnnOut);
+  w.dh = A.alloc<float>(n * kGnnHidden);
+  w.dm = A.alloc<float>(n * kGnnHidden);
+  w.dzb = A.alloc<__nv_bfloat16>(n * kGnnHidden);
+  w.dcoef = A.alloc<float>(3 * n);
+  w.vec = A.alloc<float>(5 * 15 * n);
+  w.loss = A.alloc<double>(2);
+  if (A.err != cudaSuccess) return MBA_ERR_CUDA;
+  h->gw_ready = true;
   return MBA_OK;
 }
 
@@ -300,6 +340,10 @@ SolverLaunch<T> make_launch(mba_handle* h, SolverBuffers<T>& b, const mba_solver
   s.C = b.C;
   s.precond = (o.preconditioner == MBA_PRECOND_CHAIN || o.preconditioner == MBA_PRECOND_LEARNED) && b.chain_ready
                   ? o.preconditioner : MBA_PRECOND_BLOCK_JACOBI;
+  if (s.precond == MBA_PRECOND_LEARNED && !(h->model && h->gw_ready)) s.precond = MBA_PRECOND_CHAIN;
+  s.gg = h->gg;
+  s.gw = h->gw;
+  if (h->model) s.gp = h->model->p;
   return s;
 }
 
@@ -346,9 +390,16 @@ mba_status run_solve(mba_handle* h, const mba_solver_options& o, mba_summary* su
   SolverBuffers<T>& b = buffers_of<T>(h);
   ms = ensure_solver_buffers<T>(h, b);
   if (ms != MBA_OK) return ms;
+  if (o.preconditioner == MBA_PRECOND_LEARNED) {
+    if (!h->model || h->model->device != h->device) return MBA_ERR_INVALID_ARG;
+    ms = ensure_gnn_work(h);
+    if (ms != MBA_OK) return ms;
+  }
   if (o.preconditioner == MBA_PRECOND_CHAIN || o.preconditioner == MBA_PRECOND_LEARNED) {
     ms = ensure_chain_buffers<T>(h, b);
     if (ms != MBA_OK) return ms;
+    if (o.preconditioner == MBA_PRECOND_CHAIN && chain_default_coef(b.C.coef, h->P.nkf, h->stream) != cudaSuccess)
+      return MBA_ERR_CUDA;
   }
   SolverLaunch<T> s = make_launch<T>(h, b, o);
   cudaStream_t st = h->stream;
@@ -836,6 +887,23 @@ mba_status mba_create(const mba_problem_desc* d, int32_t device, mba_handle** ou
     }
   }
 
+  // ---- neighbour lists of the co-visibility + inertial graph (learned
+  // preconditioner): per keyframe its pose-pose blocks, then its inertial edges.
+  std::vector<int64_t> nbr_off(NK + 1, 0);
+  std::vector<int32_t> nbr, nbr_blk;
+  nbr.reserve(row_col.size() + 2 * NE);
+  nbr_blk.reserve(row_col.size() + 2 * NE);
+  for (int64_t k = 0; k < NK; ++k) {
+    for (int64_t e = row_off[k]; e < row_off[k + 1]; ++e) { nbr.push_back(row_col[e]); nbr_blk.push_back(row_blk[e]); }
+    for (int64_t e = kfe_off[k]; e < kfe_off[k + 1]; ++e) {
+      const int32_t code = kfe[e];
+      const int64_t ed = code > 0 ? code - 1 : -code - 1;
+      nbr.push_back(code > 0 ? d->edge_to[ed] : d->edge_from[ed]);
+      nbr_blk.push_back((int32_t)(-(ed + 1)));
+    }
+    nbr_off[k + 1] = (int64_t)nbr.size();
+  }
+
   // ---- keyframe chains (chain preconditioner).  With inertial edges a chain
   // follows from -> to; without, the keyframes of a mission in index order.
   // All chains are laid end to end in one sequence of positions; position p
@@ -1001,6 +1069,9 @@ mba_status mba_create(const mba_problem_desc* d, int32_t device, mba_handle** ou
   S.row_blk = A.upload(row_blk, st);
   S.kfe_off = A.upload(kfe_off, st);
   S.kfe = A.upload(kfe, st);
+  h->gg.nbr_off = A.upload(nbr_off, st);
+  h->gg.nbr = A.upload(nbr, st);
+  h->gg.nbr_blk = A.upload(nbr_blk, st);
   S.chain_perm = A.upload(chain_perm, st);
   S.link_edge = A.upload(link_edge, st);
   S.link_blk = A.upload(link_blk, st);
@@ -1252,6 +1323,191 @@ mba_status mba_get_stats(mba_handle* h, mba_problem_stats* s) {
   s->num_schur_pose_blocks = 2 * h->S.npu;
   s->device_bytes = h->arena.bytes;
   return MBA_OK;
+}
+
+}  // extern "C"
+
+// ---- learned preconditioner model
+
+namespace {
+
+// Reduced system of the current state (mixed precision) with the model's
+// coefficients and their chain factorization, ready for the probe loss.
+mba_status gnn_prepare(mba_handle* h, mba_gnn* m, double radius, SolverLaunch<float>* out) {
+  mba_status ms = ensure_common_solver(h, 2);
+  if (ms != MBA_OK) return ms;
+  SolverBuffers<float>& b = h->b32;
+  if ((ms = ensure_solver_buffers<float>(h, b)) != MBA_OK) return ms;
+  if ((ms = ensure_chain_buffers<float>(h, b)) != MBA_OK) return ms;
+  if ((ms = ensure_gnn_work(h)) != MBA_OK) return ms;
+  mba_solver_options o;
+  mba_default_solver_options(&o);
+  o.precision = MBA_PRECISION_MIXED;
+  o.preconditioner = MBA_PRECOND_LEARNED;
+  mba_gnn* keep = h->model;
+  h->model = m;
+  SolverLaunch<float> s = make_launch<float>(h, b, o);
+  h->model = keep;
+  cudaStream_t st = h->stream;
+  cudaError_t e = solver_init_control(h->ctl, radius, st);
+  if (e == cudaSuccess) e = linearize_current<float>(h, b, s, o.jacobi_scaling, st);
+  if (e == cudaSuccess) e = solver_build_reduced<float>(s, st);
+  LmControl c;
+  if (e == cudaSuccess) e = cudaMemcpyAsync(&c, h->ctl, sizeof(c), cudaMemcpyDeviceToHost, st);
+  if (e == cudaSuccess) e = cudaStreamSynchronize(st);
+  if (e != cudaSuccess) return MBA_ERR_CUDA;
+  if (c.status) return (mba_status)c.status;
+  if (c.chain_failed) return MBA_ERR_NOT_SPD;
+  *out = s;
+  return MBA_OK;
+}
+
+// Coefficients and chain factorization after a parameter update.
+cudaError_t gnn_refresh(mba_handle* h, const SolverLaunch<float>& s) {
+  cudaStream_t st = h->stream;
+  cudaError_t e = cudaMemsetAsync(&h->ctl->chain_failed, 0, sizeof(int32_t), st);
+  if (e == cudaSuccess) e = gnn_forward<float>(s, s.gg, s.gp, s.gw, st);
+  if (e == cudaSuccess) e = chain_factor<float>(s, st);
+  return e;
+}
+
+}  // namespace
+
+extern "C" {
+
+int64_t mba_gnn_num_parameters(void) { return GnnLayout::make().total; }
+
+mba_status mba_gnn_create(int32_t device, uint64_t seed, mba_gnn** out) {
+  if (!out) return MBA_ERR_INVALID_ARG;
+  *out = nullptr;
+  int ndev = 0;
+  if (cudaGetDeviceCount(&ndev) != cudaSuccess || ndev == 0) return MBA_ERR_NO_DEVICE;
+  if (device < 0 || device >= ndev) return MBA_ERR_INVALID_ARG;
+  cudaSetDevice(device);
+  mba_gnn* m = new (std::nothrow) mba_gnn();
+  if (!m) return MBA_ERR_CUDA;
+  m->device = device;
+  const int64_t n = GnnLayout::make().total;
+  DeviceArena& A = m->arena;
+  m->p.w = A.alloc<float>(n);
+  m->p.wb = A.alloc<__nv_bfloat16>(n);
+  m->p.wt = A.alloc<__nv_bfloat16>(n);
+  m->p.g = A.alloc<float>(n);
+  m->p.m = A.alloc<float>(n);
+  m->p.v = A.alloc<float>(n);
+  m->p.step = 0;
+  cudaError_t e = A.err;
+  if (e == cudaSuccess) e = gnn_init_params(m->p, seed, nullptr);
+  if (e == cudaSuccess) e = cudaDeviceSynchronize();
+  if (e != cudaSuccess) {
+    A.release();
+    delete m;
+    return MBA_ERR_CUDA;
+  }
+  *out = m;
+  return MBA_OK;
+}
+
+void mba_gnn_destroy(mba_gnn* m) {
+  if (!m) return;
+  cudaSetDevice(m->device);
+  m->arena.release();
+  delete m;
+}
+
+mba_status mba_gnn_get_parameters(mba_gnn* m, float* params) {
+  if (!m || !params) return MBA_ERR_INVALID_ARG;
+  cudaSetDevice(m->device);
+  return cuda_status(cudaMemcpy(params, m->p.w, sizeof(float) * GnnLayout::make().total, cudaMemcpyDeviceToHost));
+}
+
+mba_status mba_gnn_set_parameters(mba_gnn* m, const float* params) {
+  if (!m || !params) return MBA_ERR_INVALID_ARG;
+  const int64_t n = GnnLayout::make().total;
+  for (int64_t i = 0; i < n; ++i)
+    if (!std::isfinite(params[i])) return MBA_ERR_NON_FINITE;
+  cudaSetDevice(m->device);
+  cudaError_t e = cudaMemcpy(m->p.w, params, sizeof(float) * n, cudaMemcpyHostToDevice);
+  if (e == cudaSuccess) e = cudaMemset(m->p.m, 0, sizeof(float) * n);
+  if (e == cudaSuccess) e = cudaMemset(m->p.v, 0, sizeof(float) * n);
+  m->p.step = 0;
+  if (e == cudaSuccess) e = gnn_sync_bf16(m->p, nullptr);
+  if (e == cudaSuccess) e = cudaDeviceSynchronize();
+  return cuda_status(e);
+}
+
+mba_status mba_set_preconditioner_model(mba_handle* h, mba_gnn* m) {
+  if (!h) return MBA_ERR_INVALID_ARG;
+  if (m && m->device != h->device) return MBA_ERR_INVALID_ARG;
+  h->model = m;
+  return MBA_OK;
+}
+
+mba_status mba_gnn_train(mba_handle* h, mba_gnn* m, double radius, int32_t nprobe, int32_t steps, float lr,
+                         uint64_t seed, double* losses) {
+  if (!h || !m || m->device != h->device || nprobe < 1 || steps < 0 || !(radius > 0.0) || !(lr >= 0.f))
+    return MBA_ERR_INVALID_ARG;
+  cudaSetDevice(h->device);
+  SolverLaunch<float> s;
+  mba_status ms = gnn_prepare(h, m, radius, &s);
+  if (ms != MBA_OK) return ms;
+  cudaStream_t st = h->stream;
+  for (int32_t k = 0; k < steps; ++k) {
+    cudaError_t e = gnn_loss_backward<float>(s, s.gg, m->p, s.gw, nprobe, nullptr, seed + 104729ull * k, st);
+    double loss = 0.0;
+    if (e == cudaSuccess) e = cudaMemcpyAsync(&loss, s.gw.loss, sizeof(double), cudaMemcpyDeviceToHost, st);
+    if (e == cudaSuccess) e = cudaStreamSynchronize(st);
+    if (e != cudaSuccess) return MBA_ERR_CUDA;
+    if (losses) losses[k] = loss;
+    if (!std::isfinite(loss)) return MBA_ERR_NON_FINITE;
+    if (lr > 0.f) {
+      m->p.step++;
+      e = gnn_adam(m->p, lr, st);
+      s.gp = m->p;
+      if (e == cudaSuccess) e = gnn_refresh(h, s);
+      int32_t failed = 0;
+      if (e == cudaSuccess) e = cudaMemcpyAsync(&failed, &h->ctl->chain_failed, sizeof(int32_t), cudaMemcpyDeviceToHost, st);
+      if (e == cudaSuccess) e = cudaStreamSynchronize(st);
+      if (e != cudaSuccess) return MBA_ERR_CUDA;
+      if (failed) return MBA_ERR_NOT_SPD;
+    }
+  }
+  return MBA_OK;
+}
+
+mba_status mba_gnn_gradient(mba_handle* h, mba_gnn* m, double radius, int32_t nprobe, const float* probes,
+                            uint64_t seed, float* grad, double* loss, double* coef) {
+  if (!h || !m || m->device != h->device || nprobe < 1 || !(radius > 0.0)) return MBA_ERR_INVALID_ARG;
+  cudaSetDevice(h->device);
+  SolverLaunch<float> s;
+  mba_status ms = gnn_prepare(h, m, radius, &s);
+  if (ms != MBA_OK) return ms;
+  cudaStream_t st = h->stream;
+  const int64_t n15 = 15 * h->P.nkf, np = GnnLayout::make().total;
+  float* dprobe = nullptr;
+  cudaError_t e = cudaSuccess;
+  if (probes) {
+    e = cudaMalloc(&dprobe, sizeof(float) * n15 * nprobe);
+    if (e == cudaSuccess) e = cudaMemcpyAsync(dprobe, probes, sizeof(float) * n15 * nprobe, cudaMemcpyHostToDevice, st);
+  }
+  if (e == cudaSuccess) e = gnn_loss_backward<float>(s, s.gg, m->p, s.gw, nprobe, dprobe, seed, st);
+  if (e == cudaSuccess && grad) e = cudaMemcpyAsync(grad, m->p.g, sizeof(float) * np, cudaMemcpyDeviceToHost, st);
+  if (e == cudaSuccess && loss) e = cudaMemcpyAsync(loss, s.gw.loss, sizeof(double), cudaMemcpyDeviceToHost, st);
+  if (e == cudaSuccess && coef) e = cudaMemcpyAsync(coef, s.C.coef, sizeof(double) * 3 * h->P.nkf, cudaMemcpyDeviceToHost, st);
+  if (e == cudaSuccess) e = cudaStreamSynchronize(st);
+  if (dprobe) cudaFree(dprobe);
+  return cuda_status(e);
+}
+
+mba_status mba_chain_structure(mba_handle* h, int32_t* perm, int32_t* link_edge, int32_t* link_blk) {
+  if (!h) return MBA_ERR_INVALID_ARG;
+  cudaSetDevice(h->device);
+  const int64_t n = h->P.nkf;
+  cudaError_t e = cudaSuccess;
+  if (perm) e = cudaMemcpy(perm, h->S.chain_perm, sizeof(int32_t) * n, cudaMemcpyDeviceToHost);
+  if (e == cudaSuccess && link_edge) e = cudaMemcpy(link_edge, h->S.link_edge, sizeof(int32_t) * n, cudaMemcpyDeviceToHost);
+  if (e == cudaSuccess && link_blk) e = cudaMemcpy(link_blk, h->S.link_blk, sizeof(int32_t) * n, cudaMemcpyDeviceToHost);
+  return cuda_status(e);
 }
 
 }  // extern "C"

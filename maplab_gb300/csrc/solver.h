@@ -4,6 +4,7 @@
 #include <cuda_runtime.h>
 #include <stdint.h>
 
+#include "gnn.h"
 #include "internal.h"
 
 namespace mba {
@@ -130,6 +131,7 @@ struct ChainSystem {
   T *F, *CL, *CR, *XL, *XR;  // working-precision copies read by the sweeps
   T* w;          // [n*15] forward-sweep vector (position order)
   double* coef;  // [n][3] gamma_ine, gamma_vis (link p -> p-1), alpha (node p)
+  double* comp;  // [n][6] off-chain |S| row sums of the pose rows (alpha's direction)
 };
 
 struct ScaleVectors {
@@ -152,6 +154,9 @@ struct SolverLaunch {
   double* lm_cand;             // [nlm][4]
   ChainSystem<T> C;
   int32_t precond = 0;         // MBA_PRECOND_*
+  GnnGraph gg{};               // learned preconditioner (precond == MBA_PRECOND_LEARNED)
+  GnnParams gp{};
+  GnnWork gw{};
 };
 
 // kernels_solver.cu
@@ -191,5 +196,20 @@ template <typename T>
 cudaError_t chain_apply(const SolverLaunch<T>& s, const T* r, T* z, double* rz, cudaStream_t st);
 // Fixed coefficients of the untrained chain preconditioner (gamma = 1, alpha = 0).
 cudaError_t chain_default_coef(double* coef, int64_t n, cudaStream_t st);
+
+// kernels_gnn.cu: the coefficient network.
+cudaError_t gnn_init_params(GnnParams p, uint64_t seed, cudaStream_t st);
+cudaError_t gnn_sync_bf16(GnnParams p, cudaStream_t st);
+// Features, forward pass and chain coefficients (s.C.coef) for the reduced
+// system held in s.L.
+template <typename T>
+cudaError_t gnn_forward(const SolverLaunch<T>& s, GnnGraph g, GnnParams p, GnnWork w, cudaStream_t st);
+// Probe loss mean |T^-1 S w - w|^2 over nprobe probes (device `probes`
+// [nprobe][15 n] if given, else seeded normal draws) into w.loss, and its
+// gradient into p.g.  Needs the chain factorization of the current coef.
+template <typename T>
+cudaError_t gnn_loss_backward(const SolverLaunch<T>& s, GnnGraph g, GnnParams p, GnnWork w, int nprobe,
+                              const float* probes, uint64_t seed, cudaStream_t st);
+cudaError_t gnn_adam(GnnParams p, float lr, cudaStream_t st);
 
 }  // namespace mba
