@@ -11,8 +11,11 @@ visual observation of the workload, the evaluation half of one LM iteration.
   e2e    : the same metric through the C ABI with pinned HOST buffers: state
            upload (mba_write_state), linearization, and the residuals and
            Jacobians read back in the caller's order (mba_linearize_visual).
-  ba     : time-to-cost-tolerance of the device LM (plain FP64 vs mixed) on the
-           same map, 20 iterations, block-Jacobi PCG (<= 100 its, tol 1e-6).
+  ba     : time-to-cost-tolerance on the 20,000-keyframe 10-mission map: plain
+           FP64 device LM (20 iterations, block-Jacobi PCG <= 100 its, tol
+           1e-6) against mixed precision with the learned chain
+           preconditioner, stopped at the plain path's cost * (1 + 1e-6);
+           reprojection RMS of both final states.
 
 --impl reference times the CPU restatement of the reference's evaluation
 (oracle/, all host threads) on the same map.  Multi-GPU runs are independent
@@ -31,7 +34,7 @@ import time
 ROOT = os.path.dirname(os.path.abspath(__file__))
 sys.path.insert(0, ROOT)
 
-METRIC = "obs Jacobian evals/s"
+METRIC = "BA time-to-cost-tol (s) and obs Jacobian evals/s: mixed+learned vs plain FP64 on GB300"
 WORKLOAD = "C2: plain method on GPU, 2,000 keyframes, 200k landmarks, ~1.6M observations, 2 cameras (radtan + equidistant)"
 
 
@@ -137,6 +140,65 @@ def run_reference(args):
     print(json.dumps(line), flush=True)
 
 
+def _reprojection_rms(g, m):
+    """RMS reprojection error (px) over the observations still in the problem
+    (landmark not rejected, projection valid) at the handle's state."""
+    import numpy as np
+    r, _ = g.evaluate_visual(blocks=[])
+    sig = m.array("obs_sigma")
+    flags, _ = g.rejected_landmarks()
+    keep = ~flags[m.array("obs_landmark")] & np.any(r != 0.0, axis=1)
+    e2 = np.sum((r * sig[:, None]) ** 2, axis=1)[keep]
+    return float(np.sqrt(e2.mean())), int(keep.sum())
+
+
+def ba_time_to_cost(args, device):
+    """Plain FP64 path (block-Jacobi PCG <= 100 its, 20 LM iterations) against
+    the mixed-precision path with the learned chain preconditioner (PCG <= 25
+    its), stopped at the plain path's final cost * (1 + 1e-6).  Times are CUDA
+    events from the first device launch of the solve."""
+    from maplab_gb300 import _native as N
+    from maplab_gb300 import ba, synth
+    from maplab_gb300 import train_preconditioner as TP
+    m = synth.generate(args.ba_config)
+    d = m.desc
+    common = dict(check_tolerances=0, linear_tolerance=1e-6, outlier_use_reprojection_error=args.reproj_rejection)
+    g64 = ba.BundleAdjuster(d, device=device)
+    s64 = g64.solve(ba.default_options(max_num_iterations=20, max_linear_iterations=100, **common))
+    rms64, n64 = _reprojection_rms(g64, m)
+    g64.close()
+    target = s64["final_cost"] * (1 + 1e-6)
+    model = TP.load_default_model(device)
+    pre = N.MBA_PRECOND_LEARNED if model is not None else N.MBA_PRECOND_CHAIN
+    g32 = ba.BundleAdjuster(d, device=device)
+    if model is not None:
+        g32.set_preconditioner_model(model)
+    s32 = g32.solve(ba.default_options(max_num_iterations=40, max_linear_iterations=args.fast_pcg, stop_cost=target,
+                                       precision=N.MBA_PRECISION_MIXED, preconditioner=pre, **common))
+    rms32, n32 = _reprojection_rms(g32, m)
+    g32.close()
+    if model is not None:
+        model.close()
+    t64 = s64["iterations"][-1]["time_ms"] / 1e3
+    t32 = s32["time_to_stop_cost_ms"] / 1e3 if s32["time_to_stop_cost_ms"] >= 0 else None
+    return {
+        "workload": f"{args.ba_config}: {d.num_keyframes} keyframes, {d.num_landmarks} landmarks, "
+                    f"{d.num_observations} observations, {d.num_missions} missions",
+        "plain_fp64_s": t64, "plain_fp64_final_cost": s64["final_cost"],
+        "plain_fp64_pcg_iterations": s64["linear_iterations"], "plain_fp64_rejected_landmarks": s64["rejected_landmarks"],
+        "plain_fp64_rms_px": rms64,
+        "mixed_learned_time_to_cost_s": t32, "mixed_learned_final_cost": s32["final_cost"],
+        "mixed_learned_iterations": s32["num_iterations"] - 1, "mixed_learned_pcg_iterations": s32["linear_iterations"],
+        "mixed_learned_rejected_landmarks": s32["rejected_landmarks"], "mixed_learned_rms_px": rms32,
+        "rms_difference_px": abs(rms32 - rms64),
+        "speedup": (t64 / t32) if t32 else None,
+        "preconditioner": "learned" if pre == N.MBA_PRECOND_LEARNED else "chain",
+        "cost_tolerance": "1e-6 relative to the plain FP64 path's 20-iteration cost",
+        "outlier_rejection": "every 3 iterations, depth <= 0" +
+                             (" or reprojection error > 50 px" if args.reproj_rejection else ""),
+    }
+
+
 def run_ours(args):
     import numpy as np
     import torch
@@ -213,27 +275,10 @@ def run_ours(args):
             "traffic": (tr["dram_bytes_per_launch"] if tr else None),
             "algorithmic_bytes_per_launch": alg_bytes}
 
-    # ---- BA time-to-cost-tolerance: plain FP64 vs mixed (rank-local)
+    # ---- BA time-to-cost-tolerance: plain FP64 vs mixed + learned (rank-local)
     ba_info = None
     if args.solve:
-        ba_info = {}
-        opts64 = ba.default_options(max_num_iterations=20, max_linear_iterations=100, linear_tolerance=1e-6,
-                                    check_tolerances=0)
-        g64 = ba.BundleAdjuster(d, device=local)
-        s64 = g64.solve(opts64)
-        g64.close()
-        target = s64["final_cost"] * (1 + 1e-6)
-        opts32 = ba.default_options(max_num_iterations=40, max_linear_iterations=100, linear_tolerance=1e-6,
-                                    check_tolerances=0, precision=N.MBA_PRECISION_MIXED, stop_cost=target)
-        g32 = ba.BundleAdjuster(d, device=local)
-        s32 = g32.solve(opts32)
-        g32.close()
-        ba_info = {"fp64_20_iters_s": s64["total_time_ms"] / 1e3, "fp64_final_cost": s64["final_cost"],
-                   "fp64_initial_cost": s64["initial_cost"], "fp64_pcg_iterations": s64["linear_iterations"],
-                   "mixed_time_to_cost_tol_s": (s32["time_to_stop_cost_ms"] / 1e3
-                                                if s32["time_to_stop_cost_ms"] >= 0 else None),
-                   "mixed_final_cost": s32["final_cost"], "mixed_iterations": s32["num_iterations"] - 1,
-                   "cost_tolerance": "1e-6 relative to the FP64 path's 20-iteration cost"}
+        ba_info = ba_time_to_cost(args, local)
 
     # ---- CPU baseline (rank 0, N=1 only): the oracle on the host cores
     cpu = None
@@ -284,6 +329,9 @@ def main():
     ap.add_argument("--cpu-sample", type=int, default=400_000)
     ap.add_argument("--solve", type=int, default=1)
     ap.add_argument("--skip-cpu", action="store_true")
+    ap.add_argument("--ba-config", default="c4")
+    ap.add_argument("--fast-pcg", type=int, default=25)
+    ap.add_argument("--reproj-rejection", type=int, default=1)
     args = ap.parse_args()
     if args.warmup < 3:
         args.warmup = 3
