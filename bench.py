@@ -173,8 +173,10 @@ def ba_time_to_cost(args, device):
     g32 = ba.BundleAdjuster(d, device=device)
     if model is not None:
         g32.set_preconditioner_model(model)
+    g32.autotune(N.MBA_PRECISION_MIXED)
     s32 = g32.solve(ba.default_options(max_num_iterations=40, max_linear_iterations=args.fast_pcg, stop_cost=target,
-                                       precision=N.MBA_PRECISION_MIXED, preconditioner=pre, **common))
+                                       precision=N.MBA_PRECISION_MIXED, preconditioner=pre, use_cuda_graph=2,
+                                       **common))
     rms32, n32 = _reprojection_rms(g32, m)
     g32.close()
     if model is not None:
@@ -197,6 +199,43 @@ def ba_time_to_cost(args, device):
         "outlier_rejection": "every 3 iterations, depth <= 0" +
                              (" or reprojection error > 50 px" if args.reproj_rejection else ""),
     }
+
+
+def batched_missions(args, device):
+    """64 independent missions of uneven size (50..1500 keyframes) in one
+    problem: autotuned launch parameters, the whole LM loop as one device-
+    driven graph (mixed precision, learned chain preconditioner), against the
+    plain FP64 path's 20-iteration cost."""
+    from maplab_gb300 import _native as N
+    from maplab_gb300 import ba, synth
+    from maplab_gb300 import train_preconditioner as TP
+    m = synth.generate("c3")
+    d = m.desc
+    common = dict(check_tolerances=0, linear_tolerance=1e-6, outlier_use_reprojection_error=args.reproj_rejection)
+    with ba.BundleAdjuster(d, device=device) as g:
+        s64 = g.solve(ba.default_options(max_num_iterations=20, max_linear_iterations=100, **common))
+    target = s64["final_cost"] * (1 + 1e-6)
+    model = TP.load_default_model(device)
+    with ba.BundleAdjuster(d, device=device) as g:
+        t0 = time.perf_counter()
+        tun = g.autotune(N.MBA_PRECISION_MIXED)
+        tune_s = time.perf_counter() - t0
+        pre = N.MBA_PRECOND_CHAIN
+        if model is not None:
+            g.set_preconditioner_model(model)
+            pre = N.MBA_PRECOND_LEARNED
+        s32 = g.solve(ba.default_options(max_num_iterations=40, max_linear_iterations=args.fast_pcg, stop_cost=target,
+                                         precision=N.MBA_PRECISION_MIXED, preconditioner=pre, use_cuda_graph=2,
+                                         **common))
+    if model is not None:
+        model.close()
+    t64 = s64["iterations"][-1]["time_ms"] / 1e3
+    t32 = s32["time_to_stop_cost_ms"] / 1e3 if s32["time_to_stop_cost_ms"] >= 0 else None
+    return {"workload": f"c3: {d.num_missions} independent missions, {d.num_keyframes} keyframes, "
+                        f"{d.num_observations} observations",
+            "tuning": tun, "autotune_s": tune_s, "plain_fp64_s": t64, "plain_fp64_final_cost": s64["final_cost"],
+            "mixed_learned_device_loop_time_to_cost_s": t32, "mixed_learned_iterations": s32["num_iterations"] - 1,
+            "speedup": (t64 / t32) if t32 else None, "launches_per_solve": 1}
 
 
 def run_ours(args):
@@ -277,8 +316,11 @@ def run_ours(args):
 
     # ---- BA time-to-cost-tolerance: plain FP64 vs mixed + learned (rank-local)
     ba_info = None
+    c3_info = None
     if args.solve:
         ba_info = ba_time_to_cost(args, local)
+    if args.c3:
+        c3_info = batched_missions(args, local)
 
     # ---- CPU baseline (rank 0, N=1 only): the oracle on the host cores
     cpu = None
@@ -311,6 +353,7 @@ def run_ours(args):
             "clocks": clk.summary(),
             "gpu_launches": args.steps,
             "ba_time_to_cost_tol": ba_info,
+            "batched_missions": c3_info,
         }
         print(json.dumps(line), flush=True)
     g.close()
@@ -330,6 +373,7 @@ def main():
     ap.add_argument("--solve", type=int, default=1)
     ap.add_argument("--skip-cpu", action="store_true")
     ap.add_argument("--ba-config", default="c4")
+    ap.add_argument("--c3", type=int, default=1)
     ap.add_argument("--fast-pcg", type=int, default=25)
     ap.add_argument("--reproj-rejection", type=int, default=1)
     args = ap.parse_args()

@@ -337,6 +337,23 @@ mba_status mba_gnn_gradient(mba_handle* h, mba_gnn* m, double radius, int32_t np
  * upper j - N_pu; -1: none).  Any pointer may be NULL. */
 mba_status mba_chain_structure(mba_handle* h, int32_t* perm, int32_t* link_edge, int32_t* link_blk);
 
+/* Launch and schedule parameters of one problem (no reference counterpart).
+ * mba_autotune times each candidate on the handle's own data with CUDA
+ * events and keeps the fastest; later solves on the handle use them. */
+typedef struct mba_tuning {
+  int32_t visual_block;         /* threads per block of the evaluation kernel (64, 128, 256) */
+  int32_t schur_chunk;          /* slot pairs summed per thread by the Schur pair kernel */
+  int32_t chain_tail_nodes;     /* chain positions below which one block finishes a chain sweep */
+  int32_t pad_;
+  double visual_ms;             /* per launch, chosen setting */
+  double schur_ms;
+  double chain_apply_ms;
+} mba_tuning;
+mba_status mba_autotune(mba_handle* h, int32_t precision, mba_tuning* out);
+/* Applies tuning values (e.g. cached from an earlier mba_autotune of a
+ * problem of the same shape); a field of 0 keeps the current setting. */
+mba_status mba_set_tuning(mba_handle* h, const mba_tuning* t);
+
 /* Problem statistics (for reports): sizes of the reduced camera system. */
 typedef struct mba_problem_stats {
   int64_t num_keyframes, num_landmarks, num_observations, num_imu_edges;

@@ -161,6 +161,18 @@ class Summary(ctypes.Structure):
     ]
 
 
+class Tuning(ctypes.Structure):
+    _fields_ = [
+        ("visual_block", ctypes.c_int32),
+        ("schur_chunk", ctypes.c_int32),
+        ("chain_tail_nodes", ctypes.c_int32),
+        ("pad_", ctypes.c_int32),
+        ("visual_ms", ctypes.c_double),
+        ("schur_ms", ctypes.c_double),
+        ("chain_apply_ms", ctypes.c_double),
+    ]
+
+
 class ProblemStats(ctypes.Structure):
     _fields_ = [
         ("num_keyframes", ctypes.c_int64),
@@ -299,6 +311,8 @@ def load_ba():
                                                   ctypes.c_float, ctypes.c_uint64, c_double_p])
     _declare(lib, "mba_gnn_gradient", ctypes.c_int, [vp, vp, ctypes.c_double, ctypes.c_int32, f32p, ctypes.c_uint64,
                                                      f32p, c_double_p, c_double_p])
+    _declare(lib, "mba_autotune", ctypes.c_int, [vp, ctypes.c_int32, ctypes.POINTER(Tuning)])
+    _declare(lib, "mba_set_tuning", ctypes.c_int, [vp, ctypes.POINTER(Tuning)])
     _declare(lib, "mba_chain_structure", ctypes.c_int, [vp, i32p, i32p, i32p])
     _declare(lib, "mba_rejected_landmarks", ctypes.c_int, [vp, ctypes.POINTER(ctypes.c_uint8), ctypes.POINTER(ctypes.c_int64)])
     _declare(lib, "mba_reduced_system", ctypes.c_int,

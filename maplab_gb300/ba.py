@@ -239,6 +239,18 @@ class BundleAdjuster:
                                           N.ptr(coef)), "mba_gnn_gradient")
         return loss.value, grad, coef
 
+    def autotune(self, precision=N.MBA_PRECISION_MIXED):
+        """Times launch / schedule candidates on this problem and keeps the fastest."""
+        t = N.Tuning()
+        _check(self._lib.mba_autotune(self._h, precision, ctypes.byref(t)), "mba_autotune")
+        return {f: getattr(t, f) for f, _ in t._fields_ if f != "pad_"}
+
+    def set_tuning(self, **kw):
+        t = N.Tuning()
+        for k, v in kw.items():
+            setattr(t, k, v)
+        _check(self._lib.mba_set_tuning(self._h, ctypes.byref(t)), "mba_set_tuning")
+
     def chain_structure(self):
         n = self.desc.num_keyframes
         perm = np.zeros(n, dtype=np.int32); le = np.zeros(n, dtype=np.int32); lb = np.zeros(n, dtype=np.int32)

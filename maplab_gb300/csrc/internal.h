@@ -13,6 +13,8 @@ namespace mba {
 // Observations are sorted by landmark (contiguous per landmark).
 struct DevProblem {
   int64_t nkf, nlm, nobs, ncam, nmis, nedge, nsamp;
+  int32_t vis_block;        // threads per block of the evaluation kernel (tuned; 0 = default)
+  int32_t pad_;
   // observations
   const double2* obs_uv;
   const double* obs_sinv;   // 1 / sigma
@@ -100,7 +102,8 @@ template <typename T>
 cudaError_t launch_visual_linearize_gated(const DevProblem& P, VisualLin<T> out, double* cost_accum, const int* run_if,
                                           const int* skip_if, cudaStream_t s);
 cudaError_t launch_visual_cost_gated(const DevProblem& P, const double* kf_state, const double* lm_p,
-                                     double* cost_accum, int* nonfinite, const int* skip_if, cudaStream_t s);
+                                     double* cost_accum, int* nonfinite, const int* skip_if, cudaStream_t s,
+                                     const int* run_if = nullptr);
 cudaError_t launch_inertial_gated(const DevProblem& P, const double* kf_state, InertialLin<double> lin,
                                   double* cost_accum, int* status, const int* skip_if, cudaStream_t s,
                                   bool f32 = false);
@@ -122,6 +125,6 @@ cudaError_t launch_inertial_f32(const DevProblem& P, const InertialLin<double>& 
 // <= 0 in the observing camera or, if use_reprojection, a reprojection error
 // above max_px.  Newly rejected landmarks are counted into *count.
 cudaError_t launch_find_outliers(const DevProblem& P, int use_reprojection, double max_px, int* count,
-                                 const int* skip_if, cudaStream_t s);
+                                 const int* run_if, const int* skip_if, cudaStream_t s);
 
 }  // namespace mba

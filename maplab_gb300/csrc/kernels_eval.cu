@@ -291,8 +291,9 @@ __device__ void obs_point_C(const DevProblem& P, const double* kf_state, const d
 }
 
 __global__ void __launch_bounds__(kBlock) k_visual_cost(DevProblem P, const double* kf_state, const double* lm_p,
-                                                        double* cost_accum, int* nonfinite, const int* skip_if) {
-  if (gated(nullptr, skip_if)) return;
+                                                        double* cost_accum, int* nonfinite, const int* run_if,
+                                                        const int* skip_if) {
+  if (gated(run_if, skip_if)) return;
   const int64_t i = blockIdx.x * (int64_t)blockDim.x + threadIdx.x;
   double cost = 0.0;
   if (i < P.nobs && !P.lm_off[P.obs_lm[i]]) {
@@ -319,8 +320,8 @@ __global__ void __launch_bounds__(kBlock) k_visual_cost(DevProblem P, const doub
 // p_C.z <= 0, or (optionally) squared reprojection error in pixels above
 // max_px^2, marks the landmark.  Landmarks already out are skipped.
 __global__ void __launch_bounds__(kBlock) k_find_outliers(DevProblem P, int use_reprojection, double max_px2,
-                                                          int* count, const int* skip_if) {
-  if (gated(nullptr, skip_if)) return;
+                                                          int* count, const int* run_if, const int* skip_if) {
+  if (gated(run_if, skip_if)) return;
   const int64_t i = blockIdx.x * (int64_t)blockDim.x + threadIdx.x;
   if (i >= P.nobs) return;
   const int lm = P.obs_lm[i];
@@ -537,11 +538,13 @@ template <typename T>
 cudaError_t launch_visual_linearize_gated(const DevProblem& P, VisualLin<T> out, double* cost_accum, const int* run_if,
                                           const int* skip_if, cudaStream_t s) {
   if (P.nobs == 0) return cudaSuccess;
-  const int64_t blocks = (P.nobs + kBlock - 1) / kBlock;
+  // Block size: tuned per problem (mba_autotune), at most the launch bound.
+  const int bs = (P.vis_block > 0 && P.vis_block <= kBlock) ? P.vis_block : kBlock;
+  const int64_t blocks = (P.nobs + bs - 1) / bs;
   if (cost_accum)
-    k_visual_linearize<T, true><<<(unsigned)blocks, kBlock, 0, s>>>(P, visual_inputs<T>(P), out, cost_accum, run_if, skip_if);
+    k_visual_linearize<T, true><<<(unsigned)blocks, bs, 0, s>>>(P, visual_inputs<T>(P), out, cost_accum, run_if, skip_if);
   else
-    k_visual_linearize<T, false><<<(unsigned)blocks, kBlock, 0, s>>>(P, visual_inputs<T>(P), out, nullptr, run_if, skip_if);
+    k_visual_linearize<T, false><<<(unsigned)blocks, bs, 0, s>>>(P, visual_inputs<T>(P), out, nullptr, run_if, skip_if);
   return cudaGetLastError();
 }
 template <typename T>
@@ -556,18 +559,19 @@ template cudaError_t launch_visual_linearize_gated<float>(const DevProblem&, Vis
                                                           const int*, cudaStream_t);
 
 cudaError_t launch_find_outliers(const DevProblem& P, int use_reprojection, double max_px, int* count,
-                                 const int* skip_if, cudaStream_t s) {
+                                 const int* run_if, const int* skip_if, cudaStream_t s) {
   if (P.nobs == 0) return cudaSuccess;
   const int64_t blocks = (P.nobs + kBlock - 1) / kBlock;
-  k_find_outliers<<<(unsigned)blocks, kBlock, 0, s>>>(P, use_reprojection, max_px * max_px, count, skip_if);
+  k_find_outliers<<<(unsigned)blocks, kBlock, 0, s>>>(P, use_reprojection, max_px * max_px, count, run_if, skip_if);
   return cudaGetLastError();
 }
 
 cudaError_t launch_visual_cost_gated(const DevProblem& P, const double* kf_state, const double* lm_p,
-                                     double* cost_accum, int* nonfinite, const int* skip_if, cudaStream_t s) {
+                                     double* cost_accum, int* nonfinite, const int* skip_if, cudaStream_t s,
+                                     const int* run_if) {
   if (P.nobs == 0) return cudaSuccess;
   const int64_t blocks = (P.nobs + kBlock - 1) / kBlock;
-  k_visual_cost<<<(unsigned)blocks, kBlock, 0, s>>>(P, kf_state, lm_p, cost_accum, nonfinite, skip_if);
+  k_visual_cost<<<(unsigned)blocks, kBlock, 0, s>>>(P, kf_state, lm_p, cost_accum, nonfinite, run_if, skip_if);
   return cudaGetLastError();
 }
 cudaError_t launch_visual_cost(const DevProblem& P, const double* kf_state, const double* lm_p, double* cost_accum,

@@ -205,7 +205,8 @@ __global__ void __launch_bounds__(128) k_assemble_inertial(DevProblem P, Inertia
 // Jacobi scaling from the unscaled diagonal of J^T J (first linearization
 // only); FP64 and T copies of the scale vectors.
 template <typename T>
-__global__ void k_scale(DevProblem P, LinearSystem<T> L, ScaleVectors sc, int jacobi) {
+__global__ void k_scale(DevProblem P, LinearSystem<T> L, ScaleVectors sc, int jacobi, const int* run_if) {
+  if (run_if && !*run_if) return;
   const int64_t i = blockIdx.x * (int64_t)blockDim.x + threadIdx.x;
   const int64_t nk = 15 * P.nkf, nl = 3 * P.nlm;
   if (i < nk) {
@@ -832,6 +833,8 @@ __global__ void k_decide(LmControl* ctl, LmParams prm, mba_iteration_summary* lo
   }
   if (!ctl->terminated && ctl->radius < prm.min_radius) { ctl->terminated = 1; ctl->termination = 4; }
   if (!ctl->terminated && it >= prm.max_num_iterations) { ctl->terminated = 1; ctl->termination = 0; }
+  // maplab's outlier-rejection solve restarts every n iterations (not after the last one).
+  ctl->restart_now = !ctl->terminated && prm.reject_every > 0 && it % prm.reject_every == 0;
   if (log && it <= prm.max_num_iterations) {
     mba_iteration_summary& e = log[it];
     e.iteration = it;
@@ -843,7 +846,9 @@ __global__ void k_decide(LmControl* ctl, LmParams prm, mba_iteration_summary* lo
     e.step_norm = step_norm;
     e.relative_decrease = rel;
     e.trust_region_radius = ctl->radius;
-    e.iteration_time_ms = 0.0;
+    unsigned long long now;
+    asm volatile("mov.u64 %0, %%globaltimer;" : "=l"(now));
+    e.iteration_time_ms = ctl->t0_ns ? (double)(now - ctl->t0_ns) * 1e-6 : 0.0;
   }
 }
 
@@ -941,7 +946,7 @@ cudaError_t solver_assemble(const SolverLaunch<T>& s, const int* gate, cudaStrea
 template <typename T>
 cudaError_t solver_compute_scale(const SolverLaunch<T>& s, int jacobi, cudaStream_t st) {
   const int64_t n = 15 * s.P.nkf + 3 * s.P.nlm;
-  k_scale<T><<<nblk(n, kB), kB, 0, st>>>(s.P, s.L, s.sc, jacobi);
+  k_scale<T><<<nblk(n, kB), kB, 0, st>>>(s.P, s.L, s.sc, jacobi, nullptr);
   const int64_t m = 12 * s.P.nlm + 18 * s.S.nslot + 240 * s.P.nkf + 36 * s.S.npu + 225 * s.P.nedge;
   k_scale_inplace<T><<<gridcap(m), kB, 0, st>>>(s.P, s.S, s.L, nullptr, nullptr);
   return cudaGetLastError();
@@ -962,6 +967,12 @@ cudaError_t solver_build_reduced(const SolverLaunch<T>& s, cudaStream_t st) {
     if (e != cudaSuccess) return e;
     return chain_factor<T>(s, st);
   }
+  return cudaGetLastError();
+}
+
+template <typename T>
+cudaError_t solver_schur_pairs(const SolverLaunch<T>& s, cudaStream_t st) {
+  if (s.S.nchunk) k_schur_pairs<T><<<nblk(s.S.nchunk, kB), kB, 0, st>>>(s);
   return cudaGetLastError();
 }
 
@@ -1021,34 +1032,69 @@ cudaError_t solver_relinearize(const SolverLaunch<T>& s, const InertialLin<doubl
   return solver_assemble<T>(s, &s.ctl->accepted, st);
 }
 
+// Outlier rejection + restart, run when ctl->restart_now (set by k_decide).
 __global__ void k_restart_begin(LmControl* ctl) {
-  if (ctl->terminated) return;
+  if (!ctl->restart_now) return;
   ctl->cost = 0.0;
+  ctl->reject_count = 0;
 }
 
-__global__ void k_restart_end(LmControl* ctl, const int* count) {
-  if (ctl->terminated) return;
+__global__ void k_restart_end(LmControl* ctl) {
+  if (!ctl->restart_now) return;
   ctl->cost += ctl->cost_ine;
   ctl->decrease_factor = 2.0;
-  ctl->rejected += *count;
+  ctl->rejected += ctl->reject_count;
 }
 
 template <typename T>
 cudaError_t solver_reject_and_restart(const SolverLaunch<T>& s, int use_reprojection, double max_px, int jacobi,
                                       cudaStream_t st) {
   LmControl* c = s.ctl;
-  int* count = &c->reject_count;
-  cudaError_t e = cudaMemsetAsync(count, 0, sizeof(int), st);
-  if (e == cudaSuccess) e = launch_find_outliers(s.P, use_reprojection, max_px, count, &c->terminated, st);
-  if (e != cudaSuccess) return e;
+  const int* run = &c->restart_now;
   k_restart_begin<<<1, 1, 0, st>>>(c);
-  e = launch_visual_cost_gated(s.P, s.P.kf_state, s.P.lm_p, &c->cost, nullptr, &c->terminated, st);
+  cudaError_t e = launch_find_outliers(s.P, use_reprojection, max_px, &c->reject_count, run, nullptr, st);
+  if (e == cudaSuccess) e = launch_visual_cost_gated(s.P, s.P.kf_state, s.P.lm_p, &c->cost, nullptr, nullptr, st, run);
   if (e != cudaSuccess) return e;
-  k_restart_end<<<1, 1, 0, st>>>(c, count);
-  e = launch_visual_linearize_gated<T>(s.P, s.vis, nullptr, nullptr, &c->terminated, st);
-  if (e == cudaSuccess) e = solver_assemble<T>(s, nullptr, st);
-  if (e == cudaSuccess) e = solver_compute_scale<T>(s, jacobi, st);
-  return e;
+  k_restart_end<<<1, 1, 0, st>>>(c);
+  e = launch_visual_linearize_gated<T>(s.P, s.vis, nullptr, run, nullptr, st);
+  if (e != cudaSuccess) return e;
+  // Fresh assembly and Jacobi scaling (the restarted Ceres solve rescales).
+  k_zero<T><<<gridcap(225 * s.P.nkf), kB, 0, st>>>(s.L.Dbase, 225 * s.P.nkf, run, nullptr);
+  k_zero<T><<<gridcap(15 * s.P.nkf), kB, 0, st>>>(s.L.gc, 15 * s.P.nkf, run, nullptr);
+  if (s.S.npu) k_zero<T><<<gridcap(36 * s.S.npu), kB, 0, st>>>(s.L.Pbase, 36 * s.S.npu, run, nullptr);
+  if (s.P.nlm) k_assemble_lm<T><<<nblk(s.P.nlm, kB), kB, 0, st>>>(s.P, s.S, s.vis, s.L, run, nullptr);
+  if (s.P.nedge) k_assemble_inertial<T><<<nblk(32 * s.P.nedge, 128), 128, 0, st>>>(s.P, s.ine, s.L, run, nullptr);
+  const int64_t n = 15 * s.P.nkf + 3 * s.P.nlm;
+  k_scale<T><<<nblk(n, kB), kB, 0, st>>>(s.P, s.L, s.sc, jacobi, run);
+  const int64_t m = 12 * s.P.nlm + 18 * s.S.nslot + 240 * s.P.nkf + 36 * s.S.npu + 225 * s.P.nedge;
+  k_scale_inplace<T><<<gridcap(m), kB, 0, st>>>(s.P, s.S, s.L, run, nullptr);
+  return cudaGetLastError();
+}
+
+__global__ void k_loop_start(LmControl* ctl) {
+  unsigned long long now;
+  asm volatile("mov.u64 %0, %%globaltimer;" : "=l"(now));
+  ctl->t0_ns = now;
+}
+
+__global__ void k_loop_control(LmControl* ctl, cudaGraphConditionalHandle handle, const volatile int* cancel) {
+  if (!ctl->terminated && cancel && *cancel) {
+    ctl->terminated = 1;
+    ctl->termination = 5;
+  }
+  ctl->loop_active = !ctl->terminated;
+  cudaGraphSetConditional(handle, ctl->terminated ? 0u : 1u);
+}
+
+cudaError_t solver_loop_start(LmControl* ctl, cudaStream_t st) {
+  k_loop_start<<<1, 1, 0, st>>>(ctl);
+  return cudaGetLastError();
+}
+
+cudaError_t solver_loop_control(LmControl* ctl, cudaGraphConditionalHandle handle, const volatile int* cancel,
+                                cudaStream_t st) {
+  k_loop_control<<<1, 1, 0, st>>>(ctl, handle, cancel);
+  return cudaGetLastError();
 }
 
 template cudaError_t solver_assemble<double>(const SolverLaunch<double>&, const int*, cudaStream_t);
@@ -1057,6 +1103,8 @@ template cudaError_t solver_compute_scale<double>(const SolverLaunch<double>&, i
 template cudaError_t solver_compute_scale<float>(const SolverLaunch<float>&, int, cudaStream_t);
 template cudaError_t solver_build_reduced<double>(const SolverLaunch<double>&, cudaStream_t);
 template cudaError_t solver_build_reduced<float>(const SolverLaunch<float>&, cudaStream_t);
+template cudaError_t solver_schur_pairs<double>(const SolverLaunch<double>&, cudaStream_t);
+template cudaError_t solver_schur_pairs<float>(const SolverLaunch<float>&, cudaStream_t);
 template cudaError_t solver_step<double>(const SolverLaunch<double>&, cudaStream_t);
 template cudaError_t solver_step<float>(const SolverLaunch<float>&, cudaStream_t);
 template cudaError_t solver_evaluate_candidate<double>(const SolverLaunch<double>&, InertialLin<double>, cudaStream_t);

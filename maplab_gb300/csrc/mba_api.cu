@@ -168,9 +168,39 @@ struct mba_handle {
   GnnWork gw{};
   bool gw_ready = false;
   mba_gnn* model = nullptr;
+  // options of the running solve read while recording the iteration graph
+  int outlier_reproj = 0;
+  double outlier_max_px = 50.0;
+  int jacobi = 1;
+  // cancellation seen by the device-driven loop (mapped pinned host memory)
+  volatile int* cancel_host = nullptr;
+  const volatile int* cancel_dev = nullptr;
+  // Schur pair targets in kernel order (pair range per target) for re-cutting
+  // the chunks under a tuned chunk size
+  std::vector<int64_t> tgt_off, tgt_order;
+  mba_tuning tuning{};
 };
 
 namespace {
+
+// Cuts each target's contiguous pair range [off[r], off[r+1]) into chunks of
+// at most `chunk` pairs (one thread each); a target spanning several chunks
+// is marked by the bitwise-not of its id.
+void cut_chunks(const std::vector<int64_t>& off, const std::vector<int64_t>& order, int64_t chunk,
+                std::vector<int32_t>* tgt, std::vector<int64_t>* coff) {
+  tgt->clear();
+  coff->assign(1, 0);
+  const int64_t ntgt = (int64_t)order.size();
+  for (int64_t r = 0; r < ntgt; ++r) {
+    const int64_t b0 = off[r], b1 = off[r + 1];
+    if (b1 == b0) continue;
+    const bool whole = b1 - b0 <= chunk;
+    for (int64_t c0 = b0; c0 < b1; c0 += chunk) {
+      tgt->push_back(whole ? (int32_t)order[r] : ~(int32_t)order[r]);
+      coff->push_back(std::min(b1, c0 + chunk));
+    }
+  }
+}
 
 mba_status cuda_status(cudaError_t e) { return e == cudaSuccess ? MBA_OK : MBA_ERR_CUDA; }
 
@@ -325,6 +355,10 @@ SolverLaunch<T> make_launch(mba_handle* h, SolverBuffers<T>& b, const mba_solver
   s.prm.max_num_iterations = o.max_num_iterations;
   s.prm.max_linear_iterations = std::max(1, o.max_linear_iterations);
   s.prm.check_tolerances = o.check_tolerances;
+  s.prm.reject_every = std::max(0, o.reject_outliers_every_n_iters);
+  h->outlier_reproj = o.outlier_use_reprojection_error;
+  h->outlier_max_px = o.outlier_max_reprojection_error_px;
+  h->jacobi = o.jacobi_scaling;
   s.prm.max_radius = o.max_trust_region_radius;
   s.prm.min_radius = o.min_trust_region_radius;
   s.prm.function_tolerance = o.function_tolerance;
@@ -380,6 +414,8 @@ cudaError_t record_iteration(mba_handle* h, const SolverLaunch<T>& s) {
   if (e == cudaSuccess) e = solver_evaluate_candidate<T>(s, h->ine_cand, st);
   if (e == cudaSuccess) e = solver_decide_and_accept<T>(s, h->ine_cand, h->ine_cur, st);
   if (e == cudaSuccess) e = solver_relinearize<T>(s, h->ine_cur, st);
+  if (e == cudaSuccess && s.prm.reject_every > 0)
+    e = solver_reject_and_restart<T>(s, h->outlier_reproj, h->outlier_max_px, h->jacobi, st);
   return e;
 }
 
@@ -404,27 +440,48 @@ mba_status run_solve(mba_handle* h, const mba_solver_options& o, mba_summary* su
   SolverLaunch<T> s = make_launch<T>(h, b, o);
   cudaStream_t st = h->stream;
   cudaError_t e = cudaSuccess;
-  cudaEvent_t ev0, ev1;
-  cudaEventCreate(&ev0);
-  cudaEventCreate(&ev1);
-  std::vector<cudaEvent_t> evs(o.max_num_iterations);
-  for (auto& ev : evs) cudaEventCreate(&ev);
-  cudaEventRecord(ev0, st);
-  // Initial evaluation: FP64 cost, inertial linearization, visual linearization, assembly, scaling.
-  e = solver_init_control(h->ctl, o.initial_trust_region_radius, st);
-  if (e == cudaSuccess) e = linearize_current<T>(h, b, s, o.jacobi_scaling, st);
-  if (e != cudaSuccess) return MBA_ERR_CUDA;
-  double initial_cost = 0.0;
-  int flags[2] = {0, 0};
-  e = cudaMemcpyAsync(&initial_cost, &h->ctl->cost, sizeof(double), cudaMemcpyDeviceToHost, st);
-  if (e == cudaSuccess) e = cudaMemcpyAsync(flags, h->iscratch, 2 * sizeof(int), cudaMemcpyDeviceToHost, st);
-  if (e == cudaSuccess) e = cudaStreamSynchronize(st);
-  if (e != cudaSuccess) return MBA_ERR_CUDA;
-  if (flags[1]) return (mba_status)flags[1];
-  if (flags[0] || !std::isfinite(initial_cost)) return MBA_ERR_NON_FINITE;
-  // Capture one LM iteration as a graph (or launch it eagerly).
-  cudaGraphExec_t exec = nullptr, restart = nullptr;
-  if (o.use_cuda_graph) {
+  // Graphs first (host work outside the timed region): the whole LM loop as
+  // one graph with a device-evaluated while condition, or one iteration per
+  // graph launched from the host.
+  cudaGraphExec_t exec = nullptr;
+  bool device_loop = false;
+  if (o.use_cuda_graph == 2) {
+    cudaGraph_t graph = nullptr;
+    cudaGraphConditionalHandle cond;
+    e = cudaGraphCreate(&graph, 0);
+    if (e == cudaSuccess) e = cudaGraphConditionalHandleCreate(&cond, graph, 1, cudaGraphCondAssignDefault);
+    // cudaGraphNodeParams (a union of node parameter types) is zero-initialised storage.
+    alignas(cudaGraphNodeParams) unsigned char np_raw[sizeof(cudaGraphNodeParams)];
+    std::memset(np_raw, 0, sizeof(np_raw));
+    cudaGraphNodeParams& np = *reinterpret_cast<cudaGraphNodeParams*>(np_raw);
+    np.type = cudaGraphNodeTypeConditional;
+    np.conditional.handle = cond;
+    np.conditional.type = cudaGraphCondTypeWhile;
+    np.conditional.size = 1;
+    cudaGraphNode_t node;
+    if (e == cudaSuccess) e = cudaGraphAddNode(&node, graph, nullptr, nullptr, 0, &np);
+    if (e == cudaSuccess) {
+      cudaGraph_t body = np.conditional.phGraph_out[0];
+      e = cudaStreamBeginCaptureToGraph(st, body, nullptr, nullptr, 0, cudaStreamCaptureModeThreadLocal);
+      if (e == cudaSuccess) {
+        cudaError_t e2 = record_iteration<T>(h, s);
+        if (e2 == cudaSuccess) e2 = solver_loop_control(h->ctl, cond, h->cancel_dev, st);
+        e = cudaStreamEndCapture(st, &body);
+        if (e2 != cudaSuccess) e = e2;
+      }
+    }
+    if (e == cudaSuccess) e = cudaGraphInstantiate(&exec, graph, 0);
+    if (graph) cudaGraphDestroy(graph);
+    if (e == cudaSuccess) {
+      device_loop = true;
+    } else {  // no conditional nodes here: fall back to one graph per iteration
+      if (exec) cudaGraphExecDestroy(exec);
+      exec = nullptr;
+      cudaGetLastError();
+      e = cudaSuccess;
+    }
+  }
+  if (!exec && o.use_cuda_graph) {
     cudaGraph_t graph = nullptr;
     e = cudaStreamBeginCapture(st, cudaStreamCaptureModeThreadLocal);
     if (e == cudaSuccess) {
@@ -434,60 +491,62 @@ mba_status run_solve(mba_handle* h, const mba_solver_options& o, mba_summary* su
     }
     if (e == cudaSuccess) e = cudaGraphInstantiate(&exec, graph, 0);
     if (graph) cudaGraphDestroy(graph);
-    graph = nullptr;
-    if (e == cudaSuccess && o.reject_outliers_every_n_iters > 0) {
-      e = cudaStreamBeginCapture(st, cudaStreamCaptureModeThreadLocal);
-      if (e == cudaSuccess) {
-        cudaError_t e2 = solver_reject_and_restart<T>(s, o.outlier_use_reprojection_error,
-                                                      o.outlier_max_reprojection_error_px, o.jacobi_scaling, st);
-        e = cudaStreamEndCapture(st, &graph);
-        if (e2 != cudaSuccess) e = e2;
-      }
-      if (e == cudaSuccess) e = cudaGraphInstantiate(&restart, graph, 0);
-      if (graph) cudaGraphDestroy(graph);
-    }
     if (e != cudaSuccess) {
       if (exec) cudaGraphExecDestroy(exec);
       return MBA_ERR_CUDA;
     }
   }
+  if (h->cancel_host) *h->cancel_host = 0;
+  cudaEvent_t ev0;
+  cudaEventCreate(&ev0);
+  std::vector<cudaEvent_t> evs(device_loop ? 0 : o.max_num_iterations);
+  for (auto& ev : evs) cudaEventCreate(&ev);
   const auto t0 = std::chrono::steady_clock::now();
   cudaEventRecord(ev0, st);
-  int launched = 0;
+  // Initial evaluation: FP64 cost, inertial linearization, visual linearization, assembly, scaling.
+  e = solver_init_control(h->ctl, o.initial_trust_region_radius, st);
+  if (e == cudaSuccess) e = solver_loop_start(h->ctl, st);
+  if (e == cudaSuccess) e = linearize_current<T>(h, b, s, o.jacobi_scaling, st);
+  double initial_cost = 0.0;
+  int flags[2] = {0, 0};
+  if (e == cudaSuccess) e = cudaMemcpyAsync(&initial_cost, &h->ctl->cost, sizeof(double), cudaMemcpyDeviceToHost, st);
+  if (e == cudaSuccess) e = cudaMemcpyAsync(flags, h->iscratch, 2 * sizeof(int), cudaMemcpyDeviceToHost, st);
+  if (e == cudaSuccess) e = cudaStreamSynchronize(st);
   mba_status result = MBA_OK;
-  for (int it = 0; it < o.max_num_iterations; ++it) {
-    if (h->cancel.load()) { result = MBA_ERR_CANCELLED; break; }
-    e = exec ? cudaGraphLaunch(exec, st) : record_iteration<T>(h, s);
-    if (e != cudaSuccess) break;
-    // maplab's outlier-rejection solver: every n iterations, drop outlier
-    // landmarks and restart (scaling, cost, linearization; radius kept).
-    const int nrej = o.reject_outliers_every_n_iters;
-    if (nrej > 0 && (it + 1) % nrej == 0 && it + 1 < o.max_num_iterations) {
-      e = restart ? cudaGraphLaunch(restart, st)
-                  : solver_reject_and_restart<T>(s, o.outlier_use_reprojection_error,
-                                                 o.outlier_max_reprojection_error_px, o.jacobi_scaling, st);
+  if (e != cudaSuccess) result = MBA_ERR_CUDA;
+  else if (flags[1]) result = (mba_status)flags[1];
+  else if (flags[0] || !std::isfinite(initial_cost)) result = MBA_ERR_NON_FINITE;
+  int launched = 0;
+  if (result == MBA_OK && device_loop) {
+    e = cudaGraphLaunch(exec, st);
+    launched = o.max_num_iterations;
+  } else if (result == MBA_OK) {
+    for (int it = 0; it < o.max_num_iterations; ++it) {
+      if (h->cancel.load()) { result = MBA_ERR_CANCELLED; break; }
+      e = exec ? cudaGraphLaunch(exec, st) : record_iteration<T>(h, s);
       if (e != cudaSuccess) break;
-    }
-    cudaEventRecord(evs[it], st);
-    ++launched;
-    // Poll for early termination every few iterations without stalling the queue.
-    if ((it & 3) == 3) {
-      int term = 0;
-      cudaMemcpyAsync(&term, &h->ctl->terminated, sizeof(int), cudaMemcpyDeviceToHost, st);
-      cudaStreamSynchronize(st);
-      if (term) break;
+      cudaEventRecord(evs[it], st);
+      ++launched;
+      // Poll for early termination every few iterations without stalling the queue.
+      if ((it & 3) == 3) {
+        int term = 0;
+        cudaMemcpyAsync(&term, &h->ctl->terminated, sizeof(int), cudaMemcpyDeviceToHost, st);
+        cudaStreamSynchronize(st);
+        if (term) break;
+      }
     }
   }
   if (e == cudaSuccess) e = cudaStreamSynchronize(st);
   const double wall_ms = std::chrono::duration<double, std::milli>(std::chrono::steady_clock::now() - t0).count();
   if (exec) cudaGraphExecDestroy(exec);
-  if (restart) cudaGraphExecDestroy(restart);
-  if (e != cudaSuccess) return MBA_ERR_CUDA;
+  if (e != cudaSuccess) result = MBA_ERR_CUDA;
   LmControl c;
-  cudaMemcpy(&c, h->ctl, sizeof(c), cudaMemcpyDeviceToHost);
+  std::memset(&c, 0, sizeof(c));
+  if (result == MBA_OK || result == MBA_ERR_CANCELLED) cudaMemcpy(&c, h->ctl, sizeof(c), cudaMemcpyDeviceToHost);
+  if (device_loop && c.termination == 5) result = MBA_ERR_CANCELLED;
   std::vector<mba_iteration_summary> log(o.max_num_iterations + 1);
   cudaMemcpy(log.data(), h->log, sizeof(mba_iteration_summary) * log.size(), cudaMemcpyDeviceToHost);
-  if (sum) {
+  if (sum && (result == MBA_OK || result == MBA_ERR_CANCELLED)) {
     sum->initial_cost = initial_cost;
     sum->final_cost = c.cost;
     sum->num_iterations = c.iteration + 1;
@@ -497,11 +556,15 @@ mba_status run_solve(mba_handle* h, const mba_solver_options& o, mba_summary* su
     sum->total_time_ms = wall_ms;
     sum->time_to_stop_cost_ms = -1.0;
     sum->num_rejected_landmarks = c.rejected;
-    if (c.stop_iteration > 0 && c.stop_iteration <= launched) {
+    // Times from the first launch of the solve: device global timer (device
+    // loop) or events after each iteration (host loop).
+    auto iter_ms = [&](int it) -> double {
+      if (device_loop) return log[it].iteration_time_ms;
       float ms = 0.f;
-      cudaEventElapsedTime(&ms, ev0, evs[c.stop_iteration - 1]);
-      sum->time_to_stop_cost_ms = ms;
-    }
+      if (it - 1 < launched) cudaEventElapsedTime(&ms, ev0, evs[it - 1]);
+      return ms;
+    };
+    if (c.stop_iteration > 0 && c.stop_iteration <= launched) sum->time_to_stop_cost_ms = iter_ms(c.stop_iteration);
     if (sum->iterations && sum->max_iterations_capacity > 0) {
       mba_iteration_summary& z = sum->iterations[0];
       std::memset(&z, 0, sizeof(z));
@@ -510,15 +573,12 @@ mba_status run_solve(mba_handle* h, const mba_solver_options& o, mba_summary* su
       z.trust_region_radius = o.initial_trust_region_radius;
       for (int it = 1; it <= c.iteration && it < sum->max_iterations_capacity; ++it) {
         sum->iterations[it] = log[it];
-        float ms = 0.f;
-        if (it - 1 < launched) cudaEventElapsedTime(&ms, ev0, evs[it - 1]);
-        sum->iterations[it].iteration_time_ms = ms;
+        sum->iterations[it].iteration_time_ms = iter_ms(it);
       }
     }
   }
   for (auto& ev : evs) cudaEventDestroy(ev);
   cudaEventDestroy(ev0);
-  cudaEventDestroy(ev1);
   return result;
 }
 
@@ -720,6 +780,19 @@ mba_status mba_create(const mba_problem_desc* d, int32_t device, mba_handle** ou
   if (!h) return MBA_ERR_CUDA;
   h->device = device;
   if (cudaStreamCreateWithFlags(&h->stream, cudaStreamNonBlocking) != cudaSuccess) { delete h; return MBA_ERR_CUDA; }
+  {
+    void* hp = nullptr;
+    void* dp = nullptr;
+    if (cudaHostAlloc(&hp, sizeof(int), cudaHostAllocMapped) == cudaSuccess &&
+        cudaHostGetDevicePointer(&dp, hp, 0) == cudaSuccess) {
+      h->cancel_host = static_cast<volatile int*>(hp);
+      *h->cancel_host = 0;
+      h->cancel_dev = static_cast<const volatile int*>(dp);
+    } else if (hp) {
+      cudaFreeHost(hp);
+    }
+    cudaGetLastError();
+  }
   cudaStream_t st = h->stream;
 
   // ---- observation types and landmark-sorted order
@@ -851,16 +924,9 @@ mba_status mba_create(const mba_problem_desc* d, int32_t device, mba_handle** ou
         pa[dst] = ta[q]; pb[dst] = tb[q];
       }
     }
-    chunk_off.push_back(0);
-    for (int64_t r = 0; r < ntgt; ++r) {
-      const int64_t b0 = cnt[r], b1 = cnt[r + 1];
-      if (b1 == b0) continue;
-      const bool whole = b1 - b0 <= kSchurChunk;
-      for (int64_t c0 = b0; c0 < b1; c0 += kSchurChunk) {
-        chunk_tgt.push_back(whole ? (int32_t)order[r] : ~(int32_t)order[r]);
-        chunk_off.push_back(std::min(b1, c0 + kSchurChunk));
-      }
-    }
+    cut_chunks(cnt, order, kSchurChunk, &chunk_tgt, &chunk_off);
+    h->tgt_off = std::move(cnt);
+    h->tgt_order = std::move(order);
   }
   const int64_t npu = pm.count;
   std::vector<int64_t> row_off(NK + 1, 0);
@@ -1080,6 +1146,9 @@ mba_status mba_create(const mba_problem_desc* d, int32_t device, mba_handle** ou
   S.chain_tail = 0;
   while (S.chain_tail < S.chain_levels && ((NK + ((int64_t)1 << S.chain_tail) - 1) >> S.chain_tail) > 128)
     ++S.chain_tail;
+  h->tuning.visual_block = 256;
+  h->tuning.schur_chunk = (int32_t)kSchurChunk;
+  h->tuning.chain_tail_nodes = 128;
   // Inertial scratch (kernels_inertial.cu): dt per step, end state per edge,
   // 4 RK4 stages x 15 values per step.
   P.ine_scratch = A.alloc<double>((NSMP - NE) + 16 * NE + 60 * (NSMP - NE) + 1);
@@ -1098,6 +1167,7 @@ void mba_destroy(mba_handle* h) {
   cudaSetDevice(h->device);
   if (h->stream) cudaStreamSynchronize(h->stream);
   h->arena.release();
+  if (h->cancel_host) cudaFreeHost((void*)h->cancel_host);
   if (h->stream) cudaStreamDestroy(h->stream);
   delete h;
 }
@@ -1246,7 +1316,9 @@ mba_status mba_write_state(mba_handle* h, const double* kx, const double* kv, co
 }
 
 void mba_cancel(mba_handle* h) {
-  if (h) h->cancel.store(1);
+  if (!h) return;
+  h->cancel.store(1);
+  if (h->cancel_host) *h->cancel_host = 1;  // seen by the device-driven loop
 }
 
 mba_status mba_time_visual_kernel(mba_handle* h, int32_t mode, int32_t iters, double* ms_per_launch) {
@@ -1508,6 +1580,132 @@ mba_status mba_chain_structure(mba_handle* h, int32_t* perm, int32_t* link_edge,
   if (e == cudaSuccess && link_edge) e = cudaMemcpy(link_edge, h->S.link_edge, sizeof(int32_t) * n, cudaMemcpyDeviceToHost);
   if (e == cudaSuccess && link_blk) e = cudaMemcpy(link_blk, h->S.link_blk, sizeof(int32_t) * n, cudaMemcpyDeviceToHost);
   return cuda_status(e);
+}
+
+}  // extern "C"
+
+// ---- autotuning
+
+namespace {
+
+int chain_tail_level(int64_t n, int levels, int64_t nodes) {
+  int l = 0;
+  while (l < levels && ((n + ((int64_t)1 << l) - 1) >> l) > nodes) ++l;
+  return l;
+}
+
+mba_status apply_schur_chunk(mba_handle* h, int chunk) {
+  std::vector<int32_t> tgt;
+  std::vector<int64_t> off;
+  cut_chunks(h->tgt_off, h->tgt_order, chunk, &tgt, &off);
+  int32_t* dt = h->arena.upload(tgt, h->stream);
+  int64_t* doff = h->arena.upload(off, h->stream);
+  if (h->arena.err != cudaSuccess || cudaStreamSynchronize(h->stream) != cudaSuccess) return MBA_ERR_CUDA;
+  h->S.chunk_tgt = dt;
+  h->S.chunk_off = doff;
+  h->S.nchunk = (int64_t)tgt.size();
+  h->tuning.schur_chunk = chunk;
+  return MBA_OK;
+}
+
+// Mean milliseconds per call of fn over `reps` calls after `warm` calls.
+template <typename F>
+double time_ms(cudaStream_t st, int warm, int reps, F fn) {
+  for (int i = 0; i < warm; ++i) fn();
+  cudaEvent_t a, b;
+  cudaEventCreate(&a);
+  cudaEventCreate(&b);
+  cudaEventRecord(a, st);
+  for (int i = 0; i < reps; ++i) fn();
+  cudaEventRecord(b, st);
+  cudaEventSynchronize(b);
+  float ms = 0.f;
+  cudaEventElapsedTime(&ms, a, b);
+  cudaEventDestroy(a);
+  cudaEventDestroy(b);
+  return ms / reps;
+}
+
+template <typename T>
+mba_status autotune(mba_handle* h, mba_tuning* out) {
+  mba_status ms = ensure_common_solver(h, 2);
+  if (ms != MBA_OK) return ms;
+  SolverBuffers<T>& b = buffers_of<T>(h);
+  if ((ms = ensure_solver_buffers<T>(h, b)) != MBA_OK) return ms;
+  if ((ms = ensure_chain_buffers<T>(h, b)) != MBA_OK) return ms;
+  mba_solver_options o;
+  mba_default_solver_options(&o);
+  o.preconditioner = MBA_PRECOND_CHAIN;
+  cudaStream_t st = h->stream;
+  if (chain_default_coef(b.C.coef, h->P.nkf, st) != cudaSuccess) return MBA_ERR_CUDA;
+  SolverLaunch<T> s = make_launch<T>(h, b, o);
+  cudaError_t e = solver_init_control(h->ctl, o.initial_trust_region_radius, st);
+  if (e == cudaSuccess) e = linearize_current<T>(h, b, s, o.jacobi_scaling, st);
+  if (e == cudaSuccess) e = solver_build_reduced<T>(s, st);
+  if (e == cudaSuccess) e = cudaStreamSynchronize(st);
+  if (e != cudaSuccess) return MBA_ERR_CUDA;
+  mba_tuning best = h->tuning;
+  // evaluation kernel block size
+  double tbest = 1e30;
+  for (int bs : {64, 128, 256}) {
+    DevProblem P = h->P;
+    P.vis_block = bs;
+    const double t = time_ms(st, 2, 8, [&]() { launch_visual_linearize<T>(P, b.vis, nullptr, st); });
+    if (t < tbest) { tbest = t; best.visual_block = bs; best.visual_ms = t; }
+  }
+  h->P.vis_block = best.visual_block;
+  // Schur pairs per thread
+  tbest = 1e30;
+  for (int chunk : {4, 8, 16, 32, 64}) {
+    if ((ms = apply_schur_chunk(h, chunk)) != MBA_OK) return ms;
+    SolverLaunch<T> sc = make_launch<T>(h, b, o);
+    const double t = time_ms(st, 1, 5, [&]() { solver_schur_pairs<T>(sc, st); });
+    if (t < tbest) { tbest = t; best.schur_chunk = chunk; best.schur_ms = t; }
+  }
+  if ((ms = apply_schur_chunk(h, best.schur_chunk)) != MBA_OK) return ms;
+  // single-block tail of the chain sweeps (the factorization from the build is reused)
+  tbest = 1e30;
+  const int levels = h->S.chain_levels;
+  for (int nodes : {32, 64, 128, 256, 512}) {
+    h->S.chain_tail = chain_tail_level(h->P.nkf, levels, nodes);
+    SolverLaunch<T> sc = make_launch<T>(h, b, o);
+    const double t = time_ms(st, 2, 10, [&]() { chain_apply<T>(sc, sc.L.rhs, sc.L.z, &h->ctl->pcg_rz0, st); });
+    if (t < tbest) { tbest = t; best.chain_tail_nodes = nodes; best.chain_apply_ms = t; }
+  }
+  h->S.chain_tail = chain_tail_level(h->P.nkf, levels, best.chain_tail_nodes);
+  if (cudaStreamSynchronize(st) != cudaSuccess || cudaGetLastError() != cudaSuccess) return MBA_ERR_CUDA;
+  h->tuning = best;
+  if (out) *out = best;
+  return MBA_OK;
+}
+
+}  // namespace
+
+extern "C" {
+
+mba_status mba_autotune(mba_handle* h, int32_t precision, mba_tuning* out) {
+  if (!h) return MBA_ERR_INVALID_ARG;
+  if (precision != MBA_PRECISION_FP64 && precision != MBA_PRECISION_MIXED) return MBA_ERR_INVALID_ARG;
+  cudaSetDevice(h->device);
+  if (h->P.nkf == 0) return MBA_ERR_INVALID_ARG;
+  return precision == MBA_PRECISION_MIXED ? autotune<float>(h, out) : autotune<double>(h, out);
+}
+
+mba_status mba_set_tuning(mba_handle* h, const mba_tuning* t) {
+  if (!h || !t) return MBA_ERR_INVALID_ARG;
+  if (t->visual_block && (t->visual_block < 32 || t->visual_block > 256 || t->visual_block % 32)) return MBA_ERR_INVALID_ARG;
+  if (t->schur_chunk < 0 || t->chain_tail_nodes < 0) return MBA_ERR_INVALID_ARG;
+  cudaSetDevice(h->device);
+  if (t->visual_block) { h->P.vis_block = t->visual_block; h->tuning.visual_block = t->visual_block; }
+  if (t->schur_chunk && t->schur_chunk != h->tuning.schur_chunk) {
+    mba_status ms = apply_schur_chunk(h, t->schur_chunk);
+    if (ms != MBA_OK) return ms;
+  }
+  if (t->chain_tail_nodes) {
+    h->S.chain_tail = chain_tail_level(h->P.nkf, h->S.chain_levels, t->chain_tail_nodes);
+    h->tuning.chain_tail_nodes = t->chain_tail_nodes;
+  }
+  return MBA_OK;
 }
 
 }  // extern "C"

@@ -78,14 +78,17 @@ struct LmControl {
   int32_t chain_failed;    // chain factorization hit a non-SPD pivot: PCG falls back to block-Jacobi
   int32_t rejected;        // landmarks rejected as outliers during this solve
   int32_t reject_count;    // landmarks rejected by the last outlier pass
+  int32_t restart_now;     // set by the LM decision: outlier rejection + restart after this iteration
+  int32_t loop_active;     // device-driven LM loop: 1 while another iteration follows
   int32_t pad_;
+  unsigned long long t0_ns;  // device global timer at the start of the solve
 };
 
 struct LmParams {
   int32_t max_num_iterations;
   int32_t max_linear_iterations;
   int32_t check_tolerances;
-  int32_t pad_;
+  int32_t reject_every;    // outlier rejection + restart every n iterations (0: off)
   double max_radius, min_radius;
   double function_tolerance, parameter_tolerance, min_relative_decrease;
   double min_lm_diagonal, max_lm_diagonal;
@@ -168,6 +171,9 @@ cudaError_t solver_compute_scale(const SolverLaunch<T>& s, int jacobi, cudaStrea
 // inverses, at the radius held in the control block.
 template <typename T>
 cudaError_t solver_build_reduced(const SolverLaunch<T>& s, cudaStream_t st);
+// The Schur pair kernel alone (autotuning).
+template <typename T>
+cudaError_t solver_schur_pairs(const SolverLaunch<T>& s, cudaStream_t st);
 template <typename T>
 cudaError_t solver_step(const SolverLaunch<T>& s, cudaStream_t st);
 template <typename T>
@@ -187,6 +193,11 @@ cudaError_t solver_add_inertial_cost(LmControl* ctl, cudaStream_t st);
 template <typename T>
 cudaError_t solver_reject_and_restart(const SolverLaunch<T>& s, int use_reprojection, double max_px, int jacobi,
                                       cudaStream_t st);
+// Device-driven loop: records the solve's start time; ends the loop (and
+// reports cancellation) through the conditional handle.
+cudaError_t solver_loop_start(LmControl* ctl, cudaStream_t st);
+cudaError_t solver_loop_control(LmControl* ctl, cudaGraphConditionalHandle handle, const volatile int* cancel,
+                                cudaStream_t st);
 
 // kernels_chain.cu: factorization of the chain matrix (after the reduced
 // system is built) and z = T^-1 r with the r.z dot added to *rz.

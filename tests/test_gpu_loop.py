@@ -1,0 +1,85 @@
+"""Device-driven LM loop (the whole solve as one CUDA graph with a while
+condition evaluated on the device) and per-problem autotuning."""
+import threading
+import time
+
+import numpy as np
+import pytest
+
+from maplab_gb300 import _native as N
+from maplab_gb300 import ba, synth
+
+pytestmark = pytest.mark.gpu
+
+
+def _opts(**kw):
+    kw.setdefault("max_num_iterations", 10)
+    kw.setdefault("check_tolerances", 0)
+    return ba.default_options(**kw)
+
+
+def test_device_loop_matches_host_loop():
+    m = synth.generate("c1")
+    with ba.BundleAdjuster(m.desc) as g:
+        host = g.solve(_opts(use_cuda_graph=1))
+    with ba.BundleAdjuster(m.desc) as g:
+        dev = g.solve(_opts(use_cuda_graph=2))
+    assert dev["num_iterations"] == host["num_iterations"]
+    assert dev["rejected_landmarks"] == host["rejected_landmarks"]
+    for a, b in zip(dev["iterations"], host["iterations"]):
+        assert a["ok"] == b["ok"]
+        assert abs(a["cost"] - b["cost"]) <= 1e-6 * b["cost"], (a, b)
+    times = [it["time_ms"] for it in dev["iterations"][1:]]
+    assert all(t > 0 for t in times) and times == sorted(times)
+
+
+def test_device_loop_stop_cost_and_mixed():
+    m = synth.generate("c1")
+    with ba.BundleAdjuster(m.desc) as g:
+        s64 = g.solve(_opts(max_num_iterations=10))
+    target = s64["final_cost"] * (1 + 1e-6)
+    with ba.BundleAdjuster(m.desc) as g:
+        s = g.solve(_opts(max_num_iterations=30, use_cuda_graph=2, stop_cost=target, precision=N.MBA_PRECISION_MIXED,
+                          preconditioner=N.MBA_PRECOND_CHAIN, max_linear_iterations=25))
+    assert s["termination"] == 6 and s["final_cost"] <= target
+    assert 0 < s["time_to_stop_cost_ms"] <= s["iterations"][-1]["time_ms"] + 1e-9
+
+
+def test_device_loop_cancel():
+    m = synth.generate("c2", keyframes_per_mission=1000, num_landmarks=100000)
+    with ba.BundleAdjuster(m.desc) as g:
+        out = {}
+
+        def run():
+            out["s"] = None
+            try:
+                out["s"] = g.solve(_opts(max_num_iterations=200, use_cuda_graph=2, max_linear_iterations=100,
+                                         reject_outliers_every_n_iters=0))
+            except ba.BAError as e:
+                out["err"] = e
+
+        t = threading.Thread(target=run)
+        t.start()
+        time.sleep(0.3)
+        g.cancel()
+        t.join(timeout=120)
+        assert not t.is_alive()
+    assert "err" in out and out["err"].status == 7  # MBA_ERR_CANCELLED
+
+
+def test_autotune_keeps_results():
+    m = synth.generate("c1")
+    with ba.BundleAdjuster(m.desc) as g:
+        base = g.solve(_opts())
+    with ba.BundleAdjuster(m.desc) as g:
+        tun = g.autotune(N.MBA_PRECISION_FP64)
+        assert tun["visual_block"] in (64, 128, 256)
+        assert tun["schur_chunk"] in (4, 8, 16, 32, 64)
+        assert tun["chain_tail_nodes"] in (32, 64, 128, 256, 512)
+        assert tun["visual_ms"] > 0 and tun["schur_ms"] > 0 and tun["chain_apply_ms"] > 0
+        tuned = g.solve(_opts())
+    assert abs(tuned["final_cost"] - base["final_cost"]) <= 1e-6 * base["final_cost"]
+    with ba.BundleAdjuster(m.desc) as g:
+        g.set_tuning(visual_block=64, schur_chunk=4, chain_tail_nodes=32)
+        s = g.solve(_opts())
+    assert abs(s["final_cost"] - base["final_cost"]) <= 1e-6 * base["final_cost"]
