@@ -344,7 +344,7 @@ typedef struct mba_tuning {
   int32_t visual_block;         /* threads per block of the evaluation kernel (64, 128, 256) */
   int32_t schur_chunk;          /* slot pairs summed per thread by the Schur pair kernel */
   int32_t chain_tail_nodes;     /* chain positions below which one block finishes a chain sweep */
-  int32_t pad_;
+  int32_t visual_min_blocks;    /* 1, or 3: register-lean evaluation kernel (3 blocks of 256 per SM) */
   double visual_ms;             /* per launch, chosen setting */
   double schur_ms;
   double chain_apply_ms;

@@ -166,7 +166,7 @@ class Tuning(ctypes.Structure):
         ("visual_block", ctypes.c_int32),
         ("schur_chunk", ctypes.c_int32),
         ("chain_tail_nodes", ctypes.c_int32),
-        ("pad_", ctypes.c_int32),
+        ("visual_min_blocks", ctypes.c_int32),
         ("visual_ms", ctypes.c_double),
         ("schur_ms", ctypes.c_double),
         ("chain_apply_ms", ctypes.c_double),

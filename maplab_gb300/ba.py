@@ -243,7 +243,7 @@ class BundleAdjuster:
         """Times launch / schedule candidates on this problem and keeps the fastest."""
         t = N.Tuning()
         _check(self._lib.mba_autotune(self._h, precision, ctypes.byref(t)), "mba_autotune")
-        return {f: getattr(t, f) for f, _ in t._fields_ if f != "pad_"}
+        return {f: getattr(t, f) for f, _ in t._fields_}
 
     def set_tuning(self, **kw):
         t = N.Tuning()

@@ -14,7 +14,7 @@ namespace mba {
 struct DevProblem {
   int64_t nkf, nlm, nobs, ncam, nmis, nedge, nsamp;
   int32_t vis_block;        // threads per block of the evaluation kernel (tuned; 0 = default)
-  int32_t pad_;
+  int32_t vis_minb;         // > 1: register-lean variant of the evaluation kernel (tuned)
   // observations
   const double2* obs_uv;
   const double* obs_sinv;   // 1 / sigma

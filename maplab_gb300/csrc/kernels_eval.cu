@@ -94,8 +94,10 @@ __device__ __forceinline__ void rot_basis(const DevProblem& P, const S* mis, int
 // Tangent-space, Huber-corrected linearization of every observation.  kCost
 // adds the FP64 cost reduction (FP64 path only): the FP32 instantiation reads
 // the FP32 mirrors and executes no FP64 instruction.
-template <typename T, bool kCost>
-__global__ void __launch_bounds__(kBlock) k_visual_linearize(DevProblem P, VisualInputs<T> in, VisualLin<T> out,
+// kMinBlocks > 1 trades registers (spilled to L1) for resident warps;
+// the autotuner picks the variant per problem.
+template <typename T, bool kCost, int kMinBlocks>
+__global__ void __launch_bounds__(kBlock, kMinBlocks) k_visual_linearize(DevProblem P, VisualInputs<T> in, VisualLin<T> out,
                                                              double* cost_accum, const int* run_if,
                                                              const int* skip_if) {
   if (gated(run_if, skip_if)) return;
@@ -541,10 +543,18 @@ cudaError_t launch_visual_linearize_gated(const DevProblem& P, VisualLin<T> out,
   // Block size: tuned per problem (mba_autotune), at most the launch bound.
   const int bs = (P.vis_block > 0 && P.vis_block <= kBlock) ? P.vis_block : kBlock;
   const int64_t blocks = (P.nobs + bs - 1) / bs;
-  if (cost_accum)
-    k_visual_linearize<T, true><<<(unsigned)blocks, bs, 0, s>>>(P, visual_inputs<T>(P), out, cost_accum, run_if, skip_if);
-  else
-    k_visual_linearize<T, false><<<(unsigned)blocks, bs, 0, s>>>(P, visual_inputs<T>(P), out, nullptr, run_if, skip_if);
+  const bool lean = P.vis_minb > 1;
+  if (cost_accum) {
+    if (lean)
+      k_visual_linearize<T, true, 3><<<(unsigned)blocks, bs, 0, s>>>(P, visual_inputs<T>(P), out, cost_accum, run_if, skip_if);
+    else
+      k_visual_linearize<T, true, 1><<<(unsigned)blocks, bs, 0, s>>>(P, visual_inputs<T>(P), out, cost_accum, run_if, skip_if);
+  } else {
+    if (lean)
+      k_visual_linearize<T, false, 3><<<(unsigned)blocks, bs, 0, s>>>(P, visual_inputs<T>(P), out, nullptr, run_if, skip_if);
+    else
+      k_visual_linearize<T, false, 1><<<(unsigned)blocks, bs, 0, s>>>(P, visual_inputs<T>(P), out, nullptr, run_if, skip_if);
+  }
   return cudaGetLastError();
 }
 template <typename T>

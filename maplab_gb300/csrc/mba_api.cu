@@ -1147,6 +1147,7 @@ mba_status mba_create(const mba_problem_desc* d, int32_t device, mba_handle** ou
   while (S.chain_tail < S.chain_levels && ((NK + ((int64_t)1 << S.chain_tail) - 1) >> S.chain_tail) > 128)
     ++S.chain_tail;
   h->tuning.visual_block = 256;
+  h->tuning.visual_min_blocks = 1;
   h->tuning.schur_chunk = (int32_t)kSchurChunk;
   h->tuning.chain_tail_nodes = 128;
   // Inertial scratch (kernels_inertial.cu): dt per step, end state per edge,
@@ -1647,13 +1648,16 @@ mba_status autotune(mba_handle* h, mba_tuning* out) {
   mba_tuning best = h->tuning;
   // evaluation kernel block size
   double tbest = 1e30;
-  for (int bs : {64, 128, 256}) {
-    DevProblem P = h->P;
-    P.vis_block = bs;
-    const double t = time_ms(st, 2, 8, [&]() { launch_visual_linearize<T>(P, b.vis, nullptr, st); });
-    if (t < tbest) { tbest = t; best.visual_block = bs; best.visual_ms = t; }
-  }
+  for (int minb : {1, 3})
+    for (int bs : {64, 128, 256}) {
+      DevProblem P = h->P;
+      P.vis_block = bs;
+      P.vis_minb = minb;
+      const double t = time_ms(st, 2, 8, [&]() { launch_visual_linearize<T>(P, b.vis, nullptr, st); });
+      if (t < tbest) { tbest = t; best.visual_block = bs; best.visual_min_blocks = minb; best.visual_ms = t; }
+    }
   h->P.vis_block = best.visual_block;
+  h->P.vis_minb = best.visual_min_blocks;
   // Schur pairs per thread
   tbest = 1e30;
   for (int chunk : {4, 8, 16, 32, 64}) {
@@ -1697,6 +1701,11 @@ mba_status mba_set_tuning(mba_handle* h, const mba_tuning* t) {
   if (t->schur_chunk < 0 || t->chain_tail_nodes < 0) return MBA_ERR_INVALID_ARG;
   cudaSetDevice(h->device);
   if (t->visual_block) { h->P.vis_block = t->visual_block; h->tuning.visual_block = t->visual_block; }
+  if (t->visual_min_blocks) {
+    if (t->visual_min_blocks != 1 && t->visual_min_blocks != 3) return MBA_ERR_INVALID_ARG;
+    h->P.vis_minb = t->visual_min_blocks;
+    h->tuning.visual_min_blocks = t->visual_min_blocks;
+  }
   if (t->schur_chunk && t->schur_chunk != h->tuning.schur_chunk) {
     mba_status ms = apply_schur_chunk(h, t->schur_chunk);
     if (ms != MBA_OK) return ms;
