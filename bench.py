@@ -178,6 +178,7 @@ def ba_time_to_cost(args, device):
                                        precision=N.MBA_PRECISION_MIXED, preconditioner=pre, use_cuda_graph=2,
                                        **common))
     rms32, n32 = _reprojection_rms(g32, m)
+    cost32_fp64 = g32.cost()  # the mixed path's final state re-evaluated in full FP64
     g32.close()
     if model is not None:
         model.close()
@@ -190,6 +191,8 @@ def ba_time_to_cost(args, device):
         "plain_fp64_pcg_iterations": s64["linear_iterations"], "plain_fp64_rejected_landmarks": s64["rejected_landmarks"],
         "plain_fp64_rms_px": rms64,
         "mixed_learned_time_to_cost_s": t32, "mixed_learned_final_cost": s32["final_cost"],
+        "mixed_learned_final_cost_fp64_eval": cost32_fp64,
+        "mixed_reaches_target_in_fp64": bool(cost32_fp64 <= target),
         "mixed_learned_iterations": s32["num_iterations"] - 1, "mixed_learned_pcg_iterations": s32["linear_iterations"],
         "mixed_learned_rejected_landmarks": s32["rejected_landmarks"], "mixed_learned_rms_px": rms32,
         "rms_difference_px": abs(rms32 - rms64),

@@ -124,6 +124,10 @@ cudaError_t launch_inertial_f32(const DevProblem& P, const InertialLin<double>& 
 // a landmark goes out of the problem when one of its observations has depth
 // <= 0 in the observing camera or, if use_reprojection, a reprojection error
 // above max_px.  Newly rejected landmarks are counted into *count.
+// FP32 residuals of the state in FP32 copies (pose q p pad [n][8], landmark
+// [n][4]); cost summed in FP64.
+cudaError_t launch_visual_cost_f32(const DevProblem& P, const float* kf, const float* lm, double* cost_accum,
+                                   int* nonfinite, const int* skip_if, cudaStream_t s);
 cudaError_t launch_find_outliers(const DevProblem& P, int use_reprojection, double max_px, int* count,
                                  const int* run_if, const int* skip_if, cudaStream_t s);
 

@@ -318,6 +318,63 @@ __global__ void __launch_bounds__(kBlock) k_visual_cost(DevProblem P, const doub
   block_accumulate(cost, cost_accum);
 }
 
+// FP32 candidate cost (mixed path): the visual term's frame chain and
+// projection in FP32 from FP32 copies of the candidate state, robustified
+// cost summed in FP64.  No FP64 arithmetic per observation.
+__global__ void __launch_bounds__(kBlock) k_visual_cost_f32(DevProblem P, const float* kf, const float* lp,
+                                                            double* cost_accum, int* nonfinite, const int* skip_if) {
+  if (gated(nullptr, skip_if)) return;
+  const int64_t i = blockIdx.x * (int64_t)blockDim.x + threadIdx.x;
+  double cost = 0.0;
+  if (i < P.nobs && !P.lm_off[P.obs_lm[i]]) {
+    const int lm = P.obs_lm[i], k = P.obs_kf[i], st = P.obs_store[i], type = P.obs_type[i];
+    const DevCameraT<float>& cam = P.cams_f[P.obs_cam[i]];
+    const float pB[3] = {lp[4 * (int64_t)lm], lp[4 * (int64_t)lm + 1], lp[4 * (int64_t)lm + 2]};
+    M3<float> RCI;
+    jplR(cam.q_CI, RCI);
+    float pI[3];
+    if (type == MBA_LOCAL_KEYFRAME) {
+      pI[0] = pB[0]; pI[1] = pB[1]; pI[2] = pB[2];
+    } else {
+      const float* xs = kf + 8 * (int64_t)st;
+      const float* xo = kf + 8 * (int64_t)k;
+      M3<float> RBLM, RIM;
+      jplR(xs, RBLM);
+      jplR(xo, RIM);
+      float pM[3];
+      mtv3(RBLM, pB, pM);
+      pM[0] += xs[4]; pM[1] += xs[5]; pM[2] += xs[6];
+      if (type == MBA_GLOBAL) {
+        const float* ml = P.mis_f + 8 * P.kf_mis[st];
+        const float* mo = P.mis_f + 8 * P.kf_mis[k];
+        M3<float> RGLM, RGM;
+        jplR(ml, RGLM);
+        jplR(mo, RGM);
+        float pG[3];
+        mv3(RGLM, pM, pG);
+        pG[0] += ml[4] - mo[4]; pG[1] += ml[5] - mo[5]; pG[2] += ml[6] - mo[6];
+        mtv3(RGM, pG, pM);
+      }
+      const float d[3] = {pM[0] - xo[4], pM[1] - xo[5], pM[2] - xo[6]};
+      mv3(RIM, d, pI);
+    }
+    float pC[3];
+    mv3(RCI, pI, pC);
+    pC[0] += cam.p_CI[0]; pC[1] += cam.p_CI[1]; pC[2] += cam.p_CI[2];
+    float kp[2];
+    if (!project<float>(cam, pC, kp, nullptr)) {
+      const float2 uv = P.obs_uv_f[i];
+      const float sinv = P.obs_sinv_f[i];
+      const float r0 = (kp[0] - uv.x) * sinv, r1 = (kp[1] - uv.y) * sinv;
+      const double sq = (double)r0 * r0 + (double)r1 * r1;
+      const double a = (double)P.obs_huber_f[i];
+      cost = (a > 0.0 && sq > a * a) ? 0.5 * (2.0 * a * sqrt(sq) - a * a) : 0.5 * sq;
+      if (!isfinite(cost) && nonfinite) *nonfinite = 1;
+    }
+  }
+  block_accumulate(cost, cost_accum);
+}
+
 // Outlier test per observation (outlier-rejection-solver.cc:28-103): depth
 // p_C.z <= 0, or (optionally) squared reprojection error in pixels above
 // max_px^2, marks the landmark.  Landmarks already out are skipped.
@@ -582,6 +639,13 @@ cudaError_t launch_visual_cost_gated(const DevProblem& P, const double* kf_state
   if (P.nobs == 0) return cudaSuccess;
   const int64_t blocks = (P.nobs + kBlock - 1) / kBlock;
   k_visual_cost<<<(unsigned)blocks, kBlock, 0, s>>>(P, kf_state, lm_p, cost_accum, nonfinite, run_if, skip_if);
+  return cudaGetLastError();
+}
+cudaError_t launch_visual_cost_f32(const DevProblem& P, const float* kf, const float* lm, double* cost_accum,
+                                   int* nonfinite, const int* skip_if, cudaStream_t s) {
+  if (P.nobs == 0) return cudaSuccess;
+  const int64_t blocks = (P.nobs + kBlock - 1) / kBlock;
+  k_visual_cost_f32<<<(unsigned)blocks, kBlock, 0, s>>>(P, kf, lm, cost_accum, nonfinite, skip_if);
   return cudaGetLastError();
 }
 cudaError_t launch_visual_cost(const DevProblem& P, const double* kf_state, const double* lm_p, double* cost_accum,

@@ -767,6 +767,8 @@ __global__ void __launch_bounds__(kB) k_retract(SolverLaunch<T> s) {
     }
     for (int a = 0; a < 4; ++a) o[a] = q[a];
     for (int a = 0; a < 12; ++a) o[4 + a] = x[4 + a] + d[3 + a];
+    if (s.kf_cand_f)
+      for (int a = 0; a < 7; ++a) s.kf_cand_f[8 * k + a] = (float)o[a];
     const bool pose_var = (m & 0x3f) != 0;
     if (pose_var)
       for (int a = 0; a < 7; ++a) { sn += (o[a] - x[a]) * (o[a] - x[a]); xn += x[a] * x[a]; }
@@ -781,6 +783,7 @@ __global__ void __launch_bounds__(kB) k_retract(SolverLaunch<T> s) {
     for (int a = 0; a < 3; ++a) {
       const double d = act ? s.sc.slm[a * NL + l] * s.L.dl[a * NL + l] : 0.0;
       o[a] = x[a] + d;
+      if (s.lm_cand_f) s.lm_cand_f[4 * l + a] = (float)o[a];
       if (act) { sn += d * d; xn += x[a] * x[a]; }
     }
     o[3] = 0.0;
@@ -1007,8 +1010,12 @@ cudaError_t solver_step(const SolverLaunch<T>& s, cudaStream_t st) {
 
 template <typename T>
 cudaError_t solver_evaluate_candidate(const SolverLaunch<T>& s, InertialLin<double> ine_cand, cudaStream_t st) {
-  cudaError_t e = launch_visual_cost_gated(s.P, s.kf_cand, s.lm_cand, &s.ctl->cost_cand, &s.ctl->nonfinite,
-                                           &s.ctl->terminated, st);
+  // Mixed path: FP32 residuals from FP32 copies of the candidate, FP64 sum.
+  cudaError_t e = (sizeof(T) == 4 && s.kf_cand_f)
+                      ? launch_visual_cost_f32(s.P, s.kf_cand_f, s.lm_cand_f, &s.ctl->cost_cand, &s.ctl->nonfinite,
+                                               &s.ctl->terminated, st)
+                      : launch_visual_cost_gated(s.P, s.kf_cand, s.lm_cand, &s.ctl->cost_cand, &s.ctl->nonfinite,
+                                                 &s.ctl->terminated, st);
   if (e != cudaSuccess) return e;
   // Mixed path: Phi / Q propagated in FP32 (state, Cholesky, residual FP64).
   return launch_inertial_gated(s.P, s.kf_cand, ine_cand, &s.ctl->cost_cand_ine, &s.ctl->inertial_status,

@@ -157,6 +157,8 @@ struct mba_handle {
   int log_capacity = 0;
   double* kf_cand = nullptr;
   double* lm_cand = nullptr;
+  float* kf_cand_f = nullptr;
+  float* lm_cand_f = nullptr;
   double* scratch = nullptr;  // [4] cost accumulators
   int* iscratch = nullptr;    // [4] flags
   // staging in the caller's layout (lazily allocated)
@@ -326,6 +328,8 @@ mba_status ensure_common_solver(mba_handle* h, int capacity) {
     h->ctl = A.alloc<LmControl>(1);
     h->kf_cand = A.alloc<double>(16 * P.nkf);
     h->lm_cand = A.alloc<double>(4 * P.nlm);
+    h->kf_cand_f = A.alloc<float>(8 * P.nkf);
+    h->lm_cand_f = A.alloc<float>(4 * P.nlm);
     if (A.err != cudaSuccess) return MBA_ERR_CUDA;
     h->solver_ready = true;
   }
@@ -371,6 +375,8 @@ SolverLaunch<T> make_launch(mba_handle* h, SolverBuffers<T>& b, const mba_solver
   s.log = h->log;
   s.kf_cand = h->kf_cand;
   s.lm_cand = h->lm_cand;
+  s.kf_cand_f = sizeof(T) == 4 ? h->kf_cand_f : nullptr;
+  s.lm_cand_f = sizeof(T) == 4 ? h->lm_cand_f : nullptr;
   s.C = b.C;
   s.precond = (o.preconditioner == MBA_PRECOND_CHAIN || o.preconditioner == MBA_PRECOND_LEARNED) && b.chain_ready
                   ? o.preconditioner : MBA_PRECOND_BLOCK_JACOBI;

@@ -155,6 +155,8 @@ struct SolverLaunch {
   mba_iteration_summary* log;  // device [max_num_iterations + 1]
   double* kf_cand;             // [nkf][16]
   double* lm_cand;             // [nlm][4]
+  float* kf_cand_f;            // [nkf][8] FP32 pose copies of the candidate (mixed path)
+  float* lm_cand_f;            // [nlm][4]
   ChainSystem<T> C;
   int32_t precond = 0;         // MBA_PRECOND_*
   GnnGraph gg{};               // learned preconditioner (precond == MBA_PRECOND_LEARNED)

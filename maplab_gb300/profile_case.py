@@ -1,0 +1,58 @@
+"""Runs one configuration of the bundle adjuster for profiling (ncu, or the
+CUDA-event times it prints).
+
+    # the evaluation kernel alone, L2 flushed before each launch
+    python -m maplab_gb300.profile_case visual --config c2 --block 64 --min-blocks 3 --launches 3
+    # one solve
+    python -m maplab_gb300.profile_case solve --config c4 --precision mixed --precond learned --iters 6
+"""
+import argparse
+import json
+
+from . import _native as N
+from . import ba, synth
+
+
+def main():
+    ap = argparse.ArgumentParser()
+    ap.add_argument("what", choices=["visual", "solve"])
+    ap.add_argument("--config", default="c2")
+    ap.add_argument("--block", type=int, default=0)
+    ap.add_argument("--min-blocks", type=int, default=0)
+    ap.add_argument("--launches", type=int, default=3)
+    ap.add_argument("--precision", choices=["fp64", "mixed"], default="mixed")
+    ap.add_argument("--precond", choices=["jacobi", "chain", "learned"], default="learned")
+    ap.add_argument("--iters", type=int, default=6)
+    ap.add_argument("--pcg", type=int, default=25)
+    ap.add_argument("--autotune", action="store_true")
+    ap.add_argument("--device-loop", type=int, default=1)
+    a = ap.parse_args()
+    m = synth.generate(a.config)
+    with ba.BundleAdjuster(m.desc) as g:
+        if a.block or a.min_blocks:
+            g.set_tuning(visual_block=a.block, visual_min_blocks=a.min_blocks)
+        prec = N.MBA_PRECISION_MIXED if a.precision == "mixed" else N.MBA_PRECISION_FP64
+        if a.autotune:
+            print(json.dumps({"tuning": g.autotune(prec)}))
+        if a.what == "visual":
+            ms = g.time_visual_kernel(mode=1 if prec == N.MBA_PRECISION_MIXED else 0, iters=a.launches)
+            print(json.dumps({"visual_ms_per_launch": ms, "observations": m.desc.num_observations}))
+            return
+        pre = {"jacobi": N.MBA_PRECOND_BLOCK_JACOBI, "chain": N.MBA_PRECOND_CHAIN,
+               "learned": N.MBA_PRECOND_LEARNED}[a.precond]
+        model = None
+        if pre == N.MBA_PRECOND_LEARNED:
+            from . import train_preconditioner as TP
+            model = TP.load_default_model()
+            g.set_preconditioner_model(model)
+        s = g.solve(ba.default_options(max_num_iterations=a.iters, max_linear_iterations=a.pcg, precision=prec,
+                                       preconditioner=pre, check_tolerances=0,
+                                       use_cuda_graph=2 if a.device_loop else 1))
+        print(json.dumps({"iterations": s["num_iterations"] - 1, "final_cost": s["final_cost"],
+                          "time_ms": s["iterations"][-1]["time_ms"], "pcg": s["linear_iterations"]}))
+        if model is not None:
+            model.close()
+
+
+if __name__ == "__main__":
+    main()

@@ -83,3 +83,14 @@ def test_autotune_keeps_results():
         g.set_tuning(visual_block=64, schur_chunk=4, chain_tail_nodes=32)
         s = g.solve(_opts())
     assert abs(s["final_cost"] - base["final_cost"]) <= 1e-6 * base["final_cost"]
+
+
+def test_mixed_candidate_cost_agrees_with_fp64():
+    """The mixed path evaluates candidate costs from FP32 residuals (FP64 sum);
+    its final cost agrees with the full FP64 evaluation of the same state."""
+    m = synth.generate("c2", keyframes_per_mission=500, num_landmarks=50000)
+    with ba.BundleAdjuster(m.desc) as g:
+        s = g.solve(_opts(max_num_iterations=8, precision=N.MBA_PRECISION_MIXED, preconditioner=N.MBA_PRECOND_CHAIN,
+                          max_linear_iterations=25, use_cuda_graph=2))
+        c64 = g.cost()
+    assert abs(s["final_cost"] - c64) <= 1e-6 * c64, (s["final_cost"], c64)
