@@ -130,6 +130,17 @@ typedef struct mba_problem_desc {
   int32_t pad_;
   double huber_delta_local;
   double huber_delta_global;
+  /* Relative 6-DoF pose edges: odometry and wheel-odometry TransformationEdges
+   * (addRelativePoseTermsForEdges, optimization-terms-addition.cc:543-640),
+   * residual SixDoFBlockPoseErrorTermWithExtrinsics
+   * (six-dof-block-pose-error-term-with-extrinsics-autodiff-inl.h), no loss.
+   * Sensor extrinsics are constant (ba_fix_*_extrinsics). */
+  int64_t num_pose_edges;
+  const int32_t* pose_edge_from;       /* [N_pe] keyframe of T_Bk */
+  const int32_t* pose_edge_to;         /* [N_pe] keyframe of T_Bkp1 */
+  const double* pose_edge_T_Bk_Bkp1;   /* [N_pe][7] measured q (x y z w) | p, aslam::Transformation */
+  const double* pose_edge_covariance;  /* [N_pe][36] row-major, order (p, q): get_T_A_B_Covariance_p_q */
+  const double* pose_edge_q_I_B_p_B_I; /* [N_pe][7] extrinsics block q_I_B (x y z w) | p_B_I */
 } mba_problem_desc;
 
 /* Subset of ceres::Solver::Options used by map_optimization
@@ -251,6 +262,12 @@ mba_status mba_evaluate_inertial(mba_handle* h, double* residuals, double* const
 mba_status mba_linearize_visual(mba_handle* h, int32_t precision, double* r,
                                 double* J_landmark, double* J_store, double* J_observer);
 
+/* Relative pose edges at the current state: whitened residual [N_pe][6] and
+ * tangent Jacobians [N_pe][6x6] w.r.t. the (theta, p) tangent of the from /
+ * to keyframe (Ceres: autodiff ambient Jacobian times the JPL pose
+ * parameterization's ComputeJacobian).  Host pointers, each may be NULL. */
+mba_status mba_linearize_pose_edges(mba_handle* h, double* r, double* J_from, double* J_to);
+
 /* Ceres-style total cost 0.5 * sum rho(|r|^2) at the current state. */
 mba_status mba_cost(mba_handle* h, int32_t precision, double* cost);
 
@@ -288,7 +305,8 @@ mba_status mba_time_visual_kernel(mba_handle* h, int32_t mode, int32_t iters, do
  *   upper_ij [N_pu][2] keyframe pairs (i < j) and upper [N_pu][6][6], the
  *     pose-pose (theta, p) block of row i, column j,
  *     N_pu = mba_problem_stats.num_schur_pose_blocks / 2;
- *   inertial [N_edge][15][15], row = edge's from keyframe, column = to;
+ *   inertial [N_edge][15][15] (IMU edges, then pose edges), row = edge's
+ *   from keyframe, column = to;
  *   rhs [N_kf][15].
  * precision MBA_PRECISION_FP64 or MBA_PRECISION_MIXED (FP32 system). */
 mba_status mba_reduced_system(mba_handle* h, int32_t precision, double radius, double* diag, int32_t* upper_ij,
@@ -359,6 +377,7 @@ typedef struct mba_problem_stats {
   int64_t num_keyframes, num_landmarks, num_observations, num_imu_edges;
   int64_t num_schur_pose_blocks;   /* off-diagonal 6x6 pose-pose blocks (both triangles) */
   int64_t device_bytes;            /* bytes held on the device by the handle */
+  int64_t num_pose_edges;          /* relative pose edges (after the IMU edges) */
 } mba_problem_stats;
 mba_status mba_get_stats(mba_handle* h, mba_problem_stats* stats);
 

@@ -53,6 +53,10 @@ typedef struct mba_synth_config {
   double shared_landmark_fraction;/* co-registered missions: fraction of landmarks seen by two missions */
   int32_t include_inertial;
   int32_t co_registered;          /* missions share one circle (overlapping trajectories) */
+  int32_t pose_edges;             /* 1: odometry edge between consecutive keyframes of a mission */
+  int32_t pad_;
+  double pose_edge_sigma_p;       /* odometry position noise (m) */
+  double pose_edge_sigma_q;       /* odometry rotation noise (rad) */
 } mba_synth_config;
 
 typedef struct mba_synth_map mba_synth_map;

@@ -99,6 +99,12 @@ class ProblemDesc(ctypes.Structure):
         ("pad_", ctypes.c_int32),
         ("huber_delta_local", ctypes.c_double),
         ("huber_delta_global", ctypes.c_double),
+        ("num_pose_edges", ctypes.c_int64),
+        ("pose_edge_from", c_int32_p),
+        ("pose_edge_to", c_int32_p),
+        ("pose_edge_T_Bk_Bkp1", c_double_p),
+        ("pose_edge_covariance", c_double_p),
+        ("pose_edge_q_I_B_p_B_I", c_double_p),
     ]
 
 
@@ -181,6 +187,7 @@ class ProblemStats(ctypes.Structure):
         ("num_imu_edges", ctypes.c_int64),
         ("num_schur_pose_blocks", ctypes.c_int64),
         ("device_bytes", ctypes.c_int64),
+        ("num_pose_edges", ctypes.c_int64),
     ]
 
 
@@ -246,6 +253,10 @@ class SynthConfig(ctypes.Structure):
         ("shared_landmark_fraction", ctypes.c_double),
         ("include_inertial", ctypes.c_int32),
         ("co_registered", ctypes.c_int32),
+        ("pose_edges", ctypes.c_int32),
+        ("pad_", ctypes.c_int32),
+        ("pose_edge_sigma_p", ctypes.c_double),
+        ("pose_edge_sigma_q", ctypes.c_double),
     ]
 
 
@@ -292,6 +303,7 @@ def load_ba():
     _declare(lib, "mba_evaluate_visual", ctypes.c_int, [vp, c_double_p, ctypes.POINTER(c_double_p)])
     _declare(lib, "mba_evaluate_inertial", ctypes.c_int, [vp, c_double_p, ctypes.POINTER(c_double_p)])
     _declare(lib, "mba_linearize_visual", ctypes.c_int, [vp, ctypes.c_int32] + [c_double_p] * 4)
+    _declare(lib, "mba_linearize_pose_edges", ctypes.c_int, [vp] + [c_double_p] * 3)
     _declare(lib, "mba_cost", ctypes.c_int, [vp, ctypes.c_int32, c_double_p])
     _declare(lib, "mba_solve", ctypes.c_int, [vp, ctypes.POINTER(SolverOptions), ctypes.POINTER(Summary)])
     _declare(lib, "mba_read_state", ctypes.c_int, [vp] + [c_double_p] * 5)

@@ -148,6 +148,16 @@ class BundleAdjuster:
                "mba_linearize_visual")
         return r, Jl, Js, Jo
 
+    def linearize_pose_edges(self):
+        """Relative pose edges at the current state: whitened residual
+        [N_pe, 6] and (theta, p) tangent Jacobians [N_pe, 36] of the from and
+        to keyframes."""
+        n = self.desc.num_pose_edges
+        r = np.zeros((n, 6)); Jf = np.zeros((n, 36)); Jt = np.zeros((n, 36))
+        _check(self._lib.mba_linearize_pose_edges(self._h, N.ptr(r), N.ptr(Jf), N.ptr(Jt)),
+               "mba_linearize_pose_edges")
+        return r, Jf, Jt
+
     def cost(self):
         c = ctypes.c_double()
         _check(self._lib.mba_cost(self._h, 0, ctypes.byref(c)), "mba_cost")
@@ -191,15 +201,18 @@ class BundleAdjuster:
         dict of diag [N_kf,15,15], upper_ij [N_pu,2], upper [N_pu,6,6],
         inertial [N_e,15,15] (with edge_from / edge_to) and rhs [N_kf,15]."""
         st = self.stats()
-        nk, ne, npu = st["num_keyframes"], st["num_imu_edges"], st["num_schur_pose_blocks"] // 2
+        nk, npu = st["num_keyframes"], st["num_schur_pose_blocks"] // 2
+        ni, npe = st["num_imu_edges"], st["num_pose_edges"]
+        ne = ni + npe
         D = np.zeros((nk, 15, 15)); ij = np.zeros((npu, 2), dtype=np.int32); U = np.zeros((npu, 6, 6))
         E = np.zeros((ne, 15, 15)); b = np.zeros((nk, 15))
         _check(self._lib.mba_reduced_system(self._h, precision, radius, N.ptr(D),
                                             ij.ctypes.data_as(ctypes.POINTER(ctypes.c_int32)), N.ptr(U), N.ptr(E),
                                             N.ptr(b)), "mba_reduced_system")
         d = self.desc
-        ef = np.ctypeslib.as_array(d.edge_from, (ne,)).copy() if ne else np.zeros(0, np.int32)
-        et = np.ctypeslib.as_array(d.edge_to, (ne,)).copy() if ne else np.zeros(0, np.int32)
+        part = lambda p, n: np.ctypeslib.as_array(p, (n,)).copy() if n else np.zeros(0, np.int32)
+        ef = np.concatenate([part(d.edge_from, ni), part(d.pose_edge_from, npe)]).astype(np.int32)
+        et = np.concatenate([part(d.edge_to, ni), part(d.pose_edge_to, npe)]).astype(np.int32)
         return dict(diag=D, upper_ij=ij, upper=U, inertial=E, edge_from=ef, edge_to=et, rhs=b)
 
     def rejected_landmarks(self):

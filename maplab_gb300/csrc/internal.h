@@ -13,6 +13,7 @@ namespace mba {
 // Observations are sorted by landmark (contiguous per landmark).
 struct DevProblem {
   int64_t nkf, nlm, nobs, ncam, nmis, nedge, nsamp;
+  int64_t nimu;             // edges [0, nimu) are inertial, [nimu, nedge) relative pose edges
   int32_t vis_block;        // threads per block of the evaluation kernel (tuned; 0 = default)
   int32_t vis_minb;         // > 1: register-lean variant of the evaluation kernel (tuned)
   // observations
@@ -44,6 +45,10 @@ struct DevProblem {
   const int64_t* imu_ts;
   const double* imu;        // [nsamp][6]
   double gyro_noise2, gyro_bias2, acc_noise2, acc_bias2, gravity;
+  // relative pose edges (index j = edge - nimu)
+  const double* pe_meas;    // [npe][7] T_Bk_Bk+1 q(x y z w, Hamilton) p
+  const double* pe_sqrt;    // [npe][36] row-major M with e_w = e^T M (M = L^-T, cov = L L^T)
+  const double* pe_ext;     // [npe][7] q_I_B (JPL) p_B_I
   // Inertial scratch: dt per step, end state per edge, RK4 stage inputs
   // (15 values x 4 stages per step, FP64 or FP32).
   double* ine_scratch;
@@ -118,6 +123,11 @@ cudaError_t launch_pack_state(const DevProblem& P, const double* kx, const doubl
 cudaError_t launch_inertial_v2(const DevProblem& P, const double* kf_state, bool f32_matrices, InertialLin<double> lin,
                                double* amb_res, double* const* amb_jac, double* cost_accum, int* status,
                                const int* skip_if, cudaStream_t s);
+// Relative pose edges (kernels_pose.cu): residual rows 0-5 and the (theta, p)
+// Jacobian columns of edges [nimu, nedge) into lin (if lin.r), cost into
+// cost_accum.
+cudaError_t launch_pose_edges(const DevProblem& P, const double* kf_state, InertialLin<double> lin,
+                              double* cost_accum, const int* skip_if, cudaStream_t s);
 cudaError_t launch_inertial_f32(const DevProblem& P, const InertialLin<double>& src, InertialLin<float> dst,
                                 cudaStream_t s);
 // Outlier landmarks at the current state (outlier-rejection-solver.cc:28-103):

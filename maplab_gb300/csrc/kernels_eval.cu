@@ -664,7 +664,9 @@ cudaError_t launch_inertial(const DevProblem& P, const double* kf_state, Inertia
 }
 cudaError_t launch_inertial_gated(const DevProblem& P, const double* kf_state, InertialLin<double> lin,
                                   double* cost_accum, int* status, const int* skip_if, cudaStream_t s, bool f32) {
-  return launch_inertial_impl(P, kf_state, lin, nullptr, nullptr, cost_accum, status, skip_if, s, f32);
+  cudaError_t e = launch_inertial_impl(P, kf_state, lin, nullptr, nullptr, cost_accum, status, skip_if, s, f32);
+  if (e == cudaSuccess) e = launch_pose_edges(P, kf_state, lin, cost_accum, skip_if, s);
+  return e;
 }
 
 cudaError_t launch_inertial_f32(const DevProblem& P, const InertialLin<double>& src, InertialLin<float> dst,

@@ -91,7 +91,7 @@ __global__ void __launch_bounds__(128) k_inertial_state(DevProblem P, const doub
                                                         const int* skip_if) {
   if (gated_i(skip_if)) return;
   const int64_t e = blockIdx.x * (int64_t)blockDim.x + threadIdx.x;
-  if (e >= P.nedge) return;
+  if (e >= P.nimu) return;
   const double* xf = kf_state + 16 * (int64_t)P.e_from[e];
   // integrator layout: q(4) b_g(3) v(3) b_a(3) p(3)
   double s0[16];
@@ -177,7 +177,7 @@ __global__ void __launch_bounds__(32 * kWarps) k_inertial_mat(DevProblem P, cons
   __shared__ int fail_sh[kWarps];
   const int w = threadIdx.x >> 5, lane = threadIdx.x & 31;
   const int64_t e = blockIdx.x * (int64_t)kWarps + w;
-  if (e >= P.nedge) return;
+  if (e >= P.nimu) return;
   MatSmem<TM>& S = smem[w];
   const TM gn = TM(P.gyro_noise2), gb = TM(P.gyro_bias2), an = TM(P.acc_noise2), ab = TM(P.acc_bias2);
   for (int a = lane; a < 225; a += 32) {
@@ -427,7 +427,7 @@ __global__ void __launch_bounds__(32 * kWarps) k_inertial_mat(DevProblem P, cons
 cudaError_t launch_inertial_v2(const DevProblem& P, const double* kf_state, bool f32_matrices, InertialLin<double> lin,
                                double* amb_res, double* const* amb_jac, double* cost_accum, int* status,
                                const int* skip_if, cudaStream_t s) {
-  if (P.nedge == 0) return cudaSuccess;
+  if (P.nimu == 0) return cudaSuccess;
   InertialOutputs o;
   o.lin_r = lin.r;
   o.lin_Jf = lin.Jf;
@@ -436,20 +436,20 @@ cudaError_t launch_inertial_v2(const DevProblem& P, const double* kf_state, bool
   for (int b = 0; b < 8; ++b) o.amb_J[b] = amb_jac ? amb_jac[b] : nullptr;
   o.cost = cost_accum;
   o.status = status;
-  const int64_t nsteps = P.nsamp - P.nedge;
+  const int64_t nsteps = P.nsamp - P.nimu;
   double* dt = P.ine_scratch;
   double* endst = dt + nsteps;
-  void* stage = endst + 16 * P.nedge;
-  const unsigned gA = (unsigned)((P.nedge + 127) / 128);
+  void* stage = endst + 16 * P.nimu;
+  const unsigned gA = (unsigned)((P.nimu + 127) / 128);
   if (f32_matrices) {
     k_inertial_state<float><<<gA, 128, 0, s>>>(P, kf_state, (float*)stage, dt, endst, status, skip_if);
     constexpr int W = 4;
-    k_inertial_mat<float, W><<<(unsigned)((P.nedge + W - 1) / W), 32 * W, 0, s>>>(P, kf_state, (const float*)stage, dt,
+    k_inertial_mat<float, W><<<(unsigned)((P.nimu + W - 1) / W), 32 * W, 0, s>>>(P, kf_state, (const float*)stage, dt,
                                                                                    endst, o, skip_if);
   } else {
     k_inertial_state<double><<<gA, 128, 0, s>>>(P, kf_state, (double*)stage, dt, endst, status, skip_if);
     constexpr int W = 1;
-    k_inertial_mat<double, W><<<(unsigned)((P.nedge + W - 1) / W), 32 * W, 0, s>>>(P, kf_state, (const double*)stage,
+    k_inertial_mat<double, W><<<(unsigned)((P.nimu + W - 1) / W), 32 * W, 0, s>>>(P, kf_state, (const double*)stage,
                                                                                     dt, endst, o, skip_if);
   }
   return cudaGetLastError();

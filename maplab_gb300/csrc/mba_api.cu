@@ -211,6 +211,34 @@ bool quat_ok(const double* q) {
   return std::isfinite(n) && std::fabs(n - 1.0) < 1e-5;  // assertValidQuaternion (optimization-state-buffer.h:63-80)
 }
 
+// Square-root information M = L^-1 (row-major, lower triangular) of a 6x6
+// covariance with cov = L L^T, so that the whitened residual is e^T M
+// (SixDoFBlockPoseErrorTermWithExtrinsics constructor: Cholesky of the
+// covariance, then the inverse of its factor).  False if not positive definite.
+bool pose_edge_sqrt_information(const double* cov, double* M) {
+  double L[36] = {};
+  for (int j = 0; j < 6; ++j) {
+    double diag = cov[7 * j];
+    for (int k = 0; k < j; ++k) diag -= L[6 * j + k] * L[6 * j + k];
+    if (!(diag > 0.0)) return false;
+    L[7 * j] = std::sqrt(diag);
+    for (int i = j + 1; i < 6; ++i) {
+      double v = cov[6 * i + j];
+      for (int k = 0; k < j; ++k) v -= L[6 * i + k] * L[6 * j + k];
+      L[6 * i + j] = v / L[7 * j];
+    }
+  }
+  // forward substitution, one column of L^-1 at a time
+  for (int c = 0; c < 6; ++c)
+    for (int i = 0; i < 6; ++i) {
+      if (i < c) { M[6 * i + c] = 0.0; continue; }
+      double v = (i == c) ? 1.0 : 0.0;
+      for (int k = c; k < i; ++k) v -= L[6 * i + k] * M[6 * k + c];
+      M[6 * i + c] = v / L[7 * i];
+    }
+  return true;
+}
+
 template <typename T>
 mba_status ensure_solver_buffers(mba_handle* h, SolverBuffers<T>& b) {
   if (b.ready) return MBA_OK;
@@ -728,14 +756,19 @@ mba_status mba_create(const mba_problem_desc* d, int32_t device, mba_handle** ou
   if (!d || !out) return MBA_ERR_INVALID_ARG;
   *out = nullptr;
   const int64_t NK = d->num_keyframes, NL = d->num_landmarks, N = d->num_observations, NC = d->num_cameras,
-                NM = d->num_missions, NE = d->num_imu_edges, NSMP = d->num_imu_samples;
-  if (NK <= 0 || NL < 0 || N < 0 || NC <= 0 || NC > 255 || NM <= 0 || NE < 0 || NSMP < 0) return MBA_ERR_INVALID_ARG;
+                NM = d->num_missions, NIMU = d->num_imu_edges, NPE = d->num_pose_edges,
+                NE = NIMU + NPE, NSMP = d->num_imu_samples;
+  if (NK <= 0 || NL < 0 || N < 0 || NC <= 0 || NC > 255 || NM <= 0 || NIMU < 0 || NPE < 0 || NSMP < 0)
+    return MBA_ERR_INVALID_ARG;
   if (NK >= (1ll << 31) || NL >= (1ll << 31) || N >= (1ll << 31)) return MBA_ERR_INVALID_ARG;
   if (!d->kf_q_IM_p_MI || !d->kf_v_M || !d->kf_b_g || !d->kf_b_a || !d->kf_mission || !d->mission_q_GM_p_GM || !d->cameras)
     return MBA_ERR_INVALID_ARG;
   if (N > 0 && (!d->obs_uv || !d->obs_sigma || !d->obs_landmark || !d->obs_keyframe || !d->obs_camera)) return MBA_ERR_INVALID_ARG;
   if (NL > 0 && (!d->lm_p_B || !d->lm_store_keyframe)) return MBA_ERR_INVALID_ARG;
-  if (NE > 0 && (!d->edge_from || !d->edge_to || !d->edge_sample_offset || !d->imu_timestamp_ns || !d->imu_acc_gyro))
+  if (NIMU > 0 && (!d->edge_from || !d->edge_to || !d->edge_sample_offset || !d->imu_timestamp_ns || !d->imu_acc_gyro))
+    return MBA_ERR_INVALID_ARG;
+  if (NPE > 0 && (!d->pose_edge_from || !d->pose_edge_to || !d->pose_edge_T_Bk_Bkp1 || !d->pose_edge_covariance ||
+                  !d->pose_edge_q_I_B_p_B_I))
     return MBA_ERR_INVALID_ARG;
   // ---- validation (host)
   for (int64_t k = 0; k < NK; ++k) {
@@ -763,11 +796,11 @@ mba_status mba_create(const mba_problem_desc* d, int32_t device, mba_handle** ou
     if (!(d->obs_sigma[i] > 0.0)) return MBA_ERR_INVALID_ARG;
     if (!std::isfinite(d->obs_uv[2 * i]) || !std::isfinite(d->obs_uv[2 * i + 1])) return MBA_ERR_NON_FINITE;
   }
-  if (NE > 0) {
-    if (d->edge_sample_offset[0] < 0 || d->edge_sample_offset[NE] > NSMP) return MBA_ERR_OUT_OF_RANGE_INDEX;
+  if (NIMU > 0) {
+    if (d->edge_sample_offset[0] < 0 || d->edge_sample_offset[NIMU] > NSMP) return MBA_ERR_OUT_OF_RANGE_INDEX;
     if (!(d->gyro_noise_sigma > 0 && d->gyro_bias_sigma > 0 && d->acc_noise_sigma > 0 && d->acc_bias_sigma > 0))
       return MBA_ERR_INVALID_ARG;
-    for (int64_t e = 0; e < NE; ++e) {
+    for (int64_t e = 0; e < NIMU; ++e) {
       if (d->edge_from[e] < 0 || d->edge_from[e] >= NK || d->edge_to[e] < 0 || d->edge_to[e] >= NK ||
           d->edge_from[e] == d->edge_to[e])
         return MBA_ERR_OUT_OF_RANGE_INDEX;
@@ -776,6 +809,30 @@ mba_status mba_create(const mba_problem_desc* d, int32_t device, mba_handle** ou
       for (int64_t j = a; j + 1 < b; ++j) if (d->imu_timestamp_ns[j + 1] < d->imu_timestamp_ns[j]) return MBA_ERR_UNORDERED_IMU;
       for (int64_t j = 6 * a; j < 6 * b; ++j) if (!std::isfinite(d->imu_acc_gyro[j])) return MBA_ERR_NON_FINITE;
     }
+  }
+  // Edges: the IMU edges, then the relative pose edges (square-root
+  // information of each covariance computed here, as the error term's
+  // constructor does).
+  std::vector<int32_t> e_from(NE), e_to(NE);
+  std::vector<double> pe_meas(7 * NPE), pe_sqrt(36 * NPE), pe_ext(7 * NPE);
+  if (NIMU > 0) {
+    std::copy(d->edge_from, d->edge_from + NIMU, e_from.begin());
+    std::copy(d->edge_to, d->edge_to + NIMU, e_to.begin());
+  }
+  for (int64_t j = 0; j < NPE; ++j) {
+    const int32_t f = d->pose_edge_from[j], t = d->pose_edge_to[j];
+    if (f < 0 || f >= NK || t < 0 || t >= NK || f == t) return MBA_ERR_OUT_OF_RANGE_INDEX;
+    const double* T = d->pose_edge_T_Bk_Bkp1 + 7 * j;
+    const double* X = d->pose_edge_q_I_B_p_B_I + 7 * j;
+    const double* C = d->pose_edge_covariance + 36 * j;
+    for (int a = 0; a < 7; ++a) if (!std::isfinite(T[a]) || !std::isfinite(X[a])) return MBA_ERR_NON_FINITE;
+    for (int a = 0; a < 36; ++a) if (!std::isfinite(C[a])) return MBA_ERR_NON_FINITE;
+    if (!quat_ok(T) || !quat_ok(X)) return MBA_ERR_INVALID_ARG;
+    if (!pose_edge_sqrt_information(C, &pe_sqrt[36 * j])) return MBA_ERR_NOT_SPD;
+    std::copy(T, T + 7, &pe_meas[7 * j]);
+    std::copy(X, X + 7, &pe_ext[7 * j]);
+    e_from[NIMU + j] = f;
+    e_to[NIMU + j] = t;
   }
   int ndev = 0;
   if (cudaGetDeviceCount(&ndev) != cudaSuccess || ndev <= 0) { cudaGetLastError(); return MBA_ERR_NO_DEVICE; }
@@ -833,7 +890,9 @@ mba_status mba_create(const mba_problem_desc* d, int32_t device, mba_handle** ou
   }
   // ---- keyframe tangent masks (active dims), landmark activity
   std::vector<uint8_t> in_inertial(NK, 0), in_visual(NK, 0);
-  for (int64_t e = 0; e < NE; ++e) { in_inertial[d->edge_from[e]] = 1; in_inertial[d->edge_to[e]] = 1; }
+  for (int64_t e = 0; e < NIMU; ++e) { in_inertial[e_from[e]] = 1; in_inertial[e_to[e]] = 1; }
+  // a pose edge makes the pose blocks of its keyframes active, not v / b_g / b_a
+  for (int64_t e = NIMU; e < NE; ++e) { in_visual[e_from[e]] = 1; in_visual[e_to[e]] = 1; }
   for (int64_t s = 0; s < N; ++s)
     if (otype[s] != MBA_LOCAL_KEYFRAME) { in_visual[okf[s]] = 1; in_visual[ost[s]] = 1; }
   std::vector<uint16_t> mask(NK);
@@ -948,14 +1007,14 @@ mba_status mba_create(const mba_problem_desc* d, int32_t device, mba_handle** ou
     }
   }
   std::vector<int64_t> kfe_off(NK + 1, 0);
-  for (int64_t e = 0; e < NE; ++e) { kfe_off[d->edge_from[e] + 1]++; kfe_off[d->edge_to[e] + 1]++; }
+  for (int64_t e = 0; e < NE; ++e) { kfe_off[e_from[e] + 1]++; kfe_off[e_to[e] + 1]++; }
   for (int64_t k = 0; k < NK; ++k) kfe_off[k + 1] += kfe_off[k];
   std::vector<int32_t> kfe(2 * NE);
   {
     std::vector<int64_t> fill(kfe_off.begin(), kfe_off.end() - 1);
     for (int64_t e = 0; e < NE; ++e) {
-      kfe[fill[d->edge_from[e]]++] = (int32_t)(e + 1);
-      kfe[fill[d->edge_to[e]]++] = (int32_t)(-(e + 1));
+      kfe[fill[e_from[e]]++] = (int32_t)(e + 1);
+      kfe[fill[e_to[e]]++] = (int32_t)(-(e + 1));
     }
   }
 
@@ -970,7 +1029,7 @@ mba_status mba_create(const mba_problem_desc* d, int32_t device, mba_handle** ou
     for (int64_t e = kfe_off[k]; e < kfe_off[k + 1]; ++e) {
       const int32_t code = kfe[e];
       const int64_t ed = code > 0 ? code - 1 : -code - 1;
-      nbr.push_back(code > 0 ? d->edge_to[ed] : d->edge_from[ed]);
+      nbr.push_back(code > 0 ? e_to[ed] : e_from[ed]);
       nbr_blk.push_back((int32_t)(-(ed + 1)));
     }
     nbr_off[k + 1] = (int64_t)nbr.size();
@@ -987,7 +1046,7 @@ mba_status mba_create(const mba_problem_desc* d, int32_t device, mba_handle** ou
     std::vector<int32_t> next(NK, -1), next_e(NK, -1);
     std::vector<char> has_prev(NK, 0), seen(NK, 0), start(NK, 0);
     for (int64_t e = 0; e < NE; ++e) {
-      const int32_t f = d->edge_from[e], t = d->edge_to[e];
+      const int32_t f = e_from[e], t = e_to[e];
       if (next[f] < 0 && !has_prev[t]) { next[f] = t; next_e[f] = (int32_t)e; has_prev[t] = 1; }
     }
     auto follow = [&](int32_t k) {
@@ -1043,13 +1102,11 @@ mba_status mba_create(const mba_problem_desc* d, int32_t device, mba_handle** ou
     o.width = s.width;
     o.height = s.height;
   }
-  std::vector<int32_t> e_from(NE), e_to(NE), kfm(NK);
-  std::vector<int64_t> e_off(NE + 1, 0), ts;
+  std::vector<int32_t> kfm(NK);
+  std::vector<int64_t> e_off(NIMU + 1, 0), ts;
   std::vector<double> imu;
-  if (NE > 0) {
-    e_from.assign(d->edge_from, d->edge_from + NE);
-    e_to.assign(d->edge_to, d->edge_to + NE);
-    e_off.assign(d->edge_sample_offset, d->edge_sample_offset + NE + 1);
+  if (NIMU > 0) {
+    e_off.assign(d->edge_sample_offset, d->edge_sample_offset + NIMU + 1);
     ts.assign(d->imu_timestamp_ns, d->imu_timestamp_ns + NSMP);
     imu.assign(d->imu_acc_gyro, d->imu_acc_gyro + 6 * NSMP);
   }
@@ -1058,7 +1115,7 @@ mba_status mba_create(const mba_problem_desc* d, int32_t device, mba_handle** ou
   // ---- upload
   DeviceArena& A = h->arena;
   DevProblem& P = h->P;
-  P.nkf = NK; P.nlm = NL; P.nobs = N; P.ncam = NC; P.nmis = NM; P.nedge = NE; P.nsamp = NSMP;
+  P.nkf = NK; P.nlm = NL; P.nobs = N; P.ncam = NC; P.nmis = NM; P.nedge = NE; P.nimu = NIMU; P.nsamp = NSMP;
   P.obs_uv = reinterpret_cast<const double2*>(A.upload(uv, st));
   P.obs_sinv = A.upload(sinv, st);
   P.obs_huber = A.upload(hub, st);
@@ -1084,6 +1141,9 @@ mba_status mba_create(const mba_problem_desc* d, int32_t device, mba_handle** ou
   P.e_off = A.upload(e_off, st);
   P.imu_ts = A.upload(ts, st);
   P.imu = A.upload(imu, st);
+  P.pe_meas = A.upload(pe_meas, st);
+  P.pe_sqrt = A.upload(pe_sqrt, st);
+  P.pe_ext = A.upload(pe_ext, st);
   {
     // FP32 mirrors for the FP32 evaluation kernel.
     std::vector<float> uvf(2 * N), sinvf(N), hubf(N), lmf(4 * NL, 0.f), kff(8 * NK, 0.f), misf(8 * NM, 0.f);
@@ -1158,7 +1218,7 @@ mba_status mba_create(const mba_problem_desc* d, int32_t device, mba_handle** ou
   h->tuning.chain_tail_nodes = 128;
   // Inertial scratch (kernels_inertial.cu): dt per step, end state per edge,
   // 4 RK4 stages x 15 values per step.
-  P.ine_scratch = A.alloc<double>((NSMP - NE) + 16 * NE + 60 * (NSMP - NE) + 1);
+  P.ine_scratch = A.alloc<double>((NSMP - NIMU) + 16 * NIMU + 60 * (NSMP - NIMU) + 1);
   h->scratch = A.alloc<double>(4);
   h->iscratch = A.alloc<int>(4);
   if (A.err != cudaSuccess || cudaStreamSynchronize(st) != cudaSuccess) {
@@ -1203,7 +1263,7 @@ mba_status mba_evaluate_visual(mba_handle* h, double* residuals, double* const* 
 mba_status mba_evaluate_inertial(mba_handle* h, double* residuals, double* const* jacobians) {
   if (!h) return MBA_ERR_INVALID_ARG;
   cudaSetDevice(h->device);
-  const int64_t NE = h->P.nedge;
+  const int64_t NE = h->P.nimu;
   if (NE == 0) return MBA_OK;
   static const int sz[8] = {105, 45, 45, 45, 105, 45, 45, 45};
   DeviceArena tmp;
@@ -1227,6 +1287,41 @@ mba_status mba_evaluate_inertial(mba_handle* h, double* residuals, double* const
   return (mba_status)status;
 }
 
+mba_status mba_linearize_pose_edges(mba_handle* h, double* r, double* J_from, double* J_to) {
+  if (!h) return MBA_ERR_INVALID_ARG;
+  cudaSetDevice(h->device);
+  const int64_t NIMU = h->P.nimu, NPE = h->P.nedge - NIMU;
+  if (NPE == 0) return MBA_OK;
+  // The kernel writes rows of the full 15x15 edge blocks; a scratch copy of
+  // the linearization keeps the solver's buffers untouched.
+  DeviceArena tmp;
+  InertialLin<double> lin{};
+  lin.r = tmp.alloc<double>(15 * h->P.nedge);
+  lin.Jf = tmp.alloc<double>(225 * h->P.nedge);
+  lin.Jt = tmp.alloc<double>(225 * h->P.nedge);
+  cudaError_t e = tmp.err;
+  if (e == cudaSuccess) e = launch_pose_edges(h->P, h->P.kf_state, lin, nullptr, nullptr, h->stream);
+  std::vector<double> hr(15 * NPE), hf(225 * NPE), ht(225 * NPE);
+  if (e == cudaSuccess)
+    e = cudaMemcpyAsync(hr.data(), lin.r + 15 * NIMU, sizeof(double) * 15 * NPE, cudaMemcpyDeviceToHost, h->stream);
+  if (e == cudaSuccess && J_from)
+    e = cudaMemcpyAsync(hf.data(), lin.Jf + 225 * NIMU, sizeof(double) * 225 * NPE, cudaMemcpyDeviceToHost, h->stream);
+  if (e == cudaSuccess && J_to)
+    e = cudaMemcpyAsync(ht.data(), lin.Jt + 225 * NIMU, sizeof(double) * 225 * NPE, cudaMemcpyDeviceToHost, h->stream);
+  if (e == cudaSuccess) e = cudaStreamSynchronize(h->stream);
+  tmp.release();
+  if (e != cudaSuccess) return MBA_ERR_CUDA;
+  for (int64_t j = 0; j < NPE; ++j)
+    for (int a = 0; a < 6; ++a) {
+      if (r) r[6 * j + a] = hr[15 * j + a];
+      for (int c = 0; c < 6; ++c) {
+        if (J_from) J_from[36 * j + 6 * a + c] = hf[225 * j + 15 * a + c];
+        if (J_to) J_to[36 * j + 6 * a + c] = ht[225 * j + 15 * a + c];
+      }
+    }
+  return MBA_OK;
+}
+
 mba_status mba_linearize_visual(mba_handle* h, int32_t precision, double* r, double* Jl, double* Js, double* Jo) {
   if (!h) return MBA_ERR_INVALID_ARG;
   cudaSetDevice(h->device);
@@ -1246,6 +1341,7 @@ mba_status mba_cost(mba_handle* h, int32_t precision, double* cost) {
   if (e == cudaSuccess) e = launch_visual_cost(h->P, h->P.kf_state, h->P.lm_p, h->scratch, h->iscratch, st);
   InertialLin<double> none{};
   if (e == cudaSuccess) e = launch_inertial(h->P, h->P.kf_state, none, nullptr, nullptr, h->scratch, h->iscratch + 1, st);
+  if (e == cudaSuccess) e = launch_pose_edges(h->P, h->P.kf_state, none, h->scratch, nullptr, st);
   int flags[2] = {0, 0};
   if (e == cudaSuccess) e = cudaMemcpyAsync(cost, h->scratch, sizeof(double), cudaMemcpyDeviceToHost, st);
   if (e == cudaSuccess) e = cudaMemcpyAsync(flags, h->iscratch, 2 * sizeof(int), cudaMemcpyDeviceToHost, st);
@@ -1398,9 +1494,10 @@ mba_status mba_get_stats(mba_handle* h, mba_problem_stats* s) {
   s->num_keyframes = h->P.nkf;
   s->num_landmarks = h->P.nlm;
   s->num_observations = h->P.nobs;
-  s->num_imu_edges = h->P.nedge;
+  s->num_imu_edges = h->P.nimu;
   s->num_schur_pose_blocks = 2 * h->S.npu;
   s->device_bytes = h->arena.bytes;
+  s->num_pose_edges = h->P.nedge - h->P.nimu;
   return MBA_OK;
 }
 

@@ -81,6 +81,50 @@ void quatFromJplR(const Mat3& R, double* q) {
   const double n = std::sqrt(w * w + x * x + y * y + z * z);
   q[0] = x / n; q[1] = y / n; q[2] = z / n; q[3] = w / n;
 }
+
+// Hamilton quaternion (x y z w) algebra for the odometry measurement model.
+void hMul(const double* a, const double* b, double* o) {
+  o[3] = a[3] * b[3] - a[0] * b[0] - a[1] * b[1] - a[2] * b[2];
+  o[0] = a[3] * b[0] + a[0] * b[3] + a[1] * b[2] - a[2] * b[1];
+  o[1] = a[3] * b[1] - a[0] * b[2] + a[1] * b[3] + a[2] * b[0];
+  o[2] = a[3] * b[2] + a[0] * b[1] - a[1] * b[0] + a[2] * b[3];
+}
+void hRot(const double* q, const double* v, double* o) {
+  double uv[3] = {2 * (q[1] * v[2] - q[2] * v[1]), 2 * (q[2] * v[0] - q[0] * v[2]), 2 * (q[0] * v[1] - q[1] * v[0])};
+  o[0] = v[0] + q[3] * uv[0] + (q[1] * uv[2] - q[2] * uv[1]);
+  o[1] = v[1] + q[3] * uv[1] + (q[2] * uv[0] - q[0] * uv[2]);
+  o[2] = v[2] + q[3] * uv[2] + (q[0] * uv[1] - q[1] * uv[0]);
+}
+// Transformations (q, p): x -> R(q) x + p.
+void tMul(const double* A, const double* B, double* O) {
+  hMul(A, B, O);
+  double r[3];
+  hRot(A, B + 4, r);
+  for (int i = 0; i < 3; ++i) O[4 + i] = r[i] + A[4 + i];
+}
+void tInv(const double* A, double* O) {
+  O[0] = -A[0]; O[1] = -A[1]; O[2] = -A[2]; O[3] = A[3];
+  double r[3];
+  hRot(O, A + 4, r);
+  for (int i = 0; i < 3; ++i) O[4 + i] = -r[i];
+}
+void odometryFromStates(const double* xa, const double* xb, const double* ext, double* T) {
+  const double TBI[7] = {-ext[0], -ext[1], -ext[2], ext[3], ext[4], ext[5], ext[6]};
+  double TaI[7], TBIi[7], X[7], Y[7];
+  tInv(xa, TaI);
+  tInv(TBI, TBIi);
+  tMul(TBI, TaI, X);
+  tMul(X, xb, Y);
+  tMul(Y, TBIi, T);
+}
+void hamiltonPerturb(double* T, const double* d) {
+  const double th = std::sqrt(d[0] * d[0] + d[1] * d[1] + d[2] * d[2]);
+  const double s = th > 0 ? std::sin(0.5 * th) / th : 0.5;
+  const double dq[4] = {s * d[0], s * d[1], s * d[2], std::cos(0.5 * th)};
+  double q[4];
+  hMul(T, dq, q);
+  for (int i = 0; i < 4; ++i) T[i] = q[i];
+}
 // JPL box-plus used only to perturb initial orientations.
 void jplPlus(const double* q, const double* d, double* out) {
   const double th = std::sqrt(d[0] * d[0] + d[1] * d[1] + d[2] * d[2]);
@@ -143,6 +187,8 @@ struct mba_synth_map {
   std::vector<int32_t> e_from, e_to;
   std::vector<int64_t> e_off, ts;
   std::vector<double> imu;
+  std::vector<int32_t> pe_from, pe_to;
+  std::vector<double> pe_meas, pe_cov, pe_ext;
   double gravity = 9.81;
 };
 
@@ -169,6 +215,9 @@ void mba_synth_default_config(mba_synth_config* c) {
   c->acc_noise = 0.02; c->gyro_noise = 0.002;
   c->acc_bias_rw = 0.002; c->gyro_bias_rw = 0.0002;
   c->rot_perturb = 0.05; c->pos_perturb = 0.1; c->lm_perturb = 0.2; c->vel_perturb = 0.05;
+  c->pose_edges = 0;
+  c->pose_edge_sigma_p = 0.02;
+  c->pose_edge_sigma_q = 0.005;
   c->include_inertial = 1;
   c->co_registered = 1;
 }
@@ -537,6 +586,33 @@ mba_status mba_synth_generate(const mba_synth_config* cfg, mba_synth_map** out) 
   for (int64_t l = 0; l < M->nlm; ++l)
     if (!M->lm_const[l])
       for (int i = 0; i < 3; ++i) M->lm_p[3 * l + i] += cfg->lm_perturb * rng.normal();
+  // Odometry edges between consecutive keyframes: the relative pose
+  // T_B_I T_M_Ik^-1 T_M_Ik+1 T_B_I^-1 of the true state (the measurement model
+  // of SixDoFBlockPoseErrorTermWithExtrinsics; Hamilton quaternions on the
+  // state's JPL coefficients), perturbed by the stated noise.  Drawn last so
+  // that maps without them keep their random stream.
+  if (cfg->pose_edges) {
+    const double ext[7] = {0.0, 0.0, std::sin(0.05), std::cos(0.05), 0.10, -0.02, 0.05};  // q_I_B | p_B_I
+    for (int m = 0; m < nm; ++m)
+      for (int k = 0; k + 1 < nk[m]; ++k) {
+        const int64_t a = kf0[m] + k, b = a + 1;
+        double T[7];
+        odometryFromStates(&M->kf_x_true[7 * a], &M->kf_x_true[7 * b], ext, T);
+        const double dq[3] = {cfg->pose_edge_sigma_q * rng.normal(), cfg->pose_edge_sigma_q * rng.normal(),
+                              cfg->pose_edge_sigma_q * rng.normal()};
+        hamiltonPerturb(T, dq);
+        for (int i = 0; i < 3; ++i) T[4 + i] += cfg->pose_edge_sigma_p * rng.normal();
+        M->pe_from.push_back((int32_t)a);
+        M->pe_to.push_back((int32_t)b);
+        for (int i = 0; i < 7; ++i) M->pe_meas.push_back(T[i]);
+        for (int i = 0; i < 7; ++i) M->pe_ext.push_back(ext[i]);
+        for (int r = 0; r < 6; ++r)
+          for (int c = 0; c < 6; ++c) {
+            const double sg = r < 3 ? cfg->pose_edge_sigma_p : cfg->pose_edge_sigma_q;
+            M->pe_cov.push_back(r == c ? sg * sg : 0.0);
+          }
+      }
+  }
   *out = M.release();
   return MBA_OK;
 }
@@ -556,6 +632,10 @@ mba_status mba_synth_describe(const mba_synth_map* M, mba_problem_desc* d) {
   d->mission_q_GM_p_GM = M->mis.data(); d->cameras = M->cams.data();
   d->edge_from = M->e_from.data(); d->edge_to = M->e_to.data(); d->edge_sample_offset = M->e_off.data();
   d->imu_timestamp_ns = M->ts.data(); d->imu_acc_gyro = M->imu.data();
+  d->num_pose_edges = (int64_t)M->pe_from.size();
+  d->pose_edge_from = M->pe_from.data(); d->pose_edge_to = M->pe_to.data();
+  d->pose_edge_T_Bk_Bkp1 = M->pe_meas.data(); d->pose_edge_covariance = M->pe_cov.data();
+  d->pose_edge_q_I_B_p_B_I = M->pe_ext.data();
   d->gyro_noise_sigma = M->cfg.gyro_noise; d->gyro_bias_sigma = M->cfg.gyro_bias_rw;
   d->acc_noise_sigma = M->cfg.acc_noise; d->acc_bias_sigma = M->cfg.acc_bias_rw;
   d->gravity_magnitude = M->gravity;

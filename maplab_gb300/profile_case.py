@@ -48,8 +48,11 @@ def main():
         s = g.solve(ba.default_options(max_num_iterations=a.iters, max_linear_iterations=a.pcg, precision=prec,
                                        preconditioner=pre, check_tolerances=0,
                                        use_cuda_graph=2 if a.device_loop else 1))
+        st = g.stats()
         print(json.dumps({"iterations": s["num_iterations"] - 1, "final_cost": s["final_cost"],
-                          "time_ms": s["iterations"][-1]["time_ms"], "pcg": s["linear_iterations"]}))
+                          "time_ms": s["iterations"][-1]["time_ms"], "pcg": s["linear_iterations"],
+                          "keyframes": st["num_keyframes"], "observations": st["num_observations"],
+                          "device_bytes": st["device_bytes"], "schur_pose_blocks": st["num_schur_pose_blocks"]}))
         if model is not None:
             model.close()
 

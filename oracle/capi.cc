@@ -21,6 +21,7 @@ int reducedSystemDense(Problem& p, const mba_solver_options& o, double radius, d
 // problem object is opaque to callers.
 namespace oracle {
 int oracleLinearizeVisual(Problem* p, double* r, double* Jl, double* Js, double* Jo, double* cost);
+int oracleLinearizePoseEdges(Problem* p, double* r, double* Jf, double* Jt);
 int oracleReadState(Problem* p, double* kx, double* kv, double* kbg, double* kba, double* lp);
 int oracleWriteState(Problem* p, const double* kx, const double* kv, const double* kbg, const double* kba, const double* lp);
 void oracleDestroy(Problem* p);
@@ -54,6 +55,19 @@ int oracle_solve(void* h, const mba_solver_options* o, mba_summary* s) {
 }
 int oracle_reduced_system(void* h, const mba_solver_options* o, double radius, double* A, double* b) {
   return oracle::reducedSystemDense(*(oracle::Problem*)h, *o, radius, A, b);
+}
+int oracle_linearize_pose_edges(void* h, double* r, double* Jf, double* Jt) {
+  return oracle::oracleLinearizePoseEdges((oracle::Problem*)h, r, Jf, Jt);
+}
+// One relative pose term: residual [6] and ambient Jacobians [6][7] (q, p) of
+// both keyframe blocks; cov [36] (p, q order).  Returns 0, or 1 if cov is not
+// positive definite.
+int oracle_pose_edge(const double* xk, const double* xk1, const double* ext, const double* meas, const double* cov,
+                     double* r, double* Jk, double* Jk1) {
+  double M[36];
+  if (!oracle::poseEdgeSqrtInfo(cov, M)) return 1;
+  oracle::poseEdgeEvaluate(xk, xk1, ext, meas, M, r, Jk, Jk1);
+  return 0;
 }
 int oracle_read_state(void* h, double* kx, double* kv, double* kbg, double* kba, double* lp) {
   return oracle::oracleReadState((oracle::Problem*)h, kx, kv, kbg, kba, lp);

@@ -149,6 +149,9 @@ int pinholeProject3(const mba_camera& cam, const double* p_C, double* kp,
 // row-major ambient blocks (2x3, 2x7, 2x7, 2x7, 2x7, 2x4, 2x3, 2x4, 2x4).
 // Returns true like Evaluate; *failed tells whether the projection failed.
 void visualPointInCamera(const double* const* params, int type, double* p_C);
+void poseEdgeEvaluate(const double* xk, const double* xk1, const double* ext, const double* meas, const double* M,
+                      double* r, double* Jk, double* Jk1);
+bool poseEdgeSqrtInfo(const double* cov, double* M);
 bool visualEvaluate(const double* const* params, const double* measurement, double pixel_sigma,
                     int error_type, const mba_camera& cam, double* residual,
                     double** jacobians, bool* failed);

@@ -39,6 +39,8 @@ static void parallelFor(int64_t n, int threads, const std::function<void(int64_t
 
 struct Problem {
   int64_t nkf = 0, nlm = 0, nobs = 0, ncam = 0, nmis = 0, nedge = 0, nsamp = 0;
+  int64_t nimu = 0;  // edges [0, nimu) are IMU edges, [nimu, nedge) relative pose edges
+  std::vector<double> pe_meas, pe_M, pe_ext;  // per pose edge: [7], [36] sqrt information, [7]
   std::vector<double> obs_uv, obs_sigma;
   std::vector<int32_t> obs_lm, obs_kf, obs_cam;
   std::vector<uint8_t> obs_type;
@@ -87,13 +89,25 @@ int createProblem(const mba_problem_desc* d, Problem** out) {
   if (d->kf_flags) p->kf_flags.assign(d->kf_flags, d->kf_flags + p->nkf);
   p->mis.assign(d->mission_q_GM_p_GM, d->mission_q_GM_p_GM + 7 * p->nmis);
   p->cams.assign(d->cameras, d->cameras + p->ncam);
-  if (p->nedge > 0) {
-    p->e_from.assign(d->edge_from, d->edge_from + p->nedge);
-    p->e_to.assign(d->edge_to, d->edge_to + p->nedge);
-    p->e_off.assign(d->edge_sample_offset, d->edge_sample_offset + p->nedge + 1);
+  p->nimu = p->nedge;
+  if (p->nimu > 0) {
+    p->e_from.assign(d->edge_from, d->edge_from + p->nimu);
+    p->e_to.assign(d->edge_to, d->edge_to + p->nimu);
+    p->e_off.assign(d->edge_sample_offset, d->edge_sample_offset + p->nimu + 1);
     p->ts.assign(d->imu_timestamp_ns, d->imu_timestamp_ns + p->nsamp);
     p->imu.assign(d->imu_acc_gyro, d->imu_acc_gyro + 6 * p->nsamp);
   }
+  // Relative pose edges follow the IMU edges.
+  for (int64_t j = 0; j < d->num_pose_edges; ++j) {
+    p->e_from.push_back(d->pose_edge_from[j]);
+    p->e_to.push_back(d->pose_edge_to[j]);
+    p->pe_meas.insert(p->pe_meas.end(), d->pose_edge_T_Bk_Bkp1 + 7 * j, d->pose_edge_T_Bk_Bkp1 + 7 * j + 7);
+    p->pe_ext.insert(p->pe_ext.end(), d->pose_edge_q_I_B_p_B_I + 7 * j, d->pose_edge_q_I_B_p_B_I + 7 * j + 7);
+    double M[36];
+    if (!poseEdgeSqrtInfo(d->pose_edge_covariance + 36 * j, M)) { delete p; return MBA_ERR_NOT_SPD; }
+    p->pe_M.insert(p->pe_M.end(), M, M + 36);
+  }
+  p->nedge = p->nimu + d->num_pose_edges;
   p->noise = {d->gyro_noise_sigma, d->gyro_bias_sigma, d->acc_noise_sigma, d->acc_bias_sigma,
               d->gravity_magnitude};
   p->use_huber = d->use_huber;
@@ -124,7 +138,10 @@ int createProblem(const mba_problem_desc* d, Problem** out) {
   // Active tangent dims.  KF tangent order: theta(3), p(3), v(3), b_g(3), b_a(3).
   p->kf_mask.assign(15 * p->nkf, 1);
   std::vector<uint8_t> in_inertial(p->nkf, 0), in_visual(p->nkf, 0);
-  for (int64_t e = 0; e < p->nedge; ++e) { in_inertial[p->e_from[e]] = 1; in_inertial[p->e_to[e]] = 1; }
+  for (int64_t e = 0; e < p->nimu; ++e) { in_inertial[p->e_from[e]] = 1; in_inertial[p->e_to[e]] = 1; }
+  // a pose edge constrains the pose blocks only (the keyframe's pose is in the
+  // problem, its speed and biases are not unless an IMU edge uses them)
+  for (int64_t e = p->nimu; e < p->nedge; ++e) { in_visual[p->e_from[e]] = 1; in_visual[p->e_to[e]] = 1; }
   for (int64_t i = 0; i < p->nobs; ++i) {
     if (p->obs_type[i] != MBA_LOCAL_KEYFRAME) { in_visual[p->obs_kf[i]] = 1; in_visual[p->lm_store[p->obs_lm[i]]] = 1; }
   }
@@ -158,7 +175,10 @@ static void poseParam(const Problem& p, int64_t k, double* P76) {
   if (p.kf_flags[k] & MBA_KF_GAUGE_ROLL_PITCH) {
     double J42[8];
     jplRollPitchJacobian(&p.mis[7 * p.kf_mis[k]], q, J42);
-    for (int r = 0; r < 4; ++r) { P76[6 * r + 0] = J42[2 * r]; P76[6 * r + 1] = J42[2 * r + 1]; }
+    for (int r = 0; r < 4; ++r) {
+      P76[6 * r + 0] = m[0] ? J42[2 * r] : 0.0;
+      P76[6 * r + 1] = m[1] ? J42[2 * r + 1] : 0.0;
+    }
   } else {
     double Jq[12];
     jplQuaternionJacobian(q, Jq);
@@ -211,7 +231,7 @@ static void inertialParams(const Problem& p, int64_t e, const double** P) {
 
 int evaluateInertialAmbient(const Problem& p, double* res, double* const* jac) {
   int status = 0;
-  parallelFor(p.nedge, p.threads, [&](int64_t b, int64_t e) {
+  parallelFor(p.nimu, p.threads, [&](int64_t b, int64_t e) {
     static const int sz[8] = {105, 45, 45, 45, 105, 45, 45, 45};
     for (int64_t i = b; i < e; ++i) {
       const double* P[8];
@@ -345,7 +365,7 @@ int linearize(const Problem& p, bool want_jac, Linearization* L) {
   int status = 0;
   {
     std::vector<std::thread> ts;
-    const int64_t chunk = (p.nedge + T - 1) / T;
+    const int64_t chunk = (p.nimu + T - 1) / T;
     auto workRange = [&](int t, int64_t b, int64_t e) {
       double acc = 0.0;
       for (int64_t i = b; i < e; ++i) {
@@ -384,14 +404,40 @@ int linearize(const Problem& p, bool want_jac, Linearization* L) {
       }
       ipart[t] = acc;
     };
-    if (p.nedge < 64) workRange(0, 0, p.nedge);
+    if (p.nimu < 64) workRange(0, 0, p.nimu);
     else {
       for (int t = 0; t < T; ++t)
-        ts.emplace_back(workRange, t, std::min<int64_t>(p.nedge, t * chunk), std::min<int64_t>(p.nedge, (t + 1) * chunk));
+        ts.emplace_back(workRange, t, std::min<int64_t>(p.nimu, t * chunk), std::min<int64_t>(p.nimu, (t + 1) * chunk));
       for (auto& t : ts) t.join();
     }
   }
   for (double v : ipart) cost += v;
+  // relative pose edges: residual rows 0-5, tangent columns (theta, p) through
+  // the pose parameterization (ambient Jacobian x ComputeJacobian).
+  for (int64_t i = p.nimu; i < p.nedge; ++i) {
+    const int64_t j = i - p.nimu, f = p.e_from[i], t = p.e_to[i];
+    double r[6], Jf7[42], Jt7[42];
+    poseEdgeEvaluate(&p.kf_x[7 * f], &p.kf_x[7 * t], &p.pe_ext[7 * j], &p.pe_meas[7 * j], &p.pe_M[36 * j], r,
+                     want_jac ? Jf7 : nullptr, want_jac ? Jt7 : nullptr);
+    double sq = 0.0;
+    for (int k = 0; k < 6; ++k) sq += r[k] * r[k];
+    cost += 0.5 * sq;
+    if (!want_jac) continue;
+    for (int k = 0; k < 6; ++k) L->ir[15 * i + k] = r[k];
+    for (int s2 = 0; s2 < 2; ++s2) {
+      const int64_t k = s2 == 0 ? f : t;
+      const double* J7 = s2 == 0 ? Jf7 : Jt7;
+      double* out = s2 == 0 ? &L->iJf[225 * i] : &L->iJt[225 * i];
+      double P76[42];
+      poseParam(p, k, P76);
+      for (int rr = 0; rr < 6; ++rr)
+        for (int c = 0; c < 6; ++c) {
+          double a = 0.0;
+          for (int mm = 0; mm < 7; ++mm) a += J7[7 * rr + mm] * P76[6 * mm + c];
+          out[15 * rr + c] = a;
+        }
+    }
+  }
   L->cost = cost;
   if (!std::isfinite(cost) && status == 0) status = MBA_ERR_NON_FINITE;
   return status;
@@ -1031,6 +1077,24 @@ int reducedSystemDense(Problem& p, const mba_solver_options& o, double radius, d
   buildPattern(p, &pattern);
   StepResult r = computeStep(p, L, sc, dkf, dlm, pattern, MBA_LINEAR_SOLVER_DENSE_SCHUR, 1, 0.0, A, b);
   return r.status;
+}
+
+// Relative pose edges at the current state: r [n][6], tangent Jacobians
+// [n][36] (rows 0-5 / columns theta, p of the 15x15 edge blocks).
+int oracleLinearizePoseEdges(Problem* p, double* r, double* Jf, double* Jt) {
+  Linearization L;
+  const int st = linearize(*p, true, &L);
+  for (int64_t i = p->nimu; i < p->nedge; ++i) {
+    const int64_t j = i - p->nimu;
+    for (int a = 0; a < 6; ++a) {
+      if (r) r[6 * j + a] = L.ir[15 * i + a];
+      for (int c = 0; c < 6; ++c) {
+        if (Jf) Jf[36 * j + 6 * a + c] = L.iJf[225 * i + 15 * a + c];
+        if (Jt) Jt[36 * j + 6 * a + c] = L.iJt[225 * i + 15 * a + c];
+      }
+    }
+  }
+  return st;
 }
 
 int oracleLinearizeVisual(Problem* p, double* r, double* Jl, double* Js, double* Jo, double* cost) {

@@ -680,4 +680,120 @@ int inertialEvaluate(const ImuNoise& n, const double* const* P, int ns, const in
   return 0;
 }
 
+
+// ---------------------------------------------------------------- pose edges
+// Forward-mode dual number with N derivative components (the role of
+// ceres::Jet in the reference's AutoDiffCostFunction).
+template <int N>
+struct Dual {
+  double a = 0.0;
+  double d[N] = {};
+  Dual() = default;
+  Dual(double v) : a(v) {}  // NOLINT
+};
+template <int N> Dual<N> operator+(const Dual<N>& x, const Dual<N>& y) { Dual<N> r(x.a + y.a); for (int i = 0; i < N; ++i) r.d[i] = x.d[i] + y.d[i]; return r; }
+template <int N> Dual<N> operator-(const Dual<N>& x, const Dual<N>& y) { Dual<N> r(x.a - y.a); for (int i = 0; i < N; ++i) r.d[i] = x.d[i] - y.d[i]; return r; }
+template <int N> Dual<N> operator-(const Dual<N>& x) { Dual<N> r(-x.a); for (int i = 0; i < N; ++i) r.d[i] = -x.d[i]; return r; }
+template <int N> Dual<N> operator*(const Dual<N>& x, const Dual<N>& y) { Dual<N> r(x.a * y.a); for (int i = 0; i < N; ++i) r.d[i] = x.a * y.d[i] + x.d[i] * y.a; return r; }
+template <int N> bool isNegative(const Dual<N>& x) { return x.a < 0.0; }
+
+// Hamilton quaternion (x y z w) product, rotation (Eigen's _transformVector
+// form), and the transformation algebra of minkindr (x -> R(q) x + p).
+template <typename S> static void hqMul(const S* a, const S* b, S* o) {
+  o[3] = a[3] * b[3] - a[0] * b[0] - a[1] * b[1] - a[2] * b[2];
+  o[0] = a[3] * b[0] + a[0] * b[3] + a[1] * b[2] - a[2] * b[1];
+  o[1] = a[3] * b[1] - a[0] * b[2] + a[1] * b[3] + a[2] * b[0];
+  o[2] = a[3] * b[2] + a[0] * b[1] - a[1] * b[0] + a[2] * b[3];
+}
+template <typename S> static void hqRot(const S* q, const S* v, S* o) {
+  const S two(2.0);
+  S uv[3] = {two * (q[1] * v[2] - q[2] * v[1]), two * (q[2] * v[0] - q[0] * v[2]), two * (q[0] * v[1] - q[1] * v[0])};
+  o[0] = v[0] + q[3] * uv[0] + (q[1] * uv[2] - q[2] * uv[1]);
+  o[1] = v[1] + q[3] * uv[1] + (q[2] * uv[0] - q[0] * uv[2]);
+  o[2] = v[2] + q[3] * uv[2] + (q[0] * uv[1] - q[1] * uv[0]);
+}
+template <typename S> static void htMul(const S* A, const S* B, S* O) {
+  hqMul(A, B, O);
+  S r[3];
+  hqRot(A, B + 4, r);
+  for (int i = 0; i < 3; ++i) O[4 + i] = r[i] + A[4 + i];
+}
+template <typename S> static void htInv(const S* A, S* O) {
+  O[0] = -A[0]; O[1] = -A[1]; O[2] = -A[2]; O[3] = A[3];
+  S r[3];
+  hqRot(O, A + 4, r);
+  for (int i = 0; i < 3; ++i) O[4 + i] = -r[i];
+}
+
+// SixDoFBlockPoseErrorTermWithExtrinsics::operator()
+// (six-dof-block-pose-error-term-with-extrinsics-autodiff-inl.h:6-55):
+// T_Bk_Bkp1_est = T_B_I T_G_Ik^-1 T_G_Ikp1 T_B_I^-1 with the keyframe blocks'
+// coefficients read as Hamilton quaternions; e = [p_meas - p_est;
+// 2 vec(q_meas^-1 q_est) (w >= 0)]; e_w = e^T sqrtinfo (row vector).
+template <typename S>
+static void poseEdgeResidual(const S* xk, const S* xk1, const double* ext, const double* meas, const double* M, S* ew) {
+  S TBI[7] = {S(-ext[0]), S(-ext[1]), S(-ext[2]), S(ext[3]), S(ext[4]), S(ext[5]), S(ext[6])};
+  S TkI[7], TBIi[7], X[7], Y[7], Te[7];
+  htInv(xk, TkI);
+  htInv(TBI, TBIi);
+  htMul(TBI, TkI, X);
+  htMul(X, xk1, Y);
+  htMul(Y, TBIi, Te);
+  const S qmi[4] = {S(-meas[0]), S(-meas[1]), S(-meas[2]), S(meas[3])};
+  S qe[4];
+  hqMul(qmi, Te, qe);
+  if (isNegative(qe[3]))
+    for (int i = 0; i < 4; ++i) qe[i] = -qe[i];
+  S e[6];
+  for (int i = 0; i < 3; ++i) e[i] = S(meas[4 + i]) - Te[4 + i];
+  for (int i = 0; i < 3; ++i) e[3 + i] = S(2.0) * qe[i];
+  for (int j = 0; j < 6; ++j) {
+    S acc(0.0);
+    for (int i = 0; i < 6; ++i) acc = acc + e[i] * S(M[6 * i + j]);
+    ew[j] = acc;
+  }
+}
+
+// Residual and ambient Jacobians ([6][7] each, w.r.t. q(4) p(3)) by forward
+// differentiation, as AutoDiffCostFunction computes them.
+void poseEdgeEvaluate(const double* xk, const double* xk1, const double* ext, const double* meas, const double* M,
+                      double* r, double* Jk, double* Jk1) {
+  typedef Dual<14> D;
+  D a[7], b[7], ew[6];
+  for (int i = 0; i < 7; ++i) { a[i] = D(xk[i]); a[i].d[i] = 1.0; b[i] = D(xk1[i]); b[i].d[7 + i] = 1.0; }
+  poseEdgeResidual(a, b, ext, meas, M, ew);
+  for (int j = 0; j < 6; ++j) {
+    r[j] = ew[j].a;
+    for (int c = 0; c < 7; ++c) {
+      if (Jk) Jk[7 * j + c] = ew[j].d[c];
+      if (Jk1) Jk1[7 * j + c] = ew[j].d[7 + c];
+    }
+  }
+}
+
+// Square-root information of a 6x6 covariance: L^-1 with L L^T = cov
+// (SixDoFBlockPoseErrorTermWithExtrinsics constructor, Eigen llt + triangular
+// solve).  Returns false if cov is not positive definite.
+bool poseEdgeSqrtInfo(const double* cov, double* M) {
+  double L[36] = {};
+  for (int j = 0; j < 6; ++j) {
+    double dsum = cov[7 * j];
+    for (int k = 0; k < j; ++k) dsum -= L[6 * j + k] * L[6 * j + k];
+    if (!(dsum > 0.0)) return false;
+    L[7 * j] = std::sqrt(dsum);
+    for (int i = j + 1; i < 6; ++i) {
+      double v = cov[6 * i + j];
+      for (int k = 0; k < j; ++k) v -= L[6 * i + k] * L[6 * j + k];
+      L[6 * i + j] = v / L[7 * j];
+    }
+  }
+  for (int c = 0; c < 6; ++c)
+    for (int i = 0; i < 6; ++i) {
+      double v = (i == c) ? 1.0 : 0.0;
+      for (int k = c; k < i; ++k) v -= L[6 * i + k] * M[6 * k + c];
+      M[6 * i + c] = (i < c) ? 0.0 : v / L[7 * i];
+    }
+  return true;
+}
+
 }  // namespace oracle

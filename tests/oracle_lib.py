@@ -36,6 +36,8 @@ def load():
         "oracle_linearize_visual": (ctypes.c_int, [vp, dp, dp, dp, dp, dp]),
         "oracle_solve": (ctypes.c_int, [vp, ctypes.POINTER(N.SolverOptions), ctypes.POINTER(N.Summary)]),
         "oracle_read_state": (ctypes.c_int, [vp, dp, dp, dp, dp, dp]),
+        "oracle_linearize_pose_edges": (ctypes.c_int, [vp, dp, dp, dp]),
+        "oracle_pose_edge": (ctypes.c_int, [dp, dp, dp, dp, dp, dp, dp, dp]),
         "oracle_reduced_system": (ctypes.c_int, [vp, ctypes.POINTER(N.SolverOptions), ctypes.c_double, dp, dp]),
         "oracle_write_state": (ctypes.c_int, [vp, dp, dp, dp, dp, dp]),
         "oracle_time_visual": (ctypes.c_double, [vp, ctypes.c_int, ctypes.c_int64, ctypes.c_int]),
@@ -136,6 +138,12 @@ class OracleProblem:
         if st != 0:
             raise RuntimeError(f"oracle_reduced_system failed: {st}")
         return A, b
+
+    def linearize_pose_edges(self):
+        n = self.desc.num_pose_edges
+        r = np.zeros((n, 6)); Jf = np.zeros((n, 36)); Jt = np.zeros((n, 36))
+        self.lib.oracle_linearize_pose_edges(self.h, N.ptr(r), N.ptr(Jf), N.ptr(Jt))
+        return r, Jf, Jt
 
     def read_state(self):
         d = self.desc
