@@ -130,18 +130,36 @@ typedef struct mba_problem_desc {
   int32_t pad_;
   double huber_delta_local;
   double huber_delta_global;
-  /* Relative 6-DoF pose edges: odometry and wheel-odometry TransformationEdges
-   * (addRelativePoseTermsForEdges, optimization-terms-addition.cc:543-640),
-   * residual SixDoFBlockPoseErrorTermWithExtrinsics
-   * (six-dof-block-pose-error-term-with-extrinsics-autodiff-inl.h), no loss.
-   * Sensor extrinsics are constant (ba_fix_*_extrinsics). */
+  /* Pose-graph terms ("pose edges"), no loss, sensor extrinsics and mission
+   * baseframes constant.  Kind per edge (pose_edge_type):
+   *  MBA_POSE_EDGE_RELATIVE: odometry / wheel-odometry TransformationEdge
+   *    (addRelativePoseTermsForEdges, optimization-terms-addition.cc:543-640),
+   *    SixDoFBlockPoseErrorTermWithExtrinsics; measurement T_Bk_Bkp1,
+   *    extrinsics q_I_B | p_B_I, covariance get_T_A_B_Covariance_p_q.
+   *  MBA_POSE_EDGE_LOOP_CLOSURE: LoopClosureEdge (augment-loopclosure.cc:
+   *    10-164), LoopClosureEdgeErrorTerm times a switch variable in [0, 1];
+   *    measurement T_A_B, covariance get_T_A_B_Covariance; extrinsics unused.
+   *    With a switch variance > 0 the switch is a variable with
+   *    SwitchPriorErrorTerm(1, variance) and bounds [0, 1]; with 0 it is held
+   *    at its given value.
+   *  MBA_POSE_EDGE_ABSOLUTE: Absolute6DoFMeasurement of keyframe `from`
+   *    (addAbsolutePoseConstraintTermsForVertices, :650-738),
+   *    BlockPosePriorErrorTermV2 with the keyframe mission's baseframe;
+   *    measurement T_G_S, covariance get_T_G_S_covariance, extrinsics the
+   *    sensor block q_S_B | p_S_B (JPL); pose_edge_to ignored.
+   * Measurements are aslam::Transformation values: q (x y z w, Hamilton) | p. */
   int64_t num_pose_edges;
-  const int32_t* pose_edge_from;       /* [N_pe] keyframe of T_Bk */
-  const int32_t* pose_edge_to;         /* [N_pe] keyframe of T_Bkp1 */
-  const double* pose_edge_T_Bk_Bkp1;   /* [N_pe][7] measured q (x y z w) | p, aslam::Transformation */
-  const double* pose_edge_covariance;  /* [N_pe][36] row-major, order (p, q): get_T_A_B_Covariance_p_q */
-  const double* pose_edge_q_I_B_p_B_I; /* [N_pe][7] extrinsics block q_I_B (x y z w) | p_B_I */
+  const int32_t* pose_edge_from;       /* [N_pe] keyframe A (T_Bk, the vertex of an absolute term) */
+  const int32_t* pose_edge_to;         /* [N_pe] keyframe B (T_Bkp1) */
+  const double* pose_edge_T_Bk_Bkp1;   /* [N_pe][7] measurement q (x y z w) | p */
+  const double* pose_edge_covariance;  /* [N_pe][36] row-major, residual order (p, q) */
+  const double* pose_edge_q_I_B_p_B_I; /* [N_pe][7] extrinsics block (see above) */
+  const int32_t* pose_edge_type;       /* [N_pe] MBA_POSE_EDGE_*; NULL = all RELATIVE */
+  const double* pose_edge_switch;      /* [N_pe] initial switch of a loop closure; NULL = 1 */
+  const double* pose_edge_switch_variance; /* [N_pe] switch prior variance; NULL = all 0 */
 } mba_problem_desc;
+
+enum { MBA_POSE_EDGE_RELATIVE = 0, MBA_POSE_EDGE_LOOP_CLOSURE = 1, MBA_POSE_EDGE_ABSOLUTE = 2 };
 
 /* Subset of ceres::Solver::Options used by map_optimization
  * (include/map-optimization/solver-options.h:26-75), same names and defaults
@@ -262,11 +280,17 @@ mba_status mba_evaluate_inertial(mba_handle* h, double* residuals, double* const
 mba_status mba_linearize_visual(mba_handle* h, int32_t precision, double* r,
                                 double* J_landmark, double* J_store, double* J_observer);
 
-/* Relative pose edges at the current state: whitened residual [N_pe][6] and
- * tangent Jacobians [N_pe][6x6] w.r.t. the (theta, p) tangent of the from /
- * to keyframe (Ceres: autodiff ambient Jacobian times the JPL pose
- * parameterization's ComputeJacobian).  Host pointers, each may be NULL. */
+/* Pose edges at the current state: whitened residual [N_pe][6] (times the
+ * switch for loop closures) and tangent Jacobians [N_pe][6x6] w.r.t. the
+ * (theta, p) tangent of the from / to keyframe (Ceres: autodiff ambient
+ * Jacobian times the JPL pose parameterization's ComputeJacobian; J_to is
+ * zero for absolute terms).  Host pointers, each may be NULL. */
 mba_status mba_linearize_pose_edges(mba_handle* h, double* r, double* J_from, double* J_to);
+
+/* Switch variables of the pose edges [N_pe] (1 for edges without one).
+ * Writing clamps nothing: values must lie in [0, 1]. */
+mba_status mba_read_switch_variables(mba_handle* h, double* s);
+mba_status mba_write_switch_variables(mba_handle* h, const double* s);
 
 /* Ceres-style total cost 0.5 * sum rho(|r|^2) at the current state. */
 mba_status mba_cost(mba_handle* h, int32_t precision, double* cost);
@@ -380,6 +404,15 @@ typedef struct mba_problem_stats {
   int64_t num_pose_edges;          /* relative pose edges (after the IMU edges) */
 } mba_problem_stats;
 mba_status mba_get_stats(mba_handle* h, mba_problem_stats* stats);
+
+/* Pose-graph relaxation (VIMapRelaxation::solveRelaxation,
+ * vi-map-relaxation.cc:97-151): the same solve with velocities, biases and
+ * landmark positions fixed (intrinsics and extrinsics are always fixed here)
+ * and the loop-closure edges added.  Host only: fills kf_flags_out [N_kf]
+ * with desc's flags plus the velocity / bias fixes and lm_constant_out [N_lm]
+ * with 1; the caller points a copy of desc at them and solves with
+ * mba_create / mba_solve as usual. */
+mba_status mba_relaxation_flags(const mba_problem_desc* desc, uint32_t* kf_flags_out, uint8_t* lm_constant_out);
 
 /* Visual observations and the state they depend on, all in DEVICE memory
  * owned by the caller, laid out as in mba_problem_desc (state arrays in the

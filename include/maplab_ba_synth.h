@@ -57,6 +57,15 @@ typedef struct mba_synth_config {
   int32_t pad_;
   double pose_edge_sigma_p;       /* odometry position noise (m) */
   double pose_edge_sigma_q;       /* odometry rotation noise (rad) */
+  /* > 0: a loop closure every this many keyframes, to the keyframe one lap
+   * later in the same mission and to the same-index keyframe of the next
+   * mission. */
+  int32_t loop_closure_stride;
+  int32_t absolute_pose_stride;   /* > 0: an absolute 6-DoF measurement every this many keyframes */
+  double loop_closure_sigma_p, loop_closure_sigma_q;
+  double loop_closure_outlier_fraction; /* loop closures replaced by a wrong transform (0.5 rad, 3 m noise) */
+  double loop_closure_switch_variance;  /* > 0: switchable loop closures; 0: switch held at 1 */
+  double absolute_pose_sigma_p, absolute_pose_sigma_q;
 } mba_synth_config;
 
 typedef struct mba_synth_map mba_synth_map;

@@ -26,6 +26,9 @@ MBA_ERR_NOT_SPD = 4
 MBA_ERR_CUDA = 5
 MBA_ERR_TIMEOUT = 6
 MBA_ERR_CANCELLED = 7
+MBA_POSE_EDGE_RELATIVE = 0
+MBA_POSE_EDGE_LOOP_CLOSURE = 1
+MBA_POSE_EDGE_ABSOLUTE = 2
 MBA_ERR_NO_DEVICE = 8
 MBA_ERR_UNORDERED_IMU = 9
 
@@ -105,6 +108,9 @@ class ProblemDesc(ctypes.Structure):
         ("pose_edge_T_Bk_Bkp1", c_double_p),
         ("pose_edge_covariance", c_double_p),
         ("pose_edge_q_I_B_p_B_I", c_double_p),
+        ("pose_edge_type", c_int32_p),
+        ("pose_edge_switch", c_double_p),
+        ("pose_edge_switch_variance", c_double_p),
     ]
 
 
@@ -257,6 +263,14 @@ class SynthConfig(ctypes.Structure):
         ("pad_", ctypes.c_int32),
         ("pose_edge_sigma_p", ctypes.c_double),
         ("pose_edge_sigma_q", ctypes.c_double),
+        ("loop_closure_stride", ctypes.c_int32),
+        ("absolute_pose_stride", ctypes.c_int32),
+        ("loop_closure_sigma_p", ctypes.c_double),
+        ("loop_closure_sigma_q", ctypes.c_double),
+        ("loop_closure_outlier_fraction", ctypes.c_double),
+        ("loop_closure_switch_variance", ctypes.c_double),
+        ("absolute_pose_sigma_p", ctypes.c_double),
+        ("absolute_pose_sigma_q", ctypes.c_double),
     ]
 
 
@@ -304,6 +318,10 @@ def load_ba():
     _declare(lib, "mba_evaluate_inertial", ctypes.c_int, [vp, c_double_p, ctypes.POINTER(c_double_p)])
     _declare(lib, "mba_linearize_visual", ctypes.c_int, [vp, ctypes.c_int32] + [c_double_p] * 4)
     _declare(lib, "mba_linearize_pose_edges", ctypes.c_int, [vp] + [c_double_p] * 3)
+    _declare(lib, "mba_read_switch_variables", ctypes.c_int, [vp, c_double_p])
+    _declare(lib, "mba_relaxation_flags", ctypes.c_int, [ctypes.POINTER(ProblemDesc), ctypes.POINTER(ctypes.c_uint32),
+                                                         ctypes.POINTER(ctypes.c_uint8)])
+    _declare(lib, "mba_write_switch_variables", ctypes.c_int, [vp, c_double_p])
     _declare(lib, "mba_cost", ctypes.c_int, [vp, ctypes.c_int32, c_double_p])
     _declare(lib, "mba_solve", ctypes.c_int, [vp, ctypes.POINTER(SolverOptions), ctypes.POINTER(Summary)])
     _declare(lib, "mba_read_state", ctypes.c_int, [vp] + [c_double_p] * 5)

@@ -213,6 +213,9 @@ class BundleAdjuster:
         part = lambda p, n: np.ctypeslib.as_array(p, (n,)).copy() if n else np.zeros(0, np.int32)
         ef = np.concatenate([part(d.edge_from, ni), part(d.pose_edge_from, npe)]).astype(np.int32)
         et = np.concatenate([part(d.edge_to, ni), part(d.pose_edge_to, npe)]).astype(np.int32)
+        if npe and d.pose_edge_type:  # an absolute term is a (zero) block of its own keyframe
+            ty = np.ctypeslib.as_array(d.pose_edge_type, (npe,))
+            et[ni:][ty == N.MBA_POSE_EDGE_ABSOLUTE] = ef[ni:][ty == N.MBA_POSE_EDGE_ABSOLUTE]
         return dict(diag=D, upper_ij=ij, upper=U, inertial=E, edge_from=ef, edge_to=et, rhs=b)
 
     def rejected_landmarks(self):
@@ -273,3 +276,41 @@ class BundleAdjuster:
 
     def cancel(self):
         self._lib.mba_cancel(self._h)
+
+    def read_switch_variables(self):
+        """Switch value per pose edge [N_pe] (1 where an edge has none)."""
+        sw = np.zeros(self.desc.num_pose_edges)
+        _check(self._lib.mba_read_switch_variables(self._h, N.ptr(sw)), "mba_read_switch_variables")
+        return sw
+
+    def write_switch_variables(self, sw):
+        sw = np.ascontiguousarray(sw, dtype=np.float64)
+        _check(self._lib.mba_write_switch_variables(self._h, N.ptr(sw)), "mba_write_switch_variables")
+
+
+class RelaxationProblem:
+    """The descriptor of a pose-graph relaxation (VIMapRelaxation::
+    solveRelaxation, vi-map-relaxation.cc:97-151): a copy of `desc` with
+    velocities, biases and landmark positions fixed; the arrays it points at
+    live as long as this object."""
+
+    def __init__(self, desc):
+        self.desc = N.ProblemDesc()
+        ctypes.memmove(ctypes.byref(self.desc), ctypes.byref(desc), ctypes.sizeof(desc))
+        self.kf_flags = np.zeros(desc.num_keyframes, dtype=np.uint32)
+        self.lm_constant = np.zeros(max(1, desc.num_landmarks), dtype=np.uint8)
+        _check(lib().mba_relaxation_flags(ctypes.byref(desc),
+                                          self.kf_flags.ctypes.data_as(ctypes.POINTER(ctypes.c_uint32)),
+                                          self.lm_constant.ctypes.data_as(ctypes.POINTER(ctypes.c_uint8))),
+               "mba_relaxation_flags")
+        self.desc.kf_flags = self.kf_flags.ctypes.data_as(ctypes.POINTER(ctypes.c_uint32))
+        self.desc.lm_constant = self.lm_constant.ctypes.data_as(ctypes.POINTER(ctypes.c_uint8))
+
+
+def relax(desc, opts=None, device=0):
+    """Runs the relaxation solve on the device; returns (summary, state,
+    switch variables)."""
+    rp = RelaxationProblem(desc)
+    with BundleAdjuster(rp.desc, device) as g:
+        s = g.solve(opts)
+        return s, g.read_state(), g.read_switch_variables()

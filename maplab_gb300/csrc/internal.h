@@ -45,10 +45,19 @@ struct DevProblem {
   const int64_t* imu_ts;
   const double* imu;        // [nsamp][6]
   double gyro_noise2, gyro_bias2, acc_noise2, acc_bias2, gravity;
-  // relative pose edges (index j = edge - nimu)
-  const double* pe_meas;    // [npe][7] T_Bk_Bk+1 q(x y z w, Hamilton) p
-  const double* pe_sqrt;    // [npe][36] row-major M with e_w = e^T M (M = L^-T, cov = L L^T)
-  const double* pe_ext;     // [npe][7] q_I_B (JPL) p_B_I
+  // pose edges (index j = edge - nimu); measurement rotation per kind:
+  // relative T_Bk_Bk+1 (Hamilton), loop closure q_AB (JPL), absolute q_S_G
+  // (Hamilton, inverse of the measured T_G_S rotation)
+  const double* pe_meas;    // [npe][7] q | p
+  const double* pe_sqrt;    // [npe][36] row-major M with e_w = e^T M (M = L^-1, cov = L L^T)
+  const double* pe_ext;     // [npe][7] q_I_B | p_B_I (relative), q_S_B | p_S_B (absolute)
+  const int32_t* pe_type;   // [npe] MBA_POSE_EDGE_*
+  const int32_t* pe_swi;    // [npe] switch variable, -1 = none
+  const double* pe_swc;     // [npe] switch value of an edge without a variable
+  int64_t nsw;              // switch variables (switchable loop closures)
+  double* sw;               // [nsw] switch state
+  const double* sw_w;       // [nsw] switch prior sqrt information (1 / sigma)
+  const int32_t* sw_e;      // [nsw] edge of each switch
   // Inertial scratch: dt per step, end state per edge, RK4 stage inputs
   // (15 values x 4 stages per step, FP64 or FP32).
   double* ine_scratch;
@@ -91,6 +100,7 @@ struct InertialLin {
   T* r;   // [nedge][15]
   T* Jf;  // [nedge][225] from-keyframe tangent (theta, p, v, b_g, b_a)
   T* Jt;  // [nedge][225] to-keyframe tangent
+  T* Js;  // [npe][6] d r / d switch of the pose edges (the unswitched residual)
 };
 
 // Launchers (kernels_eval.cu).
@@ -109,9 +119,10 @@ cudaError_t launch_visual_linearize_gated(const DevProblem& P, VisualLin<T> out,
 cudaError_t launch_visual_cost_gated(const DevProblem& P, const double* kf_state, const double* lm_p,
                                      double* cost_accum, int* nonfinite, const int* skip_if, cudaStream_t s,
                                      const int* run_if = nullptr);
+// Also evaluates the pose edges, with switch state sw_state (NULL: P.sw).
 cudaError_t launch_inertial_gated(const DevProblem& P, const double* kf_state, InertialLin<double> lin,
                                   double* cost_accum, int* status, const int* skip_if, cudaStream_t s,
-                                  bool f32 = false);
+                                  bool f32 = false, const double* sw_state = nullptr);
 template <typename T>
 cudaError_t launch_gather_visual(const DevProblem& P, VisualLin<T> v, double* r, double* Jl, double* Js, double* Jo,
                                  cudaStream_t s);
@@ -126,8 +137,8 @@ cudaError_t launch_inertial_v2(const DevProblem& P, const double* kf_state, bool
 // Relative pose edges (kernels_pose.cu): residual rows 0-5 and the (theta, p)
 // Jacobian columns of edges [nimu, nedge) into lin (if lin.r), cost into
 // cost_accum.
-cudaError_t launch_pose_edges(const DevProblem& P, const double* kf_state, InertialLin<double> lin,
-                              double* cost_accum, const int* skip_if, cudaStream_t s);
+cudaError_t launch_pose_edges(const DevProblem& P, const double* kf_state, const double* sw_state,
+                              InertialLin<double> lin, double* cost_accum, const int* skip_if, cudaStream_t s);
 cudaError_t launch_inertial_f32(const DevProblem& P, const InertialLin<double>& src, InertialLin<float> dst,
                                 cudaStream_t s);
 // Outlier landmarks at the current state (outlier-rejection-solver.cc:28-103):

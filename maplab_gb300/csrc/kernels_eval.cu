@@ -663,9 +663,10 @@ cudaError_t launch_inertial(const DevProblem& P, const double* kf_state, Inertia
   return launch_inertial_impl(P, kf_state, lin, amb_res, amb_jac, cost_accum, status, nullptr, s);
 }
 cudaError_t launch_inertial_gated(const DevProblem& P, const double* kf_state, InertialLin<double> lin,
-                                  double* cost_accum, int* status, const int* skip_if, cudaStream_t s, bool f32) {
+                                  double* cost_accum, int* status, const int* skip_if, cudaStream_t s, bool f32,
+                                  const double* sw_state) {
   cudaError_t e = launch_inertial_impl(P, kf_state, lin, nullptr, nullptr, cost_accum, status, skip_if, s, f32);
-  if (e == cudaSuccess) e = launch_pose_edges(P, kf_state, lin, cost_accum, skip_if, s);
+  if (e == cudaSuccess) e = launch_pose_edges(P, kf_state, sw_state, lin, cost_accum, skip_if, s);
   return e;
 }
 
@@ -676,6 +677,8 @@ cudaError_t launch_inertial_f32(const DevProblem& P, const InertialLin<double>& 
   k_convert_f32<<<(unsigned)((n1 + 255) / 256), 256, 0, s>>>(src.r, dst.r, n1);
   k_convert_f32<<<(unsigned)((n2 + 255) / 256), 256, 0, s>>>(src.Jf, dst.Jf, n2);
   k_convert_f32<<<(unsigned)((n2 + 255) / 256), 256, 0, s>>>(src.Jt, dst.Jt, n2);
+  const int64_t n3 = 6 * (P.nedge - P.nimu);
+  if (n3 > 0 && src.Js && dst.Js) k_convert_f32<<<(unsigned)((n3 + 255) / 256), 256, 0, s>>>(src.Js, dst.Js, n3);
   return cudaGetLastError();
 }
 

@@ -200,6 +200,29 @@ __global__ void __launch_bounds__(128) k_assemble_inertial(DevProblem P, Inertia
     atomic_add(&L.gc[15 * (int64_t)f + lane], gf);
     atomic_add(&L.gc[15 * (int64_t)t + lane], gt);
   }
+  // Switch variable of a loop closure: its J^T J, gradient (with the prior
+  // r = (1 - s) w, J = -w) and the coupling columns W = J_k^T J_s.
+  if (e >= P.nimu) {
+    const int64_t j = e - P.nimu;
+    const int q = P.pe_swi[j];
+    if (q >= 0) {
+      const T* js = in.Js + 6 * j;
+      if (lane < 15) {
+        T wf = T(0), wt = T(0);
+#pragma unroll
+        for (int m = 0; m < 6; ++m) { wf += Jf[15 * m + lane] * js[m]; wt += Jt[15 * m + lane] * js[m]; }
+        L.swW[30 * q + lane] = wf;
+        L.swW[30 * q + 15 + lane] = wt;
+      } else if (lane == 15) {
+        const double w = P.sw_w[q], rp = (1.0 - P.sw[q]) * w;
+        T h = T(w * w), g = T(-w * rp);
+#pragma unroll
+        for (int m = 0; m < 6; ++m) { h += js[m] * js[m]; g += js[m] * r[m]; }
+        L.swH[q] = h;
+        L.swg[q] = g;
+      }
+    }
+  }
 }
 
 // Jacobi scaling from the unscaled diagonal of J^T J (first linearization
@@ -219,6 +242,11 @@ __global__ void k_scale(DevProblem P, LinearSystem<T> L, ScaleVectors sc, int ja
     const double h = (double)L.Hll[(4 * a) * P.nlm + l];
     sc.slm[j] = jacobi ? 1.0 / (1.0 + sqrt(h > 0.0 ? h : 0.0)) : 1.0;
     L.slm[j] = T(sc.slm[j]);
+  } else if (i < nk + nl + P.nsw) {
+    const int64_t q = i - nk - nl;
+    const double h = (double)L.swH[q];
+    sc.ssw[q] = jacobi ? 1.0 / (1.0 + sqrt(h > 0.0 ? h : 0.0)) : 1.0;
+    L.ssw[q] = T(sc.ssw[q]);
   }
 }
 
@@ -230,8 +258,8 @@ __global__ void __launch_bounds__(kB) k_scale_inplace(DevProblem P, SchurPattern
   if (gated(run_if, skip_if)) return;
   const int64_t NL = P.nlm, NS = S.nslot, NK = P.nkf, NE = P.nedge, NPU = S.npu;
   const int64_t n1 = 9 * NL, n2 = n1 + 3 * NL, n3 = n2 + 18 * NS, n4 = n3 + 225 * NK, n5 = n4 + 36 * NPU,
-                n6 = n5 + 225 * NE, n7 = n6 + 15 * NK;
-  for (int64_t i = blockIdx.x * (int64_t)blockDim.x + threadIdx.x; i < n7; i += (int64_t)gridDim.x * blockDim.x) {
+                n6 = n5 + 225 * NE, n7 = n6 + 15 * NK, n8 = n7 + 2 * P.nsw, n9 = n8 + 30 * P.nsw;
+  for (int64_t i = blockIdx.x * (int64_t)blockDim.x + threadIdx.x; i < n9; i += (int64_t)gridDim.x * blockDim.x) {
     if (i < n1) {
       const int64_t q = i / NL, l = i % NL;
       L.Hll[i] *= L.slm[(q / 3) * NL + l] * L.slm[(q % 3) * NL + l];
@@ -251,9 +279,17 @@ __global__ void __launch_bounds__(kB) k_scale_inplace(DevProblem P, SchurPattern
     } else if (i < n6) {
       const int64_t j = i - n5, ed = j / 225, e = j % 225;
       L.Ebase[j] *= L.skf[15 * (int64_t)P.e_from[ed] + e / 15] * L.skf[15 * (int64_t)P.e_to[ed] + e % 15];
-    } else {
+    } else if (i < n7) {
       const int64_t j = i - n6;
       L.gc[j] *= L.skf[j];
+    } else if (i < n8) {
+      const int64_t j = i - n7, q = j >> 1;
+      if (j & 1) L.swg[q] *= L.ssw[q];
+      else L.swH[q] *= L.ssw[q] * L.ssw[q];
+    } else {
+      const int64_t j = i - n8, q = j / 30, c = j % 30, ed = P.sw_e[q];
+      const int64_t k = c < 15 ? P.e_from[ed] : P.e_to[ed];
+      L.swW[j] *= L.ssw[q] * L.skf[15 * k + c % 15];
     }
   }
 }
@@ -429,6 +465,36 @@ __global__ void __launch_bounds__(kB) k_schur_pairs(SolverLaunch<T> s) {
 }
 
 // Masked tangent dims -> identity rows; mirror SP to the lower orientation.
+// Switch elimination (one warp per switch variable): H = h + damping,
+// SD_ff -= W_f W_f^T / H, SD_tt -= W_t W_t^T / H, SE -= W_f W_t^T / H,
+// rhs += W g / H.  H is inverted in FP64.
+template <typename T>
+__global__ void __launch_bounds__(128) k_schur_switch(SolverLaunch<T> s) {
+  if (s.ctl->terminated) return;
+  const int64_t q = (blockIdx.x * (int64_t)blockDim.x + threadIdx.x) >> 5;
+  const int lane = threadIdx.x & 31;
+  if (q >= s.P.nsw) return;
+  const int64_t e = s.P.sw_e[q], f = s.P.e_from[e], t = s.P.e_to[e];
+  const T radius = T(s.ctl->radius), mn = T(s.prm.min_lm_diagonal), mx = T(s.prm.max_lm_diagonal);
+  const T h = s.L.swH[q];
+  const double H = (double)h + (double)lm_damp_t(h, mn, mx, radius);
+  const T hi = T(1.0 / H);
+  if (lane == 0) s.L.swHi[q] = hi;
+  const T* W = s.L.swW + 30 * q;
+  const T g = s.L.swg[q];
+  for (int a = lane; a < 225; a += 32) {
+    const int r = a / 15, c = a % 15;
+    const T wff = W[r] * W[c] * hi, wtt = W[15 + r] * W[15 + c] * hi, wft = W[r] * W[15 + c] * hi;
+    if (wff != T(0)) atomic_add(&s.L.SD[225 * f + a], -wff);
+    if (wtt != T(0)) atomic_add(&s.L.SD[225 * t + a], -wtt);
+    s.L.SE[225 * e + a] -= wft;  // one switch per edge: a single writer
+  }
+  if (lane < 15) {
+    atomic_add(&s.L.rhs[15 * f + lane], W[lane] * hi * g);
+    atomic_add(&s.L.rhs[15 * t + lane], W[15 + lane] * hi * g);
+  }
+}
+
 template <typename T>
 __global__ void __launch_bounds__(kB) k_finalize_system(SolverLaunch<T> s) {
   if (s.ctl->terminated) return;
@@ -688,6 +754,20 @@ __global__ void __launch_bounds__(kB) k_backsub(SolverLaunch<T> s) {
   }
 }
 
+// Switch back substitution: ds = (-g - W_f^T x_f - W_t^T x_t) / H.
+template <typename T>
+__global__ void __launch_bounds__(kB) k_backsub_switch(SolverLaunch<T> s) {
+  if (s.ctl->terminated) return;
+  const int64_t q = blockIdx.x * (int64_t)blockDim.x + threadIdx.x;
+  if (q >= s.P.nsw) return;
+  const int64_t e = s.P.sw_e[q], f = s.P.e_from[e], t = s.P.e_to[e];
+  const T* W = s.L.swW + 30 * q;
+  T u = -s.L.swg[q];
+#pragma unroll
+  for (int c = 0; c < 15; ++c) u -= W[c] * s.L.x[15 * f + c] + W[15 + c] * s.L.x[15 * t + c];
+  s.L.swx[q] = (double)(u * s.L.swHi[q]);
+}
+
 // Model cost change -u.(r + u/2) with u = J du (unscaled J, du = s dx);
 // u in T, the reduction in FP64.
 template <typename T>
@@ -732,6 +812,7 @@ __global__ void __launch_bounds__(128) k_model_inertial(SolverLaunch<T> s) {
   const int64_t e = (blockIdx.x * (int64_t)blockDim.x + threadIdx.x) >> 5;
   const int lane = threadIdx.x & 31;
   double m = 0.0;
+  const int q = (e < s.P.nedge && e >= s.P.nimu) ? s.P.pe_swi[e - s.P.nimu] : -1;
   if (e < s.P.nedge && lane < 15) {
     const int64_t f = s.P.e_from[e], t = s.P.e_to[e];
     T u = T(0);
@@ -739,8 +820,12 @@ __global__ void __launch_bounds__(128) k_model_inertial(SolverLaunch<T> s) {
     for (int c = 0; c < 15; ++c)
       u += s.ine.Jf[225 * e + 15 * lane + c] * s.L.skf[15 * f + c] * s.L.x[15 * f + c] +
            s.ine.Jt[225 * e + 15 * lane + c] * s.L.skf[15 * t + c] * s.L.x[15 * t + c];
+    if (q >= 0 && lane < 6) u += s.ine.Js[6 * (e - s.P.nimu) + lane] * s.L.ssw[q] * T(s.L.swx[q]);
     const double ud = (double)u;
     m = -ud * ((double)s.ine.r[15 * e + lane] + ud / 2.0);
+  } else if (q >= 0 && lane == 15) {  // switch prior: r = (1 - s) w, J = -w
+    const double w = s.P.sw_w[q], ud = -w * s.sc.ssw[q] * s.L.swx[q];
+    m = -ud * ((1.0 - s.P.sw[q]) * w + ud / 2.0);
   }
   block_add(m, &s.ctl->model_change);
 }
@@ -787,6 +872,13 @@ __global__ void __launch_bounds__(kB) k_retract(SolverLaunch<T> s) {
       if (act) { sn += d * d; xn += x[a] * x[a]; }
     }
     o[3] = 0.0;
+  } else if (i < s.P.nkf + s.P.nlm + s.P.nsw) {
+    // Switch: plain addition projected onto its bounds [0, 1].
+    const int64_t q = i - s.P.nkf - s.P.nlm;
+    const double x = s.P.sw[q], v = fmin(1.0, fmax(0.0, x + s.sc.ssw[q] * s.L.swx[q]));
+    s.sw_cand[q] = v;
+    sn += (v - x) * (v - x);
+    xn += x * x;
   }
   block_add(sn, &s.ctl->step_norm2);
   block_add(xn, &s.ctl->x_norm2);
@@ -861,7 +953,19 @@ __global__ void __launch_bounds__(kB) k_accept(SolverLaunch<T> s, InertialLin<do
   if (!s.ctl->accepted) return;
   const int64_t nk = 16 * s.P.nkf, nl = 4 * s.P.nlm, ne1 = 15 * s.P.nedge, ne2 = 225 * s.P.nedge;
   const int64_t total = nk + nl + ne1 + 2 * ne2;
-  for (int64_t i = blockIdx.x * (int64_t)blockDim.x + threadIdx.x; i < total; i += (int64_t)gridDim.x * blockDim.x) {
+  const int64_t ns = s.P.nsw, nj = 6 * (s.P.nedge - s.P.nimu);
+  for (int64_t i = blockIdx.x * (int64_t)blockDim.x + threadIdx.x; i < total + ns + nj;
+       i += (int64_t)gridDim.x * blockDim.x) {
+    if (i >= total) {
+      const int64_t j = i - total;
+      if (j < ns) {
+        s.P.sw[j] = s.sw_cand[j];
+      } else if (cand.Js) {
+        cur.Js[j - ns] = cand.Js[j - ns];
+        s.ine.Js[j - ns] = T(cand.Js[j - ns]);
+      }
+      continue;
+    }
     if (i < nk) {
       const double v = s.kf_cand[i];
       s.P.kf_state[i] = v;
@@ -948,9 +1052,9 @@ cudaError_t solver_assemble(const SolverLaunch<T>& s, const int* gate, cudaStrea
 
 template <typename T>
 cudaError_t solver_compute_scale(const SolverLaunch<T>& s, int jacobi, cudaStream_t st) {
-  const int64_t n = 15 * s.P.nkf + 3 * s.P.nlm;
+  const int64_t n = 15 * s.P.nkf + 3 * s.P.nlm + s.P.nsw;
   k_scale<T><<<nblk(n, kB), kB, 0, st>>>(s.P, s.L, s.sc, jacobi, nullptr);
-  const int64_t m = 12 * s.P.nlm + 18 * s.S.nslot + 240 * s.P.nkf + 36 * s.S.npu + 225 * s.P.nedge;
+  const int64_t m = 12 * s.P.nlm + 18 * s.S.nslot + 240 * s.P.nkf + 36 * s.S.npu + 225 * s.P.nedge + 32 * s.P.nsw;
   k_scale_inplace<T><<<gridcap(m), kB, 0, st>>>(s.P, s.S, s.L, nullptr, nullptr);
   return cudaGetLastError();
 }
@@ -962,6 +1066,7 @@ cudaError_t solver_build_reduced(const SolverLaunch<T>& s, cudaStream_t st) {
   if (s.P.nlm) k_schur_lm<T><<<nblk(s.P.nlm, kB), kB, 0, st>>>(s);
   if (s.S.nslot) k_schur_slot<T><<<nblk(s.S.nslot, kB), kB, 0, st>>>(s);
   if (s.S.nchunk) k_schur_pairs<T><<<nblk(s.S.nchunk, kB), kB, 0, st>>>(s);
+  if (s.P.nsw) k_schur_switch<T><<<nblk(32 * s.P.nsw, 128), 128, 0, st>>>(s);
   k_finalize_system<T><<<gridcap(nsys), kB, 0, st>>>(s);
   k_block_jacobi<T><<<nblk(s.P.nkf, 64), 64, 0, st>>>(s);
   if (s.precond != MBA_PRECOND_BLOCK_JACOBI) {
@@ -1002,9 +1107,10 @@ cudaError_t solver_step(const SolverLaunch<T>& s, cudaStream_t st) {
     }
   }
   if (s.P.nlm) k_backsub<T><<<nblk(s.P.nlm, kB), kB, 0, st>>>(s);
+  if (s.P.nsw) k_backsub_switch<T><<<nblk(s.P.nsw, kB), kB, 0, st>>>(s);
   if (s.P.nobs) k_model_visual<T><<<nblk(s.P.nobs, kB), kB, 0, st>>>(s);
   if (s.P.nedge) k_model_inertial<T><<<nblk(32 * s.P.nedge, 128), 128, 0, st>>>(s);
-  k_retract<T><<<nblk(s.P.nkf + s.P.nlm, kB), kB, 0, st>>>(s);
+  k_retract<T><<<nblk(s.P.nkf + s.P.nlm + s.P.nsw, kB), kB, 0, st>>>(s);
   return cudaGetLastError();
 }
 
@@ -1019,14 +1125,14 @@ cudaError_t solver_evaluate_candidate(const SolverLaunch<T>& s, InertialLin<doub
   if (e != cudaSuccess) return e;
   // Mixed path: Phi / Q propagated in FP32 (state, Cholesky, residual FP64).
   return launch_inertial_gated(s.P, s.kf_cand, ine_cand, &s.ctl->cost_cand_ine, &s.ctl->inertial_status,
-                               &s.ctl->terminated, st, sizeof(T) == 4);
+                               &s.ctl->terminated, st, sizeof(T) == 4, s.sw_cand);
 }
 
 template <typename T>
 cudaError_t solver_decide_and_accept(const SolverLaunch<T>& s, InertialLin<double> ine_cand,
                                      InertialLin<double> ine_cur, cudaStream_t st) {
   k_decide<<<1, 1, 0, st>>>(s.ctl, s.prm, s.log);
-  const int64_t total = 16 * s.P.nkf + 4 * s.P.nlm + 465 * s.P.nedge;
+  const int64_t total = 16 * s.P.nkf + 4 * s.P.nlm + 465 * s.P.nedge + s.P.nsw + 6 * (s.P.nedge - s.P.nimu);
   k_accept<T><<<gridcap(total), kB, 0, st>>>(s, ine_cand, ine_cur);
   return cudaGetLastError();
 }
@@ -1071,9 +1177,9 @@ cudaError_t solver_reject_and_restart(const SolverLaunch<T>& s, int use_reprojec
   if (s.S.npu) k_zero<T><<<gridcap(36 * s.S.npu), kB, 0, st>>>(s.L.Pbase, 36 * s.S.npu, run, nullptr);
   if (s.P.nlm) k_assemble_lm<T><<<nblk(s.P.nlm, kB), kB, 0, st>>>(s.P, s.S, s.vis, s.L, run, nullptr);
   if (s.P.nedge) k_assemble_inertial<T><<<nblk(32 * s.P.nedge, 128), 128, 0, st>>>(s.P, s.ine, s.L, run, nullptr);
-  const int64_t n = 15 * s.P.nkf + 3 * s.P.nlm;
+  const int64_t n = 15 * s.P.nkf + 3 * s.P.nlm + s.P.nsw;
   k_scale<T><<<nblk(n, kB), kB, 0, st>>>(s.P, s.L, s.sc, jacobi, run);
-  const int64_t m = 12 * s.P.nlm + 18 * s.S.nslot + 240 * s.P.nkf + 36 * s.S.npu + 225 * s.P.nedge;
+  const int64_t m = 12 * s.P.nlm + 18 * s.S.nslot + 240 * s.P.nkf + 36 * s.S.npu + 225 * s.P.nedge + 32 * s.P.nsw;
   k_scale_inplace<T><<<gridcap(m), kB, 0, st>>>(s.P, s.S, s.L, run, nullptr);
   return cudaGetLastError();
 }

@@ -159,6 +159,7 @@ struct mba_handle {
   double* lm_cand = nullptr;
   float* kf_cand_f = nullptr;
   float* lm_cand_f = nullptr;
+  double* sw_cand = nullptr;  // [nsw] candidate switch variables
   double* scratch = nullptr;  // [4] cost accumulators
   int* iscratch = nullptr;    // [4] flags
   // staging in the caller's layout (lazily allocated)
@@ -252,6 +253,7 @@ mba_status ensure_solver_buffers(mba_handle* h, SolverBuffers<T>& b) {
   b.ine.r = A.alloc<T>(15 * NE);
   b.ine.Jf = A.alloc<T>(225 * NE);
   b.ine.Jt = A.alloc<T>(225 * NE);
+  b.ine.Js = A.alloc<T>(6 * (NE - P.nimu));
   LinearSystem<T>& L = b.L;
   L.Hll = A.alloc<T>(9 * NL);
   L.gl = A.alloc<T>(3 * NL);
@@ -276,6 +278,12 @@ mba_status ensure_solver_buffers(mba_handle* h, SolverBuffers<T>& b) {
   L.dl = A.alloc<double>(3 * NL);
   L.skf = A.alloc<T>(15 * NK);
   L.slm = A.alloc<T>(3 * NL);
+  L.swH = A.alloc<T>(P.nsw);
+  L.swg = A.alloc<T>(P.nsw);
+  L.swW = A.alloc<T>(30 * P.nsw);
+  L.swHi = A.alloc<T>(P.nsw);
+  L.swx = A.alloc<double>(P.nsw);
+  L.ssw = A.alloc<T>(P.nsw);
   if (A.err != cudaSuccess) return MBA_ERR_CUDA;
   b.ready = true;
   return MBA_OK;
@@ -351,8 +359,12 @@ mba_status ensure_common_solver(mba_handle* h, int capacity) {
     h->ine_cand.r = A.alloc<double>(15 * NE);
     h->ine_cand.Jf = A.alloc<double>(225 * NE);
     h->ine_cand.Jt = A.alloc<double>(225 * NE);
+    h->ine_cur.Js = A.alloc<double>(6 * (NE - P.nimu));
+    h->ine_cand.Js = A.alloc<double>(6 * (NE - P.nimu));
     h->sc.skf = A.alloc<double>(15 * P.nkf);
     h->sc.slm = A.alloc<double>(3 * P.nlm);
+    h->sc.ssw = A.alloc<double>(P.nsw);
+    h->sw_cand = A.alloc<double>(P.nsw);
     h->ctl = A.alloc<LmControl>(1);
     h->kf_cand = A.alloc<double>(16 * P.nkf);
     h->lm_cand = A.alloc<double>(4 * P.nlm);
@@ -405,6 +417,7 @@ SolverLaunch<T> make_launch(mba_handle* h, SolverBuffers<T>& b, const mba_solver
   s.lm_cand = h->lm_cand;
   s.kf_cand_f = sizeof(T) == 4 ? h->kf_cand_f : nullptr;
   s.lm_cand_f = sizeof(T) == 4 ? h->lm_cand_f : nullptr;
+  s.sw_cand = h->sw_cand;
   s.C = b.C;
   s.precond = (o.preconditioner == MBA_PRECOND_CHAIN || o.preconditioner == MBA_PRECOND_LEARNED) && b.chain_ready
                   ? o.preconditioner : MBA_PRECOND_BLOCK_JACOBI;
@@ -810,27 +823,56 @@ mba_status mba_create(const mba_problem_desc* d, int32_t device, mba_handle** ou
       for (int64_t j = 6 * a; j < 6 * b; ++j) if (!std::isfinite(d->imu_acc_gyro[j])) return MBA_ERR_NON_FINITE;
     }
   }
-  // Edges: the IMU edges, then the relative pose edges (square-root
-  // information of each covariance computed here, as the error term's
-  // constructor does).
-  std::vector<int32_t> e_from(NE), e_to(NE);
-  std::vector<double> pe_meas(7 * NPE), pe_sqrt(36 * NPE), pe_ext(7 * NPE);
+  // Edges: the IMU edges, then the pose edges (square-root information of
+  // each covariance computed here, as the error terms' constructors do).
+  // Loop closures keep the measured rotation as JPL coefficients (the
+  // Hamilton inverse, augment-loopclosure.cc:44-49), absolute terms the
+  // inverse measured rotation q_S_G (block-pose-prior-error-term-v2.cc:13-16);
+  // both inverses as Eigen computes them (conjugate / squared norm).  An
+  // absolute term is stored as an edge from its keyframe to itself with a
+  // zero to-block.
+  std::vector<int32_t> e_from(NE), e_to(NE), pe_type(NPE), pe_swi(NPE, -1), sw_e;
+  std::vector<double> pe_meas(7 * NPE), pe_sqrt(36 * NPE), pe_ext(7 * NPE), pe_swc(NPE, 1.0), sw0, sw_w;
   if (NIMU > 0) {
     std::copy(d->edge_from, d->edge_from + NIMU, e_from.begin());
     std::copy(d->edge_to, d->edge_to + NIMU, e_to.begin());
   }
   for (int64_t j = 0; j < NPE; ++j) {
-    const int32_t f = d->pose_edge_from[j], t = d->pose_edge_to[j];
-    if (f < 0 || f >= NK || t < 0 || t >= NK || f == t) return MBA_ERR_OUT_OF_RANGE_INDEX;
+    const int32_t type = d->pose_edge_type ? d->pose_edge_type[j] : MBA_POSE_EDGE_RELATIVE;
+    if (type < MBA_POSE_EDGE_RELATIVE || type > MBA_POSE_EDGE_ABSOLUTE) return MBA_ERR_INVALID_ARG;
+    const int32_t f = d->pose_edge_from[j];
+    const int32_t t = type == MBA_POSE_EDGE_ABSOLUTE ? f : d->pose_edge_to[j];
+    if (f < 0 || f >= NK || t < 0 || t >= NK) return MBA_ERR_OUT_OF_RANGE_INDEX;
+    if (type != MBA_POSE_EDGE_ABSOLUTE && f == t) return MBA_ERR_OUT_OF_RANGE_INDEX;
     const double* T = d->pose_edge_T_Bk_Bkp1 + 7 * j;
     const double* X = d->pose_edge_q_I_B_p_B_I + 7 * j;
     const double* C = d->pose_edge_covariance + 36 * j;
     for (int a = 0; a < 7; ++a) if (!std::isfinite(T[a]) || !std::isfinite(X[a])) return MBA_ERR_NON_FINITE;
     for (int a = 0; a < 36; ++a) if (!std::isfinite(C[a])) return MBA_ERR_NON_FINITE;
-    if (!quat_ok(T) || !quat_ok(X)) return MBA_ERR_INVALID_ARG;
+    if (!quat_ok(T)) return MBA_ERR_INVALID_ARG;
+    if (type != MBA_POSE_EDGE_LOOP_CLOSURE && !quat_ok(X)) return MBA_ERR_INVALID_ARG;
     if (!pose_edge_sqrt_information(C, &pe_sqrt[36 * j])) return MBA_ERR_NOT_SPD;
     std::copy(T, T + 7, &pe_meas[7 * j]);
+    if (type != MBA_POSE_EDGE_RELATIVE) {
+      const double n2 = T[0] * T[0] + T[1] * T[1] + T[2] * T[2] + T[3] * T[3];
+      for (int a = 0; a < 3; ++a) pe_meas[7 * j + a] = -T[a] / n2;
+      pe_meas[7 * j + 3] = T[3] / n2;
+    }
     std::copy(X, X + 7, &pe_ext[7 * j]);
+    pe_type[j] = type;
+    if (type == MBA_POSE_EDGE_LOOP_CLOSURE) {
+      const double s0 = d->pose_edge_switch ? d->pose_edge_switch[j] : 1.0;
+      const double var = d->pose_edge_switch_variance ? d->pose_edge_switch_variance[j] : 0.0;
+      if (!std::isfinite(s0) || !std::isfinite(var)) return MBA_ERR_NON_FINITE;
+      if (s0 < 0.0 || s0 > 1.0 || var < 0.0) return MBA_ERR_INVALID_ARG;  // SwitchPriorErrorTerm CHECKs
+      pe_swc[j] = s0;
+      if (var > 0.0) {
+        pe_swi[j] = (int32_t)sw0.size();
+        sw0.push_back(s0);
+        sw_w.push_back(std::sqrt(1.0 / var));
+        sw_e.push_back((int32_t)(NIMU + j));
+      }
+    }
     e_from[NIMU + j] = f;
     e_to[NIMU + j] = t;
   }
@@ -1007,12 +1049,15 @@ mba_status mba_create(const mba_problem_desc* d, int32_t device, mba_handle** ou
     }
   }
   std::vector<int64_t> kfe_off(NK + 1, 0);
-  for (int64_t e = 0; e < NE; ++e) { kfe_off[e_from[e] + 1]++; kfe_off[e_to[e] + 1]++; }
+  // Per-keyframe edge lists (couplings; an absolute term couples nothing).
+  for (int64_t e = 0; e < NE; ++e)
+    if (e_from[e] != e_to[e]) { kfe_off[e_from[e] + 1]++; kfe_off[e_to[e] + 1]++; }
   for (int64_t k = 0; k < NK; ++k) kfe_off[k + 1] += kfe_off[k];
-  std::vector<int32_t> kfe(2 * NE);
+  std::vector<int32_t> kfe(kfe_off[NK]);
   {
     std::vector<int64_t> fill(kfe_off.begin(), kfe_off.end() - 1);
     for (int64_t e = 0; e < NE; ++e) {
+      if (e_from[e] == e_to[e]) continue;
       kfe[fill[e_from[e]]++] = (int32_t)(e + 1);
       kfe[fill[e_to[e]]++] = (int32_t)(-(e + 1));
     }
@@ -1035,8 +1080,10 @@ mba_status mba_create(const mba_problem_desc* d, int32_t device, mba_handle** ou
     nbr_off[k + 1] = (int64_t)nbr.size();
   }
 
-  // ---- keyframe chains (chain preconditioner).  With inertial edges a chain
-  // follows from -> to; without, the keyframes of a mission in index order.
+  // ---- keyframe chains (chain preconditioner).  With edges that couple two
+  // keyframes (IMU, odometry, loop closures) a chain follows from -> to, the
+  // first such edge of a keyframe; without, the keyframes of a mission in
+  // index order.
   // All chains are laid end to end in one sequence of positions; position p
   // couples to p - 1 only inside a chain (link_edge / link_blk give the
   // blocks of that coupling, -1 where absent).
@@ -1047,6 +1094,7 @@ mba_status mba_create(const mba_problem_desc* d, int32_t device, mba_handle** ou
     std::vector<char> has_prev(NK, 0), seen(NK, 0), start(NK, 0);
     for (int64_t e = 0; e < NE; ++e) {
       const int32_t f = e_from[e], t = e_to[e];
+      if (f == t) continue;
       if (next[f] < 0 && !has_prev[t]) { next[f] = t; next_e[f] = (int32_t)e; has_prev[t] = 1; }
     }
     auto follow = [&](int32_t k) {
@@ -1057,7 +1105,7 @@ mba_status mba_create(const mba_problem_desc* d, int32_t device, mba_handle** ou
         k = next[k];
       }
     };
-    if (NE > 0) {
+    if (kfe_off[NK] > 0) {
       for (int32_t k = 0; k < NK; ++k) if (!has_prev[k] && !seen[k]) follow(k);
       for (int32_t k = 0; k < NK; ++k) if (!seen[k]) follow(k);
     } else {
@@ -1073,7 +1121,7 @@ mba_status mba_create(const mba_problem_desc* d, int32_t device, mba_handle** ou
     for (int64_t q = 1; q < NK; ++q) {
       const int32_t a = chain_perm[q - 1], b = chain_perm[q];
       if (start[b]) continue;
-      if (NE > 0 && next[a] == b) link_edge[q] = next_e[a];  // SE[e] is the (a, b) block
+      if (next[a] == b) link_edge[q] = next_e[a];  // SE[e] is the (a, b) block
       const int32_t blk = pm.find(a, b);
       if (blk >= 0) link_blk[q] = (b < a) ? blk : (int32_t)(npu + blk);  // SP block with rows b, columns a
     }
@@ -1144,6 +1192,13 @@ mba_status mba_create(const mba_problem_desc* d, int32_t device, mba_handle** ou
   P.pe_meas = A.upload(pe_meas, st);
   P.pe_sqrt = A.upload(pe_sqrt, st);
   P.pe_ext = A.upload(pe_ext, st);
+  P.pe_type = A.upload(pe_type, st);
+  P.pe_swi = A.upload(pe_swi, st);
+  P.pe_swc = A.upload(pe_swc, st);
+  P.nsw = (int64_t)sw0.size();
+  P.sw = A.upload(sw0, st);
+  P.sw_w = A.upload(sw_w, st);
+  P.sw_e = A.upload(sw_e, st);
   {
     // FP32 mirrors for the FP32 evaluation kernel.
     std::vector<float> uvf(2 * N), sinvf(N), hubf(N), lmf(4 * NL, 0.f), kff(8 * NK, 0.f), misf(8 * NM, 0.f);
@@ -1300,7 +1355,7 @@ mba_status mba_linearize_pose_edges(mba_handle* h, double* r, double* J_from, do
   lin.Jf = tmp.alloc<double>(225 * h->P.nedge);
   lin.Jt = tmp.alloc<double>(225 * h->P.nedge);
   cudaError_t e = tmp.err;
-  if (e == cudaSuccess) e = launch_pose_edges(h->P, h->P.kf_state, lin, nullptr, nullptr, h->stream);
+  if (e == cudaSuccess) e = launch_pose_edges(h->P, h->P.kf_state, nullptr, lin, nullptr, nullptr, h->stream);
   std::vector<double> hr(15 * NPE), hf(225 * NPE), ht(225 * NPE);
   if (e == cudaSuccess)
     e = cudaMemcpyAsync(hr.data(), lin.r + 15 * NIMU, sizeof(double) * 15 * NPE, cudaMemcpyDeviceToHost, h->stream);
@@ -1322,6 +1377,59 @@ mba_status mba_linearize_pose_edges(mba_handle* h, double* r, double* J_from, do
   return MBA_OK;
 }
 
+mba_status mba_relaxation_flags(const mba_problem_desc* d, uint32_t* kf_flags_out, uint8_t* lm_constant_out) {
+  if (!d || !kf_flags_out || (d->num_landmarks > 0 && !lm_constant_out) || d->num_keyframes <= 0 ||
+      d->num_landmarks < 0)
+    return MBA_ERR_INVALID_ARG;
+  // options.fix_velocity / fix_gyro_bias / fix_accel_bias / fix_landmark_positions = true
+  const uint32_t fixes = MBA_KF_VELOCITY_CONSTANT | MBA_KF_GYRO_BIAS_CONSTANT | MBA_KF_ACCEL_BIAS_CONSTANT;
+  for (int64_t k = 0; k < d->num_keyframes; ++k) kf_flags_out[k] = (d->kf_flags ? d->kf_flags[k] : 0u) | fixes;
+  for (int64_t l = 0; l < d->num_landmarks; ++l) lm_constant_out[l] = 1;
+  return MBA_OK;
+}
+
+mba_status mba_read_switch_variables(mba_handle* h, double* s) {
+  if (!h || !s) return MBA_ERR_INVALID_ARG;
+  cudaSetDevice(h->device);
+  const int64_t NPE = h->P.nedge - h->P.nimu;
+  if (NPE == 0) return MBA_OK;
+  std::vector<int32_t> swi(NPE);
+  std::vector<double> swc(NPE), sw(h->P.nsw);
+  cudaError_t e = cudaMemcpyAsync(swi.data(), h->P.pe_swi, sizeof(int32_t) * NPE, cudaMemcpyDeviceToHost, h->stream);
+  if (e == cudaSuccess) e = cudaMemcpyAsync(swc.data(), h->P.pe_swc, sizeof(double) * NPE, cudaMemcpyDeviceToHost, h->stream);
+  if (e == cudaSuccess && h->P.nsw)
+    e = cudaMemcpyAsync(sw.data(), h->P.sw, sizeof(double) * h->P.nsw, cudaMemcpyDeviceToHost, h->stream);
+  if (e == cudaSuccess) e = cudaStreamSynchronize(h->stream);
+  if (e != cudaSuccess) return MBA_ERR_CUDA;
+  for (int64_t j = 0; j < NPE; ++j) s[j] = swi[j] >= 0 ? sw[swi[j]] : swc[j];
+  return MBA_OK;
+}
+
+mba_status mba_write_switch_variables(mba_handle* h, const double* s) {
+  if (!h || !s) return MBA_ERR_INVALID_ARG;
+  cudaSetDevice(h->device);
+  const int64_t NPE = h->P.nedge - h->P.nimu;
+  if (NPE == 0) return MBA_OK;
+  for (int64_t j = 0; j < NPE; ++j)
+    if (!(s[j] >= 0.0 && s[j] <= 1.0)) return MBA_ERR_INVALID_ARG;
+  std::vector<int32_t> swi(NPE);
+  cudaError_t e = cudaMemcpyAsync(swi.data(), h->P.pe_swi, sizeof(int32_t) * NPE, cudaMemcpyDeviceToHost, h->stream);
+  if (e == cudaSuccess) e = cudaStreamSynchronize(h->stream);
+  if (e != cudaSuccess) return MBA_ERR_CUDA;
+  std::vector<double> sw(h->P.nsw), swc(NPE);
+  for (int64_t j = 0; j < NPE; ++j) {
+    swc[j] = s[j];
+    if (swi[j] >= 0) sw[swi[j]] = s[j];
+  }
+  // pe_swc is read-only for the kernels; it is device memory owned by the handle.
+  e = cudaMemcpyAsync(const_cast<double*>(h->P.pe_swc), swc.data(), sizeof(double) * NPE, cudaMemcpyHostToDevice,
+                      h->stream);
+  if (e == cudaSuccess && h->P.nsw)
+    e = cudaMemcpyAsync(h->P.sw, sw.data(), sizeof(double) * h->P.nsw, cudaMemcpyHostToDevice, h->stream);
+  if (e == cudaSuccess) e = cudaStreamSynchronize(h->stream);
+  return e == cudaSuccess ? MBA_OK : MBA_ERR_CUDA;
+}
+
 mba_status mba_linearize_visual(mba_handle* h, int32_t precision, double* r, double* Jl, double* Js, double* Jo) {
   if (!h) return MBA_ERR_INVALID_ARG;
   cudaSetDevice(h->device);
@@ -1341,7 +1449,7 @@ mba_status mba_cost(mba_handle* h, int32_t precision, double* cost) {
   if (e == cudaSuccess) e = launch_visual_cost(h->P, h->P.kf_state, h->P.lm_p, h->scratch, h->iscratch, st);
   InertialLin<double> none{};
   if (e == cudaSuccess) e = launch_inertial(h->P, h->P.kf_state, none, nullptr, nullptr, h->scratch, h->iscratch + 1, st);
-  if (e == cudaSuccess) e = launch_pose_edges(h->P, h->P.kf_state, none, h->scratch, nullptr, st);
+  if (e == cudaSuccess) e = launch_pose_edges(h->P, h->P.kf_state, nullptr, none, h->scratch, nullptr, st);
   int flags[2] = {0, 0};
   if (e == cudaSuccess) e = cudaMemcpyAsync(cost, h->scratch, sizeof(double), cudaMemcpyDeviceToHost, st);
   if (e == cudaSuccess) e = cudaMemcpyAsync(flags, h->iscratch, 2 * sizeof(int), cudaMemcpyDeviceToHost, st);

@@ -116,6 +116,16 @@ struct LinearSystem {
   double* dl;    // [3][nlm] scaled landmark step
   T* skf;        // [nkf*15] Jacobi scale (T copy)
   T* slm;        // [3][nlm]
+  // Switch variables, eliminated like landmarks (1-dim blocks, each touching
+  // one edge's two keyframes): J^T J and gradient (scaled in place), W_f | W_t
+  // (scaled Jacobian columns of the keyframes times the switch column), the
+  // damped inverse, the scaled step.
+  T* swH;        // [nsw]
+  T* swg;        // [nsw]
+  T* swW;        // [nsw][30]
+  T* swHi;       // [nsw]
+  double* swx;   // [nsw]
+  T* ssw;        // [nsw] Jacobi scale (T copy)
 };
 
 // Block cyclic reduction of the chain matrix T (block-tridiagonal in chain
@@ -140,6 +150,7 @@ struct ChainSystem {
 struct ScaleVectors {
   double* skf;  // [nkf*15]
   double* slm;  // [3][nlm]
+  double* ssw;  // [nsw]
 };
 
 template <typename T>
@@ -157,6 +168,7 @@ struct SolverLaunch {
   double* lm_cand;             // [nlm][4]
   float* kf_cand_f;            // [nkf][8] FP32 pose copies of the candidate (mixed path)
   float* lm_cand_f;            // [nlm][4]
+  double* sw_cand;             // [nsw] candidate switch variables
   ChainSystem<T> C;
   int32_t precond = 0;         // MBA_PRECOND_*
   GnnGraph gg{};               // learned preconditioner (precond == MBA_PRECOND_LEARNED)

@@ -125,6 +125,50 @@ void hamiltonPerturb(double* T, const double* d) {
   hMul(T, dq, q);
   for (int i = 0; i < 4; ++i) T[i] = q[i];
 }
+// JPL quaternion product (left-multiplication matrix of a times b),
+// normalized with w >= 0.
+void jplProd(const double* a, const double* b, double* o) {
+  double p[4];
+  p[0] = a[3] * b[0] + a[2] * b[1] - a[1] * b[2] + a[0] * b[3];
+  p[1] = -a[2] * b[0] + a[3] * b[1] + a[0] * b[2] + a[1] * b[3];
+  p[2] = a[1] * b[0] - a[0] * b[1] + a[3] * b[2] + a[2] * b[3];
+  p[3] = -a[0] * b[0] - a[1] * b[1] - a[2] * b[2] + a[3] * b[3];
+  const double n = std::sqrt(p[0] * p[0] + p[1] * p[1] + p[2] * p[2] + p[3] * p[3]);
+  const double sgn = p[3] < 0 ? -1.0 : 1.0;
+  for (int i = 0; i < 4; ++i) o[i] = sgn * p[i] / n;
+}
+// Relative pose T_A_B (Hamilton q | p) of vertex blocks xa, xb (q_I_M JPL |
+// p_M_I) in missions with baseframes ba, bb (q_G_M JPL | p_G_M): the
+// measurement model of LoopClosureEdgeErrorTerm.
+void loopClosureFromStates(const double* ba, const double* xa, const double* bb, const double* xb, double* T) {
+  double qi[4], qGA[4], qGB[4], qAB[4], pGA[3], pGB[3];
+  qi[0] = -xa[0]; qi[1] = -xa[1]; qi[2] = -xa[2]; qi[3] = xa[3];
+  jplProd(ba, qi, qGA);
+  qi[0] = -xb[0]; qi[1] = -xb[1]; qi[2] = -xb[2]; qi[3] = xb[3];
+  jplProd(bb, qi, qGB);
+  mv(jplR(ba), xa + 4, pGA);
+  mv(jplR(bb), xb + 4, pGB);
+  for (int i = 0; i < 3; ++i) { pGA[i] += ba[4 + i]; pGB[i] += bb[4 + i]; }
+  qi[0] = -qGA[0]; qi[1] = -qGA[1]; qi[2] = -qGA[2]; qi[3] = qGA[3];
+  jplProd(qi, qGB, qAB);
+  const double d[3] = {pGB[0] - pGA[0], pGB[1] - pGA[1], pGB[2] - pGA[2]};
+  mv(jplR(qi), d, T + 4);
+  T[0] = -qAB[0]; T[1] = -qAB[1]; T[2] = -qAB[2]; T[3] = qAB[3];  // Hamilton coefficients
+}
+// Sensor pose T_G_S (Hamilton q | p) of vertex block x in a mission with
+// baseframe b, sensor extrinsics ext = q_S_B (JPL) | p_S_B: the measurement
+// model of BlockPosePriorErrorTermV2.
+void absolutePoseFromState(const double* b, const double* x, const double* ext, double* T) {
+  const Mat3 RGM = jplR(b), RMB = tr(jplR(x)), RBS = tr(jplR(ext));
+  const Mat3 A = mul(RGM, RMB), RGS = mul(A, RBS);
+  double pBS[3], a[3], c[3];
+  mv(RBS, ext + 4, pBS);
+  for (int i = 0; i < 3; ++i) pBS[i] = -pBS[i];
+  mv(A, pBS, a);
+  mv(RGM, x + 4, c);
+  for (int i = 0; i < 3; ++i) T[4 + i] = a[i] + c[i] + b[4 + i];
+  quatFromJplR(tr(RGS), T);  // Hamilton quaternion of R_G_S
+}
 // JPL box-plus used only to perturb initial orientations.
 void jplPlus(const double* q, const double* d, double* out) {
   const double th = std::sqrt(d[0] * d[0] + d[1] * d[1] + d[2] * d[2]);
@@ -187,8 +231,8 @@ struct mba_synth_map {
   std::vector<int32_t> e_from, e_to;
   std::vector<int64_t> e_off, ts;
   std::vector<double> imu;
-  std::vector<int32_t> pe_from, pe_to;
-  std::vector<double> pe_meas, pe_cov, pe_ext;
+  std::vector<int32_t> pe_from, pe_to, pe_type;
+  std::vector<double> pe_meas, pe_cov, pe_ext, pe_sw, pe_swvar;
   double gravity = 9.81;
 };
 
@@ -218,6 +262,11 @@ void mba_synth_default_config(mba_synth_config* c) {
   c->pose_edges = 0;
   c->pose_edge_sigma_p = 0.02;
   c->pose_edge_sigma_q = 0.005;
+  c->loop_closure_sigma_p = 0.05;
+  c->loop_closure_sigma_q = 0.01;
+  c->loop_closure_switch_variance = 1e-2;
+  c->absolute_pose_sigma_p = 0.1;
+  c->absolute_pose_sigma_q = 0.02;
   c->include_inertial = 1;
   c->co_registered = 1;
 }
@@ -611,6 +660,59 @@ mba_status mba_synth_generate(const mba_synth_config* cfg, mba_synth_map** out) 
             const double sg = r < 3 ? cfg->pose_edge_sigma_p : cfg->pose_edge_sigma_q;
             M->pe_cov.push_back(r == c ? sg * sg : 0.0);
           }
+        M->pe_type.push_back(MBA_POSE_EDGE_RELATIVE);
+        M->pe_sw.push_back(1.0);
+        M->pe_swvar.push_back(0.0);
+      }
+  }
+  auto push_measurement = [&](int64_t a, int64_t b, int type, double* T, double sp, double sq, double nsp, double nsq,
+                              const double* ext) {
+    const double dq[3] = {nsq * rng.normal(), nsq * rng.normal(), nsq * rng.normal()};
+    hamiltonPerturb(T, dq);
+    for (int i = 0; i < 3; ++i) T[4 + i] += nsp * rng.normal();
+    M->pe_from.push_back((int32_t)a);
+    M->pe_to.push_back((int32_t)b);
+    for (int i = 0; i < 7; ++i) M->pe_meas.push_back(T[i]);
+    for (int i = 0; i < 7; ++i) M->pe_ext.push_back(ext[i]);
+    for (int r = 0; r < 6; ++r)
+      for (int c = 0; c < 6; ++c) {
+        const double sg = r < 3 ? sp : sq;
+        M->pe_cov.push_back(r == c ? sg * sg : 0.0);
+      }
+    M->pe_type.push_back(type);
+    M->pe_sw.push_back(1.0);
+    M->pe_swvar.push_back(type == MBA_POSE_EDGE_LOOP_CLOSURE ? cfg->loop_closure_switch_variance : 0.0);
+  };
+  // Loop closures (true relative pose plus noise; a fraction replaced by a
+  // grossly wrong transform) and absolute 6-DoF measurements.
+  if (cfg->loop_closure_stride > 0) {
+    static const double kNone[7] = {0.0, 0.0, 0.0, 1.0, 0.0, 0.0, 0.0};
+    const int64_t lap = std::max<int64_t>(1, std::llround(cfg->keyframes_per_lap));
+    auto add_lc = [&](int64_t a, int64_t b) {
+      const bool same = M->kf_mis[a] == M->kf_mis[b];
+      const double* ba = same ? kNone : &M->mis[7 * M->kf_mis[a]];
+      const double* bb = same ? kNone : &M->mis[7 * M->kf_mis[b]];
+      double T[7];
+      loopClosureFromStates(ba, &M->kf_x_true[7 * a], bb, &M->kf_x_true[7 * b], T);
+      const bool outlier = rng.uniform() < cfg->loop_closure_outlier_fraction;
+      push_measurement(a, b, MBA_POSE_EDGE_LOOP_CLOSURE, T, cfg->loop_closure_sigma_p, cfg->loop_closure_sigma_q,
+                       outlier ? 3.0 : cfg->loop_closure_sigma_p, outlier ? 0.5 : cfg->loop_closure_sigma_q, kNone);
+    };
+    for (int m = 0; m < nm; ++m)
+      for (int64_t k = 0; k + lap < nk[m]; k += cfg->loop_closure_stride) add_lc(kf0[m] + k, kf0[m] + k + lap);
+    for (int m = 0; m + 1 < nm; ++m)
+      for (int64_t k = 0; k < std::min<int64_t>(nk[m], nk[m + 1]); k += cfg->loop_closure_stride)
+        add_lc(kf0[m] + k, kf0[m + 1] + k);
+  }
+  if (cfg->absolute_pose_stride > 0) {
+    const double ext[7] = {std::sin(0.05), 0.0, 0.0, std::cos(0.05), 0.2, 0.0, -0.1};  // q_S_B | p_S_B
+    for (int m = 0; m < nm; ++m)
+      for (int64_t k = 0; k < nk[m]; k += cfg->absolute_pose_stride) {
+        const int64_t K = kf0[m] + k;
+        double T[7];
+        absolutePoseFromState(&M->mis[7 * m], &M->kf_x_true[7 * K], ext, T);
+        push_measurement(K, K, MBA_POSE_EDGE_ABSOLUTE, T, cfg->absolute_pose_sigma_p, cfg->absolute_pose_sigma_q,
+                         cfg->absolute_pose_sigma_p, cfg->absolute_pose_sigma_q, ext);
       }
   }
   *out = M.release();
@@ -636,6 +738,9 @@ mba_status mba_synth_describe(const mba_synth_map* M, mba_problem_desc* d) {
   d->pose_edge_from = M->pe_from.data(); d->pose_edge_to = M->pe_to.data();
   d->pose_edge_T_Bk_Bkp1 = M->pe_meas.data(); d->pose_edge_covariance = M->pe_cov.data();
   d->pose_edge_q_I_B_p_B_I = M->pe_ext.data();
+  d->pose_edge_type = M->pe_type.data();
+  d->pose_edge_switch = M->pe_sw.data();
+  d->pose_edge_switch_variance = M->pe_swvar.data();
   d->gyro_noise_sigma = M->cfg.gyro_noise; d->gyro_bias_sigma = M->cfg.gyro_bias_rw;
   d->acc_noise_sigma = M->cfg.acc_noise; d->acc_bias_sigma = M->cfg.acc_bias_rw;
   d->gravity_magnitude = M->gravity;

@@ -122,7 +122,8 @@ class SyntheticMap:
             "imu_timestamp_ns": (d.num_imu_samples,), "imu_acc_gyro": (d.num_imu_samples, 6),
             "pose_edge_from": (d.num_pose_edges,), "pose_edge_to": (d.num_pose_edges,),
             "pose_edge_T_Bk_Bkp1": (d.num_pose_edges, 7), "pose_edge_covariance": (d.num_pose_edges, 36),
-            "pose_edge_q_I_B_p_B_I": (d.num_pose_edges, 7),
+            "pose_edge_q_I_B_p_B_I": (d.num_pose_edges, 7), "pose_edge_type": (d.num_pose_edges,),
+            "pose_edge_switch": (d.num_pose_edges,), "pose_edge_switch_variance": (d.num_pose_edges,),
         }
         p = getattr(d, name)
         n = int(np.prod(shapes[name]))

@@ -23,6 +23,7 @@ namespace oracle {
 int oracleLinearizeVisual(Problem* p, double* r, double* Jl, double* Js, double* Jo, double* cost);
 int oracleLinearizePoseEdges(Problem* p, double* r, double* Jf, double* Jt);
 int oracleReadState(Problem* p, double* kx, double* kv, double* kbg, double* kba, double* lp);
+int oracleReadSwitches(Problem* p, double* s);
 int oracleWriteState(Problem* p, const double* kx, const double* kv, const double* kbg, const double* kba, const double* lp);
 void oracleDestroy(Problem* p);
 void oracleSetThreads(Problem* p, int t);
@@ -67,6 +68,25 @@ int oracle_pose_edge(const double* xk, const double* xk1, const double* ext, con
   double M[36];
   if (!oracle::poseEdgeSqrtInfo(cov, M)) return 1;
   oracle::poseEdgeEvaluate(xk, xk1, ext, meas, M, r, Jk, Jk1);
+  return 0;
+}
+int oracle_read_switches(void* h, double* s) { return oracle::oracleReadSwitches((oracle::Problem*)h, s); }
+// One loop-closure term without its switch (baseframes, vertex blocks,
+// measurement q_AB JPL | p_AB, covariance): residual [6], ambient Jacobians.
+int oracle_loop_closure(const double* bfA, const double* bfB, const double* xA, const double* xB, const double* meas,
+                        const double* cov, double* r, double* JA, double* JB) {
+  double M[36];
+  if (!oracle::poseEdgeSqrtInfo(cov, M)) return 1;
+  oracle::loopClosureEvaluate(bfA, bfB, xA, xB, meas, M, r, JA, JB);
+  return 0;
+}
+// One absolute pose term (baseframe, vertex block, sensor extrinsics q_S_B |
+// p_S_B, measurement q_S_G Hamilton | p_G_S, covariance).
+int oracle_absolute_pose(const double* bf, const double* x, const double* ext, const double* meas, const double* cov,
+                         double* r, double* J) {
+  double M[36];
+  if (!oracle::poseEdgeSqrtInfo(cov, M)) return 1;
+  oracle::absolutePoseEvaluate(bf, x, ext, meas, M, r, J);
   return 0;
 }
 int oracle_read_state(void* h, double* kx, double* kv, double* kbg, double* kba, double* lp) {

@@ -152,6 +152,14 @@ void visualPointInCamera(const double* const* params, int type, double* p_C);
 void poseEdgeEvaluate(const double* xk, const double* xk1, const double* ext, const double* meas, const double* M,
                       double* r, double* Jk, double* Jk1);
 bool poseEdgeSqrtInfo(const double* cov, double* M);
+// LoopClosureEdgeErrorTerm without the switch factor: residual [6], ambient
+// Jacobians [6][7] of the two vertex blocks (may be NULL).
+void loopClosureEvaluate(const double* bfA, const double* bfB, const double* xA, const double* xB, const double* meas,
+                         const double* M, double* r, double* JA, double* JB);
+// BlockPosePriorErrorTermV2: residual [6], ambient Jacobian [6][7] of the
+// vertex block (may be NULL).
+void absolutePoseEvaluate(const double* bf, const double* x, const double* ext, const double* meas, const double* M,
+                          double* r, double* J);
 bool visualEvaluate(const double* const* params, const double* measurement, double pixel_sigma,
                     int error_type, const mba_camera& cam, double* residual,
                     double** jacobians, bool* failed);

@@ -41,6 +41,9 @@ struct Problem {
   int64_t nkf = 0, nlm = 0, nobs = 0, ncam = 0, nmis = 0, nedge = 0, nsamp = 0;
   int64_t nimu = 0;  // edges [0, nimu) are IMU edges, [nimu, nedge) relative pose edges
   std::vector<double> pe_meas, pe_M, pe_ext;  // per pose edge: [7], [36] sqrt information, [7]
+  std::vector<int32_t> pe_type, pe_swi;       // per pose edge: MBA_POSE_EDGE_*, switch variable (-1: none)
+  std::vector<double> pe_swc;                 // switch value of an edge without a switch variable
+  std::vector<double> sw, sw_w;               // switch variables and their prior's sqrt information
   std::vector<double> obs_uv, obs_sigma;
   std::vector<int32_t> obs_lm, obs_kf, obs_cam;
   std::vector<uint8_t> obs_type;
@@ -98,14 +101,39 @@ int createProblem(const mba_problem_desc* d, Problem** out) {
     p->imu.assign(d->imu_acc_gyro, d->imu_acc_gyro + 6 * p->nsamp);
   }
   // Relative pose edges follow the IMU edges.
+  // Loop closures store the measured rotation as JPL coefficients (the
+  // Hamilton inverse, augment-loopclosure.cc:44-49) and absolute terms as the
+  // inverse measured rotation q_S_G (block-pose-prior-error-term-v2.cc:13-16);
+  // both inverses as Eigen computes them (conjugate / squared norm).
   for (int64_t j = 0; j < d->num_pose_edges; ++j) {
-    p->e_from.push_back(d->pose_edge_from[j]);
-    p->e_to.push_back(d->pose_edge_to[j]);
-    p->pe_meas.insert(p->pe_meas.end(), d->pose_edge_T_Bk_Bkp1 + 7 * j, d->pose_edge_T_Bk_Bkp1 + 7 * j + 7);
+    const int type = d->pose_edge_type ? d->pose_edge_type[j] : MBA_POSE_EDGE_RELATIVE;
+    const int32_t f = d->pose_edge_from[j];
+    p->e_from.push_back(f);
+    p->e_to.push_back(type == MBA_POSE_EDGE_ABSOLUTE ? f : d->pose_edge_to[j]);
+    p->pe_type.push_back(type);
+    double T[7];
+    std::memcpy(T, d->pose_edge_T_Bk_Bkp1 + 7 * j, sizeof(T));
+    if (type != MBA_POSE_EDGE_RELATIVE) {
+      const double n2 = T[0] * T[0] + T[1] * T[1] + T[2] * T[2] + T[3] * T[3];
+      for (int i = 0; i < 3; ++i) T[i] = -T[i] / n2;
+      T[3] = T[3] / n2;
+    }
+    p->pe_meas.insert(p->pe_meas.end(), T, T + 7);
     p->pe_ext.insert(p->pe_ext.end(), d->pose_edge_q_I_B_p_B_I + 7 * j, d->pose_edge_q_I_B_p_B_I + 7 * j + 7);
     double M[36];
     if (!poseEdgeSqrtInfo(d->pose_edge_covariance + 36 * j, M)) { delete p; return MBA_ERR_NOT_SPD; }
     p->pe_M.insert(p->pe_M.end(), M, M + 36);
+    const double s0 = (type == MBA_POSE_EDGE_LOOP_CLOSURE && d->pose_edge_switch) ? d->pose_edge_switch[j] : 1.0;
+    const double var = (type == MBA_POSE_EDGE_LOOP_CLOSURE && d->pose_edge_switch_variance)
+                           ? d->pose_edge_switch_variance[j] : 0.0;
+    if (var > 0.0) {
+      p->pe_swi.push_back((int32_t)p->sw.size());
+      p->sw.push_back(s0);
+      p->sw_w.push_back(std::sqrt(1.0 / var));  // SwitchPriorErrorTerm (switch-prior-error-term.h:17-20)
+    } else {
+      p->pe_swi.push_back(-1);
+    }
+    p->pe_swc.push_back(s0);
   }
   p->nedge = p->nimu + d->num_pose_edges;
   p->noise = {d->gyro_noise_sigma, d->gyro_bias_sigma, d->acc_noise_sigma, d->acc_bias_sigma,
@@ -254,6 +282,7 @@ int evaluateInertialAmbient(const Problem& p, double* res, double* const* jac) {
 struct Linearization {
   std::vector<double> vr, vJl, vJs, vJo;  // visual: 2, 2x3, 2x6, 2x6 per obs
   std::vector<double> ir, iJf, iJt;       // inertial: 15, 15x15, 15x15 per edge
+  std::vector<double> sJ;                 // pose edges: d residual / d switch [6] (= unswitched residual)
   double cost = 0.0;
 };
 
@@ -292,6 +321,7 @@ int linearize(const Problem& p, bool want_jac, Linearization* L) {
     L->vr.assign(2 * p.nobs, 0.0); L->vJl.assign(6 * p.nobs, 0.0);
     L->vJs.assign(12 * p.nobs, 0.0); L->vJo.assign(12 * p.nobs, 0.0);
     L->ir.assign(15 * p.nedge, 0.0); L->iJf.assign(225 * p.nedge, 0.0); L->iJt.assign(225 * p.nedge, 0.0);
+    L->sJ.assign(6 * (p.nedge - p.nimu), 0.0);
   }
   const int T = p.threads;
   std::vector<double> part(T + 1, 0.0);
@@ -412,18 +442,41 @@ int linearize(const Problem& p, bool want_jac, Linearization* L) {
     }
   }
   for (double v : ipart) cost += v;
-  // relative pose edges: residual rows 0-5, tangent columns (theta, p) through
-  // the pose parameterization (ambient Jacobian x ComputeJacobian).
+  // pose edges: residual rows 0-5, tangent columns (theta, p) through the
+  // pose parameterization (ambient Jacobian x ComputeJacobian); loop closures
+  // scaled by their switch, whose prior adds 0.5 ((1 - s) w)^2.
+  static const double kIdentityPose[7] = {0.0, 0.0, 0.0, 1.0, 0.0, 0.0, 0.0};
   for (int64_t i = p.nimu; i < p.nedge; ++i) {
     const int64_t j = i - p.nimu, f = p.e_from[i], t = p.e_to[i];
-    double r[6], Jf7[42], Jt7[42];
-    poseEdgeEvaluate(&p.kf_x[7 * f], &p.kf_x[7 * t], &p.pe_ext[7 * j], &p.pe_meas[7 * j], &p.pe_M[36 * j], r,
-                     want_jac ? Jf7 : nullptr, want_jac ? Jt7 : nullptr);
+    double r[6], Jf7[42] = {}, Jt7[42] = {};
+    const int type = p.pe_type[j];
+    const double* xf = &p.kf_x[7 * f];
+    const double* xt = &p.kf_x[7 * t];
+    if (type == MBA_POSE_EDGE_LOOP_CLOSURE) {
+      const bool same = p.kf_mis[f] == p.kf_mis[t];
+      const double* bfA = same ? kIdentityPose : &p.mis[7 * p.kf_mis[f]];
+      const double* bfB = same ? kIdentityPose : &p.mis[7 * p.kf_mis[t]];
+      loopClosureEvaluate(bfA, bfB, xf, xt, &p.pe_meas[7 * j], &p.pe_M[36 * j], r, want_jac ? Jf7 : nullptr,
+                          want_jac ? Jt7 : nullptr);
+    } else if (type == MBA_POSE_EDGE_ABSOLUTE) {
+      absolutePoseEvaluate(&p.mis[7 * p.kf_mis[f]], xf, &p.pe_ext[7 * j], &p.pe_meas[7 * j], &p.pe_M[36 * j], r,
+                           want_jac ? Jf7 : nullptr);
+    } else {
+      poseEdgeEvaluate(xf, xt, &p.pe_ext[7 * j], &p.pe_meas[7 * j], &p.pe_M[36 * j], r, want_jac ? Jf7 : nullptr,
+                       want_jac ? Jt7 : nullptr);
+    }
+    const int q = p.pe_swi[j];
+    const double sw = q >= 0 ? p.sw[q] : p.pe_swc[j];
     double sq = 0.0;
-    for (int k = 0; k < 6; ++k) sq += r[k] * r[k];
+    for (int k = 0; k < 6; ++k) sq += (sw * r[k]) * (sw * r[k]);
     cost += 0.5 * sq;
+    if (q >= 0) {
+      const double rp = (1.0 - sw) * p.sw_w[q];
+      cost += 0.5 * rp * rp;
+    }
     if (!want_jac) continue;
-    for (int k = 0; k < 6; ++k) L->ir[15 * i + k] = r[k];
+    for (int k = 0; k < 6; ++k) { L->ir[15 * i + k] = sw * r[k]; L->sJ[6 * j + k] = r[k]; }
+    for (int k = 0; k < 42; ++k) { Jf7[k] *= sw; Jt7[k] *= sw; }
     for (int s2 = 0; s2 < 2; ++s2) {
       const int64_t k = s2 == 0 ? f : t;
       const double* J7 = s2 == 0 ? Jf7 : Jt7;
@@ -537,14 +590,51 @@ static bool inv3(const double* A, double* B) {
 }
 
 struct StepResult {
-  std::vector<double> dc, dl;  // scaled step (keyframes 15N, landmarks 3N)
+  std::vector<double> dc, dl, ds;  // scaled step (keyframes 15N, landmarks 3N, switches)
   int linear_iterations = 0;
   int status = 0;
 };
 
 struct Scaled {
-  std::vector<double> skf, slm;  // Jacobi scale per tangent dim
+  std::vector<double> skf, slm, ssw;  // Jacobi scale per tangent dim and per switch variable
 };
+
+// block(i, j) += s u v^T for 15-vectors u (rows of i) and v (rows of j).
+static void addOuter(BlockSystem* S, int64_t i, int64_t j, const double* u, const double* v, double s) {
+  double* B = &S->blocks[225 * S->find(i, j)];
+  const bool swap = i > j;
+  for (int r = 0; r < 15; ++r)
+    for (int c = 0; c < 15; ++c) {
+      if (!swap) B[15 * r + c] += s * u[r] * v[c];
+      else B[15 * c + r] += s * u[r] * v[c];
+    }
+}
+
+// Per switch variable of the pose edge j: the scaled Jacobian columns of the
+// edge's two keyframes times the switch column (W_f, W_t), the switch's
+// scaled gradient and J^T J (landmark-style elimination of a 1-dim block).
+struct SwitchTerms {
+  double W[30];  // W_f (15) | W_t (15)
+  double g, h;   // scaled gradient, scaled J^T J (undamped)
+};
+static SwitchTerms switchTerms(const Problem& p, const Linearization& L, const Scaled& sc, int64_t j) {
+  SwitchTerms o{};
+  const int q = p.pe_swi[j];
+  const int64_t e = p.nimu + j, f = p.e_from[e], t = p.e_to[e];
+  const double ss = sc.ssw[q], w = p.sw_w[q], rp = (1.0 - p.sw[q]) * w;
+  const double* js = &L.sJ[6 * j];
+  double jj = w * w, g = -w * rp;
+  for (int k = 0; k < 6; ++k) { jj += js[k] * js[k]; g += js[k] * L.ir[15 * e + k]; }
+  o.h = jj * ss * ss;
+  o.g = g * ss;
+  for (int c = 0; c < 15; ++c) {
+    double a = 0.0, b = 0.0;
+    for (int k = 0; k < 6; ++k) { a += L.iJf[225 * e + 15 * k + c] * js[k]; b += L.iJt[225 * e + 15 * k + c] * js[k]; }
+    o.W[c] = a * sc.skf[15 * f + c] * ss;
+    o.W[15 + c] = b * sc.skf[15 * t + c] * ss;
+  }
+  return o;
+}
 
 // Solves (J^T J + D^2) d = -J^T r for the scaled Jacobian via Schur
 // elimination of the landmarks.
@@ -552,8 +642,8 @@ struct Scaled {
 // row-major) and its right-hand side are written there and nothing is solved.
 static StepResult computeStep(const Problem& p, const Linearization& L, const Scaled& sc,
                               const std::vector<double>& dkf, const std::vector<double>& dlm,
-                              const BlockSystem& pattern, int solver, int max_it, double tol,
-                              double* dense_A = nullptr, double* dense_b = nullptr) {
+                              const std::vector<double>& dsw, const BlockSystem& pattern, int solver, int max_it,
+                              double tol, double* dense_A = nullptr, double* dense_b = nullptr) {
   StepResult out;
   const int64_t N = p.nkf;
   BlockSystem S = pattern;  // copies pattern + zeroed blocks
@@ -663,6 +753,26 @@ static StepResult computeStep(const Problem& p, const Linearization& L, const Sc
             B[15 * r + c] -= v;  // ks sorted => a<=b => (ks[a], ks[b]) is the stored orientation
           }
       }
+    }
+  }
+  // Schur elimination of each switch variable: S_ab -= W_a W_b^T / H,
+  // rhs_a += W_a g / H for a, b in {from, to}.
+  const int64_t npe = p.nedge - p.nimu;
+  std::vector<SwitchTerms> swt(npe);
+  for (int64_t j = 0; j < npe; ++j) {
+    const int q = p.pe_swi[j];
+    if (q < 0) continue;
+    swt[j] = switchTerms(p, L, sc, j);
+    SwitchTerms& w = swt[j];
+    w.h += dsw[q];
+    const int64_t e = p.nimu + j, f = p.e_from[e], t = p.e_to[e];
+    const double hi = 1.0 / w.h;
+    addOuter(&S, f, f, w.W, w.W, -hi);
+    addOuter(&S, t, t, w.W + 15, w.W + 15, -hi);
+    addOuter(&S, f, t, w.W, w.W + 15, -hi);
+    for (int c = 0; c < 15; ++c) {
+      bc[15 * f + c] += w.W[c] * hi * w.g;
+      bc[15 * t + c] += w.W[15 + c] * hi * w.g;
     }
   }
   // Masked keyframe dims: identity rows, zero rhs.
@@ -791,6 +901,16 @@ static StepResult computeStep(const Problem& p, const Linearization& L, const Sc
     for (int a = 0; a < 3; ++a)
       out.dl[3 * l + a] = Vi[3 * a] * t[3 * l] + Vi[3 * a + 1] * t[3 * l + 1] + Vi[3 * a + 2] * t[3 * l + 2];
   }
+  // Switches: ds = (-g - W_f^T dc_f - W_t^T dc_t) / H.
+  out.ds.assign(p.sw.size(), 0.0);
+  for (int64_t j = 0; j < npe; ++j) {
+    const int q = p.pe_swi[j];
+    if (q < 0) continue;
+    const int64_t e = p.nimu + j, f = p.e_from[e], te = p.e_to[e];
+    double u = -swt[j].g;
+    for (int c = 0; c < 15; ++c) u -= swt[j].W[c] * x[15 * f + c] + swt[j].W[15 + c] * x[15 * te + c];
+    out.ds[q] = u / swt[j].h;
+  }
   return out;
 }
 
@@ -826,10 +946,25 @@ static void plusState(const Problem& p, const std::vector<double>& dkf, const st
       for (int i = 0; i < 3; ++i) (*lp)[3 * l + i] += dlm[3 * l + i];
 }
 
+// Switch retraction: plain addition projected onto the bounds [0, 1], as
+// Ceres applies parameter bounds after Plus.
+static void plusSwitches(const std::vector<double>& ds, std::vector<double>* sw) {
+  for (size_t q = 0; q < sw->size(); ++q) (*sw)[q] = std::min(1.0, std::max(0.0, (*sw)[q] + ds[q]));
+}
+
 // Jacobi scaling 1 / (1 + |column|) and the column norms of the Jacobian.
-static void columnNorms(const Problem& p, const Linearization& L, std::vector<double>& nkf, std::vector<double>& nlm) {
+static void columnNorms(const Problem& p, const Linearization& L, std::vector<double>& nkf, std::vector<double>& nlm,
+                        std::vector<double>& nsw) {
   nkf.assign(15 * p.nkf, 0.0);
   nlm.assign(3 * p.nlm, 0.0);
+  nsw.assign(p.sw.size(), 0.0);
+  for (int64_t j = 0; j < p.nedge - p.nimu; ++j) {
+    const int q = p.pe_swi[j];
+    if (q < 0) continue;
+    double a = p.sw_w[q] * p.sw_w[q];
+    for (int k = 0; k < 6; ++k) a += L.sJ[6 * j + k] * L.sJ[6 * j + k];
+    nsw[q] = a;
+  }
   for (int64_t i = 0; i < p.nobs; ++i) {
     const int l = p.obs_lm[i];
     for (int a = 0; a < 3; ++a) nlm[3 * l + a] += L.vJl[6 * i + a] * L.vJl[6 * i + a] + L.vJl[6 * i + 3 + a] * L.vJl[6 * i + 3 + a];
@@ -886,13 +1021,17 @@ int solve(Problem& p, const mba_solver_options& o, mba_summary* sum) {
   Scaled sc;
   sc.skf.assign(15 * p.nkf, 1.0);
   sc.slm.assign(3 * p.nlm, 1.0);
-  auto colnorms = [&](std::vector<double>& nkf, std::vector<double>& nlm) { columnNorms(p, L, nkf, nlm); };
-  std::vector<double> nkf, nlm;
-  colnorms(nkf, nlm);
-  if (o.jacobi_scaling) {
+  sc.ssw.assign(p.sw.size(), 1.0);
+  std::vector<double> nkf, nlm, nsw;
+  auto colnorms = [&]() { columnNorms(p, L, nkf, nlm, nsw); };
+  auto jacobi = [&]() {
+    if (!o.jacobi_scaling) return;
     for (size_t a = 0; a < nkf.size(); ++a) sc.skf[a] = 1.0 / (1.0 + std::sqrt(nkf[a]));
     for (size_t a = 0; a < nlm.size(); ++a) sc.slm[a] = 1.0 / (1.0 + std::sqrt(nlm[a]));
-  }
+    for (size_t a = 0; a < nsw.size(); ++a) sc.ssw[a] = 1.0 / (1.0 + std::sqrt(nsw[a]));
+  };
+  colnorms();
+  jacobi();
   BlockSystem pattern;
   buildPattern(p, &pattern);
 
@@ -900,7 +1039,7 @@ int solve(Problem& p, const mba_solver_options& o, mba_summary* sum) {
   double radius = o.initial_trust_region_radius;
   double decrease_factor = 2.0;
   bool reuse_diag = false;
-  std::vector<double> dkf(15 * p.nkf), dlm(3 * p.nlm);
+  std::vector<double> dkf(15 * p.nkf), dlm(3 * p.nlm), dsw(p.sw.size());
   if (sum) {
     sum->initial_cost = cost;
     sum->num_iterations = 0;
@@ -935,23 +1074,23 @@ int solve(Problem& p, const mba_solver_options& o, mba_summary* sum) {
       st = linearize(p, true, &L);
       if (st) return st;
       cost = L.cost;
-      colnorms(nkf, nlm);
-      if (o.jacobi_scaling) {
-        for (size_t a = 0; a < nkf.size(); ++a) sc.skf[a] = 1.0 / (1.0 + std::sqrt(nkf[a]));
-        for (size_t a = 0; a < nlm.size(); ++a) sc.slm[a] = 1.0 / (1.0 + std::sqrt(nlm[a]));
-      }
+      colnorms();
+      jacobi();
       decrease_factor = 2.0;
       reuse_diag = false;
     }
     // LM diagonal from the scaled Jacobian column norms.
     if (!reuse_diag) {
-      colnorms(nkf, nlm);
+      colnorms();
       for (size_t a = 0; a < nkf.size(); ++a) nkf[a] = std::min(std::max(nkf[a] * sc.skf[a] * sc.skf[a], o.min_lm_diagonal), o.max_lm_diagonal);
       for (size_t a = 0; a < nlm.size(); ++a) nlm[a] = std::min(std::max(nlm[a] * sc.slm[a] * sc.slm[a], o.min_lm_diagonal), o.max_lm_diagonal);
+      for (size_t a = 0; a < nsw.size(); ++a) nsw[a] = std::min(std::max(nsw[a] * sc.ssw[a] * sc.ssw[a], o.min_lm_diagonal), o.max_lm_diagonal);
     }
     for (size_t a = 0; a < nkf.size(); ++a) dkf[a] = nkf[a] / radius;
     for (size_t a = 0; a < nlm.size(); ++a) dlm[a] = nlm[a] / radius;
-    StepResult s = computeStep(p, L, sc, dkf, dlm, pattern, o.linear_solver, o.max_linear_iterations, o.linear_tolerance);
+    for (size_t a = 0; a < nsw.size(); ++a) dsw[a] = nsw[a] / radius;
+    StepResult s = computeStep(p, L, sc, dkf, dlm, dsw, pattern, o.linear_solver, o.max_linear_iterations,
+                               o.linear_tolerance);
     if (sum) sum->total_linear_iterations += s.linear_iterations;
     double mcc = 0.0;
     if (s.status == 0) {
@@ -972,12 +1111,18 @@ int solve(Problem& p, const mba_solver_options& o, mba_summary* sum) {
       }
       for (int64_t e = 0; e < p.nedge; ++e) {
         const int64_t f = p.e_from[e], t = p.e_to[e];
+        const int q = e >= p.nimu ? p.pe_swi[e - p.nimu] : -1;
         for (int rr = 0; rr < 15; ++rr) {
           double u = 0.0;
           for (int c = 0; c < 15; ++c)
             u += L.iJf[225 * e + 15 * rr + c] * sc.skf[15 * f + c] * s.dc[15 * f + c] +
                  L.iJt[225 * e + 15 * rr + c] * sc.skf[15 * t + c] * s.dc[15 * t + c];
+          if (q >= 0 && rr < 6) u += L.sJ[6 * (e - p.nimu) + rr] * sc.ssw[q] * s.ds[q];
           mcc -= u * (L.ir[15 * e + rr] + u / 2.0);
+        }
+        if (q >= 0) {  // switch prior: r = (1 - s) w, J = -w
+          const double w = p.sw_w[q], u = -w * sc.ssw[q] * s.ds[q];
+          mcc -= u * ((1.0 - p.sw[q]) * w + u / 2.0);
         }
       }
     }
@@ -990,12 +1135,18 @@ int solve(Problem& p, const mba_solver_options& o, mba_summary* sum) {
       continue;
     }
     // Unscale and retract.
-    std::vector<double> ukf(15 * p.nkf), ulm(3 * p.nlm);
+    std::vector<double> ukf(15 * p.nkf), ulm(3 * p.nlm), usw(p.sw.size());
     for (size_t a = 0; a < ukf.size(); ++a) ukf[a] = s.dc[a] * sc.skf[a];
     for (size_t a = 0; a < ulm.size(); ++a) ulm[a] = s.dl[a] * sc.slm[a];
-    std::vector<double> kx = p.kf_x, kv = p.kf_v, kbg = p.kf_bg, kba = p.kf_ba, lp = p.lm_p;
+    for (size_t a = 0; a < usw.size(); ++a) usw[a] = s.ds[a] * sc.ssw[a];
+    std::vector<double> kx = p.kf_x, kv = p.kf_v, kbg = p.kf_bg, kba = p.kf_ba, lp = p.lm_p, swv = p.sw;
     plusState(p, ukf, ulm, &kx, &kv, &kbg, &kba, &lp);
-    std::swap(kx, p.kf_x); std::swap(kv, p.kf_v); std::swap(kbg, p.kf_bg); std::swap(kba, p.kf_ba); std::swap(lp, p.lm_p);
+    plusSwitches(usw, &swv);
+    auto swap_state = [&]() {
+      std::swap(kx, p.kf_x); std::swap(kv, p.kf_v); std::swap(kbg, p.kf_bg); std::swap(kba, p.kf_ba);
+      std::swap(lp, p.lm_p); std::swap(swv, p.sw);
+    };
+    swap_state();
     Linearization Lc;
     const int cst = linearize(p, false, &Lc);
     const double new_cost = cst ? INFINITY : Lc.cost;
@@ -1003,19 +1154,20 @@ int solve(Problem& p, const mba_solver_options& o, mba_summary* sum) {
     double step_norm = 0.0, x_norm = 0.0;
     for (size_t a = 0; a < kx.size(); ++a) { const double dd = p.kf_x[a] - kx[a]; step_norm += dd * dd; x_norm += kx[a] * kx[a]; }
     for (size_t a = 0; a < lp.size(); ++a) { const double dd = p.lm_p[a] - lp[a]; step_norm += dd * dd; x_norm += lp[a] * lp[a]; }
+    for (size_t a = 0; a < swv.size(); ++a) { const double dd = p.sw[a] - swv[a]; step_norm += dd * dd; x_norm += swv[a] * swv[a]; }
     step_norm = std::sqrt(step_norm);
     x_norm = std::sqrt(x_norm);
     const double rel = (cost - new_cost) / mcc;
     const bool ok = std::isfinite(new_cost) && rel > o.min_relative_decrease;
     if (o.check_tolerances && step_norm <= o.parameter_tolerance * (x_norm + o.parameter_tolerance)) {
-      if (!ok) { std::swap(kx, p.kf_x); std::swap(kv, p.kf_v); std::swap(kbg, p.kf_bg); std::swap(kba, p.kf_ba); std::swap(lp, p.lm_p); }
+      if (!ok) swap_state();
       record(iter, ok, s.linear_iterations, ok ? new_cost : cost, cost - new_cost, step_norm, rel);
       if (ok) cost = new_cost;
       if (sum) sum->termination = 3;
       break;
     }
     if (o.check_tolerances && std::fabs(cost - new_cost) <= o.function_tolerance * cost) {
-      if (!ok) { std::swap(kx, p.kf_x); std::swap(kv, p.kf_v); std::swap(kbg, p.kf_bg); std::swap(kba, p.kf_ba); std::swap(lp, p.lm_p); }
+      if (!ok) swap_state();
       record(iter, ok, s.linear_iterations, ok ? new_cost : cost, cost - new_cost, step_norm, rel);
       if (ok) cost = new_cost;
       if (sum) sum->termination = 1;
@@ -1037,7 +1189,7 @@ int solve(Problem& p, const mba_solver_options& o, mba_summary* sum) {
         sum->termination = 6;
       }
     } else {
-      std::swap(kx, p.kf_x); std::swap(kv, p.kf_v); std::swap(kbg, p.kf_bg); std::swap(kba, p.kf_ba); std::swap(lp, p.lm_p);
+      swap_state();
       radius /= decrease_factor;
       decrease_factor *= 2.0;
       reuse_diag = true;
@@ -1060,22 +1212,26 @@ int reducedSystemDense(Problem& p, const mba_solver_options& o, double radius, d
   int st = linearize(p, true, &L);
   if (st) return st;
   Scaled sc;
-  std::vector<double> nkf, nlm;
-  columnNorms(p, L, nkf, nlm);
+  std::vector<double> nkf, nlm, nsw;
+  columnNorms(p, L, nkf, nlm, nsw);
   sc.skf.assign(15 * p.nkf, 1.0);
   sc.slm.assign(3 * p.nlm, 1.0);
+  sc.ssw.assign(p.sw.size(), 1.0);
   if (o.jacobi_scaling) {
     for (size_t a = 0; a < nkf.size(); ++a) sc.skf[a] = 1.0 / (1.0 + std::sqrt(nkf[a]));
     for (size_t a = 0; a < nlm.size(); ++a) sc.slm[a] = 1.0 / (1.0 + std::sqrt(nlm[a]));
+    for (size_t a = 0; a < nsw.size(); ++a) sc.ssw[a] = 1.0 / (1.0 + std::sqrt(nsw[a]));
   }
-  std::vector<double> dkf(15 * p.nkf), dlm(3 * p.nlm);
+  std::vector<double> dkf(15 * p.nkf), dlm(3 * p.nlm), dsw(p.sw.size());
+  for (size_t a = 0; a < nsw.size(); ++a)
+    dsw[a] = std::min(std::max(nsw[a] * sc.ssw[a] * sc.ssw[a], o.min_lm_diagonal), o.max_lm_diagonal) / radius;
   for (size_t a = 0; a < nkf.size(); ++a)
     dkf[a] = std::min(std::max(nkf[a] * sc.skf[a] * sc.skf[a], o.min_lm_diagonal), o.max_lm_diagonal) / radius;
   for (size_t a = 0; a < nlm.size(); ++a)
     dlm[a] = std::min(std::max(nlm[a] * sc.slm[a] * sc.slm[a], o.min_lm_diagonal), o.max_lm_diagonal) / radius;
   BlockSystem pattern;
   buildPattern(p, &pattern);
-  StepResult r = computeStep(p, L, sc, dkf, dlm, pattern, MBA_LINEAR_SOLVER_DENSE_SCHUR, 1, 0.0, A, b);
+  StepResult r = computeStep(p, L, sc, dkf, dlm, dsw, pattern, MBA_LINEAR_SOLVER_DENSE_SCHUR, 1, 0.0, A, b);
   return r.status;
 }
 
@@ -1106,6 +1262,12 @@ int oracleLinearizeVisual(Problem* p, double* r, double* Jl, double* Js, double*
   if (Jo) std::memcpy(Jo, L.vJo.data(), L.vJo.size() * sizeof(double));
   if (cost) *cost = L.cost;
   return st;
+}
+
+// Switch value per pose edge (1 for edges without a switch variable).
+int oracleReadSwitches(Problem* p, double* s) {
+  for (int64_t j = 0; j < p->nedge - p->nimu; ++j) s[j] = p->pe_swi[j] >= 0 ? p->sw[p->pe_swi[j]] : p->pe_swc[j];
+  return 0;
 }
 
 int oracleReadState(Problem* p, double* kx, double* kv, double* kbg, double* kba, double* lp) {

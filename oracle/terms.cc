@@ -695,6 +695,21 @@ template <int N> Dual<N> operator+(const Dual<N>& x, const Dual<N>& y) { Dual<N>
 template <int N> Dual<N> operator-(const Dual<N>& x, const Dual<N>& y) { Dual<N> r(x.a - y.a); for (int i = 0; i < N; ++i) r.d[i] = x.d[i] - y.d[i]; return r; }
 template <int N> Dual<N> operator-(const Dual<N>& x) { Dual<N> r(-x.a); for (int i = 0; i < N; ++i) r.d[i] = -x.d[i]; return r; }
 template <int N> Dual<N> operator*(const Dual<N>& x, const Dual<N>& y) { Dual<N> r(x.a * y.a); for (int i = 0; i < N; ++i) r.d[i] = x.a * y.d[i] + x.d[i] * y.a; return r; }
+template <int N> Dual<N> operator/(const Dual<N>& x, const Dual<N>& y) {
+  const double inv = 1.0 / y.a, q = x.a * inv;
+  Dual<N> r(q);
+  for (int i = 0; i < N; ++i) r.d[i] = (x.d[i] - q * y.d[i]) * inv;
+  return r;
+}
+template <int N> Dual<N> sqrtS(const Dual<N>& x) {
+  const double v = std::sqrt(x.a), h = 0.5 / v;
+  Dual<N> r(v);
+  for (int i = 0; i < N; ++i) r.d[i] = x.d[i] * h;
+  return r;
+}
+static inline double sqrtS(double x) { return std::sqrt(x); }
+template <int N> double valueOf(const Dual<N>& x) { return x.a; }
+static inline double valueOf(double x) { return x; }
 template <int N> bool isNegative(const Dual<N>& x) { return x.a < 0.0; }
 
 // Hamilton quaternion (x y z w) product, rotation (Eigen's _transformVector
@@ -751,6 +766,178 @@ static void poseEdgeResidual(const S* xk, const S* xk1, const double* ext, const
     S acc(0.0);
     for (int i = 0; i < 6; ++i) acc = acc + e[i] * S(M[6 * i + j]);
     ew[j] = acc;
+  }
+}
+
+// JPL quaternion algebra on any scalar (quaternion-math-inl.h):
+// toRotationMatrixJPL (:6-27), quaternionInverseJPL (:156-163) and
+// positiveQuaternionProductJPL (:112-154: left-multiplication matrix of q1
+// times q2, normalized, sign flipped to w >= 0).
+template <typename S> static void jplRotS(const S* q, S* R) {
+  const S one(1.0), two(2.0);
+  R[0] = one - two * (q[1] * q[1] + q[2] * q[2]);
+  R[1] = two * (q[0] * q[1] + q[2] * q[3]);
+  R[2] = two * (q[0] * q[2] - q[1] * q[3]);
+  R[3] = two * (q[0] * q[1] - q[2] * q[3]);
+  R[4] = one - two * (q[0] * q[0] + q[2] * q[2]);
+  R[5] = two * (q[1] * q[2] + q[0] * q[3]);
+  R[6] = two * (q[0] * q[2] + q[1] * q[3]);
+  R[7] = two * (q[1] * q[2] - q[0] * q[3]);
+  R[8] = one - two * (q[0] * q[0] + q[1] * q[1]);
+}
+template <typename S> static void jplInvS(const S* q, S* o) { o[0] = -q[0]; o[1] = -q[1]; o[2] = -q[2]; o[3] = q[3]; }
+template <typename S> static void jplProdPosS(const S* a, const S* b, S* o) {
+  S p[4];
+  p[0] = a[3] * b[0] + a[2] * b[1] - a[1] * b[2] + a[0] * b[3];
+  p[1] = -a[2] * b[0] + a[3] * b[1] + a[0] * b[2] + a[1] * b[3];
+  p[2] = a[1] * b[0] - a[0] * b[1] + a[3] * b[2] + a[2] * b[3];
+  p[3] = -a[0] * b[0] - a[1] * b[1] - a[2] * b[2] + a[3] * b[3];
+  const S z = p[0] * p[0] + p[1] * p[1] + p[2] * p[2] + p[3] * p[3];
+  if (valueOf(z) > 0.0) {
+    const S n = sqrtS(z);
+    for (int i = 0; i < 4; ++i) p[i] = p[i] / n;
+  }
+  const bool flip = isNegative(p[3]);
+  for (int i = 0; i < 4; ++i) o[i] = flip ? -p[i] : p[i];
+}
+template <typename S> static void mat3MulS(const S* A, const S* B, S* C) {
+  for (int i = 0; i < 3; ++i)
+    for (int j = 0; j < 3; ++j) C[3 * i + j] = A[3 * i] * B[j] + A[3 * i + 1] * B[3 + j] + A[3 * i + 2] * B[6 + j];
+}
+template <typename S> static void mat3VecS(const S* A, const S* v, S* o) {
+  for (int i = 0; i < 3; ++i) o[i] = A[3 * i] * v[0] + A[3 * i + 1] * v[1] + A[3 * i + 2] * v[2];
+}
+template <typename S> static void transpose3S(const S* A, S* B) {
+  for (int i = 0; i < 3; ++i)
+    for (int j = 0; j < 3; ++j) B[3 * j + i] = A[3 * i + j];
+}
+
+// Rotation matrix (row-major) to Hamilton quaternion (x y z w), the
+// trace / largest-diagonal method (K. Shoemake, "Animating rotation with
+// quaternion curves", SIGGRAPH 1985), in the form Eigen's
+// Quaternion(const Matrix3&) constructor uses.
+template <typename S> static void rotToHamiltonS(const S* m, S* q) {
+  const S tr = m[0] + m[4] + m[8];
+  if (valueOf(tr) > 0.0) {
+    S t = sqrtS(tr + S(1.0));
+    q[3] = S(0.5) * t;
+    t = S(0.5) / t;
+    q[0] = (m[7] - m[5]) * t;
+    q[1] = (m[2] - m[6]) * t;
+    q[2] = (m[3] - m[1]) * t;
+  } else {
+    int i = 0;
+    if (valueOf(m[4]) > valueOf(m[0])) i = 1;
+    if (valueOf(m[8]) > valueOf(m[4 * i])) i = 2;
+    const int j = (i + 1) % 3, k = (j + 1) % 3;
+    S t = sqrtS(m[4 * i] - m[4 * j] - m[4 * k] + S(1.0));
+    q[i] = S(0.5) * t;
+    t = S(0.5) / t;
+    q[3] = (m[3 * k + j] - m[3 * j + k]) * t;
+    q[j] = (m[3 * j + i] + m[3 * i + j]) * t;
+    q[k] = (m[3 * k + i] + m[3 * i + k]) * t;
+  }
+}
+
+template <typename S> static void whiten6(const S* e, const double* M, S* ew) {
+  for (int j = 0; j < 6; ++j) {
+    S acc(0.0);
+    for (int i = 0; i < 6; ++i) acc = acc + e[i] * S(M[6 * i + j]);
+    ew[j] = acc;
+  }
+}
+
+// LoopClosureEdgeErrorTerm::operator() (loop-closure-edge-error-term-inl.h:
+// 6-81), without the switch factor: baseframes T_G_MA, T_G_MB (JPL q | p,
+// constants; identity for two vertices of one mission, :83-95), vertex
+// blocks q_IA_MA | p_MA_IA; measurement q_AB (JPL) | p_AB.
+template <typename S>
+static void loopClosureResidual(const double* bfA, const double* bfB, const S* xA, const S* xB, const double* meas,
+                                const double* M, S* ew) {
+  S qGMA[4], qGMB[4], RGMA[9], RGMB[9];
+  for (int i = 0; i < 4; ++i) { qGMA[i] = S(bfA[i]); qGMB[i] = S(bfB[i]); }
+  jplRotS(qGMA, RGMA);
+  jplRotS(qGMB, RGMB);
+  S pA[3], pB[3], pGIA[3], pGIB[3];
+  mat3VecS(RGMA, xA + 4, pA);
+  mat3VecS(RGMB, xB + 4, pB);
+  for (int i = 0; i < 3; ++i) { pGIA[i] = S(bfA[4 + i]) + pA[i]; pGIB[i] = S(bfB[4 + i]) + pB[i]; }
+  S qi[4], qGIA[4], qGIB[4], qIAIB[4], qlci[4], qerr[4];
+  jplInvS(xA, qi);
+  jplProdPosS(qGMA, qi, qGIA);
+  jplInvS(xB, qi);
+  jplProdPosS(qGMB, qi, qGIB);
+  jplInvS(qGIA, qi);
+  jplProdPosS(qi, qGIB, qIAIB);
+  const S qlc[4] = {S(meas[0]), S(meas[1]), S(meas[2]), S(meas[3])};
+  jplInvS(qlc, qlci);
+  jplProdPosS(qlci, qIAIB, qerr);
+  S RIAG[9], d[3], e[6];
+  jplInvS(qGIA, qi);
+  jplRotS(qi, RIAG);
+  for (int i = 0; i < 3; ++i) d[i] = pGIB[i] - pGIA[i];
+  mat3VecS(RIAG, d, e);
+  for (int i = 0; i < 3; ++i) e[i] = e[i] - S(meas[4 + i]);
+  for (int i = 0; i < 3; ++i) e[3 + i] = S(2.0) * qerr[i];
+  whiten6(e, M, ew);
+}
+
+// BlockPosePriorErrorTermV2::operator() (block-pose-prior-error-term-v2-inl.h:
+// 8-60): baseframe q_G_M | p_G_M and sensor extrinsics q_S_B | p_S_B (JPL,
+// constants), vertex block q_B_M | p_M_B; measurement q_S_G (Hamilton, the
+// inverse of the measured rotation, as the constructor stores it) | p_G_S.
+template <typename S>
+static void absolutePoseResidual(const double* bf, const S* x, const double* ext, const double* meas, const double* M,
+                                 S* ew) {
+  S q[4], RGM[9], RBM[9], RMB[9], RSB[9], RBS[9], A[9], RGS[9];
+  for (int i = 0; i < 4; ++i) q[i] = S(bf[i]);
+  jplRotS(q, RGM);
+  jplRotS(x, RBM);
+  transpose3S(RBM, RMB);
+  for (int i = 0; i < 4; ++i) q[i] = S(ext[i]);
+  jplRotS(q, RSB);
+  transpose3S(RSB, RBS);
+  mat3MulS(RGM, RMB, A);
+  mat3MulS(A, RBS, RGS);
+  const S pSB[3] = {S(ext[4]), S(ext[5]), S(ext[6])};
+  S pBS[3], a[3], b[3], e[6];
+  mat3VecS(RBS, pSB, pBS);
+  for (int i = 0; i < 3; ++i) pBS[i] = -pBS[i];
+  mat3VecS(A, pBS, a);
+  mat3VecS(RGM, x + 4, b);
+  for (int i = 0; i < 3; ++i) e[i] = a[i] + b[i] + S(bf[4 + i]) - S(meas[4 + i]);
+  S qGS[4], qd[4];
+  rotToHamiltonS(RGS, qGS);
+  const S qSG[4] = {S(meas[0]), S(meas[1]), S(meas[2]), S(meas[3])};
+  hqMul(qGS, qSG, qd);
+  for (int i = 0; i < 3; ++i) e[3 + i] = S(2.0) * qd[i];
+  whiten6(e, M, ew);
+}
+
+void loopClosureEvaluate(const double* bfA, const double* bfB, const double* xA, const double* xB, const double* meas,
+                         const double* M, double* r, double* JA, double* JB) {
+  typedef Dual<14> D;
+  D a[7], b[7], ew[6];
+  for (int i = 0; i < 7; ++i) { a[i] = D(xA[i]); a[i].d[i] = 1.0; b[i] = D(xB[i]); b[i].d[7 + i] = 1.0; }
+  loopClosureResidual(bfA, bfB, a, b, meas, M, ew);
+  for (int j = 0; j < 6; ++j) {
+    r[j] = ew[j].a;
+    for (int c = 0; c < 7; ++c) {
+      if (JA) JA[7 * j + c] = ew[j].d[c];
+      if (JB) JB[7 * j + c] = ew[j].d[7 + c];
+    }
+  }
+}
+
+void absolutePoseEvaluate(const double* bf, const double* x, const double* ext, const double* meas, const double* M,
+                          double* r, double* J) {
+  typedef Dual<7> D;
+  D a[7], ew[6];
+  for (int i = 0; i < 7; ++i) { a[i] = D(x[i]); a[i].d[i] = 1.0; }
+  absolutePoseResidual(bf, a, ext, meas, M, ew);
+  for (int j = 0; j < 6; ++j) {
+    r[j] = ew[j].a;
+    if (J) for (int c = 0; c < 7; ++c) J[7 * j + c] = ew[j].d[c];
   }
 }
 

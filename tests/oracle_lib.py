@@ -38,6 +38,9 @@ def load():
         "oracle_read_state": (ctypes.c_int, [vp, dp, dp, dp, dp, dp]),
         "oracle_linearize_pose_edges": (ctypes.c_int, [vp, dp, dp, dp]),
         "oracle_pose_edge": (ctypes.c_int, [dp, dp, dp, dp, dp, dp, dp, dp]),
+        "oracle_loop_closure": (ctypes.c_int, [dp, dp, dp, dp, dp, dp, dp, dp, dp]),
+        "oracle_absolute_pose": (ctypes.c_int, [dp, dp, dp, dp, dp, dp, dp]),
+        "oracle_read_switches": (ctypes.c_int, [vp, dp]),
         "oracle_reduced_system": (ctypes.c_int, [vp, ctypes.POINTER(N.SolverOptions), ctypes.c_double, dp, dp]),
         "oracle_write_state": (ctypes.c_int, [vp, dp, dp, dp, dp, dp]),
         "oracle_time_visual": (ctypes.c_double, [vp, ctypes.c_int, ctypes.c_int64, ctypes.c_int]),
@@ -138,6 +141,11 @@ class OracleProblem:
         if st != 0:
             raise RuntimeError(f"oracle_reduced_system failed: {st}")
         return A, b
+
+    def read_switches(self):
+        s = np.zeros(self.desc.num_pose_edges)
+        self.lib.oracle_read_switches(self.h, N.ptr(s))
+        return s
 
     def linearize_pose_edges(self):
         n = self.desc.num_pose_edges
