@@ -386,10 +386,14 @@ typedef struct mba_tuning {
   int32_t visual_block;         /* threads per block of the evaluation kernel (64, 128, 256) */
   int32_t schur_chunk;          /* slot pairs summed per thread by the Schur pair kernel */
   int32_t chain_tail_nodes;     /* chain positions below which one block finishes a chain sweep */
-  int32_t visual_min_blocks;    /* 1, or 3: register-lean evaluation kernel (3 blocks of 256 per SM) */
+  int32_t visual_min_blocks;    /* register cap of the evaluation kernel: blocks of 256 per SM (1 = none;
+                                 * one thread per observation: 1 or 3; pipelined: 1 or 2) */
   double visual_ms;             /* per launch, chosen setting */
   double schur_ms;
   double chain_apply_ms;
+  int32_t visual_pipelined;     /* 1: software-pipelined persistent evaluation kernel, 2: one thread per
+                                 * observation (0 in mba_set_tuning keeps the current setting) */
+  int32_t pad_;
 } mba_tuning;
 mba_status mba_autotune(mba_handle* h, int32_t precision, mba_tuning* out);
 /* Applies tuning values (e.g. cached from an earlier mba_autotune of a

@@ -182,6 +182,8 @@ class Tuning(ctypes.Structure):
         ("visual_ms", ctypes.c_double),
         ("schur_ms", ctypes.c_double),
         ("chain_apply_ms", ctypes.c_double),
+        ("visual_pipelined", ctypes.c_int32),
+        ("pad_", ctypes.c_int32),
     ]
 
 

@@ -16,6 +16,7 @@ struct DevProblem {
   int64_t nimu;             // edges [0, nimu) are inertial, [nimu, nedge) relative pose edges
   int32_t vis_block;        // threads per block of the evaluation kernel (tuned; 0 = default)
   int32_t vis_minb;         // > 1: register-lean variant of the evaluation kernel (tuned)
+  int32_t vis_pipe;         // 1: pipelined persistent variant of the evaluation kernel (tuned)
   // observations
   const double2* obs_uv;
   const double* obs_sinv;   // 1 / sigma
@@ -123,9 +124,12 @@ cudaError_t launch_visual_cost_gated(const DevProblem& P, const double* kf_state
 cudaError_t launch_inertial_gated(const DevProblem& P, const double* kf_state, InertialLin<double> lin,
                                   double* cost_accum, int* status, const int* skip_if, cudaStream_t s,
                                   bool f32 = false, const double* sw_state = nullptr);
+// obs_inv: caller index -> sorted index (launch_invert_perm).  Destinations
+// may be device or mapped page-locked host memory.
 template <typename T>
-cudaError_t launch_gather_visual(const DevProblem& P, VisualLin<T> v, double* r, double* Jl, double* Js, double* Jo,
-                                 cudaStream_t s);
+cudaError_t launch_gather_visual(const DevProblem& P, const int64_t* obs_inv, VisualLin<T> v, double* r, double* Jl,
+                                 double* Js, double* Jo, cudaStream_t s);
+cudaError_t launch_invert_perm(const DevProblem& P, int64_t* inv, cudaStream_t s);
 // to_device = 1: host-layout device arrays -> kf_state / lm_p; 0: the reverse.
 cudaError_t launch_pack_state(const DevProblem& P, const double* kx, const double* kv, const double* kbg,
                               const double* kba, const double* lp, int to_device, cudaStream_t s);

@@ -9,6 +9,8 @@
 //   (algorithms/imu-integrator-rk4/include/imu-integrator/imu-integrator-inl.h:17-334).
 #include <cuda_runtime.h>
 
+#include <algorithm>
+
 #include "internal.h"
 
 namespace mba {
@@ -94,8 +96,197 @@ __device__ __forceinline__ void rot_basis(const DevProblem& P, const S* mis, int
 // Tangent-space, Huber-corrected linearization of every observation.  kCost
 // adds the FP64 cost reduction (FP64 path only): the FP32 instantiation reads
 // the FP32 mirrors and executes no FP64 instruction.
-// kMinBlocks > 1 trades registers (spilled to L1) for resident warps;
-// the autotuner picks the variant per problem.
+//
+// The global reads of one observation are split in two stages so that a
+// pipelined loop can overlap them with the arithmetic of the previous
+// observation: load_obs_stream (the observation's own streamed fields,
+// coalesced) and load_obs_gather (landmark and keyframe poses addressed by
+// them).  compute_obs holds the arithmetic and the stores.
+template <typename T>
+struct ObsInputs {
+  typename Vec2<T>::type uv;
+  T sinv, ha;
+  T pB[3];
+  T xs[7], xo[7];  // store / observer pose q | p
+  int lm, kf, st, type, cam;
+  int lm_off, lm_active;
+};
+
+template <typename T>
+__device__ __forceinline__ void load_obs_stream(const DevProblem& P, const VisualInputs<T>& in, int64_t i,
+                                                ObsInputs<T>& o) {
+  o.lm = P.obs_lm[i];
+  o.kf = P.obs_kf[i];
+  o.st = P.obs_store[i];
+  o.type = P.obs_type[i];
+  o.cam = P.obs_cam[i];
+  o.uv = in.uv[i];
+  o.sinv = in.sinv[i];
+  o.ha = in.huber[i];
+}
+
+template <typename T>
+__device__ __forceinline__ void load_obs_gather(const DevProblem& P, const VisualInputs<T>& in, ObsInputs<T>& o) {
+  const T* lp = in.lm_p + 4 * (int64_t)o.lm;
+  o.pB[0] = lp[0]; o.pB[1] = lp[1]; o.pB[2] = lp[2];
+  o.lm_off = P.lm_off[o.lm];
+  o.lm_active = P.lm_active[o.lm];
+  if (o.type != MBA_LOCAL_KEYFRAME) {
+    const T* xs = in.kf + (int64_t)in.kf_stride * o.st;
+    const T* xo = in.kf + (int64_t)in.kf_stride * o.kf;
+#pragma unroll
+    for (int a = 0; a < 7; ++a) { o.xs[a] = xs[a]; o.xo[a] = xo[a]; }
+  }
+}
+
+// Arithmetic and stores of observation i; returns its cost (kCost).
+template <typename T, bool kCost>
+__device__ __forceinline__ double compute_obs(const DevProblem& P, const VisualInputs<T>& in, const ObsInputs<T>& o,
+                                              const VisualLin<T>& out, int64_t i, int64_t N) {
+  double cost = 0.0;
+  const int kf = o.kf, st = o.st, type = o.type;
+  const DevCameraT<T>& cam = in.cams[o.cam];
+  const auto uv = o.uv;
+  const T sinv = o.sinv;
+  const T ha = o.ha;
+  const T pB[3] = {o.pB[0], o.pB[1], o.pB[2]};
+  M3<T> RCI;
+  jplR(cam.q_CI, RCI);
+  T pI[3];
+  M3<T> RIM, RBLM, RMG, RGLM;
+  T qst[4], qob[4], pLMB[3], pMI[3];
+  if (type == MBA_LOCAL_KEYFRAME) {
+    pI[0] = pB[0]; pI[1] = pB[1]; pI[2] = pB[2];
+  } else {
+#pragma unroll
+    for (int a = 0; a < 4; ++a) { qst[a] = o.xs[a]; qob[a] = o.xo[a]; }
+    pLMB[0] = o.xs[4]; pLMB[1] = o.xs[5]; pLMB[2] = o.xs[6];
+    pMI[0] = o.xo[4]; pMI[1] = o.xo[5]; pMI[2] = o.xo[6];
+    jplR(qst, RBLM);
+    jplR(qob, RIM);
+    T pM[3];
+    mtv3(RBLM, pB, pM);  // R_LM_B p_B
+    pM[0] += pLMB[0]; pM[1] += pLMB[1]; pM[2] += pLMB[2];
+    if (type == MBA_GLOBAL) {
+      const T* ml = in.mis + 8 * P.kf_mis[st];
+      const T* mo = in.mis + 8 * P.kf_mis[kf];
+      jplR(ml, RGLM);
+      M3<T> RGM;
+      jplR(mo, RGM);
+      T pG[3];
+      mv3(RGLM, pM, pG);
+      pG[0] += ml[4] - mo[4]; pG[1] += ml[5] - mo[5]; pG[2] += ml[6] - mo[6];
+      mtv3(RGM, pG, pM);  // R_M_G (p_G - p_G_M)
+#pragma unroll
+      for (int a = 0; a < 3; ++a)
+#pragma unroll
+        for (int b = 0; b < 3; ++b) RMG.m[3 * a + b] = RGM.m[3 * b + a];
+    }
+    T d[3] = {pM[0] - pMI[0], pM[1] - pMI[1], pM[2] - pMI[2]};
+    mv3(RIM, d, pI);
+  }
+  T pC[3];
+  mv3(RCI, pI, pC);
+  pC[0] += cam.p_CI[0]; pC[1] += cam.p_CI[1]; pC[2] += cam.p_CI[2];
+  T kp[2], Jkp[6];
+  const bool failed = project<T>(cam, pC, kp, Jkp) || o.lm_off;
+  T r[2], Jl[6], Js[12], Jo[12];
+#pragma unroll
+  for (int a = 0; a < 12; ++a) { Js[a] = T(0); Jo[a] = T(0); }
+  if (failed) {
+    r[0] = r[1] = T(0);
+#pragma unroll
+    for (int a = 0; a < 6; ++a) Jl[a] = T(0);
+  } else {
+    r[0] = (kp[0] - uv.x) * sinv;
+    r[1] = (kp[1] - uv.y) * sinv;
+    T A[6];
+    m23x33(Jkp, RCI, A);  // Jkp * R_C_I
+    if (type == MBA_LOCAL_KEYFRAME) {
+#pragma unroll
+      for (int a = 0; a < 6; ++a) Jl[a] = A[a] * sinv;
+    } else {
+      T B[6], Cp[6];
+      m23x33(A, RIM, B);  // Jkp R_C_I R_I_M  (= -J_p_M_I)
+      if (type == MBA_LOCAL_MISSION) {
+#pragma unroll
+        for (int a = 0; a < 6; ++a) Cp[a] = B[a];
+      } else {
+        T D[6];
+        m23x33(B, RMG, D);   // J_p_G_LM
+        m23x33(D, RGLM, Cp); // J_p_LM_B
+      }
+      // J_p_B = J_p_LM_B * R_LM_B  (R_LM_B = R_B_LM^T)
+      T JpB[6];
+#pragma unroll
+      for (int rr = 0; rr < 2; ++rr)
+#pragma unroll
+        for (int c = 0; c < 3; ++c)
+          JpB[3 * rr + c] = Cp[3 * rr] * RBLM.m[3 * c] + Cp[3 * rr + 1] * RBLM.m[3 * c + 1] + Cp[3 * rr + 2] * RBLM.m[3 * c + 2];
+      T Jqs[6], Jqo[6];
+      m23xskew(JpB, pB, Jqs);  // -J_q_B_LM
+      m23xskew(A, pI, Jqo);    // J_q_I_M
+      M3<T> Bs, Bo;
+      rot_basis<T>(P, in.mis, st, qst, RBLM, Bs);
+      rot_basis<T>(P, in.mis, kf, qob, RIM, Bo);
+      const uint16_t ms = P.kf_mask[st], mo = P.kf_mask[kf];
+#pragma unroll
+      for (int rr = 0; rr < 2; ++rr) {
+#pragma unroll
+        for (int c = 0; c < 3; ++c) {
+          Js[6 * rr + c] = -(Jqs[3 * rr] * Bs.m[c] + Jqs[3 * rr + 1] * Bs.m[3 + c] + Jqs[3 * rr + 2] * Bs.m[6 + c]) * sinv;
+          Jo[6 * rr + c] = (Jqo[3 * rr] * Bo.m[c] + Jqo[3 * rr + 1] * Bo.m[3 + c] + Jqo[3 * rr + 2] * Bo.m[6 + c]) * sinv;
+          Js[6 * rr + 3 + c] = (ms & (8u << c)) ? Cp[3 * rr + c] * sinv : T(0);
+          Jo[6 * rr + 3 + c] = (mo & (8u << c)) ? -B[3 * rr + c] * sinv : T(0);
+        }
+      }
+#pragma unroll
+      for (int a = 0; a < 6; ++a) Jl[a] = JpB[a] * sinv;
+    }
+    if (!o.lm_active) {
+#pragma unroll
+      for (int a = 0; a < 6; ++a) Jl[a] = T(0);
+    }
+  }
+  const T s = r[0] * r[0] + r[1] * r[1];
+  if (ha > T(0)) {
+    T rho0, sq1, rs, as;
+    huber_corrector<T>(ha, s, &rho0, &sq1, &rs, &as);
+    if (kCost) cost = 0.5 * double(rho0);
+    // J' = sq1 (J - as r (r^T J)), r' = rs r
+#pragma unroll
+    for (int c = 0; c < 3; ++c) {
+      const T t = r[0] * Jl[c] + r[1] * Jl[3 + c];
+      Jl[c] = sq1 * (Jl[c] - as * r[0] * t);
+      Jl[3 + c] = sq1 * (Jl[3 + c] - as * r[1] * t);
+    }
+#pragma unroll
+    for (int c = 0; c < 6; ++c) {
+      const T t = r[0] * Js[c] + r[1] * Js[6 + c];
+      Js[c] = sq1 * (Js[c] - as * r[0] * t);
+      Js[6 + c] = sq1 * (Js[6 + c] - as * r[1] * t);
+      const T u = r[0] * Jo[c] + r[1] * Jo[6 + c];
+      Jo[c] = sq1 * (Jo[c] - as * r[0] * u);
+      Jo[6 + c] = sq1 * (Jo[6 + c] - as * r[1] * u);
+    }
+    r[0] *= rs;
+    r[1] *= rs;
+  } else if (kCost) {
+    cost = 0.5 * double(s);
+  }
+  out.r[i] = r[0];
+  out.r[N + i] = r[1];
+#pragma unroll
+  for (int a = 0; a < 6; ++a) out.Jl[a * N + i] = Jl[a];
+#pragma unroll
+  for (int a = 0; a < 12; ++a) out.Js[a * N + i] = Js[a];
+#pragma unroll
+  for (int a = 0; a < 12; ++a) out.Jo[a * N + i] = Jo[a];
+  return cost;
+}
+
+// One thread per observation.  kMinBlocks > 1 trades registers (spilled to
+// L1) for resident warps; the autotuner picks the variant per problem.
 template <typename T, bool kCost, int kMinBlocks>
 __global__ void __launch_bounds__(kBlock, kMinBlocks) k_visual_linearize(DevProblem P, VisualInputs<T> in, VisualLin<T> out,
                                                              double* cost_accum, const int* run_if,
@@ -104,151 +295,42 @@ __global__ void __launch_bounds__(kBlock, kMinBlocks) k_visual_linearize(DevProb
   const int64_t i = blockIdx.x * (int64_t)blockDim.x + threadIdx.x;
   double cost = 0.0;
   if (i < P.nobs) {
-    const int64_t N = P.nobs;
-    const int lm = P.obs_lm[i];
-    const int kf = P.obs_kf[i];
-    const int st = P.obs_store[i];
-    const int type = P.obs_type[i];
-    const DevCameraT<T>& cam = in.cams[P.obs_cam[i]];
-    const auto uv = in.uv[i];
-    const T sinv = in.sinv[i];
-    const T ha = in.huber[i];
-    const T* lp = in.lm_p + 4 * (int64_t)lm;
-    const T pB[3] = {lp[0], lp[1], lp[2]};
-    M3<T> RCI;
-    jplR(cam.q_CI, RCI);
-    T pI[3];
-    M3<T> RIM, RBLM, RMG, RGLM;
-    T qst[4], qob[4], pLMB[3], pMI[3];
-    if (type == MBA_LOCAL_KEYFRAME) {
-      pI[0] = pB[0]; pI[1] = pB[1]; pI[2] = pB[2];
-    } else {
-      const T* xs = in.kf + (int64_t)in.kf_stride * st;
-      const T* xo = in.kf + (int64_t)in.kf_stride * kf;
-#pragma unroll
-      for (int a = 0; a < 4; ++a) { qst[a] = xs[a]; qob[a] = xo[a]; }
-      pLMB[0] = xs[4]; pLMB[1] = xs[5]; pLMB[2] = xs[6];
-      pMI[0] = xo[4]; pMI[1] = xo[5]; pMI[2] = xo[6];
-      jplR(qst, RBLM);
-      jplR(qob, RIM);
-      T pM[3];
-      mtv3(RBLM, pB, pM);  // R_LM_B p_B
-      pM[0] += pLMB[0]; pM[1] += pLMB[1]; pM[2] += pLMB[2];
-      if (type == MBA_GLOBAL) {
-        const T* ml = in.mis + 8 * P.kf_mis[st];
-        const T* mo = in.mis + 8 * P.kf_mis[kf];
-        jplR(ml, RGLM);
-        M3<T> RGM;
-        jplR(mo, RGM);
-        T pG[3];
-        mv3(RGLM, pM, pG);
-        pG[0] += ml[4] - mo[4]; pG[1] += ml[5] - mo[5]; pG[2] += ml[6] - mo[6];
-        mtv3(RGM, pG, pM);  // R_M_G (p_G - p_G_M)
-#pragma unroll
-        for (int a = 0; a < 3; ++a)
-#pragma unroll
-          for (int b = 0; b < 3; ++b) RMG.m[3 * a + b] = RGM.m[3 * b + a];
-      }
-      T d[3] = {pM[0] - pMI[0], pM[1] - pMI[1], pM[2] - pMI[2]};
-      mv3(RIM, d, pI);
-    }
-    T pC[3];
-    mv3(RCI, pI, pC);
-    pC[0] += cam.p_CI[0]; pC[1] += cam.p_CI[1]; pC[2] += cam.p_CI[2];
-    T kp[2], Jkp[6];
-    const bool failed = project<T>(cam, pC, kp, Jkp) || P.lm_off[lm];
-    T r[2], Jl[6], Js[12], Jo[12];
-#pragma unroll
-    for (int a = 0; a < 12; ++a) { Js[a] = T(0); Jo[a] = T(0); }
-    if (failed) {
-      r[0] = r[1] = T(0);
-#pragma unroll
-      for (int a = 0; a < 6; ++a) Jl[a] = T(0);
-    } else {
-      r[0] = (kp[0] - uv.x) * sinv;
-      r[1] = (kp[1] - uv.y) * sinv;
-      T A[6];
-      m23x33(Jkp, RCI, A);  // Jkp * R_C_I
-      if (type == MBA_LOCAL_KEYFRAME) {
-#pragma unroll
-        for (int a = 0; a < 6; ++a) Jl[a] = A[a] * sinv;
-      } else {
-        T B[6], Cp[6];
-        m23x33(A, RIM, B);  // Jkp R_C_I R_I_M  (= -J_p_M_I)
-        if (type == MBA_LOCAL_MISSION) {
-#pragma unroll
-          for (int a = 0; a < 6; ++a) Cp[a] = B[a];
-        } else {
-          T D[6];
-          m23x33(B, RMG, D);   // J_p_G_LM
-          m23x33(D, RGLM, Cp); // J_p_LM_B
-        }
-        // J_p_B = J_p_LM_B * R_LM_B  (R_LM_B = R_B_LM^T)
-        T JpB[6];
-#pragma unroll
-        for (int rr = 0; rr < 2; ++rr)
-#pragma unroll
-          for (int c = 0; c < 3; ++c)
-            JpB[3 * rr + c] = Cp[3 * rr] * RBLM.m[3 * c] + Cp[3 * rr + 1] * RBLM.m[3 * c + 1] + Cp[3 * rr + 2] * RBLM.m[3 * c + 2];
-        T Jqs[6], Jqo[6];
-        m23xskew(JpB, pB, Jqs);  // -J_q_B_LM
-        m23xskew(A, pI, Jqo);    // J_q_I_M
-        M3<T> Bs, Bo;
-        rot_basis<T>(P, in.mis, st, qst, RBLM, Bs);
-        rot_basis<T>(P, in.mis, kf, qob, RIM, Bo);
-        const uint16_t ms = P.kf_mask[st], mo = P.kf_mask[kf];
-#pragma unroll
-        for (int rr = 0; rr < 2; ++rr) {
-#pragma unroll
-          for (int c = 0; c < 3; ++c) {
-            Js[6 * rr + c] = -(Jqs[3 * rr] * Bs.m[c] + Jqs[3 * rr + 1] * Bs.m[3 + c] + Jqs[3 * rr + 2] * Bs.m[6 + c]) * sinv;
-            Jo[6 * rr + c] = (Jqo[3 * rr] * Bo.m[c] + Jqo[3 * rr + 1] * Bo.m[3 + c] + Jqo[3 * rr + 2] * Bo.m[6 + c]) * sinv;
-            Js[6 * rr + 3 + c] = (ms & (8u << c)) ? Cp[3 * rr + c] * sinv : T(0);
-            Jo[6 * rr + 3 + c] = (mo & (8u << c)) ? -B[3 * rr + c] * sinv : T(0);
-          }
-        }
-#pragma unroll
-        for (int a = 0; a < 6; ++a) Jl[a] = JpB[a] * sinv;
-      }
-      if (!P.lm_active[lm]) {
-#pragma unroll
-        for (int a = 0; a < 6; ++a) Jl[a] = T(0);
-      }
-    }
-    const T s = r[0] * r[0] + r[1] * r[1];
-    if (ha > T(0)) {
-      T rho0, sq1, rs, as;
-      huber_corrector<T>(ha, s, &rho0, &sq1, &rs, &as);
-      if (kCost) cost = 0.5 * double(rho0);
-      // J' = sq1 (J - as r (r^T J)), r' = rs r
-#pragma unroll
-      for (int c = 0; c < 3; ++c) {
-        const T t = r[0] * Jl[c] + r[1] * Jl[3 + c];
-        Jl[c] = sq1 * (Jl[c] - as * r[0] * t);
-        Jl[3 + c] = sq1 * (Jl[3 + c] - as * r[1] * t);
-      }
-#pragma unroll
-      for (int c = 0; c < 6; ++c) {
-        const T t = r[0] * Js[c] + r[1] * Js[6 + c];
-        Js[c] = sq1 * (Js[c] - as * r[0] * t);
-        Js[6 + c] = sq1 * (Js[6 + c] - as * r[1] * t);
-        const T u = r[0] * Jo[c] + r[1] * Jo[6 + c];
-        Jo[c] = sq1 * (Jo[c] - as * r[0] * u);
-        Jo[6 + c] = sq1 * (Jo[6 + c] - as * r[1] * u);
-      }
-      r[0] *= rs;
-      r[1] *= rs;
-    } else if (kCost) {
-      cost = 0.5 * double(s);
-    }
-    out.r[i] = r[0];
-    out.r[N + i] = r[1];
-#pragma unroll
-    for (int a = 0; a < 6; ++a) out.Jl[a * N + i] = Jl[a];
-#pragma unroll
-    for (int a = 0; a < 12; ++a) out.Js[a * N + i] = Js[a];
-#pragma unroll
-    for (int a = 0; a < 12; ++a) out.Jo[a * N + i] = Jo[a];
+    ObsInputs<T> o;
+    load_obs_stream(P, in, i, o);
+    load_obs_gather(P, in, o);
+    cost = compute_obs<T, kCost>(P, in, o, out, i, P.nobs);
+  }
+  if (kCost) block_accumulate(cost, cost_accum);
+}
+
+// Persistent, software-pipelined: a grid of resident blocks strides over the
+// observations; while observation i is computed, the gathers of i + stride
+// (whose indices arrived during the previous iteration) and the streamed
+// fields of i + 2 stride are in flight.  Three observations per thread are in
+// the memory system at once instead of one.  kMinBlocks = 2 caps the
+// registers (more resident warps, some spilling).
+template <typename T, bool kCost, int kMinBlocks>
+__global__ void __launch_bounds__(kBlock, kMinBlocks) k_visual_linearize_pipe(DevProblem P, VisualInputs<T> in, VisualLin<T> out,
+                                                                  double* cost_accum, const int* run_if,
+                                                                  const int* skip_if) {
+  if (gated(run_if, skip_if)) return;
+  const int64_t N = P.nobs, stride = (int64_t)gridDim.x * blockDim.x;
+  int64_t i = blockIdx.x * (int64_t)blockDim.x + threadIdx.x;
+  double cost = 0.0;
+  ObsInputs<T> cur, nxt;
+  if (i < N) {
+    load_obs_stream(P, in, i, cur);
+    load_obs_gather(P, in, cur);
+  }
+  if (i + stride < N) load_obs_stream(P, in, i + stride, nxt);
+  for (; i < N; i += stride) {
+    const int64_t j = i + stride;
+    if (j < N) load_obs_gather(P, in, nxt);
+    ObsInputs<T> nn;
+    if (j + stride < N) load_obs_stream(P, in, j + stride, nn);
+    cost += compute_obs<T, kCost>(P, in, cur, out, i, N);
+    cur = nxt;
+    nxt = nn;
   }
   if (kCost) block_accumulate(cost, cost_accum);
 }
@@ -599,6 +681,20 @@ cudaError_t launch_visual_linearize_gated(const DevProblem& P, VisualLin<T> out,
   if (P.nobs == 0) return cudaSuccess;
   // Block size: tuned per problem (mba_autotune), at most the launch bound.
   const int bs = (P.vis_block > 0 && P.vis_block <= kBlock) ? P.vis_block : kBlock;
+  if (P.vis_pipe) {
+    // Pipelined persistent variant: as many blocks as stay resident.
+    int per_sm = 0, sms = 0, dev = 0;
+    cudaGetDevice(&dev);
+    cudaDeviceGetAttribute(&sms, cudaDevAttrMultiProcessorCount, dev);
+    const bool capped = P.vis_minb == 2;
+    auto kern = cost_accum ? (capped ? k_visual_linearize_pipe<T, true, 2> : k_visual_linearize_pipe<T, true, 1>)
+                           : (capped ? k_visual_linearize_pipe<T, false, 2> : k_visual_linearize_pipe<T, false, 1>);
+    cudaOccupancyMaxActiveBlocksPerMultiprocessor(&per_sm, kern, bs, 0);
+    const int64_t need = (P.nobs + bs - 1) / bs;
+    const int64_t grid = std::min<int64_t>(need, (int64_t)std::max(1, per_sm) * std::max(1, sms));
+    kern<<<(unsigned)grid, bs, 0, s>>>(P, visual_inputs<T>(P), out, cost_accum, run_if, skip_if);
+    return cudaGetLastError();
+  }
   const int64_t blocks = (P.nobs + bs - 1) / bs;
   const bool lean = P.vis_minb > 1;
   if (cost_accum) {
@@ -683,16 +779,37 @@ cudaError_t launch_inertial_f32(const DevProblem& P, const InertialLin<double>& 
 }
 
 namespace {
+// Caller-order rows of the linearization in FP64: r [N][2], J_l [N][6],
+// J_s [N][12], J_o [N][12] (each may be null).  A block takes kGatherRows
+// consecutive caller indices o, reads sorted index inv[o] from the SoA
+// buffers, stages the rows in shared memory (component-major, conflict-free)
+// and writes each array's part as one contiguous run, so that the stores
+// coalesce also when the destination is page-locked host memory.
+constexpr int kGatherRows = 128;
 template <typename T>
-__global__ void k_gather_visual(int64_t N, const int64_t* perm, VisualLin<T> v, double* r, double* Jl, double* Js,
-                                double* Jo) {
-  const int64_t i = blockIdx.x * (int64_t)blockDim.x + threadIdx.x;
-  if (i >= N) return;
-  const int64_t o = perm[i];
-  if (r) for (int c = 0; c < 2; ++c) r[2 * o + c] = (double)v.r[c * N + i];
-  if (Jl) for (int c = 0; c < 6; ++c) Jl[6 * o + c] = (double)v.Jl[c * N + i];
-  if (Js) for (int c = 0; c < 12; ++c) Js[12 * o + c] = (double)v.Js[c * N + i];
-  if (Jo) for (int c = 0; c < 12; ++c) Jo[12 * o + c] = (double)v.Jo[c * N + i];
+__global__ void __launch_bounds__(kGatherRows) k_gather_rows(int64_t N, const int64_t* inv, VisualLin<T> v, double* r,
+                                                             double* Jl, double* Js, double* Jo) {
+  __shared__ double sh[32 * kGatherRows];
+  const int64_t base = (int64_t)blockIdx.x * kGatherRows;
+  const int t = threadIdx.x;
+  const int cnt = (int)(N - base < kGatherRows ? N - base : kGatherRows);
+  if (t < cnt) {
+    const int64_t i = inv[base + t];
+    if (r) for (int c = 0; c < 2; ++c) sh[c * kGatherRows + t] = (double)v.r[c * N + i];
+    if (Jl) for (int c = 0; c < 6; ++c) sh[(2 + c) * kGatherRows + t] = (double)v.Jl[c * N + i];
+    if (Js) for (int c = 0; c < 12; ++c) sh[(8 + c) * kGatherRows + t] = (double)v.Js[c * N + i];
+    if (Jo) for (int c = 0; c < 12; ++c) sh[(20 + c) * kGatherRows + t] = (double)v.Jo[c * N + i];
+  }
+  __syncthreads();
+  double* dst[4] = {r, Jl, Js, Jo};
+  const int width[4] = {2, 6, 12, 12}, first[4] = {0, 2, 8, 20};
+#pragma unroll
+  for (int a = 0; a < 4; ++a) {
+    if (!dst[a]) continue;
+    const int w = width[a];
+    double* out = dst[a] + base * w;
+    for (int k = t; k < cnt * w; k += kGatherRows) out[k] = sh[(first[a] + k % w) * kGatherRows + k / w];
+  }
 }
 
 __global__ void k_pack_state(int64_t NK, int64_t NL, double* kf_state, double* lm_p, float* kf_pose_f, float* lm_p_f,
@@ -735,16 +852,30 @@ __global__ void k_pack_state(int64_t NK, int64_t NL, double* kf_state, double* l
 }  // namespace
 
 template <typename T>
-cudaError_t launch_gather_visual(const DevProblem& P, VisualLin<T> v, double* r, double* Jl, double* Js, double* Jo,
-                                 cudaStream_t s) {
+cudaError_t launch_gather_visual(const DevProblem& P, const int64_t* obs_inv, VisualLin<T> v, double* r, double* Jl,
+                                 double* Js, double* Jo, cudaStream_t s) {
   if (P.nobs == 0) return cudaSuccess;
-  k_gather_visual<T><<<(unsigned)((P.nobs + 255) / 256), 256, 0, s>>>(P.nobs, P.obs_perm, v, r, Jl, Js, Jo);
+  k_gather_rows<T><<<(unsigned)((P.nobs + kGatherRows - 1) / kGatherRows), kGatherRows, 0, s>>>(P.nobs, obs_inv, v, r,
+                                                                                                  Jl, Js, Jo);
   return cudaGetLastError();
 }
-template cudaError_t launch_gather_visual<double>(const DevProblem&, VisualLin<double>, double*, double*, double*,
-                                                  double*, cudaStream_t);
-template cudaError_t launch_gather_visual<float>(const DevProblem&, VisualLin<float>, double*, double*, double*,
-                                                 double*, cudaStream_t);
+template cudaError_t launch_gather_visual<double>(const DevProblem&, const int64_t*, VisualLin<double>, double*,
+                                                  double*, double*, double*, cudaStream_t);
+template cudaError_t launch_gather_visual<float>(const DevProblem&, const int64_t*, VisualLin<float>, double*, double*,
+                                                 double*, double*, cudaStream_t);
+
+namespace {
+__global__ void k_invert_perm(int64_t N, const int64_t* perm, int64_t* inv) {
+  const int64_t i = blockIdx.x * (int64_t)blockDim.x + threadIdx.x;
+  if (i < N) inv[perm[i]] = i;
+}
+}  // namespace
+
+cudaError_t launch_invert_perm(const DevProblem& P, int64_t* inv, cudaStream_t s) {
+  if (P.nobs == 0) return cudaSuccess;
+  k_invert_perm<<<(unsigned)((P.nobs + 255) / 256), 256, 0, s>>>(P.nobs, P.obs_perm, inv);
+  return cudaGetLastError();
+}
 
 cudaError_t launch_pack_state(const DevProblem& P, const double* kx, const double* kv, const double* kbg,
                               const double* kba, const double* lp, int to_device, cudaStream_t s) {

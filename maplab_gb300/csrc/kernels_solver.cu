@@ -464,7 +464,6 @@ __global__ void __launch_bounds__(kB) k_schur_pairs(SolverLaunch<T> s) {
   }
 }
 
-// Masked tangent dims -> identity rows; mirror SP to the lower orientation.
 // Switch elimination (one warp per switch variable): H = h + damping,
 // SD_ff -= W_f W_f^T / H, SD_tt -= W_t W_t^T / H, SE -= W_f W_t^T / H,
 // rhs += W g / H.  H is inverted in FP64.
@@ -495,6 +494,7 @@ __global__ void __launch_bounds__(128) k_schur_switch(SolverLaunch<T> s) {
   }
 }
 
+// Masked tangent dims -> identity rows; mirror SP to the lower orientation.
 template <typename T>
 __global__ void __launch_bounds__(kB) k_finalize_system(SolverLaunch<T> s) {
   if (s.ctl->terminated) return;

@@ -165,6 +165,7 @@ struct mba_handle {
   // staging in the caller's layout (lazily allocated)
   double* stage_state = nullptr;  // 16 NK + 3 NL
   double* stage_lin = nullptr;    // 32 N
+  int64_t* obs_inv = nullptr;     // [N] caller observation index -> sorted index
   char* l2_flush = nullptr;       // buffer larger than L2 for timing hygiene
   // learned preconditioner
   GnnGraph gg{};
@@ -681,12 +682,48 @@ void unpermute_soa(const std::vector<double>& sorted_soa, int64_t N, int comps, 
   }
 }
 
+// Device address of a page-locked host range [p, p + bytes) of one mapping,
+// or null (pageable or unknown memory, or a range that leaves the mapping).
+void* mapped_host_range(void* p, size_t bytes) {
+  if (!p || bytes == 0) return nullptr;
+  cudaPointerAttributes a{}, z{};
+  if (cudaPointerGetAttributes(&a, p) != cudaSuccess) { cudaGetLastError(); return nullptr; }
+  if (a.type != cudaMemoryTypeHost || !a.devicePointer) return nullptr;
+  char* last = static_cast<char*>(p) + bytes - 1;
+  if (cudaPointerGetAttributes(&z, last) != cudaSuccess) { cudaGetLastError(); return nullptr; }
+  if (z.type != cudaMemoryTypeHost || z.devicePointer != static_cast<char*>(a.devicePointer) + bytes - 1) return nullptr;
+  return a.devicePointer;
+}
+
 template <typename T>
 mba_status linearize_visual_host(mba_handle* h, double* r, double* Jl, double* Js, double* Jo) {
   SolverBuffers<T>& b = buffers_of<T>(h);
   mba_status ms = ensure_solver_buffers<T>(h, b);
   if (ms != MBA_OK) return ms;
   const int64_t N = h->P.nobs;
+  cudaStream_t st = h->stream;
+  if (!h->obs_inv) {
+    h->obs_inv = h->arena.alloc<int64_t>(N);
+    if (h->arena.err != cudaSuccess) return MBA_ERR_CUDA;
+    if (launch_invert_perm(h->P, h->obs_inv, st) != cudaSuccess) return MBA_ERR_CUDA;
+  }
+  // Page-locked host destinations are written by the gather kernel over the
+  // host link directly (one pass, no HBM staging, no separate copies).
+  double* out[4] = {r, Jl, Js, Jo};
+  const int64_t width[4] = {2, 6, 12, 12};
+  double* mapped[4] = {nullptr, nullptr, nullptr, nullptr};
+  bool direct = true;
+  for (int a = 0; a < 4; ++a) {
+    if (!out[a]) continue;
+    mapped[a] = static_cast<double*>(mapped_host_range(out[a], sizeof(double) * width[a] * N));
+    direct = direct && mapped[a];
+  }
+  cudaError_t e = launch_visual_linearize<T>(h->P, b.vis, nullptr, st);
+  if (direct) {
+    if (e == cudaSuccess) e = launch_gather_visual<T>(h->P, h->obs_inv, b.vis, mapped[0], mapped[1], mapped[2], mapped[3], st);
+    if (e == cudaSuccess) e = cudaStreamSynchronize(st);
+    return cuda_status(e);
+  }
   if (!h->stage_lin) {
     h->stage_lin = h->arena.alloc<double>(32 * N);
     if (h->arena.err != cudaSuccess) return MBA_ERR_CUDA;
@@ -695,10 +732,8 @@ mba_status linearize_visual_host(mba_handle* h, double* r, double* Jl, double* J
   double* dJl = dr + 2 * N;
   double* dJs = dJl + 6 * N;
   double* dJo = dJs + 12 * N;
-  cudaStream_t st = h->stream;
-  cudaError_t e = launch_visual_linearize<T>(h->P, b.vis, nullptr, st);
   if (e == cudaSuccess)
-    e = launch_gather_visual<T>(h->P, b.vis, r ? dr : nullptr, Jl ? dJl : nullptr, Js ? dJs : nullptr,
+    e = launch_gather_visual<T>(h->P, h->obs_inv, b.vis, r ? dr : nullptr, Jl ? dJl : nullptr, Js ? dJs : nullptr,
                                 Jo ? dJo : nullptr, st);
   if (e == cudaSuccess && r) e = cudaMemcpyAsync(r, dr, sizeof(double) * 2 * N, cudaMemcpyDeviceToHost, st);
   if (e == cudaSuccess && Jl) e = cudaMemcpyAsync(Jl, dJl, sizeof(double) * 6 * N, cudaMemcpyDeviceToHost, st);
@@ -1269,6 +1304,7 @@ mba_status mba_create(const mba_problem_desc* d, int32_t device, mba_handle** ou
     ++S.chain_tail;
   h->tuning.visual_block = 256;
   h->tuning.visual_min_blocks = 1;
+  h->tuning.visual_pipelined = 2;
   h->tuning.schur_chunk = (int32_t)kSchurChunk;
   h->tuning.chain_tail_nodes = 128;
   // Inertial scratch (kernels_inertial.cu): dt per step, end state per edge,
@@ -1857,18 +1893,30 @@ mba_status autotune(mba_handle* h, mba_tuning* out) {
   if (e == cudaSuccess) e = cudaStreamSynchronize(st);
   if (e != cudaSuccess) return MBA_ERR_CUDA;
   mba_tuning best = h->tuning;
-  // evaluation kernel block size
+  // evaluation kernel: one thread per observation (plain or register-lean)
+  // or the pipelined persistent loop, and the block size
   double tbest = 1e30;
-  for (int minb : {1, 3})
-    for (int bs : {64, 128, 256}) {
-      DevProblem P = h->P;
-      P.vis_block = bs;
-      P.vis_minb = minb;
-      const double t = time_ms(st, 2, 8, [&]() { launch_visual_linearize<T>(P, b.vis, nullptr, st); });
-      if (t < tbest) { tbest = t; best.visual_block = bs; best.visual_min_blocks = minb; best.visual_ms = t; }
+  for (int pipe : {0, 1})
+    for (int minb : {1, 2, 3}) {
+      if (pipe ? minb == 3 : minb == 2) continue;  // one-per-thread: 1 or 3 blocks; pipelined: 1 or 2
+      for (int bs : {64, 128, 256}) {
+        DevProblem P = h->P;
+        P.vis_block = bs;
+        P.vis_minb = minb;
+        P.vis_pipe = pipe;
+        const double t = time_ms(st, 2, 8, [&]() { launch_visual_linearize<T>(P, b.vis, nullptr, st); });
+        if (t < tbest) {
+          tbest = t;
+          best.visual_block = bs;
+          best.visual_min_blocks = minb;
+          best.visual_pipelined = pipe ? 1 : 2;
+          best.visual_ms = t;
+        }
+      }
     }
   h->P.vis_block = best.visual_block;
   h->P.vis_minb = best.visual_min_blocks;
+  h->P.vis_pipe = best.visual_pipelined == 1;
   // Schur pairs per thread
   tbest = 1e30;
   for (int chunk : {4, 8, 16, 32, 64}) {
@@ -1913,9 +1961,14 @@ mba_status mba_set_tuning(mba_handle* h, const mba_tuning* t) {
   cudaSetDevice(h->device);
   if (t->visual_block) { h->P.vis_block = t->visual_block; h->tuning.visual_block = t->visual_block; }
   if (t->visual_min_blocks) {
-    if (t->visual_min_blocks != 1 && t->visual_min_blocks != 3) return MBA_ERR_INVALID_ARG;
+    if (t->visual_min_blocks < 1 || t->visual_min_blocks > 3) return MBA_ERR_INVALID_ARG;
     h->P.vis_minb = t->visual_min_blocks;
     h->tuning.visual_min_blocks = t->visual_min_blocks;
+  }
+  if (t->visual_pipelined) {
+    if (t->visual_pipelined != 1 && t->visual_pipelined != 2) return MBA_ERR_INVALID_ARG;
+    h->P.vis_pipe = t->visual_pipelined == 1;
+    h->tuning.visual_pipelined = t->visual_pipelined;
   }
   if (t->schur_chunk && t->schur_chunk != h->tuning.schur_chunk) {
     mba_status ms = apply_schur_chunk(h, t->schur_chunk);
