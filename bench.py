@@ -173,7 +173,7 @@ def ba_time_to_cost(args, device):
     g32 = ba.BundleAdjuster(d, device=device)
     if model is not None:
         g32.set_preconditioner_model(model)
-    g32.autotune(N.MBA_PRECISION_MIXED)
+    tun32 = g32.autotune(N.MBA_PRECISION_MIXED)
     s32 = g32.solve(ba.default_options(max_num_iterations=40, max_linear_iterations=args.fast_pcg, stop_cost=target,
                                        precision=N.MBA_PRECISION_MIXED, preconditioner=pre, use_cuda_graph=2,
                                        **common))
@@ -197,6 +197,7 @@ def ba_time_to_cost(args, device):
         "mixed_learned_rejected_landmarks": s32["rejected_landmarks"], "mixed_learned_rms_px": rms32,
         "rms_difference_px": abs(rms32 - rms64),
         "speedup": (t64 / t32) if t32 else None,
+        "tuning": tun32,
         "preconditioner": "learned" if pre == N.MBA_PRECOND_LEARNED else "chain",
         "cost_tolerance": "1e-6 relative to the plain FP64 path's 20-iteration cost",
         "outlier_rejection": "every 3 iterations, depth <= 0" +

@@ -148,12 +148,13 @@ cudaError_t launch_inertial_f32(const DevProblem& P, const InertialLin<double>& 
 // Outlier landmarks at the current state (outlier-rejection-solver.cc:28-103):
 // a landmark goes out of the problem when one of its observations has depth
 // <= 0 in the observing camera or, if use_reprojection, a reprojection error
-// above max_px.  Newly rejected landmarks are counted into *count.
+// above max_px.  Newly rejected landmarks are counted into *count.  f32:
+// the same test on the FP32 copies of the state (mixed path).
+cudaError_t launch_find_outliers(const DevProblem& P, int use_reprojection, double max_px, int* count,
+                                 const int* run_if, const int* skip_if, cudaStream_t s, bool f32 = false);
 // FP32 residuals of the state in FP32 copies (pose q p pad [n][8], landmark
 // [n][4]); cost summed in FP64.
 cudaError_t launch_visual_cost_f32(const DevProblem& P, const float* kf, const float* lm, double* cost_accum,
-                                   int* nonfinite, const int* skip_if, cudaStream_t s);
-cudaError_t launch_find_outliers(const DevProblem& P, int use_reprojection, double max_px, int* count,
-                                 const int* run_if, const int* skip_if, cudaStream_t s);
+                                   int* nonfinite, const int* skip_if, cudaStream_t s, const int* run_if = nullptr);
 
 }  // namespace mba

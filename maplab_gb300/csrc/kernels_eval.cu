@@ -403,46 +403,54 @@ __global__ void __launch_bounds__(kBlock) k_visual_cost(DevProblem P, const doub
 // FP32 candidate cost (mixed path): the visual term's frame chain and
 // projection in FP32 from FP32 copies of the candidate state, robustified
 // cost summed in FP64.  No FP64 arithmetic per observation.
+// FP32 landmark of observation i in the observing camera frame, from FP32
+// copies of the state (pose q p pad [n][8], landmark [n][4]).
+__device__ void obs_point_C_f32(const DevProblem& P, const float* kf, const float* lp, int64_t i, float* pC) {
+  const int lm = P.obs_lm[i], k = P.obs_kf[i], st = P.obs_store[i], type = P.obs_type[i];
+  const DevCameraT<float>& cam = P.cams_f[P.obs_cam[i]];
+  const float pB[3] = {lp[4 * (int64_t)lm], lp[4 * (int64_t)lm + 1], lp[4 * (int64_t)lm + 2]};
+  M3<float> RCI;
+  jplR(cam.q_CI, RCI);
+  float pI[3];
+  if (type == MBA_LOCAL_KEYFRAME) {
+    pI[0] = pB[0]; pI[1] = pB[1]; pI[2] = pB[2];
+  } else {
+    const float* xs = kf + 8 * (int64_t)st;
+    const float* xo = kf + 8 * (int64_t)k;
+    M3<float> RBLM, RIM;
+    jplR(xs, RBLM);
+    jplR(xo, RIM);
+    float pM[3];
+    mtv3(RBLM, pB, pM);
+    pM[0] += xs[4]; pM[1] += xs[5]; pM[2] += xs[6];
+    if (type == MBA_GLOBAL) {
+      const float* ml = P.mis_f + 8 * P.kf_mis[st];
+      const float* mo = P.mis_f + 8 * P.kf_mis[k];
+      M3<float> RGLM, RGM;
+      jplR(ml, RGLM);
+      jplR(mo, RGM);
+      float pG[3];
+      mv3(RGLM, pM, pG);
+      pG[0] += ml[4] - mo[4]; pG[1] += ml[5] - mo[5]; pG[2] += ml[6] - mo[6];
+      mtv3(RGM, pG, pM);
+    }
+    const float d[3] = {pM[0] - xo[4], pM[1] - xo[5], pM[2] - xo[6]};
+    mv3(RIM, d, pI);
+  }
+  mv3(RCI, pI, pC);
+  pC[0] += cam.p_CI[0]; pC[1] += cam.p_CI[1]; pC[2] += cam.p_CI[2];
+}
+
 __global__ void __launch_bounds__(kBlock) k_visual_cost_f32(DevProblem P, const float* kf, const float* lp,
-                                                            double* cost_accum, int* nonfinite, const int* skip_if) {
-  if (gated(nullptr, skip_if)) return;
+                                                            double* cost_accum, int* nonfinite, const int* run_if,
+                                                            const int* skip_if) {
+  if (gated(run_if, skip_if)) return;
   const int64_t i = blockIdx.x * (int64_t)blockDim.x + threadIdx.x;
   double cost = 0.0;
   if (i < P.nobs && !P.lm_off[P.obs_lm[i]]) {
-    const int lm = P.obs_lm[i], k = P.obs_kf[i], st = P.obs_store[i], type = P.obs_type[i];
     const DevCameraT<float>& cam = P.cams_f[P.obs_cam[i]];
-    const float pB[3] = {lp[4 * (int64_t)lm], lp[4 * (int64_t)lm + 1], lp[4 * (int64_t)lm + 2]};
-    M3<float> RCI;
-    jplR(cam.q_CI, RCI);
-    float pI[3];
-    if (type == MBA_LOCAL_KEYFRAME) {
-      pI[0] = pB[0]; pI[1] = pB[1]; pI[2] = pB[2];
-    } else {
-      const float* xs = kf + 8 * (int64_t)st;
-      const float* xo = kf + 8 * (int64_t)k;
-      M3<float> RBLM, RIM;
-      jplR(xs, RBLM);
-      jplR(xo, RIM);
-      float pM[3];
-      mtv3(RBLM, pB, pM);
-      pM[0] += xs[4]; pM[1] += xs[5]; pM[2] += xs[6];
-      if (type == MBA_GLOBAL) {
-        const float* ml = P.mis_f + 8 * P.kf_mis[st];
-        const float* mo = P.mis_f + 8 * P.kf_mis[k];
-        M3<float> RGLM, RGM;
-        jplR(ml, RGLM);
-        jplR(mo, RGM);
-        float pG[3];
-        mv3(RGLM, pM, pG);
-        pG[0] += ml[4] - mo[4]; pG[1] += ml[5] - mo[5]; pG[2] += ml[6] - mo[6];
-        mtv3(RGM, pG, pM);
-      }
-      const float d[3] = {pM[0] - xo[4], pM[1] - xo[5], pM[2] - xo[6]};
-      mv3(RIM, d, pI);
-    }
     float pC[3];
-    mv3(RCI, pI, pC);
-    pC[0] += cam.p_CI[0]; pC[1] += cam.p_CI[1]; pC[2] += cam.p_CI[2];
+    obs_point_C_f32(P, kf, lp, i, pC);
     float kp[2];
     if (!project<float>(cam, pC, kp, nullptr)) {
       const float2 uv = P.obs_uv_f[i];
@@ -475,6 +483,27 @@ __global__ void __launch_bounds__(kBlock) k_find_outliers(DevProblem P, int use_
     project<double>(P.cams[P.obs_cam[i]], pC, kp, nullptr);
     const double2 uv = P.obs_uv[i];
     const double e0 = kp[0] - uv.x, e1 = kp[1] - uv.y;
+    out = !(e0 * e0 + e1 * e1 <= max_px2);
+  }
+  if (out && atomicExch(&P.lm_off[lm], 1) == 0) atomicAdd(count, 1);
+}
+
+// The same test on the FP32 copies of the state (mixed path).
+__global__ void __launch_bounds__(kBlock) k_find_outliers_f32(DevProblem P, int use_reprojection, float max_px2,
+                                                              int* count, const int* run_if, const int* skip_if) {
+  if (gated(run_if, skip_if)) return;
+  const int64_t i = blockIdx.x * (int64_t)blockDim.x + threadIdx.x;
+  if (i >= P.nobs) return;
+  const int lm = P.obs_lm[i];
+  if (P.lm_off[lm]) return;
+  float pC[3];
+  obs_point_C_f32(P, P.kf_pose_f, P.lm_p_f, i, pC);
+  bool out = !(pC[2] > 0.0f);
+  if (!out && use_reprojection) {
+    float kp[2];
+    project<float>(P.cams_f[P.obs_cam[i]], pC, kp, nullptr);
+    const float2 uv = P.obs_uv_f[i];
+    const float e0 = kp[0] - uv.x, e1 = kp[1] - uv.y;
     out = !(e0 * e0 + e1 * e1 <= max_px2);
   }
   if (out && atomicExch(&P.lm_off[lm], 1) == 0) atomicAdd(count, 1);
@@ -722,10 +751,14 @@ template cudaError_t launch_visual_linearize_gated<float>(const DevProblem&, Vis
                                                           const int*, cudaStream_t);
 
 cudaError_t launch_find_outliers(const DevProblem& P, int use_reprojection, double max_px, int* count,
-                                 const int* run_if, const int* skip_if, cudaStream_t s) {
+                                 const int* run_if, const int* skip_if, cudaStream_t s, bool f32) {
   if (P.nobs == 0) return cudaSuccess;
   const int64_t blocks = (P.nobs + kBlock - 1) / kBlock;
-  k_find_outliers<<<(unsigned)blocks, kBlock, 0, s>>>(P, use_reprojection, max_px * max_px, count, run_if, skip_if);
+  if (f32)
+    k_find_outliers_f32<<<(unsigned)blocks, kBlock, 0, s>>>(P, use_reprojection, (float)(max_px * max_px), count,
+                                                             run_if, skip_if);
+  else
+    k_find_outliers<<<(unsigned)blocks, kBlock, 0, s>>>(P, use_reprojection, max_px * max_px, count, run_if, skip_if);
   return cudaGetLastError();
 }
 
@@ -738,10 +771,10 @@ cudaError_t launch_visual_cost_gated(const DevProblem& P, const double* kf_state
   return cudaGetLastError();
 }
 cudaError_t launch_visual_cost_f32(const DevProblem& P, const float* kf, const float* lm, double* cost_accum,
-                                   int* nonfinite, const int* skip_if, cudaStream_t s) {
+                                   int* nonfinite, const int* skip_if, cudaStream_t s, const int* run_if) {
   if (P.nobs == 0) return cudaSuccess;
   const int64_t blocks = (P.nobs + kBlock - 1) / kBlock;
-  k_visual_cost_f32<<<(unsigned)blocks, kBlock, 0, s>>>(P, kf, lm, cost_accum, nonfinite, skip_if);
+  k_visual_cost_f32<<<(unsigned)blocks, kBlock, 0, s>>>(P, kf, lm, cost_accum, nonfinite, run_if, skip_if);
   return cudaGetLastError();
 }
 cudaError_t launch_visual_cost(const DevProblem& P, const double* kf_state, const double* lm_p, double* cost_accum,

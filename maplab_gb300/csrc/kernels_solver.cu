@@ -52,18 +52,23 @@ __device__ __forceinline__ void atomic_add(T* a, T v) {
   atomicAdd(a, v);
 }
 
-// Loads the 18 values of one slot (slot-major W or U rows).
+// Loads the 18 values of one slot (slot-major W or U rows, kSlotStride apart).
 __device__ __forceinline__ void load_slot(const float* p, float* v) {
-  const float2* q = reinterpret_cast<const float2*>(p);  // 72-byte rows: 8-byte aligned
+  const float4* q = reinterpret_cast<const float4*>(p);  // 80-byte rows: 16-byte aligned
 #pragma unroll
-  for (int i = 0; i < 9; ++i) {
-    const float2 t = q[i];
-    v[2 * i] = t.x;
-    v[2 * i + 1] = t.y;
+  for (int i = 0; i < 4; ++i) {
+    const float4 t = q[i];
+    v[4 * i] = t.x;
+    v[4 * i + 1] = t.y;
+    v[4 * i + 2] = t.z;
+    v[4 * i + 3] = t.w;
   }
+  const float2 t = reinterpret_cast<const float2*>(p)[8];
+  v[16] = t.x;
+  v[17] = t.y;
 }
 __device__ __forceinline__ void load_slot(const double* p, double* v) {
-  const double2* q = reinterpret_cast<const double2*>(p);  // 144-byte rows: 16-byte aligned
+  const double2* q = reinterpret_cast<const double2*>(p);  // 160-byte rows: 16-byte aligned
 #pragma unroll
   for (int i = 0; i < 9; ++i) {
     const double2 t = q[i];
@@ -81,16 +86,26 @@ __global__ void __launch_bounds__(kB) k_zero(T* a, int64_t n, const int* run_if,
 }
 
 // One thread per landmark: H_ll, g_l, slot blocks W and the direct
-// camera-camera terms of its observations.
+// camera-camera terms of its observations.  The keyframes' 6x6 pose blocks of
+// D are symmetric: only their upper triangle is accumulated here (and by the
+// inertial assembly); k_mirror_pose_blocks fills the lower one afterwards.
+// scaled != 0 (re-linearizations inside the LM loop, whose Jacobi scale is
+// fixed): the Jacobian columns are multiplied by the scale as they are read,
+// so the assembled blocks come out scaled (no separate scaling pass).
 template <typename T>
 __global__ void __launch_bounds__(kB) k_assemble_lm(DevProblem P, SchurPattern S, VisualLin<T> v, LinearSystem<T> L,
-                                                    const int* run_if, const int* skip_if) {
+                                                    int scaled, const int* run_if, const int* skip_if) {
   if (gated(run_if, skip_if)) return;
   const int64_t l = blockIdx.x * (int64_t)blockDim.x + threadIdx.x;
   if (l >= P.nlm) return;
   const int64_t N = P.nobs, NL = P.nlm;
   const int64_t s0 = S.lm_slot_off[l];
   const int st = S.slot_kf[s0];
+  T sl[3], ss[6];
+#pragma unroll
+  for (int a = 0; a < 3; ++a) sl[a] = scaled ? L.slm[a * NL + l] : T(1);
+#pragma unroll
+  for (int a = 0; a < 6; ++a) ss[a] = scaled ? L.skf[15 * (int64_t)st + a] : T(1);
   T H[9], g[3], Wst[18], Dst[36], gst[6];
 #pragma unroll
   for (int a = 0; a < 9; ++a) H[a] = T(0);
@@ -107,7 +122,7 @@ __global__ void __launch_bounds__(kB) k_assemble_lm(DevProblem P, SchurPattern S
     T r[2] = {v.r[i], v.r[N + i]};
     T Jl[6];
 #pragma unroll
-    for (int a = 0; a < 6; ++a) Jl[a] = v.Jl[a * N + i];
+    for (int a = 0; a < 6; ++a) Jl[a] = v.Jl[a * N + i] * sl[a % 3];
 #pragma unroll
     for (int a = 0; a < 3; ++a) {
 #pragma unroll
@@ -118,22 +133,25 @@ __global__ void __launch_bounds__(kB) k_assemble_lm(DevProblem P, SchurPattern S
     if (slot < 0) continue;
     any_cam = true;
     T Js[12], Jo[12];
-#pragma unroll
-    for (int a = 0; a < 12; ++a) { Js[a] = v.Js[a * N + i]; Jo[a] = v.Jo[a * N + i]; }
     const int ob = P.obs_kf[i];
+#pragma unroll
+    for (int a = 0; a < 12; ++a) {
+      Js[a] = v.Js[a * N + i] * ss[a % 6];
+      Jo[a] = v.Jo[a * N + i] * (scaled ? L.skf[15 * (int64_t)ob + a % 6] : T(1));
+    }
 #pragma unroll
     for (int x = 0; x < 3; ++x)
 #pragma unroll
       for (int c = 0; c < 6; ++c) {
         Wst[6 * x + c] += Jl[x] * Js[c] + Jl[3 + x] * Js[6 + c];
-        L.Wslot[18 * (int64_t)slot + 6 * x + c] = Jl[x] * Jo[c] + Jl[3 + x] * Jo[6 + c];
+        L.Wslot[kSlotStride * (int64_t)slot + 6 * x + c] = Jl[x] * Jo[c] + Jl[3 + x] * Jo[6 + c];
       }
 #pragma unroll
     for (int a = 0; a < 6; ++a) {
       gst[a] += Js[a] * r[0] + Js[6 + a] * r[1];
       atomic_add(&L.gc[15 * (int64_t)ob + a], Jo[a] * r[0] + Jo[6 + a] * r[1]);
 #pragma unroll
-      for (int b = 0; b < 6; ++b) {
+      for (int b = a; b < 6; ++b) {
         Dst[6 * a + b] += Js[a] * Js[b] + Js[6 + a] * Js[6 + b];
         atomic_add(&L.Dbase[225 * (int64_t)ob + 15 * a + b], Jo[a] * Jo[b] + Jo[6 + a] * Jo[6 + b]);
       }
@@ -157,13 +175,13 @@ __global__ void __launch_bounds__(kB) k_assemble_lm(DevProblem P, SchurPattern S
 #pragma unroll
   for (int a = 0; a < 3; ++a) L.gl[a * NL + l] = g[a];
 #pragma unroll
-  for (int a = 0; a < 18; ++a) L.Wslot[18 * s0 + a] = Wst[a];
+  for (int a = 0; a < 18; ++a) L.Wslot[kSlotStride * s0 + a] = Wst[a];
   if (any_cam) {
 #pragma unroll
     for (int a = 0; a < 6; ++a) {
       atomic_add(&L.gc[15 * (int64_t)st + a], gst[a]);
 #pragma unroll
-      for (int b = 0; b < 6; ++b) atomic_add(&L.Dbase[225 * (int64_t)st + 15 * a + b], Dst[6 * a + b]);
+      for (int b = a; b < 6; ++b) atomic_add(&L.Dbase[225 * (int64_t)st + 15 * a + b], Dst[6 * a + b]);
     }
   }
 }
@@ -171,7 +189,7 @@ __global__ void __launch_bounds__(kB) k_assemble_lm(DevProblem P, SchurPattern S
 // One warp per inertial edge.
 template <typename T>
 __global__ void __launch_bounds__(128) k_assemble_inertial(DevProblem P, InertialLin<T> in, LinearSystem<T> L,
-                                                           const int* run_if, const int* skip_if) {
+                                                           int scaled, const int* run_if, const int* skip_if) {
   if (gated(run_if, skip_if)) return;
   const int64_t e = (blockIdx.x * (int64_t)blockDim.x + threadIdx.x) >> 5;
   const int lane = threadIdx.x & 31;
@@ -189,14 +207,28 @@ __global__ void __launch_bounds__(128) k_assemble_inertial(DevProblem P, Inertia
       dtt += Jt[15 * m + rr] * Jt[15 * m + c];
       eft += Jf[15 * m + rr] * Jt[15 * m + c];
     }
-    atomic_add(&L.Dbase[225 * (int64_t)f + a], dff);
-    atomic_add(&L.Dbase[225 * (int64_t)t + a], dtt);
+    if (scaled) {
+      const T* sf = L.skf + 15 * (int64_t)f;
+      const T* sto = L.skf + 15 * (int64_t)t;
+      dff *= sf[rr] * sf[c];
+      dtt *= sto[rr] * sto[c];
+      eft *= sf[rr] * sto[c];
+    }
+    const bool pose_lower = rr < 6 && c < rr;  // mirrored from the upper triangle
+    if (!pose_lower) {
+      atomic_add(&L.Dbase[225 * (int64_t)f + a], dff);
+      atomic_add(&L.Dbase[225 * (int64_t)t + a], dtt);
+    }
     L.Ebase[225 * e + a] = eft;
   }
   if (lane < 15) {
     T gf = T(0), gt = T(0);
 #pragma unroll
     for (int m = 0; m < 15; ++m) { gf += Jf[15 * m + lane] * r[m]; gt += Jt[15 * m + lane] * r[m]; }
+    if (scaled) {
+      gf *= L.skf[15 * (int64_t)f + lane];
+      gt *= L.skf[15 * (int64_t)t + lane];
+    }
     atomic_add(&L.gc[15 * (int64_t)f + lane], gf);
     atomic_add(&L.gc[15 * (int64_t)t + lane], gt);
   }
@@ -211,6 +243,10 @@ __global__ void __launch_bounds__(128) k_assemble_inertial(DevProblem P, Inertia
         T wf = T(0), wt = T(0);
 #pragma unroll
         for (int m = 0; m < 6; ++m) { wf += Jf[15 * m + lane] * js[m]; wt += Jt[15 * m + lane] * js[m]; }
+        if (scaled) {
+          wf *= L.ssw[q] * L.skf[15 * (int64_t)f + lane];
+          wt *= L.ssw[q] * L.skf[15 * (int64_t)t + lane];
+        }
         L.swW[30 * q + lane] = wf;
         L.swW[30 * q + 15 + lane] = wt;
       } else if (lane == 15) {
@@ -218,11 +254,28 @@ __global__ void __launch_bounds__(128) k_assemble_inertial(DevProblem P, Inertia
         T h = T(w * w), g = T(-w * rp);
 #pragma unroll
         for (int m = 0; m < 6; ++m) { h += js[m] * js[m]; g += js[m] * r[m]; }
+        if (scaled) {
+          h *= L.ssw[q] * L.ssw[q];
+          g *= L.ssw[q];
+        }
         L.swH[q] = h;
         L.swg[q] = g;
       }
     }
   }
+}
+
+// Lower triangle of each keyframe's 6x6 pose block of D from its upper one.
+template <typename T>
+__global__ void __launch_bounds__(kB) k_mirror_pose_blocks(int64_t nkf, T* D, const int* run_if, const int* skip_if) {
+  if (gated(run_if, skip_if)) return;
+  const int64_t i = blockIdx.x * (int64_t)blockDim.x + threadIdx.x;
+  if (i >= 15 * nkf) return;
+  const int64_t k = i / 15;
+  int q = (int)(i % 15), a = 1;  // the 15 strictly-lower entries (a, b), b < a < 6
+  while (q >= a) { q -= a; ++a; }
+  T* B = D + 225 * k;
+  B[15 * a + q] = B[15 * q + a];
 }
 
 // Jacobi scaling from the unscaled diagonal of J^T J (first linearization
@@ -269,7 +322,7 @@ __global__ void __launch_bounds__(kB) k_scale_inplace(DevProblem P, SchurPattern
       (void)l;
     } else if (i < n3) {
       const int64_t j = i - n2, q = j % 18, sl = j / 18;
-      L.Wslot[j] *= L.slm[(q / 6) * NL + S.slot_lm[sl]] * L.skf[15 * (int64_t)S.slot_kf[sl] + q % 6];
+      L.Wslot[kSlotStride * sl + q] *= L.slm[(q / 6) * NL + S.slot_lm[sl]] * L.skf[15 * (int64_t)S.slot_kf[sl] + q % 6];
     } else if (i < n4) {
       const int64_t j = i - n3, k = j / 225, e = j % 225;
       L.Dbase[j] *= L.skf[15 * k + e / 15] * L.skf[15 * k + e % 15];
@@ -387,7 +440,7 @@ __global__ void __launch_bounds__(kB) k_schur_lm(SolverLaunch<T> s) {
       const int64_t k = s.S.slot_kf[si];
 #pragma unroll
       for (int c = 0; c < 6; ++c) {
-        const T* w = s.L.Wslot + 18 * si;
+        const T* w = s.L.Wslot + kSlotStride * si;
         const T acc = w[c] * Vg[0] + w[6 + c] * Vg[1] + w[12 + c] * Vg[2];
         if (acc != T(0)) atomic_add(&s.L.rhs[15 * k + c], acc);
       }
@@ -406,14 +459,14 @@ __global__ void __launch_bounds__(kB) k_schur_slot(SolverLaunch<T> s) {
   if (i >= NS) return;
   const int64_t l = s.S.slot_lm[i];
   T W[18], V[9];
-  load_slot(s.L.Wslot + 18 * i, W);
+  load_slot(s.L.Wslot + kSlotStride * i, W);
 #pragma unroll
   for (int a = 0; a < 9; ++a) V[a] = s.L.V[a * NL + l];
 #pragma unroll
   for (int x = 0; x < 3; ++x)
 #pragma unroll
     for (int c = 0; c < 6; ++c)
-      s.L.U[18 * i + 6 * x + c] = V[3 * x] * W[c] + V[3 * x + 1] * W[6 + c] + V[3 * x + 2] * W[12 + c];
+      s.L.U[kSlotStride * i + 6 * x + c] = V[3 * x] * W[c] + V[3 * x + 1] * W[6 + c] + V[3 * x + 2] * W[12 + c];
 }
 
 // Landmark elimination, part 3: S(k_a, k_b) -= W_a^T U_b for every slot pair.
@@ -433,12 +486,13 @@ __global__ void __launch_bounds__(kB) k_schur_pairs(SolverLaunch<T> s) {
   T acc[36];
 #pragma unroll
   for (int q = 0; q < 36; ++q) acc[q] = T(0);
-  const int64_t p1 = s.S.chunk_off[c + 1];
-  for (int64_t p = s.S.chunk_off[c]; p < p1; ++p) {
-    const int64_t a = s.S.pair_a[p], b = s.S.pair_b[p];
+  const int64_t p0 = s.S.chunk_beg[c], p1 = p0 + s.S.chunk_len[c];
+  for (int64_t p = p0; p < p1; ++p) {
+    const int2 ab = s.S.pair_ab[p];
+    const int64_t a = ab.x, b = ab.y;
     T Wa[18], Ub[18];
-    load_slot(s.L.Wslot + 18 * a, Wa);
-    load_slot(s.L.U + 18 * b, Ub);
+    load_slot(s.L.Wslot + kSlotStride * a, Wa);
+    load_slot(s.L.U + kSlotStride * b, Ub);
     const bool sym = diag && a != b;
 #pragma unroll
     for (int r = 0; r < 6; ++r)
@@ -740,7 +794,7 @@ __global__ void __launch_bounds__(kB) k_backsub(SolverLaunch<T> s) {
     for (int x = 0; x < 3; ++x) {
       T acc = T(0);
 #pragma unroll
-      for (int c = 0; c < 6; ++c) acc += s.L.Wslot[18 * i + 6 * x + c] * xv[c];
+      for (int c = 0; c < 6; ++c) acc += s.L.Wslot[kSlotStride * i + 6 * x + c] * xv[c];
       t[x] -= acc;
     }
   }
@@ -1039,14 +1093,13 @@ cudaError_t solver_assemble(const SolverLaunch<T>& s, const int* gate, cudaStrea
   k_zero<T><<<gridcap(225 * s.P.nkf), kB, 0, st>>>(s.L.Dbase, 225 * s.P.nkf, gate, skip);
   k_zero<T><<<gridcap(15 * s.P.nkf), kB, 0, st>>>(s.L.gc, 15 * s.P.nkf, gate, skip);
   if (s.S.npu) k_zero<T><<<gridcap(36 * s.S.npu), kB, 0, st>>>(s.L.Pbase, 36 * s.S.npu, gate, skip);
-  if (s.P.nlm) k_assemble_lm<T><<<nblk(s.P.nlm, kB), kB, 0, st>>>(s.P, s.S, s.vis, s.L, gate, skip);
-  if (s.P.nedge) k_assemble_inertial<T><<<nblk(32 * s.P.nedge, 128), 128, 0, st>>>(s.P, s.ine, s.L, gate, skip);
-  // Relinearizations inside the LM loop apply the (fixed) Jacobi scaling right
-  // away; the first assembly is scaled by solver_compute_scale.
-  if (gate) {
-    const int64_t n = 12 * s.P.nlm + 18 * s.S.nslot + 240 * s.P.nkf + 36 * s.S.npu + 225 * s.P.nedge;
-    k_scale_inplace<T><<<gridcap(n), kB, 0, st>>>(s.P, s.S, s.L, gate, skip);
-  }
+  // Relinearizations inside the LM loop (gate set) assemble with the fixed
+  // Jacobi scale applied; the first assembly is scaled by solver_compute_scale.
+  const int scaled = gate ? 1 : 0;
+  if (s.P.nlm) k_assemble_lm<T><<<nblk(s.P.nlm, kB), kB, 0, st>>>(s.P, s.S, s.vis, s.L, scaled, gate, skip);
+  if (s.P.nedge)
+    k_assemble_inertial<T><<<nblk(32 * s.P.nedge, 128), 128, 0, st>>>(s.P, s.ine, s.L, scaled, gate, skip);
+  k_mirror_pose_blocks<T><<<nblk(15 * s.P.nkf, kB), kB, 0, st>>>(s.P.nkf, s.L.Dbase, gate, skip);
   return cudaGetLastError();
 }
 
@@ -1165,8 +1218,13 @@ cudaError_t solver_reject_and_restart(const SolverLaunch<T>& s, int use_reprojec
   LmControl* c = s.ctl;
   const int* run = &c->restart_now;
   k_restart_begin<<<1, 1, 0, st>>>(c);
-  cudaError_t e = launch_find_outliers(s.P, use_reprojection, max_px, &c->reject_count, run, nullptr, st);
-  if (e == cudaSuccess) e = launch_visual_cost_gated(s.P, s.P.kf_state, s.P.lm_p, &c->cost, nullptr, nullptr, st, run);
+  // The mixed path tests and costs in FP32 from the state's FP32 copies, as
+  // its candidates are costed (one precision on both sides of the gain ratio).
+  constexpr bool f32 = sizeof(T) == 4;
+  cudaError_t e = launch_find_outliers(s.P, use_reprojection, max_px, &c->reject_count, run, nullptr, st, f32);
+  if (e == cudaSuccess)
+    e = f32 ? launch_visual_cost_f32(s.P, s.P.kf_pose_f, s.P.lm_p_f, &c->cost, nullptr, nullptr, st, run)
+            : launch_visual_cost_gated(s.P, s.P.kf_state, s.P.lm_p, &c->cost, nullptr, nullptr, st, run);
   if (e != cudaSuccess) return e;
   k_restart_end<<<1, 1, 0, st>>>(c);
   e = launch_visual_linearize_gated<T>(s.P, s.vis, nullptr, run, nullptr, st);
@@ -1175,8 +1233,9 @@ cudaError_t solver_reject_and_restart(const SolverLaunch<T>& s, int use_reprojec
   k_zero<T><<<gridcap(225 * s.P.nkf), kB, 0, st>>>(s.L.Dbase, 225 * s.P.nkf, run, nullptr);
   k_zero<T><<<gridcap(15 * s.P.nkf), kB, 0, st>>>(s.L.gc, 15 * s.P.nkf, run, nullptr);
   if (s.S.npu) k_zero<T><<<gridcap(36 * s.S.npu), kB, 0, st>>>(s.L.Pbase, 36 * s.S.npu, run, nullptr);
-  if (s.P.nlm) k_assemble_lm<T><<<nblk(s.P.nlm, kB), kB, 0, st>>>(s.P, s.S, s.vis, s.L, run, nullptr);
-  if (s.P.nedge) k_assemble_inertial<T><<<nblk(32 * s.P.nedge, 128), 128, 0, st>>>(s.P, s.ine, s.L, run, nullptr);
+  if (s.P.nlm) k_assemble_lm<T><<<nblk(s.P.nlm, kB), kB, 0, st>>>(s.P, s.S, s.vis, s.L, 0, run, nullptr);
+  if (s.P.nedge) k_assemble_inertial<T><<<nblk(32 * s.P.nedge, 128), 128, 0, st>>>(s.P, s.ine, s.L, 0, run, nullptr);
+  k_mirror_pose_blocks<T><<<nblk(15 * s.P.nkf, kB), kB, 0, st>>>(s.P.nkf, s.L.Dbase, run, nullptr);
   const int64_t n = 15 * s.P.nkf + 3 * s.P.nlm + s.P.nsw;
   k_scale<T><<<nblk(n, kB), kB, 0, st>>>(s.P, s.L, s.sc, jacobi, run);
   const int64_t m = 12 * s.P.nlm + 18 * s.S.nslot + 240 * s.P.nkf + 36 * s.S.npu + 225 * s.P.nedge + 32 * s.P.nsw;

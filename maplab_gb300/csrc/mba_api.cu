@@ -189,20 +189,35 @@ namespace {
 
 // Cuts each target's contiguous pair range [off[r], off[r+1]) into chunks of
 // at most `chunk` pairs (one thread each); a target spanning several chunks
-// is marked by the bitwise-not of its id.
+// is marked by the bitwise-not of its id.  Chunks are then ordered by length
+// (longest first, stable), so that the 32 lanes of a warp loop over similar
+// pair counts.
 void cut_chunks(const std::vector<int64_t>& off, const std::vector<int64_t>& order, int64_t chunk,
-                std::vector<int32_t>* tgt, std::vector<int64_t>* coff) {
-  tgt->clear();
-  coff->assign(1, 0);
+                std::vector<int32_t>* tgt, std::vector<int64_t>* beg, std::vector<int32_t>* len) {
+  std::vector<int32_t> t;
+  std::vector<int64_t> b;
+  std::vector<int32_t> n;
   const int64_t ntgt = (int64_t)order.size();
   for (int64_t r = 0; r < ntgt; ++r) {
     const int64_t b0 = off[r], b1 = off[r + 1];
     if (b1 == b0) continue;
     const bool whole = b1 - b0 <= chunk;
     for (int64_t c0 = b0; c0 < b1; c0 += chunk) {
-      tgt->push_back(whole ? (int32_t)order[r] : ~(int32_t)order[r]);
-      coff->push_back(std::min(b1, c0 + chunk));
+      t.push_back(whole ? (int32_t)order[r] : ~(int32_t)order[r]);
+      b.push_back(c0);
+      n.push_back((int32_t)(std::min(b1, c0 + chunk) - c0));
     }
+  }
+  std::vector<int64_t> idx(t.size());
+  std::iota(idx.begin(), idx.end(), 0);
+  std::stable_sort(idx.begin(), idx.end(), [&](int64_t x, int64_t y) { return n[x] > n[y]; });
+  tgt->resize(t.size());
+  beg->resize(t.size());
+  len->resize(t.size());
+  for (size_t q = 0; q < idx.size(); ++q) {
+    (*tgt)[q] = t[idx[q]];
+    (*beg)[q] = b[idx[q]];
+    (*len)[q] = n[idx[q]];
   }
 }
 
@@ -258,7 +273,7 @@ mba_status ensure_solver_buffers(mba_handle* h, SolverBuffers<T>& b) {
   LinearSystem<T>& L = b.L;
   L.Hll = A.alloc<T>(9 * NL);
   L.gl = A.alloc<T>(3 * NL);
-  L.Wslot = A.alloc<T>(18 * NS);
+  L.Wslot = A.alloc<T>(kSlotStride * NS);
   L.Dbase = A.alloc<T>(225 * NK);
   L.Pbase = A.alloc<T>(36 * NPU);
   L.Ebase = A.alloc<T>(225 * NE);
@@ -268,7 +283,7 @@ mba_status ensure_solver_buffers(mba_handle* h, SolverBuffers<T>& b) {
   L.SE = A.alloc<T>(225 * NE);
   L.rhs = A.alloc<T>(15 * NK);
   L.V = A.alloc<T>(9 * NL);
-  L.U = A.alloc<T>(18 * NS);
+  L.U = A.alloc<T>(kSlotStride * NS);
   L.Minv = A.alloc<T>(225 * NK);
   L.x = A.alloc<T>(15 * NK);
   L.r = A.alloc<T>(15 * NK);
@@ -436,7 +451,11 @@ cudaError_t linearize_current(mba_handle* h, SolverBuffers<T>& b, SolverLaunch<T
   cudaError_t e = cudaMemsetAsync(&h->ctl->cost, 0, sizeof(double), st);
   if (e == cudaSuccess) e = cudaMemsetAsync(&h->ctl->cost_ine, 0, sizeof(double), st);
   if (e == cudaSuccess) e = cudaMemsetAsync(h->iscratch, 0, 2 * sizeof(int), st);
-  if (e == cudaSuccess) e = launch_visual_cost(h->P, h->P.kf_state, h->P.lm_p, &h->ctl->cost, h->iscratch, st);
+  // Mixed path: FP32 residuals from the FP32 state copies, FP64 sum (as its
+  // candidates are costed).
+  if (e == cudaSuccess)
+    e = sizeof(T) == 4 ? launch_visual_cost_f32(h->P, h->P.kf_pose_f, h->P.lm_p_f, &h->ctl->cost, h->iscratch, nullptr, st)
+                       : launch_visual_cost(h->P, h->P.kf_state, h->P.lm_p, &h->ctl->cost, h->iscratch, st);
   if (e == cudaSuccess)
     e = launch_inertial_gated(h->P, h->P.kf_state, h->ine_cur, &h->ctl->cost_ine, h->iscratch + 1, nullptr, st,
                               sizeof(T) == 4);
@@ -1022,9 +1041,10 @@ mba_status mba_create(const mba_problem_desc* d, int32_t device, mba_handle** ou
   // by (i, j) so consecutive targets touch landmarks of nearby keyframes, and
   // each target's pairs are cut into chunks of at most kSchurChunk pairs,
   // one chunk per thread.
-  std::vector<int32_t> pa, pb;
+  std::vector<int2> pab;
   std::vector<int32_t> chunk_tgt;
-  std::vector<int64_t> chunk_off;
+  std::vector<int64_t> chunk_beg;
+  std::vector<int32_t> chunk_len;
   {
     std::vector<int32_t> ta, tb;
     std::vector<int64_t> tt;
@@ -1058,15 +1078,15 @@ mba_status mba_create(const mba_problem_desc* d, int32_t device, mba_handle** ou
     for (int64_t t : tt) cnt[rank[t] + 1]++;
     for (int64_t r = 0; r < ntgt; ++r) cnt[r + 1] += cnt[r];
     const int64_t np = (int64_t)tt.size();
-    pa.resize(np); pb.resize(np);
+    pab.resize(np);
     {
       std::vector<int64_t> fill(cnt.begin(), cnt.end() - 1);
       for (int64_t q = 0; q < np; ++q) {
         const int64_t dst = fill[rank[tt[q]]]++;
-        pa[dst] = ta[q]; pb[dst] = tb[q];
+        pab[dst] = make_int2(ta[q], tb[q]);
       }
     }
-    cut_chunks(cnt, order, kSchurChunk, &chunk_tgt, &chunk_off);
+    cut_chunks(cnt, order, kSchurChunk, &chunk_tgt, &chunk_beg, &chunk_len);
     h->tgt_off = std::move(cnt);
     h->tgt_order = std::move(order);
   }
@@ -1273,17 +1293,17 @@ mba_status mba_create(const mba_problem_desc* d, int32_t device, mba_handle** ou
   SchurPattern& S = h->S;
   S.nslot = (int64_t)slot_kf.size();
   S.npu = npu;
-  S.npair = (int64_t)pa.size();
+  S.npair = (int64_t)pab.size();
   S.lm_slot_off = A.upload(slot_off, st);
   S.slot_kf = A.upload(slot_kf, st);
   S.slot_lm = A.upload(slot_lm, st);
   S.obs_slot = A.upload(obs_slot, st);
   S.obs_pblk = A.upload(obs_pblk, st);
-  S.pair_a = A.upload(pa, st);
-  S.pair_b = A.upload(pb, st);
+  S.pair_ab = A.upload(pab, st);
   S.nchunk = (int64_t)chunk_tgt.size();
   S.chunk_tgt = A.upload(chunk_tgt, st);
-  S.chunk_off = A.upload(chunk_off, st);
+  S.chunk_beg = A.upload(chunk_beg, st);
+  S.chunk_len = A.upload(chunk_len, st);
   S.pu_i = A.upload(pm.bi, st);
   S.pu_j = A.upload(pm.bj, st);
   S.row_off = A.upload(row_off, st);
@@ -1843,14 +1863,16 @@ int chain_tail_level(int64_t n, int levels, int64_t nodes) {
 }
 
 mba_status apply_schur_chunk(mba_handle* h, int chunk) {
-  std::vector<int32_t> tgt;
-  std::vector<int64_t> off;
-  cut_chunks(h->tgt_off, h->tgt_order, chunk, &tgt, &off);
+  std::vector<int32_t> tgt, len;
+  std::vector<int64_t> beg;
+  cut_chunks(h->tgt_off, h->tgt_order, chunk, &tgt, &beg, &len);
   int32_t* dt = h->arena.upload(tgt, h->stream);
-  int64_t* doff = h->arena.upload(off, h->stream);
+  int64_t* db = h->arena.upload(beg, h->stream);
+  int32_t* dl = h->arena.upload(len, h->stream);
   if (h->arena.err != cudaSuccess || cudaStreamSynchronize(h->stream) != cudaSuccess) return MBA_ERR_CUDA;
   h->S.chunk_tgt = dt;
-  h->S.chunk_off = doff;
+  h->S.chunk_beg = db;
+  h->S.chunk_len = dl;
   h->S.nchunk = (int64_t)tgt.size();
   h->tuning.schur_chunk = chunk;
   return MBA_OK;

@@ -14,6 +14,10 @@ namespace mba {
 constexpr int64_t kSchurChunk = 16;
 
 // Static sparsity of the reduced camera system, built on the host at create.
+// Landmark slot rows (W and U, 18 values: 3 x 6) are padded to 20 values so
+// that every row starts on a 16-byte boundary (vector loads).
+constexpr int kSlotStride = 20;
+
 struct SchurPattern {
   int64_t nslot = 0;      // landmark slots: slot 0 = store keyframe, then one per non-keyframe observation
   int64_t npu = 0;        // upper (i < j) pose-pose 6x6 blocks
@@ -24,11 +28,11 @@ struct SchurPattern {
   int32_t* obs_slot;      // [nobs] slot of the observer, -1 for kLocalKeyframe
   int32_t* obs_pblk;      // [nobs] upper block of (store, observer), -1 for kLocalKeyframe
   int64_t nchunk = 0;     // pair chunks (contiguous pair ranges of one target)
-  int32_t* pair_a;        // [npair] global slot ids, sorted by target; slot_kf[a] <= slot_kf[b]
-  int32_t* pair_b;
+  int2* pair_ab;          // [npair] global slot ids (a, b), sorted by target; slot_kf[a] <= slot_kf[b]
   int32_t* chunk_tgt;     // [nchunk] target id (kf for diagonal, nkf + upper block);
                           //   bitwise-not of it when the target spans several chunks
-  int64_t* chunk_off;     // [nchunk+1] pair range of each chunk
+  int64_t* chunk_beg;     // [nchunk] first pair of each chunk (chunks ordered by length, longest first)
+  int32_t* chunk_len;     // [nchunk] pairs in the chunk
   int32_t* pu_i;          // [npu]
   int32_t* pu_j;
   int64_t* row_off;       // [nkf+1] full (both orientations) pose-pose rows

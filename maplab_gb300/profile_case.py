@@ -5,8 +5,12 @@ CUDA-event times it prints).
     python -m maplab_gb300.profile_case visual --config c2 --block 64 --min-blocks 3 --launches 3
     # one solve
     python -m maplab_gb300.profile_case solve --config c4 --precision mixed --precond learned --iters 6
+    # the same after autotuning, with only the solve inside the profiler range
+    # (ncu --profile-from-start off)
+    python -m maplab_gb300.profile_case solve --config c4 --autotune --profile-range
 """
 import argparse
+import ctypes
 import json
 
 from . import _native as N
@@ -26,6 +30,10 @@ def main():
     ap.add_argument("--pcg", type=int, default=25)
     ap.add_argument("--autotune", action="store_true")
     ap.add_argument("--device-loop", type=int, default=1)
+    ap.add_argument("--reject-every", type=int, default=0)
+    ap.add_argument("--reproj", type=int, default=0)
+    ap.add_argument("--profile-range", action="store_true",
+                    help="cuProfilerStart / cuProfilerStop around the solve only")
     a = ap.parse_args()
     m = synth.generate(a.config)
     with ba.BundleAdjuster(m.desc) as g:
@@ -45,9 +53,16 @@ def main():
             from . import train_preconditioner as TP
             model = TP.load_default_model()
             g.set_preconditioner_model(model)
-        s = g.solve(ba.default_options(max_num_iterations=a.iters, max_linear_iterations=a.pcg, precision=prec,
-                                       preconditioner=pre, check_tolerances=0,
-                                       use_cuda_graph=2 if a.device_loop else 1))
+        opts = ba.default_options(max_num_iterations=a.iters, max_linear_iterations=a.pcg, precision=prec,
+                                  preconditioner=pre, check_tolerances=0, use_cuda_graph=2 if a.device_loop else 1,
+                                  reject_outliers_every_n_iters=a.reject_every,
+                                  outlier_use_reprojection_error=a.reproj)
+        cuda = ctypes.CDLL("libcuda.so.1") if a.profile_range else None
+        if cuda is not None:
+            cuda.cuProfilerStart()
+        s = g.solve(opts)
+        if cuda is not None:
+            cuda.cuProfilerStop()
         st = g.stats()
         print(json.dumps({"iterations": s["num_iterations"] - 1, "final_cost": s["final_cost"],
                           "time_ms": s["iterations"][-1]["time_ms"], "pcg": s["linear_iterations"],
