@@ -486,14 +486,22 @@ __global__ void __launch_bounds__(kB) k_schur_pairs(SolverLaunch<T> s) {
   T acc[36];
 #pragma unroll
   for (int q = 0; q < 36; ++q) acc[q] = T(0);
+  // Software pipeline: the slots of pair p + 1 are loaded while pair p is
+  // multiplied (two pairs' loads in flight per thread at the same occupancy).
   const int64_t p0 = s.S.chunk_beg[c], p1 = p0 + s.S.chunk_len[c];
+  int2 ab = s.S.pair_ab[p0];
+  T Wa[18], Ub[18];
+  load_slot(s.L.Wslot + kSlotStride * (int64_t)ab.x, Wa);
+  load_slot(s.L.U + kSlotStride * (int64_t)ab.y, Ub);
   for (int64_t p = p0; p < p1; ++p) {
-    const int2 ab = s.S.pair_ab[p];
-    const int64_t a = ab.x, b = ab.y;
-    T Wa[18], Ub[18];
-    load_slot(s.L.Wslot + kSlotStride * a, Wa);
-    load_slot(s.L.U + kSlotStride * b, Ub);
-    const bool sym = diag && a != b;
+    const bool sym = diag && ab.x != ab.y;
+    T Wn[18], Un[18];
+    int2 abn = ab;
+    if (p + 1 < p1) {
+      abn = s.S.pair_ab[p + 1];
+      load_slot(s.L.Wslot + kSlotStride * (int64_t)abn.x, Wn);
+      load_slot(s.L.U + kSlotStride * (int64_t)abn.y, Un);
+    }
 #pragma unroll
     for (int r = 0; r < 6; ++r)
 #pragma unroll
@@ -502,6 +510,11 @@ __global__ void __launch_bounds__(kB) k_schur_pairs(SolverLaunch<T> s) {
         acc[6 * r + q] += m;
         if (sym) acc[6 * q + r] += m;
       }
+    if (p + 1 < p1) {
+#pragma unroll
+      for (int k = 0; k < 18; ++k) { Wa[k] = Wn[k]; Ub[k] = Un[k]; }
+      ab = abn;
+    }
   }
   T* dst = diag ? s.L.SD + 225 * tid : s.L.SP + 36 * (tid - s.P.nkf);
   const int ld = diag ? 15 : 6;
