@@ -418,6 +418,25 @@ mba_status mba_get_stats(mba_handle* h, mba_problem_stats* stats);
  * mba_create / mba_solve as usual. */
 mba_status mba_relaxation_flags(const mba_problem_desc* desc, uint32_t* kf_flags_out, uint8_t* lm_constant_out);
 
+/* Landmark quality (isVisualLandmarkWellConstrained,
+ * map-structure/vi-map/src/landmark-quality-metrics.cc:103-166), the filter
+ * constructOptimizationProblem applies before adding a landmark's terms:
+ * enough observers, closest observing camera (signed by the landmark's depth
+ * in it) within a distance band, wide enough maximum disparity angle between
+ * the incidence rays, optionally every reprojection error below a bound.
+ * Evaluated on the device at the handle's current state; flags [N_lm], 1 =
+ * well constrained.  The defaults are the elq_* gflags. */
+typedef struct mba_landmark_quality_options {
+  int32_t min_observers;                     /* elq_min_observers (4) */
+  int32_t pad_;
+  double min_observation_angle_deg;          /* elq_min_observation_angle_deg (5) */
+  double max_distance_from_closest_observer; /* elq_max_distance_from_closest_observer (40 m) */
+  double min_distance_from_closest_observer; /* elq_min_distance_from_closest_observer (0.05 m) */
+  double max_reprojection_error_px;          /* elq_max_reprojection_error_px (-1: no test) */
+} mba_landmark_quality_options;
+void mba_default_landmark_quality_options(mba_landmark_quality_options* o);
+mba_status mba_landmark_quality(mba_handle* h, const mba_landmark_quality_options* o, uint8_t* well_constrained);
+
 /* Visual observations and the state they depend on, all in DEVICE memory
  * owned by the caller, laid out as in mba_problem_desc (state arrays in the
  * caller's layout: kf_q_IM_p_MI [N_kf][7], lm_p_B [N_lm][3], ...). */

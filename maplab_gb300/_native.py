@@ -173,6 +173,17 @@ class Summary(ctypes.Structure):
     ]
 
 
+class LandmarkQualityOptions(ctypes.Structure):
+    _fields_ = [
+        ("min_observers", ctypes.c_int32),
+        ("pad_", ctypes.c_int32),
+        ("min_observation_angle_deg", ctypes.c_double),
+        ("max_distance_from_closest_observer", ctypes.c_double),
+        ("min_distance_from_closest_observer", ctypes.c_double),
+        ("max_reprojection_error_px", ctypes.c_double),
+    ]
+
+
 class Tuning(ctypes.Structure):
     _fields_ = [
         ("visual_block", ctypes.c_int32),
@@ -321,6 +332,8 @@ def load_ba():
     _declare(lib, "mba_linearize_visual", ctypes.c_int, [vp, ctypes.c_int32] + [c_double_p] * 4)
     _declare(lib, "mba_linearize_pose_edges", ctypes.c_int, [vp] + [c_double_p] * 3)
     _declare(lib, "mba_read_switch_variables", ctypes.c_int, [vp, c_double_p])
+    _declare(lib, "mba_default_landmark_quality_options", None, [ctypes.POINTER(LandmarkQualityOptions)])
+    _declare(lib, "mba_landmark_quality", ctypes.c_int, [vp, ctypes.POINTER(LandmarkQualityOptions), c_uint8_p])
     _declare(lib, "mba_relaxation_flags", ctypes.c_int, [ctypes.POINTER(ProblemDesc), ctypes.POINTER(ctypes.c_uint32),
                                                          ctypes.POINTER(ctypes.c_uint8)])
     _declare(lib, "mba_write_switch_variables", ctypes.c_int, [vp, c_double_p])

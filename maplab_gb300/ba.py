@@ -47,6 +47,14 @@ def default_options(**kw):
     return o
 
 
+def default_landmark_quality_options(**kw):
+    o = N.LandmarkQualityOptions()
+    lib().mba_default_landmark_quality_options(ctypes.byref(o))
+    for k, v in kw.items():
+        setattr(o, k, v)
+    return o
+
+
 class PreconditionerModel:
     """Learned chain-preconditioner network (mba_gnn): FP32 master weights on
     one device, BF16 copies used by the kernels."""
@@ -276,6 +284,15 @@ class BundleAdjuster:
 
     def cancel(self):
         self._lib.mba_cancel(self._h)
+
+    def landmark_quality(self, **kw):
+        """isVisualLandmarkWellConstrained per landmark at the current state
+        (bool [N_lm]); keyword arguments override the elq_* defaults."""
+        o = default_landmark_quality_options(**kw)
+        good = np.zeros(max(1, self.desc.num_landmarks), dtype=np.uint8)
+        _check(self._lib.mba_landmark_quality(self._h, ctypes.byref(o), good.ctypes.data_as(N.c_uint8_p)),
+               "mba_landmark_quality")
+        return good[:self.desc.num_landmarks].astype(bool)
 
     def read_switch_variables(self):
         """Switch value per pose edge [N_pe] (1 where an edge has none)."""

@@ -130,6 +130,9 @@ template <typename T>
 cudaError_t launch_gather_visual(const DevProblem& P, const int64_t* obs_inv, VisualLin<T> v, double* r, double* Jl,
                                  double* Js, double* Jo, cudaStream_t s);
 cudaError_t launch_invert_perm(const DevProblem& P, int64_t* inv, cudaStream_t s);
+// isVisualLandmarkWellConstrained per landmark at the current state (good [nlm]).
+cudaError_t launch_landmark_quality(const DevProblem& P, const mba_landmark_quality_options& o, uint8_t* good,
+                                    cudaStream_t s);
 // to_device = 1: host-layout device arrays -> kf_state / lm_p; 0: the reverse.
 cudaError_t launch_pack_state(const DevProblem& P, const double* kx, const double* kv, const double* kbg,
                               const double* kba, const double* lp, int to_device, cudaStream_t s);

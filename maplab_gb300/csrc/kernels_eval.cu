@@ -509,6 +509,94 @@ __global__ void __launch_bounds__(kBlock) k_find_outliers_f32(DevProblem P, int 
   if (out && atomicExch(&P.lm_off[lm], 1) == 0) atomicAdd(count, 1);
 }
 
+// isVisualLandmarkWellConstrained (landmark-quality-metrics.cc:103-166), one
+// thread per landmark, FP64.  The observing cameras' global positions and the
+// landmark's global position give the incidence rays; the maximum disparity
+// angle is acos of the smallest |cos| over all ray pairs
+// (getMaxDisparityRadAngleOfUnitVectorBundle, maplab-common geometry.cc:30-44),
+// recomputed per pair instead of stored.
+__device__ void camera_center_G(const DevProblem& P, int k, int cam, double* pG) {
+  const DevCamera& c = P.cams[cam];
+  M3<double> RCI, RIM, RGM;
+  jplR(c.q_CI, RCI);
+  double pIC[3];
+  mtv3(RCI, c.p_CI, pIC);  // R_C_I^T p_C_I
+  pIC[0] = -pIC[0]; pIC[1] = -pIC[1]; pIC[2] = -pIC[2];
+  const double* x = P.kf_state + 16 * (int64_t)k;
+  jplR(x, RIM);
+  double pM[3];
+  mtv3(RIM, pIC, pM);
+  pM[0] += x[4]; pM[1] += x[5]; pM[2] += x[6];
+  const double* mg = P.mis + 8 * P.kf_mis[k];
+  jplR(mg, RGM);
+  mv3(RGM, pM, pG);
+  pG[0] += mg[4]; pG[1] += mg[5]; pG[2] += mg[6];
+}
+
+__global__ void __launch_bounds__(kBlock) k_landmark_quality(DevProblem P, mba_landmark_quality_options o,
+                                                             uint8_t* good) {
+  const int64_t l = blockIdx.x * (int64_t)blockDim.x + threadIdx.x;
+  if (l >= P.nlm) return;
+  const int64_t i0 = P.lm_obs_off[l], i1 = P.lm_obs_off[l + 1];
+  if (i1 - i0 < o.min_observers || i1 == i0) { good[l] = 0; return; }
+  // global position of the landmark from its store keyframe
+  const int st = P.obs_store[i0];
+  const double* xs = P.kf_state + 16 * (int64_t)st;
+  M3<double> R;
+  jplR(xs, R);
+  const double* pB = P.lm_p + 4 * l;
+  double pM[3], pG[3];
+  mtv3(R, pB, pM);
+  pM[0] += xs[4]; pM[1] += xs[5]; pM[2] += xs[6];
+  const double* mg = P.mis + 8 * P.kf_mis[st];
+  jplR(mg, R);
+  mv3(R, pM, pG);
+  pG[0] += mg[4]; pG[1] += mg[5]; pG[2] += mg[6];
+  const double max_px2 = o.max_reprojection_error_px * o.max_reprojection_error_px;
+  double min_sd = 1.79769313486231570e308;
+  for (int64_t i = i0; i < i1; ++i) {
+    double c[3], pC[3];
+    camera_center_G(P, P.obs_kf[i], P.obs_cam[i], c);
+    obs_point_C(P, P.kf_state, P.lm_p, i, pC);
+    const double rx = c[0] - pG[0], ry = c[1] - pG[1], rz = c[2] - pG[2];
+    const double d = sqrt(rx * rx + ry * ry + rz * rz);
+    min_sd = fmin(min_sd, pC[2] < 0.0 ? -d : d);
+    if (o.max_reprojection_error_px > 0.0) {
+      double kp[2];
+      project<double>(P.cams[P.obs_cam[i]], pC, kp, nullptr);
+      const double2 uv = P.obs_uv[i];
+      const double e2 = pC[2] > 1e-10 ? (kp[0] - uv.x) * (kp[0] - uv.x) + (kp[1] - uv.y) * (kp[1] - uv.y)
+                                      : 1.79769313486231570e308;
+      if (e2 > max_px2) { good[l] = 0; return; }
+    }
+  }
+  if (min_sd > o.max_distance_from_closest_observer || min_sd < o.min_distance_from_closest_observer) {
+    good[l] = 0;
+    return;
+  }
+  double min_cos = 1.0;
+  int nrays = 0;
+  for (int64_t i = i0; i < i1; ++i) {
+    double a[3];
+    camera_center_G(P, P.obs_kf[i], P.obs_cam[i], a);
+    a[0] -= pG[0]; a[1] -= pG[1]; a[2] -= pG[2];
+    const double da = sqrt(a[0] * a[0] + a[1] * a[1] + a[2] * a[2]);
+    if (!(da > 0.0)) continue;
+    ++nrays;
+    for (int64_t j = i + 1; j < i1; ++j) {
+      double b[3];
+      camera_center_G(P, P.obs_kf[j], P.obs_cam[j], b);
+      b[0] -= pG[0]; b[1] -= pG[1]; b[2] -= pG[2];
+      const double db = sqrt(b[0] * b[0] + b[1] * b[1] + b[2] * b[2]);
+      if (!(db > 0.0)) continue;
+      const double dot = (a[0] / da) * (b[0] / db) + (a[1] / da) * (b[1] / db) + (a[2] / da) * (b[2] / db);
+      min_cos = fmin(min_cos, fabs(dot));
+    }
+  }
+  const double angle_deg = nrays < 2 ? 0.0 : acos(min_cos) * (180.0 / 3.14159265358979323846);
+  good[l] = angle_deg < o.min_observation_angle_deg ? 0 : 1;
+}
+
 // Distortion-parameter Jacobian at the undistorted normalized point
 // (distortion-radtan.cc:67-91, distortion-equidistant.cc:109-142).
 __device__ void dist_param_jac(int dtype, const double* pt, double* J) {
@@ -903,6 +991,13 @@ __global__ void k_invert_perm(int64_t N, const int64_t* perm, int64_t* inv) {
   if (i < N) inv[perm[i]] = i;
 }
 }  // namespace
+
+cudaError_t launch_landmark_quality(const DevProblem& P, const mba_landmark_quality_options& o, uint8_t* good,
+                                    cudaStream_t s) {
+  if (P.nlm == 0) return cudaSuccess;
+  k_landmark_quality<<<(unsigned)((P.nlm + kBlock - 1) / kBlock), kBlock, 0, s>>>(P, o, good);
+  return cudaGetLastError();
+}
 
 cudaError_t launch_invert_perm(const DevProblem& P, int64_t* inv, cudaStream_t s) {
   if (P.nobs == 0) return cudaSuccess;

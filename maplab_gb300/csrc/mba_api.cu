@@ -1444,6 +1444,32 @@ mba_status mba_relaxation_flags(const mba_problem_desc* d, uint32_t* kf_flags_ou
   return MBA_OK;
 }
 
+void mba_default_landmark_quality_options(mba_landmark_quality_options* o) {
+  if (!o) return;
+  std::memset(o, 0, sizeof(*o));
+  o->min_observers = 4;
+  o->min_observation_angle_deg = 5.0;
+  o->max_distance_from_closest_observer = 40.0;
+  o->min_distance_from_closest_observer = 0.05;
+  o->max_reprojection_error_px = -1.0;
+}
+
+mba_status mba_landmark_quality(mba_handle* h, const mba_landmark_quality_options* o, uint8_t* well_constrained) {
+  if (!h || !o || (h->P.nlm > 0 && !well_constrained)) return MBA_ERR_INVALID_ARG;
+  if (o->min_observers < 0) return MBA_ERR_INVALID_ARG;
+  cudaSetDevice(h->device);
+  const int64_t NL = h->P.nlm;
+  if (NL == 0) return MBA_OK;
+  DeviceArena tmp;
+  uint8_t* d = tmp.alloc<uint8_t>(NL);
+  cudaError_t e = tmp.err;
+  if (e == cudaSuccess) e = launch_landmark_quality(h->P, *o, d, h->stream);
+  if (e == cudaSuccess) e = cudaMemcpyAsync(well_constrained, d, NL, cudaMemcpyDeviceToHost, h->stream);
+  if (e == cudaSuccess) e = cudaStreamSynchronize(h->stream);
+  tmp.release();
+  return e == cudaSuccess ? MBA_OK : MBA_ERR_CUDA;
+}
+
 mba_status mba_read_switch_variables(mba_handle* h, double* s) {
   if (!h || !s) return MBA_ERR_INVALID_ARG;
   cudaSetDevice(h->device);

@@ -24,6 +24,7 @@ int oracleLinearizeVisual(Problem* p, double* r, double* Jl, double* Js, double*
 int oracleLinearizePoseEdges(Problem* p, double* r, double* Jf, double* Jt);
 int oracleReadState(Problem* p, double* kx, double* kv, double* kbg, double* kba, double* lp);
 int oracleReadSwitches(Problem* p, double* s);
+int oracleLandmarkQuality(Problem* p, const mba_landmark_quality_options* o, uint8_t* good);
 int oracleWriteState(Problem* p, const double* kx, const double* kv, const double* kbg, const double* kba, const double* lp);
 void oracleDestroy(Problem* p);
 void oracleSetThreads(Problem* p, int t);
@@ -71,6 +72,9 @@ int oracle_pose_edge(const double* xk, const double* xk1, const double* ext, con
   return 0;
 }
 int oracle_read_switches(void* h, double* s) { return oracle::oracleReadSwitches((oracle::Problem*)h, s); }
+int oracle_landmark_quality(void* h, const mba_landmark_quality_options* o, uint8_t* good) {
+  return oracle::oracleLandmarkQuality((oracle::Problem*)h, o, good);
+}
 // One loop-closure term without its switch (baseframes, vertex blocks,
 // measurement q_AB JPL | p_AB, covariance): residual [6], ambient Jacobians.
 int oracle_loop_closure(const double* bfA, const double* bfB, const double* xA, const double* xB, const double* meas,

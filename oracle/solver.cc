@@ -13,10 +13,12 @@
 // Landmarks are eliminated by the Schur complement; the reduced camera system
 // is solved by dense Cholesky or by block-Jacobi PCG.
 #include <algorithm>
+#include <array>
 #include <chrono>
 #include <cmath>
 #include <cstring>
 #include <functional>
+#include <limits>
 #include <thread>
 #include <unordered_map>
 #include <vector>
@@ -1262,6 +1264,77 @@ int oracleLinearizeVisual(Problem* p, double* r, double* Jl, double* Js, double*
   if (Jo) std::memcpy(Jo, L.vJo.data(), L.vJo.size() * sizeof(double));
   if (cost) *cost = L.cost;
   return st;
+}
+
+// isVisualLandmarkWellConstrained (map-structure/vi-map/src/
+// landmark-quality-metrics.cc:103-166) with the options of
+// mba_landmark_quality_options: observer count, signed distance of the
+// closest observing camera (negative when the landmark lies behind it),
+// maximum disparity angle of the unit incidence rays
+// (getMaxDisparityRadAngleOfUnitVectorBundle, maplab-common geometry.cc:30-44)
+// and the optional reprojection bound (a projection counts when the point's
+// depth exceeds kMinimumDepth = 1e-10).
+static void cameraCenterG(const Problem& p, int64_t k, int cam, double* c) {
+  const mba_camera& cm = p.cams[cam];
+  double RCI[9], RIM[9], RGM[9], pIC[3], pM[3];
+  toRotationMatrixJPL(cm.q_CI_p_CI, RCI);
+  for (int i = 0; i < 3; ++i)
+    pIC[i] = -(RCI[i] * cm.q_CI_p_CI[4] + RCI[3 + i] * cm.q_CI_p_CI[5] + RCI[6 + i] * cm.q_CI_p_CI[6]);
+  const double* x = &p.kf_x[7 * k];
+  toRotationMatrixJPL(x, RIM);
+  for (int i = 0; i < 3; ++i) pM[i] = RIM[i] * pIC[0] + RIM[3 + i] * pIC[1] + RIM[6 + i] * pIC[2] + x[4 + i];
+  const double* mg = &p.mis[7 * p.kf_mis[k]];
+  toRotationMatrixJPL(mg, RGM);
+  for (int i = 0; i < 3; ++i) c[i] = RGM[3 * i] * pM[0] + RGM[3 * i + 1] * pM[1] + RGM[3 * i + 2] * pM[2] + mg[4 + i];
+}
+
+int oracleLandmarkQuality(Problem* pp, const mba_landmark_quality_options* o, uint8_t* good) {
+  const Problem& p = *pp;
+  for (int64_t l = 0; l < p.nlm; ++l) {
+    const int64_t a0 = p.lm_obs_off[l], a1 = p.lm_obs_off[l + 1];
+    good[l] = 0;
+    if (a1 - a0 < o->min_observers || a1 == a0) continue;
+    const int64_t st = p.lm_store[l];
+    double R[9], pM[3], pG[3];
+    toRotationMatrixJPL(&p.kf_x[7 * st], R);
+    const double* pB = &p.lm_p[3 * l];
+    for (int i = 0; i < 3; ++i) pM[i] = R[i] * pB[0] + R[3 + i] * pB[1] + R[6 + i] * pB[2] + p.kf_x[7 * st + 4 + i];
+    const double* mg = &p.mis[7 * p.kf_mis[st]];
+    toRotationMatrixJPL(mg, R);
+    for (int i = 0; i < 3; ++i) pG[i] = R[3 * i] * pM[0] + R[3 * i + 1] * pM[1] + R[3 * i + 2] * pM[2] + mg[4 + i];
+    std::vector<std::array<double, 3>> rays;
+    double min_sd = std::numeric_limits<double>::max();
+    bool reproj_fail = false;
+    for (int64_t a = a0; a < a1; ++a) {
+      const int64_t i = p.lm_obs_idx[a];
+      double c[3], pC[3];
+      cameraCenterG(p, p.obs_kf[i], p.obs_cam[i], c);
+      const double* P9[9];
+      visualParams(p, i, P9);
+      visualPointInCamera(P9, p.obs_type[i], pC);
+      const double r[3] = {c[0] - pG[0], c[1] - pG[1], c[2] - pG[2]};
+      const double d = std::sqrt(r[0] * r[0] + r[1] * r[1] + r[2] * r[2]);
+      min_sd = std::min(min_sd, pC[2] < 0.0 ? -d : d);
+      if (d > 0) rays.push_back({r[0] / d, r[1] / d, r[2] / d});
+      if (o->max_reprojection_error_px > 0.0) {
+        double kp[2];
+        pinholeProject3(p.cams[p.obs_cam[i]], pC, kp, nullptr, nullptr, nullptr);
+        const double e2 = pC[2] > 1e-10 ? (kp[0] - p.obs_uv[2 * i]) * (kp[0] - p.obs_uv[2 * i]) +
+                                              (kp[1] - p.obs_uv[2 * i + 1]) * (kp[1] - p.obs_uv[2 * i + 1])
+                                        : std::numeric_limits<double>::max();
+        if (e2 > o->max_reprojection_error_px * o->max_reprojection_error_px) { reproj_fail = true; break; }
+      }
+    }
+    if (reproj_fail) continue;
+    if (min_sd > o->max_distance_from_closest_observer || min_sd < o->min_distance_from_closest_observer) continue;
+    double min_cos = 1.0;
+    for (size_t x = 0; x < rays.size(); ++x)
+      for (size_t y = x + 1; y < rays.size(); ++y)
+        min_cos = std::min(min_cos, std::abs(rays[x][0] * rays[y][0] + rays[x][1] * rays[y][1] + rays[x][2] * rays[y][2]));
+    const double angle = rays.size() < 2 ? 0.0 : std::acos(min_cos) * (180.0 / M_PI);
+    good[l] = angle < o->min_observation_angle_deg ? 0 : 1;
+  }
+  return 0;
 }
 
 // Switch value per pose edge (1 for edges without a switch variable).

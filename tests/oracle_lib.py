@@ -41,6 +41,8 @@ def load():
         "oracle_loop_closure": (ctypes.c_int, [dp, dp, dp, dp, dp, dp, dp, dp, dp]),
         "oracle_absolute_pose": (ctypes.c_int, [dp, dp, dp, dp, dp, dp, dp]),
         "oracle_read_switches": (ctypes.c_int, [vp, dp]),
+        "oracle_landmark_quality": (ctypes.c_int, [vp, ctypes.POINTER(N.LandmarkQualityOptions),
+                                                   ctypes.POINTER(ctypes.c_uint8)]),
         "oracle_reduced_system": (ctypes.c_int, [vp, ctypes.POINTER(N.SolverOptions), ctypes.c_double, dp, dp]),
         "oracle_write_state": (ctypes.c_int, [vp, dp, dp, dp, dp, dp]),
         "oracle_time_visual": (ctypes.c_double, [vp, ctypes.c_int, ctypes.c_int64, ctypes.c_int]),
@@ -141,6 +143,11 @@ class OracleProblem:
         if st != 0:
             raise RuntimeError(f"oracle_reduced_system failed: {st}")
         return A, b
+
+    def landmark_quality(self, opts):
+        good = np.zeros(max(1, self.desc.num_landmarks), dtype=np.uint8)
+        self.lib.oracle_landmark_quality(self.h, ctypes.byref(opts), good.ctypes.data_as(ctypes.POINTER(ctypes.c_uint8)))
+        return good[:self.desc.num_landmarks].astype(bool)
 
     def read_switches(self):
         s = np.zeros(self.desc.num_pose_edges)
