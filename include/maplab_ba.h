@@ -418,6 +418,22 @@ mba_status mba_get_stats(mba_handle* h, mba_problem_stats* stats);
  * mba_create / mba_solve as usual. */
 mba_status mba_relaxation_flags(const mba_problem_desc* desc, uint32_t* kf_flags_out, uint8_t* lm_constant_out);
 
+/* Gauge fixes of constructOptimizationProblem (vi-optimization-builder.cc:
+ * 240-361, OptimizationProblem::applyGaugeFixesForInitialVertices,
+ * optimization-problem.cc:19-176).  Missions are clustered by co-observed
+ * landmarks and loop closures; per cluster the observability of scale,
+ * global position, yaw and roll/pitch follows from the constraints every
+ * mission of the cluster has (IMU edges, visual observations, odometry edges,
+ * absolute 6-DoF terms), and the first keyframe in the problem of the
+ * cluster's first mission gets the open degrees of freedom fixed: rotation
+ * all (pose constant), yaw (roll/pitch parameterization), position; an
+ * unobservable scale fixes the first landmark stored at that keyframe.
+ * Host only: kf_flags_out [N_kf] = desc's flags plus the fixes,
+ * lm_constant_out [N_lm] = desc's constants plus the fixes (either output may
+ * be NULL); *num_clusters (may be NULL) receives the cluster count. */
+mba_status mba_gauge_fixes(const mba_problem_desc* desc, uint32_t* kf_flags_out, uint8_t* lm_constant_out,
+                           int32_t* num_clusters);
+
 /* Landmark quality (isVisualLandmarkWellConstrained,
  * map-structure/vi-map/src/landmark-quality-metrics.cc:103-166), the filter
  * constructOptimizationProblem applies before adding a landmark's terms:

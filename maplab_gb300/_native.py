@@ -334,6 +334,8 @@ def load_ba():
     _declare(lib, "mba_read_switch_variables", ctypes.c_int, [vp, c_double_p])
     _declare(lib, "mba_default_landmark_quality_options", None, [ctypes.POINTER(LandmarkQualityOptions)])
     _declare(lib, "mba_landmark_quality", ctypes.c_int, [vp, ctypes.POINTER(LandmarkQualityOptions), c_uint8_p])
+    _declare(lib, "mba_gauge_fixes", ctypes.c_int, [ctypes.POINTER(ProblemDesc), ctypes.POINTER(ctypes.c_uint32),
+                                                    c_uint8_p, ctypes.POINTER(ctypes.c_int32)])
     _declare(lib, "mba_relaxation_flags", ctypes.c_int, [ctypes.POINTER(ProblemDesc), ctypes.POINTER(ctypes.c_uint32),
                                                          ctypes.POINTER(ctypes.c_uint8)])
     _declare(lib, "mba_write_switch_variables", ctypes.c_int, [vp, c_double_p])

@@ -1444,6 +1444,89 @@ mba_status mba_relaxation_flags(const mba_problem_desc* d, uint32_t* kf_flags_ou
   return MBA_OK;
 }
 
+mba_status mba_gauge_fixes(const mba_problem_desc* d, uint32_t* kf_flags_out, uint8_t* lm_constant_out,
+                           int32_t* num_clusters) {
+  if (!d || d->num_keyframes <= 0 || d->num_missions <= 0 || d->num_landmarks < 0 || !d->kf_mission) return MBA_ERR_INVALID_ARG;
+  const int64_t NK = d->num_keyframes, NL = d->num_landmarks, N = d->num_observations, NM = d->num_missions;
+  const int64_t NI = d->num_imu_edges, NPE = d->num_pose_edges;
+  if ((N > 0 && (!d->obs_landmark || !d->obs_keyframe)) || (NL > 0 && !d->lm_store_keyframe)) return MBA_ERR_INVALID_ARG;
+  for (int64_t k = 0; k < NK; ++k)
+    if (d->kf_mission[k] < 0 || d->kf_mission[k] >= NM) return MBA_ERR_OUT_OF_RANGE_INDEX;
+  // mission clusters: co-observed landmarks and loop closures (union-find)
+  std::vector<int64_t> parent(NM);
+  std::iota(parent.begin(), parent.end(), 0);
+  auto find = [&](int64_t a) {
+    while (parent[a] != a) a = parent[a] = parent[parent[a]];
+    return a;
+  };
+  auto unite = [&](int64_t a, int64_t b) {
+    a = find(a); b = find(b);
+    if (a != b) parent[std::max(a, b)] = std::min(a, b);
+  };
+  std::vector<char> kf_in(NK, 0), mis_visual(NM, 0), mis_imu(NM, 0), mis_odo(NM, 0);
+  std::vector<int64_t> mis_abs(NM, 0);
+  for (int64_t i = 0; i < N; ++i) {
+    const int64_t l = d->obs_landmark[i], k = d->obs_keyframe[i];
+    if (l < 0 || l >= NL || k < 0 || k >= NK) return MBA_ERR_OUT_OF_RANGE_INDEX;
+    const int64_t st = d->lm_store_keyframe[l];
+    if (st < 0 || st >= NK) return MBA_ERR_OUT_OF_RANGE_INDEX;
+    unite(d->kf_mission[k], d->kf_mission[st]);
+    kf_in[k] = kf_in[st] = 1;
+    mis_visual[d->kf_mission[k]] = 1;
+  }
+  for (int64_t e = 0; e < NI; ++e) {
+    const int64_t f = d->edge_from[e], t = d->edge_to[e];
+    if (f < 0 || f >= NK || t < 0 || t >= NK) return MBA_ERR_OUT_OF_RANGE_INDEX;
+    kf_in[f] = kf_in[t] = 1;
+    mis_imu[d->kf_mission[f]] = 1;
+  }
+  for (int64_t j = 0; j < NPE; ++j) {
+    const int type = d->pose_edge_type ? d->pose_edge_type[j] : MBA_POSE_EDGE_RELATIVE;
+    const int64_t f = d->pose_edge_from[j], t = type == MBA_POSE_EDGE_ABSOLUTE ? f : d->pose_edge_to[j];
+    if (f < 0 || f >= NK || t < 0 || t >= NK) return MBA_ERR_OUT_OF_RANGE_INDEX;
+    kf_in[f] = kf_in[t] = 1;
+    if (type == MBA_POSE_EDGE_LOOP_CLOSURE) unite(d->kf_mission[f], d->kf_mission[t]);
+    else if (type == MBA_POSE_EDGE_ABSOLUTE) mis_abs[d->kf_mission[f]]++;
+    else mis_odo[d->kf_mission[f]] = 1;
+  }
+  if (kf_flags_out)
+    for (int64_t k = 0; k < NK; ++k) kf_flags_out[k] = d->kf_flags ? d->kf_flags[k] : 0u;
+  if (lm_constant_out)
+    for (int64_t l = 0; l < NL; ++l) lm_constant_out[l] = d->lm_constant ? d->lm_constant[l] : 0;
+  int32_t clusters = 0;
+  for (int64_t root = 0; root < NM; ++root) {
+    if (find(root) != root) continue;  // root = lowest mission index of its cluster ("first mission")
+    ++clusters;
+    bool all_imu = true, all_visual = true, all_odo = true;
+    int64_t n_abs = 0;
+    for (int64_t m = 0; m < NM; ++m) {
+      if (find(m) != root) continue;
+      all_imu = all_imu && mis_imu[m];
+      all_visual = all_visual && mis_visual[m];
+      all_odo = all_odo && mis_odo[m];
+      n_abs += mis_abs[m];
+    }
+    const bool scale_obs = all_imu || all_odo || (all_visual && n_abs > 1);
+    const bool pos_obs = n_abs > 0, yaw_obs = n_abs > 0, rp_obs = n_abs > 0 || all_imu;
+    // first keyframe of the first mission that is part of the problem
+    int64_t K = -1;
+    for (int64_t k = 0; k < NK && K < 0; ++k)
+      if (d->kf_mission[k] == root && kf_in[k]) K = k;
+    if (K < 0) continue;
+    if (kf_flags_out) {
+      uint32_t& f = kf_flags_out[K];
+      if (!rp_obs) f |= MBA_KF_POSE_CONSTANT;                 // rotation kAll: the pose block is constant
+      else if (!yaw_obs) f |= MBA_KF_GAUGE_ROLL_PITCH;        // kYaw
+      if (!pos_obs) f |= MBA_KF_POSITION_CONSTANT;
+    }
+    if (!scale_obs && lm_constant_out)
+      for (int64_t l = 0; l < NL; ++l)
+        if (d->lm_store_keyframe[l] == K) { lm_constant_out[l] = 1; break; }
+  }
+  if (num_clusters) *num_clusters = clusters;
+  return MBA_OK;
+}
+
 void mba_default_landmark_quality_options(mba_landmark_quality_options* o) {
   if (!o) return;
   std::memset(o, 0, sizeof(*o));
