@@ -28,7 +28,8 @@ def test_landmark_quality_matches_oracle(qmap, kw):
     with ba.BundleAdjuster(qmap.desc) as g:
         got = g.landmark_quality(**kw)
     assert (got != ref).sum() == 0, np.flatnonzero(got != ref)[:10]
-    assert 0 < got.sum() < len(got)
+    if not kw:  # the defaults keep some landmarks and drop others on these maps
+        assert 0 < got.sum() < len(got)
 
 
 def test_landmark_quality_follows_the_state():
