@@ -154,7 +154,7 @@ def _reprojection_rms(g, m):
 
 def ba_time_to_cost(args, device):
     """Plain FP64 path (block-Jacobi PCG <= 100 its, 20 LM iterations) against
-    the mixed-precision path with the learned chain preconditioner (PCG <= 25
+    the mixed-precision path with the learned chain preconditioner (PCG <= 15
     its), stopped at the plain path's final cost * (1 + 1e-6).  Times are CUDA
     events from the first device launch of the solve."""
     from maplab_gb300 import _native as N
@@ -180,6 +180,15 @@ def ba_time_to_cost(args, device):
     rms32, n32 = _reprojection_rms(g32, m)
     cost32_fp64 = g32.cost()  # the mixed path's final state re-evaluated in full FP64
     g32.close()
+    # the same mixed solve with the chain preconditioner's fixed coefficients
+    # (no network): the learned coefficients' gain at the same PCG cap
+    gch = ba.BundleAdjuster(d, device=device)
+    gch.autotune(N.MBA_PRECISION_MIXED)
+    sch = gch.solve(ba.default_options(max_num_iterations=40, max_linear_iterations=args.fast_pcg, stop_cost=target,
+                                       precision=N.MBA_PRECISION_MIXED, preconditioner=N.MBA_PRECOND_CHAIN,
+                                       use_cuda_graph=2, **common))
+    gch.close()
+    tch = sch["time_to_stop_cost_ms"] / 1e3 if sch["time_to_stop_cost_ms"] >= 0 else None
     if model is not None:
         model.close()
     t64 = s64["iterations"][-1]["time_ms"] / 1e3
@@ -197,6 +206,8 @@ def ba_time_to_cost(args, device):
         "mixed_learned_rejected_landmarks": s32["rejected_landmarks"], "mixed_learned_rms_px": rms32,
         "rms_difference_px": abs(rms32 - rms64),
         "speedup": (t64 / t32) if t32 else None,
+        "pcg_cap": args.fast_pcg,
+        "mixed_chain_time_to_cost_s": tch, "mixed_chain_iterations": sch["num_iterations"] - 1,
         "tuning": tun32,
         "preconditioner": "learned" if pre == N.MBA_PRECOND_LEARNED else "chain",
         "cost_tolerance": "1e-6 relative to the plain FP64 path's 20-iteration cost",
@@ -228,7 +239,7 @@ def batched_missions(args, device):
         if model is not None:
             g.set_preconditioner_model(model)
             pre = N.MBA_PRECOND_LEARNED
-        s32 = g.solve(ba.default_options(max_num_iterations=40, max_linear_iterations=args.fast_pcg, stop_cost=target,
+        s32 = g.solve(ba.default_options(max_num_iterations=40, max_linear_iterations=args.c3_pcg, stop_cost=target,
                                          precision=N.MBA_PRECISION_MIXED, preconditioner=pre, use_cuda_graph=2,
                                          **common))
     if model is not None:
@@ -381,7 +392,8 @@ def main():
     ap.add_argument("--skip-cpu", action="store_true")
     ap.add_argument("--ba-config", default="c4")
     ap.add_argument("--c3", type=int, default=1)
-    ap.add_argument("--fast-pcg", type=int, default=25)
+    ap.add_argument("--fast-pcg", type=int, default=15)
+    ap.add_argument("--c3-pcg", type=int, default=25)
     ap.add_argument("--reproj-rejection", type=int, default=1)
     args = ap.parse_args()
     if args.warmup < 3:
