@@ -154,7 +154,7 @@ def _reprojection_rms(g, m):
 
 def ba_time_to_cost(args, device):
     """Plain FP64 path (block-Jacobi PCG <= 100 its, 20 LM iterations) against
-    the mixed-precision path with the learned chain preconditioner (PCG <= 15
+    the mixed-precision path with the learned chain preconditioner (PCG <= 25
     its), stopped at the plain path's final cost * (1 + 1e-6).  Times are CUDA
     events from the first device launch of the solve."""
     from maplab_gb300 import _native as N
@@ -392,7 +392,7 @@ def main():
     ap.add_argument("--skip-cpu", action="store_true")
     ap.add_argument("--ba-config", default="c4")
     ap.add_argument("--c3", type=int, default=1)
-    ap.add_argument("--fast-pcg", type=int, default=15)
+    ap.add_argument("--fast-pcg", type=int, default=25)
     ap.add_argument("--c3-pcg", type=int, default=25)
     ap.add_argument("--reproj-rejection", type=int, default=1)
     args = ap.parse_args()

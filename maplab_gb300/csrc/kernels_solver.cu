@@ -474,61 +474,97 @@ __global__ void __launch_bounds__(kB) k_schur_slot(SolverLaunch<T> s) {
 // pairs in registers and writes the block once (plain read-modify-write when
 // it owns the whole target, atomics otherwise).  Diagonal targets take
 // M + M^T for a != b; upper pairs are oriented so M lands untransposed.
+// Chunks are grouped by the target's keyframe row i (k_a = i): one block per
+// row stages the row's W slots in shared memory (rows of kSlotStride values,
+// if they fit in stage_cap slots), so that only U_b is gathered from global
+// memory; the next pair's rows are loaded while a pair is multiplied.
 template <typename T>
-__global__ void __launch_bounds__(kB) k_schur_pairs(SolverLaunch<T> s) {
+__global__ void __launch_bounds__(kB, sizeof(T) == 4 ? 2 : 1) k_schur_pairs(SolverLaunch<T> s, int64_t stage_cap) {
   if (s.ctl->terminated) return;
-  const int64_t c = blockIdx.x * (int64_t)blockDim.x + threadIdx.x;
-  if (c >= s.S.nchunk) return;
-  const int32_t raw = s.S.chunk_tgt[c];
-  const bool whole = raw >= 0;
-  const int64_t tid = whole ? raw : ~raw;
-  const bool diag = tid < s.P.nkf;
-  T acc[36];
+  extern __shared__ __align__(16) unsigned char schur_smem[];
+  T* sW = reinterpret_cast<T*>(schur_smem);
+  const int64_t i = blockIdx.x;
+  const int64_t c0 = s.S.row_chunk_off[i], c1 = s.S.row_chunk_off[i + 1];
+  if (c0 == c1) return;
+  const int64_t s0 = s.S.kf_slot_off[i], ns = s.S.kf_slot_off[i + 1] - s0;
+  const bool staged = ns <= stage_cap;
+  if (staged)
+    for (int64_t q = threadIdx.x; q < 18 * ns; q += blockDim.x)
+      sW[kSlotStride * (q / 18) + q % 18] = s.L.Wslot[kSlotStride * (int64_t)s.S.kf_slot[s0 + q / 18] + q % 18];
+  __syncthreads();
+  auto wrow = [&](int a) -> const T* {
+    return staged ? sW + kSlotStride * (int64_t)a : s.L.Wslot + kSlotStride * (int64_t)s.S.kf_slot[s0 + a];
+  };
+  for (int64_t c = c0 + threadIdx.x; c < c1; c += blockDim.x) {
+    const int32_t raw = s.S.chunk_tgt[c];
+    const bool whole = raw >= 0;
+    const int64_t tid = whole ? raw : ~raw;
+    const bool diag = tid < s.P.nkf;
+    T acc[36];
 #pragma unroll
-  for (int q = 0; q < 36; ++q) acc[q] = T(0);
-  // Software pipeline: the slots of pair p + 1 are loaded while pair p is
-  // multiplied (two pairs' loads in flight per thread at the same occupancy).
-  const int64_t p0 = s.S.chunk_beg[c], p1 = p0 + s.S.chunk_len[c];
-  int2 ab = s.S.pair_ab[p0];
-  T Wa[18], Ub[18];
-  load_slot(s.L.Wslot + kSlotStride * (int64_t)ab.x, Wa);
-  load_slot(s.L.U + kSlotStride * (int64_t)ab.y, Ub);
-  for (int64_t p = p0; p < p1; ++p) {
-    const bool sym = diag && ab.x != ab.y;
-    T Wn[18], Un[18];
-    int2 abn = ab;
-    if (p + 1 < p1) {
-      abn = s.S.pair_ab[p + 1];
-      load_slot(s.L.Wslot + kSlotStride * (int64_t)abn.x, Wn);
-      load_slot(s.L.U + kSlotStride * (int64_t)abn.y, Un);
-    }
-#pragma unroll
-    for (int r = 0; r < 6; ++r)
-#pragma unroll
-      for (int q = 0; q < 6; ++q) {
-        const T m = Wa[r] * Ub[q] + Wa[6 + r] * Ub[6 + q] + Wa[12 + r] * Ub[12 + q];
-        acc[6 * r + q] += m;
-        if (sym) acc[6 * q + r] += m;
+    for (int q = 0; q < 36; ++q) acc[q] = T(0);
+    const int64_t p0 = s.S.chunk_beg[c], p1 = p0 + s.S.chunk_len[c];
+    int2 ab = s.S.pair_rb[p0];
+    T Wa[18], Ub[18];
+    load_slot(wrow(ab.x), Wa);
+    load_slot(s.L.U + kSlotStride * (int64_t)ab.y, Ub);
+    for (int64_t p = p0; p < p1; ++p) {
+      const bool sym = diag && s.S.kf_slot[s0 + ab.x] != ab.y;
+      T Wn[18], Un[18];
+      int2 abn = ab;
+      if (p + 1 < p1) {
+        abn = s.S.pair_rb[p + 1];
+        load_slot(wrow(abn.x), Wn);
+        load_slot(s.L.U + kSlotStride * (int64_t)abn.y, Un);
       }
-    if (p + 1 < p1) {
 #pragma unroll
-      for (int k = 0; k < 18; ++k) { Wa[k] = Wn[k]; Ub[k] = Un[k]; }
-      ab = abn;
+      for (int r = 0; r < 6; ++r)
+#pragma unroll
+        for (int q = 0; q < 6; ++q) {
+          const T m = Wa[r] * Ub[q] + Wa[6 + r] * Ub[6 + q] + Wa[12 + r] * Ub[12 + q];
+          acc[6 * r + q] += m;
+          if (sym) acc[6 * q + r] += m;
+        }
+      if (p + 1 < p1) {
+#pragma unroll
+        for (int k = 0; k < 18; ++k) { Wa[k] = Wn[k]; Ub[k] = Un[k]; }
+        ab = abn;
+      }
+    }
+    T* dst = diag ? s.L.SD + 225 * tid : s.L.SP + 36 * (tid - s.P.nkf);
+    const int ld = diag ? 15 : 6;
+    if (whole) {
+#pragma unroll
+      for (int r = 0; r < 6; ++r)
+#pragma unroll
+        for (int q = 0; q < 6; ++q) dst[ld * r + q] -= acc[6 * r + q];
+    } else {
+#pragma unroll
+      for (int r = 0; r < 6; ++r)
+#pragma unroll
+        for (int q = 0; q < 6; ++q) atomic_add(&dst[ld * r + q], -acc[6 * r + q]);
     }
   }
-  T* dst = diag ? s.L.SD + 225 * tid : s.L.SP + 36 * (tid - s.P.nkf);
-  const int ld = diag ? 15 : 6;
-  if (whole) {
-#pragma unroll
-    for (int r = 0; r < 6; ++r)
-#pragma unroll
-      for (int q = 0; q < 6; ++q) dst[ld * r + q] -= acc[6 * r + q];
-  } else {
-#pragma unroll
-    for (int r = 0; r < 6; ++r)
-#pragma unroll
-      for (int q = 0; q < 6; ++q) atomic_add(&dst[ld * r + q], -acc[6 * r + q]);
-  }
+}
+
+// Shared-memory bytes of k_schur_pairs (a row's staged W slots) and the slot
+// count that fits; longer rows read W from global memory.
+template <typename T>
+int64_t schur_pairs_smem(const SchurPattern& S, int64_t* cap) {
+  const int64_t limit = sizeof(T) == 4 ? 96 * 1024 : 200 * 1024;  // FP32: two blocks per SM
+  const int64_t fit = limit / (kSlotStride * (int64_t)sizeof(T));
+  *cap = S.max_row_slots < fit ? S.max_row_slots : fit;
+  return *cap * kSlotStride * (int64_t)sizeof(T);
+}
+
+// The shared-memory opt-in is set by solver_prepare (outside graph capture).
+template <typename T>
+cudaError_t launch_schur_pairs(const SolverLaunch<T>& s, cudaStream_t st) {
+  if (s.S.nchunk == 0) return cudaSuccess;
+  int64_t cap = 0;
+  const int64_t bytes = schur_pairs_smem<T>(s.S, &cap);
+  k_schur_pairs<T><<<(unsigned)s.P.nkf, kB, (size_t)bytes, st>>>(s, cap);
+  return cudaGetLastError();
 }
 
 // Switch elimination (one warp per switch variable): H = h + damping,
@@ -1131,7 +1167,10 @@ cudaError_t solver_build_reduced(const SolverLaunch<T>& s, cudaStream_t st) {
   k_build_system<T><<<gridcap(nsys), kB, 0, st>>>(s);
   if (s.P.nlm) k_schur_lm<T><<<nblk(s.P.nlm, kB), kB, 0, st>>>(s);
   if (s.S.nslot) k_schur_slot<T><<<nblk(s.S.nslot, kB), kB, 0, st>>>(s);
-  if (s.S.nchunk) k_schur_pairs<T><<<nblk(s.S.nchunk, kB), kB, 0, st>>>(s);
+  if (s.S.nchunk) {
+    const cudaError_t e = launch_schur_pairs<T>(s, st);
+    if (e != cudaSuccess) return e;
+  }
   if (s.P.nsw) k_schur_switch<T><<<nblk(32 * s.P.nsw, 128), 128, 0, st>>>(s);
   k_finalize_system<T><<<gridcap(nsys), kB, 0, st>>>(s);
   k_block_jacobi<T><<<nblk(s.P.nkf, 64), 64, 0, st>>>(s);
@@ -1145,9 +1184,16 @@ cudaError_t solver_build_reduced(const SolverLaunch<T>& s, cudaStream_t st) {
 }
 
 template <typename T>
+cudaError_t solver_prepare(const SchurPattern& S) {
+  int64_t cap = 0;
+  const int64_t bytes = schur_pairs_smem<T>(S, &cap);
+  if (bytes <= 48 * 1024) return cudaSuccess;
+  return cudaFuncSetAttribute(k_schur_pairs<T>, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)bytes);
+}
+
+template <typename T>
 cudaError_t solver_schur_pairs(const SolverLaunch<T>& s, cudaStream_t st) {
-  if (s.S.nchunk) k_schur_pairs<T><<<nblk(s.S.nchunk, kB), kB, 0, st>>>(s);
-  return cudaGetLastError();
+  return launch_schur_pairs<T>(s, st);
 }
 
 template <typename T>
@@ -1288,6 +1334,8 @@ template cudaError_t solver_compute_scale<double>(const SolverLaunch<double>&, i
 template cudaError_t solver_compute_scale<float>(const SolverLaunch<float>&, int, cudaStream_t);
 template cudaError_t solver_build_reduced<double>(const SolverLaunch<double>&, cudaStream_t);
 template cudaError_t solver_build_reduced<float>(const SolverLaunch<float>&, cudaStream_t);
+template cudaError_t solver_prepare<double>(const SchurPattern&);
+template cudaError_t solver_prepare<float>(const SchurPattern&);
 template cudaError_t solver_schur_pairs<double>(const SolverLaunch<double>&, cudaStream_t);
 template cudaError_t solver_schur_pairs<float>(const SolverLaunch<float>&, cudaStream_t);
 template cudaError_t solver_step<double>(const SolverLaunch<double>&, cudaStream_t);

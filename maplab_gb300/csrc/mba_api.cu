@@ -182,6 +182,7 @@ struct mba_handle {
   // Schur pair targets in kernel order (pair range per target) for re-cutting
   // the chunks under a tuned chunk size
   std::vector<int64_t> tgt_off, tgt_order;
+  std::vector<int32_t> tgt_row;  // keyframe row of each target in tgt_order
   mba_tuning tuning{};
 };
 
@@ -189,14 +190,16 @@ namespace {
 
 // Cuts each target's contiguous pair range [off[r], off[r+1]) into chunks of
 // at most `chunk` pairs (one thread each); a target spanning several chunks
-// is marked by the bitwise-not of its id.  Chunks are then ordered by length
-// (longest first, stable), so that the 32 lanes of a warp loop over similar
-// pair counts.
-void cut_chunks(const std::vector<int64_t>& off, const std::vector<int64_t>& order, int64_t chunk,
-                std::vector<int32_t>* tgt, std::vector<int64_t>* beg, std::vector<int32_t>* len) {
-  std::vector<int32_t> t;
+// is marked by the bitwise-not of its id.  Chunks are then grouped by the
+// target's keyframe row (row_of[r], rows ascending; one block per row) and,
+// within a row, ordered by length (longest first, stable) so that the 32
+// lanes of a warp loop over similar pair counts.  row_chunk_off [nkf + 1]
+// receives each row's chunk range.
+void cut_chunks(const std::vector<int64_t>& off, const std::vector<int64_t>& order,
+                const std::vector<int32_t>& row_of, int64_t nkf, int64_t chunk, std::vector<int32_t>* tgt,
+                std::vector<int64_t>* beg, std::vector<int32_t>* len, std::vector<int64_t>* row_chunk_off) {
+  std::vector<int32_t> t, n, rw;
   std::vector<int64_t> b;
-  std::vector<int32_t> n;
   const int64_t ntgt = (int64_t)order.size();
   for (int64_t r = 0; r < ntgt; ++r) {
     const int64_t b0 = off[r], b1 = off[r + 1];
@@ -206,11 +209,17 @@ void cut_chunks(const std::vector<int64_t>& off, const std::vector<int64_t>& ord
       t.push_back(whole ? (int32_t)order[r] : ~(int32_t)order[r]);
       b.push_back(c0);
       n.push_back((int32_t)(std::min(b1, c0 + chunk) - c0));
+      rw.push_back(row_of[r]);
     }
   }
   std::vector<int64_t> idx(t.size());
   std::iota(idx.begin(), idx.end(), 0);
-  std::stable_sort(idx.begin(), idx.end(), [&](int64_t x, int64_t y) { return n[x] > n[y]; });
+  std::stable_sort(idx.begin(), idx.end(), [&](int64_t x, int64_t y) {
+    return rw[x] != rw[y] ? rw[x] < rw[y] : n[x] > n[y];
+  });
+  row_chunk_off->assign(nkf + 1, 0);
+  for (int32_t r : rw) (*row_chunk_off)[r + 1]++;
+  for (int64_t k = 0; k < nkf; ++k) (*row_chunk_off)[k + 1] += (*row_chunk_off)[k];
   tgt->resize(t.size());
   beg->resize(t.size());
   len->resize(t.size());
@@ -301,6 +310,7 @@ mba_status ensure_solver_buffers(mba_handle* h, SolverBuffers<T>& b) {
   L.swx = A.alloc<double>(P.nsw);
   L.ssw = A.alloc<T>(P.nsw);
   if (A.err != cudaSuccess) return MBA_ERR_CUDA;
+  if (solver_prepare<T>(h->S) != cudaSuccess) return MBA_ERR_CUDA;
   b.ready = true;
   return MBA_OK;
 }
@@ -1041,10 +1051,13 @@ mba_status mba_create(const mba_problem_desc* d, int32_t device, mba_handle** ou
   // by (i, j) so consecutive targets touch landmarks of nearby keyframes, and
   // each target's pairs are cut into chunks of at most kSchurChunk pairs,
   // one chunk per thread.
-  std::vector<int2> pab;
-  std::vector<int32_t> chunk_tgt;
-  std::vector<int64_t> chunk_beg;
+  // A pair stores a as its position in its row's keyframe-major slot list (the
+  // row's W slots are staged in shared memory) and b as a global slot.
+  std::vector<int2> prb;
+  std::vector<int32_t> chunk_tgt, kf_slot, tgt_row;
+  std::vector<int64_t> chunk_beg, row_chunk_off, kf_slot_off(NK + 1, 0);
   std::vector<int32_t> chunk_len;
+  int64_t max_row_slots = 0;
   {
     std::vector<int32_t> ta, tb;
     std::vector<int64_t> tt;
@@ -1078,17 +1091,39 @@ mba_status mba_create(const mba_problem_desc* d, int32_t device, mba_handle** ou
     for (int64_t t : tt) cnt[rank[t] + 1]++;
     for (int64_t r = 0; r < ntgt; ++r) cnt[r + 1] += cnt[r];
     const int64_t np = (int64_t)tt.size();
-    pab.resize(np);
+    const int64_t nsl = (int64_t)slot_kf.size();
+    for (int64_t x = 0; x < nsl; ++x) kf_slot_off[slot_kf[x] + 1]++;
+    for (int64_t k = 0; k < NK; ++k) {
+      max_row_slots = std::max(max_row_slots, kf_slot_off[k + 1]);
+      kf_slot_off[k + 1] += kf_slot_off[k];
+    }
+    kf_slot.resize(nsl);
+    std::vector<int32_t> kpos(nsl);
+    {
+      std::vector<int64_t> fill(kf_slot_off.begin(), kf_slot_off.end() - 1);
+      for (int64_t x = 0; x < nsl; ++x) {
+        const int64_t at = fill[slot_kf[x]]++;
+        kf_slot[at] = (int32_t)x;
+        kpos[x] = (int32_t)(at - kf_slot_off[slot_kf[x]]);
+      }
+    }
+    prb.resize(np);
     {
       std::vector<int64_t> fill(cnt.begin(), cnt.end() - 1);
       for (int64_t q = 0; q < np; ++q) {
         const int64_t dst = fill[rank[tt[q]]]++;
-        pab[dst] = make_int2(ta[q], tb[q]);
+        prb[dst] = make_int2(kpos[ta[q]], tb[q]);
       }
     }
-    cut_chunks(cnt, order, kSchurChunk, &chunk_tgt, &chunk_beg, &chunk_len);
+    tgt_row.resize(ntgt);
+    for (int64_t r = 0; r < ntgt; ++r) {
+      const int64_t t = order[r];
+      tgt_row[r] = (int32_t)(t < NK ? t : pm.bi[t - NK]);
+    }
+    cut_chunks(cnt, order, tgt_row, NK, kSchurChunk, &chunk_tgt, &chunk_beg, &chunk_len, &row_chunk_off);
     h->tgt_off = std::move(cnt);
     h->tgt_order = std::move(order);
+    h->tgt_row = std::move(tgt_row);
   }
   const int64_t npu = pm.count;
   std::vector<int64_t> row_off(NK + 1, 0);
@@ -1293,13 +1328,17 @@ mba_status mba_create(const mba_problem_desc* d, int32_t device, mba_handle** ou
   SchurPattern& S = h->S;
   S.nslot = (int64_t)slot_kf.size();
   S.npu = npu;
-  S.npair = (int64_t)pab.size();
+  S.npair = (int64_t)prb.size();
   S.lm_slot_off = A.upload(slot_off, st);
   S.slot_kf = A.upload(slot_kf, st);
   S.slot_lm = A.upload(slot_lm, st);
   S.obs_slot = A.upload(obs_slot, st);
   S.obs_pblk = A.upload(obs_pblk, st);
-  S.pair_ab = A.upload(pab, st);
+  S.pair_rb = A.upload(prb, st);
+  S.kf_slot_off = A.upload(kf_slot_off, st);
+  S.kf_slot = A.upload(kf_slot, st);
+  S.max_row_slots = max_row_slots;
+  S.row_chunk_off = A.upload(row_chunk_off, st);
   S.nchunk = (int64_t)chunk_tgt.size();
   S.chunk_tgt = A.upload(chunk_tgt, st);
   S.chunk_beg = A.upload(chunk_beg, st);
@@ -1973,15 +2012,17 @@ int chain_tail_level(int64_t n, int levels, int64_t nodes) {
 
 mba_status apply_schur_chunk(mba_handle* h, int chunk) {
   std::vector<int32_t> tgt, len;
-  std::vector<int64_t> beg;
-  cut_chunks(h->tgt_off, h->tgt_order, chunk, &tgt, &beg, &len);
+  std::vector<int64_t> beg, rco;
+  cut_chunks(h->tgt_off, h->tgt_order, h->tgt_row, h->P.nkf, chunk, &tgt, &beg, &len, &rco);
   int32_t* dt = h->arena.upload(tgt, h->stream);
   int64_t* db = h->arena.upload(beg, h->stream);
   int32_t* dl = h->arena.upload(len, h->stream);
+  int64_t* dr = h->arena.upload(rco, h->stream);
   if (h->arena.err != cudaSuccess || cudaStreamSynchronize(h->stream) != cudaSuccess) return MBA_ERR_CUDA;
   h->S.chunk_tgt = dt;
   h->S.chunk_beg = db;
   h->S.chunk_len = dl;
+  h->S.row_chunk_off = dr;
   h->S.nchunk = (int64_t)tgt.size();
   h->tuning.schur_chunk = chunk;
   return MBA_OK;

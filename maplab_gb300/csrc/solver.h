@@ -28,10 +28,15 @@ struct SchurPattern {
   int32_t* obs_slot;      // [nobs] slot of the observer, -1 for kLocalKeyframe
   int32_t* obs_pblk;      // [nobs] upper block of (store, observer), -1 for kLocalKeyframe
   int64_t nchunk = 0;     // pair chunks (contiguous pair ranges of one target)
-  int2* pair_ab;          // [npair] global slot ids (a, b), sorted by target; slot_kf[a] <= slot_kf[b]
+  int2* pair_rb;          // [npair] (a as position in its row's slot list, b global slot), sorted by target;
+                          //   slot_kf[a] <= slot_kf[b]
+  int64_t* kf_slot_off;   // [nkf+1] keyframe-major slot lists (a row's W slots are staged from them)
+  int32_t* kf_slot;       // [nslot]
+  int64_t max_row_slots = 0;
+  int64_t* row_chunk_off; // [nkf+1] chunks of the targets of keyframe row i
   int32_t* chunk_tgt;     // [nchunk] target id (kf for diagonal, nkf + upper block);
                           //   bitwise-not of it when the target spans several chunks
-  int64_t* chunk_beg;     // [nchunk] first pair of each chunk (chunks ordered by length, longest first)
+  int64_t* chunk_beg;     // [nchunk] first pair of each chunk (grouped by row; by length within a row)
   int32_t* chunk_len;     // [nchunk] pairs in the chunk
   int32_t* pu_i;          // [npu]
   int32_t* pu_j;
@@ -189,6 +194,10 @@ cudaError_t solver_compute_scale(const SolverLaunch<T>& s, int jacobi, cudaStrea
 // inverses, at the radius held in the control block.
 template <typename T>
 cudaError_t solver_build_reduced(const SolverLaunch<T>& s, cudaStream_t st);
+// Per-problem launch preparation (shared-memory opt-in of the Schur pair
+// kernel); call before the solver's kernels are launched or captured.
+template <typename T>
+cudaError_t solver_prepare(const SchurPattern& S);
 // The Schur pair kernel alone (autotuning).
 template <typename T>
 cudaError_t solver_schur_pairs(const SolverLaunch<T>& s, cudaStream_t st);
