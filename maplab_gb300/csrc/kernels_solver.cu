@@ -93,7 +93,8 @@ __global__ void __launch_bounds__(kB) k_zero(T* a, int64_t n, const int* run_if,
 // fixed): the Jacobian columns are multiplied by the scale as they are read,
 // so the assembled blocks come out scaled (no separate scaling pass).
 template <typename T>
-__global__ void __launch_bounds__(kB) k_assemble_lm(DevProblem P, SchurPattern S, VisualLin<T> v, LinearSystem<T> L,
+__global__ void __launch_bounds__(kB, sizeof(T) == 4 ? 2 : 1) k_assemble_lm(DevProblem P, SchurPattern S, VisualLin<T> v,
+                                                                            LinearSystem<T> L,
                                                     int scaled, const int* run_if, const int* skip_if) {
   if (gated(run_if, skip_if)) return;
   const int64_t l = blockIdx.x * (int64_t)blockDim.x + threadIdx.x;
@@ -149,25 +150,48 @@ __global__ void __launch_bounds__(kB) k_assemble_lm(DevProblem P, SchurPattern S
 #pragma unroll
     for (int a = 0; a < 6; ++a) {
       gst[a] += Js[a] * r[0] + Js[6 + a] * r[1];
-      atomic_add(&L.gc[15 * (int64_t)ob + a], Jo[a] * r[0] + Jo[6 + a] * r[1]);
 #pragma unroll
-      for (int b = a; b < 6; ++b) {
-        Dst[6 * a + b] += Js[a] * Js[b] + Js[6 + a] * Js[6 + b];
-        atomic_add(&L.Dbase[225 * (int64_t)ob + 15 * a + b], Jo[a] * Jo[b] + Jo[6 + a] * Jo[6 + b]);
-      }
+      for (int b = a; b < 6; ++b) Dst[6 * a + b] += Js[a] * Js[b] + Js[6 + a] * Js[6 + b];
     }
     const int blk = S.obs_pblk[i];
     T* Pb = L.Pbase + 36 * (int64_t)blk;
-    if (st < ob) {
+    const T* X = st < ob ? Js : Jo;  // P block rows: the lower keyframe of the pair
+    const T* Y = st < ob ? Jo : Js;
+    if constexpr (sizeof(T) == 4) {
+      // 16-byte vector atomics: the (store, observer) block, the observer's
+      // pose block (full 6x6) and its gradient.
+      float4* P4 = reinterpret_cast<float4*>(Pb);
+      float4* D4 = reinterpret_cast<float4*>(L.Dpose + 36 * (int64_t)ob);
+      float4* g4 = reinterpret_cast<float4*>(L.gpose + 8 * (int64_t)ob);
 #pragma unroll
-      for (int a = 0; a < 6; ++a)
+      for (int q = 0; q < 9; ++q) {
+        float pv[4], dv[4];
 #pragma unroll
-        for (int b = 0; b < 6; ++b) atomic_add(&Pb[6 * a + b], Js[a] * Jo[b] + Js[6 + a] * Jo[6 + b]);
+        for (int u = 0; u < 4; ++u) {
+          const int a = (4 * q + u) / 6, b = (4 * q + u) % 6;
+          pv[u] = X[a] * Y[b] + X[6 + a] * Y[6 + b];
+          dv[u] = Jo[a] * Jo[b] + Jo[6 + a] * Jo[6 + b];
+        }
+        atomicAdd(P4 + q, make_float4(pv[0], pv[1], pv[2], pv[3]));
+        atomicAdd(D4 + q, make_float4(dv[0], dv[1], dv[2], dv[3]));
+      }
+      float gv[6];
+#pragma unroll
+      for (int a = 0; a < 6; ++a) gv[a] = Jo[a] * r[0] + Jo[6 + a] * r[1];
+      atomicAdd(g4, make_float4(gv[0], gv[1], gv[2], gv[3]));
+      atomicAdd(g4 + 1, make_float4(gv[4], gv[5], 0.f, 0.f));
     } else {
 #pragma unroll
+      for (int a = 0; a < 6; ++a) {
+        atomic_add(&L.gc[15 * (int64_t)ob + a], Jo[a] * r[0] + Jo[6 + a] * r[1]);
+#pragma unroll
+        for (int b = a; b < 6; ++b)
+          atomic_add(&L.Dbase[225 * (int64_t)ob + 15 * a + b], Jo[a] * Jo[b] + Jo[6 + a] * Jo[6 + b]);
+      }
+#pragma unroll
       for (int a = 0; a < 6; ++a)
 #pragma unroll
-        for (int b = 0; b < 6; ++b) atomic_add(&Pb[6 * a + b], Jo[a] * Js[b] + Jo[6 + a] * Js[6 + b]);
+        for (int b = 0; b < 6; ++b) atomic_add(&Pb[6 * a + b], X[a] * Y[b] + X[6 + a] * Y[6 + b]);
     }
   }
 #pragma unroll
@@ -177,13 +201,42 @@ __global__ void __launch_bounds__(kB) k_assemble_lm(DevProblem P, SchurPattern S
 #pragma unroll
   for (int a = 0; a < 18; ++a) L.Wslot[kSlotStride * s0 + a] = Wst[a];
   if (any_cam) {
+    if constexpr (sizeof(T) == 4) {
+      float4* D4 = reinterpret_cast<float4*>(L.Dpose + 36 * (int64_t)st);
+      float4* g4 = reinterpret_cast<float4*>(L.gpose + 8 * (int64_t)st);
 #pragma unroll
-    for (int a = 0; a < 6; ++a) {
-      atomic_add(&L.gc[15 * (int64_t)st + a], gst[a]);
+      for (int q = 0; q < 9; ++q) {
+        float dv[4];
 #pragma unroll
-      for (int b = a; b < 6; ++b) atomic_add(&L.Dbase[225 * (int64_t)st + 15 * a + b], Dst[6 * a + b]);
+        for (int u = 0; u < 4; ++u) {
+          const int a = (4 * q + u) / 6, b = (4 * q + u) % 6;
+          dv[u] = a <= b ? Dst[6 * a + b] : Dst[6 * b + a];
+        }
+        atomicAdd(D4 + q, make_float4(dv[0], dv[1], dv[2], dv[3]));
+      }
+      atomicAdd(g4, make_float4(gst[0], gst[1], gst[2], gst[3]));
+      atomicAdd(g4 + 1, make_float4(gst[4], gst[5], 0.f, 0.f));
+    } else {
+#pragma unroll
+      for (int a = 0; a < 6; ++a) {
+        atomic_add(&L.gc[15 * (int64_t)st + a], gst[a]);
+#pragma unroll
+        for (int b = a; b < 6; ++b) atomic_add(&L.Dbase[225 * (int64_t)st + 15 * a + b], Dst[6 * a + b]);
+      }
     }
   }
+}
+
+// FP32 path: adds the vector-accumulated visual pose blocks (full 6x6) and
+// gradients into D and g_c (before the lower triangles are mirrored).
+__global__ void __launch_bounds__(kB) k_merge_pose(int64_t nkf, const float* Dpose, const float* gpose, float* D,
+                                                   float* gc, const int* run_if, const int* skip_if) {
+  if (gated(run_if, skip_if)) return;
+  const int64_t i = blockIdx.x * (int64_t)blockDim.x + threadIdx.x;
+  if (i >= 42 * nkf) return;
+  const int64_t k = i / 42, q = i % 42;
+  if (q < 36) D[225 * k + 15 * (q / 6) + q % 6] += Dpose[36 * k + q];
+  else gc[15 * k + q - 36] += gpose[8 * k + q - 36];
 }
 
 // One warp per inertial edge.
@@ -1142,12 +1195,18 @@ cudaError_t solver_assemble(const SolverLaunch<T>& s, const int* gate, cudaStrea
   k_zero<T><<<gridcap(225 * s.P.nkf), kB, 0, st>>>(s.L.Dbase, 225 * s.P.nkf, gate, skip);
   k_zero<T><<<gridcap(15 * s.P.nkf), kB, 0, st>>>(s.L.gc, 15 * s.P.nkf, gate, skip);
   if (s.S.npu) k_zero<T><<<gridcap(36 * s.S.npu), kB, 0, st>>>(s.L.Pbase, 36 * s.S.npu, gate, skip);
+  if constexpr (sizeof(T) == 4) {
+    k_zero<float><<<gridcap(36 * s.P.nkf), kB, 0, st>>>(s.L.Dpose, 36 * s.P.nkf, gate, skip);
+    k_zero<float><<<gridcap(8 * s.P.nkf), kB, 0, st>>>(s.L.gpose, 8 * s.P.nkf, gate, skip);
+  }
   // Relinearizations inside the LM loop (gate set) assemble with the fixed
   // Jacobi scale applied; the first assembly is scaled by solver_compute_scale.
   const int scaled = gate ? 1 : 0;
   if (s.P.nlm) k_assemble_lm<T><<<nblk(s.P.nlm, kB), kB, 0, st>>>(s.P, s.S, s.vis, s.L, scaled, gate, skip);
   if (s.P.nedge)
     k_assemble_inertial<T><<<nblk(32 * s.P.nedge, 128), 128, 0, st>>>(s.P, s.ine, s.L, scaled, gate, skip);
+  if constexpr (sizeof(T) == 4)
+    k_merge_pose<<<nblk(42 * s.P.nkf, kB), kB, 0, st>>>(s.P.nkf, s.L.Dpose, s.L.gpose, s.L.Dbase, s.L.gc, gate, skip);
   k_mirror_pose_blocks<T><<<nblk(15 * s.P.nkf, kB), kB, 0, st>>>(s.P.nkf, s.L.Dbase, gate, skip);
   return cudaGetLastError();
 }
@@ -1292,8 +1351,15 @@ cudaError_t solver_reject_and_restart(const SolverLaunch<T>& s, int use_reprojec
   k_zero<T><<<gridcap(225 * s.P.nkf), kB, 0, st>>>(s.L.Dbase, 225 * s.P.nkf, run, nullptr);
   k_zero<T><<<gridcap(15 * s.P.nkf), kB, 0, st>>>(s.L.gc, 15 * s.P.nkf, run, nullptr);
   if (s.S.npu) k_zero<T><<<gridcap(36 * s.S.npu), kB, 0, st>>>(s.L.Pbase, 36 * s.S.npu, run, nullptr);
+  if constexpr (sizeof(T) == 4) {
+    k_zero<float><<<gridcap(36 * s.P.nkf), kB, 0, st>>>(s.L.Dpose, 36 * s.P.nkf, run, nullptr);
+    k_zero<float><<<gridcap(8 * s.P.nkf), kB, 0, st>>>(s.L.gpose, 8 * s.P.nkf, run, nullptr);
+  }
   if (s.P.nlm) k_assemble_lm<T><<<nblk(s.P.nlm, kB), kB, 0, st>>>(s.P, s.S, s.vis, s.L, 0, run, nullptr);
   if (s.P.nedge) k_assemble_inertial<T><<<nblk(32 * s.P.nedge, 128), 128, 0, st>>>(s.P, s.ine, s.L, 0, run, nullptr);
+  if constexpr (sizeof(T) == 4)
+    k_merge_pose<<<nblk(42 * s.P.nkf, kB), kB, 0, st>>>(s.P.nkf, s.L.Dpose, s.L.gpose, s.L.Dbase, s.L.gc, run,
+                                                        nullptr);
   k_mirror_pose_blocks<T><<<nblk(15 * s.P.nkf, kB), kB, 0, st>>>(s.P.nkf, s.L.Dbase, run, nullptr);
   const int64_t n = 15 * s.P.nkf + 3 * s.P.nlm + s.P.nsw;
   k_scale<T><<<nblk(n, kB), kB, 0, st>>>(s.P, s.L, s.sc, jacobi, run);

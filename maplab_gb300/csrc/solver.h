@@ -129,6 +129,10 @@ struct LinearSystem {
   // one edge's two keyframes): J^T J and gradient (scaled in place), W_f | W_t
   // (scaled Jacobian columns of the keyframes times the switch column), the
   // damped inverse, the scaled step.
+  // FP32 path: the visual terms' 6x6 pose blocks of D and their gradient,
+  // accumulated with 16-byte vector atomics and merged into Dbase / gc.
+  float* Dpose;  // [nkf][36]
+  float* gpose;  // [nkf][8] (6 used)
   T* swH;        // [nsw]
   T* swg;        // [nsw]
   T* swW;        // [nsw][30]
