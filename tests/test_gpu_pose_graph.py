@@ -159,3 +159,23 @@ def test_switch_write_read_round_trip_and_cost():
     m.array("pose_edge_switch")[ty == N.MBA_POSE_EDGE_LOOP_CLOSURE] = 0.5
     co = O.OracleProblem(m.desc).cost()
     assert abs(c - co) <= 1e-12 * co, (c, co)
+
+
+def test_pure_pose_graph_matches_oracle_dense():
+    """No landmarks, no observations: odometry, loop closures with switches
+    and absolute terms only (the kernels of the visual part launch nothing)."""
+    from test_oracle_pose_graph import pose_graph_only
+    m = synth.generate("c1", include_inertial=0, keyframes_per_mission=150, pose_edges=1, loop_closure_stride=5,
+                       loop_closure_outlier_fraction=0.2, absolute_pose_stride=30, seed=13)
+    d = pose_graph_only(m)
+    o = O.OracleProblem(d)
+    so = o.solve(_oracle_opts(8))
+    with ba.BundleAdjuster(d) as g:
+        sg = g.solve(_gpu_opts(8))
+        swg = g.read_switch_variables()
+    _compare_runs(sg, so)
+    np.testing.assert_allclose(swg, o.read_switches(), atol=1e-5)
+    with ba.BundleAdjuster(d) as g:
+        smx = g.solve(ba.default_options(max_num_iterations=15, check_tolerances=0, precision=N.MBA_PRECISION_MIXED,
+                                         preconditioner=N.MBA_PRECOND_CHAIN, use_cuda_graph=2))
+    assert smx["final_cost"] <= sg["final_cost"] * (1 + 1e-3)

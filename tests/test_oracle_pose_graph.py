@@ -186,3 +186,29 @@ def test_library_validates_pose_graph_fields(what, status):
     h = ctypes.c_void_p()
     assert ba.lib().mba_create(ctypes.byref(m.desc), 0, ctypes.byref(h)) == status
     assert not h.value
+
+
+def pose_graph_only(m):
+    """m's descriptor without landmarks and observations (a pure pose graph:
+    odometry, loop closures, absolute terms); the arrays stay owned by m."""
+    d = N.ProblemDesc()
+    ctypes.memmove(ctypes.byref(d), ctypes.byref(m.desc), ctypes.sizeof(d))
+    d.num_landmarks = 0
+    d.num_observations = 0
+    for f in ("obs_uv", "obs_sigma", "obs_landmark", "obs_keyframe", "obs_camera", "lm_p_B", "lm_store_keyframe",
+              "lm_constant"):
+        setattr(d, f, None)
+    return d
+
+
+def test_oracle_solves_a_pure_pose_graph():
+    m = synth.generate("c1", include_inertial=0, keyframes_per_mission=150, pose_edges=1, loop_closure_stride=5,
+                       loop_closure_outlier_fraction=0.2, absolute_pose_stride=30, seed=13)
+    d = pose_graph_only(m)
+    o = O.OracleProblem(d)
+    opts = N.default_solver_options()
+    opts.max_num_iterations = 10
+    opts.linear_solver = N.MBA_LINEAR_SOLVER_DENSE_SCHUR
+    opts.check_tolerances = 0
+    s = o.solve(opts)
+    assert s["final_cost"] < 1e-2 * s["initial_cost"]
