@@ -275,10 +275,12 @@ mba_status ensure_solver_buffers(mba_handle* h, SolverBuffers<T>& b) {
   b.vis.Jl = A.alloc<T>(6 * N);
   b.vis.Js = A.alloc<T>(12 * N);
   b.vis.Jo = A.alloc<T>(12 * N);
-  b.ine.r = A.alloc<T>(15 * NE);
-  b.ine.Jf = A.alloc<T>(225 * NE);
-  b.ine.Jt = A.alloc<T>(225 * NE);
-  b.ine.Js = A.alloc<T>(6 * (NE - P.nimu));
+  if constexpr (sizeof(T) == 4) {  // FP64: the handle's current linearization (make_launch)
+    b.ine.r = A.alloc<T>(15 * NE);
+    b.ine.Jf = A.alloc<T>(225 * NE);
+    b.ine.Jt = A.alloc<T>(225 * NE);
+    b.ine.Js = A.alloc<T>(6 * (NE - P.nimu));
+  }
   LinearSystem<T>& L = b.L;
   L.Hll = A.alloc<T>(9 * NL);
   L.gl = A.alloc<T>(3 * NL);
@@ -416,6 +418,9 @@ SolverBuffers<T>& buffers_of(mba_handle* h) {
 
 template <typename T>
 SolverLaunch<T> make_launch(mba_handle* h, SolverBuffers<T>& b, const mba_solver_options& o) {
+  // FP64 path: the solver reads the current inertial linearization directly.
+  // Set before any graph capture records the pointer.
+  if constexpr (sizeof(T) == 8) b.ine = h->ine_cur;
   SolverLaunch<T> s;
   s.P = h->P;
   s.S = h->S;
@@ -474,10 +479,6 @@ cudaError_t linearize_current(mba_handle* h, SolverBuffers<T>& b, SolverLaunch<T
   if (e == cudaSuccess) e = solver_add_inertial_cost(h->ctl, st);
   if constexpr (sizeof(T) == 4) {
     if (e == cudaSuccess) e = launch_inertial_f32(h->P, h->ine_cur, b.ine, st);
-  } else {
-    // FP64 path: the solver reads the current inertial linearization directly.
-    b.ine = h->ine_cur;
-    s.ine = b.ine;
   }
   if (e == cudaSuccess) e = launch_visual_linearize<T>(h->P, b.vis, nullptr, st);
   if (e == cudaSuccess) e = solver_assemble<T>(s, nullptr, st);

@@ -18,17 +18,29 @@ def _opts(**kw):
     return ba.default_options(**kw)
 
 
-def test_device_loop_matches_host_loop():
+@pytest.mark.parametrize("precision", [N.MBA_PRECISION_FP64, N.MBA_PRECISION_MIXED])
+def test_device_loop_matches_host_loop(precision):
+    """Direct launches, one graph per iteration and the device-driven loop
+    run the same iterations: costs, and the gain ratios (model cost change of
+    the visual and the inertial terms) of every step, on a fresh handle each.
+    FP64 within 1e-6; the mixed path assembles with FP32 atomics (summation
+    order differs from run to run) and stops PCG at its iteration cap, so its
+    runs agree within 1e-3."""
     m = synth.generate("c1")
-    with ba.BundleAdjuster(m.desc) as g:
-        host = g.solve(_opts(use_cuda_graph=1))
-    with ba.BundleAdjuster(m.desc) as g:
-        dev = g.solve(_opts(use_cuda_graph=2))
-    assert dev["num_iterations"] == host["num_iterations"]
-    assert dev["rejected_landmarks"] == host["rejected_landmarks"]
-    for a, b in zip(dev["iterations"], host["iterations"]):
-        assert a["ok"] == b["ok"]
-        assert abs(a["cost"] - b["cost"]) <= 1e-6 * b["cost"], (a, b)
+    runs = []
+    for mode in (0, 1, 2):
+        with ba.BundleAdjuster(m.desc) as g:
+            runs.append(g.solve(_opts(use_cuda_graph=mode, precision=precision)))
+    plain, host, dev = runs
+    tol = 1e-6 if precision == N.MBA_PRECISION_FP64 else 1e-3
+    for other in (host, dev):
+        assert other["num_iterations"] == plain["num_iterations"]
+        assert other["rejected_landmarks"] == plain["rejected_landmarks"]
+        for a, b in zip(other["iterations"], plain["iterations"]):
+            assert a["ok"] == b["ok"]
+            assert abs(a["cost"] - b["cost"]) <= tol * b["cost"], (a, b)
+            if precision == N.MBA_PRECISION_FP64:
+                assert abs(a["relative_decrease"] - b["relative_decrease"]) <= 1e-6, (a, b)
     times = [it["time_ms"] for it in dev["iterations"][1:]]
     assert all(t > 0 for t in times) and times == sorted(times)
 

@@ -161,9 +161,12 @@ def test_switch_write_read_round_trip_and_cost():
     assert abs(c - co) <= 1e-12 * co, (c, co)
 
 
-def test_pure_pose_graph_matches_oracle_dense():
+@pytest.mark.parametrize("graph_mode", [0, 1, 2])
+def test_pure_pose_graph_matches_oracle_dense(graph_mode):
     """No landmarks, no observations: odometry, loop closures with switches
-    and absolute terms only (the kernels of the visual part launch nothing)."""
+    and absolute terms only (the kernels of the visual part launch nothing).
+    Every step's gain ratio rests on the pose edges' model cost change alone,
+    in each loop mode (direct launches, graph per iteration, device loop)."""
     from test_oracle_pose_graph import pose_graph_only
     m = synth.generate("c1", include_inertial=0, keyframes_per_mission=150, pose_edges=1, loop_closure_stride=5,
                        loop_closure_outlier_fraction=0.2, absolute_pose_stride=30, seed=13)
@@ -171,7 +174,7 @@ def test_pure_pose_graph_matches_oracle_dense():
     o = O.OracleProblem(d)
     so = o.solve(_oracle_opts(8))
     with ba.BundleAdjuster(d) as g:
-        sg = g.solve(_gpu_opts(8))
+        sg = g.solve(_gpu_opts(8, use_cuda_graph=graph_mode))
         swg = g.read_switch_variables()
     _compare_runs(sg, so)
     np.testing.assert_allclose(swg, o.read_switches(), atol=1e-5)
