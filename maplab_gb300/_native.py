@@ -184,6 +184,49 @@ class LandmarkQualityOptions(ctypes.Structure):
     ]
 
 
+class VimapInfo(ctypes.Structure):
+    """mba_vimap_info (include/maplab_vimap.h)."""
+    _fields_ = [(n, ctypes.c_int64) for n in (
+        "num_missions", "num_vertices", "num_landmarks", "num_keypoints", "num_viwls_edges", "num_odometry_edges",
+        "num_wheel_odometry_edges", "num_loop_closure_edges", "num_other_edges", "num_absolute_measurements",
+        "num_sensors", "num_cameras")]
+
+
+class VimapExportOptions(ctypes.Structure):
+    """mba_vimap_export_options (include/maplab_vimap.h)."""
+    _fields_ = [
+        ("num_missions", ctypes.c_int32),
+        ("pad0_", ctypes.c_int32),
+        ("missions", ctypes.POINTER(ctypes.c_int32)),
+        ("add_visual_constraints", ctypes.c_int32),
+        ("add_inertial_constraints", ctypes.c_int32),
+        ("add_6dof_odometry_constraints", ctypes.c_int32),
+        ("add_wheel_odometry_constraints", ctypes.c_int32),
+        ("add_absolute_pose_constraints", ctypes.c_int32),
+        ("add_loop_closure_edges", ctypes.c_int32),
+        ("fix_landmark_positions", ctypes.c_int32),
+        ("fix_velocity", ctypes.c_int32),
+        ("fix_gyro_bias", ctypes.c_int32),
+        ("fix_accel_bias", ctypes.c_int32),
+        ("fix_vertices", ctypes.c_int32),
+        ("min_landmarks_per_frame", ctypes.c_int32),
+        ("feature_type", ctypes.c_int32),
+        ("apply_gauge_fixes", ctypes.c_int32),
+        ("landmark_selection", ctypes.c_int32),
+        ("pad1_", ctypes.c_int32),
+        ("landmark_keep", ctypes.POINTER(ctypes.c_uint8)),
+        ("quality", LandmarkQualityOptions),
+        ("gravity_magnitude", ctypes.c_double),
+        ("use_huber", ctypes.c_int32),
+        ("pad2_", ctypes.c_int32),
+    ]
+
+
+MBA_VIMAP_LANDMARKS_QUALITY = 0
+MBA_VIMAP_LANDMARKS_ALL = 1
+MBA_VIMAP_LANDMARKS_MASK = 2
+
+
 class Tuning(ctypes.Structure):
     _fields_ = [
         ("visual_block", ctypes.c_int32),
@@ -367,6 +410,17 @@ def load_ba():
               c_double_p, c_double_p])
     _declare(lib, "mba_visual_cost_noalloc", ctypes.c_int,
              [ctypes.POINTER(VisualBatchDevice), ctypes.c_int32, vp, vp])
+    u64p = ctypes.POINTER(ctypes.c_uint64)
+    _declare(lib, "mba_vimap_load", ctypes.c_int, [ctypes.c_char_p, ctypes.POINTER(vp)])
+    _declare(lib, "mba_vimap_destroy", None, [vp])
+    _declare(lib, "mba_vimap_get_info", ctypes.c_int, [vp, ctypes.POINTER(VimapInfo)])
+    _declare(lib, "mba_vimap_mission_ids", ctypes.c_int, [vp, u64p])
+    _declare(lib, "mba_vimap_default_export_options", None, [ctypes.POINTER(VimapExportOptions)])
+    _declare(lib, "mba_vimap_export", ctypes.c_int, [vp, ctypes.POINTER(VimapExportOptions), ctypes.POINTER(ProblemDesc)])
+    _declare(lib, "mba_vimap_export_ids", ctypes.c_int, [vp, u64p, u64p, u64p, u64p])
+    _declare(lib, "mba_vimap_landmark_ids", ctypes.c_int, [vp, u64p])
+    _declare(lib, "mba_vimap_import_state", ctypes.c_int, [vp] + [c_double_p] * 6)
+    _declare(lib, "mba_vimap_save", ctypes.c_int, [vp, ctypes.c_char_p])
     return lib
 
 

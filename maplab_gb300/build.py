@@ -1,6 +1,7 @@
 """Builds the native libraries in-tree (maplab_gb300/_build/).
 
-* libmaplab_ba.so  — the CUDA back-end (sm_103a only), C ABI of include/maplab_ba.h
+* libmaplab_ba.so  — the CUDA back-end (sm_103a only), C ABI of include/maplab_ba.h, and the
+                    host VIMap map-folder reader / exporter of include/maplab_vimap.h
 * libmba_synth.so  — host-only synthetic map generator (include/maplab_ba_synth.h)
 
 Each translation unit compiles in its own process so a build takes about as
@@ -18,6 +19,7 @@ BUILD = os.path.join(HERE, "_build")
 
 CUDA_SOURCES = ["mba_api.cu", "kernels_eval.cu", "kernels_inertial.cu", "kernels_solver.cu", "kernels_chain.cu",
                 "kernels_gnn.cu", "kernels_pose.cu", "noalloc.cu"]
+HOST_SOURCES = ["vimap_io.cc"]  # host-only parts of libmaplab_ba.so (g++)
 ARCH = ["-gencode", "arch=compute_103a,code=sm_103a"]
 NVCC_FLAGS = ["-O3", "-lineinfo", "-std=c++17", "-Xcompiler", "-fPIC", "-Xcompiler", "-O2",
               "--expt-relaxed-constexpr"]
@@ -65,6 +67,13 @@ def build(verbose=False, ptxas_verbose=False):
             if ptxas_verbose:
                 cmd += ["-Xptxas", "-v"]
             cmds.append(cmd)
+    for src in HOST_SOURCES:
+        s = os.path.join(CSRC, src)
+        o = os.path.join(BUILD, src.replace(".cc", ".o"))
+        objs.append(o)
+        if _stale(o, [s] + headers):
+            cmds.append(["g++", "-O2", "-std=c++17", "-fPIC", "-Wall", "-I", os.path.join(ROOT, "include"), "-c", s,
+                         "-o", o])
     synth_src = os.path.join(CSRC, "synth_map.cc")
     synth_so = os.path.join(BUILD, "libmba_synth.so")
     if _stale(synth_so, [synth_src] + headers):

@@ -36,6 +36,15 @@ def test_ba_library_exports_every_declared_symbol():
     N.load_ba()  # loads (resolves libcudart) without touching a device
 
 
+def test_vimap_entry_points_are_exported():
+    """include/maplab_vimap.h is served by libmaplab_ba.so (host code)."""
+    path = os.path.join(N.BUILD_DIR, "libmaplab_ba.so")
+    decl = _declared("maplab_vimap.h")
+    assert len(decl) >= 10, decl
+    missing = [d for d in decl if d not in _exported(path)]
+    assert not missing, missing
+
+
 def test_synth_library_exports_every_declared_symbol():
     path = os.path.join(N.BUILD_DIR, "libmba_synth.so")
     decl = _declared("maplab_ba_synth.h")
@@ -47,11 +56,13 @@ STRUCTS = {
     "mba_camera": N.Camera, "mba_problem_desc": N.ProblemDesc, "mba_solver_options": N.SolverOptions,
     "mba_iteration_summary": N.IterationSummary, "mba_summary": N.Summary, "mba_problem_stats": N.ProblemStats,
     "mba_synth_config": N.SynthConfig, "mba_visual_batch_device": N.VisualBatchDevice,
+    "mba_vimap_info": N.VimapInfo, "mba_vimap_export_options": N.VimapExportOptions,
 }
 
 
 def test_ctypes_layouts_match_c():
-    lines = ['#include <stdio.h>', '#include <stddef.h>', '#include "maplab_ba_synth.h"', 'int main(void) {']
+    lines = ['#include <stdio.h>', '#include <stddef.h>', '#include "maplab_ba_synth.h"',
+             '#include "maplab_vimap.h"', 'int main(void) {']
     for cname, cls in STRUCTS.items():
         lines.append(f'printf("{cname} sizeof %zu\\n", sizeof({cname}));')
         for f, _ in cls._fields_:
