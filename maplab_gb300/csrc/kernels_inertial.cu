@@ -174,7 +174,6 @@ __global__ void __launch_bounds__(32 * kWarps) k_inertial_mat(DevProblem P, cons
   if (gated_i(skip_if)) return;
   __shared__ MatSmem<TM> smem[kWarps];
   __shared__ double Ld[kWarps][225], Xd[kWarps][225], rsh[kWarps][16];
-  __shared__ int fail_sh[kWarps];
   const int w = threadIdx.x >> 5, lane = threadIdx.x & 31;
   const int64_t e = blockIdx.x * (int64_t)kWarps + w;
   if (e >= P.nimu) return;
@@ -295,28 +294,52 @@ __global__ void __launch_bounds__(32 * kWarps) k_inertial_mat(DevProblem P, cons
     }
     __syncwarp();
   }
-  // ---- FP64 from here: Cholesky of Q_acc (lane 0), L^-1, residual, Jacobians.
+  // ---- FP64 from here: Cholesky of Q_acc, L^-1, residual, Jacobians.
+  // Right-looking Cholesky spread over the warp (Eigen's LLT is a textbook
+  // Cholesky; the order of the subtractions differs, the factor agrees to
+  // rounding).  Lane `lane` owns the lower-triangle elements t = lane + 32 s
+  // (s < 4, t < 120, row-major); each column's pivot square root and
+  // reciprocal are computed by every lane from a broadcast read, and the
+  // reciprocals replace the divisions of the triangular inverse.
   double* L = Ld[w];
   double* X = Xd[w];
-  if (lane == 0) {
-    int fail = 0;
-    for (int a = 0; a < 225; ++a) L[a] = 0.0;
-    for (int j = 0; j < 15 && !fail; ++j) {
-      double d = (double)S.Q[j * 15 + j];
-      for (int q = 0; q < j; ++q) d -= L[j * 15 + q] * L[j * 15 + q];
-      if (!(d > 0.0)) { fail = 1; break; }
-      const double ljj = sqrt(d);
-      L[j * 15 + j] = ljj;
-      for (int i = j + 1; i < 15; ++i) {
-        double v = (double)S.Q[i * 15 + j];
-        for (int q = 0; q < j; ++q) v -= L[i * 15 + q] * L[j * 15 + q];
-        L[i * 15 + j] = v / ljj;
-      }
-    }
-    fail_sh[w] = fail;
+  double* dinv = rsh[w];  // 1 / L_jj until the residual needs rsh
+  int own_i[4], own_k[4];
+#pragma unroll
+  for (int s = 0; s < 4; ++s) {
+    const int t = lane + 32 * s;
+    int r = 0;
+    while ((r + 1) * (r + 2) / 2 <= t) ++r;  // t in row r of the lower triangle
+    own_i[s] = t < 120 ? r : -1;
+    own_k[s] = t < 120 ? t - r * (r + 1) / 2 : -1;
   }
+  for (int a = lane; a < 225; a += 32) L[a] = (double)S.Q[a];
   __syncwarp();
-  if (fail_sh[w]) {
+  int fail = 0;
+  for (int j = 0; j < 15; ++j) {
+    const double d = L[j * 16];
+    if (!(d > 0.0)) {  // the same value in every lane: a uniform exit
+      fail = 1;
+      break;
+    }
+    const double ljj = sqrt(d), inv = 1.0 / ljj;
+    // Phase 1: scale column j below the pivot (every lane has read the pivot
+    // before any lane writes column j).
+#pragma unroll
+    for (int s = 0; s < 4; ++s)
+      if (own_k[s] == j && own_i[s] > j) L[own_i[s] * 15 + j] *= inv;
+    if (lane == 0) dinv[j] = inv;
+    __syncwarp();
+    // Phase 2: the pivot, and the trailing update from the scaled column
+    // (which no lane writes in this phase).
+#pragma unroll
+    for (int s = 0; s < 4; ++s) {
+      if (own_k[s] == j && own_i[s] == j) L[j * 16] = ljj;
+      if (own_k[s] > j) L[own_i[s] * 15 + own_k[s]] -= L[own_i[s] * 15 + j] * L[own_k[s] * 15 + j];
+    }
+    __syncwarp();
+  }
+  if (fail) {
     if (lane == 0 && out.status) atomicMax(out.status, (int)MBA_ERR_NOT_SPD);
     return;
   }
@@ -324,7 +347,7 @@ __global__ void __launch_bounds__(32 * kWarps) k_inertial_mat(DevProblem P, cons
     for (int i = 0; i < 15; ++i) {
       double v = (i == lane) ? 1.0 : 0.0;
       for (int q = 0; q < i; ++q) v -= L[i * 15 + q] * X[q * 15 + lane];
-      X[i * 15 + lane] = v / L[i * 15 + i];
+      X[i * 15 + lane] = v * dinv[i];
     }
   }
   __syncwarp();
