@@ -497,6 +497,15 @@ typedef struct mba_visual_batch_device {
 mba_status mba_visual_cost_noalloc(const mba_visual_batch_device* batch, int32_t device, void* stream,
                                    double* cost_out_device);
 
+/* The learned preconditioner's node update on the tensor cores
+ * (tcgen05, TMA): Z = A W^T + A2 W2^T + bias, H = bf16(relu(Z)), for
+ * kernel-level checks.  Host buffers: A, A2 [n][k] and W, W2 [64][k] as BF16
+ * bit patterns (A2 / W2 may be NULL), bias [64] (may be NULL), Z [n][64],
+ * H [n][64] BF16 bit patterns (may be NULL); k = 32 or 64.  No counterpart
+ * in the reference (maplab preconditions with SCHUR_JACOBI). */
+mba_status mba_gnn_gemm(int32_t device, int64_t n, int32_t k, const uint16_t* A, const uint16_t* W,
+                        const uint16_t* A2, const uint16_t* W2, const float* bias, float* Z, uint16_t* H);
+
 #ifdef __cplusplus
 }
 #endif

@@ -410,6 +410,9 @@ def load_ba():
               c_double_p, c_double_p])
     _declare(lib, "mba_visual_cost_noalloc", ctypes.c_int,
              [ctypes.POINTER(VisualBatchDevice), ctypes.c_int32, vp, vp])
+    u16p = ctypes.POINTER(ctypes.c_uint16)
+    _declare(lib, "mba_gnn_gemm", ctypes.c_int, [ctypes.c_int32, ctypes.c_int64, ctypes.c_int32, u16p, u16p, u16p, u16p,
+                                                 ctypes.POINTER(ctypes.c_float), ctypes.POINTER(ctypes.c_float), u16p])
     u64p = ctypes.POINTER(ctypes.c_uint64)
     _declare(lib, "mba_vimap_load", ctypes.c_int, [ctypes.c_char_p, ctypes.POINTER(vp)])
     _declare(lib, "mba_vimap_destroy", None, [vp])

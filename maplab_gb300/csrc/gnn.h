@@ -86,4 +86,12 @@ struct GnnGraph {
   int32_t* nbr_blk;   // [nnz] >= 0: SP block index (row kf, col nbr); < 0: -(e+1) inertial edge
 };
 
+// Tensor-core node update (kernels_gnn_tc.cu): Z = A W^T (+ A2 W2^T) + bias,
+// H = bf16(relu(Z)); K = 32 or 64, 64 outputs.  `fatal` is raised if a
+// bounded wait of the tensor-core pipeline runs out.
+cudaError_t gnn_gemm_tc_prepare();
+cudaError_t gnn_gemm_tc(int64_t n, int K, const __nv_bfloat16* A, const __nv_bfloat16* W, const __nv_bfloat16* A2,
+                        const __nv_bfloat16* W2, const float* bias, float* Z, __nv_bfloat16* H, int* fatal,
+                        cudaStream_t st);
+
 }  // namespace mba

@@ -430,11 +430,12 @@ __global__ void k_gnn_init(GnnParams p, uint64_t seed) {
   p.g[i] = 0.f;
 }
 
+// The forward node update runs on the tcgen05 tensor cores
+// (kernels_gnn_tc.cu); k_gnn_gemm serves the backward products.
 template <int K>
 cudaError_t launch_gemm_fwd(int64_t n, const bf16* A, const bf16* W, const bf16* A2, const bf16* W2, const float* bias,
-                            float* Z, bf16* H, cudaStream_t st) {
-  k_gnn_gemm<K, kGnnHidden><<<nb(n, 64), 128, 0, st>>>(n, A, W, A2, W2, bias, Z, H);
-  return cudaGetLastError();
+                            float* Z, bf16* H, int* fatal, cudaStream_t st) {
+  return gnn_gemm_tc(n, K, A, W, A2, W2, bias, Z, H, fatal, st);
 }
 
 }  // namespace
@@ -472,11 +473,11 @@ cudaError_t gnn_forward(const SolverLaunch<T>& s, GnnGraph g, GnnParams p, GnnWo
   for (int l = 0; l < kGnnLayers; ++l) {
     if (l == 0) {
       k_gnn_aggregate<kGnnIn><<<nb(32 * n, 128), 128, 0, st>>>(n, g, w.wgt, w.deg, w.h[0], w.m[0]);
-      launch_gemm_fwd<kGnnIn>(n, w.h[0], p.wb + L.w1[0], w.m[0], p.wb + L.w2[0], p.w + L.b[0], w.z[0], w.h[1], st);
+      launch_gemm_fwd<kGnnIn>(n, w.h[0], p.wb + L.w1[0], w.m[0], p.wb + L.w2[0], p.w + L.b[0], w.z[0], w.h[1], &s.ctl->fatal, st);
     } else {
       k_gnn_aggregate<kGnnHidden><<<nb(32 * n, 128), 128, 0, st>>>(n, g, w.wgt, w.deg, w.h[l], w.m[l]);
       launch_gemm_fwd<kGnnHidden>(n, w.h[l], p.wb + L.w1[l], w.m[l], p.wb + L.w2[l], p.w + L.b[l], w.z[l],
-                                  w.h[l + 1], st);
+                                  w.h[l + 1], &s.ctl->fatal, st);
     }
   }
   k_gnn_head<T><<<nb(n, 128), 128, 0, st>>>(s, p, w.h[kGnnLayers], w.o);

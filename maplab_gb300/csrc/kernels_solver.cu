@@ -1043,6 +1043,11 @@ __global__ void __launch_bounds__(kB) k_retract(SolverLaunch<T> s) {
 // The LM decision (single thread).
 __global__ void k_decide(LmControl* ctl, LmParams prm, mba_iteration_summary* log) {
   if (ctl->terminated) return;
+  if (ctl->fatal) {  // a bounded wait in a device pipeline ran out: stop (the host reports MBA_ERR_TIMEOUT)
+    ctl->terminated = 1;
+    ctl->termination = 7;
+    return;
+  }
   const int it = ++ctl->iteration;
   const double mcc = ctl->model_change;
   const double cost = ctl->cost;
@@ -1161,6 +1166,7 @@ __global__ void k_init_control(LmControl* ctl, double radius) {
   ctl->reject_count = 0;
   ctl->cost_ine = 0.0;
   ctl->cost_cand_ine = 0.0;
+  ctl->fatal = 0;
 }
 
 __global__ void k_add_inertial_cost(LmControl* ctl) { ctl->cost += ctl->cost_ine; }

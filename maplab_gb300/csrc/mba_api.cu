@@ -374,6 +374,7 @@ mba_status ensure_gnn_work(mba_handle* h) {
   w.vec = A.alloc<float>(5 * 15 * n);
   w.loss = A.alloc<double>(2);
   if (A.err != cudaSuccess) return MBA_ERR_CUDA;
+  if (gnn_gemm_tc_prepare() != cudaSuccess) return MBA_ERR_CUDA;  // shared-memory opt-in, outside graph capture
   h->gw_ready = true;
   return MBA_OK;
 }
@@ -624,6 +625,7 @@ mba_status run_solve(mba_handle* h, const mba_solver_options& o, mba_summary* su
   std::memset(&c, 0, sizeof(c));
   if (result == MBA_OK || result == MBA_ERR_CANCELLED) cudaMemcpy(&c, h->ctl, sizeof(c), cudaMemcpyDeviceToHost);
   if (device_loop && c.termination == 5) result = MBA_ERR_CANCELLED;
+  if (c.fatal) result = MBA_ERR_TIMEOUT;
   std::vector<mba_iteration_summary> log(o.max_num_iterations + 1);
   cudaMemcpy(log.data(), h->log, sizeof(mba_iteration_summary) * log.size(), cudaMemcpyDeviceToHost);
   if (sum && (result == MBA_OK || result == MBA_ERR_CANCELLED)) {
@@ -2154,6 +2156,43 @@ mba_status mba_set_tuning(mba_handle* h, const mba_tuning* t) {
     h->tuning.chain_tail_nodes = t->chain_tail_nodes;
   }
   return MBA_OK;
+}
+
+mba_status mba_gnn_gemm(int32_t device, int64_t n, int32_t k, const uint16_t* A, const uint16_t* W,
+                        const uint16_t* A2, const uint16_t* W2, const float* bias, float* Z, uint16_t* H) {
+  if (n <= 0 || (k != 32 && k != 64) || !A || !W || !Z || (!A2) != (!W2)) return MBA_ERR_INVALID_ARG;
+  if (cudaSetDevice(device) != cudaSuccess) return MBA_ERR_NO_DEVICE;
+  if (gnn_gemm_tc_prepare() != cudaSuccess) return MBA_ERR_CUDA;
+  const size_t na = sizeof(uint16_t) * (size_t)n * k, nw = sizeof(uint16_t) * 64 * (size_t)k;
+  void *dA = nullptr, *dW = nullptr, *dA2 = nullptr, *dW2 = nullptr, *db = nullptr, *dZ = nullptr, *dH = nullptr,
+       *df = nullptr;
+  cudaError_t e = cudaMalloc(&dA, na);
+  if (e == cudaSuccess) e = cudaMalloc(&dW, nw);
+  if (e == cudaSuccess && A2) e = cudaMalloc(&dA2, na);
+  if (e == cudaSuccess && W2) e = cudaMalloc(&dW2, nw);
+  if (e == cudaSuccess && bias) e = cudaMalloc(&db, 64 * sizeof(float));
+  if (e == cudaSuccess) e = cudaMalloc(&dZ, sizeof(float) * 64 * (size_t)n);
+  if (e == cudaSuccess && H) e = cudaMalloc(&dH, sizeof(uint16_t) * 64 * (size_t)n);
+  if (e == cudaSuccess) e = cudaMalloc(&df, sizeof(int));
+  if (e == cudaSuccess) e = cudaMemcpy(dA, A, na, cudaMemcpyHostToDevice);
+  if (e == cudaSuccess) e = cudaMemcpy(dW, W, nw, cudaMemcpyHostToDevice);
+  if (e == cudaSuccess && A2) e = cudaMemcpy(dA2, A2, na, cudaMemcpyHostToDevice);
+  if (e == cudaSuccess && W2) e = cudaMemcpy(dW2, W2, nw, cudaMemcpyHostToDevice);
+  if (e == cudaSuccess && bias) e = cudaMemcpy(db, bias, 64 * sizeof(float), cudaMemcpyHostToDevice);
+  if (e == cudaSuccess) e = cudaMemset(df, 0, sizeof(int));
+  if (e == cudaSuccess)
+    e = gnn_gemm_tc(n, k, (const __nv_bfloat16*)dA, (const __nv_bfloat16*)dW, (const __nv_bfloat16*)dA2,
+                    (const __nv_bfloat16*)dW2, (const float*)db, (float*)dZ, (__nv_bfloat16*)dH, (int*)df, 0);
+  if (e == cudaSuccess) e = cudaDeviceSynchronize();
+  int fatal = 0;
+  if (e == cudaSuccess) e = cudaMemcpy(&fatal, df, sizeof(int), cudaMemcpyDeviceToHost);
+  if (e == cudaSuccess) e = cudaMemcpy(Z, dZ, sizeof(float) * 64 * (size_t)n, cudaMemcpyDeviceToHost);
+  if (e == cudaSuccess && H) e = cudaMemcpy(H, dH, sizeof(uint16_t) * 64 * (size_t)n, cudaMemcpyDeviceToHost);
+  for (void* p : {dA, dW, dA2, dW2, db, dZ, dH, df})
+    if (p) cudaFree(p);
+  if (e == cudaErrorInvalidValue) return MBA_ERR_INVALID_ARG;
+  if (e != cudaSuccess) return MBA_ERR_CUDA;
+  return fatal ? MBA_ERR_TIMEOUT : MBA_OK;
 }
 
 }  // extern "C"

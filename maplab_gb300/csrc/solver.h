@@ -89,7 +89,7 @@ struct LmControl {
   int32_t reject_count;    // landmarks rejected by the last outlier pass
   int32_t restart_now;     // set by the LM decision: outlier rejection + restart after this iteration
   int32_t loop_active;     // device-driven LM loop: 1 while another iteration follows
-  int32_t pad_;
+  int32_t fatal;           // a bounded device wait ran out (tensor-core pipeline): the solve fails with MBA_ERR_TIMEOUT
   unsigned long long t0_ns;  // device global timer at the start of the solve
 };
 
