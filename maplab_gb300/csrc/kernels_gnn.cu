@@ -1,6 +1,7 @@
 // Graph network for the learned chain-preconditioner coefficients: features,
-// forward pass (BF16 tensor-core products with FP32 accumulation), probe
-// loss with adjoint chain solves, backward pass and Adam.
+// forward pass (the node updates are BF16 products with FP32 accumulation on
+// the tcgen05 tensor cores, kernels_gnn_tc.cu), probe loss with adjoint chain
+// solves, backward pass and Adam.
 #include <cuda_bf16.h>
 #include <cuda_runtime.h>
 
@@ -13,69 +14,7 @@ typedef __nv_bfloat16 bf16;
 
 inline unsigned nb(int64_t n, int b) { return (unsigned)((n + b - 1) / b); }
 
-__device__ __forceinline__ uint32_t ld32(const bf16* p) { return *reinterpret_cast<const uint32_t*>(p); }
-
 __device__ __forceinline__ float sigm(float x) { return 1.f / (1.f + __expf(-x)); }
-
-// D = A B + C, m16n8k16, A row-major BF16, B column-major BF16, FP32 accumulators.
-__device__ __forceinline__ void mma_bf16(float* d, const uint32_t* a, const uint32_t* b) {
-  asm volatile(
-      "mma.sync.aligned.m16n8k16.row.col.f32.bf16.bf16.f32 {%0,%1,%2,%3}, {%4,%5,%6,%7}, {%8,%9}, "
-      "{%0,%1,%2,%3};\n"
-      : "+f"(d[0]), "+f"(d[1]), "+f"(d[2]), "+f"(d[3])
-      : "r"(a[0]), "r"(a[1]), "r"(a[2]), "r"(a[3]), "r"(b[0]), "r"(b[1]));
-}
-
-// Y[n][NOUT] = A[n][KIN] W[NOUT][KIN]^T (+ A2 W2^T) (+ bias); Z gets the FP32
-// result, H (if given) bf16(relu(Y)).  One warp per 16 rows.
-template <int KIN, int NOUT>
-__global__ void __launch_bounds__(128) k_gnn_gemm(int64_t n, const bf16* A, const bf16* W, const bf16* A2,
-                                                  const bf16* W2, const float* bias, float* Z, bf16* H) {
-  const int warp = threadIdx.x >> 5, lane = threadIdx.x & 31;
-  const int64_t row0 = ((int64_t)blockIdx.x * 4 + warp) * 16;
-  if (row0 >= n) return;
-  const int gid = lane >> 2, tig = lane & 3;
-  float acc[NOUT / 8][4];
-#pragma unroll
-  for (int t = 0; t < NOUT / 8; ++t) acc[t][0] = acc[t][1] = acc[t][2] = acc[t][3] = 0.f;
-  const int64_t r0 = row0 + gid, r1 = row0 + gid + 8;
-  for (int src = 0; src < (A2 ? 2 : 1); ++src) {
-    const bf16* Am = src ? A2 : A;
-    const bf16* Wm = src ? W2 : W;
-#pragma unroll
-    for (int ks = 0; ks < KIN / 16; ++ks) {
-      const int c0 = ks * 16 + tig * 2;
-      uint32_t a[4];
-      a[0] = r0 < n ? ld32(Am + r0 * KIN + c0) : 0u;
-      a[1] = r1 < n ? ld32(Am + r1 * KIN + c0) : 0u;
-      a[2] = r0 < n ? ld32(Am + r0 * KIN + c0 + 8) : 0u;
-      a[3] = r1 < n ? ld32(Am + r1 * KIN + c0 + 8) : 0u;
-#pragma unroll
-      for (int t = 0; t < NOUT / 8; ++t) {
-        const int col = t * 8 + gid;
-        uint32_t b[2] = {ld32(Wm + col * KIN + c0), ld32(Wm + col * KIN + c0 + 8)};
-        mma_bf16(acc[t], a, b);
-      }
-    }
-  }
-#pragma unroll
-  for (int t = 0; t < NOUT / 8; ++t) {
-    const int col = t * 8 + tig * 2;
-    const float b0 = bias ? bias[col] : 0.f, b1 = bias ? bias[col + 1] : 0.f;
-#pragma unroll
-    for (int hf = 0; hf < 2; ++hf) {
-      const int64_t row = hf ? r1 : r0;
-      if (row >= n) continue;
-      const float z0 = acc[t][2 * hf] + b0, z1 = acc[t][2 * hf + 1] + b1;
-      Z[row * NOUT + col] = z0;
-      Z[row * NOUT + col + 1] = z1;
-      if (H) {
-        H[row * NOUT + col] = __float2bfloat16_rn(fmaxf(z0, 0.f));
-        H[row * NOUT + col + 1] = __float2bfloat16_rn(fmaxf(z1, 0.f));
-      }
-    }
-  }
-}
 
 // ---- graph features
 
@@ -430,8 +369,7 @@ __global__ void k_gnn_init(GnnParams p, uint64_t seed) {
   p.g[i] = 0.f;
 }
 
-// The forward node update runs on the tcgen05 tensor cores
-// (kernels_gnn_tc.cu); k_gnn_gemm serves the backward products.
+// The forward node update runs on the tcgen05 tensor cores (kernels_gnn_tc.cu).
 template <int K>
 cudaError_t launch_gemm_fwd(int64_t n, const bf16* A, const bf16* W, const bf16* A2, const bf16* W2, const float* bias,
                             float* Z, bf16* H, int* fatal, cudaStream_t st) {
@@ -523,11 +461,13 @@ cudaError_t gnn_loss_backward(const SolverLaunch<T>& s, GnnGraph g, GnnParams p,
       k_gnn_wgrad<kGnnHidden><<<nb(n, 64), 256, 0, st>>>(n, w.dzb, w.m[l], p.g + L.w2[l]);
     }
     if (l == 0) break;
-    // dh_l = dz W1 + aggregation^T (dz W2); W^T products on the tensor cores.
-    k_gnn_gemm<kGnnHidden, kGnnHidden><<<nb(n, 64), 128, 0, st>>>(n, w.dzb, p.wt + L.w1[l], nullptr, nullptr,
-                                                                   nullptr, w.dh, nullptr);
-    k_gnn_gemm<kGnnHidden, kGnnHidden><<<nb(n, 64), 128, 0, st>>>(n, w.dzb, p.wt + L.w2[l], nullptr, nullptr,
-                                                                   nullptr, w.dm, nullptr);
+    // dh_l = dz W1 + aggregation^T (dz W2); the W^T products on the tcgen05 tensor cores.
+    cudaError_t e2 = gnn_gemm_tc(n, kGnnHidden, w.dzb, p.wt + L.w1[l], nullptr, nullptr, nullptr, w.dh, nullptr,
+                                 &s.ctl->fatal, st);
+    if (e2 == cudaSuccess)
+      e2 = gnn_gemm_tc(n, kGnnHidden, w.dzb, p.wt + L.w2[l], nullptr, nullptr, nullptr, w.dm, nullptr, &s.ctl->fatal,
+                       st);
+    if (e2 != cudaSuccess) return e2;
     k_gnn_aggregate_bwd<kGnnHidden><<<nb(32 * n, 128), 128, 0, st>>>(n, g, w.wgt, w.deg, w.dm, w.dh);
   }
   return cudaGetLastError();

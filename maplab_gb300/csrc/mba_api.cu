@@ -1946,11 +1946,15 @@ mba_status mba_gnn_train(mba_handle* h, mba_gnn* m, double radius, int32_t nprob
   if (ms != MBA_OK) return ms;
   cudaStream_t st = h->stream;
   for (int32_t k = 0; k < steps; ++k) {
-    cudaError_t e = gnn_loss_backward<float>(s, s.gg, m->p, s.gw, nprobe, nullptr, seed + 104729ull * k, st);
+    cudaError_t e = cudaMemsetAsync(&h->ctl->fatal, 0, sizeof(int32_t), st);
+    if (e == cudaSuccess) e = gnn_loss_backward<float>(s, s.gg, m->p, s.gw, nprobe, nullptr, seed + 104729ull * k, st);
     double loss = 0.0;
+    int32_t fatal = 0;
     if (e == cudaSuccess) e = cudaMemcpyAsync(&loss, s.gw.loss, sizeof(double), cudaMemcpyDeviceToHost, st);
+    if (e == cudaSuccess) e = cudaMemcpyAsync(&fatal, &h->ctl->fatal, sizeof(int32_t), cudaMemcpyDeviceToHost, st);
     if (e == cudaSuccess) e = cudaStreamSynchronize(st);
     if (e != cudaSuccess) return MBA_ERR_CUDA;
+    if (fatal) return MBA_ERR_TIMEOUT;
     if (losses) losses[k] = loss;
     if (!std::isfinite(loss)) return MBA_ERR_NON_FINITE;
     if (lr > 0.f) {
@@ -1983,12 +1987,16 @@ mba_status mba_gnn_gradient(mba_handle* h, mba_gnn* m, double radius, int32_t np
     e = cudaMalloc(&dprobe, sizeof(float) * n15 * nprobe);
     if (e == cudaSuccess) e = cudaMemcpyAsync(dprobe, probes, sizeof(float) * n15 * nprobe, cudaMemcpyHostToDevice, st);
   }
+  if (e == cudaSuccess) e = cudaMemsetAsync(&h->ctl->fatal, 0, sizeof(int32_t), st);
   if (e == cudaSuccess) e = gnn_loss_backward<float>(s, s.gg, m->p, s.gw, nprobe, dprobe, seed, st);
+  int32_t fatal = 0;
   if (e == cudaSuccess && grad) e = cudaMemcpyAsync(grad, m->p.g, sizeof(float) * np, cudaMemcpyDeviceToHost, st);
   if (e == cudaSuccess && loss) e = cudaMemcpyAsync(loss, s.gw.loss, sizeof(double), cudaMemcpyDeviceToHost, st);
   if (e == cudaSuccess && coef) e = cudaMemcpyAsync(coef, s.C.coef, sizeof(double) * 3 * h->P.nkf, cudaMemcpyDeviceToHost, st);
+  if (e == cudaSuccess) e = cudaMemcpyAsync(&fatal, &h->ctl->fatal, sizeof(int32_t), cudaMemcpyDeviceToHost, st);
   if (e == cudaSuccess) e = cudaStreamSynchronize(st);
   if (dprobe) cudaFree(dprobe);
+  if (e == cudaSuccess && fatal) return MBA_ERR_TIMEOUT;
   return cuda_status(e);
 }
 
