@@ -387,7 +387,7 @@ typedef struct mba_tuning {
   int32_t schur_chunk;          /* slot pairs summed per thread by the Schur pair kernel */
   int32_t chain_tail_nodes;     /* chain positions below which one block finishes a chain sweep */
   int32_t visual_min_blocks;    /* register cap of the evaluation kernel: blocks of 256 per SM (1 = none;
-                                 * one thread per observation: 1 or 3; pipelined: 1 or 2) */
+                                 * one thread per observation: 1, 3 or 4; pipelined: 1 or 2) */
   double visual_ms;             /* per launch, chosen setting */
   double schur_ms;
   double chain_apply_ms;

@@ -813,18 +813,12 @@ cudaError_t launch_visual_linearize_gated(const DevProblem& P, VisualLin<T> out,
     return cudaGetLastError();
   }
   const int64_t blocks = (P.nobs + bs - 1) / bs;
-  const bool lean = P.vis_minb > 1;
-  if (cost_accum) {
-    if (lean)
-      k_visual_linearize<T, true, 3><<<(unsigned)blocks, bs, 0, s>>>(P, visual_inputs<T>(P), out, cost_accum, run_if, skip_if);
-    else
-      k_visual_linearize<T, true, 1><<<(unsigned)blocks, bs, 0, s>>>(P, visual_inputs<T>(P), out, cost_accum, run_if, skip_if);
-  } else {
-    if (lean)
-      k_visual_linearize<T, false, 3><<<(unsigned)blocks, bs, 0, s>>>(P, visual_inputs<T>(P), out, nullptr, run_if, skip_if);
-    else
-      k_visual_linearize<T, false, 1><<<(unsigned)blocks, bs, 0, s>>>(P, visual_inputs<T>(P), out, nullptr, run_if, skip_if);
-  }
+  // Register caps: minb 1 none, 3 -> 85 registers, 4 -> 64 registers (more warps per SM, more spills).
+  auto kern = cost_accum ? (P.vis_minb >= 4 ? k_visual_linearize<T, true, 4>
+                            : P.vis_minb > 1 ? k_visual_linearize<T, true, 3> : k_visual_linearize<T, true, 1>)
+                         : (P.vis_minb >= 4 ? k_visual_linearize<T, false, 4>
+                            : P.vis_minb > 1 ? k_visual_linearize<T, false, 3> : k_visual_linearize<T, false, 1>);
+  kern<<<(unsigned)blocks, bs, 0, s>>>(P, visual_inputs<T>(P), out, cost_accum, run_if, skip_if);
   return cudaGetLastError();
 }
 template <typename T>

@@ -2082,8 +2082,8 @@ mba_status autotune(mba_handle* h, mba_tuning* out) {
   // or the pipelined persistent loop, and the block size
   double tbest = 1e30;
   for (int pipe : {0, 1})
-    for (int minb : {1, 2, 3}) {
-      if (pipe ? minb == 3 : minb == 2) continue;  // one-per-thread: 1 or 3 blocks; pipelined: 1 or 2
+    for (int minb : {1, 2, 3, 4}) {
+      if (pipe ? minb >= 3 : minb == 2) continue;  // one-per-thread: 1, 3 or 4 blocks; pipelined: 1 or 2
       for (int bs : {64, 128, 256}) {
         DevProblem P = h->P;
         P.vis_block = bs;
@@ -2146,7 +2146,7 @@ mba_status mba_set_tuning(mba_handle* h, const mba_tuning* t) {
   cudaSetDevice(h->device);
   if (t->visual_block) { h->P.vis_block = t->visual_block; h->tuning.visual_block = t->visual_block; }
   if (t->visual_min_blocks) {
-    if (t->visual_min_blocks < 1 || t->visual_min_blocks > 3) return MBA_ERR_INVALID_ARG;
+    if (t->visual_min_blocks < 1 || t->visual_min_blocks > 4) return MBA_ERR_INVALID_ARG;
     h->P.vis_minb = t->visual_min_blocks;
     h->tuning.visual_min_blocks = t->visual_min_blocks;
   }
