@@ -784,18 +784,25 @@ __global__ void __launch_bounds__(128) k_pcg_spmv(SolverLaunch<T> s, int it, con
   double pq = 0.0;
   if (k < s.P.nkf) {
     // Pose-pose blocks of row k: 5 blocks per warp step, 6 lanes per block,
-    // lane r of a block owns output row r (6 contiguous values of the block).
+    // lane r of a block owns output row r.  A block below the diagonal is
+    // read as the transpose of the stored upper block (column r), so both
+    // rows of a co-visible pair read the same bytes and the second read
+    // mostly hits L2 (the pair's rows run close together).
     T acc = T(0);
     const int sub = lane / 6, r = lane - 6 * (lane / 6);
+    const int64_t npu = s.S.npu;
     if (sub < 5) {
       const int64_t e1 = s.S.row_off[k + 1];
       for (int64_t e = s.S.row_off[k] + sub; e < e1; e += 5) {
         const int64_t j = s.S.row_col[e];
-        const T* B = s.L.SP + 36 * (int64_t)s.S.row_blk[e] + 6 * r;
+        const int64_t blk = s.S.row_blk[e];
+        const bool lower = blk >= npu;
+        const T* B = lower ? s.L.SP + 36 * (blk - npu) + r : s.L.SP + 36 * blk + 6 * r;
+        const int step = lower ? 6 : 1;
         const T* zj = z + 15 * j;
         const T* pj = pa + 15 * j;
 #pragma unroll
-        for (int c = 0; c < 6; ++c) acc += B[c] * (zj[c] + tb * pj[c]);
+        for (int c = 0; c < 6; ++c) acc += B[c * step] * (zj[c] + tb * pj[c]);
       }
     }
     red[w][lane] = acc;
