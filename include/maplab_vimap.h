@@ -89,7 +89,7 @@ typedef struct mba_vimap_export_options {
   int32_t landmark_selection;            /* MBA_VIMAP_LANDMARKS_* */
   int32_t pad1_;
   const uint8_t* landmark_keep;          /* [num_landmarks of the map] for MBA_VIMAP_LANDMARKS_MASK */
-  mba_landmark_quality_options quality;  /* elq_* flags for kUnknown landmarks (reprojection test unsupported here) */
+  mba_landmark_quality_options quality;  /* elq_* flags for kUnknown landmarks */
   double gravity_magnitude;              /* default GravityProvider(392 m, 47.22 deg) of ba_altitude_meters /
                                             ba_latitude; <= 0: the mission IMU's gravity_magnitude_mps2 */
   int32_t use_huber;                     /* visual Huber loss (optimization-terms-addition.cc:189-198), 1 */
@@ -104,7 +104,8 @@ void mba_vimap_default_export_options(mba_vimap_export_options* o);
  * backbone from the root vertex (getAllVertexIdsInMissionAlongGraph,
  * vi-map.cc:2281-2316); landmarks by store keyframe, then store order;
  * observations by observer keyframe, frame, keypoint; inertial edges along
- * the backbone; pose edges odometry, wheel odometry, absolute, loop closures. */
+ * the backbone; pose edges wheel odometry, 6-DoF odometry, absolute, loop
+ * closures (the builder's order). */
 mba_status mba_vimap_export(mba_vimap* m, const mba_vimap_export_options* o, mba_problem_desc* desc);
 
 /* Ids of the last export's rows (2 x uint64 each; NULL skips an array):

@@ -600,6 +600,7 @@ void jpl_block(const double* T_X_B, double* out) {
 struct Frame {
   bool set = false;    // frame id valid (an unset frame carries the invalid id)
   bool valid = true;   // is_valid absent or true
+  int64_t timestamp_ns = 0;
   std::vector<double> uv;     // 2 per keypoint
   std::vector<double> sigma;  // 1 per keypoint
   std::vector<Id> lm;         // observed landmark per keypoint (may be invalid)
@@ -733,6 +734,12 @@ bool parse_frame(Bytes b, Frame* f) {
       case 1:
         if (!w.bytes(&sub) || !read_id(sub, &id)) return false;
         break;
+      case 2: {
+        uint64_t t;
+        if (wt != 0 || !w.varint(&t)) return false;
+        f->timestamp_ns = (int64_t)t;
+        break;
+      }
       case 3:
         if (!w.doubles(wt, &f->uv)) return false;
         break;
@@ -1425,6 +1432,37 @@ const Camera* camera_of(const mba_vimap* M, const Vertex& v, int frame) {
   return &nc.cameras[frame];
 }
 
+// Squared pixel error of p_C against a keypoint (computeSquaredReprojectionError,
+// landmark-quality-metrics.cc:57-73): pinhole projection with the camera's
+// distortion (camera-pinhole.cc:65-164, distortion-radtan.cc:14-65,
+// distortion-equidistant.cc:14-50); points not in front of the camera give
+// the largest double.  Keypoints outside the image box still count.
+double reprojection_sq(const mba_camera& c, const double* pC, double u, double v) {
+  if (!(pC[2] > 1e-10)) return std::numeric_limits<double>::max();
+  const double rz = 1.0 / pC[2];
+  double x = pC[0] * rz, y = pC[1] * rz;
+  const double* k = c.distortion;
+  if (c.distortion_type == MBA_DISTORTION_RADTAN) {
+    const double xx = x * x, yy = y * y, xy = x * y, r2 = xx + yy;
+    const double rad = k[0] * r2 + k[1] * r2 * r2;
+    const double nx = x + x * rad + 2.0 * k[2] * xy + k[3] * (r2 + 2.0 * xx);
+    const double ny = y + y * rad + 2.0 * k[3] * xy + k[2] * (r2 + 2.0 * yy);
+    x = nx;
+    y = ny;
+  } else if (c.distortion_type == MBA_DISTORTION_EQUIDISTANT) {
+    const double r = std::sqrt(x * x + y * y);
+    if (r >= 1e-10) {
+      const double th = std::atan(r), t2 = th * th, t4 = t2 * t2, t6 = t2 * t4, t8 = t4 * t4;
+      const double thd = th * (1 + k[0] * t2 + k[1] * t4 + k[2] * t6 + k[3] * t8);
+      const double s = thd / r;
+      x *= s;
+      y *= s;
+    }
+  }
+  const double du = c.intrinsics[0] * x + c.intrinsics[2] - u, dv = c.intrinsics[1] * y + c.intrinsics[3] - v;
+  return du * du + dv * dv;
+}
+
 // isVisualLandmarkWellConstrained (landmark-quality-metrics.cc:105-172) on
 // the map: observers from the landmark's back-links, camera centres and the
 // landmark in G through the Hamilton T_G_M, T_M_I and T_B_C of the map.
@@ -1469,6 +1507,13 @@ int well_constrained(const mba_vimap* M, const Landmark& L, const Vertex& store,
     const double d = std::sqrt(r[0] * r[0] + r[1] * r[1] + r[2] * r[2]);
     min_sd = std::min(min_sd, pC[2] < 0.0 ? -d : d);
     if (d > 0) rays.push_back({r[0] / d, r[1] / d, r[2] / d});
+    if (q.max_reprojection_error_px > 0.0) {
+      const Frame& fr = ov.frames[b.frame];
+      if (!fr.set || b.keypoint < 0 || b.keypoint >= (int32_t)fr.sigma.size()) return -1;
+      mba_camera cc = cam->c;
+      const double e2 = reprojection_sq(cc, pC, fr.uv[2 * b.keypoint], fr.uv[2 * b.keypoint + 1]);
+      if (e2 > q.max_reprojection_error_px * q.max_reprojection_error_px) return 0;
+    }
   }
   if (min_sd > q.max_distance_from_closest_observer || min_sd < q.min_distance_from_closest_observer) return 0;
   double min_cos = 1.0;
@@ -1511,8 +1556,6 @@ mba_status do_export(mba_vimap* M, const mba_vimap_export_options& o, mba_proble
   std::vector<int> pm_of(M->missions.size(), -1);
   for (size_t p = 0; p < sel.size(); ++p) pm_of[sel[p]] = (int)p;
   X.mission = sel;
-  if (o.landmark_selection == MBA_VIMAP_LANDMARKS_QUALITY && o.quality.max_reprojection_error_px > 0.0)
-    return MBA_ERR_INVALID_ARG;  // the reprojection test runs on the device (mba_landmark_quality)
   if (o.landmark_selection < 0 || o.landmark_selection > 2) return MBA_ERR_INVALID_ARG;
   if (o.landmark_selection == MBA_VIMAP_LANDMARKS_MASK && !o.landmark_keep) return MBA_ERR_INVALID_ARG;
 
@@ -1795,8 +1838,13 @@ mba_status do_export(mba_vimap* M, const mba_vimap_export_options& o, mba_proble
       if (st != MBA_OK) return st;
       for (int k : mission_kfs[p]) {
         const Vertex& v = M->vertices[X.kf_vertex[k]];
+        // Vertex::getMinTimestampNanoseconds: the earliest set frame.
+        int64_t min_ts = std::numeric_limits<int64_t>::max();
+        for (const Frame& f : v.frames)
+          if (f.set) min_ts = std::min(min_ts, f.timestamp_ns);
         for (size_t a = 0; a < v.abs.size(); ++a) {
           if (v.abs[a].sensor != m.absolute) return MBA_ERR_INVALID_ARG;  // :684-687
+          if (v.abs[a].timestamp_ns != min_ts) return MBA_ERR_INVALID_ARG;  // :688-693
           push_pe(MBA_POSE_EDGE_ABSOLUTE, k, k, v.abs[a].T_G_S, v.abs[a].cov, ext, 1.0, 0.0, 1, X.kf_vertex[k],
                   (int)a);
         }

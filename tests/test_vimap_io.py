@@ -156,6 +156,22 @@ def test_unknown_quality_is_evaluated_like_the_oracle(tmp_path):
     assert d.num_observations == int(np.isin(m.array("obs_landmark"), np.flatnonzero(good)).sum())
 
 
+@pytest.mark.parametrize("max_px", [0.8, 2.5])
+def test_unknown_quality_with_the_reprojection_test(tmp_path, max_px):
+    """elq_max_reprojection_error_px > 0: the host metric projects every
+    observation (pinhole + distortion) like the oracle does."""
+    m, folder = _quality_case(tmp_path, 0)
+    q = ba.default_landmark_quality_options(max_reprojection_error_px=max_px)
+    good = O.OracleProblem(m.desc).landmark_quality(q)
+    base = O.OracleProblem(m.desc).landmark_quality(ba.default_landmark_quality_options())
+    assert good.sum() < base.sum()  # the bound removes landmarks
+    with vimap.VIMap(folder) as vm:
+        vm.export(quality=dict(max_reprojection_error_px=max_px))
+        kept = np.zeros(m.desc.num_landmarks, dtype=bool)
+        kept[synth_index(vm.export_ids()["landmarks"])] = True
+    np.testing.assert_array_equal(kept, good)
+
+
 def test_quality_flags_decide_without_evaluation(tmp_path):
     q = np.where(np.arange(2000) % 3 == 0, 1, 2)  # every third landmark kBad, the rest kGood
     m, folder = _quality_case(tmp_path, q)
@@ -257,6 +273,30 @@ def test_reference_sensor_files(tmp_path, name, ncam):
     T_B_C = T_inverse(from_jpl_block(b))
     np.testing.assert_allclose(quat_R(T_B_C[:4]), M[:, :3], atol=1e-6)
     np.testing.assert_allclose(T_B_C[4:], M[:, 3], atol=1e-9)
+
+
+def test_absolute_measurement_timestamp_must_match_the_vertex(tmp_path):
+    """addAbsolutePoseConstraintTermsForVertices CHECKs that a measurement
+    carries its vertex's timestamp; the export refuses a mismatch."""
+    from vimap_writer import f_varint
+    m = synth.generate("c1", absolute_pose_stride=25)
+    folder = tmp_path / "map"
+    write_map(m, str(folder))
+    k = int(m.array("pose_edge_from")[m.array("pose_edge_type") == N.MBA_POSE_EDGE_ABSOLUTE][0])
+    with vimap.VIMap(str(folder)) as vm:
+        d = vm.export(add_absolute_pose_constraints=1)
+        assert d.num_pose_edges > 0
+    # the measurement of vertex k is stamped 1000 k: give it another time
+    f = next(p for p in sorted((folder / "vi_map").iterdir()) if p.name.startswith("vertices") and
+             f_varint(1, 1000 * k) + bytes([0x12]) in p.read_bytes())
+    b = f.read_bytes()
+    old_ts = f_varint(1, 1000 * k) + bytes([0x12])
+    f.write_bytes(b.replace(old_ts, f_varint(1, 1000 * k + 1) + bytes([0x12]), 1))
+    with vimap.VIMap(str(folder)) as vm:
+        with pytest.raises(ba.BAError) as e:
+            vm.export(add_absolute_pose_constraints=1)
+        assert e.value.status == N.MBA_ERR_INVALID_ARG
+        vm.export()  # without absolute terms the map exports
 
 
 def test_packed_encoding_reads_the_same(tmp_path):
