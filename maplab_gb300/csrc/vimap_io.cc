@@ -695,6 +695,7 @@ struct mba_vimap {
   std::vector<Sensor> sensors;
   IdMap<int> sensor_of;
   IdMap<std::array<double, 7>> T_B_S;        // extrinsics by sensor id
+  int64_t legacy_index_ids = 0, index_entries = 0;
 
   // Last export.
   struct Export {
@@ -1126,7 +1127,12 @@ bool parse_vimap_file(int file, mba_vimap* M) {
       if (wt != 2 || !w.bytes(&sub)) return false;
       (fld == 2 ? vmsg : fld == 4 ? emsg : fld == 6 ? mmsg : bmsg).push_back(sub);
     } else if (fld == 9) {
-      return false;  // legacy store/global landmark ids (vi-map-serialization.cc:194-212): not supported
+      // Legacy store/global landmark ids: the frames name landmarks by these;
+      // after loading, their ids are rewritten from the landmarks' back-links
+      // (vi-map-serialization.cc:194-212).
+      Id id;
+      if (wt != 2 || !w.bytes(&sub) || !read_id(sub, &id)) return false;
+      ++M->legacy_index_ids;
     } else if (fld == 10) {
       if (wt != 2 || !w.bytes(&sub)) return false;
       Wire r(sub);
@@ -1143,6 +1149,7 @@ bool parse_vimap_file(int file, mba_vimap* M) {
       }
       if (!r.ok() || !vtx.valid() || !lm.valid()) return false;
       M->landmark_store[lm] = vtx;
+      ++M->index_entries;
     } else if (!w.skip(wt)) {
       return false;
     }
@@ -1403,6 +1410,21 @@ mba_status load(const char* folder, mba_vimap* M) {
     if (!M->vertex_of.count(kv.second)) return MBA_ERR_OUT_OF_RANGE_INDEX;
   }
   for (const auto& kv : M->landmark_at) M->landmark_store[kv.first] = M->vertices[kv.second.first].id;
+  if (M->legacy_index_ids > 0) {
+    if (M->legacy_index_ids != M->index_entries) return MBA_ERR_INVALID_ARG;  // vi-map-serialization.cc:198
+    // Every observation names its landmark by the landmark's own id again.
+    for (const Vertex& sv : M->vertices)
+      for (const Landmark& L : sv.landmarks)
+        for (const Backlink& b : L.obs) {
+          auto vi = M->vertex_of.find(b.vertex);
+          if (vi == M->vertex_of.end()) return MBA_ERR_OUT_OF_RANGE_INDEX;
+          Vertex& ov = M->vertices[vi->second];
+          if (b.frame < 0 || b.frame >= (int32_t)ov.frames.size()) return MBA_ERR_OUT_OF_RANGE_INDEX;
+          Frame& f = ov.frames[b.frame];
+          if (b.keypoint < 0 || b.keypoint >= (int32_t)f.lm.size()) return MBA_ERR_OUT_OF_RANGE_INDEX;
+          f.lm[b.keypoint] = L.id;
+        }
+  }
   for (const Edge& e : M->edges) {
     if (!M->vertex_of.count(e.from) || !M->vertex_of.count(e.to)) return MBA_ERR_OUT_OF_RANGE_INDEX;
     if (e.kind == kViwls)

@@ -299,6 +299,23 @@ def test_absolute_measurement_timestamp_must_match_the_vertex(tmp_path):
         vm.export()  # without absolute terms the map exports
 
 
+def test_legacy_landmark_index_ids_are_rewritten(tmp_path):
+    """Legacy maps (landmark_index_ids present): the frames' landmark ids are
+    replaced by those of the landmarks' back-links
+    (vi-map-serialization.cc:194-212); the export equals the modern map's."""
+    m = synth.generate("c1", keyframes_per_mission=40, num_landmarks=500)
+    write_map(m, str(tmp_path / "new"))
+    write_map(m, str(tmp_path / "old"), legacy_ids=True)
+    with vimap.VIMap(str(tmp_path / "new")) as a, vimap.VIMap(str(tmp_path / "old")) as b:
+        da = a.export(landmark_selection=N.MBA_VIMAP_LANDMARKS_ALL)
+        db = b.export(landmark_selection=N.MBA_VIMAP_LANDMARKS_ALL)
+        assert da.num_observations == db.num_observations == m.desc.num_observations
+        for name, shape, dt in (("obs_landmark", (da.num_observations,), np.int32),
+                                ("obs_uv", (da.num_observations, 2), np.float64),
+                                ("lm_p_B", (da.num_landmarks, 3), np.float64)):
+            np.testing.assert_array_equal(arr(da, name, shape, dt), arr(db, name, shape, dt))
+
+
 def test_packed_encoding_reads_the_same(tmp_path):
     m = synth.generate("c1", include_inertial=0, pose_edges=1)
     for packed in (False, True):

@@ -128,10 +128,11 @@ def _yaml_vector(v, indent):
     return f"{pad}rows: {len(v)}\n{pad}cols: 1\n{pad}data:\n{data}\n"
 
 
-def write_map(m, folder, quality=2, vertices_per_file=40, edges_per_file=60, packed=False):
+def write_map(m, folder, quality=2, vertices_per_file=40, edges_per_file=60, packed=False, legacy_ids=False):
     """Writes synthetic map `m` to `folder`.  quality: landmark quality for all
     landmarks (0 kUnknown, 1 kBad, 2 kGood) or an array per landmark.
-    Returns the ids used, for the tests' checks."""
+    legacy_ids: the frames name landmarks by separate "global" ids listed in
+    landmark_index_ids (the legacy map layout).  Returns the ids used."""
     d = m.desc
     NK, NL, NO, NC, NM = d.num_keyframes, d.num_landmarks, d.num_observations, d.num_cameras, d.num_missions
     kx, kv, kbg, kba = m.array("kf_q_IM_p_MI"), m.array("kf_v_M"), m.array("kf_b_g"), m.array("kf_b_a")
@@ -153,6 +154,7 @@ def write_map(m, folder, quality=2, vertices_per_file=40, edges_per_file=60, pac
 
     vid = [make_id("vertex", k) for k in range(NK)]
     lid = [make_id("landmark", l) for l in range(NL)]
+    gid = [(w0, w1 ^ 0xABCD00) for (w0, w1) in lid] if legacy_ids else lid  # ids the frames carry
     mid = [make_id("mission", q) for q in range(NM)]
     bid = [make_id("baseframe", q) for q in range(NM)]
     imu_sensor, ncam_sensor = make_id("sensor", 0), make_id("sensor", 1)
@@ -223,7 +225,7 @@ def write_map(m, folder, quality=2, vertices_per_file=40, edges_per_file=60, pac
             obs = by_frame.get((k, c), [])
             fb = (f_id(1, make_id("frame", k * 64 + c)) + f_varint(2, 1000 * k) +
                   f_doubles(3, ouv[obs] if obs else [], packed) + f_doubles(4, osig[obs] if obs else [], packed) +
-                  b"".join(f_id(7, lid[olm[i]]) for i in obs) + f_bytes(5, b"") + f_varint(9, 1))
+                  b"".join(f_id(7, gid[olm[i]]) for i in obs) + f_bytes(5, b"") + f_varint(9, 1))
             frames += f_bytes(2, fb)
         nframe = f_id(1, make_id("nframe", k)) + frames
         store = b""
@@ -271,7 +273,8 @@ def write_map(m, folder, quality=2, vertices_per_file=40, edges_per_file=60, pac
     for fi, a in enumerate(range(0, max(len(edges), 1), edges_per_file)):
         data = b"".join(f_id(3, eid[i]) + f_bytes(4, edges[i][2]) for i in range(a, min(len(edges), a + edges_per_file)))
         put(f"edges{fi}", 2, data)
-    put("landmark_index", 3, b"".join(f_bytes(10, f_id(1, vid[lst[l]]) + f_id(2, lid[l])) for l in range(NL)))
+    put("landmark_index", 3, b"".join(f_bytes(10, f_id(1, vid[lst[l]]) + f_id(2, lid[l])) for l in range(NL)) +
+        (b"".join(f_id(9, gid[l]) for l in range(NL)) if legacy_ids else b""))
 
     meta = "".join(f'files {{\n  file_type: {t}\n  path: "{n}"\n}}\n' for t, n in files)
     with open(os.path.join(vi_dir, "vi_map_metadata"), "w") as f:
