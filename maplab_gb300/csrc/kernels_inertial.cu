@@ -182,6 +182,8 @@ __global__ void __launch_bounds__(32 * kWarps) k_inertial_mat(DevProblem P, cons
   for (int a = lane; a < 225; a += 32) {
     S.Q[a] = TM(0);
     S.Phi[a] = (a % 16 == 0) ? TM(1) : TM(0);
+    S.td[a] = TM(0);  // rows 3-5 and 9-11 of td / PC stay zero for the whole edge
+    S.PC[a] = TM(0);
   }
   __syncwarp();
   const int64_t o0 = P.e_off[e];
@@ -212,9 +214,10 @@ __global__ void __launch_bounds__(32 * kWarps) k_inertial_mat(DevProblem P, cons
 #pragma unroll
         for (int j = 0; j < 3; ++j)
           F60[3 * i + j] = F69[3 * i] * axm[j] + F69[3 * i + 1] * axm[3 + j] + F69[3 * i + 2] * axm[6 + j];
-      // td = F T (T = I + D) and PC = F Pm, rows 0-2, 6-8, 12-14.
-      for (int a = lane; a < 225; a += 32) {
-        const int r = a / 15, c = a % 15;
+      // td = F T (T = I + D) and PC = F Pm, rows 0-2, 6-8, 12-14 (the other
+      // rows are zero: the 135 active elements are spread over the lanes).
+      for (int qa = lane; qa < 135; qa += 32) {
+        const int r = 6 * (qa / 45) + (qa % 45) / 15, c = qa % 15, a = 15 * r + c;
         TM t = TM(0), pc = TM(0);
         if (r < 3) {
           t = (c < 3 ? F00[3 * r + c] : TM(0)) + F00[3 * r] * S.D[c] + F00[3 * r + 1] * S.D[15 + c] +
@@ -258,17 +261,15 @@ __global__ void __launch_bounds__(32 * kWarps) k_inertial_mat(DevProblem P, cons
       S.Pm[a] = dt * S.sumcd[a] / TM(6);
     }
     __syncwarp();
-    // M = A Q (td), N = A Phi (PC); only active rows are non-zero.
-    for (int a = lane; a < 225; a += 32) {
-      const int r = a / 15, c = a % 15;
+    // M = A Q (td), N = A Phi (PC); only the active rows are non-zero.
+    for (int qa = lane; qa < 135; qa += 32) {
+      const int r = 6 * (qa / 45) + (qa % 45) / 15, c = qa % 15, a = 15 * r + c;
       TM m = TM(0), n = TM(0);
-      if (active_row(r)) {
 #pragma unroll
-        for (int j = 0; j < 15; ++j) {
-          const TM arj = S.D[r * 15 + j];
-          m += arj * S.Q[j * 15 + c];
-          n += arj * S.Phi[j * 15 + c];
-        }
+      for (int j = 0; j < 15; ++j) {
+        const TM arj = S.D[r * 15 + j];
+        m += arj * S.Q[j * 15 + c];
+        n += arj * S.Phi[j * 15 + c];
       }
       S.td[a] = m;
       S.PC[a] = n;
