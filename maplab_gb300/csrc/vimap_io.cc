@@ -439,6 +439,11 @@ class YParser {
     return true;
   }
   bool block(size_t* i, int indent, YNode* n) {
+    if (++depth_ > 64) return fail();  // the sensor files nest a handful of levels
+    struct Leave {
+      int& d;
+      ~Leave() { --d; }
+    } leave{depth_};
     const YLine& first = lines_[*i];
     const bool is_seq = first.text == "-" || first.text.compare(0, 2, "- ") == 0;
     n->kind = is_seq ? YNode::kSeq : YNode::kMap;
@@ -487,6 +492,7 @@ class YParser {
   }
   std::vector<YLine> lines_;
   bool ok_ = true;
+  int depth_ = 0;
 };
 
 // YAML matrix: {rows, cols, data} with data flat or a list of rows (values
@@ -1425,6 +1431,12 @@ mba_status load(const char* folder, mba_vimap* M) {
           f.lm[b.keypoint] = L.id;
         }
   }
+  for (const Vertex& v : M->vertices) {  // Vertex::incoming / outgoing name existing edges
+    for (const Id& id : v.outgoing)
+      if (!M->edge_of.count(id)) return MBA_ERR_OUT_OF_RANGE_INDEX;
+    for (const Id& id : v.incoming)
+      if (!M->edge_of.count(id)) return MBA_ERR_OUT_OF_RANGE_INDEX;
+  }
   for (const Edge& e : M->edges) {
     if (!M->vertex_of.count(e.from) || !M->vertex_of.count(e.to)) return MBA_ERR_OUT_OF_RANGE_INDEX;
     if (e.kind == kViwls)
@@ -2114,11 +2126,15 @@ extern "C" {
 mba_status mba_vimap_load(const char* map_folder, mba_vimap** out) {
   if (!map_folder || !out) return MBA_ERR_INVALID_ARG;
   *out = nullptr;
-  std::unique_ptr<mba_vimap> M(new mba_vimap());
-  const mba_status s = load(map_folder, M.get());
-  if (s != MBA_OK) return s;
-  *out = M.release();
-  return MBA_OK;
+  try {
+    std::unique_ptr<mba_vimap> M(new mba_vimap());
+    const mba_status s = load(map_folder, M.get());
+    if (s != MBA_OK) return s;
+    *out = M.release();
+    return MBA_OK;
+  } catch (...) {  // allocation failure or a lookup the validation missed: a status, never an abort
+    return MBA_ERR_INVALID_ARG;
+  }
 }
 
 void mba_vimap_destroy(mba_vimap* m) { delete m; }
@@ -2168,7 +2184,12 @@ void mba_vimap_default_export_options(mba_vimap_export_options* o) {
 
 mba_status mba_vimap_export(mba_vimap* m, const mba_vimap_export_options* o, mba_problem_desc* desc) {
   if (!m || !o || !desc) return MBA_ERR_INVALID_ARG;
-  const mba_status s = do_export(m, *o, desc);
+  mba_status s;
+  try {
+    s = do_export(m, *o, desc);
+  } catch (...) {
+    s = MBA_ERR_INVALID_ARG;
+  }
   if (s != MBA_OK) m->ex = mba_vimap::Export();
   return s;
 }
@@ -2237,10 +2258,14 @@ mba_status mba_vimap_save(const mba_vimap* m, const char* map_folder) {
   if (mkdir(dir.c_str(), 0755) != 0) return MBA_ERR_INVALID_ARG;
   if (!write_file(join(dir, "vi_map_metadata"), m->metadata_text)) return MBA_ERR_INVALID_ARG;
   if (!write_file(join(dir, "sensors.yaml"), m->sensors_text)) return MBA_ERR_INVALID_ARG;
-  for (size_t f = 0; f < m->files.size(); ++f) {
-    std::string data;
-    if (!rewrite_file(m, (int)f, &data)) return MBA_ERR_INVALID_ARG;
-    if (!write_file(join(dir, m->file_names[f]), data)) return MBA_ERR_INVALID_ARG;
+  try {
+    for (size_t f = 0; f < m->files.size(); ++f) {
+      std::string data;
+      if (!rewrite_file(m, (int)f, &data)) return MBA_ERR_INVALID_ARG;
+      if (!write_file(join(dir, m->file_names[f]), data)) return MBA_ERR_INVALID_ARG;
+    }
+  } catch (...) {
+    return MBA_ERR_INVALID_ARG;
   }
   return MBA_OK;
 }

@@ -376,6 +376,33 @@ def test_malformed_maps_are_refused(tmp_path):
         i = b.index(t0 + t1)
         p.write_bytes(b[:i] + t1 + t0 + b[i + len(t0) + len(t1):])
 
+    def deep_yaml(d):
+        (d / "sensors.yaml").write_text("".join(" " * i + "a:\n" for i in range(200)) + " " * 200 + "b: 1\n")
+
+    def dangling_outgoing(d):
+        from vimap_writer import f_bytes, f_id, make_id
+        # vertices0's first vertex names an edge that does not exist
+        p = d / "vertices0"
+        b = p.read_bytes()
+        vid = f_id(1, make_id("vertex", 0))
+        assert b.startswith(vid)
+        # the vertex message follows the id: prepend an outgoing edge id to its body
+        rest = b[len(vid):]
+        assert rest[0] == 0x12  # field 2, length-delimited
+        from vimap_writer import _varint
+        i, n, shift = 1, 0, 0
+        while True:
+            byte = rest[i]
+            n |= (byte & 0x7F) << shift
+            i += 1
+            shift += 7
+            if not byte & 0x80:
+                break
+        body = f_id(2, make_id("edge", 99999)) + rest[i:i + n]
+        p.write_bytes(vid + f_bytes(2, body) + rest[i + n:])
+
+    assert variant("deep", deep_yaml) == N.MBA_ERR_INVALID_ARG
+    assert variant("outgoing", dangling_outgoing) == N.MBA_ERR_OUT_OF_RANGE_INDEX
     assert variant("trunc", truncate) == N.MBA_ERR_INVALID_ARG
     assert variant("meta", bad_meta) == N.MBA_ERR_INVALID_ARG
     assert variant("escape", escape_meta) == N.MBA_ERR_INVALID_ARG
