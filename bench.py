@@ -45,6 +45,57 @@ def _dist():
     return ws, rank, local
 
 
+class Replicas:
+    """The processes of a torchrun launch: one per GPU, each solving its own
+    copy of the workload (the path has no exchange step, so no collective
+    touches the data).  Provides the barrier around the timed region, the
+    maximum of a per-rank time, and which rank reports.  backend "nccl" on
+    GPUs; "gloo" runs the same logic on CPU processes."""
+
+    def __init__(self, backend="nccl"):
+        self.ws, self.rank, self.local = _dist()
+        self.backend = backend
+        self.dist = None
+        if self.ws > 1:
+            import torch
+            import torch.distributed as dist
+            if backend == "nccl":
+                dist.init_process_group("nccl", device_id=torch.device("cuda", self.local))
+            else:
+                dist.init_process_group(backend)
+            self.dist = dist
+
+    def barrier(self):
+        if self.dist is not None:
+            self.dist.barrier()
+        if self.backend == "nccl":
+            import torch
+            torch.cuda.synchronize()
+
+    def max(self, x):
+        """The largest of the ranks' values of x (the job time is the slowest rank's)."""
+        if self.dist is None:
+            return x
+        import torch
+        t = torch.tensor([x], dtype=torch.float64, device="cuda" if self.backend == "nccl" else "cpu")
+        self.dist.all_reduce(t, op=self.dist.ReduceOp.MAX)
+        return float(t.item())
+
+    @property
+    def reports(self):
+        return self.rank == 0
+
+    def close(self):
+        if self.dist is not None:
+            self.dist.destroy_process_group()
+            self.dist = None
+
+
+def job_throughput(ws, units_per_rank, seconds_max):
+    """Whole-job throughput of ws replicas: all ranks' units over the slowest rank's time."""
+    return ws * units_per_rank / seconds_max
+
+
 class ClockSampler:
     """nvidia-smi clocks / throttle reasons sampled during the timed region."""
 
@@ -260,24 +311,9 @@ def run_ours(args):
     from maplab_gb300 import ba
 
     ws, rank, local = _dist()
-    if ws > 1:
-        import torch.distributed as dist
-        dist.init_process_group("nccl", device_id=torch.device("cuda", local))
     torch.cuda.set_device(local)
-
-    def barrier():
-        if ws > 1:
-            import torch.distributed as dist
-            dist.barrier()
-        torch.cuda.synchronize()
-
-    def max_over_ranks(x):
-        if ws == 1:
-            return x
-        import torch.distributed as dist
-        t = torch.tensor([x], dtype=torch.float64, device="cuda")
-        dist.all_reduce(t, op=dist.ReduceOp.MAX)
-        return float(t.item())
+    rep = Replicas("nccl")
+    barrier, max_over_ranks = rep.barrier, rep.max
 
     m = _make_map(args)
     d = m.desc
@@ -296,7 +332,7 @@ def run_ours(args):
         wall = time.perf_counter() - t0
     ms32 = max_over_ranks(ms32)
     ms64 = max_over_ranks(g.time_visual_kernel(mode=0, iters=max(3, args.steps // 2)))
-    value = ws * n / (ms32 * 1e-3)
+    value = job_throughput(ws, n, ms32 * 1e-3)
 
     # ---- e2e through the C ABI with pinned host buffers
     st = g.read_state()
@@ -362,10 +398,10 @@ def run_ours(args):
             "config": {"workload": WORKLOAD, "observations": n, "landmarks": nl, "keyframes": nk,
                        "precision": "mixed: FP32 Jacobians/residuals, FP64 inputs and cost",
                        "l2": "256 MiB write before every timed launch (L2 flushed)",
-                       "fp64_kernel_ms": ms64, "fp64_evals_per_s": ws * n / (ms64 * 1e-3),
+                       "fp64_kernel_ms": ms64, "fp64_evals_per_s": job_throughput(ws, n, ms64 * 1e-3),
                        "timed_wall_s": wall, "parallelism": f"replicas x{ws}",
                        "tuning": tuning},
-            "e2e": {"value": ws * n / e2e_sec, "unit": "evals/s", "h2d_bytes_per_step": h2d, "d2h_bytes_per_step": d2h},
+            "e2e": {"value": job_throughput(ws, n, e2e_sec), "unit": "evals/s", "h2d_bytes_per_step": h2d, "d2h_bytes_per_step": d2h},
             "roofline": roof,
             "cpu_baseline": cpu,
             "clocks": clk.summary(),
@@ -375,9 +411,7 @@ def run_ours(args):
         }
         print(json.dumps(line), flush=True)
     g.close()
-    if ws > 1:
-        import torch.distributed as dist
-        dist.destroy_process_group()
+    rep.close()
 
 
 def main():
