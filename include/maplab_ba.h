@@ -506,6 +506,14 @@ mba_status mba_visual_cost_noalloc(const mba_visual_batch_device* batch, int32_t
 mba_status mba_gnn_gemm(int32_t device, int64_t n, int32_t k, const uint16_t* A, const uint16_t* W,
                         const uint16_t* A2, const uint16_t* W2, const float* bias, float* Z, uint16_t* H);
 
+/* Failure detection without a fault: launches the tensor-core node update
+ * with its operand copies left out, so that the kernel's bounded wait on the
+ * load barrier runs out (a barrier nothing signals).  Returns MBA_ERR_TIMEOUT
+ * when the kernel reported the timeout and the device stayed usable (a
+ * following synchronize succeeds); MBA_OK would mean the timeout went
+ * unreported. */
+mba_status mba_gnn_gemm_wait_check(int32_t device);
+
 #ifdef __cplusplus
 }
 #endif

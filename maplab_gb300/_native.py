@@ -413,6 +413,7 @@ def load_ba():
     u16p = ctypes.POINTER(ctypes.c_uint16)
     _declare(lib, "mba_gnn_gemm", ctypes.c_int, [ctypes.c_int32, ctypes.c_int64, ctypes.c_int32, u16p, u16p, u16p, u16p,
                                                  ctypes.POINTER(ctypes.c_float), ctypes.POINTER(ctypes.c_float), u16p])
+    _declare(lib, "mba_gnn_gemm_wait_check", ctypes.c_int, [ctypes.c_int32])
     u64p = ctypes.POINTER(ctypes.c_uint64)
     _declare(lib, "mba_vimap_load", ctypes.c_int, [ctypes.c_char_p, ctypes.POINTER(vp)])
     _declare(lib, "mba_vimap_destroy", None, [vp])

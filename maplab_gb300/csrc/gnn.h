@@ -90,6 +90,11 @@ struct GnnGraph {
 // H = bf16(relu(Z)); K = 32 or 64, 64 outputs.  `fatal` is raised if a
 // bounded wait of the tensor-core pipeline runs out.
 cudaError_t gnn_gemm_tc_prepare();
+// The same kernel with its operand copies left out and a short wait limit:
+// the load barrier is never signalled, the wait runs out, `fatal` is raised
+// and the kernel returns with its tensor memory freed (K = 64, A / W valid).
+cudaError_t gnn_gemm_tc_wait_check(int64_t n, const __nv_bfloat16* A, const __nv_bfloat16* W, float* Z, int* fatal,
+                                   cudaStream_t st);
 cudaError_t gnn_gemm_tc(int64_t n, int K, const __nv_bfloat16* A, const __nv_bfloat16* W, const __nv_bfloat16* A2,
                         const __nv_bfloat16* W2, const float* bias, float* Z, __nv_bfloat16* H, int* fatal,
                         cudaStream_t st);

@@ -33,14 +33,14 @@ using bf16 = __nv_bfloat16;
 constexpr int kTileM = 128;
 constexpr int kTileN = kGnnHidden;  // 64
 constexpr int kTmemCols = 64;       // power of two >= 32
-constexpr long kWaitLimit = 1L << 22;
+constexpr long kWaitLimit = 1L << 22;  // try_wait polls before a wait counts as run out
 
 __device__ __forceinline__ uint32_t smem_u32(const void* p) {
   return (uint32_t)__cvta_generic_to_shared(p);
 }
 
-__device__ __forceinline__ bool mbar_wait(uint32_t bar, uint32_t parity) {
-  for (long i = 0; i < kWaitLimit; ++i) {
+__device__ __forceinline__ bool mbar_wait(uint32_t bar, uint32_t parity, long limit) {
+  for (long i = 0; i < limit; ++i) {
     uint32_t done;
     asm volatile(
         "{\n .reg .pred p;\n mbarrier.try_wait.parity.shared::cta.b64 p, [%1], %2;\n selp.u32 %0, 1, 0, p;\n}\n"
@@ -85,7 +85,8 @@ __global__ void __launch_bounds__(128) k_gnn_gemm_tc(int64_t n, const __grid_con
                                                      const __grid_constant__ CUtensorMap tA2,
                                                      const __grid_constant__ CUtensorMap tW2, int has2,
                                                      const float* __restrict__ bias, float* __restrict__ Z,
-                                                     bf16* __restrict__ H, int* fatal) {
+                                                     bf16* __restrict__ H, int* fatal, long wait_limit,
+                                                     int skip_loads) {
   using L = TcSmem<K>;
   extern __shared__ uint8_t smem_raw[];
   __shared__ __align__(8) uint64_t bars[2];
@@ -118,7 +119,9 @@ __global__ void __launch_bounds__(128) k_gnn_gemm_tc(int64_t n, const __grid_con
     const int pairs = has2 ? 2 : 1;
     const uint32_t bytes = (uint32_t)(pairs * (L::kA + L::kW));
     asm volatile("mbarrier.arrive.expect_tx.shared::cta.b64 _, [%0], %1;" ::"r"(bar_load), "r"(bytes) : "memory");
-    for (int p = 0; p < pairs; ++p) {
+    // skip_loads (the wait-timeout check only): no copy is issued, so the
+    // load barrier never completes and the bounded wait below runs out.
+    for (int p = 0; p < (skip_loads ? 0 : pairs); ++p) {
       const CUtensorMap* ta = p ? &tA2 : &tA;
       const CUtensorMap* tw = p ? &tW2 : &tW;
       asm volatile(
@@ -132,9 +135,9 @@ __global__ void __launch_bounds__(128) k_gnn_gemm_tc(int64_t n, const __grid_con
           "l"((uint64_t)tw), "r"(0), "r"(0), "r"(bar_load)
           : "memory");
     }
-    if (!mbar_wait(bar_load, 0)) {
+    if (!mbar_wait(bar_load, 0, wait_limit)) {
       state = 1;
-      mbar_wait(bar_load, 0);  // the copies may still land: wait once more before the tile is given up
+      mbar_wait(bar_load, 0, wait_limit);  // the copies may still land: wait once more before the tile is given up
     } else {
       asm volatile("tcgen05.fence::after_thread_sync;" ::: "memory");
       int first = 1;
@@ -157,9 +160,9 @@ __global__ void __launch_bounds__(128) k_gnn_gemm_tc(int64_t n, const __grid_con
   }
   __syncthreads();
   if (state == 0) {
-    if (!mbar_wait(bar_mma, 0)) {
+    if (!mbar_wait(bar_mma, 0, wait_limit)) {
       state = 2;  // every thread that sees the timeout records it (same value)
-      mbar_wait(bar_mma, 0);
+      mbar_wait(bar_mma, 0, wait_limit);
     }
   }
   __syncthreads();
@@ -238,7 +241,8 @@ bool tensor_map(CUtensorMap* m, const bf16* ptr, int64_t rows, int K, int box_ro
 
 template <int K>
 cudaError_t launch_tc(int64_t n, const bf16* A, const bf16* W, const bf16* A2, const bf16* W2, const float* bias,
-                      float* Z, bf16* H, int* fatal, cudaStream_t st) {
+                      float* Z, bf16* H, int* fatal, cudaStream_t st, long wait_limit = kWaitLimit,
+                      int skip_loads = 0) {
   CUtensorMap tA, tW, tA2, tW2;
   const bool two = A2 && W2;
   if (!tensor_map(&tA, A, n, K, kTileM) || !tensor_map(&tW, W, kTileN, K, kTileN)) return cudaErrorInvalidValue;
@@ -250,7 +254,8 @@ cudaError_t launch_tc(int64_t n, const bf16* A, const bf16* W, const bf16* A2, c
   }
   if (((uintptr_t)Z & 15) || ((uintptr_t)H & 15) || ((uintptr_t)bias & 15)) return cudaErrorInvalidValue;
   const unsigned grid = (unsigned)((n + kTileM - 1) / kTileM);
-  k_gnn_gemm_tc<K><<<grid, 128, TcSmem<K>::kBytes, st>>>(n, tA, tW, tA2, tW2, two ? 1 : 0, bias, Z, H, fatal);
+  k_gnn_gemm_tc<K><<<grid, 128, TcSmem<K>::kBytes, st>>>(n, tA, tW, tA2, tW2, two ? 1 : 0, bias, Z, H, fatal,
+                                                          wait_limit, skip_loads);
   return cudaGetLastError();
 }
 
@@ -262,6 +267,11 @@ cudaError_t gnn_gemm_tc_prepare() {
   if (e == cudaSuccess)
     e = cudaFuncSetAttribute(k_gnn_gemm_tc<32>, cudaFuncAttributeMaxDynamicSharedMemorySize, TcSmem<32>::kBytes);
   return e;
+}
+
+cudaError_t gnn_gemm_tc_wait_check(int64_t n, const bf16* A, const bf16* W, float* Z, int* fatal, cudaStream_t st) {
+  if (n <= 0) return cudaErrorInvalidValue;
+  return launch_tc<64>(n, A, W, nullptr, nullptr, nullptr, Z, nullptr, fatal, st, 1L << 14, 1);
 }
 
 cudaError_t gnn_gemm_tc(int64_t n, int K, const bf16* A, const bf16* W, const bf16* A2, const bf16* W2,

@@ -2166,6 +2166,27 @@ mba_status mba_set_tuning(mba_handle* h, const mba_tuning* t) {
   return MBA_OK;
 }
 
+mba_status mba_gnn_gemm_wait_check(int32_t device) {
+  if (cudaSetDevice(device) != cudaSuccess) return MBA_ERR_NO_DEVICE;
+  if (gnn_gemm_tc_prepare() != cudaSuccess) return MBA_ERR_CUDA;
+  const int64_t n = 128;
+  void *dA = nullptr, *dW = nullptr, *dZ = nullptr, *df = nullptr;
+  cudaError_t e = cudaMalloc(&dA, sizeof(uint16_t) * n * 64);
+  if (e == cudaSuccess) e = cudaMalloc(&dW, sizeof(uint16_t) * 64 * 64);
+  if (e == cudaSuccess) e = cudaMalloc(&dZ, sizeof(float) * n * 64);
+  if (e == cudaSuccess) e = cudaMalloc(&df, sizeof(int));
+  if (e == cudaSuccess) e = cudaMemset(df, 0, sizeof(int));
+  if (e == cudaSuccess)
+    e = gnn_gemm_tc_wait_check(n, (const __nv_bfloat16*)dA, (const __nv_bfloat16*)dW, (float*)dZ, (int*)df, 0);
+  if (e == cudaSuccess) e = cudaDeviceSynchronize();
+  int fatal = 0;
+  if (e == cudaSuccess) e = cudaMemcpy(&fatal, df, sizeof(int), cudaMemcpyDeviceToHost);
+  for (void* p : {dA, dW, dZ, df})
+    if (p) cudaFree(p);
+  if (e != cudaSuccess) return MBA_ERR_CUDA;
+  return fatal ? MBA_ERR_TIMEOUT : MBA_OK;
+}
+
 mba_status mba_gnn_gemm(int32_t device, int64_t n, int32_t k, const uint16_t* A, const uint16_t* W,
                         const uint16_t* A2, const uint16_t* W2, const float* bias, float* Z, uint16_t* H) {
   if (n <= 0 || (k != 32 && k != 64) || !A || !W || !Z || (!A2) != (!W2)) return MBA_ERR_INVALID_ARG;

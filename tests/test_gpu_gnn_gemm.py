@@ -67,3 +67,12 @@ def test_invalid_arguments_are_refused():
     st = ba.lib().mba_gnn_gemm(0, 4, 48, _ptr16(A), _ptr16(A), None, None, None,
                                Z.ctypes.data_as(ctypes.POINTER(ctypes.c_float)), None)
     assert st == N.MBA_ERR_INVALID_ARG
+
+
+def test_bounded_wait_reports_a_timeout_and_the_device_stays_usable():
+    """Failure detection without a fault: a barrier nothing signals (the
+    operand copies left out) makes the kernel's bounded wait run out; the
+    kernel raises its error flag and returns, the host reads MBA_ERR_TIMEOUT,
+    and a normal launch right after gives correct results."""
+    assert ba.lib().mba_gnn_gemm_wait_check(0) == N.MBA_ERR_TIMEOUT
+    test_tensor_core_node_update_matches_fp32(64, 300, True, True)
