@@ -3,23 +3,30 @@
 
 One step = one robustified tangent-space linearization (residual + landmark,
 store-pose and observer-pose Jacobian blocks + Huber corrector + cost) of every
-visual observation of the workload, the evaluation half of one LM iteration.
+visual observation of the workload, the evaluation half of one LM iteration,
+in FP64 (the reference's arithmetic).
 
-  value  : device-resident throughput of the evaluation kernel (mixed path:
-           FP32 Jacobians), CUDA events on the launching stream, L2 flushed
-           (256 MiB write) before every timed launch.
+  value  : device-resident throughput of the FP64 evaluation kernel (launch
+           parameters autotuned on the map), CUDA events on the launching
+           stream, L2 flushed (256 MiB write) before every timed launch.
   e2e    : the same metric through the C ABI with pinned HOST buffers: state
-           upload (mba_write_state), linearization, and the residuals and
+           upload (mba_write_state), FP64 linearization, and the residuals and
            Jacobians read back in the caller's order (mba_linearize_visual).
+  mixed_f32 : the FP32 evaluation kernel of the mixed path (extra key).
   ba     : time-to-cost-tolerance on the 20,000-keyframe 10-mission map: plain
            FP64 device LM (20 iterations, block-Jacobi PCG <= 100 its, tol
-           1e-6) against mixed precision with the learned chain
-           preconditioner, stopped at the plain path's cost * (1 + 1e-6);
-           reprojection RMS of both final states.
+           1e-6) against the other forms ({FP64, mixed} x {block-Jacobi,
+           chain} and mixed + learned), each stopped at the plain path's cost
+           * (1 + 1e-6); every arm autotuned, times reported with and without
+           the tuning time; reprojection RMS of the final states.
+  ba_cpu : the CPU oracle's LM (all host cores) on the 100-keyframe map (10
+           iterations, dense Schur) and on the 2,000-keyframe map (2 of its 20
+           iterations timed, block-Jacobi PCG <= 100) beside the device solve.
 
 --impl reference times the CPU restatement of the reference's evaluation
-(oracle/, all host threads) on the same map.  Multi-GPU runs are independent
-replicas (the workload does not shard here): value is summed over ranks.
+(oracle/, all host threads) on every observation of the same map.  Multi-GPU
+runs are independent replicas (the workload does not shard here): value is
+summed over ranks.
 """
 import argparse
 import ctypes
@@ -35,7 +42,8 @@ ROOT = os.path.dirname(os.path.abspath(__file__))
 sys.path.insert(0, ROOT)
 
 METRIC = "BA time-to-cost-tol (s) and obs Jacobian evals/s: mixed+learned vs plain FP64 on GB300"
-WORKLOAD = "C2: plain method on GPU, 2,000 keyframes, 200k landmarks, ~1.6M observations, 2 cameras (radtan + equidistant)"
+WORKLOAD = ("C2: plain method on GPU, FP64, 2,000 keyframes, 200k landmarks, ~1.6M observations, "
+            "2 cameras (radtan + equidistant)")
 
 
 def _dist():
@@ -114,6 +122,7 @@ class ClockSampler:
                                          stdout=subprocess.PIPE, stderr=subprocess.DEVNULL, text=True)
             self.reader = threading.Thread(target=self._read, daemon=True)
             self.reader.start()
+            time.sleep(0.3)  # the first sample lands before the timed region starts
         except OSError:
             self.proc = None
         return self
@@ -151,9 +160,10 @@ def _peaks():
         return {"hbm_gbs": 6800.0, "bf16_tflops": 1900.0}, "fallback"
 
 
-def _traffic_summary():
+def _profile(name):
+    """Per-launch counters of a kernel from its committed ncu summary (JSON)."""
     try:
-        return json.load(open(os.path.join(ROOT, "profiles", "visual_linearize_c2_traffic.json")))
+        return json.load(open(os.path.join(ROOT, "profiles", name)))
     except OSError:
         return None
 
@@ -173,19 +183,18 @@ def run_reference(args):
     n = m.desc.num_observations
     threads = os.cpu_count() or 1
     o = oracle_lib.OracleProblem(m.desc, threads=threads)
-    sample = min(n, args.cpu_sample)
     for _ in range(args.warmup):
-        o.time_visual(threads, sample, 1)
-    t = [o.time_visual(threads, sample, 1) for _ in range(args.steps)]
+        o.time_visual(threads, n, 1)
+    t = [o.time_visual(threads, n, 1) for _ in range(args.steps)]
     sec = sum(t) / len(t)
-    v = sample / sec
+    v = n / sec
     line = {
         "impl": "reference", "metric": METRIC, "value": v, "unit": "evals/s", "n_gpus": ws, "steps": args.steps,
         "warmup": args.warmup, "ms_per_step": sec * 1e3, "higher_is_better": True, "scaling": "weak",
         "vs_baseline": None, "dtype": "f64", "data": "synthetic (seeded generator restating vi-map-generator-6dof)",
-        "config": {"workload": WORKLOAD, "observations": n, "sample_per_step": sample},
+        "config": {"workload": WORKLOAD, "observations": n, "sample_per_step": n},
         "cpu_baseline": {"value": v, "unit": "evals/s", "cores": threads, "kind": "port",
-                         "sample": f"{sample} observations per step of the {n}-observation workload"},
+                         "sample": f"all {n} observations of the workload per step"},
         "e2e": {"value": v, "unit": "evals/s", "h2d_bytes_per_step": 0, "d2h_bytes_per_step": 0},
     }
     print(json.dumps(line), flush=True)
@@ -203,105 +212,167 @@ def _reprojection_rms(g, m):
     return float(np.sqrt(e2.mean())), int(keep.sum())
 
 
+def _tuned_solve(d, device, precision, opts, model=None):
+    """A fresh handle, autotuned for `precision`, solved with `opts`.  Returns
+    (summary, autotune seconds, tuning, handle) with the handle still open."""
+    from maplab_gb300 import ba
+    g = ba.BundleAdjuster(d, device=device)
+    if model is not None:
+        g.set_preconditioner_model(model)
+    t0 = time.perf_counter()
+    tun = g.autotune(precision)
+    tune_s = time.perf_counter() - t0
+    s = g.solve(opts)
+    return s, tune_s, tun, g
+
+
 def ba_time_to_cost(args, device):
     """Plain FP64 path (block-Jacobi PCG <= 100 its, 20 LM iterations) against
-    the mixed-precision path with the learned chain preconditioner (PCG <= 25
-    its), stopped at the plain path's final cost * (1 + 1e-6).  Times are CUDA
-    events from the first device launch of the solve."""
+    the other forms, each stopped at the plain path's final cost * (1 + 1e-6).
+    Times are CUDA events from the first device launch of the solve; every arm
+    is autotuned first and its tuning time is reported beside it."""
     from maplab_gb300 import _native as N
     from maplab_gb300 import ba, synth
     from maplab_gb300 import train_preconditioner as TP
     m = synth.generate(args.ba_config)
     d = m.desc
     common = dict(check_tolerances=0, linear_tolerance=1e-6, outlier_use_reprojection_error=args.reproj_rejection)
-    g64 = ba.BundleAdjuster(d, device=device)
-    s64 = g64.solve(ba.default_options(max_num_iterations=20, max_linear_iterations=100, **common))
+    s64, tune64, tun64, g64 = _tuned_solve(d, device, N.MBA_PRECISION_FP64,
+                                           ba.default_options(max_num_iterations=20, max_linear_iterations=100,
+                                                              **common))
     rms64, n64 = _reprojection_rms(g64, m)
     g64.close()
     target = s64["final_cost"] * (1 + 1e-6)
-    model = TP.load_default_model(device)
-    pre = N.MBA_PRECOND_LEARNED if model is not None else N.MBA_PRECOND_CHAIN
-    g32 = ba.BundleAdjuster(d, device=device)
-    if model is not None:
-        g32.set_preconditioner_model(model)
-    tun32 = g32.autotune(N.MBA_PRECISION_MIXED)
-    s32 = g32.solve(ba.default_options(max_num_iterations=40, max_linear_iterations=args.fast_pcg, stop_cost=target,
-                                       precision=N.MBA_PRECISION_MIXED, preconditioner=pre, use_cuda_graph=2,
-                                       **common))
-    rms32, n32 = _reprojection_rms(g32, m)
-    cost32_fp64 = g32.cost()  # the mixed path's final state re-evaluated in full FP64
-    g32.close()
-    # the same mixed solve with the chain preconditioner's fixed coefficients
-    # (no network): the learned coefficients' gain at the same PCG cap
-    gch = ba.BundleAdjuster(d, device=device)
-    gch.autotune(N.MBA_PRECISION_MIXED)
-    sch = gch.solve(ba.default_options(max_num_iterations=40, max_linear_iterations=args.fast_pcg, stop_cost=target,
-                                       precision=N.MBA_PRECISION_MIXED, preconditioner=N.MBA_PRECOND_CHAIN,
-                                       use_cuda_graph=2, **common))
-    gch.close()
-    tch = sch["time_to_stop_cost_ms"] / 1e3 if sch["time_to_stop_cost_ms"] >= 0 else None
-    if model is not None:
-        model.close()
     t64 = s64["iterations"][-1]["time_ms"] / 1e3
-    t32 = s32["time_to_stop_cost_ms"] / 1e3 if s32["time_to_stop_cost_ms"] >= 0 else None
-    return {
+    out = {
         "workload": f"{args.ba_config}: {d.num_keyframes} keyframes, {d.num_landmarks} landmarks, "
                     f"{d.num_observations} observations, {d.num_missions} missions",
-        "plain_fp64_s": t64, "plain_fp64_final_cost": s64["final_cost"],
-        "plain_fp64_pcg_iterations": s64["linear_iterations"], "plain_fp64_rejected_landmarks": s64["rejected_landmarks"],
-        "plain_fp64_rms_px": rms64,
-        "mixed_learned_time_to_cost_s": t32, "mixed_learned_final_cost": s32["final_cost"],
-        "mixed_learned_final_cost_fp64_eval": cost32_fp64,
-        "mixed_reaches_target_in_fp64": bool(cost32_fp64 <= target),
-        "mixed_learned_iterations": s32["num_iterations"] - 1, "mixed_learned_pcg_iterations": s32["linear_iterations"],
-        "mixed_learned_rejected_landmarks": s32["rejected_landmarks"], "mixed_learned_rms_px": rms32,
-        "rms_difference_px": abs(rms32 - rms64),
-        "speedup": (t64 / t32) if t32 else None,
-        "pcg_cap": args.fast_pcg,
-        "mixed_chain_time_to_cost_s": tch, "mixed_chain_iterations": sch["num_iterations"] - 1,
-        "tuning": tun32,
-        "preconditioner": "learned" if pre == N.MBA_PRECOND_LEARNED else "chain",
+        "plain_fp64_s": t64, "plain_fp64_autotune_s": tune64, "plain_fp64_s_incl_autotune": t64 + tune64,
+        "plain_fp64_final_cost": s64["final_cost"], "plain_fp64_pcg_iterations": s64["linear_iterations"],
+        "plain_fp64_rejected_landmarks": s64["rejected_landmarks"], "plain_fp64_rms_px": rms64,
         "cost_tolerance": "1e-6 relative to the plain FP64 path's 20-iteration cost",
         "outlier_rejection": "every 3 iterations, depth <= 0" +
                              (" or reprojection error > 50 px" if args.reproj_rejection else ""),
+        "pcg_cap": {"block_jacobi": 100, "chain_and_learned": args.fast_pcg},
     }
+    model = TP.load_default_model(device)
+    arms = [("fp64_chain", N.MBA_PRECISION_FP64, N.MBA_PRECOND_CHAIN, args.fast_pcg, 2),
+            ("mixed_block_jacobi", N.MBA_PRECISION_MIXED, N.MBA_PRECOND_BLOCK_JACOBI, 100, 2),
+            ("mixed_chain", N.MBA_PRECISION_MIXED, N.MBA_PRECOND_CHAIN, args.fast_pcg, 2)]
+    if model is not None:
+        arms.append(("mixed_learned", N.MBA_PRECISION_MIXED, N.MBA_PRECOND_LEARNED, args.fast_pcg, 2))
+    split = {}
+    for name, prec, pre, cap, graph in arms:
+        o = ba.default_options(max_num_iterations=40, max_linear_iterations=cap, stop_cost=target, precision=prec,
+                               preconditioner=pre, use_cuda_graph=graph, **common)
+        s, tune_s, tun, g = _tuned_solve(d, device, prec, o, model if pre == N.MBA_PRECOND_LEARNED else None)
+        t = s["time_to_stop_cost_ms"] / 1e3 if s["time_to_stop_cost_ms"] >= 0 else None
+        rms, _ = _reprojection_rms(g, m)
+        cost_fp64 = g.cost()  # the final state re-evaluated in full FP64
+        g.close()
+        split[name] = {"time_to_cost_s": t, "autotune_s": tune_s,
+                       "time_to_cost_incl_autotune_s": (t + tune_s) if t is not None else None,
+                       "iterations": s["num_iterations"] - 1, "pcg_iterations": s["linear_iterations"],
+                       "final_cost": s["final_cost"], "final_cost_fp64_eval": cost_fp64,
+                       "reaches_target_in_fp64": bool(cost_fp64 <= target), "rms_px": rms,
+                       "rms_difference_px": abs(rms - rms64), "speedup_vs_plain_fp64": (t64 / t) if t else None,
+                       "speedup_vs_plain_fp64_incl_autotune": ((t64 + tune64) / (t + tune_s)) if t else None,
+                       "pcg_cap": cap, "tuning": tun}
+    if model is not None:
+        model.close()
+    out["split"] = split
+    head = split.get("mixed_learned") or split["mixed_chain"]
+    out["preconditioner"] = "learned" if "mixed_learned" in split else "chain"
+    out["mixed_learned_time_to_cost_s"] = head["time_to_cost_s"]
+    out["mixed_chain_time_to_cost_s"] = split["mixed_chain"]["time_to_cost_s"]
+    out["speedup"] = head["speedup_vs_plain_fp64"]
+    out["speedup_incl_autotune"] = head["speedup_vs_plain_fp64_incl_autotune"]
+    lt, ct = out["mixed_learned_time_to_cost_s"], out["mixed_chain_time_to_cost_s"]
+    out["learned_vs_chain"] = ("learned faster than the fixed chain" if lt and ct and lt < ct else
+                               "learned NOT faster than the fixed chain (no gain from the network on this map)")
+    return out
 
 
 def batched_missions(args, device):
     """64 independent missions of uneven size (50..1500 keyframes) in one
     problem: autotuned launch parameters, the whole LM loop as one device-
     driven graph (mixed precision, learned chain preconditioner), against the
-    plain FP64 path's 20-iteration cost."""
+    plain FP64 path's 20-iteration cost (plain path autotuned too)."""
     from maplab_gb300 import _native as N
     from maplab_gb300 import ba, synth
     from maplab_gb300 import train_preconditioner as TP
     m = synth.generate("c3")
     d = m.desc
     common = dict(check_tolerances=0, linear_tolerance=1e-6, outlier_use_reprojection_error=args.reproj_rejection)
-    with ba.BundleAdjuster(d, device=device) as g:
-        s64 = g.solve(ba.default_options(max_num_iterations=20, max_linear_iterations=100, **common))
+    s64, tune64, _, g = _tuned_solve(d, device, N.MBA_PRECISION_FP64,
+                                     ba.default_options(max_num_iterations=20, max_linear_iterations=100, **common))
+    g.close()
     target = s64["final_cost"] * (1 + 1e-6)
     model = TP.load_default_model(device)
-    with ba.BundleAdjuster(d, device=device) as g:
-        t0 = time.perf_counter()
-        tun = g.autotune(N.MBA_PRECISION_MIXED)
-        tune_s = time.perf_counter() - t0
-        pre = N.MBA_PRECOND_CHAIN
-        if model is not None:
-            g.set_preconditioner_model(model)
-            pre = N.MBA_PRECOND_LEARNED
-        s32 = g.solve(ba.default_options(max_num_iterations=40, max_linear_iterations=args.c3_pcg, stop_cost=target,
-                                         precision=N.MBA_PRECISION_MIXED, preconditioner=pre, use_cuda_graph=2,
-                                         **common))
+    pre = N.MBA_PRECOND_LEARNED if model is not None else N.MBA_PRECOND_CHAIN
+    s32, tune_s, tun, g = _tuned_solve(d, device, N.MBA_PRECISION_MIXED,
+                                       ba.default_options(max_num_iterations=40, max_linear_iterations=args.c3_pcg,
+                                                          stop_cost=target, precision=N.MBA_PRECISION_MIXED,
+                                                          preconditioner=pre, use_cuda_graph=2, **common), model)
+    g.close()
     if model is not None:
         model.close()
     t64 = s64["iterations"][-1]["time_ms"] / 1e3
     t32 = s32["time_to_stop_cost_ms"] / 1e3 if s32["time_to_stop_cost_ms"] >= 0 else None
     return {"workload": f"c3: {d.num_missions} independent missions, {d.num_keyframes} keyframes, "
                         f"{d.num_observations} observations",
-            "tuning": tun, "autotune_s": tune_s, "plain_fp64_s": t64, "plain_fp64_final_cost": s64["final_cost"],
+            "tuning": tun, "autotune_s": tune_s, "plain_fp64_s": t64, "plain_fp64_autotune_s": tune64,
+            "plain_fp64_final_cost": s64["final_cost"],
             "mixed_learned_device_loop_time_to_cost_s": t32, "mixed_learned_iterations": s32["num_iterations"] - 1,
-            "speedup": (t64 / t32) if t32 else None, "launches_per_solve": 1}
+            "speedup": (t64 / t32) if t32 else None,
+            "speedup_incl_autotune": ((t64 + tune64) / (t32 + tune_s)) if t32 else None,
+            "launches_per_solve": 1}
+
+
+def ba_cpu_baseline(device):
+    """The oracle's LM on the host cores beside the device FP64 solve of the
+    same problem: the 100-keyframe map in full (10 iterations, dense Schur +
+    Cholesky on the CPU, block-Jacobi PCG to 1e-10 on the device) and 2 of the
+    20 iterations of the 2,000-keyframe map (block-Jacobi PCG <= 100, 1e-6 on
+    both sides; per-iteration seconds)."""
+    from maplab_gb300 import _native as N
+    from maplab_gb300 import ba, synth
+    sys.path.insert(0, os.path.join(ROOT, "tests"))
+    import oracle_lib
+    threads = os.cpu_count() or 1
+    out = {"cores": threads, "kind": "port"}
+    for cfg, iters, dense in (("c1", 10, True), ("c2", 2, False)):
+        m = synth.generate(cfg)
+        o = oracle_lib.OracleProblem(m.desc, threads=threads)
+        oo = N.default_solver_options()
+        oo.max_num_iterations = iters
+        oo.check_tolerances = 0
+        oo.reject_outliers_every_n_iters = 0
+        oo.linear_solver = N.MBA_LINEAR_SOLVER_DENSE_SCHUR if dense else N.MBA_LINEAR_SOLVER_PCG
+        oo.max_linear_iterations = 100
+        oo.linear_tolerance = 1e-6
+        t0 = time.perf_counter()
+        so = o.solve(oo)
+        cpu_s = time.perf_counter() - t0
+        del o
+        gopts = ba.default_options(max_num_iterations=iters if dense else 20, check_tolerances=0,
+                                   reject_outliers_every_n_iters=0,
+                                   max_linear_iterations=6000 if dense else 100,
+                                   linear_tolerance=1e-10 if dense else 1e-6)
+        with ba.BundleAdjuster(m.desc, device=device) as g:
+            sg = g.solve(gopts)
+        its = sg["iterations"]
+        gpu_s = its[-1]["time_ms"] / 1e3
+        gpu_iter_s = gpu_s / max(1, len(its) - 1)
+        row = {"cpu_s": cpu_s, "cpu_iterations": iters, "cpu_s_per_iteration": cpu_s / iters,
+               "cpu_final_cost": so["final_cost"], "gpu_fp64_s": gpu_s, "gpu_fp64_iterations": len(its) - 1,
+               "gpu_fp64_s_per_iteration": gpu_iter_s, "cpu_over_gpu_per_iteration": (cpu_s / iters) / gpu_iter_s,
+               "linear_solver_cpu": "dense Schur + Cholesky" if dense else "block-Jacobi PCG <= 100, 1e-6",
+               "linear_solver_gpu": "block-Jacobi PCG, 1e-10" if dense else "block-Jacobi PCG <= 100, 1e-6"}
+        if dense:
+            row["gpu_fp64_final_cost"] = sg["final_cost"]
+        out[cfg] = row
+    return out
 
 
 def run_ours(args):
@@ -320,21 +391,25 @@ def run_ours(args):
     n, nl, nk = d.num_observations, d.num_landmarks, d.num_keyframes
     g = ba.BundleAdjuster(d, device=local)
 
-    # ---- value: device-resident kernel throughput (mixed FP32 Jacobians),
-    # launch configuration chosen by the autotuner on this problem
-    tuning = g.autotune(N.MBA_PRECISION_MIXED)
-    g.time_visual_kernel(mode=1, iters=max(args.warmup, 3))
+    # ---- extra: the mixed path's FP32 evaluation kernel, tuned for it
+    tuning32 = g.autotune(N.MBA_PRECISION_MIXED)
+    g.time_visual_kernel(mode=1, iters=3)
+    ms32 = max_over_ranks(g.time_visual_kernel(mode=1, iters=max(3, args.steps)))
+
+    # ---- value: device-resident FP64 evaluation kernel, launch configuration
+    # chosen by the autotuner on this problem
+    tuning = g.autotune(N.MBA_PRECISION_FP64)
+    g.time_visual_kernel(mode=0, iters=max(args.warmup, 3))
     with ClockSampler(local) as clk:
         barrier()
         t0 = time.perf_counter()
-        ms32 = g.time_visual_kernel(mode=1, iters=args.steps)
+        ms64 = g.time_visual_kernel(mode=0, iters=args.steps)
         barrier()
         wall = time.perf_counter() - t0
-    ms32 = max_over_ranks(ms32)
-    ms64 = max_over_ranks(g.time_visual_kernel(mode=0, iters=max(3, args.steps // 2)))
-    value = job_throughput(ws, n, ms32 * 1e-3)
+    ms64 = max_over_ranks(ms64)
+    value = job_throughput(ws, n, ms64 * 1e-3)
 
-    # ---- e2e through the C ABI with pinned host buffers
+    # ---- e2e through the C ABI with pinned host buffers (FP64 linearization)
     st = g.read_state()
     pin = lambda a: torch.from_numpy(np.ascontiguousarray(a)).pin_memory()
     h_kx, h_kv, h_kbg, h_kba, h_lp = (pin(st[k]) for k in ("kf_q_IM_p_MI", "kf_v_M", "kf_b_g", "kf_b_a", "lm_p_B"))
@@ -344,7 +419,7 @@ def run_ours(args):
 
     def e2e_step():
         assert lib.mba_write_state(g.handle, P(h_kx), P(h_kv), P(h_kbg), P(h_kba), P(h_lp)) == 0
-        assert lib.mba_linearize_visual(g.handle, N.MBA_PRECISION_MIXED, *[P(o) for o in out]) == 0
+        assert lib.mba_linearize_visual(g.handle, N.MBA_PRECISION_FP64, *[P(o) for o in out]) == 0
 
     for _ in range(args.warmup):
         e2e_step()
@@ -357,57 +432,75 @@ def run_ours(args):
     h2d = 8 * (16 * nk + 3 * nl)
     d2h = 8 * 32 * n
 
-    # ---- roofline of the evaluation kernel
+    # ---- roofline of the FP64 evaluation kernel: FP64-pipe bound on GB300
+    # (FP64 FLOPs per launch from the kernel's ncu instruction counters,
+    # against the FP64 rate measured live), HBM fraction beside it
     peaks, peak_kind = _peaks()
-    alg_bytes = 40 * n + 24 * nl + 56 * nk + 128 * n
-    achieved = alg_bytes / (ms32 * 1e-3) / 1e9
-    tr = _traffic_summary()
-    roof = {"bound": "hbm", "achieved": achieved, "peak": peaks["hbm_gbs"], "unit": "GB/s",
-            "frac": achieved / peaks["hbm_gbs"], "peak_kind": peak_kind,
-            "traffic": (tr["dram_bytes_per_launch"] if tr else None),
-            "algorithmic_bytes_per_launch": alg_bytes}
+    fp64_peak = ba.measure_fp64_peak(local)
+    prof64 = _profile("visual_linearize_f64_c2_counts.json")
+    alg_bytes64 = 40 * n + 24 * nl + 56 * nk + 256 * n
+    hbm64 = alg_bytes64 / (ms64 * 1e-3) / 1e9
+    flops = prof64["fp64_flops_per_launch"] if prof64 else None
+    achieved = flops / (ms64 * 1e-3) / 1e12 if flops else None
+    roof = {"bound": "fp64", "achieved": achieved, "peak": fp64_peak, "unit": "TFLOP/s",
+            "frac": (achieved / fp64_peak) if achieved else None,
+            "peak_kind": "measured live in this run (mba_measure_fp64_peak: FP64 FMA chains on every SM)",
+            "traffic": (prof64["dram_bytes_per_launch"] if prof64 else None),
+            "fp64_flops_per_launch": flops, "fp64_flops_per_observation": (flops / n) if flops else None,
+            "algorithmic_bytes_per_launch": alg_bytes64,
+            "hbm": {"achieved": hbm64, "peak": peaks["hbm_gbs"], "unit": "GB/s", "frac": hbm64 / peaks["hbm_gbs"],
+                    "peak_kind": peak_kind}}
+    prof32 = _profile("visual_linearize_c2_traffic.json")
+    alg_bytes32 = 40 * n + 24 * nl + 56 * nk + 128 * n
+    hbm32 = alg_bytes32 / (ms32 * 1e-3) / 1e9
+    mixed32 = {"value": job_throughput(ws, n, ms32 * 1e-3), "unit": "evals/s", "ms_per_step": ms32, "dtype": "f32",
+               "tuning": tuning32,
+               "roofline": {"bound": "hbm", "achieved": hbm32, "peak": peaks["hbm_gbs"], "unit": "GB/s",
+                            "frac": hbm32 / peaks["hbm_gbs"], "peak_kind": peak_kind,
+                            "traffic": (prof32["dram_bytes_per_launch"] if prof32 else None),
+                            "algorithmic_bytes_per_launch": alg_bytes32}}
 
-    # ---- BA time-to-cost-tolerance: plain FP64 vs mixed + learned (rank-local)
-    ba_info = None
-    c3_info = None
-    if args.solve:
-        ba_info = ba_time_to_cost(args, local)
-    if args.c3:
-        c3_info = batched_missions(args, local)
+    # ---- BA time-to-cost-tolerance (rank-local)
+    ba_info = ba_time_to_cost(args, local) if args.solve else None
+    c3_info = batched_missions(args, local) if args.c3 else None
 
-    # ---- CPU baseline (rank 0, N=1 only): the oracle on the host cores
+    # ---- CPU baselines (rank 0, N=1 only): the oracle on the host cores
     cpu = None
+    ba_cpu = None
     if rank == 0 and ws == 1 and not args.skip_cpu:
         sys.path.insert(0, os.path.join(ROOT, "tests"))
         import oracle_lib
         threads = os.cpu_count() or 1
         o = oracle_lib.OracleProblem(d, threads=threads)
-        sample = min(n, args.cpu_sample)
-        o.time_visual(threads, sample, 1)
-        reps = max(1, int(10.0 / max(1e-3, o.time_visual(threads, sample, 1))))
-        sec = o.time_visual(threads, sample, min(reps, 200))
-        cpu = {"value": sample / sec, "unit": "evals/s", "cores": threads, "kind": "port",
-               "sample": f"{sample} of {n} observations per pass, {min(reps, 200)} passes (about 10 s)"}
+        one = o.time_visual(threads, n, 1)
+        reps = max(1, min(200, int(10.0 / max(1e-3, one))))
+        sec = o.time_visual(threads, n, reps)
+        del o
+        cpu = {"value": n / sec, "unit": "evals/s", "cores": threads, "kind": "port",
+               "sample": f"all {n} observations per pass, {reps} passes (about 10 s)"}
+        if args.ba_cpu:
+            ba_cpu = ba_cpu_baseline(local)
 
     if rank == 0:
         line = {
             "metric": METRIC, "value": value, "unit": "evals/s", "n_gpus": ws, "steps": args.steps,
-            "warmup": args.warmup, "ms_per_step": ms32, "higher_is_better": True, "scaling": "weak",
-            "vs_baseline": None, "dtype": "f32",
+            "warmup": args.warmup, "ms_per_step": ms64, "higher_is_better": True, "scaling": "weak",
+            "vs_baseline": None, "dtype": "f64",
             "data": "synthetic (seeded generator restating test/vi-map-generator-6dof; no public dataset)",
             "config": {"workload": WORKLOAD, "observations": n, "landmarks": nl, "keyframes": nk,
-                       "precision": "mixed: FP32 Jacobians/residuals, FP64 inputs and cost",
+                       "precision": "FP64 residuals and Jacobians (the reference's arithmetic)",
                        "l2": "256 MiB write before every timed launch (L2 flushed)",
-                       "fp64_kernel_ms": ms64, "fp64_evals_per_s": job_throughput(ws, n, ms64 * 1e-3),
-                       "timed_wall_s": wall, "parallelism": f"replicas x{ws}",
-                       "tuning": tuning},
-            "e2e": {"value": job_throughput(ws, n, e2e_sec), "unit": "evals/s", "h2d_bytes_per_step": h2d, "d2h_bytes_per_step": d2h},
+                       "timed_wall_s": wall, "parallelism": f"replicas x{ws}", "tuning": tuning},
+            "e2e": {"value": job_throughput(ws, n, e2e_sec), "unit": "evals/s", "h2d_bytes_per_step": h2d,
+                    "d2h_bytes_per_step": d2h, "precision": "FP64"},
             "roofline": roof,
             "cpu_baseline": cpu,
             "clocks": clk.summary(),
             "gpu_launches": args.steps,
+            "mixed_f32": mixed32,
             "ba_time_to_cost_tol": ba_info,
             "batched_missions": c3_info,
+            "ba_cpu_baseline": ba_cpu,
         }
         print(json.dumps(line), flush=True)
     g.close()
@@ -421,9 +514,9 @@ def main():
     ap.add_argument("--warmup", type=int, default=5)
     ap.add_argument("--impl", default="ours", choices=["ours", "reference"])
     ap.add_argument("--config", default="c2")
-    ap.add_argument("--cpu-sample", type=int, default=400_000)
     ap.add_argument("--solve", type=int, default=1)
     ap.add_argument("--skip-cpu", action="store_true")
+    ap.add_argument("--ba-cpu", type=int, default=1)
     ap.add_argument("--ba-config", default="c4")
     ap.add_argument("--c3", type=int, default=1)
     ap.add_argument("--fast-pcg", type=int, default=25)
@@ -434,11 +527,10 @@ def main():
         args.warmup = 3
     from maplab_gb300 import build
     build.build()
+    subprocess.check_call(["make", "-s", "-C", os.path.join(ROOT, "oracle")])
     if args.impl == "reference":
-        subprocess.check_call(["make", "-s", "-C", os.path.join(ROOT, "oracle")])
         run_reference(args)
     else:
-        subprocess.check_call(["make", "-s", "-C", os.path.join(ROOT, "oracle")])
         run_ours(args)
 
 

@@ -297,7 +297,13 @@ mba_status mba_cost(mba_handle* h, int32_t precision, double* cost);
 
 /* Runs Levenberg-Marquardt on the device (ceres::Solve with the options of
  * solver-options.h:26-75).  The state stays on the device; read it back with
- * mba_read_state.  summary may be NULL. */
+ * mba_read_state.  summary may be NULL.
+ * MBA_ERR_TIMEOUT means a bounded device wait ran out (the learned
+ * preconditioner's tensor-core pipeline): copies or MMAs it guarded may still
+ * have been in flight, so the device state is undefined.  The handle is then
+ * poisoned: later mba_solve, mba_gnn_train and mba_gnn_gradient calls on it
+ * return MBA_ERR_TIMEOUT without launching anything, and the caller should
+ * destroy its handles and treat the CUDA context as unusable. */
 mba_status mba_solve(mba_handle* h, const mba_solver_options* opts, mba_summary* summary);
 
 /* OptimizationStateBuffer analogue: copy the optimized state out / in.
@@ -316,6 +322,12 @@ void mba_cancel(mba_handle* h);
  * mode 0: FP64 tangent linearization, 1: FP32 tangent linearization.
  * Writes the mean milliseconds per launch. */
 mba_status mba_time_visual_kernel(mba_handle* h, int32_t mode, int32_t iters, double* ms_per_launch);
+
+/* Measured FP64 arithmetic rate of `device` in TFLOP/s (one FMA = 2 FLOPs):
+ * independent FMA chains on every SM, timed with CUDA events.  The
+ * denominator of the FP64 evaluation kernel's roofline; no counterpart in
+ * the reference (a measurement aid). */
+mba_status mba_measure_fp64_peak(int32_t device, double* tflops);
 
 /* The damped reduced camera system of the current state, as one LM iteration
  * builds it (the matrix Ceres's SchurEliminator forms internally for
@@ -490,10 +502,13 @@ typedef struct mba_visual_batch_device {
  * that overlap on the GPU (other streams or threads) race; serialize them.
  * The first call on a device looks up the array's device address with that
  * device current; make that first call before any stream capture.  Runs on
- * `stream` (a cudaStream_t, NULL = legacy default stream) and returns after
- * the stream has finished the evaluation.  Out-of-range indices are skipped
- * on the device and reported as MBA_ERR_OUT_OF_RANGE_INDEX; non-finite costs
- * as MBA_ERR_NON_FINITE. */
+ * `stream` (a cudaStream_t, NULL = legacy default stream); every call copies
+ * two status flags to host memory and synchronizes `stream` before it
+ * returns.  Out-of-range indices are skipped on the device and reported as
+ * MBA_ERR_OUT_OF_RANGE_INDEX; non-finite costs as MBA_ERR_NON_FINITE (the
+ * flags are cleared at the start of every call).  A CUDA error already
+ * pending when the call starts is left in place and reported as
+ * MBA_ERR_CUDA without a launch. */
 mba_status mba_visual_cost_noalloc(const mba_visual_batch_device* batch, int32_t device, void* stream,
                                    double* cost_out_device);
 

@@ -388,6 +388,7 @@ def load_ba():
     _declare(lib, "mba_write_state", ctypes.c_int, [vp] + [c_double_p] * 5)
     _declare(lib, "mba_cancel", None, [vp])
     _declare(lib, "mba_time_visual_kernel", ctypes.c_int, [vp, ctypes.c_int32, ctypes.c_int32, c_double_p])
+    _declare(lib, "mba_measure_fp64_peak", ctypes.c_int, [ctypes.c_int32, c_double_p])
     _declare(lib, "mba_get_stats", ctypes.c_int, [vp, ctypes.POINTER(ProblemStats)])
     i32p = ctypes.POINTER(ctypes.c_int32)
     f32p = ctypes.POINTER(ctypes.c_float)

@@ -47,6 +47,13 @@ def default_options(**kw):
     return o
 
 
+def measure_fp64_peak(device=0):
+    """Measured FP64 rate of the device in TFLOP/s (mba_measure_fp64_peak)."""
+    t = ctypes.c_double()
+    _check(lib().mba_measure_fp64_peak(device, ctypes.byref(t)), "mba_measure_fp64_peak")
+    return t.value
+
+
 def default_landmark_quality_options(**kw):
     o = N.LandmarkQualityOptions()
     lib().mba_default_landmark_quality_options(ctypes.byref(o))

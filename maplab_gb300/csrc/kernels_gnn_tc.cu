@@ -137,7 +137,11 @@ __global__ void __launch_bounds__(128) k_gnn_gemm_tc(int64_t n, const __grid_con
     }
     if (!mbar_wait(bar_load, 0, wait_limit)) {
       state = 1;
-      mbar_wait(bar_load, 0, wait_limit);  // the copies may still land: wait once more before the tile is given up
+      // The copies may still land in this CTA's shared memory: wait eight
+      // times as long again before the tile is given up.  If even that runs
+      // out, copies can outlive the CTA; the host then refuses further solves
+      // on the handle and the caller must treat the context as unusable.
+      mbar_wait(bar_load, 0, 8 * wait_limit);
     } else {
       asm volatile("tcgen05.fence::after_thread_sync;" ::: "memory");
       int first = 1;
@@ -162,7 +166,7 @@ __global__ void __launch_bounds__(128) k_gnn_gemm_tc(int64_t n, const __grid_con
   if (state == 0) {
     if (!mbar_wait(bar_mma, 0, wait_limit)) {
       state = 2;  // every thread that sees the timeout records it (same value)
-      mbar_wait(bar_mma, 0, wait_limit);
+      mbar_wait(bar_mma, 0, 8 * wait_limit);  // MMAs in flight: wait longer before the tensor memory is freed
     }
   }
   __syncthreads();

@@ -184,6 +184,10 @@ struct mba_handle {
   std::vector<int64_t> tgt_off, tgt_order;
   std::vector<int32_t> tgt_row;  // keyframe row of each target in tgt_order
   mba_tuning tuning{};
+  // Set when a bounded device wait ran out during a solve or a training call
+  // (MBA_ERR_TIMEOUT): the work that wait guarded may still be in flight, so
+  // later solves and training calls on this handle are refused.
+  bool poisoned = false;
 };
 
 namespace {
@@ -625,7 +629,10 @@ mba_status run_solve(mba_handle* h, const mba_solver_options& o, mba_summary* su
   std::memset(&c, 0, sizeof(c));
   if (result == MBA_OK || result == MBA_ERR_CANCELLED) cudaMemcpy(&c, h->ctl, sizeof(c), cudaMemcpyDeviceToHost);
   if (device_loop && c.termination == 5) result = MBA_ERR_CANCELLED;
-  if (c.fatal) result = MBA_ERR_TIMEOUT;
+  if (c.fatal) {
+    result = MBA_ERR_TIMEOUT;
+    h->poisoned = true;
+  }
   std::vector<mba_iteration_summary> log(o.max_num_iterations + 1);
   cudaMemcpy(log.data(), h->log, sizeof(mba_iteration_summary) * log.size(), cudaMemcpyDeviceToHost);
   if (sum && (result == MBA_OK || result == MBA_ERR_CANCELLED)) {
@@ -1673,6 +1680,7 @@ mba_status mba_solve(mba_handle* h, const mba_solver_options* opts, mba_summary*
   mba_solver_options o;
   if (opts) o = *opts; else mba_default_solver_options(&o);
   if (o.max_num_iterations < 0 || !(o.initial_trust_region_radius > 0)) return MBA_ERR_INVALID_ARG;
+  if (h->poisoned) return MBA_ERR_TIMEOUT;
   cudaSetDevice(h->device);
   h->cancel.store(0);
   if (o.max_num_iterations == 0) {
@@ -1940,6 +1948,7 @@ mba_status mba_gnn_train(mba_handle* h, mba_gnn* m, double radius, int32_t nprob
                          uint64_t seed, double* losses) {
   if (!h || !m || m->device != h->device || nprobe < 1 || steps < 0 || !(radius > 0.0) || !(lr >= 0.f))
     return MBA_ERR_INVALID_ARG;
+  if (h->poisoned) return MBA_ERR_TIMEOUT;
   cudaSetDevice(h->device);
   SolverLaunch<float> s;
   mba_status ms = gnn_prepare(h, m, radius, &s);
@@ -1954,7 +1963,10 @@ mba_status mba_gnn_train(mba_handle* h, mba_gnn* m, double radius, int32_t nprob
     if (e == cudaSuccess) e = cudaMemcpyAsync(&fatal, &h->ctl->fatal, sizeof(int32_t), cudaMemcpyDeviceToHost, st);
     if (e == cudaSuccess) e = cudaStreamSynchronize(st);
     if (e != cudaSuccess) return MBA_ERR_CUDA;
-    if (fatal) return MBA_ERR_TIMEOUT;
+    if (fatal) {
+      h->poisoned = true;
+      return MBA_ERR_TIMEOUT;
+    }
     if (losses) losses[k] = loss;
     if (!std::isfinite(loss)) return MBA_ERR_NON_FINITE;
     if (lr > 0.f) {
@@ -1975,6 +1987,7 @@ mba_status mba_gnn_train(mba_handle* h, mba_gnn* m, double radius, int32_t nprob
 mba_status mba_gnn_gradient(mba_handle* h, mba_gnn* m, double radius, int32_t nprobe, const float* probes,
                             uint64_t seed, float* grad, double* loss, double* coef) {
   if (!h || !m || m->device != h->device || nprobe < 1 || !(radius > 0.0)) return MBA_ERR_INVALID_ARG;
+  if (h->poisoned) return MBA_ERR_TIMEOUT;
   cudaSetDevice(h->device);
   SolverLaunch<float> s;
   mba_status ms = gnn_prepare(h, m, radius, &s);
@@ -1996,7 +2009,10 @@ mba_status mba_gnn_gradient(mba_handle* h, mba_gnn* m, double radius, int32_t np
   if (e == cudaSuccess) e = cudaMemcpyAsync(&fatal, &h->ctl->fatal, sizeof(int32_t), cudaMemcpyDeviceToHost, st);
   if (e == cudaSuccess) e = cudaStreamSynchronize(st);
   if (dprobe) cudaFree(dprobe);
-  if (e == cudaSuccess && fatal) return MBA_ERR_TIMEOUT;
+  if (e == cudaSuccess && fatal) {
+    h->poisoned = true;
+    return MBA_ERR_TIMEOUT;
+  }
   return cuda_status(e);
 }
 

@@ -167,13 +167,21 @@ extern "C" mba_status mba_visual_cost_noalloc(const mba_visual_batch_device* bat
                 !batch->kf_mission || !batch->mission_q_GM_p_GM || !batch->cameras))
     return MBA_ERR_INVALID_ARG;
   if (cudaSetDevice(device) != cudaSuccess) return MBA_ERR_NO_DEVICE;
+  // An error the caller's own work left pending is not this call's to clear:
+  // report it without launching and leave it for the caller to read.
+  if (cudaPeekAtLastError() != cudaSuccess) return MBA_ERR_CUDA;
   double* scratch = nullptr;
   mba_status st = scratch_for_device(device, &scratch);
   if (st != MBA_OK) return st;
   cudaStream_t s = static_cast<cudaStream_t>(stream);
   const int nblocks = (int)((n + kThreads - 1) / kThreads);
+  // Nothing was pending on entry, so an error read here comes from these launches.
   k_noalloc_clear<<<1, 1, 0, s>>>(scratch);
-  if (nblocks > 0) k_noalloc_visual_cost<<<nblocks, kThreads, 0, s>>>(*batch, scratch);
+  if (cudaGetLastError() != cudaSuccess) return MBA_ERR_CUDA;
+  if (nblocks > 0) {
+    k_noalloc_visual_cost<<<nblocks, kThreads, 0, s>>>(*batch, scratch);
+    if (cudaGetLastError() != cudaSuccess) return MBA_ERR_CUDA;
+  }
   k_noalloc_reduce<<<1, kThreads, 0, s>>>(scratch, nblocks, cost_out_device);
   if (cudaGetLastError() != cudaSuccess) return MBA_ERR_CUDA;
   double flags[2] = {0.0, 0.0};

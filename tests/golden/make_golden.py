@@ -1,6 +1,7 @@
 """Extracts golden vectors from the reference's own unit tests (read as text).
 
-Run in a container where the maplab source tree is mounted:
+Run where the maplab source tree is available (its root as the argument or
+in the MAPLAB_REFERENCE_ROOT environment variable):
 
     python tests/golden/make_golden.py /path/to/maplab
 
@@ -110,7 +111,27 @@ def main(root):
     with open(os.path.join(here, "imu_integrator.json"), "w") as f:
         json.dump(out, f, indent=1)
     print("wrote", os.path.join(here, "imu_integrator.json"))
+    sensor_files(root, here)
+
+
+# maplab's own calibration files: the map reader's sensors.yaml parser is
+# checked against them (tests/test_vimap_io.py: test_reference_sensor_files).
+SENSOR_FILES = [
+    "maplab-launch/config/alphasense-dev-kit/calib/alphasense-dev-kit-sensors.yaml",
+    "maplab-launch/config/lidarstick/calib/lidarstick-150-deg-cams-sensors.yaml",
+]
+
+
+def sensor_files(root, here):
+    out = {"generator": "tests/golden/make_golden.py",
+           "files": {name: open(os.path.join(root, name)).read() for name in SENSOR_FILES}}
+    with open(os.path.join(here, "reference_sensors.json"), "w") as f:
+        json.dump(out, f, indent=1)
+    print("wrote", os.path.join(here, "reference_sensors.json"))
 
 
 if __name__ == "__main__":
-    main(sys.argv[1] if len(sys.argv) > 1 else "/root/reference")
+    root = sys.argv[1] if len(sys.argv) > 1 else os.environ.get("MAPLAB_REFERENCE_ROOT")
+    if not root or not os.path.isdir(root):
+        sys.exit("usage: make_golden.py <maplab source root> (or set MAPLAB_REFERENCE_ROOT)")
+    main(root)

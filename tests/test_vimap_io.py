@@ -15,7 +15,7 @@ from maplab_gb300 import _native as N
 from maplab_gb300 import ba, synth, vimap
 from vimap_writer import T_inverse, from_jpl_block, make_id, quat_R, write_map
 
-REF = "/root/reference"
+GOLDEN = os.path.join(os.path.dirname(os.path.abspath(__file__)), "golden")
 
 
 def arr(desc, name, shape, dtype=np.float64):
@@ -245,15 +245,16 @@ def _sensors_only_map(folder, yaml_text, ncamera_hex, num_frames):
         f.write(yaml_text)
 
 
-@pytest.mark.skipif(not os.path.isdir(REF), reason="the reference sources are not present")
 @pytest.mark.parametrize("name, ncam", [
     ("maplab-launch/config/alphasense-dev-kit/calib/alphasense-dev-kit-sensors.yaml", 5),
     ("maplab-launch/config/lidarstick/calib/lidarstick-150-deg-cams-sensors.yaml", None),
 ])
 def test_reference_sensor_files(tmp_path, name, ncam):
-    """maplab's own calibration files parse; the cameras' intrinsics and
-    T_B_C come out as written there."""
-    text = open(os.path.join(REF, name)).read()
+    """maplab's own calibration files (copied into tests/golden/ by
+    tests/golden/make_golden.py) parse; the cameras' intrinsics and T_B_C
+    come out as written there."""
+    import json
+    text = json.load(open(os.path.join(GOLDEN, "reference_sensors.json")))["files"][name]
     ncam_hex = re.search(r"id: ([0-9a-f]{32})\s+sensor_type: NCAMERA", text).group(1)
     block = text[text.index(ncam_hex):]
     fus = [float(x) for x in re.findall(r"intrinsics:\s+rows: 4\s+cols: 1\s+data:\s+- ([-0-9.e]+)", block)]

@@ -71,6 +71,62 @@ def test_noalloc_cost_matches_handle_cost_on_two_calls():
         torch.cuda.synchronize()
 
 
+def _small_map():
+    return synth.generate("c4", num_missions=3, keyframes_per_mission=30, num_landmarks=800,
+                          shared_landmark_fraction=0.3, include_inertial=0)
+
+
+def test_noalloc_cost_matches_the_oracle():
+    """The same cost straight against the CPU oracle's robustified cost."""
+    torch = pytest.importorskip("torch")
+    import oracle_lib
+    m = _small_map()
+    expected = oracle_lib.OracleProblem(m.desc).cost()
+    batch, keep = _device_batch(m, torch)
+    out = torch.full((1,), float("nan"), dtype=torch.float64, device="cuda")
+    torch.cuda.synchronize()
+    st = ba.lib().mba_visual_cost_noalloc(ctypes.byref(batch), torch.cuda.current_device(), None,
+                                          ctypes.c_void_p(out.data_ptr()))
+    assert st == N.MBA_OK
+    got = float(out.item())
+    assert abs(got - expected) <= 1e-12 * expected, (got, expected)
+
+
+def test_noalloc_reports_bad_index_and_non_finite_then_clears_the_flags():
+    """A batch with one landmark index past the end (skipped on the device)
+    reports MBA_ERR_OUT_OF_RANGE_INDEX; one NaN uncertainty reports
+    MBA_ERR_NON_FINITE; a valid call right after each reports MBA_OK with
+    the right cost, so the flags the bad call left are cleared."""
+    torch = pytest.importorskip("torch")
+    import oracle_lib
+    m = _small_map()
+    expected = oracle_lib.OracleProblem(m.desc).cost()
+    lib = ba.lib()
+    dev = torch.cuda.current_device()
+    batch, keep = _device_batch(m, torch)
+    out = torch.full((1,), float("nan"), dtype=torch.float64, device="cuda")
+
+    def call():
+        torch.cuda.synchronize()
+        return lib.mba_visual_cost_noalloc(ctypes.byref(batch), dev, None, ctypes.c_void_p(out.data_ptr()))
+
+    good_lm = keep["obs_landmark"][5].item()
+    keep["obs_landmark"][5] = m.desc.num_landmarks  # one past the end: never read
+    assert call() == N.MBA_ERR_OUT_OF_RANGE_INDEX
+    keep["obs_landmark"][5] = good_lm
+    assert call() == N.MBA_OK
+    assert abs(float(out.item()) - expected) <= 1e-12 * expected
+
+    r, _ = oracle_lib.OracleProblem(m.desc).evaluate_visual()
+    i = int(np.flatnonzero(np.any(r != 0.0, axis=1))[0])  # a projection that succeeds
+    good_sigma = keep["obs_sigma"][i].item()
+    keep["obs_sigma"][i] = float("nan")
+    assert call() == N.MBA_ERR_NON_FINITE
+    keep["obs_sigma"][i] = good_sigma
+    assert call() == N.MBA_OK
+    assert abs(float(out.item()) - expected) <= 1e-12 * expected
+
+
 def test_noalloc_rejects_batches_above_the_scratch_limit():
     torch = pytest.importorskip("torch")
     lib = ba.lib()
