@@ -316,11 +316,11 @@ __global__ void __launch_bounds__(32 * kWarps) k_inertial_mat(DevProblem P, cons
   }
   for (int a = lane; a < 225; a += 32) L[a] = (double)S.Q[a];
   __syncwarp();
-  int fail = 0;
+  int fail = -1;
   for (int j = 0; j < 15; ++j) {
     const double d = L[j * 16];
     if (!(d > 0.0)) {  // the same value in every lane: a uniform exit
-      fail = 1;
+      fail = j;
       break;
     }
     const double ljj = sqrt(d), inv = 1.0 / ljj;
@@ -340,9 +340,20 @@ __global__ void __launch_bounds__(32 * kWarps) k_inertial_mat(DevProblem P, cons
     }
     __syncwarp();
   }
-  if (fail) {
-    if (lane == 0 && out.status) atomicMax(out.status, (int)MBA_ERR_NOT_SPD);
-    return;
+  if (fail >= 0) {
+    // Q_acc not positive definite.  The reference factorizes with Eigen's
+    // LLT and never checks info() (inertial-error-term.cc:155-182): Eigen's
+    // column-by-column factorization stops at column `fail`, leaving that
+    // column (diagonal included) and every later column of the lower
+    // triangle at Q's own values, and the triangular solves use that matrix.
+    // Columns >= fail are restored from Q here (the right-looking updates
+    // above had already touched them).
+#pragma unroll
+    for (int s = 0; s < 4; ++s)
+      if (own_k[s] >= fail) L[own_i[s] * 15 + own_k[s]] = (double)S.Q[own_i[s] * 15 + own_k[s]];
+    __syncwarp();
+    if (lane >= fail && lane < 15) dinv[lane] = 1.0 / L[lane * 16];
+    __syncwarp();
   }
   if (lane < 15) {  // X = L^-1, column `lane`
     for (int i = 0; i < 15; ++i) {

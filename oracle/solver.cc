@@ -1154,8 +1154,28 @@ int solve(Problem& p, const mba_solver_options& o, mba_summary* sum) {
     const double new_cost = cst ? INFINITY : Lc.cost;
     // parameter tolerance bookkeeping (ambient step norm)
     double step_norm = 0.0, x_norm = 0.0;
-    for (size_t a = 0; a < kx.size(); ++a) { const double dd = p.kf_x[a] - kx[a]; step_norm += dd * dd; x_norm += kx[a] * kx[a]; }
-    for (size_t a = 0; a < lp.size(); ++a) { const double dd = p.lm_p[a] - lp[a]; step_norm += dd * dd; x_norm += lp[a] * lp[a]; }
+    // (Ceres: norms of the ambient step and state over the parameter blocks
+    // of the reduced program, i.e. the non-constant blocks)
+    auto any = [&](int64_t k, int a0, int a1) {
+      for (int a = a0; a < a1; ++a)
+        if (p.kf_mask[15 * k + a]) return true;
+      return false;
+    };
+    auto add = [&](const std::vector<double>& now, const std::vector<double>& old, int64_t b, int n) {
+      for (int a = 0; a < n; ++a) {
+        const double dd = now[n * b + a] - old[n * b + a];
+        step_norm += dd * dd;
+        x_norm += old[n * b + a] * old[n * b + a];
+      }
+    };
+    for (int64_t k = 0; k < p.nkf; ++k) {
+      if (any(k, 0, 6)) add(p.kf_x, kx, k, 7);
+      if (any(k, 6, 9)) add(p.kf_v, kv, k, 3);
+      if (any(k, 9, 12)) add(p.kf_bg, kbg, k, 3);
+      if (any(k, 12, 15)) add(p.kf_ba, kba, k, 3);
+    }
+    for (int64_t l = 0; l < p.nlm; ++l)
+      if (p.lm_mask[l]) add(p.lm_p, lp, l, 3);
     for (size_t a = 0; a < swv.size(); ++a) { const double dd = p.sw[a] - swv[a]; step_norm += dd * dd; x_norm += swv[a] * swv[a]; }
     step_norm = std::sqrt(step_norm);
     x_norm = std::sqrt(x_norm);

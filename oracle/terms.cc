@@ -580,9 +580,18 @@ bool inertialIntegrate(const ImuNoise& n, const double* begin, int ns, const int
   return true;
 }
 
-// Textbook Cholesky L L^T = A (Eigen::LLT restated); false if not SPD.
+// Eigen::LLT<Matrix15d>::compute restated (the column-by-column in-place
+// factorization Eigen uses below 32 rows): L L^T = A, lower triangle.  The
+// reference calls compute() and then matrixL() without checking info()
+// (inertial-error-term.cc:155-182), so a non-positive pivot does not fail
+// the term: the factorization stops at that column j, whose diagonal and
+// sub-diagonal keep A's values, as do all later columns of the lower
+// triangle; the triangular solves then use that matrix.  Returns false in
+// that case (the factor is still written).
 static bool cholesky15(const double* A, double* L) {
   for (int i = 0; i < 225; ++i) L[i] = 0.0;
+  for (int i = 0; i < 15; ++i)
+    for (int k = 0; k <= i; ++k) L[i * 15 + k] = A[i * 15 + k];
   for (int j = 0; j < 15; ++j) {
     double d = A[j * 15 + j];
     for (int k = 0; k < j; ++k) d -= L[j * 15 + k] * L[j * 15 + k];
@@ -618,7 +627,7 @@ int inertialEvaluate(const ImuNoise& n, const double* const* P, int ns, const in
   std::memcpy(begin + 10, P[3], 3 * sizeof(double));
   std::memcpy(begin + 13, P[0] + 4, 3 * sizeof(double));
   if (!inertialIntegrate(n, begin, ns, ts, imu, end, phi, Q)) return MBA_ERR_UNORDERED_IMU;
-  if (!cholesky15(Q, L)) return MBA_ERR_NOT_SPD;
+  cholesky15(Q, L);  // a non-positive-definite Q_accum is used as Eigen leaves it (no failure)
   const double* q_to = P[4];
   if (res) {
     // Eigen::Quaterniond::inverse(): conjugate / squaredNorm.

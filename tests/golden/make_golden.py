@@ -112,6 +112,11 @@ def main(root):
         json.dump(out, f, indent=1)
     print("wrote", os.path.join(here, "imu_integrator.json"))
     sensor_files(root, here)
+    sys.path.insert(0, here)
+    import error_term_scenarios
+    with open(os.path.join(here, "error_term_scenarios.json"), "w") as f:
+        json.dump(error_term_scenarios.extract(root), f, indent=1)
+    print("wrote", os.path.join(here, "error_term_scenarios.json"))
 
 
 # maplab's own calibration files: the map reader's sensors.yaml parser is
