@@ -34,7 +34,7 @@
 extern "C" {
 #endif
 
-#define MBA_ABI_VERSION 1
+#define MBA_ABI_VERSION 2
 
 typedef enum mba_status {
   MBA_OK = 0,
@@ -52,8 +52,35 @@ typedef enum mba_status {
 /* ceres_error_terms::LandmarkErrorType (ceres-error-terms/common.h:14). */
 enum { MBA_LOCAL_KEYFRAME = 0, MBA_LOCAL_MISSION = 1, MBA_GLOBAL = 2 };
 
-/* aslam::Distortion::Type subset: pinhole + {none, radtan, equidistant}. */
-enum { MBA_DISTORTION_NONE = 0, MBA_DISTORTION_RADTAN = 1, MBA_DISTORTION_EQUIDISTANT = 2 };
+/* aslam::Distortion::Type subset: pinhole + {none, radtan, equidistant,
+ * fisheye}.  MBA_DISTORTION_FOV is aslam's FisheyeDistortion (the
+ * field-of-view model, aslam_cv_cameras/src/distortion-fisheye.cc) with its
+ * one parameter w in distortion[0]; w^2 < 1e-5 is the identity map. */
+enum { MBA_DISTORTION_NONE = 0, MBA_DISTORTION_RADTAN = 1, MBA_DISTORTION_EQUIDISTANT = 2, MBA_DISTORTION_FOV = 3 };
+
+/* Camera calibration blocks left free in the solve (camera_flags).  maplab's
+ * builder sets the intrinsics and distortion blocks constant unless
+ * ba_fix_ncamera_intrinsics = false, and q_C_I / p_C_I unless
+ * ba_fix_ncamera_extrinsics_rotation / _translation = false
+ * (vi-optimization-builder.cc:24-35, optimization-terms-addition.cc:
+ * 203-234); the cost-term tests free each block on its own.  Intrinsics and
+ * distortion are plain additive blocks, q_C_I uses JplQuaternion-
+ * Parameterization. */
+enum {
+  MBA_CAM_INTRINSICS_FREE = 1u << 0,
+  MBA_CAM_DISTORTION_FREE = 1u << 1,
+  MBA_CAM_ROTATION_FREE = 1u << 2,
+  MBA_CAM_TRANSLATION_FREE = 1u << 3
+};
+/* Mission baseframe T_G_M left free (mission_flags).  maplab fixes all
+ * baseframes (fixAllBaseframesInProblem) unless absolute 6-DoF terms are in
+ * the problem and fix_baseframes is off (vi-optimization-builder.cc:
+ * 366-371); it then uses JplYawOnlyPoseParameterization (yaw + position,
+ * optimization-problem.cc:90-91).  The mission-baseframe tests use
+ * JplPoseParameterization (6 dof).  A free baseframe enters the kGlobal
+ * visual terms; problems that also have absolute 6-DoF or cross-mission
+ * loop-closure terms must keep their baseframes constant. */
+enum { MBA_MIS_BASEFRAME_YAW_POSITION = 1u << 0, MBA_MIS_BASEFRAME_POSE = 1u << 1 };
 
 /* Per-keyframe fix flags (kf_flags).  They restate the Ceres parameter-block
  * constness and local parameterizations chosen by the problem builder:
@@ -157,6 +184,11 @@ typedef struct mba_problem_desc {
   const int32_t* pose_edge_type;       /* [N_pe] MBA_POSE_EDGE_*; NULL = all RELATIVE */
   const double* pose_edge_switch;      /* [N_pe] initial switch of a loop closure; NULL = 1 */
   const double* pose_edge_switch_variance; /* [N_pe] switch prior variance; NULL = all 0 */
+  /* Calibration and baseframes as variables (NULL = all constant, maplab's
+   * defaults).  FP64 solves only: a mixed-precision solve of a problem with
+   * a free block returns MBA_ERR_INVALID_ARG. */
+  const uint32_t* camera_flags;  /* [N_cam] MBA_CAM_* bits */
+  const uint32_t* mission_flags; /* [N_mis] MBA_MIS_BASEFRAME_* (at most one bit) */
 } mba_problem_desc;
 
 enum { MBA_POSE_EDGE_RELATIVE = 0, MBA_POSE_EDGE_LOOP_CLOSURE = 1, MBA_POSE_EDGE_ABSOLUTE = 2 };
@@ -312,6 +344,17 @@ mba_status mba_read_state(mba_handle* h, double* kf_q_IM_p_MI, double* kf_v_M,
                           double* kf_b_g, double* kf_b_a, double* lm_p_B);
 mba_status mba_write_state(mba_handle* h, const double* kf_q_IM_p_MI, const double* kf_v_M,
                            const double* kf_b_g, const double* kf_b_a, const double* lm_p_B);
+
+/* Camera calibration and mission baseframes of the handle's current state
+ * (the blocks that mba_problem_desc's camera_flags / mission_flags leave
+ * free move during a solve): cameras [N_cam] (every field copied) and
+ * mission_q_GM_p_GM [N_mis][7].  Either pointer may be NULL.  Writing sets
+ * the intrinsics, distortion parameters, q_C_I | p_C_I and baseframes;
+ * quaternions must be unit within 1e-5 and distortion types and image sizes
+ * must match the descriptor's.  The OptimizationStateBuffer analogue for the
+ * sensor and baseframe blocks (optimization-state-buffer.cc:42-152). */
+mba_status mba_read_calibration(mba_handle* h, mba_camera* cameras, double* mission_q_GM_p_GM);
+mba_status mba_write_calibration(mba_handle* h, const mba_camera* cameras, const double* mission_q_GM_p_GM);
 
 /* Thread-safe request to stop after the current LM iteration (the SIGINT
  * handler of ceres-error-terms/src/ceres-signal-handler.cc:12-56). */

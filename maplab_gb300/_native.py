@@ -33,7 +33,14 @@ MBA_ERR_NO_DEVICE = 8
 MBA_ERR_UNORDERED_IMU = 9
 
 MBA_LOCAL_KEYFRAME, MBA_LOCAL_MISSION, MBA_GLOBAL = 0, 1, 2
-MBA_DISTORTION_NONE, MBA_DISTORTION_RADTAN, MBA_DISTORTION_EQUIDISTANT = 0, 1, 2
+MBA_DISTORTION_NONE, MBA_DISTORTION_RADTAN, MBA_DISTORTION_EQUIDISTANT, MBA_DISTORTION_FOV = 0, 1, 2, 3
+
+MBA_CAM_INTRINSICS_FREE = 1 << 0
+MBA_CAM_DISTORTION_FREE = 1 << 1
+MBA_CAM_ROTATION_FREE = 1 << 2
+MBA_CAM_TRANSLATION_FREE = 1 << 3
+MBA_MIS_BASEFRAME_YAW_POSITION = 1 << 0
+MBA_MIS_BASEFRAME_POSE = 1 << 1
 
 MBA_KF_POSE_CONSTANT = 1 << 0
 MBA_KF_GAUGE_ROLL_PITCH = 1 << 1
@@ -111,6 +118,8 @@ class ProblemDesc(ctypes.Structure):
         ("pose_edge_type", c_int32_p),
         ("pose_edge_switch", c_double_p),
         ("pose_edge_switch_variance", c_double_p),
+        ("camera_flags", c_uint32_p),
+        ("mission_flags", c_uint32_p),
     ]
 
 
@@ -385,6 +394,8 @@ def load_ba():
     _declare(lib, "mba_cost", ctypes.c_int, [vp, ctypes.c_int32, c_double_p])
     _declare(lib, "mba_solve", ctypes.c_int, [vp, ctypes.POINTER(SolverOptions), ctypes.POINTER(Summary)])
     _declare(lib, "mba_read_state", ctypes.c_int, [vp] + [c_double_p] * 5)
+    _declare(lib, "mba_read_calibration", ctypes.c_int, [vp, ctypes.POINTER(Camera), c_double_p])
+    _declare(lib, "mba_write_calibration", ctypes.c_int, [vp, ctypes.POINTER(Camera), c_double_p])
     _declare(lib, "mba_write_state", ctypes.c_int, [vp] + [c_double_p] * 5)
     _declare(lib, "mba_cancel", None, [vp])
     _declare(lib, "mba_time_visual_kernel", ctypes.c_int, [vp, ctypes.c_int32, ctypes.c_int32, c_double_p])
@@ -464,6 +475,17 @@ def make_summary(capacity=64):
     s.iterations = ctypes.cast(its, ctypes.POINTER(IterationSummary))
     s._its = its  # keep alive
     return s
+
+
+def calibration_dict(cams, mis):
+    """Per-camera and per-mission blocks as arrays: intrinsics [N_cam][4],
+    distortion [N_cam][4], q_CI [N_cam][4], p_CI [N_cam][3], baseframes
+    [N_mis][7]."""
+    return {"intrinsics": np.array([list(c.intrinsics) for c in cams]).reshape(-1, 4),
+            "distortion": np.array([list(c.distortion) for c in cams]).reshape(-1, 4),
+            "q_CI": np.array([list(c.q_CI_p_CI)[:4] for c in cams]).reshape(-1, 4),
+            "p_CI": np.array([list(c.q_CI_p_CI)[4:] for c in cams]).reshape(-1, 3),
+            "baseframes": np.asarray(mis, dtype=np.float64).reshape(-1, 7)}
 
 
 def summary_dict(s):

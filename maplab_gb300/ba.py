@@ -201,6 +201,15 @@ class BundleAdjuster:
                                                       ("kf_q_IM_p_MI", "kf_v_M", "kf_b_g", "kf_b_a", "lm_p_B")]),
                "mba_write_state")
 
+    def read_calibration(self):
+        """Cameras and mission baseframes of the current state
+        (mba_read_calibration) as arrays (see _native.calibration_dict)."""
+        d = self.desc
+        cams = (N.Camera * d.num_cameras)()
+        mis = np.zeros((d.num_missions, 7))
+        _check(self._lib.mba_read_calibration(self._h, cams, N.ptr(mis)), "mba_read_calibration")
+        return N.calibration_dict(cams, mis)
+
     def time_visual_kernel(self, mode=1, iters=20):
         ms = ctypes.c_double()
         _check(self._lib.mba_time_visual_kernel(self._h, mode, iters, ctypes.byref(ms)), "mba_time_visual_kernel")

@@ -18,7 +18,8 @@ CSRC = os.path.join(HERE, "csrc")
 BUILD = os.path.join(HERE, "_build")
 
 CUDA_SOURCES = ["mba_api.cu", "kernels_eval.cu", "kernels_inertial.cu", "kernels_solver.cu", "kernels_chain.cu",
-                "kernels_gnn.cu", "kernels_gnn_tc.cu", "kernels_pose.cu", "noalloc.cu", "kernels_peak.cu"]
+                "kernels_gnn.cu", "kernels_gnn_tc.cu", "kernels_pose.cu", "noalloc.cu", "kernels_peak.cu",
+                "kernels_border.cu"]
 HOST_SOURCES = ["vimap_io.cc"]  # host-only parts of libmaplab_ba.so (g++)
 ARCH = ["-gencode", "arch=compute_103a,code=sm_103a"]
 NVCC_FLAGS = ["-O3", "-lineinfo", "-std=c++17", "-Xcompiler", "-fPIC", "-Xcompiler", "-O2",

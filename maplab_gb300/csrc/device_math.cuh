@@ -133,6 +133,12 @@ __device__ __forceinline__ double datan<double>(double x) { return atan(x); }
 template <>
 __device__ __forceinline__ float datan<float>(float x) { return atanf(x); }
 template <typename T>
+__device__ __forceinline__ T dtan(T x);
+template <>
+__device__ __forceinline__ double dtan<double>(double x) { return tan(x); }
+template <>
+__device__ __forceinline__ float dtan<float>(float x) { return tanf(x); }
+template <typename T>
 __device__ __forceinline__ T dpow(T x, T y);
 template <>
 __device__ __forceinline__ double dpow<double>(double x, double y) { return pow(x, y); }
@@ -187,8 +193,74 @@ __device__ __forceinline__ void distort(int dtype, const T* k, T* pt, T* J) {
     const T s = (r > T(1e-8)) ? thetad / r : T(1);
     pt[0] = x * s;
     pt[1] = y * s;
+  } else if (dtype == MBA_DISTORTION_FOV) {
+    // FisheyeDistortion (distortion-fisheye.cc:14-80): r_d = atan(2 tan(w/2) r_u) / w.
+    const T w = k[0];
+    const T u = pt[0], v = pt[1];
+    const T uv2 = u * u + v * v;
+    const T r_u = dsqrt(uv2);
+    const T tanwhalf = dtan(w / T(2));
+    const T tanwhalfsq = tanwhalf * tanwhalf;
+    const T atan_wrd = datan(T(2) * tanwhalf * r_u);
+    T r_rd;
+    if (w * w < T(1e-5)) {
+      r_rd = T(1);
+      J[0] = T(1); J[1] = T(0); J[2] = T(0); J[3] = T(1);
+    } else if (r_u * r_u < T(1e-5)) {
+      r_rd = T(2) * tanwhalf / w;
+      J[0] = r_rd; J[1] = T(0); J[2] = T(0); J[3] = r_rd;
+    } else {
+      r_rd = atan_wrd / (r_u * w);
+      const T r_u_cubed = r_u * r_u * r_u;
+      const T den = w * uv2 * (T(4) * tanwhalfsq * uv2 + T(1));
+      J[0] = atan_wrd / (w * r_u) - (u * u * atan_wrd) / (w * r_u_cubed) + (T(2) * u * u * tanwhalf) / den;
+      J[1] = (T(2) * u * v * tanwhalf) / den - (u * v * atan_wrd) / (w * r_u_cubed);
+      J[2] = J[1];
+      J[3] = atan_wrd / (w * r_u) - (v * v * atan_wrd) / (w * r_u_cubed) + (T(2) * v * v * tanwhalf) / den;
+    }
+    pt[0] = u * r_rd;
+    pt[1] = v * r_rd;
   } else {
     J[0] = T(1); J[1] = T(0); J[2] = T(0); J[3] = T(1);
+  }
+}
+
+// Distortion-parameter Jacobian at the undistorted normalized point
+// (distortion-radtan.cc:67-91, distortion-equidistant.cc:109-142,
+// distortion-fisheye.cc:82-110); k = the model's parameters.
+__device__ __forceinline__ void dist_param_jac(int dtype, const double* k, const double* pt, double* J) {
+  if (dtype == MBA_DISTORTION_RADTAN) {
+    const double y0 = pt[0], y1 = pt[1], r2 = y0 * y0 + y1 * y1, r4 = r2 * r2;
+    J[0] = y0 * r2; J[1] = y0 * r4; J[2] = 2.0 * y0 * y1; J[3] = r2 + 2.0 * y0 * y0;
+    J[4] = y1 * r2; J[5] = y1 * r4; J[6] = r2 + 2.0 * y1 * y1; J[7] = 2.0 * y0 * y1;
+  } else if (dtype == MBA_DISTORTION_EQUIDISTANT) {
+    const double x = pt[0], y = pt[1];
+    const double r = sqrt(x * x + y * y);
+    const double th = atan(r);
+    if (r < 1e-10) {
+      for (int a = 0; a < 8; ++a) J[a] = 0.0;
+      return;
+    }
+    const double t3 = pow(th, 3.0), t5 = pow(th, 5.0), t7 = pow(th, 7.0), t9 = pow(th, 9.0);
+    J[0] = x * t3 / r; J[1] = x * t5 / r; J[2] = x * t7 / r; J[3] = x * t9 / r;
+    J[4] = y * t3 / r; J[5] = y * t5 / r; J[6] = y * t7 / r; J[7] = y * t9 / r;
+  } else if (dtype == MBA_DISTORTION_FOV) {
+    // distortion-fisheye.cc:82-110: d(distorted point) / dw in column 0.
+    for (int a = 0; a < 8; ++a) J[a] = 0.0;
+    const double w = k[0];
+    if (w * w < 1e-5) return;
+    const double u = pt[0], v = pt[1];
+    const double r_u = sqrt(u * u + v * v);
+    const double tanwhalf = tan(w / 2.0), tanwhalfsq = tanwhalf * tanwhalf;
+    const double atan_wrd = atan(2.0 * tanwhalf * r_u);
+    if (r_u * r_u < 1e-5) {
+      J[0] = J[4] = (w - sin(w)) / (w * w * cos(w / 2) * cos(w / 2));
+      return;
+    }
+    J[0] = (2 * u * (tanwhalfsq / 2 + 0.5)) / (w * (4 * tanwhalfsq * r_u * r_u + 1)) - (u * atan_wrd) / (w * w * r_u);
+    J[4] = (2 * v * (tanwhalfsq / 2 + 0.5)) / (w * (4 * tanwhalfsq * r_u * r_u + 1)) - (v * atan_wrd) / (w * w * r_u);
+  } else {
+    for (int a = 0; a < 8; ++a) J[a] = 0.0;
   }
 }
 
@@ -269,6 +341,18 @@ __device__ __forceinline__ void jpl_plus(const double* q, const double* d, doubl
     qd[3] = cos(nh);
   }
   qprod_pos(qd, q, out);
+}
+
+// JplYawQuaternionParameterization::Plus and ComputeJacobian
+// (quaternion-param-jpl.cc:78-105): a rotation about z by the one tangent
+// dim, applied on the left; Jacobian 4 x 1.
+__device__ __forceinline__ void jpl_yaw_plus(const double* q, const double* d, double* out) {
+  const double h = 0.5 * d[0];
+  const double qd[4] = {0.0, 0.0, sin(h), cos(fabs(h))};
+  qprod_pos(qd, q, out);
+}
+__device__ __forceinline__ void dqdyaw(const double* q, double* J) {
+  J[0] = q[1] * 0.5; J[1] = -q[0] * 0.5; J[2] = q[3] * 0.5; J[3] = -q[2] * 0.5;
 }
 
 // JplRollPitchQuaternionParameterization::Plus (quaternion-param-jpl.cc:113-142).

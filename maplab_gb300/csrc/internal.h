@@ -72,6 +72,18 @@ struct DevProblem {
   float* kf_pose_f;         // [nkf][8] = q(4) p(3) pad
   const float* mis_f;       // [nmis][8]
   const DevCameraT<float>* cams_f;
+  // Calibration / baseframe variables ("global nodes", FP64 solves): one
+  // 15-dim block per camera with a free calibration block (dims: intrinsics
+  // 0-3, distortion 4-7, theta_C_I 8-10, p_C_I 11-13) and per mission with a
+  // free baseframe (theta 0-2, or yaw 0, and p_G_M 3-5), after the keyframe
+  // blocks of the reduced system.  ng = 0: none.
+  int64_t ng;
+  const int32_t* cam_node;  // [ncam] node of each camera, -1 = constant
+  const int32_t* mis_node;  // [nmis]
+  const int32_t* node_cam;  // [ng] camera of each node (-1 for a mission node)
+  const int32_t* node_mis;  // [ng] mission of each node (-1 for a camera node)
+  const uint16_t* g_mask;   // [ng] active dims
+  const uint32_t* mis_flags;// [nmis] MBA_MIS_BASEFRAME_*
 };
 
 // Typed view of the inputs of the evaluation kernel (FP64 arrays for the

@@ -597,29 +597,6 @@ __global__ void __launch_bounds__(kBlock) k_landmark_quality(DevProblem P, mba_l
   good[l] = angle_deg < o.min_observation_angle_deg ? 0 : 1;
 }
 
-// Distortion-parameter Jacobian at the undistorted normalized point
-// (distortion-radtan.cc:67-91, distortion-equidistant.cc:109-142).
-__device__ void dist_param_jac(int dtype, const double* pt, double* J) {
-  if (dtype == MBA_DISTORTION_RADTAN) {
-    const double y0 = pt[0], y1 = pt[1], r2 = y0 * y0 + y1 * y1, r4 = r2 * r2;
-    J[0] = y0 * r2; J[1] = y0 * r4; J[2] = 2.0 * y0 * y1; J[3] = r2 + 2.0 * y0 * y0;
-    J[4] = y1 * r2; J[5] = y1 * r4; J[6] = r2 + 2.0 * y1 * y1; J[7] = 2.0 * y0 * y1;
-  } else if (dtype == MBA_DISTORTION_EQUIDISTANT) {
-    const double x = pt[0], y = pt[1];
-    const double r = sqrt(x * x + y * y);
-    const double th = atan(r);
-    if (r < 1e-10) {
-      for (int a = 0; a < 8; ++a) J[a] = 0.0;
-      return;
-    }
-    const double t3 = pow(th, 3.0), t5 = pow(th, 5.0), t7 = pow(th, 7.0), t9 = pow(th, 9.0);
-    J[0] = x * t3 / r; J[1] = x * t5 / r; J[2] = x * t7 / r; J[3] = x * t9 / r;
-    J[4] = y * t3 / r; J[5] = y * t5 / r; J[6] = y * t7 / r; J[7] = y * t9 / r;
-  } else {
-    for (int a = 0; a < 8; ++a) J[a] = 0.0;
-  }
-}
-
 struct AmbientOut {
   double* res;
   double* J[9];
@@ -753,7 +730,7 @@ __global__ void __launch_bounds__(128) k_visual_ambient(DevProblem P, AmbientOut
     }
     if (o.J[8]) {
       double Jp[8];
-      dist_param_jac(cam.dtype, un, Jp);
+      dist_param_jac(cam.dtype, cam.dist, un, Jp);
       for (int a = 0; a < 4; ++a) {
         o.J[8][8 * oi + a] = Jp[a] * cam.intr[0] * sinv;
         o.J[8][8 * oi + 4 + a] = Jp[4 + a] * cam.intr[1] * sinv;

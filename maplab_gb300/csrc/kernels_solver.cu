@@ -684,7 +684,7 @@ template <typename T>
 __global__ void __launch_bounds__(64) k_block_jacobi(SolverLaunch<T> s) {
   if (s.ctl->terminated) return;
   const int64_t k = blockIdx.x * (int64_t)blockDim.x + threadIdx.x;
-  if (k >= s.P.nkf) return;
+  if (k >= s.P.nkf + s.P.ng) return;  // keyframe blocks, then the global nodes' diagonal blocks
   double L[120];  // packed lower triangle
   const T* A = s.L.SD + 225 * k;
   int fail = 0;
@@ -730,14 +730,14 @@ template <typename T>
 __global__ void __launch_bounds__(kB) k_pcg_init(SolverLaunch<T> s) {
   if (s.ctl->terminated) return;
   const int64_t i = blockIdx.x * (int64_t)blockDim.x + threadIdx.x;
-  const int64_t n = 15 * s.P.nkf;
+  const int64_t n = 15 * (s.P.nkf + s.P.ng);  // keyframe rows, then the global nodes' rows
   const bool chain = s.precond != MBA_PRECOND_BLOCK_JACOBI && !s.ctl->chain_failed;
   double rz = 0.0, rr = 0.0;
   if (i < n) {
     const int64_t k = i / 15, a = i % 15;
     const double r = (double)s.L.rhs[i];
     double z = 0.0;
-    if (!chain) {
+    if (!chain || k >= s.P.nkf) {  // node rows: block-Jacobi also under the chain preconditioner
       const T* M = s.L.Minv + 225 * k;
       for (int b = 0; b < 15; ++b) z += (double)M[15 * a + b] * (double)s.L.rhs[15 * k + b];
       rz = r * z;
@@ -815,6 +815,15 @@ __global__ void __launch_bounds__(128) k_pcg_spmv(SolverLaunch<T> s, int it, con
 #pragma unroll
       for (int c = 0; c < 15; ++c) y += D[c] * (zk[c] + tb * pk_old[c]);
       if (lane < 6) y += red[w][lane] + red[w][lane + 6] + red[w][lane + 12] + red[w][lane + 18] + red[w][lane + 24];
+      if (lane < 6 && s.P.ng > 0) {  // keyframe-node blocks (pose rows) times the nodes' direction
+        const int64_t NK = s.P.nkf;
+        for (int64_t g = 0; g < s.P.ng; ++g) {
+          const double* Bkg = s.B.BS + 90 * (s.P.ng * k + g) + 15 * lane;
+          const T* zg = z + 15 * (NK + g);
+          const T* pg = pa + 15 * (NK + g);
+          for (int c = 0; c < 15; ++c) y += T(Bkg[c]) * (zg[c] + tb * pg[c]);
+        }
+      }
       for (int64_t e = s.S.kfe_off[k]; e < s.S.kfe_off[k + 1]; ++e) {
         const int code = s.S.kfe[e];
         const bool from = code > 0;
@@ -852,8 +861,9 @@ __global__ void __launch_bounds__(kB) k_pcg_update(SolverLaunch<T> s, int it, co
   const T alpha = T(rzprev / ctl->pcg_pq[it % 3]);
   double rr = 0.0, rz = 0.0;
   T rnew = T(0);
-  const bool act = (k < s.P.nkf) && a < 15;
-  const bool chain = s.precond != MBA_PRECOND_BLOCK_JACOBI && !ctl->chain_failed;
+  const bool act = (k < s.P.nkf + s.P.ng) && a < 15;  // keyframe rows, then the global nodes' rows
+  // the chain preconditioner covers the keyframe rows; node rows stay block-Jacobi
+  const bool chain = s.precond != MBA_PRECOND_BLOCK_JACOBI && !ctl->chain_failed && k < s.P.nkf;
   if (act) {
     const int64_t i = 15 * k + a;
     s.L.x[i] = s.L.x[i] + alpha * p[i];
@@ -894,6 +904,8 @@ __global__ void __launch_bounds__(kB) k_backsub(SolverLaunch<T> s) {
   T t[3];
 #pragma unroll
   for (int a = 0; a < 3; ++a) t[a] = -s.L.gl[a * NL + l];
+  if (s.P.ng > 0)  // W_n^T x_n of the global nodes (k_border_backsub)
+    for (int a = 0; a < 3; ++a) t[a] -= T(s.B.bl[a * NL + l]);
   for (int64_t i = s.S.lm_slot_off[l]; i < s.S.lm_slot_off[l + 1]; ++i) {
     const T* xk = s.L.x + 15 * (int64_t)s.S.slot_kf[i];
     T xv[6];
@@ -1221,6 +1233,11 @@ cudaError_t solver_assemble(const SolverLaunch<T>& s, const int* gate, cudaStrea
   if constexpr (sizeof(T) == 4)
     k_merge_pose<<<nblk(42 * s.P.nkf, kB), kB, 0, st>>>(s.P.nkf, s.L.Dpose, s.L.gpose, s.L.Dbase, s.L.gc, gate, skip);
   k_mirror_pose_blocks<T><<<nblk(15 * s.P.nkf, kB), kB, 0, st>>>(s.P.nkf, s.L.Dbase, gate, skip);
+  if constexpr (sizeof(T) == 8)
+    if (s.P.ng > 0) {
+      const cudaError_t e = border_assemble(s, gate, skip, st);
+      if (e != cudaSuccess) return e;
+    }
   return cudaGetLastError();
 }
 
@@ -1230,6 +1247,62 @@ cudaError_t solver_compute_scale(const SolverLaunch<T>& s, int jacobi, cudaStrea
   k_scale<T><<<nblk(n, kB), kB, 0, st>>>(s.P, s.L, s.sc, jacobi, nullptr);
   const int64_t m = 12 * s.P.nlm + 18 * s.S.nslot + 240 * s.P.nkf + 36 * s.S.npu + 225 * s.P.nedge + 32 * s.P.nsw;
   k_scale_inplace<T><<<gridcap(m), kB, 0, st>>>(s.P, s.S, s.L, nullptr, nullptr);
+  if constexpr (sizeof(T) == 8)
+    if (s.P.ng > 0) {
+      const cudaError_t e = border_scale(s, jacobi, nullptr, st);
+      if (e != cudaSuccess) return e;
+    }
+  return cudaGetLastError();
+}
+
+// Max |J^T r| of the current assembly (unscaled: the assembled gradients are
+// scaled by the Jacobi scale) over the variable dims: keyframes, landmarks,
+// switch variables and global nodes (whose gradient is kept unscaled).
+template <typename T>
+__global__ void __launch_bounds__(kB) k_gradient_max(SolverLaunch<T> s, const int* run_if) {
+  if (s.ctl->terminated || (run_if && !*run_if)) return;
+  const int64_t NK = s.P.nkf, NL = s.P.nlm, nk = 15 * NK, nl = 3 * NL, nn = 15 * s.P.ng;
+  double m = 0.0;
+  for (int64_t i = blockIdx.x * (int64_t)blockDim.x + threadIdx.x; i < nk + nl + s.P.nsw + nn;
+       i += (int64_t)gridDim.x * blockDim.x) {
+    double g = 0.0;
+    if (i < nk) {
+      if ((s.P.kf_mask[i / 15] >> (i % 15)) & 1) g = (double)s.L.gc[i] / s.sc.skf[i];
+    } else if (i < nk + nl) {
+      const int64_t j = i - nk, l = j % NL;
+      if (s.P.lm_active[l] && !s.P.lm_off[l]) g = (double)s.L.gl[j] / s.sc.slm[j];
+    } else if (i < nk + nl + s.P.nsw) {
+      const int64_t q = i - nk - nl;
+      g = (double)s.L.swg[q] / s.sc.ssw[q];
+    } else {
+      const int64_t j = i - nk - nl - s.P.nsw;
+      if ((s.P.g_mask[j / 15] >> (j % 15)) & 1) g = s.B.gg[j];
+    }
+    m = fmax(m, fabs(g));
+  }
+  for (int o = 16; o > 0; o >>= 1) m = fmax(m, __shfl_xor_sync(0xffffffffu, m, o));
+  if ((threadIdx.x & 31) == 0 && m > 0.0) atomicMax(&s.ctl->grad_max_bits, (unsigned long long)__double_as_longlong(m));
+}
+
+__global__ void k_gradient_reset(LmControl* ctl, const int* run_if) {
+  if (run_if && !*run_if) return;
+  ctl->grad_max_bits = 0ull;
+}
+
+__global__ void k_gradient_decide(LmControl* ctl, LmParams prm, const int* run_if) {
+  if (ctl->terminated || (run_if && !*run_if) || !prm.check_tolerances) return;
+  if (__longlong_as_double((long long)ctl->grad_max_bits) <= prm.gradient_tolerance) {
+    ctl->terminated = 1;
+    ctl->termination = 2;
+  }
+}
+
+template <typename T>
+cudaError_t solver_gradient_check(const SolverLaunch<T>& s, const int* run_if, cudaStream_t st) {
+  k_gradient_reset<<<1, 1, 0, st>>>(s.ctl, run_if);
+  const int64_t n = 15 * s.P.nkf + 3 * s.P.nlm + s.P.nsw + 15 * s.P.ng;
+  k_gradient_max<T><<<gridcap(n), kB, 0, st>>>(s, run_if);
+  k_gradient_decide<<<1, 1, 0, st>>>(s.ctl, s.prm, run_if);
   return cudaGetLastError();
 }
 
@@ -1237,6 +1310,11 @@ template <typename T>
 cudaError_t solver_build_reduced(const SolverLaunch<T>& s, cudaStream_t st) {
   const int64_t nsys = 225 * s.P.nkf + 225 * s.P.nedge + 36 * s.S.npu + 15 * s.P.nkf;
   k_build_system<T><<<gridcap(nsys), kB, 0, st>>>(s);
+  if constexpr (sizeof(T) == 8)
+    if (s.P.ng > 0) {
+      const cudaError_t e = border_build(s, st);
+      if (e != cudaSuccess) return e;
+    }
   if (s.P.nlm) k_schur_lm<T><<<nblk(s.P.nlm, kB), kB, 0, st>>>(s);
   if (s.S.nslot) k_schur_slot<T><<<nblk(s.S.nslot, kB), kB, 0, st>>>(s);
   if (s.S.nchunk) {
@@ -1245,7 +1323,13 @@ cudaError_t solver_build_reduced(const SolverLaunch<T>& s, cudaStream_t st) {
   }
   if (s.P.nsw) k_schur_switch<T><<<nblk(32 * s.P.nsw, 128), 128, 0, st>>>(s);
   k_finalize_system<T><<<gridcap(nsys), kB, 0, st>>>(s);
-  k_block_jacobi<T><<<nblk(s.P.nkf, 64), 64, 0, st>>>(s);
+  if constexpr (sizeof(T) == 8)
+    if (s.P.ng > 0) {
+      const cudaError_t e = border_schur_and_finalize(s, st);
+      if (e != cudaSuccess) return e;
+    }
+  // Block-Jacobi inverses of the keyframe blocks and of the global nodes' diagonal blocks.
+  k_block_jacobi<T><<<nblk(s.P.nkf + s.P.ng, 64), 64, 0, st>>>(s);
   if (s.precond != MBA_PRECOND_BLOCK_JACOBI) {
     cudaError_t e = cudaGetLastError();
     if (e == cudaSuccess && s.precond == MBA_PRECOND_LEARNED) e = gnn_forward<T>(s, s.gg, s.gp, s.gw, st);
@@ -1272,7 +1356,8 @@ template <typename T>
 cudaError_t solver_step(const SolverLaunch<T>& s, cudaStream_t st) {
   cudaError_t e = solver_build_reduced<T>(s, st);
   if (e != cudaSuccess) return e;
-  const int64_t n = 15 * s.P.nkf;
+  const int64_t nb = s.P.nkf + s.P.ng;  // keyframe blocks, then the global nodes
+  const int64_t n = 15 * nb;
   k_pcg_init<T><<<nblk(n, kB), kB, 0, st>>>(s);
   const bool chain = s.precond != MBA_PRECOND_BLOCK_JACOBI;
   if (chain) {
@@ -1284,27 +1369,55 @@ cudaError_t solver_step(const SolverLaunch<T>& s, cudaStream_t st) {
     T* pa = (it & 1) ? s.L.q2 : s.L.p;
     T* pb = (it & 1) ? s.L.p : s.L.q2;
     k_pcg_spmv<T><<<nblk(32 * s.P.nkf, 128), 128, 0, st>>>(s, it, pa, pb);
-    k_pcg_update<T><<<nblk(16 * s.P.nkf, kB), kB, 0, st>>>(s, it, pb, it == maxit - 1);
+    if constexpr (sizeof(T) == 8)
+      if (s.P.ng > 0) {
+        e = border_spmv(s, it, pa, pb, st);
+        if (e != cudaSuccess) return e;
+      }
+    k_pcg_update<T><<<nblk(16 * nb, kB), kB, 0, st>>>(s, it, pb, it == maxit - 1);
     if (chain) {
       e = chain_apply<T>(s, s.L.r, s.L.z, &s.ctl->pcg_rz[it % 3], st);
       if (e != cudaSuccess) return e;
     }
   }
+  if constexpr (sizeof(T) == 8)
+    if (s.P.ng > 0) {
+      e = border_backsub(s, st);
+      if (e != cudaSuccess) return e;
+    }
   if (s.P.nlm) k_backsub<T><<<nblk(s.P.nlm, kB), kB, 0, st>>>(s);
   if (s.P.nsw) k_backsub_switch<T><<<nblk(s.P.nsw, kB), kB, 0, st>>>(s);
-  if (s.P.nobs) k_model_visual<T><<<nblk(s.P.nobs, kB), kB, 0, st>>>(s);
+  bool model_done = false;
+  if constexpr (sizeof(T) == 8)
+    if (s.P.ng > 0) {
+      e = border_model_visual(s, st);
+      if (e != cudaSuccess) return e;
+      model_done = true;
+    }
+  if (s.P.nobs && !model_done) k_model_visual<T><<<nblk(s.P.nobs, kB), kB, 0, st>>>(s);
   if (s.P.nedge) k_model_inertial<T><<<nblk(32 * s.P.nedge, 128), 128, 0, st>>>(s);
   k_retract<T><<<nblk(s.P.nkf + s.P.nlm + s.P.nsw, kB), kB, 0, st>>>(s);
+  if constexpr (sizeof(T) == 8)
+    if (s.P.ng > 0) {
+      e = border_retract(s, st);
+      if (e != cudaSuccess) return e;
+    }
   return cudaGetLastError();
 }
 
 template <typename T>
 cudaError_t solver_evaluate_candidate(const SolverLaunch<T>& s, InertialLin<double> ine_cand, cudaStream_t st) {
+  // Global nodes: the candidate cameras and baseframes.
+  DevProblem Pc = s.P;
+  if (s.P.ng > 0) {
+    Pc.cams = s.B.cams_cand;
+    Pc.mis = s.B.mis_cand;
+  }
   // Mixed path: FP32 residuals from FP32 copies of the candidate, FP64 sum.
   cudaError_t e = (sizeof(T) == 4 && s.kf_cand_f)
                       ? launch_visual_cost_f32(s.P, s.kf_cand_f, s.lm_cand_f, &s.ctl->cost_cand, &s.ctl->nonfinite,
                                                &s.ctl->terminated, st)
-                      : launch_visual_cost_gated(s.P, s.kf_cand, s.lm_cand, &s.ctl->cost_cand, &s.ctl->nonfinite,
+                      : launch_visual_cost_gated(Pc, s.kf_cand, s.lm_cand, &s.ctl->cost_cand, &s.ctl->nonfinite,
                                                  &s.ctl->terminated, st);
   if (e != cudaSuccess) return e;
   // Mixed path: Phi / Q propagated in FP32 (state, Cholesky, residual FP64).
@@ -1318,6 +1431,11 @@ cudaError_t solver_decide_and_accept(const SolverLaunch<T>& s, InertialLin<doubl
   k_decide<<<1, 1, 0, st>>>(s.ctl, s.prm, s.log);
   const int64_t total = 16 * s.P.nkf + 4 * s.P.nlm + 465 * s.P.nedge + s.P.nsw + 6 * (s.P.nedge - s.P.nimu);
   k_accept<T><<<gridcap(total), kB, 0, st>>>(s, ine_cand, ine_cur);
+  if constexpr (sizeof(T) == 8)
+    if (s.P.ng > 0) {
+      const cudaError_t e = border_accept(s, st);
+      if (e != cudaSuccess) return e;
+    }
   return cudaGetLastError();
 }
 
@@ -1326,7 +1444,10 @@ cudaError_t solver_relinearize(const SolverLaunch<T>& s, const InertialLin<doubl
   (void)ine_cur;
   cudaError_t e = launch_visual_linearize_gated<T>(s.P, s.vis, nullptr, &s.ctl->accepted, &s.ctl->terminated, st);
   if (e != cudaSuccess) return e;
-  return solver_assemble<T>(s, &s.ctl->accepted, st);
+  e = solver_assemble<T>(s, &s.ctl->accepted, st);
+  if (e != cudaSuccess) return e;
+  // Ceres' gradient test after an accepted step.
+  return solver_gradient_check<T>(s, &s.ctl->accepted, st);
 }
 
 // Outlier rejection + restart, run when ctl->restart_now (set by k_decide).
@@ -1378,6 +1499,12 @@ cudaError_t solver_reject_and_restart(const SolverLaunch<T>& s, int use_reprojec
   k_scale<T><<<nblk(n, kB), kB, 0, st>>>(s.P, s.L, s.sc, jacobi, run);
   const int64_t m = 12 * s.P.nlm + 18 * s.S.nslot + 240 * s.P.nkf + 36 * s.S.npu + 225 * s.P.nedge + 32 * s.P.nsw;
   k_scale_inplace<T><<<gridcap(m), kB, 0, st>>>(s.P, s.S, s.L, run, nullptr);
+  if constexpr (sizeof(T) == 8)
+    if (s.P.ng > 0) {
+      e = border_assemble(s, run, nullptr, st);
+      if (e == cudaSuccess) e = border_scale(s, jacobi, run, st);
+      if (e != cudaSuccess) return e;
+    }
   return cudaGetLastError();
 }
 
@@ -1429,5 +1556,7 @@ template cudaError_t solver_relinearize<double>(const SolverLaunch<double>&, con
 template cudaError_t solver_relinearize<float>(const SolverLaunch<float>&, const InertialLin<double>&, cudaStream_t);
 template cudaError_t solver_reject_and_restart<double>(const SolverLaunch<double>&, int, double, int, cudaStream_t);
 template cudaError_t solver_reject_and_restart<float>(const SolverLaunch<float>&, int, double, int, cudaStream_t);
+template cudaError_t solver_gradient_check<double>(const SolverLaunch<double>&, const int*, cudaStream_t);
+template cudaError_t solver_gradient_check<float>(const SolverLaunch<float>&, const int*, cudaStream_t);
 
 }  // namespace mba

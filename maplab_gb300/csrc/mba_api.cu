@@ -188,6 +188,8 @@ struct mba_handle {
   // (MBA_ERR_TIMEOUT): the work that wait guarded may still be in flight, so
   // later solves and training calls on this handle are refused.
   bool poisoned = false;
+  // Global nodes (calibration / baseframe variables) of the reduced system.
+  BorderSystem border{};
 };
 
 namespace {
@@ -275,6 +277,7 @@ mba_status ensure_solver_buffers(mba_handle* h, SolverBuffers<T>& b) {
   const DevProblem& P = h->P;
   DeviceArena& A = h->arena;
   const int64_t N = P.nobs, NL = P.nlm, NK = P.nkf, NE = P.nedge, NS = h->S.nslot, NPU = h->S.npu;
+  const int64_t NB = NK + P.ng;  // PCG blocks: keyframes, then the global nodes
   b.vis.r = A.alloc<T>(2 * N);
   b.vis.Jl = A.alloc<T>(6 * N);
   b.vis.Js = A.alloc<T>(12 * N);
@@ -293,21 +296,21 @@ mba_status ensure_solver_buffers(mba_handle* h, SolverBuffers<T>& b) {
   L.Pbase = A.alloc<T>(36 * NPU);
   L.Ebase = A.alloc<T>(225 * NE);
   L.gc = A.alloc<T>(15 * NK);
-  L.SD = A.alloc<T>(225 * NK);
+  L.SD = A.alloc<T>(225 * NB);
   L.SP = A.alloc<T>(72 * NPU);
   L.SE = A.alloc<T>(225 * NE);
-  L.rhs = A.alloc<T>(15 * NK);
+  L.rhs = A.alloc<T>(15 * NB);
   L.V = A.alloc<T>(9 * NL);
   L.U = A.alloc<T>(kSlotStride * NS);
-  L.Minv = A.alloc<T>(225 * NK);
-  L.x = A.alloc<T>(15 * NK);
-  L.r = A.alloc<T>(15 * NK);
-  L.z = A.alloc<T>(15 * NK);
-  L.p = A.alloc<T>(15 * NK);
-  L.q = A.alloc<T>(15 * NK);
-  L.q2 = A.alloc<T>(15 * NK);
+  L.Minv = A.alloc<T>(225 * NB);
+  L.x = A.alloc<T>(15 * NB);
+  L.r = A.alloc<T>(15 * NB);
+  L.z = A.alloc<T>(15 * NB);
+  L.p = A.alloc<T>(15 * NB);
+  L.q = A.alloc<T>(15 * NB);
+  L.q2 = A.alloc<T>(15 * NB);
   L.dl = A.alloc<double>(3 * NL);
-  L.skf = A.alloc<T>(15 * NK);
+  L.skf = A.alloc<T>(15 * NB);
   L.slm = A.alloc<T>(3 * NL);
   L.Dpose = A.alloc<float>(sizeof(T) == 4 ? 36 * NK : 1);
   L.gpose = A.alloc<float>(sizeof(T) == 4 ? 8 * NK : 1);
@@ -396,7 +399,19 @@ mba_status ensure_common_solver(mba_handle* h, int capacity) {
     h->ine_cand.Jt = A.alloc<double>(225 * NE);
     h->ine_cur.Js = A.alloc<double>(6 * (NE - P.nimu));
     h->ine_cand.Js = A.alloc<double>(6 * (NE - P.nimu));
-    h->sc.skf = A.alloc<double>(15 * P.nkf);
+    h->sc.skf = A.alloc<double>(15 * (P.nkf + P.ng));
+    if (P.ng > 0) {
+      BorderSystem& B = h->border;
+      const int64_t G = P.ng;
+      B.Gb = A.alloc<double>(225 * G * G);
+      B.Bb = A.alloc<double>(90 * P.nkf * G);
+      B.gg = A.alloc<double>(15 * G);
+      B.GS = A.alloc<double>(225 * G * G);
+      B.BS = A.alloc<double>(90 * P.nkf * G);
+      B.bl = A.alloc<double>(3 * P.nlm);
+      B.cams_cand = A.alloc<DevCamera>(P.ncam);
+      B.mis_cand = A.alloc<double>(8 * P.nmis);
+    }
     h->sc.slm = A.alloc<double>(3 * P.nlm);
     h->sc.ssw = A.alloc<double>(P.nsw);
     h->sw_cand = A.alloc<double>(P.nsw);
@@ -450,6 +465,7 @@ SolverLaunch<T> make_launch(mba_handle* h, SolverBuffers<T>& b, const mba_solver
   s.prm.max_lm_diagonal = o.max_lm_diagonal;
   s.prm.linear_tolerance = o.linear_tolerance;
   s.prm.stop_cost = o.stop_cost;
+  s.prm.gradient_tolerance = o.gradient_tolerance;
   s.log = h->log;
   s.kf_cand = h->kf_cand;
   s.lm_cand = h->lm_cand;
@@ -463,6 +479,7 @@ SolverLaunch<T> make_launch(mba_handle* h, SolverBuffers<T>& b, const mba_solver
   s.gg = h->gg;
   s.gw = h->gw;
   if (h->model) s.gp = h->model->p;
+  s.B = h->border;
   return s;
 }
 
@@ -591,7 +608,14 @@ mba_status run_solve(mba_handle* h, const mba_solver_options& o, mba_summary* su
   // Initial evaluation: FP64 cost, inertial linearization, visual linearization, assembly, scaling.
   e = solver_init_control(h->ctl, o.initial_trust_region_radius, st);
   if (e == cudaSuccess) e = solver_loop_start(h->ctl, st);
+  if (e == cudaSuccess && h->P.ng > 0) {  // candidate cameras / baseframes start as the current ones
+    e = cudaMemcpyAsync(h->border.cams_cand, h->P.cams, sizeof(DevCamera) * h->P.ncam, cudaMemcpyDeviceToDevice, st);
+    if (e == cudaSuccess)
+      e = cudaMemcpyAsync(h->border.mis_cand, h->P.mis, sizeof(double) * 8 * h->P.nmis, cudaMemcpyDeviceToDevice, st);
+  }
   if (e == cudaSuccess) e = linearize_current<T>(h, b, s, o.jacobi_scaling, st);
+  // Ceres' gradient test at the start of the solve.
+  if (e == cudaSuccess) e = solver_gradient_check<T>(s, nullptr, st);
   double initial_cost = 0.0;
   int flags[2] = {0, 0};
   if (e == cudaSuccess) e = cudaMemcpyAsync(&initial_cost, &h->ctl->cost, sizeof(double), cudaMemcpyDeviceToHost, st);
@@ -872,7 +896,12 @@ mba_status mba_create(const mba_problem_desc* d, int32_t device, mba_handle** ou
   for (int64_t c = 0; c < NC; ++c) {
     const mba_camera& cam = d->cameras[c];
     if (!quat_ok(cam.q_CI_p_CI)) return MBA_ERR_INVALID_ARG;
-    if (cam.distortion_type < 0 || cam.distortion_type > 2) return MBA_ERR_INVALID_ARG;
+    if (cam.distortion_type < MBA_DISTORTION_NONE || cam.distortion_type > MBA_DISTORTION_FOV) return MBA_ERR_INVALID_ARG;
+    if (d->camera_flags && (d->camera_flags[c] & ~0xfu)) return MBA_ERR_INVALID_ARG;
+  }
+  for (int64_t m = 0; m < NM && d->mission_flags; ++m) {
+    const uint32_t f = d->mission_flags[m];
+    if (f != 0 && f != MBA_MIS_BASEFRAME_YAW_POSITION && f != MBA_MIS_BASEFRAME_POSE) return MBA_ERR_INVALID_ARG;
   }
   for (int64_t l = 0; l < NL; ++l) {
     if (d->lm_store_keyframe[l] < 0 || d->lm_store_keyframe[l] >= NK) return MBA_ERR_OUT_OF_RANGE_INDEX;
@@ -1261,6 +1290,45 @@ mba_status mba_create(const mba_problem_desc* d, int32_t device, mba_handle** ou
     imu.assign(d->imu_acc_gyro, d->imu_acc_gyro + 6 * NSMP);
   }
   kfm.assign(d->kf_mission, d->kf_mission + NK);
+  // ---- global nodes: cameras with a free calibration block, missions with a
+  // free baseframe (15-dim blocks after the keyframes; active dims as bits).
+  std::vector<int32_t> cam_node(NC, -1), mis_node(NM, -1), node_cam, node_mis;
+  std::vector<uint16_t> g_mask;
+  std::vector<uint32_t> mflags(NM, 0u);
+  for (int64_t c = 0; c < NC; ++c) {
+    const uint32_t f = d->camera_flags ? d->camera_flags[c] : 0u;
+    if (!f) continue;
+    const int dt = d->cameras[c].distortion_type;
+    const int nd = (dt == MBA_DISTORTION_RADTAN || dt == MBA_DISTORTION_EQUIDISTANT) ? 4 : (dt == MBA_DISTORTION_FOV ? 1 : 0);
+    uint32_t m = 0;
+    if (f & MBA_CAM_INTRINSICS_FREE) m |= 0xfu;
+    if (f & MBA_CAM_DISTORTION_FREE) m |= ((1u << nd) - 1u) << 4;
+    if (f & MBA_CAM_ROTATION_FREE) m |= 7u << 8;
+    if (f & MBA_CAM_TRANSLATION_FREE) m |= 7u << 11;
+    cam_node[c] = (int32_t)node_cam.size();
+    node_cam.push_back((int32_t)c);
+    node_mis.push_back(-1);
+    g_mask.push_back((uint16_t)m);
+  }
+  for (int64_t m = 0; m < NM; ++m) {
+    const uint32_t f = d->mission_flags ? d->mission_flags[m] : 0u;
+    mflags[m] = f;
+    if (!f) continue;
+    mis_node[m] = (int32_t)node_cam.size();
+    node_cam.push_back(-1);
+    node_mis.push_back((int32_t)m);
+    g_mask.push_back((uint16_t)(f == MBA_MIS_BASEFRAME_POSE ? 0x3fu : 0x39u));
+  }
+  // A free baseframe enters the visual terms only: absolute 6-DoF terms and
+  // cross-mission loop closures need their baseframes constant.
+  for (int64_t j = 0; j < NPE; ++j) {
+    const int mf = d->kf_mission[e_from[NIMU + j]], mt = d->kf_mission[e_to[NIMU + j]];
+    const bool uses_bf = pe_type[j] == MBA_POSE_EDGE_ABSOLUTE || (pe_type[j] == MBA_POSE_EDGE_LOOP_CLOSURE && mf != mt);
+    if (uses_bf && (mis_node[mf] >= 0 || mis_node[mt] >= 0)) {
+      mba_destroy(h);
+      return MBA_ERR_INVALID_ARG;
+    }
+  }
 
   // ---- upload
   DeviceArena& A = h->arena;
@@ -1286,6 +1354,15 @@ mba_status mba_create(const mba_problem_desc* d, int32_t device, mba_handle** ou
   P.kf_mask = A.upload(mask, st);
   P.mis = A.upload(mis, st);
   P.cams = A.upload(cams, st);
+  P.ng = (int64_t)node_cam.size();
+  if (P.ng > 0) {
+    P.cam_node = A.upload(cam_node, st);
+    P.mis_node = A.upload(mis_node, st);
+    P.node_cam = A.upload(node_cam, st);
+    P.node_mis = A.upload(node_mis, st);
+    P.g_mask = A.upload(g_mask, st);
+    P.mis_flags = A.upload(mflags, st);
+  }
   P.e_from = A.upload(e_from, st);
   P.e_to = A.upload(e_to, st);
   P.e_off = A.upload(e_off, st);
@@ -1681,6 +1758,9 @@ mba_status mba_solve(mba_handle* h, const mba_solver_options* opts, mba_summary*
   if (opts) o = *opts; else mba_default_solver_options(&o);
   if (o.max_num_iterations < 0 || !(o.initial_trust_region_radius > 0)) return MBA_ERR_INVALID_ARG;
   if (h->poisoned) return MBA_ERR_TIMEOUT;
+  // Calibration / baseframe variables: FP64 solves with block-Jacobi or chain preconditioning.
+  if (h->P.ng > 0 && (o.precision != MBA_PRECISION_FP64 || o.preconditioner == MBA_PRECOND_LEARNED))
+    return MBA_ERR_INVALID_ARG;
   cudaSetDevice(h->device);
   h->cancel.store(0);
   if (o.max_num_iterations == 0) {
@@ -1690,7 +1770,16 @@ mba_status mba_solve(mba_handle* h, const mba_solver_options* opts, mba_summary*
     return st;
   }
   if (o.precision == MBA_PRECISION_MIXED) return run_solve<float>(h, o, summary);
-  return run_solve<double>(h, o, summary);
+  const mba_status st = run_solve<double>(h, o, summary);
+  if (h->P.ng > 0 && (st == MBA_OK || st == MBA_ERR_CANCELLED)) {
+    // The solve moved cameras / baseframes on the device: refresh their FP32 mirrors.
+    std::vector<mba_camera> cams(h->P.ncam);
+    std::vector<double> mis(7 * h->P.nmis);
+    mba_status r = mba_read_calibration(h, cams.data(), mis.data());
+    if (r == MBA_OK) r = mba_write_calibration(h, cams.data(), mis.data());
+    if (r != MBA_OK) return r;
+  }
+  return st;
 }
 
 mba_status mba_read_state(mba_handle* h, double* kx, double* kv, double* kbg, double* kba, double* lp) {
@@ -1739,6 +1828,84 @@ mba_status mba_write_state(mba_handle* h, const double* kx, const double* kv, co
   if (e == cudaSuccess)
     e = launch_pack_state(h->P, kx ? sx : nullptr, kv ? sv : nullptr, kbg ? sg : nullptr, kba ? sa : nullptr,
                           (lp && NL) ? sl : nullptr, 1, st);
+  if (e == cudaSuccess) e = cudaStreamSynchronize(st);
+  return cuda_status(e);
+}
+
+mba_status mba_read_calibration(mba_handle* h, mba_camera* cameras, double* mission_q_GM_p_GM) {
+  if (!h) return MBA_ERR_INVALID_ARG;
+  cudaSetDevice(h->device);
+  const int64_t NC = h->P.ncam, NM = h->P.nmis;
+  std::vector<DevCamera> dc(NC);
+  std::vector<double> dm(8 * NM);
+  cudaStream_t st = h->stream;
+  cudaError_t e = cudaMemcpyAsync(dc.data(), h->P.cams, sizeof(DevCamera) * NC, cudaMemcpyDeviceToHost, st);
+  if (e == cudaSuccess) e = cudaMemcpyAsync(dm.data(), h->P.mis, sizeof(double) * 8 * NM, cudaMemcpyDeviceToHost, st);
+  if (e == cudaSuccess) e = cudaStreamSynchronize(st);
+  if (e != cudaSuccess) return MBA_ERR_CUDA;
+  for (int64_t c = 0; c < NC && cameras; ++c) {
+    mba_camera& o = cameras[c];
+    std::memset(&o, 0, sizeof(o));
+    for (int a = 0; a < 4; ++a) { o.intrinsics[a] = dc[c].intr[a]; o.distortion[a] = dc[c].dist[a]; o.q_CI_p_CI[a] = dc[c].q_CI[a]; }
+    for (int a = 0; a < 3; ++a) o.q_CI_p_CI[4 + a] = dc[c].p_CI[a];
+    o.distortion_type = dc[c].dtype;
+    o.width = dc[c].width;
+    o.height = dc[c].height;
+  }
+  for (int64_t m = 0; m < NM && mission_q_GM_p_GM; ++m)
+    for (int a = 0; a < 7; ++a) mission_q_GM_p_GM[7 * m + a] = dm[8 * m + a];
+  return MBA_OK;
+}
+
+mba_status mba_write_calibration(mba_handle* h, const mba_camera* cameras, const double* mission_q_GM_p_GM) {
+  if (!h) return MBA_ERR_INVALID_ARG;
+  cudaSetDevice(h->device);
+  const int64_t NC = h->P.ncam, NM = h->P.nmis;
+  std::vector<DevCamera> dc(NC);
+  std::vector<double> dm(8 * NM);
+  cudaStream_t st = h->stream;
+  cudaError_t e = cudaMemcpyAsync(dc.data(), h->P.cams, sizeof(DevCamera) * NC, cudaMemcpyDeviceToHost, st);
+  if (e == cudaSuccess) e = cudaMemcpyAsync(dm.data(), h->P.mis, sizeof(double) * 8 * NM, cudaMemcpyDeviceToHost, st);
+  if (e == cudaSuccess) e = cudaStreamSynchronize(st);
+  if (e != cudaSuccess) return MBA_ERR_CUDA;
+  for (int64_t c = 0; c < NC && cameras; ++c) {
+    const mba_camera& s = cameras[c];
+    if (!quat_ok(s.q_CI_p_CI)) return MBA_ERR_INVALID_ARG;
+    if (s.distortion_type != dc[c].dtype || s.width != dc[c].width || s.height != dc[c].height) return MBA_ERR_INVALID_ARG;
+    for (int a = 0; a < 4; ++a)
+      if (!std::isfinite(s.intrinsics[a]) || !std::isfinite(s.distortion[a])) return MBA_ERR_NON_FINITE;
+    for (int a = 0; a < 7; ++a) if (!std::isfinite(s.q_CI_p_CI[a])) return MBA_ERR_NON_FINITE;
+    for (int a = 0; a < 4; ++a) { dc[c].intr[a] = s.intrinsics[a]; dc[c].dist[a] = s.distortion[a]; dc[c].q_CI[a] = s.q_CI_p_CI[a]; }
+    for (int a = 0; a < 3; ++a) dc[c].p_CI[a] = s.q_CI_p_CI[4 + a];
+  }
+  for (int64_t m = 0; m < NM && mission_q_GM_p_GM; ++m) {
+    if (!quat_ok(mission_q_GM_p_GM + 7 * m)) return MBA_ERR_INVALID_ARG;
+    for (int a = 0; a < 7; ++a) {
+      if (!std::isfinite(mission_q_GM_p_GM[7 * m + a])) return MBA_ERR_NON_FINITE;
+      dm[8 * m + a] = mission_q_GM_p_GM[7 * m + a];
+    }
+  }
+  // FP32 mirrors of the mixed path
+  std::vector<DevCameraT<float>> fc(NC);
+  std::vector<float> fm(8 * NM, 0.f);
+  for (int64_t c = 0; c < NC; ++c) {
+    DevCameraT<float>& o = fc[c];
+    std::memset(&o, 0, sizeof(o));
+    for (int a = 0; a < 4; ++a) { o.intr[a] = (float)dc[c].intr[a]; o.dist[a] = (float)dc[c].dist[a]; o.q_CI[a] = (float)dc[c].q_CI[a]; }
+    for (int a = 0; a < 3; ++a) o.p_CI[a] = (float)dc[c].p_CI[a];
+    o.dtype = dc[c].dtype;
+    o.width = dc[c].width;
+    o.height = dc[c].height;
+  }
+  for (int64_t m = 0; m < 8 * NM; ++m) fm[m] = (float)dm[m];
+  e = cudaMemcpyAsync(const_cast<DevCamera*>(h->P.cams), dc.data(), sizeof(DevCamera) * NC, cudaMemcpyHostToDevice, st);
+  if (e == cudaSuccess)
+    e = cudaMemcpyAsync(const_cast<double*>(h->P.mis), dm.data(), sizeof(double) * 8 * NM, cudaMemcpyHostToDevice, st);
+  if (e == cudaSuccess && h->P.cams_f)
+    e = cudaMemcpyAsync(const_cast<DevCameraT<float>*>(h->P.cams_f), fc.data(), sizeof(DevCameraT<float>) * NC,
+                        cudaMemcpyHostToDevice, st);
+  if (e == cudaSuccess && h->P.mis_f)
+    e = cudaMemcpyAsync(const_cast<float*>(h->P.mis_f), fm.data(), sizeof(float) * 8 * NM, cudaMemcpyHostToDevice, st);
   if (e == cudaSuccess) e = cudaStreamSynchronize(st);
   return cuda_status(e);
 }

@@ -90,6 +90,7 @@ struct LmControl {
   int32_t restart_now;     // set by the LM decision: outlier rejection + restart after this iteration
   int32_t loop_active;     // device-driven LM loop: 1 while another iteration follows
   int32_t fatal;           // a bounded device wait ran out (tensor-core pipeline): the solve fails with MBA_ERR_TIMEOUT
+  unsigned long long grad_max_bits;  // max |J^T r| over the variable dims (bits of a non-negative double)
   unsigned long long t0_ns;  // device global timer at the start of the solve
 };
 
@@ -103,6 +104,7 @@ struct LmParams {
   double min_lm_diagonal, max_lm_diagonal;
   double linear_tolerance;
   double stop_cost;
+  double gradient_tolerance;  // with check_tolerances: stop once max |J^T r| <= it
 };
 
 template <typename T>
@@ -161,9 +163,23 @@ struct ChainSystem {
 };
 
 struct ScaleVectors {
-  double* skf;  // [nkf*15]
+  double* skf;  // [(nkf + ng)*15]: keyframe dims, then the global nodes' dims
   double* slm;  // [3][nlm]
   double* ssw;  // [nsw]
+};
+
+// Reduced-system blocks of the global nodes (calibration / baseframe
+// variables; FP64 solves only).  Node g is block nkf + g of the PCG vectors
+// and of SD / Minv; its couplings are stored dense.
+struct BorderSystem {
+  double* Gb;            // [ng][ng][225] node-node J^T J (unscaled, both orientations)
+  double* Bb;            // [nkf][ng][90] keyframe pose rows (6) x node dims (15), J^T J (unscaled)
+  double* gg;            // [ng][15] node gradient J^T r (unscaled)
+  double* GS;            // [ng][ng][225] scaled, damped, landmark-reduced node blocks
+  double* BS;            // [nkf][ng][90] scaled, landmark-reduced keyframe-node blocks
+  double* bl;            // [3][nlm] W_n^T x_n per landmark (back substitution)
+  DevCamera* cams_cand;  // [ncam] candidate cameras (retraction)
+  double* mis_cand;      // [nmis][8] candidate baseframes
 };
 
 template <typename T>
@@ -187,6 +203,7 @@ struct SolverLaunch {
   GnnGraph gg{};               // learned preconditioner (precond == MBA_PRECOND_LEARNED)
   GnnParams gp{};
   GnnWork gw{};
+  BorderSystem B{};            // global nodes (P.ng > 0, FP64 only)
 };
 
 // kernels_solver.cu
@@ -229,6 +246,32 @@ cudaError_t solver_reject_and_restart(const SolverLaunch<T>& s, int use_reprojec
 cudaError_t solver_loop_start(LmControl* ctl, cudaStream_t st);
 cudaError_t solver_loop_control(LmControl* ctl, cudaGraphConditionalHandle handle, const volatile int* cancel,
                                 cudaStream_t st);
+
+// Max |J^T r| over the variable dims (after an assembly) into ctl->grad_max_bits;
+// with check_tolerances, a value at or below gradient_tolerance ends the solve
+// (termination 2) when `run_if` is set (NULL: always).
+template <typename T>
+cudaError_t solver_gradient_check(const SolverLaunch<T>& s, const int* run_if, cudaStream_t st);
+
+// kernels_border.cu: the global nodes (calibration / baseframe variables) of
+// FP64 solves.  border_assemble zeroes and re-assembles the direct node
+// terms of the current linearization; border_scale sets the nodes' Jacobi
+// scale (first linearization); border_build / border_schur_and_finalize
+// form the node blocks of the reduced system around the landmark
+// elimination; border_spmv is the node rows' PCG product (after
+// k_pcg_spmv); border_backsub the node part of the landmark back
+// substitution; border_model_visual the visual model cost change with the
+// node columns; border_retract / border_accept move the candidate cameras and
+// baseframes.
+cudaError_t border_assemble(const SolverLaunch<double>& s, const int* run_if, const int* skip_if, cudaStream_t st);
+cudaError_t border_scale(const SolverLaunch<double>& s, int jacobi, const int* run_if, cudaStream_t st);
+cudaError_t border_build(const SolverLaunch<double>& s, cudaStream_t st);
+cudaError_t border_schur_and_finalize(const SolverLaunch<double>& s, cudaStream_t st);
+cudaError_t border_spmv(const SolverLaunch<double>& s, int it, const double* pa, double* pb, cudaStream_t st);
+cudaError_t border_backsub(const SolverLaunch<double>& s, cudaStream_t st);
+cudaError_t border_model_visual(const SolverLaunch<double>& s, cudaStream_t st);
+cudaError_t border_retract(const SolverLaunch<double>& s, cudaStream_t st);
+cudaError_t border_accept(const SolverLaunch<double>& s, cudaStream_t st);
 
 // kernels_chain.cu: factorization of the chain matrix (after the reduced
 // system is built) and z = T^-1 r with the r.z dot added to *rz.

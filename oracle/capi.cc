@@ -23,6 +23,7 @@ namespace oracle {
 int oracleLinearizeVisual(Problem* p, double* r, double* Jl, double* Js, double* Jo, double* cost);
 int oracleLinearizePoseEdges(Problem* p, double* r, double* Jf, double* Jt);
 int oracleReadState(Problem* p, double* kx, double* kv, double* kbg, double* kba, double* lp);
+int oracleReadCalibration(Problem* p, mba_camera* cams, double* mis);
 int oracleReadSwitches(Problem* p, double* s);
 int oracleLandmarkQuality(Problem* p, const mba_landmark_quality_options* o, uint8_t* good);
 int oracleWriteState(Problem* p, const double* kx, const double* kv, const double* kbg, const double* kba, const double* lp);
@@ -95,6 +96,9 @@ int oracle_absolute_pose(const double* bf, const double* x, const double* ext, c
 }
 int oracle_read_state(void* h, double* kx, double* kv, double* kbg, double* kba, double* lp) {
   return oracle::oracleReadState((oracle::Problem*)h, kx, kv, kbg, kba, lp);
+}
+int oracle_read_calibration(void* h, mba_camera* cams, double* mis) {
+  return oracle::oracleReadCalibration((oracle::Problem*)h, cams, mis);
 }
 int oracle_write_state(void* h, const double* kx, const double* kv, const double* kbg, const double* kba,
                        const double* lp) {

@@ -68,7 +68,23 @@ struct Problem {
   std::vector<uint8_t> kf_mask;  // 15 per keyframe, 1 = active tangent dim
   std::vector<uint8_t> lm_mask;  // 1 = active landmark
   std::vector<uint8_t> lm_off;   // 1 = rejected outlier: its terms are out of the problem
+  // Calibration / baseframe variables ("global nodes"): one 15-dim block per
+  // camera with a free calibration block and per mission with a free
+  // baseframe, after the keyframes in the reduced system (node g is block
+  // nkf + g).  Camera node dims: intrinsics 0-3, distortion 4-7 (the model's
+  // parameter count), theta_C_I 8-10, p_C_I 11-13.  Mission node dims:
+  // theta 0-2 (yaw only: 0), p_G_M 3-5.
+  int64_t ng = 0;
+  std::vector<uint32_t> cam_flags, mis_flags;
+  std::vector<int32_t> cam_node, mis_node;   // -1: constant
+  std::vector<int32_t> node_cam, node_mis;   // node -> camera / mission (-1)
+  std::vector<uint8_t> g_mask;               // 15 per node
 };
+
+// Distortion parameters per model (aslam): radtan 4, equidistant 4, FOV 1.
+static int distortionParams(int type) {
+  return type == MBA_DISTORTION_RADTAN || type == MBA_DISTORTION_EQUIDISTANT ? 4 : (type == MBA_DISTORTION_FOV ? 1 : 0);
+}
 
 int createProblem(const mba_problem_desc* d, Problem** out) {
   if (!d || !out) return MBA_ERR_INVALID_ARG;
@@ -191,6 +207,47 @@ int createProblem(const mba_problem_desc* d, Problem** out) {
   p->lm_mask.assign(p->nlm, 1);
   p->lm_off.assign(p->nlm, 0);
   for (int64_t l = 0; l < p->nlm; ++l) if (p->lm_const[l] || p->lm_obs_off[l + 1] == p->lm_obs_off[l]) p->lm_mask[l] = 0;
+  // Calibration / baseframe variables.
+  p->cam_flags.assign(p->ncam, 0u);
+  if (d->camera_flags) p->cam_flags.assign(d->camera_flags, d->camera_flags + p->ncam);
+  p->mis_flags.assign(p->nmis, 0u);
+  if (d->mission_flags) p->mis_flags.assign(d->mission_flags, d->mission_flags + p->nmis);
+  p->cam_node.assign(p->ncam, -1);
+  p->mis_node.assign(p->nmis, -1);
+  for (int64_t c = 0; c < p->ncam; ++c) {
+    const uint32_t f = p->cam_flags[c];
+    if (!(f & 0xfu)) continue;
+    std::vector<uint8_t> m(15, 0);
+    if (f & MBA_CAM_INTRINSICS_FREE) for (int a = 0; a < 4; ++a) m[a] = 1;
+    if (f & MBA_CAM_DISTORTION_FREE) for (int a = 0; a < distortionParams(p->cams[c].distortion_type); ++a) m[4 + a] = 1;
+    if (f & MBA_CAM_ROTATION_FREE) for (int a = 8; a < 11; ++a) m[a] = 1;
+    if (f & MBA_CAM_TRANSLATION_FREE) for (int a = 11; a < 14; ++a) m[a] = 1;
+    p->cam_node[c] = (int32_t)p->ng++;
+    p->node_cam.push_back((int32_t)c);
+    p->node_mis.push_back(-1);
+    p->g_mask.insert(p->g_mask.end(), m.begin(), m.end());
+  }
+  for (int64_t mi = 0; mi < p->nmis; ++mi) {
+    const uint32_t f = p->mis_flags[mi];
+    if (!f) continue;
+    if (f != MBA_MIS_BASEFRAME_YAW_POSITION && f != MBA_MIS_BASEFRAME_POSE) { delete p; return MBA_ERR_INVALID_ARG; }
+    std::vector<uint8_t> m(15, 0);
+    m[0] = 1;
+    if (f == MBA_MIS_BASEFRAME_POSE) m[1] = m[2] = 1;
+    m[3] = m[4] = m[5] = 1;
+    p->mis_node[mi] = (int32_t)p->ng++;
+    p->node_cam.push_back(-1);
+    p->node_mis.push_back((int32_t)mi);
+    p->g_mask.insert(p->g_mask.end(), m.begin(), m.end());
+  }
+  // A free baseframe enters the visual terms only: absolute 6-DoF terms and
+  // cross-mission loop closures keep their baseframes constant.
+  for (int64_t e = p->nimu; e < p->nedge; ++e) {
+    const int type = p->pe_type[e - p->nimu];
+    const int mf = p->kf_mis[p->e_from[e]], mt = p->kf_mis[p->e_to[e]];
+    const bool uses_bf = type == MBA_POSE_EDGE_ABSOLUTE || (type == MBA_POSE_EDGE_LOOP_CLOSURE && mf != mt);
+    if (uses_bf && (p->mis_node[mf] >= 0 || p->mis_node[mt] >= 0)) { delete p; return MBA_ERR_INVALID_ARG; }
+  }
   p->threads = std::max(1u, std::thread::hardware_concurrency());
   *out = p;
   return MBA_OK;
@@ -285,8 +342,76 @@ struct Linearization {
   std::vector<double> vr, vJl, vJs, vJo;  // visual: 2, 2x3, 2x6, 2x6 per obs
   std::vector<double> ir, iJf, iJt;       // inertial: 15, 15x15, 15x15 per edge
   std::vector<double> sJ;                 // pose edges: d residual / d switch [6] (= unswitched residual)
+  // Global nodes (only when the problem has some): per observation up to 3
+  // node ids (camera; the landmark's and the observer's mission baseframes
+  // of a kGlobal term; -1 = none) and their 2 x 15 tangent Jacobians.
+  std::vector<int32_t> vGn;               // 3 per obs
+  std::vector<double> vG;                 // 3 x 30 per obs
   double cost = 0.0;
 };
+
+// Tangent Jacobians (2 x 15 in node dims, masked dims zero) of observation i
+// with respect to its global nodes, from the ambient blocks of
+// VisualReprojectionError::Evaluate: intrinsics and distortion are additive
+// blocks, q_C_I goes through JplQuaternionParameterization, a baseframe
+// through JplPoseParameterization or JplYawOnlyPoseParameterization.
+static void nodeJacobians(const Problem& p, int64_t i, const double* Jbf_lm, const double* Jbf_obs,
+                          const double* Jq_CI, const double* Jp_CI, const double* Jintr, const double* Jdist,
+                          int32_t* nid, double* JN) {
+  std::memset(JN, 0, 90 * sizeof(double));
+  nid[0] = nid[1] = nid[2] = -1;
+  const int c = p.obs_cam[i];
+  const int cn = p.cam_node[c];
+  if (cn >= 0) {
+    nid[0] = cn;
+    const uint8_t* m = &p.g_mask[15 * cn];
+    double Jq[12];
+    jplQuaternionJacobian(p.cams[c].q_CI_p_CI, Jq);
+    for (int r = 0; r < 2; ++r) {
+      double* o = JN + 15 * r;
+      for (int a = 0; a < 4; ++a) o[a] = m[a] ? Jintr[4 * r + a] : 0.0;
+      for (int a = 0; a < 4; ++a) o[4 + a] = m[4 + a] ? Jdist[4 * r + a] : 0.0;
+      for (int a = 0; a < 3; ++a) {
+        double s = 0.0;
+        for (int k = 0; k < 4; ++k) s += Jq_CI[4 * r + k] * Jq[3 * k + a];
+        o[8 + a] = m[8 + a] ? s : 0.0;
+        o[11 + a] = m[11 + a] ? Jp_CI[3 * r + a] : 0.0;
+      }
+    }
+  }
+  if (p.obs_type[i] != MBA_GLOBAL) return;
+  const int l = p.obs_lm[i];
+  const int mis[2] = {p.kf_mis[p.lm_store[l]], p.kf_mis[p.obs_kf[i]]};
+  const double* Jb[2] = {Jbf_lm, Jbf_obs};
+  for (int s = 0; s < 2; ++s) {
+    const int g = p.mis_node[mis[s]];
+    if (g < 0) continue;
+    nid[1 + s] = g;
+    double* O = JN + 30 * (1 + s);
+    const uint8_t* m = &p.g_mask[15 * g];
+    const double* q = &p.mis[7 * mis[s]];
+    if (p.mis_flags[mis[s]] == MBA_MIS_BASEFRAME_YAW_POSITION) {
+      double Jy[4];
+      jplYawJacobian(q, Jy);
+      for (int r = 0; r < 2; ++r) {
+        double v = 0.0;
+        for (int k = 0; k < 4; ++k) v += Jb[s][7 * r + k] * Jy[k];
+        O[15 * r] = v;
+      }
+    } else {
+      double Jq[12];
+      jplQuaternionJacobian(q, Jq);
+      for (int r = 0; r < 2; ++r)
+        for (int a = 0; a < 3; ++a) {
+          double v = 0.0;
+          for (int k = 0; k < 4; ++k) v += Jb[s][7 * r + k] * Jq[3 * k + a];
+          O[15 * r + a] = m[a] ? v : 0.0;
+        }
+    }
+    for (int r = 0; r < 2; ++r)
+      for (int a = 0; a < 3; ++a) O[15 * r + 3 + a] = Jb[s][7 * r + 4 + a];
+  }
+}
 
 // Ceres Corrector (third-party, restated from Triggs et al. "Bundle
 // adjustment: a modern synthesis" as documented by Ceres): returns the
@@ -324,6 +449,10 @@ int linearize(const Problem& p, bool want_jac, Linearization* L) {
     L->vJs.assign(12 * p.nobs, 0.0); L->vJo.assign(12 * p.nobs, 0.0);
     L->ir.assign(15 * p.nedge, 0.0); L->iJf.assign(225 * p.nedge, 0.0); L->iJt.assign(225 * p.nedge, 0.0);
     L->sJ.assign(6 * (p.nedge - p.nimu), 0.0);
+    if (p.ng > 0) {
+      L->vGn.assign(3 * p.nobs, -1);
+      L->vG.assign(90 * p.nobs, 0.0);
+    }
   }
   const int T = p.threads;
   std::vector<double> part(T + 1, 0.0);
@@ -338,7 +467,10 @@ int linearize(const Problem& p, bool want_jac, Linearization* L) {
         const double* P[9];
         visualParams(p, i, P);
         double r[2], Jl[6], Js7[14], Jo7[14];
-        double* J[9] = {Jl, Js7, nullptr, nullptr, Jo7, nullptr, nullptr, nullptr, nullptr};
+        double Jbl[14], Jbo[14], Jqc[8], Jpc[6], Jin[8], Jdi[8];
+        const bool nodes = want_jac && p.ng > 0;
+        double* J[9] = {Jl, Js7, nodes ? Jbl : nullptr, nodes ? Jbo : nullptr, Jo7, nodes ? Jqc : nullptr,
+                        nodes ? Jpc : nullptr, nodes ? Jin : nullptr, nodes ? Jdi : nullptr};
         visualEvaluate(P, &p.obs_uv[2 * i], p.obs_sigma[i], p.obs_type[i], p.cams[p.obs_cam[i]], r,
                        want_jac ? J : nullptr, nullptr);
         const double sq = r[0] * r[0] + r[1] * r[1];
@@ -368,10 +500,17 @@ int linearize(const Problem& p, bool want_jac, Linearization* L) {
               Jot[6 * rr + c] = a;
             }
         }
+        double JN[90];
+        int32_t nid[3] = {-1, -1, -1};
+        if (nodes) nodeJacobians(p, i, Jbl, Jbo, Jqc, Jpc, Jin, Jdi, nid, JN);
         if (p.use_huber) {
-          double* Js_[3] = {Jl, Jst, Jot};
-          const int cols[3] = {3, 6, 6};
-          applyCorrector(sq, rho, r, Js_, cols, 3);
+          double* Js_[6] = {Jl, Jst, Jot, JN, JN + 30, JN + 60};
+          const int cols[6] = {3, 6, 6, 15, 15, 15};
+          applyCorrector(sq, rho, r, Js_, cols, nodes ? 6 : 3);
+        }
+        if (nodes) {
+          std::memcpy(&L->vGn[3 * i], nid, sizeof(nid));
+          std::memcpy(&L->vG[90 * i], JN, sizeof(JN));
         }
         std::memcpy(&L->vr[2 * i], r, sizeof(r));
         std::memcpy(&L->vJl[6 * i], Jl, sizeof(Jl));
@@ -521,15 +660,40 @@ struct BlockSystem {
   }
 };
 
+// Global nodes touched by observation i (block indices nkf + g), up to 3.
+static int obsNodes(const Problem& p, int64_t i, int64_t* out) {
+  int n = 0;
+  const int cn = p.cam_node[p.obs_cam[i]];
+  if (cn >= 0) out[n++] = p.nkf + cn;
+  if (p.obs_type[i] == MBA_GLOBAL) {
+    const int gl = p.mis_node[p.kf_mis[p.lm_store[p.obs_lm[i]]]], go = p.mis_node[p.kf_mis[p.obs_kf[i]]];
+    if (gl >= 0) out[n++] = p.nkf + gl;
+    if (go >= 0) out[n++] = p.nkf + go;
+  }
+  return n;
+}
+
+// Tangent dim d of block k (keyframe or global node) is active.
+static bool dimActive(const Problem& p, int64_t k, int d) {
+  return k < p.nkf ? p.kf_mask[15 * k + d] != 0 : p.g_mask[15 * (k - p.nkf) + d] != 0;
+}
+
 static void buildPattern(const Problem& p, BlockSystem* S) {
   S->nkf = p.nkf;
-  for (int64_t k = 0; k < p.nkf; ++k) S->add(k, k);
+  for (int64_t k = 0; k < p.nkf + p.ng; ++k) S->add(k, k);
   for (int64_t e = 0; e < p.nedge; ++e) S->add(p.e_from[e], p.e_to[e]);
   std::vector<int64_t> ks;
   for (int64_t l = 0; l < p.nlm; ++l) {
     ks.clear();
     ks.push_back(p.lm_store[l]);
-    for (int64_t a = p.lm_obs_off[l]; a < p.lm_obs_off[l + 1]; ++a) ks.push_back(p.obs_kf[p.lm_obs_idx[a]]);
+    for (int64_t a = p.lm_obs_off[l]; a < p.lm_obs_off[l + 1]; ++a) {
+      ks.push_back(p.obs_kf[p.lm_obs_idx[a]]);
+      if (p.ng > 0) {
+        int64_t g[3];
+        const int n = obsNodes(p, p.lm_obs_idx[a], g);
+        for (int b = 0; b < n; ++b) ks.push_back(g[b]);
+      }
+    }
     std::sort(ks.begin(), ks.end());
     ks.erase(std::unique(ks.begin(), ks.end()), ks.end());
     for (size_t a = 0; a < ks.size(); ++a)
@@ -647,11 +811,24 @@ static StepResult computeStep(const Problem& p, const Linearization& L, const Sc
                               const std::vector<double>& dsw, const BlockSystem& pattern, int solver, int max_it,
                               double tol, double* dense_A = nullptr, double* dense_b = nullptr) {
   StepResult out;
-  const int64_t N = p.nkf;
+  const int64_t N = p.nkf, NB = p.nkf + p.ng;  // keyframe blocks, then global nodes
   BlockSystem S = pattern;  // copies pattern + zeroed blocks
   std::fill(S.blocks.begin(), S.blocks.end(), 0.0);
-  std::vector<double> bc(15 * N, 0.0);  // rhs (-g_c initially)
+  std::vector<double> bc(15 * NB, 0.0);  // rhs (-g_c initially)
   std::vector<double> Hll(9 * p.nlm, 0.0), gl(3 * p.nlm, 0.0);
+  // Scaled node Jacobians of observation i: block ids (nkf + g) and 2 x 15 rows.
+  auto nodeJ = [&](int64_t i, int64_t* nb, double (*Jn)[30]) -> int {
+    if (p.ng == 0) return 0;
+    int n = 0;
+    for (int a = 0; a < 3; ++a) {
+      const int g = L.vGn[3 * i + a];
+      if (g < 0) continue;
+      nb[n] = N + g;
+      for (int c = 0; c < 30; ++c) Jn[n][c] = L.vG[90 * i + 30 * a + c] * sc.skf[15 * (N + g) + c % 15];
+      ++n;
+    }
+    return n;
+  };
   // Camera-camera terms and gradient.
   double Ja[2 * 15], Jb[2 * 15];
   for (int64_t i = 0; i < p.nobs; ++i) {
@@ -664,6 +841,13 @@ static StepResult computeStep(const Problem& p, const Linearization& L, const Sc
         Hll[9 * l + 3 * a + b] += (Jl[a] * Jl[b] + Jl[3 + a] * Jl[3 + b]) * s * sc.slm[3 * l + b];
       gl[3 * l + a] += (Jl[a] * r[0] + Jl[3 + a] * r[1]) * s;
     }
+    int64_t nb[3];
+    double Jn[3][30];
+    const int nn = nodeJ(i, nb, Jn);
+    for (int a = 0; a < nn; ++a) {
+      for (int b = a; b < nn; ++b) addJtJ(&S, nb[a], nb[b], Jn[a], Jn[b], 2, 1.0);
+      for (int c = 0; c < 15; ++c) bc[15 * nb[a] + c] -= Jn[a][c] * r[0] + Jn[a][15 + c] * r[1];
+    }
     if (p.obs_type[i] == MBA_LOCAL_KEYFRAME) continue;
     const int64_t ks = p.lm_store[l], ko = p.obs_kf[i];
     std::memset(Ja, 0, sizeof(Ja)); std::memset(Jb, 0, sizeof(Jb));
@@ -675,6 +859,10 @@ static StepResult computeStep(const Problem& p, const Linearization& L, const Sc
     addJtJ(&S, ks, ks, Ja, Ja, 2, 1.0);
     addJtJ(&S, ko, ko, Jb, Jb, 2, 1.0);
     addJtJ(&S, ks, ko, Ja, Jb, 2, 1.0);
+    for (int a = 0; a < nn; ++a) {
+      addJtJ(&S, ks, nb[a], Ja, Jn[a], 2, 1.0);
+      addJtJ(&S, ko, nb[a], Jb, Jn[a], 2, 1.0);
+    }
     for (int c = 0; c < 6; ++c) {
       bc[15 * ks + c] -= Ja[c] * r[0] + Ja[15 + c] * r[1];
       bc[15 * ko + c] -= Jb[c] * r[0] + Jb[15 + c] * r[1];
@@ -699,21 +887,47 @@ static StepResult computeStep(const Problem& p, const Linearization& L, const Sc
       bc[15 * t + c] -= b;
     }
   }
-  // LM diagonal on keyframes.
-  for (int64_t k = 0; k < N; ++k) {
+  // LM diagonal on keyframes and global nodes.
+  for (int64_t k = 0; k < NB; ++k) {
     double* B = &S.blocks[225 * S.find(k, k)];
     for (int d = 0; d < 15; ++d) B[16 * d] += dkf[15 * k + d];
   }
   // Schur elimination per landmark.
   std::vector<double> Vinv(9 * p.nlm, 0.0);
-  std::vector<int64_t> ks;
-  std::vector<double> W;  // per touched KF: 3 x 6
+  std::vector<int64_t> ks, gs;
+  std::vector<double> W;   // per touched KF: 3 x 6
+  std::vector<double> WG;  // per touched global node: 3 x 15
   for (int64_t l = 0; l < p.nlm; ++l) {
     if (!p.lm_mask[l]) continue;
     double H[9];
     for (int a = 0; a < 9; ++a) H[a] = Hll[9 * l + a];
     for (int a = 0; a < 3; ++a) H[4 * a] += dlm[3 * l + a];
     if (!inv3(H, &Vinv[9 * l])) { out.status = MBA_ERR_NOT_SPD; return out; }
+    if (p.ng > 0) {
+      // W of the landmark's global nodes: Wn = sum over its observations of J_l^T J_n.
+      gs.clear();
+      for (int64_t a = p.lm_obs_off[l]; a < p.lm_obs_off[l + 1]; ++a) {
+        int64_t g[3];
+        const int n = obsNodes(p, p.lm_obs_idx[a], g);
+        for (int b = 0; b < n; ++b) gs.push_back(g[b]);
+      }
+      std::sort(gs.begin(), gs.end());
+      gs.erase(std::unique(gs.begin(), gs.end()), gs.end());
+      WG.assign(45 * gs.size(), 0.0);
+      for (int64_t a = p.lm_obs_off[l]; a < p.lm_obs_off[l + 1]; ++a) {
+        const int64_t i = p.lm_obs_idx[a];
+        const double* Jl = &L.vJl[6 * i];
+        int64_t nb[3];
+        double Jn[3][30];
+        const int nn = nodeJ(i, nb, Jn);
+        for (int b = 0; b < nn; ++b) {
+          const size_t pos = std::lower_bound(gs.begin(), gs.end(), nb[b]) - gs.begin();
+          for (int x = 0; x < 3; ++x)
+            for (int c = 0; c < 15; ++c)
+              WG[45 * pos + 15 * x + c] += (Jl[x] * Jn[b][c] + Jl[3 + x] * Jn[b][15 + c]) * sc.slm[3 * l + x];
+        }
+      }
+    }
     ks.clear();
     ks.push_back(p.lm_store[l]);
     for (int64_t a = p.lm_obs_off[l]; a < p.lm_obs_off[l + 1]; ++a) ks.push_back(p.obs_kf[p.lm_obs_idx[a]]);
@@ -756,6 +970,34 @@ static StepResult computeStep(const Problem& p, const Linearization& L, const Sc
           }
       }
     }
+    if (!gs.empty()) {
+      // Global nodes: VWn = Vinv Wn; S(kf, n) -= W_kf^T VWn, S(n_a, n_b) -= Wn_a^T VWn_b,
+      // rhs_n += Wn^T Vinv g_l.  Node blocks come after every keyframe block.
+      std::vector<double> VWG(45 * gs.size());
+      for (size_t j = 0; j < gs.size(); ++j)
+        for (int x = 0; x < 3; ++x)
+          for (int c = 0; c < 15; ++c)
+            VWG[45 * j + 15 * x + c] = Vi[3 * x] * WG[45 * j + c] + Vi[3 * x + 1] * WG[45 * j + 15 + c] +
+                                       Vi[3 * x + 2] * WG[45 * j + 30 + c];
+      for (size_t b = 0; b < gs.size(); ++b) {
+        for (int c = 0; c < 15; ++c)
+          bc[15 * gs[b] + c] += WG[45 * b + c] * Vg[0] + WG[45 * b + 15 + c] * Vg[1] + WG[45 * b + 30 + c] * Vg[2];
+        for (size_t a = 0; a < ks.size(); ++a) {
+          double* B = &S.blocks[225 * S.find(ks[a], gs[b])];
+          for (int r = 0; r < 6; ++r)
+            for (int c = 0; c < 15; ++c)
+              B[15 * r + c] -= W[18 * a + r] * VWG[45 * b + c] + W[18 * a + 6 + r] * VWG[45 * b + 15 + c] +
+                               W[18 * a + 12 + r] * VWG[45 * b + 30 + c];
+        }
+        for (size_t a = 0; a <= b; ++a) {
+          double* B = &S.blocks[225 * S.find(gs[a], gs[b])];
+          for (int r = 0; r < 15; ++r)
+            for (int c = 0; c < 15; ++c)
+              B[15 * r + c] -= WG[45 * a + r] * VWG[45 * b + c] + WG[45 * a + 15 + r] * VWG[45 * b + 15 + c] +
+                               WG[45 * a + 30 + r] * VWG[45 * b + 30 + c];
+        }
+      }
+    }
   }
   // Schur elimination of each switch variable: S_ab -= W_a W_b^T / H,
   // rhs_a += W_a g / H for a, b in {from, to}.
@@ -783,14 +1025,14 @@ static StepResult computeStep(const Problem& p, const Linearization& L, const Sc
     double* B = &S.blocks[225 * b];
     for (int r = 0; r < 15; ++r)
       for (int c = 0; c < 15; ++c)
-        if (!p.kf_mask[15 * i + r] || !p.kf_mask[15 * j + c]) B[15 * r + c] = (i == j && r == c) ? 1.0 : 0.0;
+        if (!dimActive(p, i, r) || !dimActive(p, j, c)) B[15 * r + c] = (i == j && r == c) ? 1.0 : 0.0;
   }
-  for (int64_t k = 0; k < N; ++k)
+  for (int64_t k = 0; k < NB; ++k)
     for (int d = 0; d < 15; ++d)
-      if (!p.kf_mask[15 * k + d]) bc[15 * k + d] = 0.0;
+      if (!dimActive(p, k, d)) bc[15 * k + d] = 0.0;
 
   if (dense_A) {
-    const size_t n = 15 * N;
+    const size_t n = 15 * NB;
     std::fill(dense_A, dense_A + n * n, 0.0);
     for (size_t b = 0; b < S.bi.size(); ++b) {
       const int64_t i = S.bi[b], j = S.bj[b];
@@ -804,9 +1046,9 @@ static StepResult computeStep(const Problem& p, const Linearization& L, const Sc
     std::copy(bc.begin(), bc.end(), dense_b);
     return out;
   }
-  std::vector<double> x(15 * N, 0.0);
+  std::vector<double> x(15 * NB, 0.0);
   if (solver == MBA_LINEAR_SOLVER_DENSE_SCHUR) {
-    const int n = (int)(15 * N);
+    const int n = (int)(15 * NB);
     std::vector<double> A((size_t)n * n, 0.0);
     for (size_t b = 0; b < S.bi.size(); ++b) {
       const int64_t i = S.bi[b], j = S.bj[b];
@@ -823,8 +1065,8 @@ static StepResult computeStep(const Problem& p, const Linearization& L, const Sc
     out.linear_iterations = 1;
   } else {
     // Block-Jacobi PCG on S x = bc.
-    std::vector<std::vector<double>> Linv(N);
-    for (int64_t k = 0; k < N; ++k) {
+    std::vector<std::vector<double>> Linv(NB);
+    for (int64_t k = 0; k < NB; ++k) {
       std::vector<double> B(S.blocks.begin() + 225 * S.find(k, k), S.blocks.begin() + 225 * S.find(k, k) + 225);
       if (!cholN(B, 15)) { out.status = MBA_ERR_NOT_SPD; return out; }
       Linv[k] = B;
@@ -849,32 +1091,32 @@ static StepResult computeStep(const Problem& p, const Linearization& L, const Sc
     };
     auto precond = [&](const std::vector<double>& in, std::vector<double>& o) {
       o = in;
-      for (int64_t k = 0; k < N; ++k) cholSolve(Linv[k], 15, &o[15 * k]);
+      for (int64_t k = 0; k < NB; ++k) cholSolve(Linv[k], 15, &o[15 * k]);
     };
-    std::vector<double> r = bc, z(15 * N), pp(15 * N), q(15 * N);
+    std::vector<double> r = bc, z(15 * NB), pp(15 * NB), q(15 * NB);
     double bnorm = 0.0;
     for (double v : bc) bnorm += v * v;
     bnorm = std::sqrt(bnorm);
     precond(r, z);
     pp = z;
     double rz = 0.0;
-    for (int64_t a = 0; a < 15 * N; ++a) rz += r[a] * z[a];
+    for (int64_t a = 0; a < 15 * NB; ++a) rz += r[a] * z[a];
     int it = 0;
     if (bnorm > 0.0) {
       for (it = 0; it < max_it; ++it) {
         spmv(pp, q);
         double pq = 0.0;
-        for (int64_t a = 0; a < 15 * N; ++a) pq += pp[a] * q[a];
+        for (int64_t a = 0; a < 15 * NB; ++a) pq += pp[a] * q[a];
         const double alpha = rz / pq;
         double rn = 0.0;
-        for (int64_t a = 0; a < 15 * N; ++a) { x[a] += alpha * pp[a]; r[a] -= alpha * q[a]; rn += r[a] * r[a]; }
+        for (int64_t a = 0; a < 15 * NB; ++a) { x[a] += alpha * pp[a]; r[a] -= alpha * q[a]; rn += r[a] * r[a]; }
         if (std::sqrt(rn) <= tol * bnorm) { ++it; break; }
         precond(r, z);
         double rz2 = 0.0;
-        for (int64_t a = 0; a < 15 * N; ++a) rz2 += r[a] * z[a];
+        for (int64_t a = 0; a < 15 * NB; ++a) rz2 += r[a] * z[a];
         const double beta = rz2 / rz;
         rz = rz2;
-        for (int64_t a = 0; a < 15 * N; ++a) pp[a] = z[a] + beta * pp[a];
+        for (int64_t a = 0; a < 15 * NB; ++a) pp[a] = z[a] + beta * pp[a];
       }
     }
     out.linear_iterations = it;
@@ -885,16 +1127,23 @@ static StepResult computeStep(const Problem& p, const Linearization& L, const Sc
   std::vector<double> t(3 * p.nlm, 0.0);
   for (int64_t l = 0; l < p.nlm; ++l) for (int a = 0; a < 3; ++a) t[3 * l + a] = -gl[3 * l + a];
   for (int64_t i = 0; i < p.nobs; ++i) {
-    if (p.obs_type[i] == MBA_LOCAL_KEYFRAME) continue;
     const int l = p.obs_lm[i];
     if (!p.lm_mask[l]) continue;
     const double* Jl = &L.vJl[6 * i];
-    const int64_t ks2 = p.lm_store[l], ko = p.obs_kf[i];
     double u[2] = {0.0, 0.0};
-    for (int rr = 0; rr < 2; ++rr)
-      for (int c = 0; c < 6; ++c)
-        u[rr] += L.vJs[12 * i + 6 * rr + c] * sc.skf[15 * ks2 + c] * x[15 * ks2 + c] +
-                 L.vJo[12 * i + 6 * rr + c] * sc.skf[15 * ko + c] * x[15 * ko + c];
+    if (p.obs_type[i] != MBA_LOCAL_KEYFRAME) {
+      const int64_t ks2 = p.lm_store[l], ko = p.obs_kf[i];
+      for (int rr = 0; rr < 2; ++rr)
+        for (int c = 0; c < 6; ++c)
+          u[rr] += L.vJs[12 * i + 6 * rr + c] * sc.skf[15 * ks2 + c] * x[15 * ks2 + c] +
+                   L.vJo[12 * i + 6 * rr + c] * sc.skf[15 * ko + c] * x[15 * ko + c];
+    }
+    int64_t nb[3];
+    double Jn[3][30];
+    const int nn = nodeJ(i, nb, Jn);
+    for (int a = 0; a < nn; ++a)
+      for (int rr = 0; rr < 2; ++rr)
+        for (int c = 0; c < 15; ++c) u[rr] += Jn[a][15 * rr + c] * x[15 * nb[a] + c];
     for (int a = 0; a < 3; ++a) t[3 * l + a] -= (Jl[a] * u[0] + Jl[3 + a] * u[1]) * sc.slm[3 * l + a];
   }
   for (int64_t l = 0; l < p.nlm; ++l) {
@@ -948,6 +1197,41 @@ static void plusState(const Problem& p, const std::vector<double>& dkf, const st
       for (int i = 0; i < 3; ++i) (*lp)[3 * l + i] += dlm[3 * l + i];
 }
 
+// Retraction of the global nodes by the unscaled tangent step (dkf holds the
+// keyframe blocks, then the nodes): intrinsics, distortion and p_C_I add,
+// q_C_I by JplQuaternionParameterization::Plus; a baseframe by
+// JplPoseParameterization or JplYawOnlyPoseParameterization (the yaw Plus of
+// quaternion-param-jpl.cc:78-105 and an added position).
+static void plusNodes(const Problem& p, const std::vector<double>& dkf, std::vector<mba_camera>* cams,
+                      std::vector<double>* mis) {
+  for (int64_t g = 0; g < p.ng; ++g) {
+    const double* d = &dkf[15 * (p.nkf + g)];
+    const uint8_t* m = &p.g_mask[15 * g];
+    if (p.node_cam[g] >= 0) {
+      mba_camera& c = (*cams)[p.node_cam[g]];
+      for (int a = 0; a < 4; ++a) {
+        if (m[a]) c.intrinsics[a] += d[a];
+        if (m[4 + a]) c.distortion[a] += d[4 + a];
+      }
+      if (m[8] || m[9] || m[10]) {
+        double q[4];
+        jplQuaternionPlus(c.q_CI_p_CI, d + 8, q);
+        std::memcpy(c.q_CI_p_CI, q, sizeof(q));
+      }
+      for (int a = 0; a < 3; ++a)
+        if (m[11 + a]) c.q_CI_p_CI[4 + a] += d[11 + a];
+    } else {
+      const int mi = p.node_mis[g];
+      double* x = &(*mis)[7 * mi];
+      double q[4];
+      if (p.mis_flags[mi] == MBA_MIS_BASEFRAME_YAW_POSITION) jplYawPlus(x, d, q);
+      else jplQuaternionPlus(x, d, q);
+      std::memcpy(x, q, sizeof(q));
+      for (int a = 0; a < 3; ++a) x[4 + a] += d[3 + a];
+    }
+  }
+}
+
 // Switch retraction: plain addition projected onto the bounds [0, 1], as
 // Ceres applies parameter bounds after Plus.
 static void plusSwitches(const std::vector<double>& ds, std::vector<double>* sw) {
@@ -957,7 +1241,7 @@ static void plusSwitches(const std::vector<double>& ds, std::vector<double>* sw)
 // Jacobi scaling 1 / (1 + |column|) and the column norms of the Jacobian.
 static void columnNorms(const Problem& p, const Linearization& L, std::vector<double>& nkf, std::vector<double>& nlm,
                         std::vector<double>& nsw) {
-  nkf.assign(15 * p.nkf, 0.0);
+  nkf.assign(15 * (p.nkf + p.ng), 0.0);  // keyframe blocks, then the global nodes
   nlm.assign(3 * p.nlm, 0.0);
   nsw.assign(p.sw.size(), 0.0);
   for (int64_t j = 0; j < p.nedge - p.nimu; ++j) {
@@ -970,6 +1254,12 @@ static void columnNorms(const Problem& p, const Linearization& L, std::vector<do
   for (int64_t i = 0; i < p.nobs; ++i) {
     const int l = p.obs_lm[i];
     for (int a = 0; a < 3; ++a) nlm[3 * l + a] += L.vJl[6 * i + a] * L.vJl[6 * i + a] + L.vJl[6 * i + 3 + a] * L.vJl[6 * i + 3 + a];
+    for (int a = 0; a < 3 && p.ng > 0; ++a) {
+      const int g = L.vGn[3 * i + a];
+      if (g < 0) continue;
+      const double* J = &L.vG[90 * i + 30 * a];
+      for (int c = 0; c < 15; ++c) nkf[15 * (p.nkf + g) + c] += J[c] * J[c] + J[15 + c] * J[15 + c];
+    }
     if (p.obs_type[i] == MBA_LOCAL_KEYFRAME) continue;
     const int64_t ks = p.lm_store[l], ko = p.obs_kf[i];
     for (int c = 0; c < 6; ++c) {
@@ -983,6 +1273,54 @@ static void columnNorms(const Problem& p, const Linearization& L, std::vector<do
         nkf[15 * p.e_from[e] + c] += L.iJf[225 * e + 15 * r + c] * L.iJf[225 * e + 15 * r + c];
         nkf[15 * p.e_to[e] + c] += L.iJt[225 * e + 15 * r + c] * L.iJt[225 * e + 15 * r + c];
       }
+}
+
+// Max |g| of the robustified gradient g = J^T r over every variable tangent
+// dim (keyframes, landmarks, switch variables, global nodes), unscaled.
+static double gradientMaxNorm(const Problem& p, const Linearization& L) {
+  std::vector<double> gk(15 * (p.nkf + p.ng), 0.0), gl(3 * p.nlm, 0.0), gs(p.sw.size(), 0.0);
+  for (int64_t i = 0; i < p.nobs; ++i) {
+    const int l = p.obs_lm[i];
+    const double* r = &L.vr[2 * i];
+    for (int a = 0; a < 3; ++a) gl[3 * l + a] += L.vJl[6 * i + a] * r[0] + L.vJl[6 * i + 3 + a] * r[1];
+    if (p.obs_type[i] != MBA_LOCAL_KEYFRAME) {
+      const int64_t ks = p.lm_store[l], ko = p.obs_kf[i];
+      for (int c = 0; c < 6; ++c) {
+        gk[15 * ks + c] += L.vJs[12 * i + c] * r[0] + L.vJs[12 * i + 6 + c] * r[1];
+        gk[15 * ko + c] += L.vJo[12 * i + c] * r[0] + L.vJo[12 * i + 6 + c] * r[1];
+      }
+    }
+    for (int a = 0; a < 3 && p.ng > 0; ++a) {
+      const int g = L.vGn[3 * i + a];
+      if (g < 0) continue;
+      const double* J = &L.vG[90 * i + 30 * a];
+      for (int c = 0; c < 15; ++c) gk[15 * (p.nkf + g) + c] += J[c] * r[0] + J[15 + c] * r[1];
+    }
+  }
+  for (int64_t e = 0; e < p.nedge; ++e) {
+    const double* r = &L.ir[15 * e];
+    for (int c = 0; c < 15; ++c)
+      for (int rr = 0; rr < 15; ++rr) {
+        gk[15 * p.e_from[e] + c] += L.iJf[225 * e + 15 * rr + c] * r[rr];
+        gk[15 * p.e_to[e] + c] += L.iJt[225 * e + 15 * rr + c] * r[rr];
+      }
+    const int q = e >= p.nimu ? p.pe_swi[e - p.nimu] : -1;
+    if (q >= 0) {
+      const double w = p.sw_w[q];
+      double v = -w * (1.0 - p.sw[q]) * w;
+      for (int k = 0; k < 6; ++k) v += L.sJ[6 * (e - p.nimu) + k] * r[k];
+      gs[q] = v;
+    }
+  }
+  double m = 0.0;
+  for (int64_t k = 0; k < p.nkf + p.ng; ++k)
+    for (int d = 0; d < 15; ++d)
+      if (dimActive(p, k, d)) m = std::max(m, std::fabs(gk[15 * k + d]));
+  for (int64_t l = 0; l < p.nlm; ++l)
+    if (p.lm_mask[l] && !p.lm_off[l])
+      for (int a = 0; a < 3; ++a) m = std::max(m, std::fabs(gl[3 * l + a]));
+  for (double v : gs) m = std::max(m, std::fabs(v));
+  return m;
 }
 
 // findOutlierLandmarks (outlier-rejection-solver.cc:28-103): a landmark is
@@ -1021,7 +1359,7 @@ int solve(Problem& p, const mba_solver_options& o, mba_summary* sum) {
   int st = linearize(p, true, &L);
   if (st) return st;
   Scaled sc;
-  sc.skf.assign(15 * p.nkf, 1.0);
+  sc.skf.assign(15 * (p.nkf + p.ng), 1.0);
   sc.slm.assign(3 * p.nlm, 1.0);
   sc.ssw.assign(p.sw.size(), 1.0);
   std::vector<double> nkf, nlm, nsw;
@@ -1036,12 +1374,19 @@ int solve(Problem& p, const mba_solver_options& o, mba_summary* sum) {
   jacobi();
   BlockSystem pattern;
   buildPattern(p, &pattern);
+  // Ceres' gradient test (TrustRegionMinimizer): max |J^T r| over the
+  // variable tangent dims at or below gradient_tolerance ends the solve, at
+  // the start and after each accepted step.
+  auto gradient_converged = [&]() {
+    if (!o.check_tolerances) return false;
+    return gradientMaxNorm(p, L) <= o.gradient_tolerance;
+  };
 
   double cost = L.cost;
   double radius = o.initial_trust_region_radius;
   double decrease_factor = 2.0;
   bool reuse_diag = false;
-  std::vector<double> dkf(15 * p.nkf), dlm(3 * p.nlm), dsw(p.sw.size());
+  std::vector<double> dkf(15 * (p.nkf + p.ng)), dlm(3 * p.nlm), dsw(p.sw.size());
   if (sum) {
     sum->initial_cost = cost;
     sum->num_iterations = 0;
@@ -1063,8 +1408,13 @@ int solve(Problem& p, const mba_solver_options& o, mba_summary* sum) {
   };
   record(0, true, 0, cost, 0.0, 0.0, 0.0);
   if (sum && o.stop_cost > 0 && cost <= o.stop_cost) { sum->termination = 6; sum->time_to_stop_cost_ms = 0.0; }
+  bool done = false;
+  if (gradient_converged()) {
+    if (sum) sum->termination = 2;
+    done = true;
+  }
   int64_t rejected = 0;
-  for (int iter = 1; iter <= o.max_num_iterations; ++iter) {
+  for (int iter = 1; iter <= o.max_num_iterations && !done; ++iter) {
     if (sum && sum->termination == 6) break;
     // solveWithOutlierRejection (outlier-rejection-solver.cc:199-259): every
     // n iterations the Ceres solve ends, outlier landmarks are removed and a
@@ -1108,6 +1458,13 @@ int solve(Problem& p, const mba_solver_options& o, mba_summary* sum) {
               u[rr] += L.vJs[12 * i + 6 * rr + c] * sc.skf[15 * ks + c] * s.dc[15 * ks + c] +
                        L.vJo[12 * i + 6 * rr + c] * sc.skf[15 * ko + c] * s.dc[15 * ko + c];
           }
+          for (int a = 0; a < 3 && p.ng > 0; ++a) {
+            const int g = L.vGn[3 * i + a];
+            if (g < 0) continue;
+            const int64_t b = p.nkf + g;
+            for (int c = 0; c < 15; ++c)
+              u[rr] += L.vG[90 * i + 30 * a + 15 * rr + c] * sc.skf[15 * b + c] * s.dc[15 * b + c];
+          }
         }
         mcc -= u[0] * (L.vr[2 * i] + u[0] / 2.0) + u[1] * (L.vr[2 * i + 1] + u[1] / 2.0);
       }
@@ -1137,16 +1494,20 @@ int solve(Problem& p, const mba_solver_options& o, mba_summary* sum) {
       continue;
     }
     // Unscale and retract.
-    std::vector<double> ukf(15 * p.nkf), ulm(3 * p.nlm), usw(p.sw.size());
+    std::vector<double> ukf(15 * (p.nkf + p.ng)), ulm(3 * p.nlm), usw(p.sw.size());
     for (size_t a = 0; a < ukf.size(); ++a) ukf[a] = s.dc[a] * sc.skf[a];
     for (size_t a = 0; a < ulm.size(); ++a) ulm[a] = s.dl[a] * sc.slm[a];
     for (size_t a = 0; a < usw.size(); ++a) usw[a] = s.ds[a] * sc.ssw[a];
     std::vector<double> kx = p.kf_x, kv = p.kf_v, kbg = p.kf_bg, kba = p.kf_ba, lp = p.lm_p, swv = p.sw;
+    std::vector<mba_camera> cams = p.cams;
+    std::vector<double> mis = p.mis;
     plusState(p, ukf, ulm, &kx, &kv, &kbg, &kba, &lp);
     plusSwitches(usw, &swv);
+    if (p.ng > 0) plusNodes(p, ukf, &cams, &mis);
     auto swap_state = [&]() {
       std::swap(kx, p.kf_x); std::swap(kv, p.kf_v); std::swap(kbg, p.kf_bg); std::swap(kba, p.kf_ba);
       std::swap(lp, p.lm_p); std::swap(swv, p.sw);
+      std::swap(cams, p.cams); std::swap(mis, p.mis);
     };
     swap_state();
     Linearization Lc;
@@ -1176,6 +1537,25 @@ int solve(Problem& p, const mba_solver_options& o, mba_summary* sum) {
     }
     for (int64_t l = 0; l < p.nlm; ++l)
       if (p.lm_mask[l]) add(p.lm_p, lp, l, 3);
+    auto addv = [&](const double* now, const double* old, int n) {
+      for (int a = 0; a < n; ++a) {
+        step_norm += (now[a] - old[a]) * (now[a] - old[a]);
+        x_norm += old[a] * old[a];
+      }
+    };
+    for (int64_t g = 0; g < p.ng; ++g) {
+      const uint8_t* m = &p.g_mask[15 * g];
+      if (p.node_cam[g] >= 0) {
+        const int c = p.node_cam[g];
+        const mba_camera &now = p.cams[c], &old = cams[c];
+        if (m[0]) addv(now.intrinsics, old.intrinsics, 4);
+        if (m[4]) addv(now.distortion, old.distortion, distortionParams(old.distortion_type));
+        if (m[8]) addv(now.q_CI_p_CI, old.q_CI_p_CI, 4);
+        if (m[11]) addv(now.q_CI_p_CI + 4, old.q_CI_p_CI + 4, 3);
+      } else {
+        addv(&p.mis[7 * p.node_mis[g]], &mis[7 * p.node_mis[g]], 7);
+      }
+    }
     for (size_t a = 0; a < swv.size(); ++a) { const double dd = p.sw[a] - swv[a]; step_norm += dd * dd; x_norm += swv[a] * swv[a]; }
     step_norm = std::sqrt(step_norm);
     x_norm = std::sqrt(x_norm);
@@ -1210,6 +1590,10 @@ int solve(Problem& p, const mba_solver_options& o, mba_summary* sum) {
         sum->time_to_stop_cost_ms = std::chrono::duration<double, std::milli>(clk::now() - t0).count();
         sum->termination = 6;
       }
+      if (gradient_converged()) {
+        if (sum) sum->termination = 2;
+        break;
+      }
     } else {
       swap_state();
       radius /= decrease_factor;
@@ -1236,7 +1620,7 @@ int reducedSystemDense(Problem& p, const mba_solver_options& o, double radius, d
   Scaled sc;
   std::vector<double> nkf, nlm, nsw;
   columnNorms(p, L, nkf, nlm, nsw);
-  sc.skf.assign(15 * p.nkf, 1.0);
+  sc.skf.assign(15 * (p.nkf + p.ng), 1.0);
   sc.slm.assign(3 * p.nlm, 1.0);
   sc.ssw.assign(p.sw.size(), 1.0);
   if (o.jacobi_scaling) {
@@ -1244,7 +1628,7 @@ int reducedSystemDense(Problem& p, const mba_solver_options& o, double radius, d
     for (size_t a = 0; a < nlm.size(); ++a) sc.slm[a] = 1.0 / (1.0 + std::sqrt(nlm[a]));
     for (size_t a = 0; a < nsw.size(); ++a) sc.ssw[a] = 1.0 / (1.0 + std::sqrt(nsw[a]));
   }
-  std::vector<double> dkf(15 * p.nkf), dlm(3 * p.nlm), dsw(p.sw.size());
+  std::vector<double> dkf(15 * (p.nkf + p.ng)), dlm(3 * p.nlm), dsw(p.sw.size());
   for (size_t a = 0; a < nsw.size(); ++a)
     dsw[a] = std::min(std::max(nsw[a] * sc.ssw[a] * sc.ssw[a], o.min_lm_diagonal), o.max_lm_diagonal) / radius;
   for (size_t a = 0; a < nkf.size(); ++a)
@@ -1369,6 +1753,14 @@ int oracleReadState(Problem* p, double* kx, double* kv, double* kbg, double* kba
   if (kbg) std::memcpy(kbg, p->kf_bg.data(), p->kf_bg.size() * sizeof(double));
   if (kba) std::memcpy(kba, p->kf_ba.data(), p->kf_ba.size() * sizeof(double));
   if (lp) std::memcpy(lp, p->lm_p.data(), p->lm_p.size() * sizeof(double));
+  return 0;
+}
+
+// Cameras and mission baseframes of the current state (they move when the
+// descriptor leaves calibration or baseframe blocks free).
+int oracleReadCalibration(Problem* p, mba_camera* cams, double* mis) {
+  if (cams) std::memcpy(cams, p->cams.data(), p->cams.size() * sizeof(mba_camera));
+  if (mis) std::memcpy(mis, p->mis.data(), p->mis.size() * sizeof(double));
   return 0;
 }
 

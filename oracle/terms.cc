@@ -174,6 +174,57 @@ void equidistantParamJacobian(const double*, const double* pt, double* J) {
   J[7] = y * std::pow(theta, 9.0) * 1.0 / r;
 }
 
+void fovDistort(const double* k, double* pt, double* J) {
+  // FisheyeDistortion::distortUsingExternalCoefficients (distortion-fisheye.cc:14-80):
+  // the FOV model r_d = atan(2 tan(w / 2) r_u) / w with one parameter w.
+  const double w = k[0];
+  const double u = pt[0], v = pt[1];
+  const double r_u = std::sqrt(u * u + v * v);
+  const double r_u_cubed = r_u * r_u * r_u;
+  const double tanwhalf = std::tan(w / 2.0);
+  const double tanwhalfsq = tanwhalf * tanwhalf;
+  const double atan_wrd = std::atan(2.0 * tanwhalf * r_u);
+  double r_rd;
+  if (w * w < 1e-5) r_rd = 1.0;
+  else if (r_u * r_u < 1e-5) r_rd = 2.0 * tanwhalf / w;
+  else r_rd = atan_wrd / (r_u * w);
+  if (J) {
+    if (w * w < 1e-5) {
+      J[0] = 1.0; J[1] = 0.0; J[2] = 0.0; J[3] = 1.0;
+    } else if (r_u * r_u < 1e-5) {
+      J[0] = 2.0 * tanwhalf / w; J[1] = 0.0; J[2] = 0.0; J[3] = 2.0 * tanwhalf / w;
+    } else {
+      const double uv2 = u * u + v * v;
+      const double den = w * uv2 * (4 * tanwhalfsq * uv2 + 1);
+      J[0] = atan_wrd / (w * r_u) - (u * u * atan_wrd) / (w * r_u_cubed) + (2 * u * u * tanwhalf) / den;
+      J[1] = (2 * u * v * tanwhalf) / den - (u * v * atan_wrd) / (w * r_u_cubed);
+      J[2] = (2 * u * v * tanwhalf) / den - (u * v * atan_wrd) / (w * r_u_cubed);
+      J[3] = atan_wrd / (w * r_u) - (v * v * atan_wrd) / (w * r_u_cubed) + (2 * v * v * tanwhalf) / den;
+    }
+  }
+  pt[0] = u * r_rd;
+  pt[1] = v * r_rd;
+}
+
+void fovParamJacobian(const double* k, const double* pt, double* J) {
+  // FisheyeDistortion::distortParameterJacobian (distortion-fisheye.cc:82-110):
+  // 2 x 1 in columns 0 of the 2 x 4 block, the other columns zero.
+  const double w = k[0];
+  const double tanwhalf = std::tan(w / 2.0);
+  const double tanwhalfsq = tanwhalf * tanwhalf;
+  const double u = pt[0], v = pt[1];
+  const double r_u = std::sqrt(u * u + v * v);
+  const double atan_wrd = std::atan(2.0 * tanwhalf * r_u);
+  for (int i = 0; i < 8; ++i) J[i] = 0.0;
+  if (w * w < 1e-5) return;
+  if (r_u * r_u < 1e-5) {
+    J[0] = J[4] = (w - std::sin(w)) / (w * w * std::cos(w / 2) * std::cos(w / 2));
+    return;
+  }
+  J[0] = (2 * u * (tanwhalfsq / 2 + 0.5)) / (w * (4 * tanwhalfsq * r_u * r_u + 1)) - (u * atan_wrd) / (w * w * r_u);
+  J[4] = (2 * v * (tanwhalfsq / 2 + 0.5)) / (w * (4 * tanwhalfsq * r_u * r_u + 1)) - (v * atan_wrd) / (w * w * r_u);
+}
+
 // ---------------------------------------------------------------- camera
 int pinholeProject3(const mba_camera& cam, const double* p, double* kp, double* Jp, double* Ji,
                     double* Jd) {
@@ -188,11 +239,13 @@ int pinholeProject3(const mba_camera& cam, const double* p, double* kp, double* 
   if (Jd) {
     if (cam.distortion_type == MBA_DISTORTION_RADTAN) radtanParamJacobian(cam.distortion, kp, Jd);
     else if (cam.distortion_type == MBA_DISTORTION_EQUIDISTANT) equidistantParamJacobian(cam.distortion, kp, Jd);
+    else if (cam.distortion_type == MBA_DISTORTION_FOV) fovParamJacobian(cam.distortion, kp, Jd);
     else for (int i = 0; i < 8; ++i) Jd[i] = 0.0;
     for (int i = 0; i < 4; ++i) { Jd[i] *= fu; Jd[4 + i] *= fv; }
   }
   if (cam.distortion_type == MBA_DISTORTION_RADTAN) radtanDistort(cam.distortion, kp, Jp ? Jdist : nullptr);
   else if (cam.distortion_type == MBA_DISTORTION_EQUIDISTANT) equidistantDistort(cam.distortion, kp, Jp ? Jdist : nullptr);
+  else if (cam.distortion_type == MBA_DISTORTION_FOV) fovDistort(cam.distortion, kp, Jp ? Jdist : nullptr);
   if (Jp) {
     const double rz2 = rz * rz;
     Jp[0] = fu * Jdist[0] * rz;

@@ -36,6 +36,7 @@ def load():
         "oracle_linearize_visual": (ctypes.c_int, [vp, dp, dp, dp, dp, dp]),
         "oracle_solve": (ctypes.c_int, [vp, ctypes.POINTER(N.SolverOptions), ctypes.POINTER(N.Summary)]),
         "oracle_read_state": (ctypes.c_int, [vp, dp, dp, dp, dp, dp]),
+        "oracle_read_calibration": (ctypes.c_int, [vp, ctypes.POINTER(N.Camera), dp]),
         "oracle_linearize_pose_edges": (ctypes.c_int, [vp, dp, dp, dp]),
         "oracle_pose_edge": (ctypes.c_int, [dp, dp, dp, dp, dp, dp, dp, dp]),
         "oracle_loop_closure": (ctypes.c_int, [dp, dp, dp, dp, dp, dp, dp, dp, dp]),
@@ -167,6 +168,14 @@ class OracleProblem:
         lp = np.zeros((d.num_landmarks, 3))
         self.lib.oracle_read_state(self.h, N.ptr(kx), N.ptr(kv), N.ptr(kbg), N.ptr(kba), N.ptr(lp))
         return dict(kf_q_IM_p_MI=kx, kf_v_M=kv, kf_b_g=kbg, kf_b_a=kba, lm_p_B=lp)
+
+    def read_calibration(self):
+        """Cameras and mission baseframes of the current state."""
+        d = self.desc
+        cams = (N.Camera * d.num_cameras)()
+        mis = np.zeros((d.num_missions, 7))
+        self.lib.oracle_read_calibration(self.h, cams, N.ptr(mis))
+        return N.calibration_dict(cams, mis)
 
     def write_state(self, st):
         self.lib.oracle_write_state(self.h, N.ptr(st.get("kf_q_IM_p_MI")), N.ptr(st.get("kf_v_M")),

@@ -13,7 +13,7 @@ class OwnedDesc:
                  kf_q_IM_p_MI, kf_v_M=None, kf_b_g=None, kf_b_a=None, kf_mission=None, kf_flags=None,
                  mission_q_GM_p_GM=None, cameras=(), lm_constant=None, edge_from=None, edge_to=None,
                  edge_sample_offset=None, imu_timestamp_ns=None, imu_acc_gyro=None, imu_sigmas=(0.1, 0.1, 0.1, 0.1),
-                 gravity=9.81, use_huber=1):
+                 gravity=9.81, use_huber=1, camera_flags=None, mission_flags=None):
         f64 = lambda a: np.ascontiguousarray(np.asarray(a, dtype=np.float64))
         i32 = lambda a: np.ascontiguousarray(np.asarray(a, dtype=np.int32))
         nk = len(kf_q_IM_p_MI)
@@ -77,6 +77,12 @@ class OwnedDesc:
         d.use_huber = use_huber
         d.huber_delta_local = 3.0
         d.huber_delta_global = 10.0
+        if camera_flags is not None:
+            a["camera_flags"] = np.ascontiguousarray(np.asarray(camera_flags, dtype=np.uint32))
+            d.camera_flags = N.ptr(a["camera_flags"], ctypes.c_uint32)
+        if mission_flags is not None:
+            a["mission_flags"] = np.ascontiguousarray(np.asarray(mission_flags, dtype=np.uint32))
+            d.mission_flags = N.ptr(a["mission_flags"], ctypes.c_uint32)
         self.desc = d
 
 

@@ -110,19 +110,17 @@ def _build_visual(fam, sc):
     qci, pci = res[0]["q_CI"], res[0]["p_CI"]
     assert all(r["q_CI"] == qci and r["p_CI"] == pci for r in res)
     cam = sc["camera"]
-    requires = []
-    w = cam["fisheye_w"]
-    if w * w >= 1e-5:
-        requires.append("fisheye distortion")
-    for name, what in (("intrinsics", "intrinsics"), ("distortion", "distortion"), (qci, "extrinsics rotation"),
-                       (pci, "extrinsics translation")):
+    # The camera's blocks the test leaves free become variables; baseframes
+    # free in the test use the 6-dof JplPoseParameterization it sets.
+    cam_flags = 0
+    for name, bit in (("intrinsics", N.MBA_CAM_INTRINSICS_FREE), ("distortion", N.MBA_CAM_DISTORTION_FREE),
+                      (qci, N.MBA_CAM_ROTATION_FREE), (pci, N.MBA_CAM_TRANSLATION_FREE)):
         if name not in const:
-            requires.append(what)
-    for m in mission_names:
-        if m not in const:
-            requires.append("baseframe")
+            cam_flags |= bit
+    mis_flags = [0 if m in const else N.MBA_MIS_BASEFRAME_POSE for m in mission_names]
+    w = cam["fisheye_w"]
     c = camera(fu=cam["intrinsics"][0], fv=cam["intrinsics"][1], cu=cam["intrinsics"][2], cv=cam["intrinsics"][3],
-               w=int(cam["width"]), h=int(cam["height"]), dtype=N.MBA_DISTORTION_NONE, dist=(0, 0, 0, 0),
+               w=int(cam["width"]), h=int(cam["height"]), dtype=N.MBA_DISTORTION_FOV, dist=(w, 0, 0, 0),
                q_CI=B[qci], p_CI=B[pci])
     # the fixture's quaternion block is used as given (a unit quaternion)
     for i in range(4):
@@ -133,13 +131,14 @@ def _build_visual(fam, sc):
                    obs_keyframe=[kfs.index(r["imu_pose"]) for r in res], obs_camera=[0] * len(res),
                    lm_p_B=[block(l) for l in lms], lm_store_keyframe=[kfs.index(base_of[l]) for l in lms],
                    lm_constant=[1 if l in const else 0 for l in lms], kf_q_IM_p_MI=[B[k] for k in kfs],
-                   kf_mission=kf_mission, kf_flags=flags, mission_q_GM_p_GM=missions, cameras=[c], use_huber=0)
+                   kf_mission=kf_mission, kf_flags=flags, mission_q_GM_p_GM=missions, cameras=[c], use_huber=0,
+                   camera_flags=[cam_flags], mission_flags=mis_flags)
     where = {k: ("kf", i) for i, k in enumerate(kfs)}
     where.update({l: ("lm", i) for i, l in enumerate(lms)})
     where.update({"intrinsics": ("cam", "intrinsics"), "distortion": ("cam", "distortion"), qci: ("cam", "q_CI"),
                   pci: ("cam", "p_CI")})
     where.update({m: ("mis", i) for i, m in enumerate(mission_names)})
-    return Built(od, where, requires)
+    return Built(od, where, [])
 
 
 def _build_inertial(fam, sc):
@@ -257,8 +256,8 @@ def check(built, sc, summary, state, calibration=None):
             return np.asarray(state[key][i])
         if calibration is None:
             raise KeyError(name)
-        if kind == "cam":
-            return np.asarray(calibration[i])
+        if kind == "cam":  # the scenarios have one camera
+            return np.asarray(calibration[i][0])
         return np.asarray(calibration["baseframes"][i])
 
     for e in sc["expect"]:

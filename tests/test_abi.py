@@ -120,7 +120,7 @@ def test_create_rejects_unordered_imu_on_host():
 def test_status_strings_and_defaults():
     lib = N.load_ba()
     assert lib.mba_status_string(N.MBA_ERR_NOT_SPD) == b"matrix not positive definite"
-    assert lib.mba_abi_version() == 1
+    assert lib.mba_abi_version() == 2
     o = N.SolverOptions()
     lib.mba_default_solver_options(ctypes.byref(o))
     ref = N.default_solver_options()

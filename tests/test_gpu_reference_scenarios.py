@@ -26,5 +26,6 @@ def test_reference_scenario_on_the_device(item):
     with ba.BundleAdjuster(b.desc) as g:
         s = g.solve(R.solver_options(ba.default_options, device=True))
         st = g.read_state()
-    fails = R.check(b, sc, s, st)
+        cal = g.read_calibration()
+    fails = R.check(b, sc, s, st, cal)
     assert not fails, fails

@@ -34,5 +34,5 @@ def test_reference_scenario_on_the_oracle(item):
         pytest.skip("needs " + ", ".join(b.requires))
     o = O.OracleProblem(b.desc)
     s = o.solve(R.solver_options(N.default_solver_options, device=False))
-    fails = R.check(b, sc, s, o.read_state())
+    fails = R.check(b, sc, s, o.read_state(), o.read_calibration())
     assert not fails, fails
