@@ -2272,7 +2272,7 @@ mba_status autotune(mba_handle* h, mba_tuning* out) {
         P.vis_block = bs;
         P.vis_minb = minb;
         P.vis_pipe = pipe;
-        const double t = time_ms(st, 2, 8, [&]() { launch_visual_linearize<T>(P, b.vis, nullptr, st); });
+        const double t = time_ms(st, 1, 3, [&]() { launch_visual_linearize<T>(P, b.vis, nullptr, st); });
         if (t < tbest) {
           tbest = t;
           best.visual_block = bs;
@@ -2285,15 +2285,16 @@ mba_status autotune(mba_handle* h, mba_tuning* out) {
   h->P.vis_block = best.visual_block;
   h->P.vis_minb = best.visual_min_blocks;
   h->P.vis_pipe = best.visual_pipelined == 1;
-  // Schur pairs per thread
+  // Schur pairs per thread (each candidate re-cuts the pair chunks on the
+  // host; chunks below 16 pairs have not won on any map measured)
   tbest = 1e30;
-  for (int chunk : {4, 8, 16, 32, 64}) {
-    if ((ms = apply_schur_chunk(h, chunk)) != MBA_OK) return ms;
+  for (int chunk : {16, 32, 64}) {
+    if (chunk != h->tuning.schur_chunk && (ms = apply_schur_chunk(h, chunk)) != MBA_OK) return ms;
     SolverLaunch<T> sc = make_launch<T>(h, b, o);
-    const double t = time_ms(st, 1, 5, [&]() { solver_schur_pairs<T>(sc, st); });
+    const double t = time_ms(st, 1, 2, [&]() { solver_schur_pairs<T>(sc, st); });
     if (t < tbest) { tbest = t; best.schur_chunk = chunk; best.schur_ms = t; }
   }
-  if ((ms = apply_schur_chunk(h, best.schur_chunk)) != MBA_OK) return ms;
+  if (best.schur_chunk != h->tuning.schur_chunk && (ms = apply_schur_chunk(h, best.schur_chunk)) != MBA_OK) return ms;
   // single-block tail of the chain sweeps (the factorization from the build is reused)
   tbest = 1e30;
   const int levels = h->S.chain_levels;
