@@ -200,11 +200,15 @@ __device__ __forceinline__ double compute_obs(const DevProblem& P, const VisualI
   } else {
     r[0] = (kp[0] - uv.x) * sinv;
     r[1] = (kp[1] - uv.y) * sinv;
+    // Every Jacobian block is linear in the projection Jacobian: scale it by
+    // 1 / sigma once instead of each of the 32 outputs.
+#pragma unroll
+    for (int a = 0; a < 6; ++a) Jkp[a] *= sinv;
     T A[6];
-    m23x33(Jkp, RCI, A);  // Jkp * R_C_I
+    m23x33(Jkp, RCI, A);  // Jkp * R_C_I / sigma
     if (type == MBA_LOCAL_KEYFRAME) {
 #pragma unroll
-      for (int a = 0; a < 6; ++a) Jl[a] = A[a] * sinv;
+      for (int a = 0; a < 6; ++a) Jl[a] = A[a];
     } else {
       T B[6], Cp[6];
       m23x33(A, RIM, B);  // Jkp R_C_I R_I_M  (= -J_p_M_I)
@@ -226,22 +230,52 @@ __device__ __forceinline__ double compute_obs(const DevProblem& P, const VisualI
       T Jqs[6], Jqo[6];
       m23xskew(JpB, pB, Jqs);  // -J_q_B_LM
       m23xskew(A, pI, Jqo);    // J_q_I_M
-      M3<T> Bs, Bo;
-      rot_basis<T>(P, in.mis, st, qst, RBLM, Bs);
-      rot_basis<T>(P, in.mis, kf, qob, RIM, Bo);
       const uint16_t ms = P.kf_mask[st], mo = P.kf_mask[kf];
+      // Rotation tangent: J_theta * B.  B = |q|^2 I (masked columns zero) for
+      // JplQuaternionParameterization, a full 3 x 2 basis only for the
+      // gauge keyframe's roll / pitch parameterization; the scaled identity
+      // is applied as a scalar (same products, fewer instructions).
+      const bool rps = P.kf_flags[st] & MBA_KF_GAUGE_ROLL_PITCH, rpo = P.kf_flags[kf] & MBA_KF_GAUGE_ROLL_PITCH;
+      if (!rps) {
+        const T n2 = qst[0] * qst[0] + qst[1] * qst[1] + qst[2] * qst[2] + qst[3] * qst[3];
+#pragma unroll
+        for (int rr = 0; rr < 2; ++rr)
+#pragma unroll
+          for (int c = 0; c < 3; ++c) Js[6 * rr + c] = (ms & (1u << c)) ? -(Jqs[3 * rr + c] * n2) : T(0);
+      } else {
+        M3<T> Bs;
+        rot_basis<T>(P, in.mis, st, qst, RBLM, Bs);
+#pragma unroll
+        for (int rr = 0; rr < 2; ++rr)
+#pragma unroll
+          for (int c = 0; c < 3; ++c)
+            Js[6 * rr + c] = -(Jqs[3 * rr] * Bs.m[c] + Jqs[3 * rr + 1] * Bs.m[3 + c] + Jqs[3 * rr + 2] * Bs.m[6 + c]);
+      }
+      if (!rpo) {
+        const T n2 = qob[0] * qob[0] + qob[1] * qob[1] + qob[2] * qob[2] + qob[3] * qob[3];
+#pragma unroll
+        for (int rr = 0; rr < 2; ++rr)
+#pragma unroll
+          for (int c = 0; c < 3; ++c) Jo[6 * rr + c] = (mo & (1u << c)) ? (Jqo[3 * rr + c] * n2) : T(0);
+      } else {
+        M3<T> Bo;
+        rot_basis<T>(P, in.mis, kf, qob, RIM, Bo);
+#pragma unroll
+        for (int rr = 0; rr < 2; ++rr)
+#pragma unroll
+          for (int c = 0; c < 3; ++c)
+            Jo[6 * rr + c] = (Jqo[3 * rr] * Bo.m[c] + Jqo[3 * rr + 1] * Bo.m[3 + c] + Jqo[3 * rr + 2] * Bo.m[6 + c]);
+      }
 #pragma unroll
       for (int rr = 0; rr < 2; ++rr) {
 #pragma unroll
         for (int c = 0; c < 3; ++c) {
-          Js[6 * rr + c] = -(Jqs[3 * rr] * Bs.m[c] + Jqs[3 * rr + 1] * Bs.m[3 + c] + Jqs[3 * rr + 2] * Bs.m[6 + c]) * sinv;
-          Jo[6 * rr + c] = (Jqo[3 * rr] * Bo.m[c] + Jqo[3 * rr + 1] * Bo.m[3 + c] + Jqo[3 * rr + 2] * Bo.m[6 + c]) * sinv;
-          Js[6 * rr + 3 + c] = (ms & (8u << c)) ? Cp[3 * rr + c] * sinv : T(0);
-          Jo[6 * rr + 3 + c] = (mo & (8u << c)) ? -B[3 * rr + c] * sinv : T(0);
+          Js[6 * rr + 3 + c] = (ms & (8u << c)) ? Cp[3 * rr + c] : T(0);
+          Jo[6 * rr + 3 + c] = (mo & (8u << c)) ? -B[3 * rr + c] : T(0);
         }
       }
 #pragma unroll
-      for (int a = 0; a < 6; ++a) Jl[a] = JpB[a] * sinv;
+      for (int a = 0; a < 6; ++a) Jl[a] = JpB[a];
     }
     if (!o.lm_active) {
 #pragma unroll
@@ -249,7 +283,10 @@ __device__ __forceinline__ double compute_obs(const DevProblem& P, const VisualI
     }
   }
   const T s = r[0] * r[0] + r[1] * r[1];
-  if (ha > T(0)) {
+  // Inside the Huber threshold (s <= a^2) the loss is the identity: rho' = 1,
+  // rho'' = 0, so the corrector leaves r and J unchanged and the cost is s / 2.
+  // Only observations beyond it pay for the correction.
+  if (ha > T(0) && s > ha * ha) {
     T rho0, sq1, rs, as;
     huber_corrector<T>(ha, s, &rho0, &sq1, &rs, &as);
     if (kCost) cost = 0.5 * double(rho0);
