@@ -433,6 +433,12 @@ mba_status mba_gnn_gradient(mba_handle* h, mba_gnn* m, double radius, int32_t np
  * among the 2 N_pu oriented blocks (upper j < N_pu, else the transpose of
  * upper j - N_pu; -1: none).  Any pointer may be NULL. */
 mba_status mba_chain_structure(mba_handle* h, int32_t* perm, int32_t* link_edge, int32_t* link_blk);
+/* z = T^-1 r for the exact chain matrix T (gamma = 1, alpha = 0) of the
+ * reduced system at the current state (built as mba_reduced_system does, with
+ * trust-region radius `radius`), through the handle's chain sweeps.  r and z
+ * [N_kf][15] in keyframe order, host memory.  MBA_ERR_NOT_SPD if a pivot of
+ * the factorization failed.  For checking the sweeps. */
+mba_status mba_chain_apply(mba_handle* h, int32_t precision, double radius, const double* r, double* z);
 
 /* Launch and schedule parameters of one problem (no reference counterpart).
  * mba_autotune times each candidate on the handle's own data with CUDA
@@ -448,7 +454,9 @@ typedef struct mba_tuning {
   double chain_apply_ms;
   int32_t visual_pipelined;     /* 1: software-pipelined persistent evaluation kernel, 2: one thread per
                                  * observation (0 in mba_set_tuning keeps the current setting) */
-  int32_t pad_;
+  int32_t chain_segment;        /* chain sweeps: positions one block takes through the lower levels (a power
+                                 * of two from 2 to 128; three launches per apply), or 1: one launch per
+                                 * level (0 in mba_set_tuning keeps the current setting) */
 } mba_tuning;
 mba_status mba_autotune(mba_handle* h, int32_t precision, mba_tuning* out);
 /* Applies tuning values (e.g. cached from an earlier mba_autotune of a

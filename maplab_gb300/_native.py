@@ -246,7 +246,7 @@ class Tuning(ctypes.Structure):
         ("schur_ms", ctypes.c_double),
         ("chain_apply_ms", ctypes.c_double),
         ("visual_pipelined", ctypes.c_int32),
-        ("pad_", ctypes.c_int32),
+        ("chain_segment", ctypes.c_int32),
     ]
 
 
@@ -416,6 +416,7 @@ def load_ba():
     _declare(lib, "mba_autotune", ctypes.c_int, [vp, ctypes.c_int32, ctypes.POINTER(Tuning)])
     _declare(lib, "mba_set_tuning", ctypes.c_int, [vp, ctypes.POINTER(Tuning)])
     _declare(lib, "mba_chain_structure", ctypes.c_int, [vp, i32p, i32p, i32p])
+    _declare(lib, "mba_chain_apply", ctypes.c_int, [vp, ctypes.c_int32, ctypes.c_double, c_double_p, c_double_p])
     _declare(lib, "mba_rejected_landmarks", ctypes.c_int, [vp, ctypes.POINTER(ctypes.c_uint8), ctypes.POINTER(ctypes.c_int64)])
     _declare(lib, "mba_reduced_system", ctypes.c_int,
              [vp, ctypes.c_int32, ctypes.c_double, c_double_p, ctypes.POINTER(ctypes.c_int32), c_double_p,

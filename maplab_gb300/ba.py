@@ -298,6 +298,13 @@ class BundleAdjuster:
         _check(self._lib.mba_chain_structure(self._h, p(perm), p(le), p(lb)), "mba_chain_structure")
         return perm, le, lb
 
+    def chain_apply(self, r, precision=N.MBA_PRECISION_FP64, radius=1e5):
+        """z = T^-1 r with the exact chain matrix of the current reduced system."""
+        r = np.ascontiguousarray(r, dtype=np.float64).reshape(self.desc.num_keyframes, 15)
+        z = np.zeros_like(r)
+        _check(self._lib.mba_chain_apply(self._h, precision, radius, N.ptr(r), N.ptr(z)), "mba_chain_apply")
+        return z
+
     def cancel(self):
         self._lib.mba_cancel(self._h)
 

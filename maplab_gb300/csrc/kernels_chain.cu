@@ -13,6 +13,15 @@
 // by level, z(0) = F(0) w(0), back sweep z(p) = F(p) (w(p) - CL(p) z(p-s) -
 // CR(p) z(p+s)).  The levels with at most kTailNodes active positions run in
 // one block (one launch) instead of one launch per level.
+//
+// Segmented sweeps (chain_seg = m > 0): block j owns positions
+// [j 2^m, (j+1) 2^m) and runs the forward levels 0..m-1 in shared memory.
+// The first position q of a segment is a survivor of all those levels and
+// nobody reads its w before level m, so its left-neighbour terms
+// sum_l XR(q - 2^l) w(q - 2^l) (positions of the previous segment, final once
+// that segment is swept) are left in lc and subtracted by the tail, which runs
+// levels m.. in one block.  The back sweep of levels m-1..0 again runs per
+// segment.  Three launches per apply instead of one per level.
 #include <cuda_runtime.h>
 
 #include "solver.h"
@@ -339,8 +348,10 @@ __global__ void __launch_bounds__(128) k_chain_bwd(SolverLaunch<T> s, int l, con
 }
 
 // Levels l0.. in one block: forward sweeps, the last survivor, back sweeps.
+// seg > 0: the segments' first positions take their left-neighbour terms from
+// lc first (segmented sweeps, l0 = seg).
 template <typename T>
-__global__ void __launch_bounds__(kTailThreads) k_chain_tail(SolverLaunch<T> s, int l0, const T* rv, T* z,
+__global__ void __launch_bounds__(kTailThreads) k_chain_tail(SolverLaunch<T> s, int l0, int seg, const T* rv, T* z,
                                                              double* rz) {
   if (apply_gate(s.ctl)) return;
   __shared__ T tsh[kTailThreads];
@@ -349,6 +360,11 @@ __global__ void __launch_bounds__(kTailThreads) k_chain_tail(SolverLaunch<T> s, 
   const int grp = threadIdx.x >> 4, r = threadIdx.x & 15;
   const int ngrp = kTailThreads / 16;
   const unsigned mask = 0xffffu << (threadIdx.x & 16);
+  if (seg > 0) {
+    for (int64_t j = 1 + grp; (j << seg) < n; j += ngrp)
+      if (r < 15) s.C.w[15 * (j << seg) + r] -= s.C.lc[15 * j + r];
+    __syncthreads();
+  }
   for (int l = l0; l < L; ++l) {
     const int64_t st = (int64_t)1 << l, cnt = (n + 2 * st - 1) / (2 * st);
     for (int64_t j = grp; j < cnt; j += ngrp) fwd_node(s, st, j, r);
@@ -370,6 +386,102 @@ __global__ void __launch_bounds__(kTailThreads) k_chain_tail(SolverLaunch<T> s, 
     const int64_t st = (int64_t)1 << l, cnt = n > st ? (n - st + 2 * st - 1) / (2 * st) : 0;
     const int64_t passes = (cnt + ngrp - 1) / ngrp;
     for (int64_t q = 0; q < passes; ++q) acc += bwd_node(s, st, grp + q * ngrp, r, rv, z, tsh + 16 * grp, mask);
+    __syncthreads();
+  }
+  block_add_d(acc, rz);
+}
+
+constexpr int kSegThreads = 256;  // 16 positions at a time, thread r of a position owns row r
+
+// Segmented forward sweep: block j runs levels 0..m-1 on positions
+// [j 2^m, (j+1) 2^m) in shared memory (16 values per position), writes w and
+// the next segment's left-neighbour terms lc[j + 1].
+template <typename T>
+__global__ void __launch_bounds__(kSegThreads) k_chain_seg_fwd(SolverLaunch<T> s, int m, const T* rv) {
+  if (apply_gate(s.ctl)) return;
+  extern __shared__ __align__(16) unsigned char seg_smem[];
+  T* ws = reinterpret_cast<T*>(seg_smem);  // [2^m][16]
+  const int64_t n = s.P.nkf, base = (int64_t)blockIdx.x << m;
+  const int64_t left = n - base;
+  const int cnt = left < ((int64_t)1 << m) ? (int)left : (1 << m);
+  const int grp = threadIdx.x >> 4, r = threadIdx.x & 15, ngrp = kSegThreads / 16;
+  for (int i = threadIdx.x; i < 16 * cnt; i += kSegThreads) {
+    const int p = i >> 4, c = i & 15;
+    ws[i] = c < 15 ? rv[15 * (int64_t)s.S.chain_perm[base + p] + c] : T(0);
+  }
+  __syncthreads();
+  for (int l = 0; l < m; ++l) {
+    const int st = 1 << l, ns = (cnt + 2 * st - 1) / (2 * st);
+    for (int j = grp; j < ns; j += ngrp) {
+      const int q = 2 * st * j;  // survivor; q - st and q + st were eliminated at level l
+      if (r < 15) {
+        T v = ws[16 * q + r];
+        if (q >= st) v -= row_dot(s.C.XR + 225 * (base + q - st), r, ws + 16 * (q - st));
+        if (q + st < cnt) v -= row_dot(s.C.XL + 225 * (base + q + st), r, ws + 16 * (q + st));
+        ws[16 * q + r] = v;
+      }
+    }
+    __syncthreads();
+  }
+  for (int i = threadIdx.x; i < 16 * cnt; i += kSegThreads)
+    if ((i & 15) < 15) s.C.w[15 * base + 15 * (i >> 4) + (i & 15)] = ws[i];
+  // Terms of the next segment's first position q' = base + 2^m from this
+  // segment's positions q' - 2^l (eliminated at level l, final now).
+  if (grp == 0 && r < 15 && cnt == (1 << m) && base + cnt < n) {
+    T v = T(0);
+    for (int l = 0; l < m; ++l) {
+      const int p = cnt - (1 << l);
+      v += row_dot(s.C.XR + 225 * (base + p), r, ws + 16 * p);
+    }
+    s.C.lc[15 * ((int64_t)blockIdx.x + 1) + r] = v;
+  }
+}
+
+// Segmented back sweep: block j runs levels m-1..0 on its segment; the
+// segment's first position and the next segment's first position were solved
+// by the tail.  Writes z of the eliminated positions and adds their r.z.
+template <typename T>
+__global__ void __launch_bounds__(kSegThreads) k_chain_seg_bwd(SolverLaunch<T> s, int m, const T* rv, T* z,
+                                                               double* rz) {
+  if (apply_gate(s.ctl)) return;
+  extern __shared__ __align__(16) unsigned char seg_smem[];
+  const int seg = 1 << m;
+  T* ws = reinterpret_cast<T*>(seg_smem);  // [2^m][16] w, then the solve's right-hand side
+  T* zs = ws + 16 * seg;                   // [2^m + 1][16] z in position order
+  const int64_t n = s.P.nkf, base = (int64_t)blockIdx.x << m;
+  const int64_t left = n - base;
+  const int cnt = left < (int64_t)seg ? (int)left : seg;
+  const int grp = threadIdx.x >> 4, r = threadIdx.x & 15, ngrp = kSegThreads / 16;
+  const unsigned mask = 0xffffu << (threadIdx.x & 16);
+  for (int i = threadIdx.x; i < 16 * cnt; i += kSegThreads)
+    ws[i] = (i & 15) < 15 ? s.C.w[15 * base + 15 * (i >> 4) + (i & 15)] : T(0);
+  if (threadIdx.x < 15) zs[threadIdx.x] = z[15 * (int64_t)s.S.chain_perm[base] + threadIdx.x];
+  if (threadIdx.x >= 16 && threadIdx.x < 31 && base + seg < n)
+    zs[16 * seg + threadIdx.x - 16] = z[15 * (int64_t)s.S.chain_perm[base + seg] + threadIdx.x - 16];
+  __syncthreads();
+  double acc = 0.0;
+  for (int l = m - 1; l >= 0; --l) {
+    const int st = 1 << l, ne = cnt > st ? (cnt - st + 2 * st - 1) / (2 * st) : 0;
+    const int passes = (ne + ngrp - 1) / ngrp;
+    for (int q = 0; q < passes; ++q) {
+      const int p = st + 2 * st * (grp + q * ngrp);
+      const bool act = p < cnt && r < 15;
+      if (act) {
+        T v = ws[16 * p + r];
+        v -= row_dot(s.C.CL + 225 * (base + p), r, zs + 16 * (p - st));
+        if (base + p + st < n) v -= row_dot(s.C.CR + 225 * (base + p), r, zs + 16 * (p + st));
+        ws[16 * p + r] = v;
+      }
+      __syncwarp(mask);
+      if (act) {
+        const T zr = row_dot(s.C.F + 225 * (base + p), r, ws + 16 * p);
+        zs[16 * p + r] = zr;
+        const int64_t k = s.S.chain_perm[base + p];
+        z[15 * k + r] = zr;
+        acc += (double)rv[15 * k + r] * (double)zr;
+      }
+      __syncwarp(mask);
+    }
     __syncthreads();
   }
   block_add_d(acc, rz);
@@ -413,12 +525,21 @@ cudaError_t chain_apply(const SolverLaunch<T>& s, const T* r, T* z, double* rz, 
   const int64_t n = s.P.nkf;
   if (!n) return cudaSuccess;
   const int L = s.S.chain_levels, l0 = s.S.chain_tail;
+  if (s.S.chain_seg > 0) {
+    const int m = s.S.chain_seg;
+    const unsigned blocks = nb(n, 1 << m);
+    const size_t sm = sizeof(T) * 16 * (size_t)(1 << m);
+    k_chain_seg_fwd<T><<<blocks, kSegThreads, sm, st>>>(s, m, r);
+    k_chain_tail<T><<<1, kTailThreads, 0, st>>>(s, m, m, r, z, rz);
+    k_chain_seg_bwd<T><<<blocks, kSegThreads, 2 * sm + sizeof(T) * 16, st>>>(s, m, r, z, rz);
+    return cudaGetLastError();
+  }
   k_chain_fwd0<T><<<nb(16 * n, 128), 128, 0, st>>>(s, r);
   for (int l = 1; l < l0; ++l) {
     const int64_t sd = (int64_t)1 << l, ns = (n + 2 * sd - 1) / (2 * sd);
     k_chain_fwd<T><<<nb(16 * ns, 128), 128, 0, st>>>(s, l);
   }
-  k_chain_tail<T><<<1, kTailThreads, 0, st>>>(s, l0 < 1 ? 1 : l0, r, z, rz);
+  k_chain_tail<T><<<1, kTailThreads, 0, st>>>(s, l0 < 1 ? 1 : l0, 0, r, z, rz);
   for (int l = (l0 < 1 ? 1 : l0) - 1; l >= 0; --l) {
     const int64_t sd = (int64_t)1 << l, ne = n > sd ? (n - sd + 2 * sd - 1) / (2 * sd) : 0;
     if (ne) k_chain_bwd<T><<<nb(16 * ne, 128), 128, 0, st>>>(s, l, r, z, rz);

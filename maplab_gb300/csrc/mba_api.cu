@@ -351,6 +351,7 @@ mba_status ensure_chain_buffers(mba_handle* h, SolverBuffers<T>& b) {
     C.XR = A.alloc<T>(225 * n);
   }
   C.w = A.alloc<T>(15 * n);
+  C.lc = A.alloc<T>(15 * n + 15);
   C.coef = A.alloc<double>(3 * n);
   C.comp = A.alloc<double>(6 * n);
   if (A.err != cudaSuccess) return MBA_ERR_CUDA;
@@ -737,6 +738,36 @@ mba_status reduced_system(mba_handle* h, double radius, double* diag, int32_t* u
   int status = 0;
   cudaMemcpy(&status, &h->ctl->status, sizeof(int), cudaMemcpyDeviceToHost);
   return status ? (mba_status)status : MBA_OK;
+}
+
+// z = T^-1 r with the exact chain matrix T (gamma = 1, alpha = 0) of the
+// reduced system at the current state, through the configured sweeps.
+template <typename T>
+mba_status chain_apply_host(mba_handle* h, double radius, const double* r, double* z) {
+  mba_status ms = ensure_common_solver(h, 2);
+  if (ms != MBA_OK) return ms;
+  SolverBuffers<T>& b = buffers_of<T>(h);
+  if ((ms = ensure_solver_buffers<T>(h, b)) != MBA_OK) return ms;
+  if ((ms = ensure_chain_buffers<T>(h, b)) != MBA_OK) return ms;
+  mba_solver_options o;
+  mba_default_solver_options(&o);
+  o.preconditioner = MBA_PRECOND_CHAIN;
+  SolverLaunch<T> s = make_launch<T>(h, b, o);
+  cudaStream_t st = h->stream;
+  const int64_t n = 15 * h->P.nkf;
+  std::vector<T> rt(n);
+  for (int64_t i = 0; i < n; ++i) rt[i] = T(r[i]);
+  cudaError_t e = chain_default_coef(b.C.coef, h->P.nkf, st);
+  if (e == cudaSuccess) e = solver_init_control(h->ctl, radius, st);
+  if (e == cudaSuccess) e = linearize_current<T>(h, b, s, o.jacobi_scaling, st);
+  if (e == cudaSuccess) e = solver_build_reduced<T>(s, st);
+  if (e == cudaSuccess) e = cudaMemcpyAsync(b.L.r, rt.data(), sizeof(T) * n, cudaMemcpyHostToDevice, st);
+  if (e == cudaSuccess) e = chain_apply<T>(s, b.L.r, b.L.z, &h->ctl->pcg_rz0, st);
+  if (e == cudaSuccess) e = copy_out<T>(z, b.L.z, n, st);
+  if (e != cudaSuccess) return MBA_ERR_CUDA;
+  int failed = 0;
+  if (cudaMemcpy(&failed, &h->ctl->chain_failed, sizeof(int), cudaMemcpyDeviceToHost) != cudaSuccess) return MBA_ERR_CUDA;
+  return failed ? MBA_ERR_NOT_SPD : MBA_OK;
 }
 
 void unpermute_soa(const std::vector<double>& sorted_soa, int64_t N, int comps, const std::vector<int64_t>& perm,
@@ -1455,6 +1486,7 @@ mba_status mba_create(const mba_problem_desc* d, int32_t device, mba_handle** ou
   h->tuning.visual_pipelined = 2;
   h->tuning.schur_chunk = (int32_t)kSchurChunk;
   h->tuning.chain_tail_nodes = 128;
+  h->tuning.chain_segment = 1;
   // Inertial scratch (kernels_inertial.cu): dt per step, end state per edge,
   // 4 RK4 stages x 15 values per step.
   P.ine_scratch = A.alloc<double>((NSMP - NIMU) + 16 * NIMU + 60 * (NSMP - NIMU) + 1);
@@ -1965,6 +1997,15 @@ mba_status mba_reduced_system(mba_handle* h, int32_t precision, double radius, d
   return reduced_system<double>(h, radius, diag, upper_ij, upper, inertial, rhs);
 }
 
+mba_status mba_chain_apply(mba_handle* h, int32_t precision, double radius, const double* r, double* z) {
+  if (!h || !r || !z || !(radius > 0.0)) return MBA_ERR_INVALID_ARG;
+  if (precision != MBA_PRECISION_FP64 && precision != MBA_PRECISION_MIXED) return MBA_ERR_INVALID_ARG;
+  if (h->P.nkf == 0) return MBA_ERR_INVALID_ARG;
+  cudaSetDevice(h->device);
+  if (precision == MBA_PRECISION_MIXED) return chain_apply_host<float>(h, radius, r, z);
+  return chain_apply_host<double>(h, radius, r, z);
+}
+
 mba_status mba_rejected_landmarks(mba_handle* h, uint8_t* flags, int64_t* count) {
   if (!h) return MBA_ERR_INVALID_ARG;
   cudaSetDevice(h->device);
@@ -2206,6 +2247,14 @@ int chain_tail_level(int64_t n, int levels, int64_t nodes) {
   return l;
 }
 
+// Segment of the chain sweeps (positions per block, a power of two up to 128)
+// -> its level; 1 -> 0 (one launch per level).
+int chain_segment_level(int seg) {
+  int m = 0;
+  while ((1 << m) < seg) ++m;
+  return m;
+}
+
 mba_status apply_schur_chunk(mba_handle* h, int chunk) {
   std::vector<int32_t> tgt, len;
   std::vector<int64_t> beg, rco;
@@ -2298,13 +2347,22 @@ mba_status autotune(mba_handle* h, mba_tuning* out) {
   // single-block tail of the chain sweeps (the factorization from the build is reused)
   tbest = 1e30;
   const int levels = h->S.chain_levels;
+  h->S.chain_seg = 0;
   for (int nodes : {32, 64, 128, 256, 512}) {
     h->S.chain_tail = chain_tail_level(h->P.nkf, levels, nodes);
     SolverLaunch<T> sc = make_launch<T>(h, b, o);
     const double t = time_ms(st, 2, 10, [&]() { chain_apply<T>(sc, sc.L.rhs, sc.L.z, &h->ctl->pcg_rz0, st); });
-    if (t < tbest) { tbest = t; best.chain_tail_nodes = nodes; best.chain_apply_ms = t; }
+    if (t < tbest) { tbest = t; best.chain_tail_nodes = nodes; best.chain_segment = 1; best.chain_apply_ms = t; }
+  }
+  // segmented sweeps: positions per block
+  for (int seg : {16, 32, 64, 128}) {
+    h->S.chain_seg = chain_segment_level(seg);
+    SolverLaunch<T> sc = make_launch<T>(h, b, o);
+    const double t = time_ms(st, 2, 10, [&]() { chain_apply<T>(sc, sc.L.rhs, sc.L.z, &h->ctl->pcg_rz0, st); });
+    if (t < tbest) { tbest = t; best.chain_segment = seg; best.chain_apply_ms = t; }
   }
   h->S.chain_tail = chain_tail_level(h->P.nkf, levels, best.chain_tail_nodes);
+  h->S.chain_seg = chain_segment_level(best.chain_segment);
   if (cudaStreamSynchronize(st) != cudaSuccess || cudaGetLastError() != cudaSuccess) return MBA_ERR_CUDA;
   h->tuning = best;
   if (out) *out = best;
@@ -2327,6 +2385,8 @@ mba_status mba_set_tuning(mba_handle* h, const mba_tuning* t) {
   if (!h || !t) return MBA_ERR_INVALID_ARG;
   if (t->visual_block && (t->visual_block < 32 || t->visual_block > 256 || t->visual_block % 32)) return MBA_ERR_INVALID_ARG;
   if (t->schur_chunk < 0 || t->chain_tail_nodes < 0) return MBA_ERR_INVALID_ARG;
+  if (t->chain_segment && (t->chain_segment > 128 || (t->chain_segment & (t->chain_segment - 1))))
+    return MBA_ERR_INVALID_ARG;
   cudaSetDevice(h->device);
   if (t->visual_block) { h->P.vis_block = t->visual_block; h->tuning.visual_block = t->visual_block; }
   if (t->visual_min_blocks) {
@@ -2346,6 +2406,10 @@ mba_status mba_set_tuning(mba_handle* h, const mba_tuning* t) {
   if (t->chain_tail_nodes) {
     h->S.chain_tail = chain_tail_level(h->P.nkf, h->S.chain_levels, t->chain_tail_nodes);
     h->tuning.chain_tail_nodes = t->chain_tail_nodes;
+  }
+  if (t->chain_segment) {
+    h->S.chain_seg = chain_segment_level(t->chain_segment);
+    h->tuning.chain_segment = t->chain_segment;
   }
   return MBA_OK;
 }

@@ -54,6 +54,8 @@ struct SchurPattern {
   int32_t* link_blk;      // [nkf]
   int32_t chain_levels = 0;  // cyclic-reduction levels, 2^levels >= nkf
   int32_t chain_tail = 0;    // first level handled by the single-block tail sweep
+  int32_t chain_seg = 0;     // segmented sweeps: log2 of the positions one block sweeps through the
+                             // levels below it (0: one launch per level)
 };
 
 // Device control block of the LM loop (all scalars live on the device).
@@ -158,6 +160,7 @@ struct ChainSystem {
   double* XR64;  // [n][225] T(p + s, p) F(p)
   T *F, *CL, *CR, *XL, *XR;  // working-precision copies read by the sweeps
   T* w;          // [n*15] forward-sweep vector (position order)
+  T* lc;         // [n*15] segmented sweeps: left-neighbour terms of each segment's first position
   double* coef;  // [n][3] gamma_ine, gamma_vis (link p -> p-1), alpha (node p)
   double* comp;  // [n][6] off-chain |S| row sums of the pose rows (alpha's direction)
 };
