@@ -17,9 +17,12 @@
 //                     the stage quantities (the transition derivative is only
 //                     non-zero in rows 0-2, 6-8, 12-14), then the chain
 //                     Q_acc <- Q_acc + A Q_acc + (A Q_acc)^T + A Q_acc A^T + Q,
-//                     Phi_acc <- Phi_acc + A Phi_acc, in precision TM (FP64
-//                     for the FP64 path, FP32 for the mixed path); Cholesky,
-//                     whitening, residual and Jacobians in FP64.
+//                     Phi_acc <- Phi_acc + A Phi_acc, elementwise over the warp
+//                     from shared memory (FP64 path); Cholesky, whitening,
+//                     residual and Jacobians in FP64 (inertial_tail).
+//   k_inertial_mat_cols the same chain in FP32 (mixed path) with one half-warp
+//                     per edge and one column per lane, in registers; the
+//                     FP64 part as above.
 #include <cuda_runtime.h>
 
 #include "internal.h"
@@ -166,6 +169,172 @@ struct InertialOutputs {
 
 __device__ __forceinline__ bool active_row(int r) { return r < 3 || (r >= 6 && r < 9) || r >= 12; }
 
+// FP64 part of an edge (one full warp): Cholesky of Q_acc, L^-1, residual and
+// Jacobians from the accumulated Q_acc and Phi_acc (row-major 15x15 in shared
+// memory).  L, X (225 each) and rs (16) are the warp's FP64 scratch.
+template <typename TM>
+__device__ void inertial_tail(const DevProblem& P, const double* kf_state, const double* end_in,
+                              const InertialOutputs& out, int64_t e, const TM* Qa, const TM* Phia, double* L,
+                              double* X, double* rs, int lane) {
+  // Right-looking Cholesky spread over the warp (Eigen's LLT is a textbook
+  // Cholesky; the order of the subtractions differs, the factor agrees to
+  // rounding).  Lane `lane` owns the lower-triangle elements t = lane + 32 s
+  // (s < 4, t < 120, row-major); each column's pivot square root and
+  // reciprocal are computed by every lane from a broadcast read, and the
+  // reciprocals replace the divisions of the triangular inverse.
+  double* dinv = rs;  // 1 / L_jj until the residual needs rs
+  int own_i[4], own_k[4];
+#pragma unroll
+  for (int s = 0; s < 4; ++s) {
+    const int t = lane + 32 * s;
+    int r = 0;
+    while ((r + 1) * (r + 2) / 2 <= t) ++r;  // t in row r of the lower triangle
+    own_i[s] = t < 120 ? r : -1;
+    own_k[s] = t < 120 ? t - r * (r + 1) / 2 : -1;
+  }
+  for (int a = lane; a < 225; a += 32) L[a] = (double)Qa[a];
+  __syncwarp();
+  int fail = -1;
+  for (int j = 0; j < 15; ++j) {
+    const double d = L[j * 16];
+    if (!(d > 0.0)) {  // the same value in every lane: a uniform exit
+      fail = j;
+      break;
+    }
+    const double ljj = sqrt(d), inv = 1.0 / ljj;
+    // Phase 1: scale column j below the pivot (every lane has read the pivot
+    // before any lane writes column j).
+#pragma unroll
+    for (int s = 0; s < 4; ++s)
+      if (own_k[s] == j && own_i[s] > j) L[own_i[s] * 15 + j] *= inv;
+    if (lane == 0) dinv[j] = inv;
+    __syncwarp();
+    // Phase 2: the pivot, and the trailing update from the scaled column
+    // (which no lane writes in this phase).
+#pragma unroll
+    for (int s = 0; s < 4; ++s) {
+      if (own_k[s] == j && own_i[s] == j) L[j * 16] = ljj;
+      if (own_k[s] > j) L[own_i[s] * 15 + own_k[s]] -= L[own_i[s] * 15 + j] * L[own_k[s] * 15 + j];
+    }
+    __syncwarp();
+  }
+  if (fail >= 0) {
+    // Q_acc not positive definite.  The reference factorizes with Eigen's
+    // LLT and never checks info() (inertial-error-term.cc:155-182): Eigen's
+    // column-by-column factorization stops at column `fail`, leaving that
+    // column (diagonal included) and every later column of the lower
+    // triangle at Q's own values, and the triangular solves use that matrix.
+    // Columns >= fail are restored from Q here (the right-looking updates
+    // above had already touched them).
+#pragma unroll
+    for (int s = 0; s < 4; ++s)
+      if (own_k[s] >= fail) L[own_i[s] * 15 + own_k[s]] = (double)Qa[own_i[s] * 15 + own_k[s]];
+    __syncwarp();
+    if (lane >= fail && lane < 15) dinv[lane] = 1.0 / L[lane * 16];
+    __syncwarp();
+  }
+  if (lane < 15) {  // X = L^-1, column `lane`
+    for (int i = 0; i < 15; ++i) {
+      double v = (i == lane) ? 1.0 : 0.0;
+      for (int q = 0; q < i; ++q) v -= L[i * 15 + q] * X[q * 15 + lane];
+      X[i * 15 + lane] = v * dinv[i];
+    }
+  }
+  __syncwarp();
+  // Mx = L^-1 Phi_acc (into L, no longer needed after the next sync)
+  double mvals[8];
+  for (int j = 0, a = lane; a < 225; a += 32, ++j) {
+    const int r = a / 15, c = a % 15;
+    double v = 0.0;
+    for (int q = 0; q <= r; ++q) v += X[r * 15 + q] * (double)Phia[q * 15 + c];
+    mvals[j] = v;
+  }
+  __syncwarp();
+  for (int j = 0, a = lane; a < 225; a += 32, ++j) L[a] = mvals[j];
+  const double* xf = kf_state + 16 * (int64_t)P.e_from[e];
+  const double* xt = kf_state + 16 * (int64_t)P.e_to[e];
+  const double* en = end_in + 16 * e;  // integrator layout
+  if (lane == 0) {
+    const double n2 = en[0] * en[0] + en[1] * en[1] + en[2] * en[2] + en[3] * en[3];
+    double qinv[4] = {0, 0, 0, 0};
+    if (n2 > 0.0) { qinv[0] = -en[0] / n2; qinv[1] = -en[1] / n2; qinv[2] = -en[2] / n2; qinv[3] = en[3] / n2; }
+    double dq[4];
+    qprod_pos(xt, qinv, dq);
+    double* rr = rs;
+    rr[0] = 2.0 * dq[0]; rr[1] = 2.0 * dq[1]; rr[2] = 2.0 * dq[2];
+    for (int a = 0; a < 3; ++a) {
+      rr[3 + a] = xt[10 + a] - en[4 + a];
+      rr[6 + a] = xt[7 + a] - en[7 + a];
+      rr[9 + a] = xt[13 + a] - en[10 + a];
+      rr[12 + a] = xt[4 + a] - en[13 + a];
+    }
+  }
+  __syncwarp();
+  double rw = 0.0;
+  if (lane < 15)
+    for (int q = 0; q <= lane; ++q) rw += X[lane * 15 + q] * rs[q];
+  __syncwarp();
+  if (lane < 15) rs[lane] = rw;
+  const double sq = warp_sum_d(lane < 15 ? rw * rw : 0.0);
+  if (lane == 0 && out.cost) atomicAdd(out.cost, 0.5 * sq);
+  __syncwarp();
+  const double* Mx = L;
+  const int f = P.e_from[e], t = P.e_to[e];
+  if (out.lin_r) {
+    if (lane < 15) out.lin_r[15 * e + lane] = rs[lane];
+    double qf[4] = {xf[0], xf[1], xf[2], xf[3]}, qt[4] = {xt[0], xt[1], xt[2], xt[3]};
+    M3<double> Rf, Rt, Bf, Bt;
+    jplR(qf, Rf);
+    jplR(qt, Rt);
+    rot_basis_d(P, f, qf, Rf, Bf);
+    rot_basis_d(P, t, qt, Rt, Bt);
+    const uint16_t mf = P.kf_mask[f], mt = P.kf_mask[t];
+    const int src[15] = {0, 1, 2, 12, 13, 14, 6, 7, 8, 3, 4, 5, 9, 10, 11};
+    for (int a = lane; a < 225; a += 32) {
+      const int r = a / 15, c = a % 15;
+      double vf, vt;
+      if (c < 3) {
+        vf = -(Mx[r * 15 + 0] * Bf.m[c] + Mx[r * 15 + 1] * Bf.m[3 + c] + Mx[r * 15 + 2] * Bf.m[6 + c]);
+        vt = X[r * 15 + 0] * Bt.m[c] + X[r * 15 + 1] * Bt.m[3 + c] + X[r * 15 + 2] * Bt.m[6 + c];
+      } else {
+        vf = (mf & (1u << c)) ? -Mx[r * 15 + src[c]] : 0.0;
+        vt = (mt & (1u << c)) ? X[r * 15 + src[c]] : 0.0;
+      }
+      out.lin_Jf[225 * e + a] = vf;
+      out.lin_Jt[225 * e + a] = vt;
+    }
+  }
+  if (out.amb_res && lane < 15) out.amb_res[15 * e + lane] = rs[lane];
+  if (out.amb_J[0] || out.amb_J[4]) {
+    double Jqf[12], Jqt[12];
+    dqdtheta(xf, Jqf);
+    dqdtheta(xt, Jqt);
+    for (int a = lane; a < 105; a += 32) {
+      const int r = a / 7, c = a % 7;
+      if (out.amb_J[0]) {
+        double v;
+        if (c < 4) v = -4.0 * (Mx[r * 15] * Jqf[3 * c] + Mx[r * 15 + 1] * Jqf[3 * c + 1] + Mx[r * 15 + 2] * Jqf[3 * c + 2]);
+        else v = -Mx[r * 15 + 12 + (c - 4)];
+        out.amb_J[0][105 * e + a] = v;
+      }
+      if (out.amb_J[4]) {
+        double v;
+        if (c < 4) v = 4.0 * (X[r * 15] * Jqt[3 * c] + X[r * 15 + 1] * Jqt[3 * c + 1] + X[r * 15 + 2] * Jqt[3 * c + 2]);
+        else v = X[r * 15 + 12 + (c - 4)];
+        out.amb_J[4][105 * e + a] = v;
+      }
+    }
+  }
+  for (int b = 0; b < 3; ++b) {
+    const int col0 = (b == 0) ? 3 : (b == 1 ? 6 : 9);  // b_g, v, b_a
+    for (int a = lane; a < 45; a += 32) {
+      const int r = a / 3, c = a % 3;
+      if (out.amb_J[1 + b]) out.amb_J[1 + b][45 * e + a] = -Mx[r * 15 + col0 + c];
+      if (out.amb_J[5 + b]) out.amb_J[5 + b][45 * e + a] = X[r * 15 + col0 + c];
+    }
+  }
+}
+
 template <typename TM, int kWarps>
 __global__ void __launch_bounds__(32 * kWarps) k_inertial_mat(DevProblem P, const double* kf_state,
                                                               const TM* stage_in, const double* dt_in,
@@ -295,164 +464,168 @@ __global__ void __launch_bounds__(32 * kWarps) k_inertial_mat(DevProblem P, cons
     }
     __syncwarp();
   }
-  // ---- FP64 from here: Cholesky of Q_acc, L^-1, residual, Jacobians.
-  // Right-looking Cholesky spread over the warp (Eigen's LLT is a textbook
-  // Cholesky; the order of the subtractions differs, the factor agrees to
-  // rounding).  Lane `lane` owns the lower-triangle elements t = lane + 32 s
-  // (s < 4, t < 120, row-major); each column's pivot square root and
-  // reciprocal are computed by every lane from a broadcast read, and the
-  // reciprocals replace the divisions of the triangular inverse.
-  double* L = Ld[w];
-  double* X = Xd[w];
-  double* dinv = rsh[w];  // 1 / L_jj until the residual needs rsh
-  int own_i[4], own_k[4];
+  inertial_tail<TM>(P, kf_state, end_in, out, e, S.Q, S.Phi, Ld[w], Xd[w], rsh[w], lane);
+}
+
+// The FP32 transition / covariance chain with one half-warp per edge and one
+// lane per column: lane c keeps column c of Q_acc, Phi_acc, Pm and the stage
+// sums in registers.  Left products by the (row-sparse) RK4 derivative F and
+// by A act on columns, so they need no other lane's data; only the
+// transposes (PC^T in the stage covariance, M^T and M A^T in the Q update)
+// and the rows of A go through shared memory.  Rows of D, td, A and M are
+// kept for the active rows 0-2, 6-8, 12-14 only (index i -> row kAct(i)).
+// The FP64 part then runs for the warp's two edges one after the other.
+__device__ __forceinline__ constexpr int kAct(int i) { return i < 3 ? i : (i < 6 ? i + 3 : i + 6); }
+
+template <int kWarps>
+__global__ void __launch_bounds__(32 * kWarps, 4) k_inertial_mat_cols(DevProblem P, const double* kf_state,
+                                                                   const float* stage_in, const double* dt_in,
+                                                                   const double* end_in, InertialOutputs out,
+                                                                   const int* skip_if) {
+  if (gated_i(skip_if)) return;
+  __shared__ __align__(16) float ex[kWarps][2][512];  // per edge: X [16][16] then Y [16][16]; Q | Phi at the end
+  __shared__ double Ld[kWarps][225], Xd[kWarps][225], rsh[kWarps][16];
+  const int w = threadIdx.x >> 5, lane = threadIdx.x & 31, h = lane >> 4, c = lane & 15;
+  const int64_t e0 = 2 * (blockIdx.x * (int64_t)kWarps + w);
+  if (e0 >= P.nimu) return;  // uniform over the warp
+  const int64_t e = e0 + h;
+  const unsigned hm = 0xffffu << (16 * h);
+  float* X = ex[w][h];
+  float* Y = X + 256;
+  const bool col = c < 15;
+  if (e < P.nimu) {
+    const float gn = float(P.gyro_noise2), gb = float(P.gyro_bias2), an = float(P.acc_noise2),
+                ab = float(P.acc_bias2);
+    const float noise = c < 3 ? gn : c < 6 ? gb : c < 9 ? an : c < 12 ? ab : 0.f;  // diagonal of the stage covariance
+    const bool cact = col && active_row(c);
+    float Q[15], Phi[15];
 #pragma unroll
-  for (int s = 0; s < 4; ++s) {
-    const int t = lane + 32 * s;
-    int r = 0;
-    while ((r + 1) * (r + 2) / 2 <= t) ++r;  // t in row r of the lower triangle
-    own_i[s] = t < 120 ? r : -1;
-    own_k[s] = t < 120 ? t - r * (r + 1) / 2 : -1;
-  }
-  for (int a = lane; a < 225; a += 32) L[a] = (double)S.Q[a];
-  __syncwarp();
-  int fail = -1;
-  for (int j = 0; j < 15; ++j) {
-    const double d = L[j * 16];
-    if (!(d > 0.0)) {  // the same value in every lane: a uniform exit
-      fail = j;
-      break;
+    for (int r = 0; r < 15; ++r) {
+      Q[r] = 0.f;
+      Phi[r] = (r == c) ? 1.f : 0.f;
     }
-    const double ljj = sqrt(d), inv = 1.0 / ljj;
-    // Phase 1: scale column j below the pivot (every lane has read the pivot
-    // before any lane writes column j).
+    const int64_t o0 = P.e_off[e];
+    const int ns = (int)(P.e_off[e + 1] - o0);
+    const int64_t step0 = o0 - e;
+    for (int k = 0; k + 1 < ns; ++k) {
+      const float dt = float(dt_in[step0 + k]);
+      const float* sk = stage_in + (step0 + k) * 4 * kStageVals;
+      float D[9], Pm[15], sumtd[9], sumcd[15];
 #pragma unroll
-    for (int s = 0; s < 4; ++s)
-      if (own_k[s] == j && own_i[s] > j) L[own_i[s] * 15 + j] *= inv;
-    if (lane == 0) dinv[j] = inv;
-    __syncwarp();
-    // Phase 2: the pivot, and the trailing update from the scaled column
-    // (which no lane writes in this phase).
+      for (int i = 0; i < 9; ++i) { D[i] = 0.f; sumtd[i] = 0.f; }
 #pragma unroll
-    for (int s = 0; s < 4; ++s) {
-      if (own_k[s] == j && own_i[s] == j) L[j * 16] = ljj;
-      if (own_k[s] > j) L[own_i[s] * 15 + own_k[s]] -= L[own_i[s] * 15 + j] * L[own_k[s] * 15 + j];
-    }
-    __syncwarp();
-  }
-  if (fail >= 0) {
-    // Q_acc not positive definite.  The reference factorizes with Eigen's
-    // LLT and never checks info() (inertial-error-term.cc:155-182): Eigen's
-    // column-by-column factorization stops at column `fail`, leaving that
-    // column (diagonal included) and every later column of the lower
-    // triangle at Q's own values, and the triangular solves use that matrix.
-    // Columns >= fail are restored from Q here (the right-looking updates
-    // above had already touched them).
+      for (int r = 0; r < 15; ++r) { Pm[r] = 0.f; sumcd[r] = 0.f; }
+#pragma unroll 1
+      for (int stg = 0; stg < 4; ++stg) {
+        const float* f = sk + stg * kStageVals;
+        const float wx = f[0], wy = f[1], wz = f[2], ax = f[3], ay = f[4], az = f[5];
+        const float F00[9] = {0.f, wz, -wy, -wz, 0.f, wx, wy, -wx, 0.f};
+        float F69[9], F60[9];
 #pragma unroll
-    for (int s = 0; s < 4; ++s)
-      if (own_k[s] >= fail) L[own_i[s] * 15 + own_k[s]] = (double)S.Q[own_i[s] * 15 + own_k[s]];
-    __syncwarp();
-    if (lane >= fail && lane < 15) dinv[lane] = 1.0 / L[lane * 16];
-    __syncwarp();
-  }
-  if (lane < 15) {  // X = L^-1, column `lane`
-    for (int i = 0; i < 15; ++i) {
-      double v = (i == lane) ? 1.0 : 0.0;
-      for (int q = 0; q < i; ++q) v -= L[i * 15 + q] * X[q * 15 + lane];
-      X[i * 15 + lane] = v * dinv[i];
-    }
-  }
-  __syncwarp();
-  // Mx = L^-1 Phi_acc (into L, no longer needed after the next sync)
-  double mvals[8];
-  for (int j = 0, a = lane; a < 225; a += 32, ++j) {
-    const int r = a / 15, c = a % 15;
-    double v = 0.0;
-    for (int q = 0; q <= r; ++q) v += X[r * 15 + q] * (double)S.Phi[q * 15 + c];
-    mvals[j] = v;
-  }
-  __syncwarp();
-  for (int j = 0, a = lane; a < 225; a += 32, ++j) L[a] = mvals[j];
-  const double* xf = kf_state + 16 * (int64_t)P.e_from[e];
-  const double* xt = kf_state + 16 * (int64_t)P.e_to[e];
-  const double* en = end_in + 16 * e;  // integrator layout
-  if (lane == 0) {
-    const double n2 = en[0] * en[0] + en[1] * en[1] + en[2] * en[2] + en[3] * en[3];
-    double qinv[4] = {0, 0, 0, 0};
-    if (n2 > 0.0) { qinv[0] = -en[0] / n2; qinv[1] = -en[1] / n2; qinv[2] = -en[2] / n2; qinv[3] = en[3] / n2; }
-    double dq[4];
-    qprod_pos(xt, qinv, dq);
-    double* rr = rsh[w];
-    rr[0] = 2.0 * dq[0]; rr[1] = 2.0 * dq[1]; rr[2] = 2.0 * dq[2];
-    for (int a = 0; a < 3; ++a) {
-      rr[3 + a] = xt[10 + a] - en[4 + a];
-      rr[6 + a] = xt[7 + a] - en[7 + a];
-      rr[9 + a] = xt[13 + a] - en[10 + a];
-      rr[12 + a] = xt[4 + a] - en[13 + a];
-    }
-  }
-  __syncwarp();
-  double rw = 0.0;
-  if (lane < 15)
-    for (int q = 0; q <= lane; ++q) rw += X[lane * 15 + q] * rsh[w][q];
-  __syncwarp();
-  if (lane < 15) rsh[w][lane] = rw;
-  const double sq = warp_sum_d(lane < 15 ? rw * rw : 0.0);
-  if (lane == 0 && out.cost) atomicAdd(out.cost, 0.5 * sq);
-  __syncwarp();
-  const double* Mx = L;
-  const int f = P.e_from[e], t = P.e_to[e];
-  if (out.lin_r) {
-    if (lane < 15) out.lin_r[15 * e + lane] = rsh[w][lane];
-    double qf[4] = {xf[0], xf[1], xf[2], xf[3]}, qt[4] = {xt[0], xt[1], xt[2], xt[3]};
-    M3<double> Rf, Rt, Bf, Bt;
-    jplR(qf, Rf);
-    jplR(qt, Rt);
-    rot_basis_d(P, f, qf, Rf, Bf);
-    rot_basis_d(P, t, qt, Rt, Bt);
-    const uint16_t mf = P.kf_mask[f], mt = P.kf_mask[t];
-    const int src[15] = {0, 1, 2, 12, 13, 14, 6, 7, 8, 3, 4, 5, 9, 10, 11};
-    for (int a = lane; a < 225; a += 32) {
-      const int r = a / 15, c = a % 15;
-      double vf, vt;
-      if (c < 3) {
-        vf = -(Mx[r * 15 + 0] * Bf.m[c] + Mx[r * 15 + 1] * Bf.m[3 + c] + Mx[r * 15 + 2] * Bf.m[6 + c]);
-        vt = X[r * 15 + 0] * Bt.m[c] + X[r * 15 + 1] * Bt.m[3 + c] + X[r * 15 + 2] * Bt.m[6 + c];
-      } else {
-        vf = (mf & (1u << c)) ? -Mx[r * 15 + src[c]] : 0.0;
-        vt = (mt & (1u << c)) ? X[r * 15 + src[c]] : 0.0;
+        for (int a = 0; a < 9; ++a) F69[a] = -f[6 + a];
+        const float axm[9] = {0.f, -az, ay, az, 0.f, -ax, -ay, ax, 0.f};
+#pragma unroll
+        for (int i = 0; i < 3; ++i)
+#pragma unroll
+          for (int j = 0; j < 3; ++j)
+            F60[3 * i + j] = F69[3 * i] * axm[j] + F69[3 * i + 1] * axm[3 + j] + F69[3 * i + 2] * axm[6 + j];
+        // td = F (I + D) and PC = F Pm, column c, active rows.
+        float td[9], pc[9];
+#pragma unroll
+        for (int q = 0; q < 3; ++q) {
+          td[q] = (c < 3 ? F00[3 * q + c] : 0.f) + F00[3 * q] * D[0] + F00[3 * q + 1] * D[1] + F00[3 * q + 2] * D[2] -
+                  (c == 3 + q ? 1.f : 0.f);
+          pc[q] = F00[3 * q] * Pm[0] + F00[3 * q + 1] * Pm[1] + F00[3 * q + 2] * Pm[2] - Pm[3 + q];
+          td[3 + q] = (c < 3 ? F60[3 * q + c] : 0.f) + F60[3 * q] * D[0] + F60[3 * q + 1] * D[1] +
+                      F60[3 * q + 2] * D[2] + (c >= 9 && c < 12 ? F69[3 * q + c - 9] : 0.f);
+          pc[3 + q] = F60[3 * q] * Pm[0] + F60[3 * q + 1] * Pm[1] + F60[3 * q + 2] * Pm[2] + F69[3 * q] * Pm[9] +
+                      F69[3 * q + 1] * Pm[10] + F69[3 * q + 2] * Pm[11];
+          td[6 + q] = (c == 6 + q ? 1.f : 0.f) + D[3 + q];
+          pc[6 + q] = Pm[6 + q];
+        }
+        if (col)
+#pragma unroll
+          for (int i = 0; i < 9; ++i) X[16 * kAct(i) + c] = pc[i];
+        __syncwarp(hm);
+        // cd = PC + PC^T + noise; PC^T's column c is row c of PC (non-zero for active c).
+        const float wgt = (stg == 0 || stg == 3) ? 1.f : 2.f;
+        const float cnext = (stg == 2) ? dt : 0.5f * dt;
+        float cd[15];
+#pragma unroll
+        for (int r = 0; r < 15; ++r) cd[r] = (cact ? X[16 * c + r] : 0.f) + (r == c ? noise : 0.f);
+#pragma unroll
+        for (int i = 0; i < 9; ++i) cd[kAct(i)] += pc[i];
+#pragma unroll
+        for (int i = 0; i < 9; ++i) {
+          sumtd[i] += wgt * td[i];
+          if (stg < 3) D[i] = cnext * td[i];
+        }
+#pragma unroll
+        for (int r = 0; r < 15; ++r) {
+          sumcd[r] += wgt * cd[r];
+          if (stg < 3) Pm[r] = cnext * cd[r];
+        }
+        __syncwarp(hm);  // X is rewritten by the next stage
       }
-      out.lin_Jf[225 * e + a] = vf;
-      out.lin_Jt[225 * e + a] = vt;
-    }
-  }
-  if (out.amb_res && lane < 15) out.amb_res[15 * e + lane] = rsh[w][lane];
-  if (out.amb_J[0] || out.amb_J[4]) {
-    double Jqf[12], Jqt[12];
-    dqdtheta(xf, Jqf);
-    dqdtheta(xt, Jqt);
-    for (int a = lane; a < 105; a += 32) {
-      const int r = a / 7, c = a % 7;
-      if (out.amb_J[0]) {
-        double v;
-        if (c < 4) v = -4.0 * (Mx[r * 15] * Jqf[3 * c] + Mx[r * 15 + 1] * Jqf[3 * c + 1] + Mx[r * 15 + 2] * Jqf[3 * c + 2]);
-        else v = -Mx[r * 15 + 12 + (c - 4)];
-        out.amb_J[0][105 * e + a] = v;
+      // A = dt/6 sum(td) (rows of A to X), Qk = dt/6 sum(cd).
+      float Acol[9];
+#pragma unroll
+      for (int i = 0; i < 9; ++i) {
+        Acol[i] = dt * sumtd[i] / 6.f;
+        if (col) X[16 * kAct(i) + c] = Acol[i];
       }
-      if (out.amb_J[4]) {
-        double v;
-        if (c < 4) v = 4.0 * (X[r * 15] * Jqt[3 * c] + X[r * 15 + 1] * Jqt[3 * c + 1] + X[r * 15 + 2] * Jqt[3 * c + 2]);
-        else v = X[r * 15 + 12 + (c - 4)];
-        out.amb_J[4][105 * e + a] = v;
+      __syncwarp(hm);
+      // M = A Q, N = A Phi (column c, active rows); M to Y for the transposes.
+      float M[9], Nn[9];
+#pragma unroll
+      for (int i = 0; i < 9; ++i) {
+        float m = 0.f, n = 0.f;
+#pragma unroll
+        for (int j = 0; j < 15; ++j) {
+          const float arj = X[16 * kAct(i) + j];
+          m += arj * Q[j];
+          n += arj * Phi[j];
+        }
+        M[i] = m;
+        Nn[i] = n;
+        if (col) Y[16 * kAct(i) + c] = m;
       }
+      __syncwarp(hm);
+      // Q <- Q + M + M^T + M A^T + Qk ; Phi <- Phi + N
+      float Mfull[15];
+#pragma unroll
+      for (int r = 0; r < 15; ++r) Mfull[r] = 0.f;
+#pragma unroll
+      for (int i = 0; i < 9; ++i) Mfull[kAct(i)] = M[i];
+#pragma unroll
+      for (int r = 0; r < 15; ++r) {
+        float q = Q[r] + Mfull[r] + (cact ? Y[16 * c + r] : 0.f) + dt * sumcd[r] / 6.f;
+        if (cact && active_row(r)) {
+          float v = 0.f;
+#pragma unroll
+          for (int j = 0; j < 15; ++j) v += Y[16 * r + j] * X[16 * c + j];
+          q += v;
+        }
+        Q[r] = q;
+      }
+#pragma unroll
+      for (int i = 0; i < 9; ++i) Phi[kAct(i)] += Nn[i];
+      __syncwarp(hm);  // X and Y are rewritten by the next step
     }
+    if (col)
+#pragma unroll
+      for (int r = 0; r < 15; ++r) {
+        X[15 * r + c] = Q[r];         // Q_acc at [0, 225)
+        X[225 + 15 * r + c] = Phi[r];  // Phi_acc at [225, 450)
+      }
   }
-  for (int b = 0; b < 3; ++b) {
-    const int col0 = (b == 0) ? 3 : (b == 1 ? 6 : 9);  // b_g, v, b_a
-    for (int a = lane; a < 45; a += 32) {
-      const int r = a / 3, c = a % 3;
-      if (out.amb_J[1 + b]) out.amb_J[1 + b][45 * e + a] = -Mx[r * 15 + col0 + c];
-      if (out.amb_J[5 + b]) out.amb_J[5 + b][45 * e + a] = X[r * 15 + col0 + c];
+  __syncwarp();
+  for (int hh = 0; hh < 2; ++hh) {
+    const int64_t ee = e0 + hh;
+    if (ee < P.nimu) {  // uniform over the warp
+      const float* Qa = ex[w][hh];
+      inertial_tail<float>(P, kf_state, end_in, out, ee, Qa, Qa + 225, Ld[w], Xd[w], rsh[w], lane);
+      __syncwarp();
     }
   }
 }
@@ -478,9 +651,9 @@ cudaError_t launch_inertial_v2(const DevProblem& P, const double* kf_state, bool
   const unsigned gA = (unsigned)((P.nimu + 127) / 128);
   if (f32_matrices) {
     k_inertial_state<float><<<gA, 128, 0, s>>>(P, kf_state, (float*)stage, dt, endst, status, skip_if);
-    constexpr int W = 4;
-    k_inertial_mat<float, W><<<(unsigned)((P.nimu + W - 1) / W), 32 * W, 0, s>>>(P, kf_state, (const float*)stage, dt,
-                                                                                   endst, o, skip_if);
+    constexpr int W = 4;  // two edges per warp
+    k_inertial_mat_cols<W><<<(unsigned)((P.nimu + 2 * W - 1) / (2 * W)), 32 * W, 0, s>>>(
+        P, kf_state, (const float*)stage, dt, endst, o, skip_if);
   } else {
     k_inertial_state<double><<<gA, 128, 0, s>>>(P, kf_state, (double*)stage, dt, endst, status, skip_if);
     constexpr int W = 1;
