@@ -34,6 +34,8 @@ struct DevProblem {
   int32_t* lm_off;          // [nlm] 1 = rejected as an outlier: its terms are out of the problem
   // keyframes
   double* kf_state;         // [nkf][16] = q(4) p(3) v(3) b_g(3) b_a(3)
+  double* kf_rot;           // [nkf][16] = R_I_M (9, row-major), |q|^2, pad: written before each FP64
+                            // linearization from kf_state
   const int32_t* kf_mis;
   const uint32_t* kf_flags;
   const uint16_t* kf_mask;  // bit d set = tangent dim d active (theta, p, v, b_g, b_a)
@@ -98,6 +100,7 @@ struct VisualInputs {
   int kf_stride;
   const T* mis;        // stride 8
   const DevCameraT<T>* cams;
+  const T* kf_rot;     // FP64: per-keyframe R_I_M and |q|^2 (stride 16), else null
 };
 
 template <typename T>

@@ -140,9 +140,13 @@ __device__ __forceinline__ void load_obs_gather(const DevProblem& P, const Visua
 }
 
 // Arithmetic and stores of observation i; returns its cost (kCost).
+// rci: the camera's R_C_I (9 values, e.g. from the block's shared memory) or
+// null; FP64 inputs carry the keyframes' rotation matrices and |q|^2
+// (in.kf_rot, written by k_kf_rotations) so that the kernel does not rebuild
+// them per observation.
 template <typename T, bool kCost>
 __device__ __forceinline__ double compute_obs(const DevProblem& P, const VisualInputs<T>& in, const ObsInputs<T>& o,
-                                              const VisualLin<T>& out, int64_t i, int64_t N) {
+                                              const VisualLin<T>& out, int64_t i, int64_t N, const T* rci) {
   double cost = 0.0;
   const int kf = o.kf, st = o.st, type = o.type;
   const DevCameraT<T>& cam = in.cams[o.cam];
@@ -151,10 +155,16 @@ __device__ __forceinline__ double compute_obs(const DevProblem& P, const VisualI
   const T ha = o.ha;
   const T pB[3] = {o.pB[0], o.pB[1], o.pB[2]};
   M3<T> RCI;
-  jplR(cam.q_CI, RCI);
+  if (rci) {
+#pragma unroll
+    for (int a = 0; a < 9; ++a) RCI.m[a] = rci[a];
+  } else {
+    jplR(cam.q_CI, RCI);
+  }
   T pI[3];
   M3<T> RIM, RBLM, RMG, RGLM;
   T qst[4], qob[4], pLMB[3], pMI[3];
+  T n2s = T(0), n2o = T(0);  // |q|^2 of the store / observer keyframe
   if (type == MBA_LOCAL_KEYFRAME) {
     pI[0] = pB[0]; pI[1] = pB[1]; pI[2] = pB[2];
   } else {
@@ -162,8 +172,19 @@ __device__ __forceinline__ double compute_obs(const DevProblem& P, const VisualI
     for (int a = 0; a < 4; ++a) { qst[a] = o.xs[a]; qob[a] = o.xo[a]; }
     pLMB[0] = o.xs[4]; pLMB[1] = o.xs[5]; pLMB[2] = o.xs[6];
     pMI[0] = o.xo[4]; pMI[1] = o.xo[5]; pMI[2] = o.xo[6];
-    jplR(qst, RBLM);
-    jplR(qob, RIM);
+    if (sizeof(T) == 8 && in.kf_rot) {
+      const T* ra = in.kf_rot + 16 * (int64_t)st;
+      const T* rb = in.kf_rot + 16 * (int64_t)kf;
+#pragma unroll
+      for (int a = 0; a < 9; ++a) { RBLM.m[a] = ra[a]; RIM.m[a] = rb[a]; }
+      n2s = ra[9];
+      n2o = rb[9];
+    } else {
+      jplR(qst, RBLM);
+      jplR(qob, RIM);
+      n2s = qst[0] * qst[0] + qst[1] * qst[1] + qst[2] * qst[2] + qst[3] * qst[3];
+      n2o = qob[0] * qob[0] + qob[1] * qob[1] + qob[2] * qob[2] + qob[3] * qob[3];
+    }
     T pM[3];
     mtv3(RBLM, pB, pM);  // R_LM_B p_B
     pM[0] += pLMB[0]; pM[1] += pLMB[1]; pM[2] += pLMB[2];
@@ -237,11 +258,10 @@ __device__ __forceinline__ double compute_obs(const DevProblem& P, const VisualI
       // is applied as a scalar (same products, fewer instructions).
       const bool rps = P.kf_flags[st] & MBA_KF_GAUGE_ROLL_PITCH, rpo = P.kf_flags[kf] & MBA_KF_GAUGE_ROLL_PITCH;
       if (!rps) {
-        const T n2 = qst[0] * qst[0] + qst[1] * qst[1] + qst[2] * qst[2] + qst[3] * qst[3];
 #pragma unroll
         for (int rr = 0; rr < 2; ++rr)
 #pragma unroll
-          for (int c = 0; c < 3; ++c) Js[6 * rr + c] = (ms & (1u << c)) ? -(Jqs[3 * rr + c] * n2) : T(0);
+          for (int c = 0; c < 3; ++c) Js[6 * rr + c] = (ms & (1u << c)) ? -(Jqs[3 * rr + c] * n2s) : T(0);
       } else {
         M3<T> Bs;
         rot_basis<T>(P, in.mis, st, qst, RBLM, Bs);
@@ -252,11 +272,10 @@ __device__ __forceinline__ double compute_obs(const DevProblem& P, const VisualI
             Js[6 * rr + c] = -(Jqs[3 * rr] * Bs.m[c] + Jqs[3 * rr + 1] * Bs.m[3 + c] + Jqs[3 * rr + 2] * Bs.m[6 + c]);
       }
       if (!rpo) {
-        const T n2 = qob[0] * qob[0] + qob[1] * qob[1] + qob[2] * qob[2] + qob[3] * qob[3];
 #pragma unroll
         for (int rr = 0; rr < 2; ++rr)
 #pragma unroll
-          for (int c = 0; c < 3; ++c) Jo[6 * rr + c] = (mo & (1u << c)) ? (Jqo[3 * rr + c] * n2) : T(0);
+          for (int c = 0; c < 3; ++c) Jo[6 * rr + c] = (mo & (1u << c)) ? (Jqo[3 * rr + c] * n2o) : T(0);
       } else {
         M3<T> Bo;
         rot_basis<T>(P, in.mis, kf, qob, RIM, Bo);
@@ -322,6 +341,22 @@ __device__ __forceinline__ double compute_obs(const DevProblem& P, const VisualI
   return cost;
 }
 
+// The cameras' R_C_I, built once per block into shared memory (at most
+// kCamRot cameras; returns false for more, and compute_obs builds them).
+constexpr int kCamRot = 16;
+template <typename T>
+__device__ __forceinline__ bool stage_camera_rotations(const DevProblem& P, const VisualInputs<T>& in, T* rci) {
+  if (P.ncam > kCamRot) return false;
+  for (int c = threadIdx.x; c < P.ncam; c += blockDim.x) {
+    M3<T> R;
+    jplR(in.cams[c].q_CI, R);
+#pragma unroll
+    for (int a = 0; a < 9; ++a) rci[9 * c + a] = R.m[a];
+  }
+  __syncthreads();
+  return true;
+}
+
 // One thread per observation.  kMinBlocks > 1 trades registers (spilled to
 // L1) for resident warps; the autotuner picks the variant per problem.
 template <typename T, bool kCost, int kMinBlocks>
@@ -329,13 +364,15 @@ __global__ void __launch_bounds__(kBlock, kMinBlocks) k_visual_linearize(DevProb
                                                              double* cost_accum, const int* run_if,
                                                              const int* skip_if) {
   if (gated(run_if, skip_if)) return;
+  __shared__ T rci[9 * kCamRot];
+  const bool cam_sm = stage_camera_rotations(P, in, rci);
   const int64_t i = blockIdx.x * (int64_t)blockDim.x + threadIdx.x;
   double cost = 0.0;
   if (i < P.nobs) {
     ObsInputs<T> o;
     load_obs_stream(P, in, i, o);
     load_obs_gather(P, in, o);
-    cost = compute_obs<T, kCost>(P, in, o, out, i, P.nobs);
+    cost = compute_obs<T, kCost>(P, in, o, out, i, P.nobs, cam_sm ? rci + 9 * o.cam : nullptr);
   }
   if (kCost) block_accumulate(cost, cost_accum);
 }
@@ -351,6 +388,8 @@ __global__ void __launch_bounds__(kBlock, kMinBlocks) k_visual_linearize_pipe(De
                                                                   double* cost_accum, const int* run_if,
                                                                   const int* skip_if) {
   if (gated(run_if, skip_if)) return;
+  __shared__ T rci[9 * kCamRot];
+  const bool cam_sm = stage_camera_rotations(P, in, rci);
   const int64_t N = P.nobs, stride = (int64_t)gridDim.x * blockDim.x;
   int64_t i = blockIdx.x * (int64_t)blockDim.x + threadIdx.x;
   double cost = 0.0;
@@ -365,7 +404,7 @@ __global__ void __launch_bounds__(kBlock, kMinBlocks) k_visual_linearize_pipe(De
     if (j < N) load_obs_gather(P, in, nxt);
     ObsInputs<T> nn;
     if (j + stride < N) load_obs_stream(P, in, j + stride, nn);
-    cost += compute_obs<T, kCost>(P, in, cur, out, i, N);
+    cost += compute_obs<T, kCost>(P, in, cur, out, i, N, cam_sm ? rci + 9 * cur.cam : nullptr);
     cur = nxt;
     nxt = nn;
   }
@@ -798,18 +837,36 @@ VisualInputs<T> visual_inputs(const DevProblem& P) {
   VisualInputs<T> in;
   if constexpr (sizeof(T) == 8) {
     in.uv = P.obs_uv; in.sinv = P.obs_sinv; in.huber = P.obs_huber; in.lm_p = P.lm_p;
-    in.kf = P.kf_state; in.kf_stride = 16; in.mis = P.mis; in.cams = P.cams;
+    in.kf = P.kf_state; in.kf_stride = 16; in.mis = P.mis; in.cams = P.cams; in.kf_rot = P.kf_rot;
   } else {
     in.uv = P.obs_uv_f; in.sinv = P.obs_sinv_f; in.huber = P.obs_huber_f; in.lm_p = P.lm_p_f;
-    in.kf = P.kf_pose_f; in.kf_stride = 8; in.mis = P.mis_f; in.cams = P.cams_f;
+    in.kf = P.kf_pose_f; in.kf_stride = 8; in.mis = P.mis_f; in.cams = P.cams_f; in.kf_rot = nullptr;
   }
   return in;
+}
+
+// Rotation matrix R_I_M and |q|^2 of every keyframe (FP64 linearization):
+// built once per keyframe instead of twice per observation.
+__global__ void k_kf_rotations(const double* kf_state, int64_t nkf, double* out, const int* run_if,
+                               const int* skip_if) {
+  if (gated(run_if, skip_if)) return;
+  const int64_t k = blockIdx.x * (int64_t)blockDim.x + threadIdx.x;
+  if (k >= nkf) return;
+  const double* q = kf_state + 16 * k;
+  M3<double> R;
+  jplR(q, R);
+  double* o = out + 16 * k;
+#pragma unroll
+  for (int a = 0; a < 9; ++a) o[a] = R.m[a];
+  o[9] = q[0] * q[0] + q[1] * q[1] + q[2] * q[2] + q[3] * q[3];
 }
 
 template <typename T>
 cudaError_t launch_visual_linearize_gated(const DevProblem& P, VisualLin<T> out, double* cost_accum, const int* run_if,
                                           const int* skip_if, cudaStream_t s) {
   if (P.nobs == 0) return cudaSuccess;
+  if constexpr (sizeof(T) == 8)
+    k_kf_rotations<<<(unsigned)((P.nkf + 127) / 128), 128, 0, s>>>(P.kf_state, P.nkf, P.kf_rot, run_if, skip_if);
   // Block size: tuned per problem (mba_autotune), at most the launch bound.
   const int bs = (P.vis_block > 0 && P.vis_block <= kBlock) ? P.vis_block : kBlock;
   if (P.vis_pipe) {

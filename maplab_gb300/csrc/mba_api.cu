@@ -1380,6 +1380,7 @@ mba_status mba_create(const mba_problem_desc* d, int32_t device, mba_handle** ou
   P.lm_off = A.alloc<int32_t>(NL);
   if (NL && P.lm_off) cudaMemsetAsync(P.lm_off, 0, sizeof(int32_t) * NL, st);
   P.kf_state = A.upload(kf_state, st);
+  P.kf_rot = A.alloc<double>(16 * NK + 16);
   P.kf_mis = A.upload(kfm, st);
   P.kf_flags = A.upload(flags, st);
   P.kf_mask = A.upload(mask, st);
