@@ -391,6 +391,93 @@ __global__ void __launch_bounds__(kTailThreads) k_chain_tail(SolverLaunch<T> s, 
   block_add_d(acc, rz);
 }
 
+// The same levels with the survivors' w and z in shared memory (tail index
+// j = position >> l0): only the factor rows come from global memory.  Used
+// when 2 ceil(n / 2^l0) x 16 values fit in kTailSmem bytes.
+constexpr int kTailSmem = 96 * 1024;
+template <typename T>
+__global__ void __launch_bounds__(kTailThreads) k_chain_tail_sm(SolverLaunch<T> s, int l0, int seg, const T* rv, T* z,
+                                                                double* rz) {
+  if (apply_gate(s.ctl)) return;
+  extern __shared__ __align__(16) unsigned char tail_smem[];
+  const int64_t n = s.P.nkf;
+  const int L = s.S.chain_levels;
+  const int ns0 = (int)((n + ((int64_t)1 << l0) - 1) >> l0);
+  T* ws = reinterpret_cast<T*>(tail_smem);  // [ns0][16] w, then the solve's right-hand side
+  T* zs = ws + 16 * ns0;                    // [ns0][16] z
+  const int grp = threadIdx.x >> 4, r = threadIdx.x & 15, ngrp = kTailThreads / 16;
+  const unsigned mask = 0xffffu << (threadIdx.x & 16);
+  for (int i = threadIdx.x; i < 16 * ns0; i += kTailThreads) {
+    const int j = i >> 4, c = i & 15;
+    T v = T(0);
+    if (c < 15) {
+      v = s.C.w[15 * ((int64_t)j << l0) + c];
+      if (seg > 0 && j > 0) v -= s.C.lc[15 * (int64_t)j + c];
+    }
+    ws[i] = v;
+  }
+  __syncthreads();
+  for (int l = l0; l < L; ++l) {
+    const int st = 1 << (l - l0), cnt = (ns0 + 2 * st - 1) / (2 * st);
+    for (int j = grp; j < cnt; j += ngrp) {
+      const int q = 2 * st * j;
+      if (r < 15) {
+        T v = ws[16 * q + r];
+        if (q >= st) v -= row_dot(s.C.XR + 225 * ((int64_t)(q - st) << l0), r, ws + 16 * (q - st));
+        if (q + st < ns0) v -= row_dot(s.C.XL + 225 * ((int64_t)(q + st) << l0), r, ws + 16 * (q + st));
+        ws[16 * q + r] = v;
+      }
+    }
+    __syncthreads();
+  }
+  double acc = 0.0;
+  if (grp == 0 && r < 15) {
+    const T zr = row_dot(s.C.F, r, ws);
+    zs[r] = zr;
+    const int64_t k = s.S.chain_perm[0];
+    z[15 * k + r] = zr;
+    acc += (double)rv[15 * k + r] * (double)zr;
+  }
+  __syncthreads();
+  for (int l = L - 1; l >= l0; --l) {
+    const int st = 1 << (l - l0), cnt = ns0 > st ? (ns0 - st + 2 * st - 1) / (2 * st) : 0;
+    const int passes = (cnt + ngrp - 1) / ngrp;
+    for (int qq = 0; qq < passes; ++qq) {
+      const int p = st + 2 * st * (grp + qq * ngrp);
+      const bool act = p < ns0 && r < 15;
+      const int64_t gp = (int64_t)p << l0;
+      if (act) {
+        T v = ws[16 * p + r];
+        v -= row_dot(s.C.CL + 225 * gp, r, zs + 16 * (p - st));
+        if (p + st < ns0) v -= row_dot(s.C.CR + 225 * gp, r, zs + 16 * (p + st));
+        ws[16 * p + r] = v;
+      }
+      __syncwarp(mask);
+      if (act) {
+        const T zr = row_dot(s.C.F + 225 * gp, r, ws + 16 * p);
+        zs[16 * p + r] = zr;
+        const int64_t k = s.S.chain_perm[gp];
+        z[15 * k + r] = zr;
+        acc += (double)rv[15 * k + r] * (double)zr;
+      }
+      __syncwarp(mask);
+    }
+    __syncthreads();
+  }
+  block_add_d(acc, rz);
+}
+
+// One-block tail from level l0 (seg > 0: segmented sweeps).
+template <typename T>
+void launch_tail(const SolverLaunch<T>& s, int l0, int seg, const T* r, T* z, double* rz, cudaStream_t st) {
+  const int64_t ns0 = (s.P.nkf + ((int64_t)1 << l0) - 1) >> l0;
+  const int64_t bytes = 2 * 16 * ns0 * (int64_t)sizeof(T);
+  if (bytes <= kTailSmem)
+    k_chain_tail_sm<T><<<1, kTailThreads, (size_t)bytes, st>>>(s, l0, seg, r, z, rz);
+  else
+    k_chain_tail<T><<<1, kTailThreads, 0, st>>>(s, l0, seg, r, z, rz);
+}
+
 constexpr int kSegThreads = 256;  // 16 positions at a time, thread r of a position owns row r
 
 // Segmented forward sweep: block j runs levels 0..m-1 on positions
@@ -530,7 +617,7 @@ cudaError_t chain_apply(const SolverLaunch<T>& s, const T* r, T* z, double* rz, 
     const unsigned blocks = nb(n, 1 << m);
     const size_t sm = sizeof(T) * 16 * (size_t)(1 << m);
     k_chain_seg_fwd<T><<<blocks, kSegThreads, sm, st>>>(s, m, r);
-    k_chain_tail<T><<<1, kTailThreads, 0, st>>>(s, m, m, r, z, rz);
+    launch_tail<T>(s, m, m, r, z, rz, st);
     k_chain_seg_bwd<T><<<blocks, kSegThreads, 2 * sm + sizeof(T) * 16, st>>>(s, m, r, z, rz);
     return cudaGetLastError();
   }
@@ -539,7 +626,7 @@ cudaError_t chain_apply(const SolverLaunch<T>& s, const T* r, T* z, double* rz, 
     const int64_t sd = (int64_t)1 << l, ns = (n + 2 * sd - 1) / (2 * sd);
     k_chain_fwd<T><<<nb(16 * ns, 128), 128, 0, st>>>(s, l);
   }
-  k_chain_tail<T><<<1, kTailThreads, 0, st>>>(s, l0 < 1 ? 1 : l0, 0, r, z, rz);
+  launch_tail<T>(s, l0 < 1 ? 1 : l0, 0, r, z, rz, st);
   for (int l = (l0 < 1 ? 1 : l0) - 1; l >= 0; --l) {
     const int64_t sd = (int64_t)1 << l, ne = n > sd ? (n - sd + 2 * sd - 1) / (2 * sd) : 0;
     if (ne) k_chain_bwd<T><<<nb(16 * ne, 128), 128, 0, st>>>(s, l, r, z, rz);
@@ -548,6 +635,14 @@ cudaError_t chain_apply(const SolverLaunch<T>& s, const T* r, T* z, double* rz, 
   return cudaGetLastError();
 }
 
+// Shared-memory opt-in of the tail kernel (outside graph capture).
+template <typename T>
+cudaError_t chain_prepare() {
+  return cudaFuncSetAttribute(k_chain_tail_sm<T>, cudaFuncAttributeMaxDynamicSharedMemorySize, kTailSmem);
+}
+
+template cudaError_t chain_prepare<double>();
+template cudaError_t chain_prepare<float>();
 template cudaError_t chain_factor<double>(const SolverLaunch<double>&, cudaStream_t);
 template cudaError_t chain_factor<float>(const SolverLaunch<float>&, cudaStream_t);
 template cudaError_t chain_apply<double>(const SolverLaunch<double>&, const double*, double*, double*, cudaStream_t);

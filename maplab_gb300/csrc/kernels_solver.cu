@@ -1343,7 +1343,8 @@ template <typename T>
 cudaError_t solver_prepare(const SchurPattern& S) {
   int64_t cap = 0;
   const int64_t bytes = schur_pairs_smem<T>(S, &cap);
-  if (bytes <= 48 * 1024) return cudaSuccess;
+  const cudaError_t e = chain_prepare<T>();
+  if (e != cudaSuccess || bytes <= 48 * 1024) return e;
   return cudaFuncSetAttribute(k_schur_pairs<T>, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)bytes);
 }
 

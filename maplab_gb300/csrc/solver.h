@@ -222,6 +222,8 @@ cudaError_t solver_build_reduced(const SolverLaunch<T>& s, cudaStream_t st);
 // kernel); call before the solver's kernels are launched or captured.
 template <typename T>
 cudaError_t solver_prepare(const SchurPattern& S);
+template <typename T>
+cudaError_t chain_prepare();
 // The Schur pair kernel alone (autotuning).
 template <typename T>
 cudaError_t solver_schur_pairs(const SolverLaunch<T>& s, cudaStream_t st);
