@@ -55,6 +55,39 @@ def test_jpl_yaw_jacobian_numeric():
     np.testing.assert_allclose(J, ridders(f, 0.0), atol=1e-10)
 
 
+def _rpy_jpl(q):
+    """getRollPitchYawFromQuaternionJpl: R = toRotationMatrixJPL(q), then
+    RotationMatrixToRollPitchYaw (maplab-common geometry-inl.h:40-60)."""
+    R = np.zeros(9)
+    O.load().oracle_rotation_matrix(N.ptr(O.arr(q)), N.ptr(R))
+    R = R.reshape(3, 3)
+    pitch = math.atan2(-R[2, 0], math.sqrt(R[0, 0] ** 2 + R[1, 0] ** 2))
+    c = math.cos(pitch)
+    assert abs(c) > 1e-12
+    return np.array([math.atan2(R[2, 1] / c, R[2, 2] / c), pitch, math.atan2(R[1, 0] / c, R[0, 0] / c)])
+
+
+def test_jpl_yaw_plus_keeps_roll_pitch():
+    """test_quaternion_parameterization_test.cc:33-58 (JplYawQuaternionParameterization.Plus):
+    deltas -0.5, 0, 0.5, 1 applied in turn keep roll and pitch to 1e-6, and the
+    yaw returns to its start exactly when the deltas sum to zero."""
+    lib = O.load()
+    q = unit_quat(1, 0, 1, 1)  # Eigen::Quaterniond(1, 1, 0, 1), xyzw
+    rpy0 = _rpy_jpl(q)
+    total = 0.0
+    for delta in (-0.5, 0.0, 0.5, 1.0):
+        out = np.zeros(4)
+        lib.oracle_yaw_plus(N.ptr(O.arr(q)), N.ptr(O.arr([delta])), N.ptr(out))
+        total += delta
+        q = out
+        rpy = _rpy_jpl(q)
+        assert abs(rpy[0] - rpy0[0]) <= 1e-6 and abs(rpy[1] - rpy0[1]) <= 1e-6
+        if total == 0.0:
+            assert abs(rpy[2] - rpy0[2]) <= 1e-6
+        else:
+            assert rpy[2] != rpy0[2]
+
+
 def test_jpl_roll_pitch_jacobian_numeric():
     lib = O.load()
     # Eigen::Quaterniond q_IM(1, 1, 5, 0), q_GM(1, 5, 0, 2) (w first).
