@@ -85,6 +85,15 @@ __global__ void __launch_bounds__(kB) k_zero(T* a, int64_t n, const int* run_if,
     a[i] = T(0);
 }
 
+// Upper triangle of a symmetric 6x6 block, row by row: entry t (< 21) is
+// (up_row(t), up_col(t)); kPoseUp = 24 floats per keyframe (21 + 3 pad, six
+// float4).
+constexpr int kPoseUp = 24;
+__host__ __device__ constexpr int up_row(int t) { return t < 6 ? 0 : t < 11 ? 1 : t < 15 ? 2 : t < 18 ? 3 : t < 20 ? 4 : 5; }
+__host__ __device__ constexpr int up_col(int t) {
+  return t < 6 ? t : t < 11 ? t - 5 : t < 15 ? t - 9 : t < 18 ? t - 12 : t < 20 ? t - 14 : t - 15;
+}
+
 // One thread per landmark: H_ll, g_l, slot blocks W and the direct
 // camera-camera terms of its observations.  The keyframes' 6x6 pose blocks of
 // D are symmetric: only their upper triangle is accumulated here (and by the
@@ -159,20 +168,28 @@ __global__ void __launch_bounds__(kB, sizeof(T) == 4 ? 2 : 1) k_assemble_lm(DevP
     const T* Y = st < ob ? Jo : Js;
     if constexpr (sizeof(T) == 4) {
       // 16-byte vector atomics: the (store, observer) block, the observer's
-      // pose block (full 6x6) and its gradient.
+      // pose block (its 21 upper-triangle values) and its gradient.
       float4* P4 = reinterpret_cast<float4*>(Pb);
-      float4* D4 = reinterpret_cast<float4*>(L.Dpose + 36 * (int64_t)ob);
+      float4* D4 = reinterpret_cast<float4*>(L.Dpose + kPoseUp * (int64_t)ob);
       float4* g4 = reinterpret_cast<float4*>(L.gpose + 8 * (int64_t)ob);
 #pragma unroll
       for (int q = 0; q < 9; ++q) {
-        float pv[4], dv[4];
+        float pv[4];
 #pragma unroll
         for (int u = 0; u < 4; ++u) {
           const int a = (4 * q + u) / 6, b = (4 * q + u) % 6;
           pv[u] = X[a] * Y[b] + X[6 + a] * Y[6 + b];
-          dv[u] = Jo[a] * Jo[b] + Jo[6 + a] * Jo[6 + b];
         }
         atomicAdd(P4 + q, make_float4(pv[0], pv[1], pv[2], pv[3]));
+      }
+#pragma unroll
+      for (int q = 0; q < kPoseUp / 4; ++q) {
+        float dv[4];
+#pragma unroll
+        for (int u = 0; u < 4; ++u) {
+          const int t = 4 * q + u, a = up_row(t), b = up_col(t);
+          dv[u] = t < 21 ? Jo[a] * Jo[b] + Jo[6 + a] * Jo[6 + b] : 0.f;
+        }
         atomicAdd(D4 + q, make_float4(dv[0], dv[1], dv[2], dv[3]));
       }
       float gv[6];
@@ -202,15 +219,15 @@ __global__ void __launch_bounds__(kB, sizeof(T) == 4 ? 2 : 1) k_assemble_lm(DevP
   for (int a = 0; a < 18; ++a) L.Wslot[kSlotStride * s0 + a] = Wst[a];
   if (any_cam) {
     if constexpr (sizeof(T) == 4) {
-      float4* D4 = reinterpret_cast<float4*>(L.Dpose + 36 * (int64_t)st);
+      float4* D4 = reinterpret_cast<float4*>(L.Dpose + kPoseUp * (int64_t)st);
       float4* g4 = reinterpret_cast<float4*>(L.gpose + 8 * (int64_t)st);
 #pragma unroll
-      for (int q = 0; q < 9; ++q) {
+      for (int q = 0; q < kPoseUp / 4; ++q) {
         float dv[4];
 #pragma unroll
         for (int u = 0; u < 4; ++u) {
-          const int a = (4 * q + u) / 6, b = (4 * q + u) % 6;
-          dv[u] = a <= b ? Dst[6 * a + b] : Dst[6 * b + a];
+          const int t = 4 * q + u;
+          dv[u] = t < 21 ? Dst[6 * up_row(t) + up_col(t)] : 0.f;
         }
         atomicAdd(D4 + q, make_float4(dv[0], dv[1], dv[2], dv[3]));
       }
@@ -227,16 +244,17 @@ __global__ void __launch_bounds__(kB, sizeof(T) == 4 ? 2 : 1) k_assemble_lm(DevP
   }
 }
 
-// FP32 path: adds the vector-accumulated visual pose blocks (full 6x6) and
-// gradients into D and g_c (before the lower triangles are mirrored).
+// FP32 path: adds the vector-accumulated visual pose blocks (upper triangle)
+// and gradients into D and g_c (before the lower triangles are mirrored).
 __global__ void __launch_bounds__(kB) k_merge_pose(int64_t nkf, const float* Dpose, const float* gpose, float* D,
                                                    float* gc, const int* run_if, const int* skip_if) {
   if (gated(run_if, skip_if)) return;
   const int64_t i = blockIdx.x * (int64_t)blockDim.x + threadIdx.x;
-  if (i >= 42 * nkf) return;
-  const int64_t k = i / 42, q = i % 42;
-  if (q < 36) D[225 * k + 15 * (q / 6) + q % 6] += Dpose[36 * k + q];
-  else gc[15 * k + q - 36] += gpose[8 * k + q - 36];
+  if (i >= 27 * nkf) return;
+  const int64_t k = i / 27;
+  const int q = (int)(i % 27);
+  if (q < 21) D[225 * k + 15 * up_row(q) + up_col(q)] += Dpose[kPoseUp * k + q];
+  else gc[15 * k + q - 21] += gpose[8 * k + q - 21];
 }
 
 // One warp per inertial edge.
@@ -1221,7 +1239,7 @@ cudaError_t solver_assemble(const SolverLaunch<T>& s, const int* gate, cudaStrea
   k_zero<T><<<gridcap(15 * s.P.nkf), kB, 0, st>>>(s.L.gc, 15 * s.P.nkf, gate, skip);
   if (s.S.npu) k_zero<T><<<gridcap(36 * s.S.npu), kB, 0, st>>>(s.L.Pbase, 36 * s.S.npu, gate, skip);
   if constexpr (sizeof(T) == 4) {
-    k_zero<float><<<gridcap(36 * s.P.nkf), kB, 0, st>>>(s.L.Dpose, 36 * s.P.nkf, gate, skip);
+    k_zero<float><<<gridcap(kPoseUp * s.P.nkf), kB, 0, st>>>(s.L.Dpose, kPoseUp * s.P.nkf, gate, skip);
     k_zero<float><<<gridcap(8 * s.P.nkf), kB, 0, st>>>(s.L.gpose, 8 * s.P.nkf, gate, skip);
   }
   // Relinearizations inside the LM loop (gate set) assemble with the fixed
@@ -1231,7 +1249,7 @@ cudaError_t solver_assemble(const SolverLaunch<T>& s, const int* gate, cudaStrea
   if (s.P.nedge)
     k_assemble_inertial<T><<<nblk(32 * s.P.nedge, 128), 128, 0, st>>>(s.P, s.ine, s.L, scaled, gate, skip);
   if constexpr (sizeof(T) == 4)
-    k_merge_pose<<<nblk(42 * s.P.nkf, kB), kB, 0, st>>>(s.P.nkf, s.L.Dpose, s.L.gpose, s.L.Dbase, s.L.gc, gate, skip);
+    k_merge_pose<<<nblk(27 * s.P.nkf, kB), kB, 0, st>>>(s.P.nkf, s.L.Dpose, s.L.gpose, s.L.Dbase, s.L.gc, gate, skip);
   k_mirror_pose_blocks<T><<<nblk(15 * s.P.nkf, kB), kB, 0, st>>>(s.P.nkf, s.L.Dbase, gate, skip);
   if constexpr (sizeof(T) == 8)
     if (s.P.ng > 0) {
@@ -1487,13 +1505,13 @@ cudaError_t solver_reject_and_restart(const SolverLaunch<T>& s, int use_reprojec
   k_zero<T><<<gridcap(15 * s.P.nkf), kB, 0, st>>>(s.L.gc, 15 * s.P.nkf, run, nullptr);
   if (s.S.npu) k_zero<T><<<gridcap(36 * s.S.npu), kB, 0, st>>>(s.L.Pbase, 36 * s.S.npu, run, nullptr);
   if constexpr (sizeof(T) == 4) {
-    k_zero<float><<<gridcap(36 * s.P.nkf), kB, 0, st>>>(s.L.Dpose, 36 * s.P.nkf, run, nullptr);
+    k_zero<float><<<gridcap(kPoseUp * s.P.nkf), kB, 0, st>>>(s.L.Dpose, kPoseUp * s.P.nkf, run, nullptr);
     k_zero<float><<<gridcap(8 * s.P.nkf), kB, 0, st>>>(s.L.gpose, 8 * s.P.nkf, run, nullptr);
   }
   if (s.P.nlm) k_assemble_lm<T><<<nblk(s.P.nlm, kB), kB, 0, st>>>(s.P, s.S, s.vis, s.L, 0, run, nullptr);
   if (s.P.nedge) k_assemble_inertial<T><<<nblk(32 * s.P.nedge, 128), 128, 0, st>>>(s.P, s.ine, s.L, 0, run, nullptr);
   if constexpr (sizeof(T) == 4)
-    k_merge_pose<<<nblk(42 * s.P.nkf, kB), kB, 0, st>>>(s.P.nkf, s.L.Dpose, s.L.gpose, s.L.Dbase, s.L.gc, run,
+    k_merge_pose<<<nblk(27 * s.P.nkf, kB), kB, 0, st>>>(s.P.nkf, s.L.Dpose, s.L.gpose, s.L.Dbase, s.L.gc, run,
                                                         nullptr);
   k_mirror_pose_blocks<T><<<nblk(15 * s.P.nkf, kB), kB, 0, st>>>(s.P.nkf, s.L.Dbase, run, nullptr);
   const int64_t n = 15 * s.P.nkf + 3 * s.P.nlm + s.P.nsw;

@@ -312,7 +312,7 @@ mba_status ensure_solver_buffers(mba_handle* h, SolverBuffers<T>& b) {
   L.dl = A.alloc<double>(3 * NL);
   L.skf = A.alloc<T>(15 * NB);
   L.slm = A.alloc<T>(3 * NL);
-  L.Dpose = A.alloc<float>(sizeof(T) == 4 ? 36 * NK : 1);
+  L.Dpose = A.alloc<float>(sizeof(T) == 4 ? 24 * NK : 1);
   L.gpose = A.alloc<float>(sizeof(T) == 4 ? 8 * NK : 1);
   L.swH = A.alloc<T>(P.nsw);
   L.swg = A.alloc<T>(P.nsw);

@@ -135,7 +135,7 @@ struct LinearSystem {
   // damped inverse, the scaled step.
   // FP32 path: the visual terms' 6x6 pose blocks of D and their gradient,
   // accumulated with 16-byte vector atomics and merged into Dbase / gc.
-  float* Dpose;  // [nkf][36]
+  float* Dpose;  // [nkf][24]: upper triangle of the visual pose block (21 used)
   float* gpose;  // [nkf][8] (6 used)
   T* swH;        // [nsw]
   T* swg;        // [nsw]
