@@ -36,7 +36,7 @@ typedef struct mba_synth_config {
   int64_t num_landmarks;
   int32_t landmark_mode;          /* MBA_SYNTH_LANDMARKS_* */
   int32_t track_model;            /* MBA_SYNTH_TRACK_* */
-  int32_t track_min, track_max;   /* uniform bounds, or [2, cap] for the other models */
+  int32_t track_min, track_max;   /* uniform bounds; power law: [max(2, track_min), cap]; geometric: [2, cap] */
   double track_mean;              /* geometric mean */
   double track_alpha;             /* power-law exponent */
   int32_t num_cameras;            /* 1 or 2 */

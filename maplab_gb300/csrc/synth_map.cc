@@ -468,7 +468,9 @@ mba_status mba_synth_generate(const mba_synth_config* cfg, mba_synth_map** out) 
   // Track-length sampler.
   std::vector<double> plcdf;
   if (cfg->track_model == MBA_SYNTH_TRACK_POWER_LAW) {
-    for (int k = 2; k <= cfg->track_max; ++k) plcdf.push_back(std::pow((double)k, -cfg->track_alpha));
+    // p(L) ~ L^-alpha on [max(2, track_min), track_max]
+    for (int k = std::max(2, cfg->track_min); k <= cfg->track_max; ++k)
+      plcdf.push_back(std::pow((double)k, -cfg->track_alpha));
     std::partial_sum(plcdf.begin(), plcdf.end(), plcdf.begin());
     for (double& v : plcdf) v /= plcdf.back();
   }
@@ -481,7 +483,7 @@ mba_status mba_synth_generate(const mba_synth_config* cfg, mba_synth_map** out) 
       return std::min(std::max(L, 2), cfg->track_max);
     }
     const double u = rng.uniform();
-    return 2 + (int)(std::lower_bound(plcdf.begin(), plcdf.end(), u) - plcdf.begin());
+    return std::max(2, cfg->track_min) + (int)(std::lower_bound(plcdf.begin(), plcdf.end(), u) - plcdf.begin());
   };
 
   const int64_t NL = cfg->landmarks_per_keyframe > 0 ? (int64_t)cfg->landmarks_per_keyframe * NK : cfg->num_landmarks;

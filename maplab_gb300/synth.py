@@ -14,7 +14,7 @@ test/vi-map-generator-6dof recipe):
 * ``c4``: 10 co-registered missions (2,000 keyframes each), 2M landmarks,
   10 % of landmarks shared between two missions (kGlobal terms).
 * ``c5``: 40 missions x 1,250 keyframes, 5M landmarks, power-law tracks
-  (alpha 2.2, cap 200).
+  (alpha 2.2, lengths 3 to 200).
 """
 import ctypes
 
@@ -67,6 +67,7 @@ def config(preset="c1", seed=None, **overrides):
         c.landmark_mode = N.MBA_SYNTH_LANDMARKS_FRUSTUM
         c.track_model = N.MBA_SYNTH_TRACK_POWER_LAW
         c.track_alpha = 2.2
+        c.track_min = 3  # lower cut-off of the power law: mean track about 8.8, about 44M observations
         c.track_max = 200
         c.num_cameras = 2
         c.shared_landmark_fraction = 0.02
