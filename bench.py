@@ -329,6 +329,32 @@ def batched_missions(args, device):
             "launches_per_solve": 1}
 
 
+def largest_map(args, device):
+    """The 50,000-keyframe, 40-mission map (about 40M observations): one mixed
+    chain-preconditioned solve of 6 LM iterations (PCG <= 25, device loop,
+    autotuned), its time, the FP64 re-evaluation of its final state and the
+    device memory it holds."""
+    from maplab_gb300 import _native as N
+    from maplab_gb300 import ba, synth
+    m = synth.generate("c5")
+    d = m.desc
+    o = ba.default_options(max_num_iterations=6, max_linear_iterations=25, linear_tolerance=1e-6,
+                           precision=N.MBA_PRECISION_MIXED, preconditioner=N.MBA_PRECOND_CHAIN, use_cuda_graph=2,
+                           check_tolerances=0, outlier_use_reprojection_error=args.reproj_rejection)
+    s, tune_s, tun, g = _tuned_solve(d, device, N.MBA_PRECISION_MIXED, o)
+    cost64 = g.cost()
+    st = g.stats()
+    g.close()
+    t = s["iterations"][-1]["time_ms"] / 1e3
+    its = s["num_iterations"] - 1
+    return {"workload": f"c5: {d.num_missions} missions, {d.num_keyframes} keyframes, {d.num_landmarks} landmarks, "
+                        f"{d.num_observations} observations",
+            "solve": "mixed precision, chain preconditioner, PCG <= 25, 6 LM iterations, one graph launch",
+            "solve_s": t, "iterations": its, "s_per_iteration": t / max(1, its), "autotune_s": tune_s,
+            "initial_cost": s["initial_cost"], "final_cost": s["final_cost"], "final_cost_fp64_eval": cost64,
+            "pcg_iterations": s["linear_iterations"], "device_bytes": st["device_bytes"], "tuning": tun}
+
+
 def ba_cpu_baseline(device):
     """The oracle's LM on the host cores beside the device FP64 solve of the
     same problem: the 100-keyframe map in full (10 iterations, dense Schur +
@@ -463,6 +489,7 @@ def run_ours(args):
     # ---- BA time-to-cost-tolerance (rank-local)
     ba_info = ba_time_to_cost(args, local) if args.solve else None
     c3_info = batched_missions(args, local) if args.c3 else None
+    c5_info = largest_map(args, local) if args.c5 else None
 
     # ---- CPU baselines (rank 0, N=1 only): the oracle on the host cores
     cpu = None
@@ -500,6 +527,7 @@ def run_ours(args):
             "mixed_f32": mixed32,
             "ba_time_to_cost_tol": ba_info,
             "batched_missions": c3_info,
+            "largest_map": c5_info,
             "ba_cpu_baseline": ba_cpu,
         }
         print(json.dumps(line), flush=True)
@@ -519,6 +547,7 @@ def main():
     ap.add_argument("--ba-cpu", type=int, default=1)
     ap.add_argument("--ba-config", default="c4")
     ap.add_argument("--c3", type=int, default=1)
+    ap.add_argument("--c5", type=int, default=1)
     ap.add_argument("--fast-pcg", type=int, default=25)
     ap.add_argument("--c3-pcg", type=int, default=25)
     ap.add_argument("--reproj-rejection", type=int, default=1)
