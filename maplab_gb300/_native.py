@@ -247,6 +247,8 @@ class Tuning(ctypes.Structure):
         ("chain_apply_ms", ctypes.c_double),
         ("visual_pipelined", ctypes.c_int32),
         ("chain_segment", ctypes.c_int32),
+        ("chain_tail_smem", ctypes.c_int32),
+        ("pad_", ctypes.c_int32),
     ]
 
 

@@ -472,7 +472,7 @@ template <typename T>
 void launch_tail(const SolverLaunch<T>& s, int l0, int seg, const T* r, T* z, double* rz, cudaStream_t st) {
   const int64_t ns0 = (s.P.nkf + ((int64_t)1 << l0) - 1) >> l0;
   const int64_t bytes = 2 * 16 * ns0 * (int64_t)sizeof(T);
-  if (bytes <= kTailSmem)
+  if (s.S.chain_tail_sm && bytes <= kTailSmem)
     k_chain_tail_sm<T><<<1, kTailThreads, (size_t)bytes, st>>>(s, l0, seg, r, z, rz);
   else
     k_chain_tail<T><<<1, kTailThreads, 0, st>>>(s, l0, seg, r, z, rz);

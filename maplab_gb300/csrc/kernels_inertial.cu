@@ -21,8 +21,8 @@
 //                     from shared memory (FP64 path); Cholesky, whitening,
 //                     residual and Jacobians in FP64 (inertial_tail).
 //   k_inertial_mat_cols the same chain in FP32 (mixed path) with one half-warp
-//                     per edge and one column per lane, in registers; the
-//                     FP64 part as above.
+//                     per edge and one column per lane, in registers;
+//   k_inertial_whiten  its FP64 part (inertial_tail), one warp per edge.
 #include <cuda_runtime.h>
 
 #include "internal.h"
@@ -474,17 +474,16 @@ __global__ void __launch_bounds__(32 * kWarps) k_inertial_mat(DevProblem P, cons
 // transposes (PC^T in the stage covariance, M^T and M A^T in the Q update)
 // and the rows of A go through shared memory.  Rows of D, td, A and M are
 // kept for the active rows 0-2, 6-8, 12-14 only (index i -> row kAct(i)).
-// The FP64 part then runs for the warp's two edges one after the other.
+// Q_acc and Phi_acc go to qp_out [edge][450] (row-major, Q then Phi) for the
+// FP64 whitening kernel.
 __device__ __forceinline__ constexpr int kAct(int i) { return i < 3 ? i : (i < 6 ? i + 3 : i + 6); }
 
 template <int kWarps>
-__global__ void __launch_bounds__(32 * kWarps, 4) k_inertial_mat_cols(DevProblem P, const double* kf_state,
-                                                                   const float* stage_in, const double* dt_in,
-                                                                   const double* end_in, InertialOutputs out,
+__global__ void __launch_bounds__(32 * kWarps, 4) k_inertial_mat_cols(DevProblem P, const float* stage_in,
+                                                                   const double* dt_in, float* qp_out,
                                                                    const int* skip_if) {
   if (gated_i(skip_if)) return;
-  __shared__ __align__(16) float ex[kWarps][2][512];  // per edge: X [16][16] then Y [16][16]; Q | Phi at the end
-  __shared__ double Ld[kWarps][225], Xd[kWarps][225], rsh[kWarps][16];
+  __shared__ __align__(16) float ex[kWarps][2][512];  // per edge: X [16][16] then Y [16][16]
   const int w = threadIdx.x >> 5, lane = threadIdx.x & 31, h = lane >> 4, c = lane & 15;
   const int64_t e0 = 2 * (blockIdx.x * (int64_t)kWarps + w);
   if (e0 >= P.nimu) return;  // uniform over the warp
@@ -612,22 +611,32 @@ __global__ void __launch_bounds__(32 * kWarps, 4) k_inertial_mat_cols(DevProblem
       for (int i = 0; i < 9; ++i) Phi[kAct(i)] += Nn[i];
       __syncwarp(hm);  // X and Y are rewritten by the next step
     }
-    if (col)
+    if (col) {
+      float* o = qp_out + 450 * e;
 #pragma unroll
       for (int r = 0; r < 15; ++r) {
-        X[15 * r + c] = Q[r];         // Q_acc at [0, 225)
-        X[225 + 15 * r + c] = Phi[r];  // Phi_acc at [225, 450)
+        o[15 * r + c] = Q[r];
+        o[225 + 15 * r + c] = Phi[r];
       }
-  }
-  __syncwarp();
-  for (int hh = 0; hh < 2; ++hh) {
-    const int64_t ee = e0 + hh;
-    if (ee < P.nimu) {  // uniform over the warp
-      const float* Qa = ex[w][hh];
-      inertial_tail<float>(P, kf_state, end_in, out, ee, Qa, Qa + 225, Ld[w], Xd[w], rsh[w], lane);
-      __syncwarp();
     }
   }
+}
+
+// FP64 whitening, residual and Jacobians of the mixed path: one warp per
+// edge from the FP32 Q_acc / Phi_acc of k_inertial_mat_cols.
+template <int kWarps>
+__global__ void __launch_bounds__(32 * kWarps) k_inertial_whiten(DevProblem P, const double* kf_state,
+                                                                 const float* qp_in, const double* end_in,
+                                                                 InertialOutputs out, const int* skip_if) {
+  if (gated_i(skip_if)) return;
+  __shared__ float qs[kWarps][450];
+  __shared__ double Ld[kWarps][225], Xd[kWarps][225], rsh[kWarps][16];
+  const int w = threadIdx.x >> 5, lane = threadIdx.x & 31;
+  const int64_t e = blockIdx.x * (int64_t)kWarps + w;
+  if (e >= P.nimu) return;
+  for (int a = lane; a < 450; a += 32) qs[w][a] = qp_in[450 * e + a];
+  __syncwarp();
+  inertial_tail<float>(P, kf_state, end_in, out, e, qs[w], qs[w] + 225, Ld[w], Xd[w], rsh[w], lane);
 }
 
 }  // namespace
@@ -652,8 +661,10 @@ cudaError_t launch_inertial_v2(const DevProblem& P, const double* kf_state, bool
   if (f32_matrices) {
     k_inertial_state<float><<<gA, 128, 0, s>>>(P, kf_state, (float*)stage, dt, endst, status, skip_if);
     constexpr int W = 4;  // two edges per warp
+    float* qp = reinterpret_cast<float*>(endst + 16 * P.nimu + 60 * nsteps);
     k_inertial_mat_cols<W><<<(unsigned)((P.nimu + 2 * W - 1) / (2 * W)), 32 * W, 0, s>>>(
-        P, kf_state, (const float*)stage, dt, endst, o, skip_if);
+        P, (const float*)stage, dt, qp, skip_if);
+    k_inertial_whiten<W><<<(unsigned)((P.nimu + W - 1) / W), 32 * W, 0, s>>>(P, kf_state, qp, endst, o, skip_if);
   } else {
     k_inertial_state<double><<<gA, 128, 0, s>>>(P, kf_state, (double*)stage, dt, endst, status, skip_if);
     constexpr int W = 1;

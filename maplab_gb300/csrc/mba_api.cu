@@ -1488,9 +1488,10 @@ mba_status mba_create(const mba_problem_desc* d, int32_t device, mba_handle** ou
   h->tuning.schur_chunk = (int32_t)kSchurChunk;
   h->tuning.chain_tail_nodes = 128;
   h->tuning.chain_segment = 1;
+  h->tuning.chain_tail_smem = 2;
   // Inertial scratch (kernels_inertial.cu): dt per step, end state per edge,
-  // 4 RK4 stages x 15 values per step.
-  P.ine_scratch = A.alloc<double>((NSMP - NIMU) + 16 * NIMU + 60 * (NSMP - NIMU) + 1);
+  // 4 RK4 stages x 15 values per step, FP32 Q_acc | Phi_acc per edge.
+  P.ine_scratch = A.alloc<double>((NSMP - NIMU) + 16 * NIMU + 60 * (NSMP - NIMU) + 225 * NIMU + 1);
   h->scratch = A.alloc<double>(4);
   h->iscratch = A.alloc<int>(4);
   if (A.err != cudaSuccess || cudaStreamSynchronize(st) != cudaSuccess) {
@@ -2349,21 +2350,31 @@ mba_status autotune(mba_handle* h, mba_tuning* out) {
   tbest = 1e30;
   const int levels = h->S.chain_levels;
   h->S.chain_seg = 0;
+  h->S.chain_tail_sm = 0;
   for (int nodes : {32, 64, 128, 256, 512}) {
     h->S.chain_tail = chain_tail_level(h->P.nkf, levels, nodes);
     SolverLaunch<T> sc = make_launch<T>(h, b, o);
     const double t = time_ms(st, 2, 10, [&]() { chain_apply<T>(sc, sc.L.rhs, sc.L.z, &h->ctl->pcg_rz0, st); });
-    if (t < tbest) { tbest = t; best.chain_tail_nodes = nodes; best.chain_segment = 1; best.chain_apply_ms = t; }
+    if (t < tbest) {
+      tbest = t;
+      best.chain_tail_nodes = nodes;
+      best.chain_segment = 1;
+      best.chain_tail_smem = 2;
+      best.chain_apply_ms = t;
+    }
   }
-  // segmented sweeps: positions per block
-  for (int seg : {16, 32, 64, 128}) {
-    h->S.chain_seg = chain_segment_level(seg);
-    SolverLaunch<T> sc = make_launch<T>(h, b, o);
-    const double t = time_ms(st, 2, 10, [&]() { chain_apply<T>(sc, sc.L.rhs, sc.L.z, &h->ctl->pcg_rz0, st); });
-    if (t < tbest) { tbest = t; best.chain_segment = seg; best.chain_apply_ms = t; }
-  }
+  // segmented sweeps: positions per block; the tail's vectors in shared or global memory
+  for (int seg : {16, 32, 64, 128})
+    for (int tsm : {1, 2}) {
+      h->S.chain_seg = chain_segment_level(seg);
+      h->S.chain_tail_sm = tsm == 1;
+      SolverLaunch<T> sc = make_launch<T>(h, b, o);
+      const double t = time_ms(st, 2, 10, [&]() { chain_apply<T>(sc, sc.L.rhs, sc.L.z, &h->ctl->pcg_rz0, st); });
+      if (t < tbest) { tbest = t; best.chain_segment = seg; best.chain_tail_smem = tsm; best.chain_apply_ms = t; }
+    }
   h->S.chain_tail = chain_tail_level(h->P.nkf, levels, best.chain_tail_nodes);
   h->S.chain_seg = chain_segment_level(best.chain_segment);
+  h->S.chain_tail_sm = best.chain_tail_smem == 1;
   if (cudaStreamSynchronize(st) != cudaSuccess || cudaGetLastError() != cudaSuccess) return MBA_ERR_CUDA;
   h->tuning = best;
   if (out) *out = best;
@@ -2388,6 +2399,7 @@ mba_status mba_set_tuning(mba_handle* h, const mba_tuning* t) {
   if (t->schur_chunk < 0 || t->chain_tail_nodes < 0) return MBA_ERR_INVALID_ARG;
   if (t->chain_segment && (t->chain_segment > 128 || (t->chain_segment & (t->chain_segment - 1))))
     return MBA_ERR_INVALID_ARG;
+  if (t->chain_tail_smem < 0 || t->chain_tail_smem > 2) return MBA_ERR_INVALID_ARG;
   cudaSetDevice(h->device);
   if (t->visual_block) { h->P.vis_block = t->visual_block; h->tuning.visual_block = t->visual_block; }
   if (t->visual_min_blocks) {
@@ -2411,6 +2423,10 @@ mba_status mba_set_tuning(mba_handle* h, const mba_tuning* t) {
   if (t->chain_segment) {
     h->S.chain_seg = chain_segment_level(t->chain_segment);
     h->tuning.chain_segment = t->chain_segment;
+  }
+  if (t->chain_tail_smem) {
+    h->S.chain_tail_sm = t->chain_tail_smem == 1;
+    h->tuning.chain_tail_smem = t->chain_tail_smem;
   }
   return MBA_OK;
 }

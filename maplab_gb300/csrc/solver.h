@@ -56,6 +56,7 @@ struct SchurPattern {
   int32_t chain_tail = 0;    // first level handled by the single-block tail sweep
   int32_t chain_seg = 0;     // segmented sweeps: log2 of the positions one block sweeps through the
                              // levels below it (0: one launch per level)
+  int32_t chain_tail_sm = 0;  // 1: one-block tail with the survivors' vectors in shared memory
 };
 
 // Device control block of the LM loop (all scalars live on the device).

@@ -5,7 +5,8 @@ alpha = 0): the reduced system's diagonal blocks, and between consecutive
 keyframes of a chain the inertial block plus the pose-pose block.  numpy
 assembles T from mba_reduced_system and mba_chain_structure and solves it
 densely; the device applies T^-1 by block cyclic reduction, once with one
-launch per level and once per segment size of the segmented sweeps.  The map
+launch per level and once per segment size of the segmented sweeps, each
+with the one-block tail's vectors in shared and in global memory.  The map
 has 450 keyframes in three missions, so every segment size leaves a partial
 last segment and chain ends fall inside segments.
 """
@@ -63,14 +64,16 @@ def test_sweeps_match_dense_solve(chain_map, precision, tol):
         z_ref = np.linalg.solve(T, r.reshape(-1)).reshape(r.shape)
         out = {}
         for seg in SEGMENTS:
-            g.set_tuning(chain_segment=seg)
-            out[seg] = g.chain_apply(r, precision=precision, radius=radius)
+            for tsm in (1, 2):  # the tail's vectors in shared / global memory
+                g.set_tuning(chain_segment=seg, chain_tail_smem=tsm)
+                out[(seg, tsm)] = g.chain_apply(r, precision=precision, radius=radius)
     for seg, z in out.items():
         err = np.linalg.norm(z - z_ref) / np.linalg.norm(z_ref)
         assert err <= tol, (seg, err)
     if precision == N.MBA_PRECISION_FP64:
-        for seg in SEGMENTS[1:]:
-            np.testing.assert_allclose(out[seg], out[1], rtol=0, atol=1e-9 * np.abs(out[1]).max())
+        ref = out[(1, 2)]
+        for key, z in out.items():
+            np.testing.assert_allclose(z, ref, rtol=0, atol=1e-9 * np.abs(ref).max(), err_msg=str(key))
 
 
 def test_segment_setting_is_validated(chain_map):
