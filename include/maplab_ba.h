@@ -459,7 +459,8 @@ typedef struct mba_tuning {
                                  * level (0 in mba_set_tuning keeps the current setting) */
   int32_t chain_tail_smem;      /* 1: the one-block tail keeps the survivors' vectors in shared memory,
                                  * 2: in global memory (0 in mba_set_tuning keeps the current setting) */
-  int32_t pad_;
+  int32_t pcg_product;          /* PCG product: 1 reads each stored pose block once (transposed part by
+                                 * atomics), 2 reads it from both of its rows (0 keeps the setting) */
 } mba_tuning;
 mba_status mba_autotune(mba_handle* h, int32_t precision, mba_tuning* out);
 /* Applies tuning values (e.g. cached from an earlier mba_autotune of a

@@ -248,7 +248,7 @@ class Tuning(ctypes.Structure):
         ("visual_pipelined", ctypes.c_int32),
         ("chain_segment", ctypes.c_int32),
         ("chain_tail_smem", ctypes.c_int32),
-        ("pad_", ctypes.c_int32),
+        ("pcg_product", ctypes.c_int32),
     ]
 
 

@@ -756,6 +756,7 @@ __global__ void __launch_bounds__(kB) k_pcg_init(SolverLaunch<T> s) {
     s.L.r[i] = T(r);
     s.L.z[i] = T(z);
     s.L.p[i] = T(0);  // read with beta = 0 by the first product; must be finite
+    s.L.q[i] = T(0);  // the read-once product accumulates into q
     rr = r * r;
   }
   block_add(rz, &s.ctl->pcg_rz0);
@@ -859,6 +860,100 @@ __global__ void __launch_bounds__(128) k_pcg_spmv(SolverLaunch<T> s, int it, con
   block_add(pq, &ctl->pcg_pq[it % 3]);
 }
 
+// The same product reading each stored pose block once: the warp of row k
+// walks the upper blocks (k, j), j > k, adds B v_j to its own row and B^T v_k
+// to row j with atomics (lane c of a block owns column c).  q must be zero on
+// entry (k_pcg_init, k_pcg_update); p.q comes from k_pcg_pq once every row is
+// complete.  Keyframe rows only (no global nodes).
+template <typename T>
+__global__ void __launch_bounds__(128) k_pcg_spmv_sym(SolverLaunch<T> s, int it, const T* pa, T* pb) {
+  LmControl* ctl = s.ctl;
+  if (ctl->terminated || ctl->pcg_done || ctl->status) return;
+  if (!(ctl->pcg_bnorm2 > 0.0)) {
+    if (threadIdx.x == 0 && blockIdx.x == 0) { ctl->pcg_done = 1; ctl->pcg_iters = 0; }
+    return;
+  }
+  double beta = 0.0;
+  if (it > 0) {
+    const double tol = s.prm.linear_tolerance;
+    if (ctl->pcg_rr[(it - 1) % 3] <= tol * tol * ctl->pcg_bnorm2) {
+      if (threadIdx.x == 0 && blockIdx.x == 0) { ctl->pcg_done = 1; ctl->pcg_iters = it; }
+      return;
+    }
+    const double rzprev = (it == 1) ? ctl->pcg_rz0 : ctl->pcg_rz[(it + 1) % 3];
+    beta = ctl->pcg_rz[(it - 1) % 3] / rzprev;
+  }
+  const T tb = T(beta);
+  const T* z = s.L.z;
+  const int64_t k = (blockIdx.x * (int64_t)blockDim.x + threadIdx.x) >> 5;
+  const int lane = threadIdx.x & 31;
+  const int w = threadIdx.x >> 5;
+  __shared__ T red[4][32];
+  __shared__ T vk[4][16];
+  if (k >= s.P.nkf) return;  // whole warps: no block-wide synchronisation below
+  if (lane < 15) {
+    const T v = z[15 * k + lane] + tb * pa[15 * k + lane];
+    pb[15 * k + lane] = v;
+    vk[w][lane] = v;
+  }
+  __syncwarp();
+  T acc = T(0);
+  const int sub = lane / 6, r = lane - 6 * (lane / 6);
+  if (sub < 5) {
+    const int64_t e1 = s.S.up_off[k + 1];
+    for (int64_t e = s.S.up_off[k] + sub; e < e1; e += 5) {
+      const int64_t j = s.S.up_col[e];
+      const T* B = s.L.SP + 36 * (int64_t)s.S.up_blk[e];
+      const T* zj = z + 15 * j;
+      const T* pj = pa + 15 * j;
+      T t = T(0);
+#pragma unroll
+      for (int c = 0; c < 6; ++c) {
+        acc += B[6 * r + c] * (zj[c] + tb * pj[c]);
+        t += B[6 * c + r] * vk[w][c];
+      }
+      atomic_add(&s.L.q[15 * j + r], t);
+    }
+  }
+  red[w][lane] = acc;
+  __syncwarp();
+  if (lane < 15) {
+    const T* D = s.L.SD + 225 * k + 15 * lane;
+    T y = T(0);
+#pragma unroll
+    for (int c = 0; c < 15; ++c) y += D[c] * vk[w][c];
+    if (lane < 6) y += red[w][lane] + red[w][lane + 6] + red[w][lane + 12] + red[w][lane + 18] + red[w][lane + 24];
+    for (int64_t e = s.S.kfe_off[k]; e < s.S.kfe_off[k + 1]; ++e) {
+      const int code = s.S.kfe[e];
+      const bool from = code > 0;
+      const int64_t ed = from ? code - 1 : -code - 1;
+      const T* E = s.L.SE + 225 * ed;
+      const int64_t o = from ? s.P.e_to[ed] : s.P.e_from[ed];
+      const T* zo = z + 15 * o;
+      const T* po = pa + 15 * o;
+      if (from) {
+#pragma unroll
+        for (int c = 0; c < 15; ++c) y += E[15 * lane + c] * (zo[c] + tb * po[c]);
+      } else {
+#pragma unroll
+        for (int c = 0; c < 15; ++c) y += E[15 * c + lane] * (zo[c] + tb * po[c]);
+      }
+    }
+    atomic_add(&s.L.q[15 * k + lane], y);
+  }
+}
+
+// p.q of the read-once product.
+template <typename T>
+__global__ void __launch_bounds__(kB) k_pcg_pq(SolverLaunch<T> s, int it, const T* p) {
+  LmControl* ctl = s.ctl;
+  if (ctl->terminated || ctl->pcg_done || ctl->status) return;
+  const int64_t i = blockIdx.x * (int64_t)blockDim.x + threadIdx.x;
+  double pq = 0.0;
+  if (i < 15 * s.P.nkf) pq = (double)p[i] * (double)s.L.q[i];
+  block_add(pq, &ctl->pcg_pq[it % 3]);
+}
+
 // x += alpha p ; r -= alpha q ; z = M r ; rr, rz dots.  16 threads per keyframe.
 template <typename T>
 __global__ void __launch_bounds__(kB) k_pcg_update(SolverLaunch<T> s, int it, const T* p, int last) {
@@ -879,6 +974,7 @@ __global__ void __launch_bounds__(kB) k_pcg_update(SolverLaunch<T> s, int it, co
     s.L.x[i] = s.L.x[i] + alpha * p[i];
     rnew = s.L.r[i] - alpha * s.L.q[i];
     s.L.r[i] = rnew;
+    if (s.S.spmv_sym) s.L.q[i] = T(0);  // the next read-once product accumulates into q
   }
   rsh[threadIdx.x] = rnew;
   __syncthreads();
@@ -1362,6 +1458,20 @@ cudaError_t solver_schur_pairs(const SolverLaunch<T>& s, cudaStream_t st) {
   return launch_schur_pairs<T>(s, st);
 }
 
+// One PCG product (after the PCG start) on the current reduced system, for
+// timing the two product kernels.
+template <typename T>
+cudaError_t solver_product(const SolverLaunch<T>& s, bool sym, cudaStream_t st) {
+  k_pcg_init<T><<<nblk(15 * (s.P.nkf + s.P.ng), kB), kB, 0, st>>>(s);
+  if (sym) {
+    k_pcg_spmv_sym<T><<<nblk(32 * s.P.nkf, 128), 128, 0, st>>>(s, 0, s.L.p, s.L.q2);
+    k_pcg_pq<T><<<nblk(15 * s.P.nkf, kB), kB, 0, st>>>(s, 0, s.L.q2);
+  } else {
+    k_pcg_spmv<T><<<nblk(32 * s.P.nkf, 128), 128, 0, st>>>(s, 0, s.L.p, s.L.q2);
+  }
+  return cudaGetLastError();
+}
+
 template <typename T>
 cudaError_t solver_step(const SolverLaunch<T>& s, cudaStream_t st) {
   cudaError_t e = solver_build_reduced<T>(s, st);
@@ -1378,7 +1488,12 @@ cudaError_t solver_step(const SolverLaunch<T>& s, cudaStream_t st) {
   for (int it = 0; it < maxit; ++it) {
     T* pa = (it & 1) ? s.L.q2 : s.L.p;
     T* pb = (it & 1) ? s.L.p : s.L.q2;
-    k_pcg_spmv<T><<<nblk(32 * s.P.nkf, 128), 128, 0, st>>>(s, it, pa, pb);
+    if (s.S.spmv_sym && s.P.ng == 0) {
+      k_pcg_spmv_sym<T><<<nblk(32 * s.P.nkf, 128), 128, 0, st>>>(s, it, pa, pb);
+      k_pcg_pq<T><<<nblk(15 * s.P.nkf, kB), kB, 0, st>>>(s, it, pb);
+    } else {
+      k_pcg_spmv<T><<<nblk(32 * s.P.nkf, 128), 128, 0, st>>>(s, it, pa, pb);
+    }
     if constexpr (sizeof(T) == 8)
       if (s.P.ng > 0) {
         e = border_spmv(s, it, pa, pb, st);
@@ -1555,6 +1670,8 @@ template cudaError_t solver_prepare<float>(const SchurPattern&);
 template cudaError_t solver_schur_pairs<double>(const SolverLaunch<double>&, cudaStream_t);
 template cudaError_t solver_schur_pairs<float>(const SolverLaunch<float>&, cudaStream_t);
 template cudaError_t solver_step<double>(const SolverLaunch<double>&, cudaStream_t);
+template cudaError_t solver_product<double>(const SolverLaunch<double>&, bool, cudaStream_t);
+template cudaError_t solver_product<float>(const SolverLaunch<float>&, bool, cudaStream_t);
 template cudaError_t solver_step<float>(const SolverLaunch<float>&, cudaStream_t);
 template cudaError_t solver_evaluate_candidate<double>(const SolverLaunch<double>&, InertialLin<double>, cudaStream_t);
 template cudaError_t solver_evaluate_candidate<float>(const SolverLaunch<float>&, InertialLin<double>, cudaStream_t);

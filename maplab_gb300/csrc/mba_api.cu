@@ -1210,6 +1210,18 @@ mba_status mba_create(const mba_problem_desc* d, int32_t device, mba_handle** ou
       row_col[fill[j]] = i; row_blk[fill[j]++] = (int32_t)(npu + b);
     }
   }
+  // Upper blocks by their row i (i < j), for the product that reads each block once.
+  std::vector<int64_t> up_off(NK + 1, 0);
+  for (int64_t b = 0; b < npu; ++b) up_off[pm.bi[b] + 1]++;
+  for (int64_t k = 0; k < NK; ++k) up_off[k + 1] += up_off[k];
+  std::vector<int32_t> up_col(npu), up_blk(npu);
+  {
+    std::vector<int64_t> fill(up_off.begin(), up_off.end() - 1);
+    for (int64_t b = 0; b < npu; ++b) {
+      up_col[fill[pm.bi[b]]] = pm.bj[b];
+      up_blk[fill[pm.bi[b]]++] = (int32_t)b;
+    }
+  }
   std::vector<int64_t> kfe_off(NK + 1, 0);
   // Per-keyframe edge lists (couplings; an absolute term couples nothing).
   for (int64_t e = 0; e < NE; ++e)
@@ -1469,6 +1481,9 @@ mba_status mba_create(const mba_problem_desc* d, int32_t device, mba_handle** ou
   S.row_off = A.upload(row_off, st);
   S.row_col = A.upload(row_col, st);
   S.row_blk = A.upload(row_blk, st);
+  S.up_off = A.upload(up_off, st);
+  S.up_col = A.upload(up_col, st);
+  S.up_blk = A.upload(up_blk, st);
   S.kfe_off = A.upload(kfe_off, st);
   S.kfe = A.upload(kfe, st);
   h->gg.nbr_off = A.upload(nbr_off, st);
@@ -1489,6 +1504,7 @@ mba_status mba_create(const mba_problem_desc* d, int32_t device, mba_handle** ou
   h->tuning.chain_tail_nodes = 128;
   h->tuning.chain_segment = 1;
   h->tuning.chain_tail_smem = 2;
+  h->tuning.pcg_product = 2;
   // Inertial scratch (kernels_inertial.cu): dt per step, end state per edge,
   // 4 RK4 stages x 15 values per step, FP32 Q_acc | Phi_acc per edge.
   P.ine_scratch = A.alloc<double>((NSMP - NIMU) + 16 * NIMU + 60 * (NSMP - NIMU) + 225 * NIMU + 1);
@@ -2375,6 +2391,15 @@ mba_status autotune(mba_handle* h, mba_tuning* out) {
   h->S.chain_tail = chain_tail_level(h->P.nkf, levels, best.chain_tail_nodes);
   h->S.chain_seg = chain_segment_level(best.chain_segment);
   h->S.chain_tail_sm = best.chain_tail_smem == 1;
+  // PCG product: pose blocks read once (atomics) or from both rows
+  tbest = 1e30;
+  for (int prod : {2, 1}) {
+    h->S.spmv_sym = prod == 1;
+    SolverLaunch<T> sc = make_launch<T>(h, b, o);
+    const double t = time_ms(st, 2, 10, [&]() { solver_product<T>(sc, prod == 1, st); });
+    if (t < tbest) { tbest = t; best.pcg_product = prod; }
+  }
+  h->S.spmv_sym = best.pcg_product == 1;
   if (cudaStreamSynchronize(st) != cudaSuccess || cudaGetLastError() != cudaSuccess) return MBA_ERR_CUDA;
   h->tuning = best;
   if (out) *out = best;
@@ -2400,6 +2425,7 @@ mba_status mba_set_tuning(mba_handle* h, const mba_tuning* t) {
   if (t->chain_segment && (t->chain_segment > 128 || (t->chain_segment & (t->chain_segment - 1))))
     return MBA_ERR_INVALID_ARG;
   if (t->chain_tail_smem < 0 || t->chain_tail_smem > 2) return MBA_ERR_INVALID_ARG;
+  if (t->pcg_product < 0 || t->pcg_product > 2) return MBA_ERR_INVALID_ARG;
   cudaSetDevice(h->device);
   if (t->visual_block) { h->P.vis_block = t->visual_block; h->tuning.visual_block = t->visual_block; }
   if (t->visual_min_blocks) {
@@ -2427,6 +2453,10 @@ mba_status mba_set_tuning(mba_handle* h, const mba_tuning* t) {
   if (t->chain_tail_smem) {
     h->S.chain_tail_sm = t->chain_tail_smem == 1;
     h->tuning.chain_tail_smem = t->chain_tail_smem;
+  }
+  if (t->pcg_product) {
+    h->S.spmv_sym = t->pcg_product == 1;
+    h->tuning.pcg_product = t->pcg_product;
   }
   return MBA_OK;
 }

@@ -43,6 +43,9 @@ struct SchurPattern {
   int64_t* row_off;       // [nkf+1] full (both orientations) pose-pose rows
   int32_t* row_col;       // [2 npu]
   int32_t* row_blk;       // [2 npu] block index into SP (upper b -> b, lower -> npu + b)
+  int64_t* up_off;        // [nkf+1] upper pose-pose blocks (i < j) by row i
+  int32_t* up_col;        // [npu] j
+  int32_t* up_blk;        // [npu] block index into SP
   int64_t* kfe_off;       // [nkf+1] incident inertial edges
   int32_t* kfe;           // +(e+1): keyframe is 'from' ; -(e+1): keyframe is 'to'
   // Keyframe chains laid end to end (chain preconditioner): position -> kf,
@@ -57,6 +60,7 @@ struct SchurPattern {
   int32_t chain_seg = 0;     // segmented sweeps: log2 of the positions one block sweeps through the
                              // levels below it (0: one launch per level)
   int32_t chain_tail_sm = 0;  // 1: one-block tail with the survivors' vectors in shared memory
+  int32_t spmv_sym = 0;       // 1: PCG product reads each stored pose block once (transposed part by atomics)
 };
 
 // Device control block of the LM loop (all scalars live on the device).
@@ -225,6 +229,8 @@ template <typename T>
 cudaError_t solver_prepare(const SchurPattern& S);
 template <typename T>
 cudaError_t chain_prepare();
+template <typename T>
+cudaError_t solver_product(const SolverLaunch<T>& s, bool sym, cudaStream_t st);
 // The Schur pair kernel alone (autotuning).
 template <typename T>
 cudaError_t solver_schur_pairs(const SolverLaunch<T>& s, cudaStream_t st);

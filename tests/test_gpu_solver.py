@@ -156,6 +156,34 @@ def test_chain_preconditioner_matches_oracle_dense(c1_oracle_run):
     assert sc["linear_iterations"] < 0.5 * sb["linear_iterations"], (sc["linear_iterations"], sb["linear_iterations"])
 
 
+@pytest.mark.parametrize("product", [1, 2])
+def test_pcg_product_variants_match_oracle_dense(c1_oracle_run, product):
+    """Both PCG products (each stored pose block read once with the transposed
+    part added by atomics, or read from both of its rows) give the oracle's
+    exact-Schur LM trajectory when PCG is run to 1e-10."""
+    m, so, _ = c1_oracle_run
+    with ba.BundleAdjuster(m.desc) as g:
+        g.set_tuning(pcg_product=product)
+        sg = g.solve(_gpu_opts(10, max_linear_iterations=6000, preconditioner=N.MBA_PRECOND_CHAIN))
+    assert abs(sg["final_cost"] - so["final_cost"]) <= 1e-6 * so["final_cost"], (sg["final_cost"], so["final_cost"])
+    for a, b in zip(sg["iterations"], so["iterations"]):
+        assert abs(a["cost"] - b["cost"]) <= 1e-6 * b["cost"], (a, b)
+
+
+def test_pcg_product_variants_agree_mixed():
+    """Mixed precision on a 3-mission map with shared landmarks: the two
+    products give the same capped-PCG solve to rounding."""
+    m = synth.generate("c4", num_missions=3, keyframes_per_mission=100, num_landmarks=5000,
+                       shared_landmark_fraction=0.2)
+    out = []
+    for product in (1, 2):
+        with ba.BundleAdjuster(m.desc) as g:
+            g.set_tuning(pcg_product=product)
+            out.append(g.solve(_gpu_opts(6, max_linear_iterations=25, linear_tolerance=1e-6,
+                                         precision=N.MBA_PRECISION_MIXED, preconditioner=N.MBA_PRECOND_CHAIN)))
+    assert abs(out[0]["final_cost"] - out[1]["final_cost"]) <= 1e-5 * out[1]["final_cost"], (out[0], out[1])
+
+
 def test_chain_preconditioner_mixed_reaches_fp64_cost():
     m = synth.generate("c1")
     with ba.BundleAdjuster(m.desc) as g:
