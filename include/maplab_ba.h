@@ -461,6 +461,9 @@ typedef struct mba_tuning {
                                  * 2: in global memory (0 in mba_set_tuning keeps the current setting) */
   int32_t pcg_product;          /* PCG product: 1 reads each stored pose block once (transposed part by
                                  * atomics), 2 reads it from both of its rows (0 keeps the setting) */
+  int32_t schur_split;          /* Schur pair kernel: 1 two threads per chunk (half the output columns
+                                 * each), 2 one thread per chunk (0 keeps the setting) */
+  int32_t pad_;
 } mba_tuning;
 mba_status mba_autotune(mba_handle* h, int32_t precision, mba_tuning* out);
 /* Applies tuning values (e.g. cached from an earlier mba_autotune of a

@@ -249,6 +249,8 @@ class Tuning(ctypes.Structure):
         ("chain_segment", ctypes.c_int32),
         ("chain_tail_smem", ctypes.c_int32),
         ("pcg_product", ctypes.c_int32),
+        ("schur_split", ctypes.c_int32),
+        ("pad_", ctypes.c_int32),
     ]
 
 

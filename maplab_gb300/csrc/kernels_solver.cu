@@ -610,11 +610,131 @@ __global__ void __launch_bounds__(kB, sizeof(T) == 4 ? 2 : 1) k_schur_pairs(Solv
   }
 }
 
+// Transposed part of a diagonal target's pair product for the thread that
+// owns columns 3H..3H+2: element (q, r) of m^T, q = 3H + qq, goes to this
+// thread's acc when column r is its own, else to accT for the partner.
+template <int H, typename T>
+__device__ __forceinline__ void schur_sym_half(const T (&m)[6][3], T (&acc)[18], T (&accT)[9]) {
+#pragma unroll
+  for (int r = 0; r < 6; ++r)
+#pragma unroll
+    for (int qq = 0; qq < 3; ++qq) {
+      if (r / 3 == H) acc[3 * (3 * H + qq) + (r - 3 * H)] += m[r][qq];
+      else accT[3 * qq + (r - 3 * (1 - H))] += m[r][qq];
+    }
+}
+// The partner's transposed terms: in[3 qq + rr] is element (3 (1 - H) + qq, 3 H + rr).
+template <int H, typename T>
+__device__ __forceinline__ void schur_sym_merge(const T (&in)[9], T (&acc)[18]) {
+#pragma unroll
+  for (int qq = 0; qq < 3; ++qq)
+#pragma unroll
+    for (int rr = 0; rr < 3; ++rr) acc[3 * (3 * (1 - H) + qq) + rr] += in[3 * qq + rr];
+}
+
+// k_schur_pairs with two threads per chunk: thread h of a pair owns the
+// output columns 3h..3h+2 (18 accumulators instead of 36) and loads only those
+// columns of U_b, so a block keeps twice the partner rows in flight at fewer
+// registers per thread.  The transposed terms of a diagonal target that land
+// in the partner's columns are exchanged once per chunk.
+template <typename T>
+__global__ void __launch_bounds__(kB, sizeof(T) == 4 ? 3 : 1) k_schur_pairs_split(SolverLaunch<T> s, int64_t stage_cap) {
+  if (s.ctl->terminated) return;
+  extern __shared__ __align__(16) unsigned char schur_smem[];
+  T* sW = reinterpret_cast<T*>(schur_smem);
+  const int64_t i = blockIdx.x;
+  const int64_t c0 = s.S.row_chunk_off[i], c1 = s.S.row_chunk_off[i + 1];
+  if (c0 == c1) return;
+  const int64_t s0 = s.S.kf_slot_off[i], ns = s.S.kf_slot_off[i + 1] - s0;
+  const bool staged = ns <= stage_cap;
+  if (staged)
+    for (int64_t q = threadIdx.x; q < 18 * ns; q += blockDim.x)
+      sW[kSlotStride * (q / 18) + q % 18] = s.L.Wslot[kSlotStride * (int64_t)s.S.kf_slot[s0 + q / 18] + q % 18];
+  __syncthreads();
+  const int h = threadIdx.x & 1;
+  const unsigned pair_mask = 3u << ((threadIdx.x & 31) & ~1);
+  for (int64_t c = c0 + (threadIdx.x >> 1); c < c1; c += blockDim.x >> 1) {
+    const int32_t raw = s.S.chunk_tgt[c];
+    const bool whole = raw >= 0;
+    const int64_t tid = whole ? raw : ~raw;
+    const bool diag = tid < s.P.nkf;
+    T acc[18], accT[9];
+#pragma unroll
+    for (int q = 0; q < 18; ++q) acc[q] = T(0);
+#pragma unroll
+    for (int q = 0; q < 9; ++q) accT[q] = T(0);
+    const int64_t p0 = s.S.chunk_beg[c], p1 = p0 + s.S.chunk_len[c];
+    int2 ab = s.S.pair_rb[p0];
+    T Ub[9];  // U_b rows 0..2, columns 3h..3h+2
+    {
+      const T* u = s.L.U + kSlotStride * (int64_t)ab.y + 3 * h;
+#pragma unroll
+      for (int k = 0; k < 3; ++k)
+#pragma unroll
+        for (int qq = 0; qq < 3; ++qq) Ub[3 * k + qq] = u[6 * k + qq];
+    }
+    for (int64_t p = p0; p < p1; ++p) {
+      const bool sym = diag && s.S.kf_slot[s0 + ab.x] != ab.y;
+      const T* wa = staged ? sW + kSlotStride * (int64_t)ab.x : s.L.Wslot + kSlotStride * (int64_t)s.S.kf_slot[s0 + ab.x];
+      T Un[9];
+      int2 abn = ab;
+      if (p + 1 < p1) {
+        abn = s.S.pair_rb[p + 1];
+        const T* u = s.L.U + kSlotStride * (int64_t)abn.y + 3 * h;
+#pragma unroll
+        for (int k = 0; k < 3; ++k)
+#pragma unroll
+          for (int qq = 0; qq < 3; ++qq) Un[3 * k + qq] = u[6 * k + qq];
+      }
+      T m[6][3];
+#pragma unroll
+      for (int r = 0; r < 6; ++r) {
+        const T w0 = wa[r], w1 = wa[6 + r], w2 = wa[12 + r];
+#pragma unroll
+        for (int qq = 0; qq < 3; ++qq) {
+          m[r][qq] = w0 * Ub[qq] + w1 * Ub[3 + qq] + w2 * Ub[6 + qq];
+          acc[3 * r + qq] += m[r][qq];
+        }
+      }
+      if (sym) {
+        if (h) schur_sym_half<1>(m, acc, accT);
+        else schur_sym_half<0>(m, acc, accT);
+      }
+      if (p + 1 < p1) {
+#pragma unroll
+        for (int k = 0; k < 9; ++k) Ub[k] = Un[k];
+        ab = abn;
+      }
+    }
+    if (diag) {
+      T in[9];
+#pragma unroll
+      for (int q = 0; q < 9; ++q) in[q] = __shfl_xor_sync(pair_mask, accT[q], 1);
+      if (h) schur_sym_merge<1>(in, acc);
+      else schur_sym_merge<0>(in, acc);
+    }
+    T* dst = diag ? s.L.SD + 225 * tid : s.L.SP + 36 * (tid - s.P.nkf);
+    const int ld = diag ? 15 : 6;
+    if (whole) {
+#pragma unroll
+      for (int r = 0; r < 6; ++r)
+#pragma unroll
+        for (int qq = 0; qq < 3; ++qq) dst[ld * r + 3 * h + qq] -= acc[3 * r + qq];
+    } else {
+#pragma unroll
+      for (int r = 0; r < 6; ++r)
+#pragma unroll
+        for (int qq = 0; qq < 3; ++qq) atomic_add(&dst[ld * r + 3 * h + qq], -acc[3 * r + qq]);
+    }
+  }
+}
+
 // Shared-memory bytes of k_schur_pairs (a row's staged W slots) and the slot
 // count that fits; longer rows read W from global memory.
 template <typename T>
-int64_t schur_pairs_smem(const SchurPattern& S, int64_t* cap) {
-  const int64_t limit = sizeof(T) == 4 ? 96 * 1024 : 200 * 1024;  // FP32: two blocks per SM
+int64_t schur_pairs_smem(const SchurPattern& S, bool split, int64_t* cap) {
+  // FP32: two blocks per SM (three for the split kernel, whose rows fit in 72 KB)
+  const int64_t limit = sizeof(T) == 4 ? (split ? 72 : 96) * 1024 : 200 * 1024;
   const int64_t fit = limit / (kSlotStride * (int64_t)sizeof(T));
   *cap = S.max_row_slots < fit ? S.max_row_slots : fit;
   return *cap * kSlotStride * (int64_t)sizeof(T);
@@ -625,8 +745,11 @@ template <typename T>
 cudaError_t launch_schur_pairs(const SolverLaunch<T>& s, cudaStream_t st) {
   if (s.S.nchunk == 0) return cudaSuccess;
   int64_t cap = 0;
-  const int64_t bytes = schur_pairs_smem<T>(s.S, &cap);
-  k_schur_pairs<T><<<(unsigned)s.P.nkf, kB, (size_t)bytes, st>>>(s, cap);
+  const int64_t bytes = schur_pairs_smem<T>(s.S, s.S.schur_split != 0, &cap);
+  if (s.S.schur_split)
+    k_schur_pairs_split<T><<<(unsigned)s.P.nkf, kB, (size_t)bytes, st>>>(s, cap);
+  else
+    k_schur_pairs<T><<<(unsigned)s.P.nkf, kB, (size_t)bytes, st>>>(s, cap);
   return cudaGetLastError();
 }
 
@@ -1447,10 +1570,14 @@ cudaError_t solver_build_reduced(const SolverLaunch<T>& s, cudaStream_t st) {
 template <typename T>
 cudaError_t solver_prepare(const SchurPattern& S) {
   int64_t cap = 0;
-  const int64_t bytes = schur_pairs_smem<T>(S, &cap);
-  const cudaError_t e = chain_prepare<T>();
+  const int64_t bytes = schur_pairs_smem<T>(S, false, &cap);  // the larger of the two kernels' sizes
+  cudaError_t e = chain_prepare<T>();
   if (e != cudaSuccess || bytes <= 48 * 1024) return e;
-  return cudaFuncSetAttribute(k_schur_pairs<T>, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)bytes);
+  // both Schur pair kernels, at the larger of their shared-memory sizes
+  e = cudaFuncSetAttribute(k_schur_pairs<T>, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)bytes);
+  if (e == cudaSuccess)
+    e = cudaFuncSetAttribute(k_schur_pairs_split<T>, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)bytes);
+  return e;
 }
 
 template <typename T>

@@ -1505,6 +1505,7 @@ mba_status mba_create(const mba_problem_desc* d, int32_t device, mba_handle** ou
   h->tuning.chain_segment = 1;
   h->tuning.chain_tail_smem = 2;
   h->tuning.pcg_product = 2;
+  h->tuning.schur_split = 2;
   // Inertial scratch (kernels_inertial.cu): dt per step, end state per edge,
   // 4 RK4 stages x 15 values per step, FP32 Q_acc | Phi_acc per edge.
   P.ine_scratch = A.alloc<double>((NSMP - NIMU) + 16 * NIMU + 60 * (NSMP - NIMU) + 225 * NIMU + 1);
@@ -2357,10 +2358,14 @@ mba_status autotune(mba_handle* h, mba_tuning* out) {
   tbest = 1e30;
   for (int chunk : {16, 32, 64}) {
     if (chunk != h->tuning.schur_chunk && (ms = apply_schur_chunk(h, chunk)) != MBA_OK) return ms;
-    SolverLaunch<T> sc = make_launch<T>(h, b, o);
-    const double t = time_ms(st, 1, 2, [&]() { solver_schur_pairs<T>(sc, st); });
-    if (t < tbest) { tbest = t; best.schur_chunk = chunk; best.schur_ms = t; }
+    for (int split : {2, 1}) {  // one or two threads per chunk
+      h->S.schur_split = split == 1;
+      SolverLaunch<T> sc = make_launch<T>(h, b, o);
+      const double t = time_ms(st, 1, 2, [&]() { solver_schur_pairs<T>(sc, st); });
+      if (t < tbest) { tbest = t; best.schur_chunk = chunk; best.schur_split = split; best.schur_ms = t; }
+    }
   }
+  h->S.schur_split = best.schur_split == 1;
   if (best.schur_chunk != h->tuning.schur_chunk && (ms = apply_schur_chunk(h, best.schur_chunk)) != MBA_OK) return ms;
   // single-block tail of the chain sweeps (the factorization from the build is reused)
   tbest = 1e30;
@@ -2426,6 +2431,7 @@ mba_status mba_set_tuning(mba_handle* h, const mba_tuning* t) {
     return MBA_ERR_INVALID_ARG;
   if (t->chain_tail_smem < 0 || t->chain_tail_smem > 2) return MBA_ERR_INVALID_ARG;
   if (t->pcg_product < 0 || t->pcg_product > 2) return MBA_ERR_INVALID_ARG;
+  if (t->schur_split < 0 || t->schur_split > 2) return MBA_ERR_INVALID_ARG;
   cudaSetDevice(h->device);
   if (t->visual_block) { h->P.vis_block = t->visual_block; h->tuning.visual_block = t->visual_block; }
   if (t->visual_min_blocks) {
@@ -2457,6 +2463,10 @@ mba_status mba_set_tuning(mba_handle* h, const mba_tuning* t) {
   if (t->pcg_product) {
     h->S.spmv_sym = t->pcg_product == 1;
     h->tuning.pcg_product = t->pcg_product;
+  }
+  if (t->schur_split) {
+    h->S.schur_split = t->schur_split == 1;
+    h->tuning.schur_split = t->schur_split;
   }
   return MBA_OK;
 }

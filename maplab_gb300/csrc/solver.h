@@ -61,6 +61,7 @@ struct SchurPattern {
                              // levels below it (0: one launch per level)
   int32_t chain_tail_sm = 0;  // 1: one-block tail with the survivors' vectors in shared memory
   int32_t spmv_sym = 0;       // 1: PCG product reads each stored pose block once (transposed part by atomics)
+  int32_t schur_split = 0;    // 1: Schur pair kernel with two threads per chunk
 };
 
 // Device control block of the LM loop (all scalars live on the device).

@@ -92,6 +92,7 @@ def test_autotune_keeps_results():
         assert tun["chain_segment"] in (1, 16, 32, 64, 128)
         assert tun["chain_tail_smem"] in (1, 2)
         assert tun["pcg_product"] in (1, 2)
+        assert tun["schur_split"] in (1, 2)
         assert tun["visual_ms"] > 0 and tun["schur_ms"] > 0 and tun["chain_apply_ms"] > 0
         tuned = g.solve(_opts())
     assert abs(tuned["final_cost"] - base["final_cost"]) <= 1e-6 * base["final_cost"]

@@ -33,16 +33,34 @@ def _dense(sysd, nk):
     return A
 
 
-@pytest.fixture(scope="module")
-def c1_systems():
+@pytest.fixture(scope="module", params=[2, 1], ids=["one_thread_per_chunk", "two_threads_per_chunk"])
+def c1_systems(request):
+    """The system built by either Schur pair kernel (schur_split 2 / 1)."""
     m = synth.generate("c1")
     o = O.OracleProblem(m.desc)
     radius = 1e4
     Ao, bo = o.reduced_system(N.default_solver_options(), radius)
     with ba.BundleAdjuster(m.desc) as g:
+        g.set_tuning(schur_split=request.param)
         s64 = g.reduced_system(N.MBA_PRECISION_FP64, radius)
         s32 = g.reduced_system(N.MBA_PRECISION_MIXED, radius)
     return m.desc.num_keyframes, Ao, bo, s64, s32
+
+
+@pytest.mark.parametrize("chunk", [4, 64])
+def test_split_schur_kernel_matches_single(chunk):
+    """Two-mission map with shared landmarks (off-diagonal and multi-chunk
+    targets with atomics, diagonal targets with transposed terms): both Schur
+    pair kernels give the same FP64 system to 1e-12."""
+    m = synth.generate("c4", num_missions=2, keyframes_per_mission=60, num_landmarks=3000,
+                       shared_landmark_fraction=0.3)
+    out = []
+    for split in (2, 1):
+        with ba.BundleAdjuster(m.desc) as g:
+            g.set_tuning(schur_split=split, schur_chunk=chunk)
+            out.append(_dense(g.reduced_system(N.MBA_PRECISION_FP64, 1e4), m.desc.num_keyframes))
+    rel = np.linalg.norm(out[0] - out[1]) / np.linalg.norm(out[1])
+    assert rel <= 1e-12, rel
 
 
 def test_reduced_system_fp64_matches_oracle(c1_systems):
