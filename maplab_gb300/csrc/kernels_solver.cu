@@ -478,8 +478,7 @@ __device__ __forceinline__ bool inv3t(const T* A, T* B) {
   return true;
 }
 
-// Landmark elimination, part 1: V = (H + D)^-1, rhs += W^T V g and U = V W
-// for every slot of the landmark (scaled blocks; U = 0 for inactive ones).
+// Landmark elimination, part 1: V = (H + D)^-1 and rhs += W^T V g (scaled blocks).
 template <typename T>
 __global__ void __launch_bounds__(kB) k_schur_lm(SolverLaunch<T> s) {
   if (s.ctl->terminated) return;
@@ -487,9 +486,7 @@ __global__ void __launch_bounds__(kB) k_schur_lm(SolverLaunch<T> s) {
   const int64_t NL = s.P.nlm, NS = s.S.nslot;
   if (l >= NL) return;
   T V[9] = {T(0), T(0), T(0), T(0), T(0), T(0), T(0), T(0), T(0)};
-  T Vg[3] = {T(0), T(0), T(0)};
-  const bool active = s.P.lm_active[l];
-  if (active) {
+  if (s.P.lm_active[l]) {
     const T radius = T(s.ctl->radius), mn = T(s.prm.min_lm_diagonal), mx = T(s.prm.max_lm_diagonal);
     // The 3x3 inverse runs in FP64 in both paths: poorly constrained landmarks
     // (short baselines) make these blocks ill-conditioned.
@@ -505,25 +502,17 @@ __global__ void __launch_bounds__(kB) k_schur_lm(SolverLaunch<T> s) {
     }
 #pragma unroll
     for (int a = 0; a < 9; ++a) V[a] = T(Vd[a]);
-    T g[3];
+    T g[3], Vg[3];
 #pragma unroll
     for (int a = 0; a < 3; ++a) g[a] = s.L.gl[a * NL + l];
 #pragma unroll
     for (int a = 0; a < 3; ++a) Vg[a] = V[3 * a] * g[0] + V[3 * a + 1] * g[1] + V[3 * a + 2] * g[2];
-  }
-  for (int64_t si = s.S.lm_slot_off[l]; si < s.S.lm_slot_off[l + 1]; ++si) {
-    T W[18];
-    load_slot(s.L.Wslot + kSlotStride * si, W);
-    T* U = s.L.U + kSlotStride * si;
-#pragma unroll
-    for (int x = 0; x < 3; ++x)
-#pragma unroll
-      for (int c = 0; c < 6; ++c) U[6 * x + c] = V[3 * x] * W[c] + V[3 * x + 1] * W[6 + c] + V[3 * x + 2] * W[12 + c];
-    if (active) {
+    for (int64_t si = s.S.lm_slot_off[l]; si < s.S.lm_slot_off[l + 1]; ++si) {
       const int64_t k = s.S.slot_kf[si];
 #pragma unroll
       for (int c = 0; c < 6; ++c) {
-        const T acc = W[c] * Vg[0] + W[6 + c] * Vg[1] + W[12 + c] * Vg[2];
+        const T* w = s.L.Wslot + kSlotStride * si;
+        const T acc = w[c] * Vg[0] + w[6 + c] * Vg[1] + w[12 + c] * Vg[2];
         if (acc != T(0)) atomic_add(&s.L.rhs[15 * k + c], acc);
       }
     }
@@ -532,7 +521,26 @@ __global__ void __launch_bounds__(kB) k_schur_lm(SolverLaunch<T> s) {
   for (int a = 0; a < 9; ++a) s.L.V[a * NL + l] = V[a];
 }
 
-// Landmark elimination, part 2: S(k_a, k_b) -= W_a^T U_b for every slot pair.
+// Landmark elimination, part 2: U = V W per slot.
+template <typename T>
+__global__ void __launch_bounds__(kB) k_schur_slot(SolverLaunch<T> s) {
+  if (s.ctl->terminated) return;
+  const int64_t i = blockIdx.x * (int64_t)blockDim.x + threadIdx.x;
+  const int64_t NS = s.S.nslot, NL = s.P.nlm;
+  if (i >= NS) return;
+  const int64_t l = s.S.slot_lm[i];
+  T W[18], V[9];
+  load_slot(s.L.Wslot + kSlotStride * i, W);
+#pragma unroll
+  for (int a = 0; a < 9; ++a) V[a] = s.L.V[a * NL + l];
+#pragma unroll
+  for (int x = 0; x < 3; ++x)
+#pragma unroll
+    for (int c = 0; c < 6; ++c)
+      s.L.U[kSlotStride * i + 6 * x + c] = V[3 * x] * W[c] + V[3 * x + 1] * W[6 + c] + V[3 * x + 2] * W[12 + c];
+}
+
+// Landmark elimination, part 3: S(k_a, k_b) -= W_a^T U_b for every slot pair.
 // Pairs are sorted by target block; one thread sums a chunk of one target's
 // pairs in registers and writes the block once (plain read-modify-write when
 // it owns the whole target, atomics otherwise).  Diagonal targets take
@@ -1545,6 +1553,7 @@ cudaError_t solver_build_reduced(const SolverLaunch<T>& s, cudaStream_t st) {
       if (e != cudaSuccess) return e;
     }
   if (s.P.nlm) k_schur_lm<T><<<nblk(s.P.nlm, kB), kB, 0, st>>>(s);
+  if (s.S.nslot) k_schur_slot<T><<<nblk(s.S.nslot, kB), kB, 0, st>>>(s);
   if (s.S.nchunk) {
     const cudaError_t e = launch_schur_pairs<T>(s, st);
     if (e != cudaSuccess) return e;
