@@ -67,6 +67,19 @@ __device__ __forceinline__ void load_slot(const float* p, float* v) {
   v[16] = t.x;
   v[17] = t.y;
 }
+// Vector stores of one slot row (18 values of a 20-value row).
+__device__ __forceinline__ void store_slot(float* p, const float* v) {
+  float4* q = reinterpret_cast<float4*>(p);
+#pragma unroll
+  for (int i = 0; i < 4; ++i) q[i] = make_float4(v[4 * i], v[4 * i + 1], v[4 * i + 2], v[4 * i + 3]);
+  reinterpret_cast<float2*>(p)[8] = make_float2(v[16], v[17]);
+}
+__device__ __forceinline__ void store_slot(double* p, const double* v) {
+  double2* q = reinterpret_cast<double2*>(p);
+#pragma unroll
+  for (int i = 0; i < 9; ++i) q[i] = make_double2(v[2 * i], v[2 * i + 1]);
+}
+
 __device__ __forceinline__ void load_slot(const double* p, double* v) {
   const double2* q = reinterpret_cast<const double2*>(p);  // 160-byte rows: 16-byte aligned
 #pragma unroll
@@ -149,13 +162,15 @@ __global__ void __launch_bounds__(kB, sizeof(T) == 4 ? 2 : 1) k_assemble_lm(DevP
       Js[a] = v.Js[a * N + i] * ss[a % 6];
       Jo[a] = v.Jo[a * N + i] * (scaled ? L.skf[15 * (int64_t)ob + a % 6] : T(1));
     }
+    T Wo[18];
 #pragma unroll
     for (int x = 0; x < 3; ++x)
 #pragma unroll
       for (int c = 0; c < 6; ++c) {
         Wst[6 * x + c] += Jl[x] * Js[c] + Jl[3 + x] * Js[6 + c];
-        L.Wslot[kSlotStride * (int64_t)slot + 6 * x + c] = Jl[x] * Jo[c] + Jl[3 + x] * Jo[6 + c];
+        Wo[6 * x + c] = Jl[x] * Jo[c] + Jl[3 + x] * Jo[6 + c];
       }
+    store_slot(L.Wslot + kSlotStride * (int64_t)slot, Wo);
 #pragma unroll
     for (int a = 0; a < 6; ++a) {
       gst[a] += Js[a] * r[0] + Js[6 + a] * r[1];
@@ -215,8 +230,7 @@ __global__ void __launch_bounds__(kB, sizeof(T) == 4 ? 2 : 1) k_assemble_lm(DevP
   for (int a = 0; a < 9; ++a) L.Hll[a * NL + l] = H[a];
 #pragma unroll
   for (int a = 0; a < 3; ++a) L.gl[a * NL + l] = g[a];
-#pragma unroll
-  for (int a = 0; a < 18; ++a) L.Wslot[kSlotStride * s0 + a] = Wst[a];
+  store_slot(L.Wslot + kSlotStride * s0, Wst);
   if (any_cam) {
     if constexpr (sizeof(T) == 4) {
       float4* D4 = reinterpret_cast<float4*>(L.Dpose + kPoseUp * (int64_t)st);
@@ -376,12 +390,34 @@ __global__ void k_scale(DevProblem P, LinearSystem<T> L, ScaleVectors sc, int ja
 
 // Applies the Jacobi scaling in place to the assembled normal equations:
 // H_ll, g_l, W slots, D, P, E blocks and g_c (J s instead of J).
+// W_slot (x, c) *= slm[x] of its landmark * skf[c] of its keyframe; one
+// thread per slot row.
+template <typename T>
+__global__ void __launch_bounds__(kB) k_scale_slots(DevProblem P, SchurPattern S, LinearSystem<T> L,
+                                                    const int* run_if, const int* skip_if) {
+  if (gated(run_if, skip_if)) return;
+  const int64_t sl = blockIdx.x * (int64_t)blockDim.x + threadIdx.x;
+  if (sl >= S.nslot) return;
+  const int64_t NL = P.nlm, l = S.slot_lm[sl], k = S.slot_kf[sl];
+  T w[18], a[3], b[6];
+  load_slot(L.Wslot + kSlotStride * sl, w);
+#pragma unroll
+  for (int x = 0; x < 3; ++x) a[x] = L.slm[x * NL + l];
+#pragma unroll
+  for (int c = 0; c < 6; ++c) b[c] = L.skf[15 * k + c];
+#pragma unroll
+  for (int x = 0; x < 3; ++x)
+#pragma unroll
+    for (int c = 0; c < 6; ++c) w[6 * x + c] *= a[x] * b[c];
+  store_slot(L.Wslot + kSlotStride * sl, w);
+}
+
 template <typename T>
 __global__ void __launch_bounds__(kB) k_scale_inplace(DevProblem P, SchurPattern S, LinearSystem<T> L,
                                                       const int* run_if, const int* skip_if) {
   if (gated(run_if, skip_if)) return;
   const int64_t NL = P.nlm, NS = S.nslot, NK = P.nkf, NE = P.nedge, NPU = S.npu;
-  const int64_t n1 = 9 * NL, n2 = n1 + 3 * NL, n3 = n2 + 18 * NS, n4 = n3 + 225 * NK, n5 = n4 + 36 * NPU,
+  const int64_t n1 = 9 * NL, n2 = n1 + 3 * NL, n3 = n2 /* W slots: k_scale_slots */, n4 = n3 + 225 * NK, n5 = n4 + 36 * NPU,
                 n6 = n5 + 225 * NE, n7 = n6 + 15 * NK, n8 = n7 + 2 * P.nsw, n9 = n8 + 30 * P.nsw;
   for (int64_t i = blockIdx.x * (int64_t)blockDim.x + threadIdx.x; i < n9; i += (int64_t)gridDim.x * blockDim.x) {
     if (i < n1) {
@@ -391,9 +427,6 @@ __global__ void __launch_bounds__(kB) k_scale_inplace(DevProblem P, SchurPattern
       const int64_t j = i - n1, l = j % NL;
       L.gl[j] *= L.slm[j];
       (void)l;
-    } else if (i < n3) {
-      const int64_t j = i - n2, q = j % 18, sl = j / 18;
-      L.Wslot[kSlotStride * sl + q] *= L.slm[(q / 6) * NL + S.slot_lm[sl]] * L.skf[15 * (int64_t)S.slot_kf[sl] + q % 6];
     } else if (i < n4) {
       const int64_t j = i - n3, k = j / 225, e = j % 225;
       L.Dbase[j] *= L.skf[15 * k + e / 15] * L.skf[15 * k + e % 15];
@@ -533,11 +566,12 @@ __global__ void __launch_bounds__(kB) k_schur_slot(SolverLaunch<T> s) {
   load_slot(s.L.Wslot + kSlotStride * i, W);
 #pragma unroll
   for (int a = 0; a < 9; ++a) V[a] = s.L.V[a * NL + l];
+  T U[18];
 #pragma unroll
   for (int x = 0; x < 3; ++x)
 #pragma unroll
-    for (int c = 0; c < 6; ++c)
-      s.L.U[kSlotStride * i + 6 * x + c] = V[3 * x] * W[c] + V[3 * x + 1] * W[6 + c] + V[3 * x + 2] * W[12 + c];
+    for (int c = 0; c < 6; ++c) U[6 * x + c] = V[3 * x] * W[c] + V[3 * x + 1] * W[6 + c] + V[3 * x + 2] * W[12 + c];
+  store_slot(s.L.U + kSlotStride * i, U);
 }
 
 // Landmark elimination, part 3: S(k_a, k_b) -= W_a^T U_b for every slot pair.
@@ -1145,14 +1179,15 @@ __global__ void __launch_bounds__(kB) k_backsub(SolverLaunch<T> s) {
     for (int a = 0; a < 3; ++a) t[a] -= T(s.B.bl[a * NL + l]);
   for (int64_t i = s.S.lm_slot_off[l]; i < s.S.lm_slot_off[l + 1]; ++i) {
     const T* xk = s.L.x + 15 * (int64_t)s.S.slot_kf[i];
-    T xv[6];
+    T xv[6], w[18];
 #pragma unroll
     for (int c = 0; c < 6; ++c) xv[c] = xk[c];
+    load_slot(s.L.Wslot + kSlotStride * i, w);
 #pragma unroll
     for (int x = 0; x < 3; ++x) {
       T acc = T(0);
 #pragma unroll
-      for (int c = 0; c < 6; ++c) acc += s.L.Wslot[kSlotStride * i + 6 * x + c] * xv[c];
+      for (int c = 0; c < 6; ++c) acc += w[6 * x + c] * xv[c];
       t[x] -= acc;
     }
   }
@@ -1482,8 +1517,9 @@ template <typename T>
 cudaError_t solver_compute_scale(const SolverLaunch<T>& s, int jacobi, cudaStream_t st) {
   const int64_t n = 15 * s.P.nkf + 3 * s.P.nlm + s.P.nsw;
   k_scale<T><<<nblk(n, kB), kB, 0, st>>>(s.P, s.L, s.sc, jacobi, nullptr);
-  const int64_t m = 12 * s.P.nlm + 18 * s.S.nslot + 240 * s.P.nkf + 36 * s.S.npu + 225 * s.P.nedge + 32 * s.P.nsw;
+  const int64_t m = 12 * s.P.nlm + 240 * s.P.nkf + 36 * s.S.npu + 225 * s.P.nedge + 32 * s.P.nsw;
   k_scale_inplace<T><<<gridcap(m), kB, 0, st>>>(s.P, s.S, s.L, nullptr, nullptr);
+  if (s.S.nslot) k_scale_slots<T><<<nblk(s.S.nslot, kB), kB, 0, st>>>(s.P, s.S, s.L, nullptr, nullptr);
   if constexpr (sizeof(T) == 8)
     if (s.P.ng > 0) {
       const cudaError_t e = border_scale(s, jacobi, nullptr, st);
@@ -1758,8 +1794,9 @@ cudaError_t solver_reject_and_restart(const SolverLaunch<T>& s, int use_reprojec
   k_mirror_pose_blocks<T><<<nblk(15 * s.P.nkf, kB), kB, 0, st>>>(s.P.nkf, s.L.Dbase, run, nullptr);
   const int64_t n = 15 * s.P.nkf + 3 * s.P.nlm + s.P.nsw;
   k_scale<T><<<nblk(n, kB), kB, 0, st>>>(s.P, s.L, s.sc, jacobi, run);
-  const int64_t m = 12 * s.P.nlm + 18 * s.S.nslot + 240 * s.P.nkf + 36 * s.S.npu + 225 * s.P.nedge + 32 * s.P.nsw;
+  const int64_t m = 12 * s.P.nlm + 240 * s.P.nkf + 36 * s.S.npu + 225 * s.P.nedge + 32 * s.P.nsw;
   k_scale_inplace<T><<<gridcap(m), kB, 0, st>>>(s.P, s.S, s.L, run, nullptr);
+  if (s.S.nslot) k_scale_slots<T><<<nblk(s.S.nslot, kB), kB, 0, st>>>(s.P, s.S, s.L, run, nullptr);
   if constexpr (sizeof(T) == 8)
     if (s.P.ng > 0) {
       e = border_assemble(s, run, nullptr, st);
