@@ -542,9 +542,10 @@ __global__ void __launch_bounds__(kB) k_schur_lm(SolverLaunch<T> s) {
     for (int a = 0; a < 3; ++a) Vg[a] = V[3 * a] * g[0] + V[3 * a + 1] * g[1] + V[3 * a + 2] * g[2];
     for (int64_t si = s.S.lm_slot_off[l]; si < s.S.lm_slot_off[l + 1]; ++si) {
       const int64_t k = s.S.slot_kf[si];
+      T w[18];
+      load_slot(s.L.Wslot + kSlotStride * si, w);
 #pragma unroll
       for (int c = 0; c < 6; ++c) {
-        const T* w = s.L.Wslot + kSlotStride * si;
         const T acc = w[c] * Vg[0] + w[6 + c] * Vg[1] + w[12 + c] * Vg[2];
         if (acc != T(0)) atomic_add(&s.L.rhs[15 * k + c], acc);
       }
