@@ -455,7 +455,7 @@ typedef struct mba_tuning {
   int32_t visual_pipelined;     /* 1: software-pipelined persistent evaluation kernel, 2: one thread per
                                  * observation (0 in mba_set_tuning keeps the current setting) */
   int32_t chain_segment;        /* chain sweeps: positions one block takes through the lower levels (a power
-                                 * of two from 2 to 128; three launches per apply), or 1: one launch per
+                                 * of two from 2 to 256; three launches per apply), or 1: one launch per
                                  * level (0 in mba_set_tuning keeps the current setting) */
   int32_t chain_tail_smem;      /* 1: the one-block tail keeps the survivors' vectors in shared memory,
                                  * 2: in global memory (0 in mba_set_tuning keeps the current setting) */

@@ -638,7 +638,12 @@ cudaError_t chain_apply(const SolverLaunch<T>& s, const T* r, T* z, double* rz, 
 // Shared-memory opt-in of the tail kernel (outside graph capture).
 template <typename T>
 cudaError_t chain_prepare() {
-  return cudaFuncSetAttribute(k_chain_tail_sm<T>, cudaFuncAttributeMaxDynamicSharedMemorySize, kTailSmem);
+  cudaError_t e = cudaFuncSetAttribute(k_chain_tail_sm<T>, cudaFuncAttributeMaxDynamicSharedMemorySize, kTailSmem);
+  // segments of up to 256 positions: 2 x 256 x 16 values (+ one position) in the back sweep
+  const int seg_bytes = (int)(sizeof(T) * 16 * (2 * 256 + 1));
+  if (e == cudaSuccess) e = cudaFuncSetAttribute(k_chain_seg_fwd<T>, cudaFuncAttributeMaxDynamicSharedMemorySize, seg_bytes);
+  if (e == cudaSuccess) e = cudaFuncSetAttribute(k_chain_seg_bwd<T>, cudaFuncAttributeMaxDynamicSharedMemorySize, seg_bytes);
+  return e;
 }
 
 template cudaError_t chain_prepare<double>();

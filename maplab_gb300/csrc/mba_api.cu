@@ -2266,7 +2266,7 @@ int chain_tail_level(int64_t n, int levels, int64_t nodes) {
   return l;
 }
 
-// Segment of the chain sweeps (positions per block, a power of two up to 128)
+// Segment of the chain sweeps (positions per block, a power of two up to 256)
 // -> its level; 1 -> 0 (one launch per level).
 int chain_segment_level(int seg) {
   int m = 0;
@@ -2385,7 +2385,7 @@ mba_status autotune(mba_handle* h, mba_tuning* out) {
     }
   }
   // segmented sweeps: positions per block; the tail's vectors in shared or global memory
-  for (int seg : {16, 32, 64, 128})
+  for (int seg : {16, 32, 64, 128, 256})
     for (int tsm : {1, 2}) {
       h->S.chain_seg = chain_segment_level(seg);
       h->S.chain_tail_sm = tsm == 1;
@@ -2427,7 +2427,7 @@ mba_status mba_set_tuning(mba_handle* h, const mba_tuning* t) {
   if (!h || !t) return MBA_ERR_INVALID_ARG;
   if (t->visual_block && (t->visual_block < 32 || t->visual_block > 256 || t->visual_block % 32)) return MBA_ERR_INVALID_ARG;
   if (t->schur_chunk < 0 || t->chain_tail_nodes < 0) return MBA_ERR_INVALID_ARG;
-  if (t->chain_segment && (t->chain_segment > 128 || (t->chain_segment & (t->chain_segment - 1))))
+  if (t->chain_segment && (t->chain_segment > 256 || (t->chain_segment & (t->chain_segment - 1))))
     return MBA_ERR_INVALID_ARG;
   if (t->chain_tail_smem < 0 || t->chain_tail_smem > 2) return MBA_ERR_INVALID_ARG;
   if (t->pcg_product < 0 || t->pcg_product > 2) return MBA_ERR_INVALID_ARG;

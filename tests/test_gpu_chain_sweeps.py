@@ -18,7 +18,7 @@ from maplab_gb300 import ba, synth
 
 pytestmark = pytest.mark.gpu
 
-SEGMENTS = (1, 16, 32, 64, 128)
+SEGMENTS = (1, 16, 32, 64, 128, 256)
 
 
 def _dense_chain(g, precision, radius):
@@ -78,6 +78,6 @@ def test_sweeps_match_dense_solve(chain_map, precision, tol):
 
 def test_segment_setting_is_validated(chain_map):
     with ba.BundleAdjuster(chain_map.desc) as g:
-        for bad in (3, 256, -4):
+        for bad in (3, 512, -4):
             with pytest.raises(ba.BAError):
                 g.set_tuning(chain_segment=bad)

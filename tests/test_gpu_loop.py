@@ -89,7 +89,7 @@ def test_autotune_keeps_results():
         assert tun["visual_pipelined"] in (1, 2)
         assert tun["schur_chunk"] in (4, 8, 16, 32, 64)
         assert tun["chain_tail_nodes"] in (32, 64, 128, 256, 512)
-        assert tun["chain_segment"] in (1, 16, 32, 64, 128)
+        assert tun["chain_segment"] in (1, 16, 32, 64, 128, 256)
         assert tun["chain_tail_smem"] in (1, 2)
         assert tun["pcg_product"] in (1, 2)
         assert tun["schur_split"] in (1, 2)
