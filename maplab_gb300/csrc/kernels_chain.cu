@@ -168,7 +168,9 @@ __global__ void __launch_bounds__(32 * kCW) k_chain_init(SolverLaunch<T> s) {
   const T* D = s.L.SD + 225 * k;
   for (int idx = lane; idx < 225; idx += 32) A[idx] = (double)D[idx];
   // Diagonal compensation: alpha * sum of |S| over the off-chain pose blocks of row k.
-  {
+  // Only the learned coefficients use it (alpha = 0 and no gradient for the
+  // fixed chain), so the fixed chain skips the pass over the row's blocks.
+  if (s.precond == MBA_PRECOND_LEARNED) {
     const bool ll = p > 0 && (s.S.link_edge[p] >= 0 || s.S.link_blk[p] >= 0);
     const bool lr = p + 1 < n && (s.S.link_edge[p + 1] >= 0 || s.S.link_blk[p + 1] >= 0);
     const int64_t kl = ll ? s.S.chain_perm[p - 1] : -1, kr = lr ? s.S.chain_perm[p + 1] : -1;
