@@ -178,15 +178,15 @@ __device__ __forceinline__ void distort(int dtype, const T* k, T* pt, T* J) {
     const T poly = k1 * th2 + k2 * th4 + k3 * th6 + k4 * th8 + T(1);
     const T thetad = th * poly;
     const T r2p1 = r2 + T(1);
-    const T ir = T(1) / r;
-    const T p15 = r2 * r;  // (x2+y2)^(3/2)
     // The reference's generated expression divides each of its eight terms by
-    // r^2 + 1; the common factor is divided once here (same value up to
-    // rounding, four divisions per observation instead of twelve).
-    const T q = (T(4) * k2 * th3 + T(6) * k3 * th5 + T(8) * k4 * th7 + T(2) * k1 * th) * ir / r2p1;
+    // r^2 + 1 and further terms by r^2 (r^2 + 1) and r^3; here 1 / r and
+    // 1 / (r^2 + 1) are formed once and multiplied in (same values up to
+    // rounding, two divisions per observation instead of twelve).
+    const T ir = T(1) / r, ir2p1 = T(1) / r2p1;
+    const T q = (T(4) * k2 * th3 + T(6) * k3 * th5 + T(8) * k4 * th7 + T(2) * k1 * th) * ir * ir2p1;
     const T sx = x * q, sy = y * q;
-    const T a = (poly) / (r2 * r2p1);
-    const T b = th / p15 * poly;
+    const T a = poly * (ir * ir) * ir2p1;     // poly / (r^2 (r^2 + 1))
+    const T b = th * (ir * ir * ir) * poly;   // th / r^3 * poly
     J[0] = th * ir * poly + x * th * ir * sx + x2 * a - x2 * b;
     J[1] = x * th * ir * sy + x * y * a - x * y * b;
     J[2] = y * th * ir * sx + x * y * a - x * y * b;
