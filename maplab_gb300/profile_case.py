@@ -32,6 +32,9 @@ def main():
     ap.add_argument("--device-loop", type=int, default=1)
     ap.add_argument("--reject-every", type=int, default=0)
     ap.add_argument("--reproj", type=int, default=0)
+    ap.add_argument("--schur-split", type=int, default=0, help="1: two threads per Schur chunk, 2: one")
+    ap.add_argument("--pcg-product", type=int, default=0, help="1: read-once product, 2: both rows")
+    ap.add_argument("--chain-segment", type=int, default=0, help="segmented sweeps (positions per block) or 1")
     ap.add_argument("--profile-range", action="store_true",
                     help="cuProfilerStart / cuProfilerStop around the solve only")
     a = ap.parse_args()
@@ -39,6 +42,8 @@ def main():
     with ba.BundleAdjuster(m.desc) as g:
         if a.block or a.min_blocks:
             g.set_tuning(visual_block=a.block, visual_min_blocks=a.min_blocks)
+        if a.schur_split or a.pcg_product or a.chain_segment:
+            g.set_tuning(schur_split=a.schur_split, pcg_product=a.pcg_product, chain_segment=a.chain_segment)
         prec = N.MBA_PRECISION_MIXED if a.precision == "mixed" else N.MBA_PRECISION_FP64
         if a.autotune:
             print(json.dumps({"tuning": g.autotune(prec)}))
