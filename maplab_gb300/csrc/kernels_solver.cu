@@ -611,15 +611,15 @@ __global__ void __launch_bounds__(kB, sizeof(T) == 4 ? 2 : 1) k_schur_pairs(Solv
     for (int q = 0; q < 36; ++q) acc[q] = T(0);
     const int64_t p0 = s.S.chunk_beg[c], p1 = p0 + s.S.chunk_len[c];
     int2 ab = s.S.pair_rb[p0];
+    int2 abn = p0 + 1 < p1 ? s.S.pair_rb[p0 + 1] : ab;  // pair indices run one step ahead of the rows
     T Wa[18], Ub[18];
     load_slot(wrow(ab.x), Wa);
     load_slot(s.L.U + kSlotStride * (int64_t)ab.y, Ub);
     for (int64_t p = p0; p < p1; ++p) {
       const bool sym = diag && s.S.kf_slot[s0 + ab.x] != ab.y;
       T Wn[18], Un[18];
-      int2 abn = ab;
+      const int2 abnn = p + 2 < p1 ? s.S.pair_rb[p + 2] : abn;
       if (p + 1 < p1) {
-        abn = s.S.pair_rb[p + 1];
         load_slot(wrow(abn.x), Wn);
         load_slot(s.L.U + kSlotStride * (int64_t)abn.y, Un);
       }
@@ -635,6 +635,7 @@ __global__ void __launch_bounds__(kB, sizeof(T) == 4 ? 2 : 1) k_schur_pairs(Solv
 #pragma unroll
         for (int k = 0; k < 18; ++k) { Wa[k] = Wn[k]; Ub[k] = Un[k]; }
         ab = abn;
+        abn = abnn;
       }
     }
     T* dst = diag ? s.L.SD + 225 * tid : s.L.SP + 36 * (tid - s.P.nkf);
@@ -708,6 +709,7 @@ __global__ void __launch_bounds__(kB, sizeof(T) == 4 ? 3 : 1) k_schur_pairs_spli
     for (int q = 0; q < 9; ++q) accT[q] = T(0);
     const int64_t p0 = s.S.chunk_beg[c], p1 = p0 + s.S.chunk_len[c];
     int2 ab = s.S.pair_rb[p0];
+    int2 abn = p0 + 1 < p1 ? s.S.pair_rb[p0 + 1] : ab;  // pair indices run one step ahead of the rows
     T Ub[9];  // U_b rows 0..2, columns 3h..3h+2
     {
       const T* u = s.L.U + kSlotStride * (int64_t)ab.y + 3 * h;
@@ -720,9 +722,8 @@ __global__ void __launch_bounds__(kB, sizeof(T) == 4 ? 3 : 1) k_schur_pairs_spli
       const bool sym = diag && s.S.kf_slot[s0 + ab.x] != ab.y;
       const T* wa = staged ? sW + kSlotStride * (int64_t)ab.x : s.L.Wslot + kSlotStride * (int64_t)s.S.kf_slot[s0 + ab.x];
       T Un[9];
-      int2 abn = ab;
+      const int2 abnn = p + 2 < p1 ? s.S.pair_rb[p + 2] : abn;
       if (p + 1 < p1) {
-        abn = s.S.pair_rb[p + 1];
         const T* u = s.L.U + kSlotStride * (int64_t)abn.y + 3 * h;
 #pragma unroll
         for (int k = 0; k < 3; ++k)
@@ -747,6 +748,7 @@ __global__ void __launch_bounds__(kB, sizeof(T) == 4 ? 3 : 1) k_schur_pairs_spli
 #pragma unroll
         for (int k = 0; k < 9; ++k) Ub[k] = Un[k];
         ab = abn;
+        abn = abnn;
       }
     }
     if (diag) {
