@@ -123,10 +123,6 @@ struct InertialLin {
 cudaError_t launch_visual_ambient(const DevProblem& P, double* res, double* const* jac_dev, cudaStream_t s);
 template <typename T>
 cudaError_t launch_visual_linearize(const DevProblem& P, VisualLin<T> out, double* cost_accum, cudaStream_t s);
-// FP64 linearization into row-major arrays in caller order (inv: caller index ->
-// internal observation); any array may be null.
-cudaError_t launch_visual_linearize_rows(const DevProblem& P, const int64_t* inv, double* r, double* Jl, double* Js,
-                                         double* Jo, cudaStream_t s);
 cudaError_t launch_visual_cost(const DevProblem& P, const double* kf_state, const double* lm_p, double* cost_accum,
                                int* nonfinite, cudaStream_t s);
 // Inertial: full evaluation at `kf_state`; writes tangent linearization (if

@@ -102,20 +102,6 @@ __device__ __forceinline__ void rot_basis(const DevProblem& P, const S* mis, int
 // observation: load_obs_stream (the observation's own streamed fields,
 // coalesced) and load_obs_gather (landmark and keyframe poses addressed by
 // them).  compute_obs holds the arithmetic and the stores.
-// n (even) values to dst[off..off+n) in 16-byte stores; dst may be null.
-template <typename T>
-__device__ __forceinline__ void store_row(T* dst, int64_t off, const T* v, int n) {
-  if (!dst) return;
-  if constexpr (sizeof(T) == 8) {
-    double2* q = reinterpret_cast<double2*>(dst + off);
-#pragma unroll
-    for (int a = 0; a < 6; ++a)
-      if (2 * a < n) q[a] = make_double2(v[2 * a], v[2 * a + 1]);
-  } else {
-    for (int a = 0; a < n; ++a) dst[off + a] = v[a];
-  }
-}
-
 template <typename T>
 struct ObsInputs {
   typename Vec2<T>::type uv;
@@ -157,10 +143,8 @@ __device__ __forceinline__ void load_obs_gather(const DevProblem& P, const Visua
 // rci: the camera's R_C_I (9 values, e.g. from the block's shared memory) or
 // null; FP64 inputs carry the keyframes' rotation matrices and |q|^2
 // (in.kf_rot, written by k_kf_rotations) so that the kernel does not rebuild
-// them per observation.  kRows: the outputs are row-major arrays in the
-// caller's observation order (row i = the `i` argument, any array may be
-// null) instead of the solver's component-major layout.
-template <typename T, bool kCost, bool kRows = false>
+// them per observation.
+template <typename T, bool kCost>
 __device__ __forceinline__ double compute_obs(const DevProblem& P, const VisualInputs<T>& in, const ObsInputs<T>& o,
                                               const VisualLin<T>& out, int64_t i, int64_t N, const T* rci) {
   double cost = 0.0;
@@ -346,21 +330,14 @@ __device__ __forceinline__ double compute_obs(const DevProblem& P, const VisualI
   } else if (kCost) {
     cost = 0.5 * double(s);
   }
-  if constexpr (kRows) {
-    store_row(out.r, 2 * i, r, 2);
-    store_row(out.Jl, 6 * i, Jl, 6);
-    store_row(out.Js, 12 * i, Js, 12);
-    store_row(out.Jo, 12 * i, Jo, 12);
-  } else {
-    out.r[i] = r[0];
-    out.r[N + i] = r[1];
+  out.r[i] = r[0];
+  out.r[N + i] = r[1];
 #pragma unroll
-    for (int a = 0; a < 6; ++a) out.Jl[a * N + i] = Jl[a];
+  for (int a = 0; a < 6; ++a) out.Jl[a * N + i] = Jl[a];
 #pragma unroll
-    for (int a = 0; a < 12; ++a) out.Js[a * N + i] = Js[a];
+  for (int a = 0; a < 12; ++a) out.Js[a * N + i] = Js[a];
 #pragma unroll
-    for (int a = 0; a < 12; ++a) out.Jo[a * N + i] = Jo[a];
-  }
+  for (int a = 0; a < 12; ++a) out.Jo[a * N + i] = Jo[a];
   return cost;
 }
 
@@ -398,24 +375,6 @@ __global__ void __launch_bounds__(kBlock, kMinBlocks) k_visual_linearize(DevProb
     cost = compute_obs<T, kCost>(P, in, o, out, i, P.nobs, cam_sm ? rci + 9 * o.cam : nullptr);
   }
   if (kCost) block_accumulate(cost, cost_accum);
-}
-
-// The FP64 linearization written straight into the caller's row-major arrays
-// in caller order (thread j evaluates the caller's observation j, internal
-// index inv[j]), so that the stores to page-locked host memory overlap the
-// arithmetic instead of following it in a separate gather pass.
-__global__ void __launch_bounds__(kBlock) k_visual_linearize_rows(DevProblem P, VisualInputs<double> in,
-                                                                  VisualLin<double> out, const int64_t* inv) {
-  __shared__ double rci[9 * kCamRot];
-  const bool cam_sm = stage_camera_rotations(P, in, rci);
-  const int64_t j = blockIdx.x * (int64_t)blockDim.x + threadIdx.x;
-  if (j < P.nobs) {
-    ObsInputs<double> o;
-    const int64_t i = inv[j];
-    load_obs_stream(P, in, i, o);
-    load_obs_gather(P, in, o);
-    compute_obs<double, false, true>(P, in, o, out, j, P.nobs, cam_sm ? rci + 9 * o.cam : nullptr);
-  }
 }
 
 // Persistent, software-pipelined: a grid of resident blocks strides over the
@@ -1090,19 +1049,6 @@ template cudaError_t launch_gather_visual<double>(const DevProblem&, const int64
                                                   double*, double*, double*, cudaStream_t);
 template cudaError_t launch_gather_visual<float>(const DevProblem&, const int64_t*, VisualLin<float>, double*, double*,
                                                  double*, double*, cudaStream_t);
-
-cudaError_t launch_visual_linearize_rows(const DevProblem& P, const int64_t* inv, double* r, double* Jl, double* Js,
-                                         double* Jo, cudaStream_t s) {
-  if (P.nobs == 0) return cudaSuccess;
-  k_kf_rotations<<<(unsigned)((P.nkf + 127) / 128), 128, 0, s>>>(P.kf_state, P.nkf, P.kf_rot, nullptr, nullptr);
-  VisualLin<double> out{};
-  out.r = r;
-  out.Jl = Jl;
-  out.Js = Js;
-  out.Jo = Jo;
-  k_visual_linearize_rows<<<(unsigned)((P.nobs + 127) / 128), 128, 0, s>>>(P, visual_inputs<double>(P), out, inv);
-  return cudaGetLastError();
-}
 
 namespace {
 __global__ void k_invert_perm(int64_t N, const int64_t* perm, int64_t* inv) {

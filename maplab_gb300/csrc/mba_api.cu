@@ -814,13 +814,6 @@ mba_status linearize_visual_host(mba_handle* h, double* r, double* Jl, double* J
     mapped[a] = static_cast<double*>(mapped_host_range(out[a], sizeof(double) * width[a] * N));
     direct = direct && mapped[a];
   }
-  if (direct && sizeof(T) == 8) {
-    // FP64 into page-locked host memory: evaluation and stores in one kernel,
-    // in caller order (the device linearization buffers are not written).
-    cudaError_t e = launch_visual_linearize_rows(h->P, h->obs_inv, mapped[0], mapped[1], mapped[2], mapped[3], st);
-    if (e == cudaSuccess) e = cudaStreamSynchronize(st);
-    return cuda_status(e);
-  }
   cudaError_t e = launch_visual_linearize<T>(h->P, b.vis, nullptr, st);
   if (direct) {
     if (e == cudaSuccess) e = launch_gather_visual<T>(h->P, h->obs_inv, b.vis, mapped[0], mapped[1], mapped[2], mapped[3], st);

@@ -115,10 +115,9 @@ def test_mixed_precision_visual_linearization(c1):
 
 @pytest.mark.parametrize("precision", [N.MBA_PRECISION_FP64, N.MBA_PRECISION_MIXED])
 def test_linearize_visual_into_pinned_host_memory(multi, precision):
-    """Page-locked destinations are written directly: FP64 rows by the
-    evaluation kernel itself in caller order, FP32 ones by the gather kernel;
-    pageable ones go through the device staging buffer and copies.  All give
-    the same rows, bit for bit, also with some outputs omitted."""
+    """Page-locked destinations are written by the gather kernel directly;
+    pageable ones through the device staging buffer and copies.  Both give the
+    same rows, bit for bit, also with some outputs omitted."""
     import ctypes
     import torch
     n = multi.desc.num_observations
