@@ -206,12 +206,29 @@ __global__ void __launch_bounds__(32 * kCW) k_chain_init(SolverLaunch<T> s) {
   }
 }
 
-// Eliminates the positions of level l (or position 0 when top).
+// FP32 product of 15x15 blocks in shared memory, C = op(A) op(B) (C must not
+// alias A or B): the mixed path's factorization products.
+__device__ void w_gemm_f(const float* A, bool ta, const float* B, bool tb, float* C) {
+  const int lane = threadIdx.x & 31;
+  for (int idx = lane; idx < 225; idx += 32) {
+    const int r = idx / 15, c = idx - 15 * (idx / 15);
+    float v = 0.f;
+#pragma unroll
+    for (int q = 0; q < 15; ++q) v += (ta ? A[15 * q + r] : A[15 * r + q]) * (tb ? B[15 * c + q] : B[15 * q + c]);
+    C[idx] = v;
+  }
+  __syncwarp();
+}
+
+// Eliminates the positions of level l (or position 0 when top).  The pivot
+// block's Cholesky inverse is FP64 in both paths; the mixed path forms the
+// coupling products XL = CL^T F, XR = CR^T F in FP32 (the sweeps read them in
+// FP32) and keeps no FP64 copies of the factors.
 template <typename T>
 __global__ void __launch_bounds__(32 * kCW) k_chain_elim(SolverLaunch<T> s, int l, int top) {
   if (s.ctl->terminated) return;
   __shared__ double sm[kCW][5][225];
-  const int w = threadIdx.x >> 5;
+  const int w = threadIdx.x >> 5, lane = threadIdx.x & 31;
   const int64_t j = (blockIdx.x * (int64_t)blockDim.x + threadIdx.x) >> 5;
   const int64_t n = s.P.nkf, st = (int64_t)1 << l;
   const int64_t p = top ? (j == 0 ? 0 : n) : st + 2 * st * j;
@@ -219,22 +236,53 @@ __global__ void __launch_bounds__(32 * kCW) k_chain_elim(SolverLaunch<T> s, int 
   double *sA = sm[w][0], *sX = sm[w][1], *sF = sm[w][2], *sL = sm[w][3], *sR = sm[w][4];
   w_load(s.C.A + 225 * p, sA);
   const bool ok = w_spd_inverse(sA, sX, sF);
-  if (!ok && (threadIdx.x & 31) == 0) atomicExch(&s.ctl->chain_failed, 1);
-  w_store(sF, s.C.F64 + 225 * p, s.C.F + 225 * p);
-  if (top) return;
-  w_load(s.C.B + 225 * p, sL);  // T(p, p-s)
-  if (p + st < n) w_load(s.C.B + 225 * (p + st), sR, true);  // T(p, p+s) = T(p+s, p)^T
-  else w_zero(sR);
-  w_store(sL, s.C.CL64 + 225 * p, s.C.CL + 225 * p);
-  w_store(sR, s.C.CR64 + 225 * p, s.C.CR + 225 * p);
-  __syncwarp();
-  w_gemm(sL, true, sF, false, sA, 1.0, false);  // XL = CL^T F
-  w_store(sA, s.C.XL64 + 225 * p, s.C.XL + 225 * p);
-  w_gemm(sR, true, sF, false, sX, 1.0, false);  // XR = CR^T F
-  w_store(sX, s.C.XR64 + 225 * p, s.C.XR + 225 * p);
+  if (!ok && lane == 0) atomicExch(&s.ctl->chain_failed, 1);
+  if constexpr (sizeof(T) == 8) {
+    w_store(sF, s.C.F64 + 225 * p, s.C.F + 225 * p);
+    if (top) return;
+    w_load(s.C.B + 225 * p, sL);  // T(p, p-s)
+    if (p + st < n) w_load(s.C.B + 225 * (p + st), sR, true);  // T(p, p+s) = T(p+s, p)^T
+    else w_zero(sR);
+    w_store(sL, s.C.CL64 + 225 * p, s.C.CL + 225 * p);
+    w_store(sR, s.C.CR64 + 225 * p, s.C.CR + 225 * p);
+    __syncwarp();
+    w_gemm(sL, true, sF, false, sA, 1.0, false);  // XL = CL^T F
+    w_store(sA, s.C.XL64 + 225 * p, s.C.XL + 225 * p);
+    w_gemm(sR, true, sF, false, sX, 1.0, false);  // XR = CR^T F
+    w_store(sX, s.C.XR64 + 225 * p, s.C.XR + 225 * p);
+  } else {
+    // FP32 working copies in the (now free) A and X buffers: 3 x 225 floats fit in 2 x 225 doubles.
+    float* fF = reinterpret_cast<float*>(sA);
+    float* fL = fF + 225;
+    float* fR = reinterpret_cast<float*>(sX);
+    float* fP = fR + 225;
+    __syncwarp();
+    for (int idx = lane; idx < 225; idx += 32) {
+      fF[idx] = float(sF[idx]);
+      s.C.F[225 * p + idx] = fF[idx];
+    }
+    if (top) return;
+    const double* B1 = s.C.B + 225 * p;                                // T(p, p-s)
+    const double* B2 = p + st < n ? s.C.B + 225 * (p + st) : nullptr;  // T(p+s, p): CR = its transpose
+    for (int idx = lane; idx < 225; idx += 32) {
+      const int r = idx / 15, c = idx - 15 * (idx / 15);
+      fL[idx] = float(B1[idx]);
+      fR[idx] = B2 ? float(B2[15 * c + r]) : 0.f;
+      s.C.CL[225 * p + idx] = fL[idx];
+      s.C.CR[225 * p + idx] = fR[idx];
+    }
+    __syncwarp();
+    w_gemm_f(fL, true, fF, false, fP);  // XL = CL^T F
+    for (int idx = lane; idx < 225; idx += 32) s.C.XL[225 * p + idx] = fP[idx];
+    __syncwarp();
+    w_gemm_f(fR, true, fF, false, fP);  // XR = CR^T F
+    for (int idx = lane; idx < 225; idx += 32) s.C.XR[225 * p + idx] = fP[idx];
+  }
 }
 
-// Survivors of level l absorb their eliminated neighbours.
+// Survivors of level l absorb their eliminated neighbours (the mixed path
+// forms the products in FP32 from the FP32 factors and subtracts them from the
+// FP64 blocks).
 template <typename T>
 __global__ void __launch_bounds__(32 * kCW) k_chain_merge(SolverLaunch<T> s, int l) {
   if (s.ctl->terminated) return;
@@ -244,24 +292,54 @@ __global__ void __launch_bounds__(32 * kCW) k_chain_merge(SolverLaunch<T> s, int
   const int64_t n = s.P.nkf, st = (int64_t)1 << l;
   const int64_t q = 2 * st * j;
   if (q >= n) return;
+  const int lane = threadIdx.x & 31;
   double *sD = sm[w][0], *s1 = sm[w][1], *s2 = sm[w][2], *sB = sm[w][3];
   w_load(s.C.A + 225 * q, sD);
   w_zero(sB);
-  if (q >= st) {
-    const int64_t a = q - st;
-    w_load(s.C.XR64 + 225 * a, s1);
-    w_load(s.C.CR64 + 225 * a, s2);
-    w_gemm(s1, false, s2, false, sD, -1.0, true);
-    w_load(s.C.CL64 + 225 * a, s2);
-    w_gemm(s1, false, s2, false, sB, -1.0, false);
+  if constexpr (sizeof(T) == 8) {
+    if (q >= st) {
+      const int64_t a = q - st;
+      w_load(s.C.XR64 + 225 * a, s1);
+      w_load(s.C.CR64 + 225 * a, s2);
+      w_gemm(s1, false, s2, false, sD, -1.0, true);
+      w_load(s.C.CL64 + 225 * a, s2);
+      w_gemm(s1, false, s2, false, sB, -1.0, false);
+    }
+    if (q + st < n) {
+      const int64_t b = q + st;
+      w_load(s.C.XL64 + 225 * b, s1);
+      w_load(s.C.CL64 + 225 * b, s2);
+      w_gemm(s1, false, s2, false, sD, -1.0, true);
+    }
+  } else {
+    float* fX = reinterpret_cast<float*>(s1);
+    float* fC = fX + 225;
+    float* fP = reinterpret_cast<float*>(s2);
+    auto load_f = [&](const float* g, float* d) {
+      for (int idx = lane; idx < 225; idx += 32) d[idx] = g[idx];
+      __syncwarp();
+    };
+    if (q >= st) {
+      const int64_t a = q - st;
+      load_f(s.C.XR + 225 * a, fX);
+      load_f(s.C.CR + 225 * a, fC);
+      w_gemm_f(fX, false, fC, false, fP);
+      for (int idx = lane; idx < 225; idx += 32) sD[idx] -= double(fP[idx]);
+      __syncwarp();
+      load_f(s.C.CL + 225 * a, fC);
+      w_gemm_f(fX, false, fC, false, fP);
+      for (int idx = lane; idx < 225; idx += 32) sB[idx] = -double(fP[idx]);
+      __syncwarp();
+    }
+    if (q + st < n) {
+      const int64_t b = q + st;
+      load_f(s.C.XL + 225 * b, fX);
+      load_f(s.C.CL + 225 * b, fC);
+      w_gemm_f(fX, false, fC, false, fP);
+      for (int idx = lane; idx < 225; idx += 32) sD[idx] -= double(fP[idx]);
+      __syncwarp();
+    }
   }
-  if (q + st < n) {
-    const int64_t b = q + st;
-    w_load(s.C.XL64 + 225 * b, s1);
-    w_load(s.C.CL64 + 225 * b, s2);
-    w_gemm(s1, false, s2, false, sD, -1.0, true);
-  }
-  const int lane = threadIdx.x & 31;
   for (int idx = lane; idx < 225; idx += 32) {
     s.C.A[225 * q + idx] = sD[idx];
     s.C.B[225 * q + idx] = sB[idx];

@@ -336,14 +336,15 @@ mba_status ensure_chain_buffers(mba_handle* h, SolverBuffers<T>& b) {
   ChainSystem<T>& C = b.C;
   C.A = A.alloc<double>(225 * n);
   C.B = A.alloc<double>(225 * n);
-  C.F64 = A.alloc<double>(225 * n);
-  C.CL64 = A.alloc<double>(225 * n);
-  C.CR64 = A.alloc<double>(225 * n);
-  C.XL64 = A.alloc<double>(225 * n);
-  C.XR64 = A.alloc<double>(225 * n);
   if constexpr (sizeof(T) == 8) {
+    C.F64 = A.alloc<double>(225 * n);
+    C.CL64 = A.alloc<double>(225 * n);
+    C.CR64 = A.alloc<double>(225 * n);
+    C.XL64 = A.alloc<double>(225 * n);
+    C.XR64 = A.alloc<double>(225 * n);
     C.F = C.F64; C.CL = C.CL64; C.CR = C.CR64; C.XL = C.XL64; C.XR = C.XR64;
-  } else {
+  } else {  // the mixed path keeps the factors in FP32 only
+    C.F64 = C.CL64 = C.CR64 = C.XL64 = C.XR64 = nullptr;
     C.F = A.alloc<T>(225 * n);
     C.CL = A.alloc<T>(225 * n);
     C.CR = A.alloc<T>(225 * n);
