@@ -1069,9 +1069,13 @@ __global__ void __launch_bounds__(128) k_pcg_spmv_sym(SolverLaunch<T> s, int it,
   const int sub = lane / 6, r = lane - 6 * (lane / 6);
   if (sub < 5) {
     const int64_t e1 = s.S.up_off[k + 1];
-    for (int64_t e = s.S.up_off[k] + sub; e < e1; e += 5) {
-      const int64_t j = s.S.up_col[e];
-      const T* B = s.L.SP + 36 * (int64_t)s.S.up_blk[e];
+    int64_t e = s.S.up_off[k] + sub;
+    int64_t jn = 0, bn = 0;  // the next block's indices, loaded one step ahead
+    if (e < e1) { jn = s.S.up_col[e]; bn = s.S.up_blk[e]; }
+    for (; e < e1; e += 5) {
+      const int64_t j = jn;
+      const T* B = s.L.SP + 36 * bn;
+      if (e + 5 < e1) { jn = s.S.up_col[e + 5]; bn = s.S.up_blk[e + 5]; }
       const T* zj = z + 15 * j;
       const T* pj = pa + 15 * j;
       T t = T(0);
