@@ -972,9 +972,13 @@ __global__ void __launch_bounds__(128) k_pcg_spmv(SolverLaunch<T> s, int it, con
     const int64_t npu = s.S.npu;
     if (sub < 5) {
       const int64_t e1 = s.S.row_off[k + 1];
-      for (int64_t e = s.S.row_off[k] + sub; e < e1; e += 5) {
-        const int64_t j = s.S.row_col[e];
-        const int64_t blk = s.S.row_blk[e];
+      int64_t e = s.S.row_off[k] + sub;
+      int64_t jn = 0, bn = 0;  // the next block's indices, loaded one step ahead
+      if (e < e1) { jn = s.S.row_col[e]; bn = s.S.row_blk[e]; }
+      for (; e < e1; e += 5) {
+        const int64_t j = jn;
+        const int64_t blk = bn;
+        if (e + 5 < e1) { jn = s.S.row_col[e + 5]; bn = s.S.row_blk[e + 5]; }
         const bool lower = blk >= npu;
         const T* B = lower ? s.L.SP + 36 * (blk - npu) + r : s.L.SP + 36 * blk + 6 * r;
         const int step = lower ? 6 : 1;
