@@ -558,24 +558,21 @@ void launch_tail(const SolverLaunch<T>& s, int l0, int seg, const T* r, T* z, do
     k_chain_tail<T><<<1, kTailThreads, 0, st>>>(s, l0, seg, r, z, rz);
 }
 
-// Threads per segment block: 16 per position (thread r owns row r), enough for
-// the first level's survivors in one pass (8 x segment), at most 1024.
-constexpr int kSegThreadsMax = 1024;
-inline int seg_threads(int m) { return 8 << m < 128 ? 128 : (8 << m > kSegThreadsMax ? kSegThreadsMax : 8 << m); }
+constexpr int kSegThreads = 256;  // 16 positions at a time, thread r of a position owns row r
 
 // Segmented forward sweep: block j runs levels 0..m-1 on positions
 // [j 2^m, (j+1) 2^m) in shared memory (16 values per position), writes w and
 // the next segment's left-neighbour terms lc[j + 1].
 template <typename T>
-__global__ void __launch_bounds__(kSegThreadsMax) k_chain_seg_fwd(SolverLaunch<T> s, int m, const T* rv) {
+__global__ void __launch_bounds__(kSegThreads) k_chain_seg_fwd(SolverLaunch<T> s, int m, const T* rv) {
   if (apply_gate(s.ctl)) return;
   extern __shared__ __align__(16) unsigned char seg_smem[];
   T* ws = reinterpret_cast<T*>(seg_smem);  // [2^m][16]
   const int64_t n = s.P.nkf, base = (int64_t)blockIdx.x << m;
   const int64_t left = n - base;
   const int cnt = left < ((int64_t)1 << m) ? (int)left : (1 << m);
-  const int grp = threadIdx.x >> 4, r = threadIdx.x & 15, ngrp = blockDim.x / 16;
-  for (int i = threadIdx.x; i < 16 * cnt; i += blockDim.x) {
+  const int grp = threadIdx.x >> 4, r = threadIdx.x & 15, ngrp = kSegThreads / 16;
+  for (int i = threadIdx.x; i < 16 * cnt; i += kSegThreads) {
     const int p = i >> 4, c = i & 15;
     ws[i] = c < 15 ? rv[15 * (int64_t)s.S.chain_perm[base + p] + c] : T(0);
   }
@@ -593,7 +590,7 @@ __global__ void __launch_bounds__(kSegThreadsMax) k_chain_seg_fwd(SolverLaunch<T
     }
     __syncthreads();
   }
-  for (int i = threadIdx.x; i < 16 * cnt; i += blockDim.x)
+  for (int i = threadIdx.x; i < 16 * cnt; i += kSegThreads)
     if ((i & 15) < 15) s.C.w[15 * base + 15 * (i >> 4) + (i & 15)] = ws[i];
   // Terms of the next segment's first position q' = base + 2^m from this
   // segment's positions q' - 2^l (eliminated at level l, final now).
@@ -611,7 +608,7 @@ __global__ void __launch_bounds__(kSegThreadsMax) k_chain_seg_fwd(SolverLaunch<T
 // segment's first position and the next segment's first position were solved
 // by the tail.  Writes z of the eliminated positions and adds their r.z.
 template <typename T>
-__global__ void __launch_bounds__(kSegThreadsMax) k_chain_seg_bwd(SolverLaunch<T> s, int m, const T* rv, T* z,
+__global__ void __launch_bounds__(kSegThreads) k_chain_seg_bwd(SolverLaunch<T> s, int m, const T* rv, T* z,
                                                                double* rz) {
   if (apply_gate(s.ctl)) return;
   extern __shared__ __align__(16) unsigned char seg_smem[];
@@ -621,9 +618,9 @@ __global__ void __launch_bounds__(kSegThreadsMax) k_chain_seg_bwd(SolverLaunch<T
   const int64_t n = s.P.nkf, base = (int64_t)blockIdx.x << m;
   const int64_t left = n - base;
   const int cnt = left < (int64_t)seg ? (int)left : seg;
-  const int grp = threadIdx.x >> 4, r = threadIdx.x & 15, ngrp = blockDim.x / 16;
+  const int grp = threadIdx.x >> 4, r = threadIdx.x & 15, ngrp = kSegThreads / 16;
   const unsigned mask = 0xffffu << (threadIdx.x & 16);
-  for (int i = threadIdx.x; i < 16 * cnt; i += blockDim.x)
+  for (int i = threadIdx.x; i < 16 * cnt; i += kSegThreads)
     ws[i] = (i & 15) < 15 ? s.C.w[15 * base + 15 * (i >> 4) + (i & 15)] : T(0);
   if (threadIdx.x < 15) zs[threadIdx.x] = z[15 * (int64_t)s.S.chain_perm[base] + threadIdx.x];
   if (threadIdx.x >= 16 && threadIdx.x < 31 && base + seg < n)
@@ -699,9 +696,9 @@ cudaError_t chain_apply(const SolverLaunch<T>& s, const T* r, T* z, double* rz, 
     const int m = s.S.chain_seg;
     const unsigned blocks = nb(n, 1 << m);
     const size_t sm = sizeof(T) * 16 * (size_t)(1 << m);
-    k_chain_seg_fwd<T><<<blocks, seg_threads(m), sm, st>>>(s, m, r);
+    k_chain_seg_fwd<T><<<blocks, kSegThreads, sm, st>>>(s, m, r);
     launch_tail<T>(s, m, m, r, z, rz, st);
-    k_chain_seg_bwd<T><<<blocks, seg_threads(m), 2 * sm + sizeof(T) * 16, st>>>(s, m, r, z, rz);
+    k_chain_seg_bwd<T><<<blocks, kSegThreads, 2 * sm + sizeof(T) * 16, st>>>(s, m, r, z, rz);
     return cudaGetLastError();
   }
   k_chain_fwd0<T><<<nb(16 * n, 128), 128, 0, st>>>(s, r);
