@@ -825,12 +825,7 @@ mba_status linearize_visual_host(mba_handle* h, double* r, double* Jl, double* J
     // the internal one: the host-link stores of chunk c (rows written
     // contiguously) run on a second stream while chunk c + 1 is evaluated.
     cudaError_t e = cudaSuccess;
-    if (!h->side) {
-      // highest priority: the copy blocks are scheduled between the next chunk's evaluation blocks
-      int least = 0, greatest = 0;
-      e = cudaDeviceGetStreamPriorityRange(&least, &greatest);
-      if (e == cudaSuccess) e = cudaStreamCreateWithPriority(&h->side, cudaStreamNonBlocking, greatest);
-    }
+    if (!h->side) e = cudaStreamCreateWithFlags(&h->side, cudaStreamNonBlocking);
     for (int c = 0; c < kLinChunks && e == cudaSuccess; ++c)
       if (!h->chunk_ev[c]) e = cudaEventCreateWithFlags(&h->chunk_ev[c], cudaEventDisableTiming);
     for (int c = 0; c < kLinChunks && e == cudaSuccess; ++c) {
