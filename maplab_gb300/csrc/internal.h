@@ -124,11 +124,11 @@ struct InertialLin {
 cudaError_t launch_visual_ambient(const DevProblem& P, double* res, double* const* jac_dev, cudaStream_t s);
 template <typename T>
 cudaError_t launch_visual_linearize(const DevProblem& P, VisualLin<T> out, double* cost_accum, cudaStream_t s);
-// Caller rows [lo, hi) of a linearization (row j = internal observation
-// obs_inv[j]) to row-major arrays; any array may be null.
+// Rows of the internal observations [lo, hi) of a linearization to the
+// caller's row-major arrays at the caller's indices (any array may be null).
 template <typename T>
-cudaError_t launch_gather_rows(const DevProblem& P, const int64_t* obs_inv, int64_t lo, int64_t hi, VisualLin<T> v,
-                               double* r, double* Jl, double* Js, double* Jo, cudaStream_t s);
+cudaError_t launch_gather_range(const DevProblem& P, int64_t lo, int64_t hi, VisualLin<T> v, double* r, double* Jl,
+                                double* Js, double* Jo, cudaStream_t s);
 cudaError_t launch_visual_cost(const DevProblem& P, const double* kf_state, const double* lm_p, double* cost_accum,
                                int* nonfinite, cudaStream_t s);
 // Inertial: full evaluation at `kf_state`; writes tangent linearization (if

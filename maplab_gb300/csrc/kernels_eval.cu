@@ -974,14 +974,12 @@ namespace {
 // coalesce also when the destination is page-locked host memory.
 constexpr int kGatherRows = 128;
 template <typename T>
-__global__ void __launch_bounds__(kGatherRows) k_gather_rows(int64_t N, int64_t lo, int64_t hi, const int64_t* inv,
-                                                             VisualLin<T> v, double* r, double* Jl, double* Js,
-                                                             double* Jo) {
-  // caller rows [lo, hi); row j holds internal observation inv[j]
+__global__ void __launch_bounds__(kGatherRows) k_gather_rows(int64_t N, const int64_t* inv, VisualLin<T> v, double* r,
+                                                             double* Jl, double* Js, double* Jo) {
   __shared__ double sh[32 * kGatherRows];
-  const int64_t base = lo + (int64_t)blockIdx.x * kGatherRows;
+  const int64_t base = (int64_t)blockIdx.x * kGatherRows;
   const int t = threadIdx.x;
-  const int cnt = (int)(hi - base < kGatherRows ? hi - base : kGatherRows);
+  const int cnt = (int)(N - base < kGatherRows ? N - base : kGatherRows);
   if (t < cnt) {
     const int64_t i = inv[base + t];
     if (r) for (int c = 0; c < 2; ++c) sh[c * kGatherRows + t] = (double)v.r[c * N + i];
@@ -999,6 +997,27 @@ __global__ void __launch_bounds__(kGatherRows) k_gather_rows(int64_t N, int64_t 
     double* out = dst[a] + base * w;
     for (int k = t; k < cnt * w; k += kGatherRows) out[k] = sh[(first[a] + k % w) * kGatherRows + k / w];
   }
+}
+
+// Rows of the internal observations [lo, hi) to the caller's row-major
+// arrays at the caller's indices perm[i] (coalesced when the caller's order
+// follows the internal landmark order); any array may be null.
+template <typename T>
+__global__ void __launch_bounds__(kGatherRows) k_gather_range(int64_t N, int64_t lo, int64_t hi, const int64_t* perm,
+                                                              VisualLin<T> v, double* r, double* Jl, double* Js,
+                                                              double* Jo) {
+  const int64_t i = lo + (int64_t)blockIdx.x * kGatherRows + threadIdx.x;
+  if (i >= hi) return;
+  const int64_t j = perm[i];
+  auto put = [&](double* dst, const T* src, int w) {
+    if (!dst) return;
+    double2* q = reinterpret_cast<double2*>(dst + w * j);
+    for (int c = 0; c < w; c += 2) q[c / 2] = make_double2((double)src[c * N + i], (double)src[(c + 1) * N + i]);
+  };
+  put(r, v.r, 2);
+  put(Jl, v.Jl, 6);
+  put(Js, v.Js, 12);
+  put(Jo, v.Jo, 12);
 }
 
 __global__ void k_pack_state(int64_t NK, int64_t NL, double* kf_state, double* lm_p, float* kf_pose_f, float* lm_p_f,
@@ -1041,29 +1060,30 @@ __global__ void k_pack_state(int64_t NK, int64_t NL, double* kf_state, double* l
 }  // namespace
 
 template <typename T>
-cudaError_t launch_gather_rows(const DevProblem& P, const int64_t* obs_inv, int64_t lo, int64_t hi, VisualLin<T> v,
-                               double* r, double* Jl, double* Js, double* Jo, cudaStream_t s) {
-  if (hi <= lo) return cudaSuccess;
-  k_gather_rows<T><<<(unsigned)((hi - lo + kGatherRows - 1) / kGatherRows), kGatherRows, 0, s>>>(P.nobs, lo, hi, obs_inv,
-                                                                                                v, r, Jl, Js, Jo);
-  return cudaGetLastError();
-}
-template cudaError_t launch_gather_rows<double>(const DevProblem&, const int64_t*, int64_t, int64_t, VisualLin<double>,
-                                                double*, double*, double*, double*, cudaStream_t);
-template cudaError_t launch_gather_rows<float>(const DevProblem&, const int64_t*, int64_t, int64_t, VisualLin<float>,
-                                               double*, double*, double*, double*, cudaStream_t);
-
-template <typename T>
 cudaError_t launch_gather_visual(const DevProblem& P, const int64_t* obs_inv, VisualLin<T> v, double* r, double* Jl,
                                  double* Js, double* Jo, cudaStream_t s) {
   if (P.nobs == 0) return cudaSuccess;
-  return launch_gather_rows<T>(P, obs_inv, 0, P.nobs, v, r, Jl, Js, Jo, s);
+  k_gather_rows<T><<<(unsigned)((P.nobs + kGatherRows - 1) / kGatherRows), kGatherRows, 0, s>>>(P.nobs, obs_inv, v, r,
+                                                                                                  Jl, Js, Jo);
+  return cudaGetLastError();
 }
 template cudaError_t launch_gather_visual<double>(const DevProblem&, const int64_t*, VisualLin<double>, double*,
                                                   double*, double*, double*, cudaStream_t);
 template cudaError_t launch_gather_visual<float>(const DevProblem&, const int64_t*, VisualLin<float>, double*, double*,
                                                  double*, double*, cudaStream_t);
 
+template <typename T>
+cudaError_t launch_gather_range(const DevProblem& P, int64_t lo, int64_t hi, VisualLin<T> v, double* r, double* Jl,
+                                double* Js, double* Jo, cudaStream_t s) {
+  if (hi <= lo) return cudaSuccess;
+  k_gather_range<T><<<(unsigned)((hi - lo + kGatherRows - 1) / kGatherRows), kGatherRows, 0, s>>>(
+      P.nobs, lo, hi, P.obs_perm, v, r, Jl, Js, Jo);
+  return cudaGetLastError();
+}
+template cudaError_t launch_gather_range<double>(const DevProblem&, int64_t, int64_t, VisualLin<double>, double*,
+                                                 double*, double*, double*, cudaStream_t);
+template cudaError_t launch_gather_range<float>(const DevProblem&, int64_t, int64_t, VisualLin<float>, double*,
+                                                double*, double*, double*, cudaStream_t);
 
 namespace {
 __global__ void k_invert_perm(int64_t N, const int64_t* perm, int64_t* inv) {

@@ -150,7 +150,6 @@ struct mba_handle {
   std::atomic<int> cancel{0};
   // host copies used by the API
   std::vector<int64_t> perm;  // sorted -> caller observation index
-  bool perm_identity = false;  // the caller's observations are already in internal (landmark) order
   // solver state (lazily allocated)
   bool solver_ready = false;
   SolverBuffers<double> b64;
@@ -820,10 +819,9 @@ mba_status linearize_visual_host(mba_handle* h, double* r, double* Jl, double* J
     mapped[a] = static_cast<double*>(mapped_host_range(out[a], sizeof(double) * width[a] * N));
     direct = direct && mapped[a];
   }
-  if (direct && sizeof(T) == 8 && h->perm_identity && N >= 4096 * kLinChunks) {
-    // FP64 rows into page-locked memory in chunks when the caller's order is
-    // the internal one: the host-link stores of chunk c (rows written
-    // contiguously) run on a second stream while chunk c + 1 is evaluated.
+  if (direct && sizeof(T) == 8 && N >= 4096 * kLinChunks) {
+    // FP64 rows into page-locked memory in chunks: the host-link stores of
+    // chunk c run on a second stream while chunk c + 1 is evaluated.
     cudaError_t e = cudaSuccess;
     if (!h->side) e = cudaStreamCreateWithFlags(&h->side, cudaStreamNonBlocking);
     for (int c = 0; c < kLinChunks && e == cudaSuccess; ++c)
@@ -836,8 +834,8 @@ mba_status linearize_visual_host(mba_handle* h, double* r, double* Jl, double* J
       if (e == cudaSuccess) e = cudaEventRecord(h->chunk_ev[c], st);
       if (e == cudaSuccess) e = cudaStreamWaitEvent(h->side, h->chunk_ev[c], 0);
       if (e == cudaSuccess)
-        e = launch_gather_rows<T>(h->P, h->obs_inv, Pc.vis_lo, Pc.vis_hi, b.vis, mapped[0], mapped[1], mapped[2],
-                                  mapped[3], h->side);
+        e = launch_gather_range<T>(h->P, Pc.vis_lo, Pc.vis_hi, b.vis, mapped[0], mapped[1], mapped[2], mapped[3],
+                                   h->side);
     }
     if (e == cudaSuccess) e = cudaStreamSynchronize(h->side);
     if (e == cudaSuccess) e = cudaStreamSynchronize(st);
@@ -1079,8 +1077,6 @@ mba_status mba_create(const mba_problem_desc* d, int32_t device, mba_handle** ou
     std::vector<int64_t> fill(off.begin(), off.end() - 1);
     for (int64_t i = 0; i < N; ++i) h->perm[fill[d->obs_landmark[i]]++] = i;
   }
-  h->perm_identity = true;
-  for (int64_t i = 0; i < N && h->perm_identity; ++i) h->perm_identity = h->perm[i] == i;
   std::vector<double> uv(2 * N), sinv(N), hub(N);
   std::vector<int32_t> olm(N), okf(N), ost(N);
   std::vector<uint8_t> ocam(N), otype(N);
