@@ -17,7 +17,6 @@ struct DevProblem {
   int32_t vis_block;        // threads per block of the evaluation kernel (tuned; 0 = default)
   int32_t vis_minb;         // > 1: register-lean variant of the evaluation kernel (tuned)
   int32_t vis_pipe;         // 1: pipelined persistent variant of the evaluation kernel (tuned)
-  int64_t vis_lo, vis_hi;   // observations the evaluation kernels cover ([0, nobs) except for chunked calls)
   // observations
   const double2* obs_uv;
   const double* obs_sinv;   // 1 / sigma
@@ -124,11 +123,6 @@ struct InertialLin {
 cudaError_t launch_visual_ambient(const DevProblem& P, double* res, double* const* jac_dev, cudaStream_t s);
 template <typename T>
 cudaError_t launch_visual_linearize(const DevProblem& P, VisualLin<T> out, double* cost_accum, cudaStream_t s);
-// Rows of the internal observations [lo, hi) of a linearization to the
-// caller's row-major arrays at the caller's indices (any array may be null).
-template <typename T>
-cudaError_t launch_gather_range(const DevProblem& P, int64_t lo, int64_t hi, VisualLin<T> v, double* r, double* Jl,
-                                double* Js, double* Jo, cudaStream_t s);
 cudaError_t launch_visual_cost(const DevProblem& P, const double* kf_state, const double* lm_p, double* cost_accum,
                                int* nonfinite, cudaStream_t s);
 // Inertial: full evaluation at `kf_state`; writes tangent linearization (if

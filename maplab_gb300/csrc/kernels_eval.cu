@@ -366,9 +366,9 @@ __global__ void __launch_bounds__(kBlock, kMinBlocks) k_visual_linearize(DevProb
   if (gated(run_if, skip_if)) return;
   __shared__ T rci[9 * kCamRot];
   const bool cam_sm = stage_camera_rotations(P, in, rci);
-  const int64_t i = P.vis_lo + blockIdx.x * (int64_t)blockDim.x + threadIdx.x;
+  const int64_t i = blockIdx.x * (int64_t)blockDim.x + threadIdx.x;
   double cost = 0.0;
-  if (i < P.vis_hi) {
+  if (i < P.nobs) {
     ObsInputs<T> o;
     load_obs_stream(P, in, i, o);
     load_obs_gather(P, in, o);
@@ -390,21 +390,20 @@ __global__ void __launch_bounds__(kBlock, kMinBlocks) k_visual_linearize_pipe(De
   if (gated(run_if, skip_if)) return;
   __shared__ T rci[9 * kCamRot];
   const bool cam_sm = stage_camera_rotations(P, in, rci);
-  // observations [vis_lo, vis_hi) of the component-major outputs of stride N
-  const int64_t N = P.nobs, hi = P.vis_hi, stride = (int64_t)gridDim.x * blockDim.x;
-  int64_t i = P.vis_lo + blockIdx.x * (int64_t)blockDim.x + threadIdx.x;
+  const int64_t N = P.nobs, stride = (int64_t)gridDim.x * blockDim.x;
+  int64_t i = blockIdx.x * (int64_t)blockDim.x + threadIdx.x;
   double cost = 0.0;
   ObsInputs<T> cur, nxt;
-  if (i < hi) {
+  if (i < N) {
     load_obs_stream(P, in, i, cur);
     load_obs_gather(P, in, cur);
   }
-  if (i + stride < hi) load_obs_stream(P, in, i + stride, nxt);
-  for (; i < hi; i += stride) {
+  if (i + stride < N) load_obs_stream(P, in, i + stride, nxt);
+  for (; i < N; i += stride) {
     const int64_t j = i + stride;
-    if (j < hi) load_obs_gather(P, in, nxt);
+    if (j < N) load_obs_gather(P, in, nxt);
     ObsInputs<T> nn;
-    if (j + stride < hi) load_obs_stream(P, in, j + stride, nn);
+    if (j + stride < N) load_obs_stream(P, in, j + stride, nn);
     cost += compute_obs<T, kCost>(P, in, cur, out, i, N, cam_sm ? rci + 9 * cur.cam : nullptr);
     cur = nxt;
     nxt = nn;
@@ -865,7 +864,7 @@ __global__ void k_kf_rotations(const double* kf_state, int64_t nkf, double* out,
 template <typename T>
 cudaError_t launch_visual_linearize_gated(const DevProblem& P, VisualLin<T> out, double* cost_accum, const int* run_if,
                                           const int* skip_if, cudaStream_t s) {
-  if (P.vis_hi <= P.vis_lo) return cudaSuccess;
+  if (P.nobs == 0) return cudaSuccess;
   if constexpr (sizeof(T) == 8)
     k_kf_rotations<<<(unsigned)((P.nkf + 127) / 128), 128, 0, s>>>(P.kf_state, P.nkf, P.kf_rot, run_if, skip_if);
   // Block size: tuned per problem (mba_autotune), at most the launch bound.
@@ -879,12 +878,12 @@ cudaError_t launch_visual_linearize_gated(const DevProblem& P, VisualLin<T> out,
     auto kern = cost_accum ? (capped ? k_visual_linearize_pipe<T, true, 2> : k_visual_linearize_pipe<T, true, 1>)
                            : (capped ? k_visual_linearize_pipe<T, false, 2> : k_visual_linearize_pipe<T, false, 1>);
     cudaOccupancyMaxActiveBlocksPerMultiprocessor(&per_sm, kern, bs, 0);
-    const int64_t need = (P.vis_hi - P.vis_lo + bs - 1) / bs;
+    const int64_t need = (P.nobs + bs - 1) / bs;
     const int64_t grid = std::min<int64_t>(need, (int64_t)std::max(1, per_sm) * std::max(1, sms));
     kern<<<(unsigned)grid, bs, 0, s>>>(P, visual_inputs<T>(P), out, cost_accum, run_if, skip_if);
     return cudaGetLastError();
   }
-  const int64_t blocks = (P.vis_hi - P.vis_lo + bs - 1) / bs;
+  const int64_t blocks = (P.nobs + bs - 1) / bs;
   // Register caps: minb 1 none, 3 -> 85 registers, 4 -> 64 registers (more warps per SM, more spills).
   auto kern = cost_accum ? (P.vis_minb >= 4 ? k_visual_linearize<T, true, 4>
                             : P.vis_minb > 1 ? k_visual_linearize<T, true, 3> : k_visual_linearize<T, true, 1>)
@@ -999,27 +998,6 @@ __global__ void __launch_bounds__(kGatherRows) k_gather_rows(int64_t N, const in
   }
 }
 
-// Rows of the internal observations [lo, hi) to the caller's row-major
-// arrays at the caller's indices perm[i] (coalesced when the caller's order
-// follows the internal landmark order); any array may be null.
-template <typename T>
-__global__ void __launch_bounds__(kGatherRows) k_gather_range(int64_t N, int64_t lo, int64_t hi, const int64_t* perm,
-                                                              VisualLin<T> v, double* r, double* Jl, double* Js,
-                                                              double* Jo) {
-  const int64_t i = lo + (int64_t)blockIdx.x * kGatherRows + threadIdx.x;
-  if (i >= hi) return;
-  const int64_t j = perm[i];
-  auto put = [&](double* dst, const T* src, int w) {
-    if (!dst) return;
-    double2* q = reinterpret_cast<double2*>(dst + w * j);
-    for (int c = 0; c < w; c += 2) q[c / 2] = make_double2((double)src[c * N + i], (double)src[(c + 1) * N + i]);
-  };
-  put(r, v.r, 2);
-  put(Jl, v.Jl, 6);
-  put(Js, v.Js, 12);
-  put(Jo, v.Jo, 12);
-}
-
 __global__ void k_pack_state(int64_t NK, int64_t NL, double* kf_state, double* lm_p, float* kf_pose_f, float* lm_p_f,
                              const double* kx, const double* kv, const double* kbg, const double* kba, const double* lp,
                              int to_device) {
@@ -1071,19 +1049,6 @@ template cudaError_t launch_gather_visual<double>(const DevProblem&, const int64
                                                   double*, double*, double*, cudaStream_t);
 template cudaError_t launch_gather_visual<float>(const DevProblem&, const int64_t*, VisualLin<float>, double*, double*,
                                                  double*, double*, cudaStream_t);
-
-template <typename T>
-cudaError_t launch_gather_range(const DevProblem& P, int64_t lo, int64_t hi, VisualLin<T> v, double* r, double* Jl,
-                                double* Js, double* Jo, cudaStream_t s) {
-  if (hi <= lo) return cudaSuccess;
-  k_gather_range<T><<<(unsigned)((hi - lo + kGatherRows - 1) / kGatherRows), kGatherRows, 0, s>>>(
-      P.nobs, lo, hi, P.obs_perm, v, r, Jl, Js, Jo);
-  return cudaGetLastError();
-}
-template cudaError_t launch_gather_range<double>(const DevProblem&, int64_t, int64_t, VisualLin<double>, double*,
-                                                 double*, double*, double*, cudaStream_t);
-template cudaError_t launch_gather_range<float>(const DevProblem&, int64_t, int64_t, VisualLin<float>, double*,
-                                                double*, double*, double*, cudaStream_t);
 
 namespace {
 __global__ void k_invert_perm(int64_t N, const int64_t* perm, int64_t* inv) {

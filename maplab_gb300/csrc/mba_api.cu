@@ -137,13 +137,9 @@ struct mba_gnn {
   GnnParams p{};
 };
 
-constexpr int kLinChunks = 8;  // chunks of a linearization into page-locked host memory
-
 struct mba_handle {
   int device = 0;
   cudaStream_t stream = nullptr;
-  cudaStream_t side = nullptr;          // host-row copies overlapping the next chunk's evaluation
-  cudaEvent_t chunk_ev[kLinChunks] = {};
   DeviceArena arena;
   DevProblem P{};
   SchurPattern S{};
@@ -819,28 +815,6 @@ mba_status linearize_visual_host(mba_handle* h, double* r, double* Jl, double* J
     mapped[a] = static_cast<double*>(mapped_host_range(out[a], sizeof(double) * width[a] * N));
     direct = direct && mapped[a];
   }
-  if (direct && sizeof(T) == 8 && N >= 4096 * kLinChunks) {
-    // FP64 rows into page-locked memory in chunks: the host-link stores of
-    // chunk c run on a second stream while chunk c + 1 is evaluated.
-    cudaError_t e = cudaSuccess;
-    if (!h->side) e = cudaStreamCreateWithFlags(&h->side, cudaStreamNonBlocking);
-    for (int c = 0; c < kLinChunks && e == cudaSuccess; ++c)
-      if (!h->chunk_ev[c]) e = cudaEventCreateWithFlags(&h->chunk_ev[c], cudaEventDisableTiming);
-    for (int c = 0; c < kLinChunks && e == cudaSuccess; ++c) {
-      DevProblem Pc = h->P;
-      Pc.vis_lo = N * c / kLinChunks;
-      Pc.vis_hi = N * (c + 1) / kLinChunks;
-      e = launch_visual_linearize<T>(Pc, b.vis, nullptr, st);
-      if (e == cudaSuccess) e = cudaEventRecord(h->chunk_ev[c], st);
-      if (e == cudaSuccess) e = cudaStreamWaitEvent(h->side, h->chunk_ev[c], 0);
-      if (e == cudaSuccess)
-        e = launch_gather_range<T>(h->P, Pc.vis_lo, Pc.vis_hi, b.vis, mapped[0], mapped[1], mapped[2], mapped[3],
-                                   h->side);
-    }
-    if (e == cudaSuccess) e = cudaStreamSynchronize(h->side);
-    if (e == cudaSuccess) e = cudaStreamSynchronize(st);
-    return cuda_status(e);
-  }
   cudaError_t e = launch_visual_linearize<T>(h->P, b.vis, nullptr, st);
   if (direct) {
     if (e == cudaSuccess) e = launch_gather_visual<T>(h->P, h->obs_inv, b.vis, mapped[0], mapped[1], mapped[2], mapped[3], st);
@@ -1404,8 +1378,6 @@ mba_status mba_create(const mba_problem_desc* d, int32_t device, mba_handle** ou
   DeviceArena& A = h->arena;
   DevProblem& P = h->P;
   P.nkf = NK; P.nlm = NL; P.nobs = N; P.ncam = NC; P.nmis = NM; P.nedge = NE; P.nimu = NIMU; P.nsamp = NSMP;
-  P.vis_lo = 0;
-  P.vis_hi = N;
   P.obs_uv = reinterpret_cast<const double2*>(A.upload(uv, st));
   P.obs_sinv = A.upload(sinv, st);
   P.obs_huber = A.upload(hub, st);
@@ -1553,11 +1525,7 @@ void mba_destroy(mba_handle* h) {
   cudaSetDevice(h->device);
   if (h->stream) cudaStreamSynchronize(h->stream);
   h->arena.release();
-  if (h->side) cudaStreamSynchronize(h->side);
   if (h->cancel_host) cudaFreeHost((void*)h->cancel_host);
-  for (cudaEvent_t& ev : h->chunk_ev)
-    if (ev) cudaEventDestroy(ev);
-  if (h->side) cudaStreamDestroy(h->side);
   if (h->stream) cudaStreamDestroy(h->stream);
   delete h;
 }

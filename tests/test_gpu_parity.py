@@ -137,25 +137,6 @@ def test_linearize_visual_into_pinned_host_memory(multi, precision):
         np.testing.assert_array_equal(sub[2].numpy(), ref[2])
 
 
-def test_linearize_visual_chunked_into_pinned_host_memory():
-    """A map large enough for the chunked FP64 path (evaluation of chunk c + 1
-    overlapping the host-row stores of chunk c on a second stream): the same
-    rows, bit for bit, as the pageable path."""
-    import ctypes
-    import torch
-    m = synth.generate("c2", keyframes_per_mission=200, num_landmarks=20000)
-    n = m.desc.num_observations
-    assert n >= 4096 * 8
-    with ba.BundleAdjuster(m.desc) as g:
-        ref = g.linearize_visual(N.MBA_PRECISION_FP64)
-        pinned = [torch.full((n, c), np.nan, dtype=torch.float64).pin_memory() for c in (2, 6, 12, 12)]
-        P = lambda t: ctypes.cast(t.data_ptr(), N.c_double_p)
-        for _ in range(2):  # the second call reuses the stream and events
-            assert ba.lib().mba_linearize_visual(g.handle, N.MBA_PRECISION_FP64, *[P(t) for t in pinned]) == 0
-            for a, b in zip(pinned, ref):
-                np.testing.assert_array_equal(a.numpy(), b)
-
-
 @pytest.mark.parametrize("pipelined, min_blocks, block", [(2, 1, 256), (2, 3, 64), (1, 1, 128), (1, 2, 256), (1, 2, 64)])
 def test_evaluation_kernel_variants_agree(multi, pipelined, min_blocks, block):
     """The pipelined persistent loop and the register-capped variants run the
