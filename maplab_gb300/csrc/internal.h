@@ -17,6 +17,7 @@ struct DevProblem {
   int32_t vis_block;        // threads per block of the evaluation kernel (tuned; 0 = default)
   int32_t vis_minb;         // > 1: register-lean variant of the evaluation kernel (tuned)
   int32_t vis_pipe;         // 1: pipelined persistent variant of the evaluation kernel (tuned)
+  int64_t vis_lo, vis_hi;   // observations [vis_lo, vis_hi) of the linearization kernels (vis_hi 0: to nobs)
   // observations
   const double2* obs_uv;
   const double* obs_sinv;   // 1 / sigma
@@ -88,6 +89,9 @@ struct DevProblem {
   const uint32_t* mis_flags;// [nmis] MBA_MIS_BASEFRAME_*
 };
 
+// End of the linearization kernels' observation range.
+__host__ __device__ inline int64_t vis_end(const DevProblem& P) { return P.vis_hi > 0 ? P.vis_hi : P.nobs; }
+
 // Typed view of the inputs of the evaluation kernel (FP64 arrays for the
 // FP64 kernel, the FP32 mirrors for the FP32 kernel).
 template <typename T>
@@ -145,12 +149,30 @@ template <typename T>
 cudaError_t launch_gather_visual(const DevProblem& P, const int64_t* obs_inv, VisualLin<T> v, double* r, double* Jl,
                                  double* Js, double* Jo, cudaStream_t s);
 cudaError_t launch_invert_perm(const DevProblem& P, int64_t* inv, cudaStream_t s);
+// Caller rows [lo, hi) (inv: caller -> sorted index; null when the SoA buffers
+// are in caller order already).
+template <typename T>
+cudaError_t launch_gather_rows(const DevProblem& P, const int64_t* inv, int64_t lo, int64_t hi, VisualLin<T> v,
+                               double* r, double* Jl, double* Js, double* Jo, cudaStream_t s);
+// The observation fields the FP64 linearization reads, in the caller's order
+// (a DevProblem pointing at them evaluates caller row o as observation o).
+struct CallerObs {
+  double2* uv;
+  double* sinv;
+  double* huber;
+  int32_t *lm, *kf, *store;
+  uint8_t *cam, *type;
+};
+cudaError_t launch_caller_obs(const DevProblem& P, const int64_t* inv, CallerObs c, cudaStream_t s);
 // isVisualLandmarkWellConstrained per landmark at the current state (good [nlm]).
 cudaError_t launch_landmark_quality(const DevProblem& P, const mba_landmark_quality_options& o, uint8_t* good,
                                     cudaStream_t s);
 // to_device = 1: host-layout device arrays -> kf_state / lm_p; 0: the reverse.
+// lp is in the caller's landmark numbering: lm_caller [nlm] maps an internal
+// landmark to it (nullptr: the same numbering).
 cudaError_t launch_pack_state(const DevProblem& P, const double* kx, const double* kv, const double* kbg,
-                              const double* kba, const double* lp, int to_device, cudaStream_t s);
+                              const double* kba, const double* lp, const int32_t* lm_caller, int to_device,
+                              cudaStream_t s);
 // kernels_inertial.cu: f32_matrices selects FP32 propagation of Phi and Q
 // (mixed path); the state, Cholesky, residual and Jacobians stay FP64.
 cudaError_t launch_inertial_v2(const DevProblem& P, const double* kf_state, bool f32_matrices, InertialLin<double> lin,

@@ -368,7 +368,7 @@ __global__ void __launch_bounds__(64) k_border_schur(SolverLaunch<double> s) {
           if (v != 0.0) atomicAdd(&blk[15 * r + c], -v);
         }
     }
-    for (int64_t sl = s.S.lm_slot_off[l]; sl < s.S.lm_slot_off[l + 1]; ++sl) {
+    for (int64_t sl = s.S.lm_slot_off[l]; sl < s.S.lm_slot_end[l]; ++sl) {
       const int64_t k = s.S.slot_kf[sl];
       const double* U = s.L.U + kSlotStride * sl;  // V W_slot, 3 x 6
       double* blk = s.B.BS + 90 * (G * k + ids[b]);

@@ -366,9 +366,9 @@ __global__ void __launch_bounds__(kBlock, kMinBlocks) k_visual_linearize(DevProb
   if (gated(run_if, skip_if)) return;
   __shared__ T rci[9 * kCamRot];
   const bool cam_sm = stage_camera_rotations(P, in, rci);
-  const int64_t i = blockIdx.x * (int64_t)blockDim.x + threadIdx.x;
+  const int64_t i = P.vis_lo + blockIdx.x * (int64_t)blockDim.x + threadIdx.x;
   double cost = 0.0;
-  if (i < P.nobs) {
+  if (i < vis_end(P)) {
     ObsInputs<T> o;
     load_obs_stream(P, in, i, o);
     load_obs_gather(P, in, o);
@@ -390,20 +390,21 @@ __global__ void __launch_bounds__(kBlock, kMinBlocks) k_visual_linearize_pipe(De
   if (gated(run_if, skip_if)) return;
   __shared__ T rci[9 * kCamRot];
   const bool cam_sm = stage_camera_rotations(P, in, rci);
-  const int64_t N = P.nobs, stride = (int64_t)gridDim.x * blockDim.x;
-  int64_t i = blockIdx.x * (int64_t)blockDim.x + threadIdx.x;
+  // observations [vis_lo, hi) of the component-major outputs of stride N
+  const int64_t N = P.nobs, hi = vis_end(P), stride = (int64_t)gridDim.x * blockDim.x;
+  int64_t i = P.vis_lo + blockIdx.x * (int64_t)blockDim.x + threadIdx.x;
   double cost = 0.0;
   ObsInputs<T> cur, nxt;
-  if (i < N) {
+  if (i < hi) {
     load_obs_stream(P, in, i, cur);
     load_obs_gather(P, in, cur);
   }
-  if (i + stride < N) load_obs_stream(P, in, i + stride, nxt);
-  for (; i < N; i += stride) {
+  if (i + stride < hi) load_obs_stream(P, in, i + stride, nxt);
+  for (; i < hi; i += stride) {
     const int64_t j = i + stride;
-    if (j < N) load_obs_gather(P, in, nxt);
+    if (j < hi) load_obs_gather(P, in, nxt);
     ObsInputs<T> nn;
-    if (j + stride < N) load_obs_stream(P, in, j + stride, nn);
+    if (j + stride < hi) load_obs_stream(P, in, j + stride, nn);
     cost += compute_obs<T, kCost>(P, in, cur, out, i, N, cam_sm ? rci + 9 * cur.cam : nullptr);
     cur = nxt;
     nxt = nn;
@@ -864,8 +865,10 @@ __global__ void k_kf_rotations(const double* kf_state, int64_t nkf, double* out,
 template <typename T>
 cudaError_t launch_visual_linearize_gated(const DevProblem& P, VisualLin<T> out, double* cost_accum, const int* run_if,
                                           const int* skip_if, cudaStream_t s) {
-  if (P.nobs == 0) return cudaSuccess;
-  if constexpr (sizeof(T) == 8)
+  const int64_t n = vis_end(P) - P.vis_lo;
+  if (n <= 0) return cudaSuccess;
+  // A chunk after the first of a chunked evaluation reuses the rotations.
+  if (sizeof(T) == 8 && P.vis_lo == 0)
     k_kf_rotations<<<(unsigned)((P.nkf + 127) / 128), 128, 0, s>>>(P.kf_state, P.nkf, P.kf_rot, run_if, skip_if);
   // Block size: tuned per problem (mba_autotune), at most the launch bound.
   const int bs = (P.vis_block > 0 && P.vis_block <= kBlock) ? P.vis_block : kBlock;
@@ -878,12 +881,12 @@ cudaError_t launch_visual_linearize_gated(const DevProblem& P, VisualLin<T> out,
     auto kern = cost_accum ? (capped ? k_visual_linearize_pipe<T, true, 2> : k_visual_linearize_pipe<T, true, 1>)
                            : (capped ? k_visual_linearize_pipe<T, false, 2> : k_visual_linearize_pipe<T, false, 1>);
     cudaOccupancyMaxActiveBlocksPerMultiprocessor(&per_sm, kern, bs, 0);
-    const int64_t need = (P.nobs + bs - 1) / bs;
+    const int64_t need = (n + bs - 1) / bs;
     const int64_t grid = std::min<int64_t>(need, (int64_t)std::max(1, per_sm) * std::max(1, sms));
     kern<<<(unsigned)grid, bs, 0, s>>>(P, visual_inputs<T>(P), out, cost_accum, run_if, skip_if);
     return cudaGetLastError();
   }
-  const int64_t blocks = (P.nobs + bs - 1) / bs;
+  const int64_t blocks = (n + bs - 1) / bs;
   // Register caps: minb 1 none, 3 -> 85 registers, 4 -> 64 registers (more warps per SM, more spills).
   auto kern = cost_accum ? (P.vis_minb >= 4 ? k_visual_linearize<T, true, 4>
                             : P.vis_minb > 1 ? k_visual_linearize<T, true, 3> : k_visual_linearize<T, true, 1>)
@@ -965,22 +968,24 @@ cudaError_t launch_inertial_f32(const DevProblem& P, const InertialLin<double>& 
 }
 
 namespace {
-// Caller-order rows of the linearization in FP64: r [N][2], J_l [N][6],
-// J_s [N][12], J_o [N][12] (each may be null).  A block takes kGatherRows
-// consecutive caller indices o, reads sorted index inv[o] from the SoA
+// Caller-order rows [lo, hi) of the linearization in FP64: r [N][2],
+// J_l [N][6], J_s [N][12], J_o [N][12] (each may be null).  A block takes
+// kGatherRows consecutive caller indices o, reads sorted index inv[o] (o
+// itself when inv is null: SoA buffers already in caller order) from the SoA
 // buffers, stages the rows in shared memory (component-major, conflict-free)
 // and writes each array's part as one contiguous run, so that the stores
 // coalesce also when the destination is page-locked host memory.
 constexpr int kGatherRows = 128;
 template <typename T>
-__global__ void __launch_bounds__(kGatherRows) k_gather_rows(int64_t N, const int64_t* inv, VisualLin<T> v, double* r,
-                                                             double* Jl, double* Js, double* Jo) {
+__global__ void __launch_bounds__(kGatherRows) k_gather_rows(int64_t N, int64_t lo, int64_t hi, const int64_t* inv,
+                                                             VisualLin<T> v, double* r, double* Jl, double* Js,
+                                                             double* Jo) {
   __shared__ double sh[32 * kGatherRows];
-  const int64_t base = (int64_t)blockIdx.x * kGatherRows;
+  const int64_t base = lo + (int64_t)blockIdx.x * kGatherRows;
   const int t = threadIdx.x;
-  const int cnt = (int)(N - base < kGatherRows ? N - base : kGatherRows);
+  const int cnt = (int)(hi - base < kGatherRows ? hi - base : kGatherRows);
   if (t < cnt) {
-    const int64_t i = inv[base + t];
+    const int64_t i = inv ? inv[base + t] : base + t;
     if (r) for (int c = 0; c < 2; ++c) sh[c * kGatherRows + t] = (double)v.r[c * N + i];
     if (Jl) for (int c = 0; c < 6; ++c) sh[(2 + c) * kGatherRows + t] = (double)v.Jl[c * N + i];
     if (Js) for (int c = 0; c < 12; ++c) sh[(8 + c) * kGatherRows + t] = (double)v.Js[c * N + i];
@@ -1000,7 +1005,7 @@ __global__ void __launch_bounds__(kGatherRows) k_gather_rows(int64_t N, const in
 
 __global__ void k_pack_state(int64_t NK, int64_t NL, double* kf_state, double* lm_p, float* kf_pose_f, float* lm_p_f,
                              const double* kx, const double* kv, const double* kbg, const double* kba, const double* lp,
-                             int to_device) {
+                             const int32_t* lm_caller, int to_device) {
   const int64_t i = blockIdx.x * (int64_t)blockDim.x + threadIdx.x;
   if (i < NK) {
     double* x = kf_state + 16 * i;
@@ -1024,13 +1029,13 @@ __global__ void k_pack_state(int64_t NK, int64_t NL, double* kf_state, double* l
       }
     }
   } else if (i < NK + NL && lp) {
-    const int64_t l = i - NK;
+    const int64_t l = i - NK, c = lm_caller ? lm_caller[l] : l;
     for (int a = 0; a < 3; ++a) {
       if (to_device) {
-        lm_p[4 * l + a] = lp[3 * l + a];
-        lm_p_f[4 * l + a] = (float)lp[3 * l + a];
+        lm_p[4 * l + a] = lp[3 * c + a];
+        lm_p_f[4 * l + a] = (float)lp[3 * c + a];
       } else {
-        const_cast<double*>(lp)[3 * l + a] = lm_p[4 * l + a];
+        const_cast<double*>(lp)[3 * c + a] = lm_p[4 * l + a];
       }
     }
   }
@@ -1040,11 +1045,21 @@ __global__ void k_pack_state(int64_t NK, int64_t NL, double* kf_state, double* l
 template <typename T>
 cudaError_t launch_gather_visual(const DevProblem& P, const int64_t* obs_inv, VisualLin<T> v, double* r, double* Jl,
                                  double* Js, double* Jo, cudaStream_t s) {
-  if (P.nobs == 0) return cudaSuccess;
-  k_gather_rows<T><<<(unsigned)((P.nobs + kGatherRows - 1) / kGatherRows), kGatherRows, 0, s>>>(P.nobs, obs_inv, v, r,
-                                                                                                  Jl, Js, Jo);
+  return launch_gather_rows<T>(P, obs_inv, 0, P.nobs, v, r, Jl, Js, Jo, s);
+}
+
+template <typename T>
+cudaError_t launch_gather_rows(const DevProblem& P, const int64_t* inv, int64_t lo, int64_t hi, VisualLin<T> v,
+                               double* r, double* Jl, double* Js, double* Jo, cudaStream_t s) {
+  if (hi <= lo) return cudaSuccess;
+  k_gather_rows<T><<<(unsigned)((hi - lo + kGatherRows - 1) / kGatherRows), kGatherRows, 0, s>>>(P.nobs, lo, hi, inv,
+                                                                                                   v, r, Jl, Js, Jo);
   return cudaGetLastError();
 }
+template cudaError_t launch_gather_rows<double>(const DevProblem&, const int64_t*, int64_t, int64_t, VisualLin<double>,
+                                                double*, double*, double*, double*, cudaStream_t);
+template cudaError_t launch_gather_rows<float>(const DevProblem&, const int64_t*, int64_t, int64_t, VisualLin<float>,
+                                               double*, double*, double*, double*, cudaStream_t);
 template cudaError_t launch_gather_visual<double>(const DevProblem&, const int64_t*, VisualLin<double>, double*,
                                                   double*, double*, double*, cudaStream_t);
 template cudaError_t launch_gather_visual<float>(const DevProblem&, const int64_t*, VisualLin<float>, double*, double*,
@@ -1055,7 +1070,28 @@ __global__ void k_invert_perm(int64_t N, const int64_t* perm, int64_t* inv) {
   const int64_t i = blockIdx.x * (int64_t)blockDim.x + threadIdx.x;
   if (i < N) inv[perm[i]] = i;
 }
+
+// The FP64 linearization's observation fields in the caller's order.
+__global__ void k_caller_obs(DevProblem P, const int64_t* inv, CallerObs c) {
+  const int64_t o = blockIdx.x * (int64_t)blockDim.x + threadIdx.x;
+  if (o >= P.nobs) return;
+  const int64_t i = inv[o];
+  c.uv[o] = P.obs_uv[i];
+  c.sinv[o] = P.obs_sinv[i];
+  c.huber[o] = P.obs_huber[i];
+  c.lm[o] = P.obs_lm[i];
+  c.kf[o] = P.obs_kf[i];
+  c.store[o] = P.obs_store[i];
+  c.cam[o] = P.obs_cam[i];
+  c.type[o] = P.obs_type[i];
+}
 }  // namespace
+
+cudaError_t launch_caller_obs(const DevProblem& P, const int64_t* inv, CallerObs c, cudaStream_t s) {
+  if (P.nobs == 0) return cudaSuccess;
+  k_caller_obs<<<(unsigned)((P.nobs + 255) / 256), 256, 0, s>>>(P, inv, c);
+  return cudaGetLastError();
+}
 
 cudaError_t launch_landmark_quality(const DevProblem& P, const mba_landmark_quality_options& o, uint8_t* good,
                                     cudaStream_t s) {
@@ -1071,10 +1107,11 @@ cudaError_t launch_invert_perm(const DevProblem& P, int64_t* inv, cudaStream_t s
 }
 
 cudaError_t launch_pack_state(const DevProblem& P, const double* kx, const double* kv, const double* kbg,
-                              const double* kba, const double* lp, int to_device, cudaStream_t s) {
+                              const double* kba, const double* lp, const int32_t* lm_caller, int to_device,
+                              cudaStream_t s) {
   const int64_t n = P.nkf + P.nlm;
   k_pack_state<<<(unsigned)((n + 255) / 256), 256, 0, s>>>(P.nkf, P.nlm, P.kf_state, P.lm_p, P.kf_pose_f, P.lm_p_f,
-                                                            kx, kv, kbg, kba, lp, to_device);
+                                                            kx, kv, kbg, kba, lp, lm_caller, to_device);
   return cudaGetLastError();
 }
 

@@ -516,7 +516,7 @@ template <typename T>
 __global__ void __launch_bounds__(kB) k_schur_lm(SolverLaunch<T> s) {
   if (s.ctl->terminated) return;
   const int64_t l = blockIdx.x * (int64_t)blockDim.x + threadIdx.x;
-  const int64_t NL = s.P.nlm, NS = s.S.nslot;
+  const int64_t NL = s.P.nlm;
   if (l >= NL) return;
   T V[9] = {T(0), T(0), T(0), T(0), T(0), T(0), T(0), T(0), T(0)};
   if (s.P.lm_active[l]) {
@@ -540,7 +540,7 @@ __global__ void __launch_bounds__(kB) k_schur_lm(SolverLaunch<T> s) {
     for (int a = 0; a < 3; ++a) g[a] = s.L.gl[a * NL + l];
 #pragma unroll
     for (int a = 0; a < 3; ++a) Vg[a] = V[3 * a] * g[0] + V[3 * a + 1] * g[1] + V[3 * a + 2] * g[2];
-    for (int64_t si = s.S.lm_slot_off[l]; si < s.S.lm_slot_off[l + 1]; ++si) {
+    for (int64_t si = s.S.lm_slot_off[l]; si < s.S.lm_slot_end[l]; ++si) {
       const int64_t k = s.S.slot_kf[si];
       T w[18];
       load_slot(s.L.Wslot + kSlotStride * si, w);
@@ -1188,7 +1188,7 @@ __global__ void __launch_bounds__(kB) k_backsub(SolverLaunch<T> s) {
   for (int a = 0; a < 3; ++a) t[a] = -s.L.gl[a * NL + l];
   if (s.P.ng > 0)  // W_n^T x_n of the global nodes (k_border_backsub)
     for (int a = 0; a < 3; ++a) t[a] -= T(s.B.bl[a * NL + l]);
-  for (int64_t i = s.S.lm_slot_off[l]; i < s.S.lm_slot_off[l + 1]; ++i) {
+  for (int64_t i = s.S.lm_slot_off[l]; i < s.S.lm_slot_end[l]; ++i) {
     const T* xk = s.L.x + 15 * (int64_t)s.S.slot_kf[i];
     T xv[6], w[18];
 #pragma unroll

@@ -137,15 +137,21 @@ struct mba_gnn {
   GnnParams p{};
 };
 
+constexpr int kLinChunks = 8;  // chunks of the FP64 linearization into page-locked host memory
+
 struct mba_handle {
   int device = 0;
   cudaStream_t stream = nullptr;
+  cudaStream_t copy = nullptr;             // device-to-host copies overlapping the next chunk's evaluation
+  cudaEvent_t chunk_ev[kLinChunks] = {};
   DeviceArena arena;
   DevProblem P{};
   SchurPattern S{};
   std::atomic<int> cancel{0};
   // host copies used by the API
   std::vector<int64_t> perm;  // sorted -> caller observation index
+  std::vector<int32_t> lm_caller;  // internal -> caller landmark index (empty: the same)
+  int32_t* lm_caller_dev = nullptr;
   // solver state (lazily allocated)
   bool solver_ready = false;
   SolverBuffers<double> b64;
@@ -166,6 +172,7 @@ struct mba_handle {
   double* stage_state = nullptr;  // 16 NK + 3 NL
   double* stage_lin = nullptr;    // 32 N
   int64_t* obs_inv = nullptr;     // [N] caller observation index -> sorted index
+  CallerObs cobs{};               // observation fields in caller order (chunked host linearization)
   char* l2_flush = nullptr;       // buffer larger than L2 for timing hygiene
   // learned preconditioner
   GnnGraph gg{};
@@ -792,6 +799,69 @@ void* mapped_host_range(void* p, size_t bytes) {
   return a.devicePointer;
 }
 
+// FP64 rows into page-locked host memory in kLinChunks chunks of caller rows.
+// Chunk c is evaluated from caller-ordered copies of the observation fields
+// (so that its rows depend on no other chunk), transposed into the device
+// staging rows, and copied to the host by the copy engine on a second stream
+// while chunk c + 1 is evaluated.
+mba_status linearize_visual_chunked(mba_handle* h, SolverBuffers<double>& b, double* const* out) {
+  const int64_t N = h->P.nobs;
+  cudaStream_t st = h->stream;
+  cudaError_t e = cudaSuccess;
+  DeviceArena& A = h->arena;
+  if (!h->cobs.uv) {
+    CallerObs c{};
+    c.uv = A.alloc<double2>(N);
+    c.sinv = A.alloc<double>(N);
+    c.huber = A.alloc<double>(N);
+    c.lm = A.alloc<int32_t>(N);
+    c.kf = A.alloc<int32_t>(N);
+    c.store = A.alloc<int32_t>(N);
+    c.cam = A.alloc<uint8_t>(N);
+    c.type = A.alloc<uint8_t>(N);
+    if (A.err != cudaSuccess || launch_caller_obs(h->P, h->obs_inv, c, st) != cudaSuccess) return MBA_ERR_CUDA;
+    h->cobs = c;
+  }
+  if (!h->stage_lin) {
+    h->stage_lin = A.alloc<double>(32 * N);
+    if (A.err != cudaSuccess) return MBA_ERR_CUDA;
+  }
+  if (!h->copy) e = cudaStreamCreateWithFlags(&h->copy, cudaStreamNonBlocking);
+  for (int c = 0; c < kLinChunks && e == cudaSuccess; ++c)
+    if (!h->chunk_ev[c]) e = cudaEventCreateWithFlags(&h->chunk_ev[c], cudaEventDisableTiming);
+  DevProblem Pc = h->P;
+  Pc.obs_uv = h->cobs.uv;
+  Pc.obs_sinv = h->cobs.sinv;
+  Pc.obs_huber = h->cobs.huber;
+  Pc.obs_lm = h->cobs.lm;
+  Pc.obs_kf = h->cobs.kf;
+  Pc.obs_store = h->cobs.store;
+  Pc.obs_cam = h->cobs.cam;
+  Pc.obs_type = h->cobs.type;
+  const int64_t width[4] = {2, 6, 12, 12}, first[4] = {0, 2, 8, 20};
+  double* rows[4];
+  for (int a = 0; a < 4; ++a) rows[a] = out[a] ? h->stage_lin + first[a] * N : nullptr;
+  for (int c = 0; c < kLinChunks && e == cudaSuccess; ++c) {
+    const int64_t lo = N * c / kLinChunks, hi = N * (c + 1) / kLinChunks;
+    Pc.vis_lo = lo;
+    Pc.vis_hi = hi;
+    e = launch_visual_linearize<double>(Pc, b.vis, nullptr, st);
+    if (e == cudaSuccess) e = launch_gather_rows<double>(Pc, nullptr, lo, hi, b.vis, rows[0], rows[1], rows[2], rows[3], st);
+    if (e == cudaSuccess) e = cudaEventRecord(h->chunk_ev[c], st);
+    if (e == cudaSuccess) e = cudaStreamWaitEvent(h->copy, h->chunk_ev[c], 0);
+    for (int a = 0; a < 4 && e == cudaSuccess; ++a)
+      if (out[a])
+        e = cudaMemcpyAsync(out[a] + width[a] * lo, rows[a] + width[a] * lo, sizeof(double) * width[a] * (hi - lo),
+                            cudaMemcpyDeviceToHost, h->copy);
+  }
+  if (h->copy) {
+    const cudaError_t e2 = cudaStreamSynchronize(h->copy);
+    if (e == cudaSuccess) e = e2;
+  }
+  if (e == cudaSuccess) e = cudaStreamSynchronize(st);
+  return cuda_status(e);
+}
+
 template <typename T>
 mba_status linearize_visual_host(mba_handle* h, double* r, double* Jl, double* Js, double* Jo) {
   SolverBuffers<T>& b = buffers_of<T>(h);
@@ -815,6 +885,8 @@ mba_status linearize_visual_host(mba_handle* h, double* r, double* Jl, double* J
     mapped[a] = static_cast<double*>(mapped_host_range(out[a], sizeof(double) * width[a] * N));
     direct = direct && mapped[a];
   }
+  if constexpr (sizeof(T) == 8)
+    if (direct && N >= 4096 * kLinChunks) return linearize_visual_chunked(h, b, out);
   cudaError_t e = launch_visual_linearize<T>(h->P, b.vis, nullptr, st);
   if (direct) {
     if (e == cudaSuccess) e = launch_gather_visual<T>(h->P, h->obs_inv, b.vis, mapped[0], mapped[1], mapped[2], mapped[3], st);
@@ -1037,6 +1109,74 @@ mba_status mba_create(const mba_problem_desc* d, int32_t device, mba_handle** ou
   }
   cudaStream_t st = h->stream;
 
+  // ---- internal landmark numbering.  by_kf lists the landmarks by store
+  // keyframe (longer tracks first within one keyframe).  The internal order
+  // takes them round robin: the first landmark of every keyframe in keyframe
+  // order, then the second, and so on.  Neighbouring landmarks then belong to
+  // different store keyframes, so the atomics of neighbouring lanes of the
+  // landmark assembly seldom meet on one block, while observations (sorted by
+  // internal landmark below) stay contiguous per lane.  The slots are
+  // numbered in by_kf order instead, so that the partner rows a Schur target
+  // gathers lie close together.  The state, rejection and quality entry
+  // points translate to the caller's numbering (h->lm_caller: internal ->
+  // caller index).
+  mba_problem_desc dint;
+  std::vector<int32_t> lm_rank, int_store, int_obs_lm, slot_order(NL);
+  std::vector<double> int_lm_p;
+  std::vector<uint8_t> int_lm_const;
+  {
+    std::vector<int64_t> cnt(NL, 0), end(NK + 1, 0);
+    for (int64_t i = 0; i < N; ++i) cnt[d->obs_landmark[i]]++;
+    for (int64_t l = 0; l < NL; ++l) end[d->lm_store_keyframe[l] + 1]++;
+    int64_t most = 0;
+    for (int64_t k = 0; k < NK; ++k) {
+      most = std::max(most, end[k + 1]);
+      end[k + 1] += end[k];
+    }
+    std::vector<int32_t> by_kf(NL);
+    std::vector<int64_t> fill(end.begin(), end.end() - 1);
+    for (int64_t l = 0; l < NL; ++l) by_kf[fill[d->lm_store_keyframe[l]]++] = (int32_t)l;
+    for (int64_t k = 0; k < NK; ++k)
+      std::stable_sort(by_kf.begin() + end[k], by_kf.begin() + end[k + 1],
+                       [&](int32_t x, int32_t y) { return cnt[x] > cnt[y]; });
+    // round robin = stable counting sort of by_kf by the rank within its keyframe
+    std::vector<int64_t> at(most + 1, 0);
+    for (int64_t k = 0; k < NK; ++k)
+      for (int64_t q = end[k]; q < end[k + 1]; ++q) at[q - end[k] + 1]++;
+    for (int64_t r = 0; r < most; ++r) at[r + 1] += at[r];
+    h->lm_caller.resize(NL);
+    for (int64_t k = 0; k < NK; ++k)
+      for (int64_t q = end[k]; q < end[k + 1]; ++q) h->lm_caller[at[q - end[k]]++] = by_kf[q];
+    lm_rank.resize(NL);
+    for (int64_t l = 0; l < NL; ++l) lm_rank[h->lm_caller[l]] = (int32_t)l;
+    for (int64_t q = 0; q < NL; ++q) slot_order[q] = lm_rank[by_kf[q]];
+    bool identity = true;
+    for (int64_t l = 0; l < NL && identity; ++l) identity = h->lm_caller[l] == l;
+    if (identity) {
+      h->lm_caller.clear();
+    } else {
+      int_store.resize(NL);
+      int_lm_p.resize(3 * NL);
+      for (int64_t l = 0; l < NL; ++l) {
+        const int32_t c = h->lm_caller[l];
+        int_store[l] = d->lm_store_keyframe[c];
+        for (int a = 0; a < 3; ++a) int_lm_p[3 * l + a] = d->lm_p_B[3 * c + a];
+      }
+      if (d->lm_constant) {
+        int_lm_const.resize(NL);
+        for (int64_t l = 0; l < NL; ++l) int_lm_const[l] = d->lm_constant[h->lm_caller[l]];
+      }
+      int_obs_lm.resize(N);
+      for (int64_t i = 0; i < N; ++i) int_obs_lm[i] = lm_rank[d->obs_landmark[i]];
+      dint = *d;
+      dint.lm_store_keyframe = int_store.data();
+      dint.lm_p_B = int_lm_p.data();
+      dint.lm_constant = d->lm_constant ? int_lm_const.data() : nullptr;
+      dint.obs_landmark = int_obs_lm.data();
+      d = &dint;
+    }
+  }
+
   // ---- observation types and landmark-sorted order
   std::vector<uint8_t> type(N);
   for (int64_t i = 0; i < N; ++i) {
@@ -1095,12 +1235,13 @@ mba_status mba_create(const mba_problem_desc* d, int32_t device, mba_handle** ou
     if ((d->lm_constant && d->lm_constant[l]) || off[l + 1] == off[l]) lm_active[l] = 0;
 
   // ---- Schur pattern
-  std::vector<int64_t> slot_off(NL + 1, 0);
+  std::vector<int64_t> slot_off(NL, 0), slot_end(NL, 0);
   std::vector<int32_t> slot_kf, slot_lm, obs_slot(N, -1), obs_pblk(N, -1);
   slot_kf.reserve(NL + N);
   slot_lm.reserve(NL + N);
   int64_t npair_est = 0;
-  for (int64_t l = 0; l < NL; ++l) {
+  for (int64_t q = 0; q < NL; ++q) {
+    const int64_t l = slot_order[q];
     slot_off[l] = (int64_t)slot_kf.size();
     slot_kf.push_back(d->lm_store_keyframe[l]);
     slot_lm.push_back((int32_t)l);
@@ -1110,10 +1251,10 @@ mba_status mba_create(const mba_problem_desc* d, int32_t device, mba_handle** ou
       slot_kf.push_back(okf[s]);
       slot_lm.push_back((int32_t)l);
     }
-    const int64_t m = (int64_t)slot_kf.size() - slot_off[l];
+    slot_end[l] = (int64_t)slot_kf.size();
+    const int64_t m = slot_end[l] - slot_off[l];
     if (lm_active[l]) npair_est += m * (m + 1) / 2;
   }
-  slot_off[NL] = (int64_t)slot_kf.size();
   PairMap pm(std::max<int64_t>(1024, N + NE));
   for (int64_t s = 0; s < N; ++s)
     if (otype[s] != MBA_LOCAL_KEYFRAME) obs_pblk[s] = pm.get(ost[s], okf[s]);
@@ -1137,8 +1278,8 @@ mba_status mba_create(const mba_problem_desc* d, int32_t device, mba_handle** ou
     ta.reserve(npair_est); tb.reserve(npair_est); tt.reserve(npair_est);
     for (int64_t l = 0; l < NL; ++l) {
       if (!lm_active[l]) continue;
-      for (int64_t x = slot_off[l]; x < slot_off[l + 1]; ++x)
-        for (int64_t y = x; y < slot_off[l + 1]; ++y) {
+      for (int64_t x = slot_off[l]; x < slot_end[l]; ++x)
+        for (int64_t y = x; y < slot_end[l]; ++y) {
           const int32_t kx = slot_kf[x], ky = slot_kf[y];
           if (kx == ky) {
             ta.push_back((int32_t)x); tb.push_back((int32_t)y); tt.push_back(kx);
@@ -1392,6 +1533,7 @@ mba_status mba_create(const mba_problem_desc* d, int32_t device, mba_handle** ou
   P.lm_active = A.upload(lm_active, st);
   P.lm_off = A.alloc<int32_t>(NL);
   if (NL && P.lm_off) cudaMemsetAsync(P.lm_off, 0, sizeof(int32_t) * NL, st);
+  if (!h->lm_caller.empty()) h->lm_caller_dev = A.upload(h->lm_caller, st);
   P.kf_state = A.upload(kf_state, st);
   P.kf_rot = A.alloc<double>(16 * NK + 16);
   P.kf_mis = A.upload(kfm, st);
@@ -1464,6 +1606,7 @@ mba_status mba_create(const mba_problem_desc* d, int32_t device, mba_handle** ou
   S.npu = npu;
   S.npair = (int64_t)prb.size();
   S.lm_slot_off = A.upload(slot_off, st);
+  S.lm_slot_end = A.upload(slot_end, st);
   S.slot_kf = A.upload(slot_kf, st);
   S.slot_lm = A.upload(slot_lm, st);
   S.obs_slot = A.upload(obs_slot, st);
@@ -1524,8 +1667,12 @@ void mba_destroy(mba_handle* h) {
   if (!h) return;
   cudaSetDevice(h->device);
   if (h->stream) cudaStreamSynchronize(h->stream);
+  if (h->copy) cudaStreamSynchronize(h->copy);
   h->arena.release();
   if (h->cancel_host) cudaFreeHost((void*)h->cancel_host);
+  for (cudaEvent_t& ev : h->chunk_ev)
+    if (ev) cudaEventDestroy(ev);
+  if (h->copy) cudaStreamDestroy(h->copy);
   if (h->stream) cudaStreamDestroy(h->stream);
   delete h;
 }
@@ -1726,10 +1873,14 @@ mba_status mba_landmark_quality(mba_handle* h, const mba_landmark_quality_option
   DeviceArena tmp;
   uint8_t* d = tmp.alloc<uint8_t>(NL);
   cudaError_t e = tmp.err;
+  std::vector<uint8_t> good(h->lm_caller.empty() ? 0 : NL);
+  uint8_t* host = h->lm_caller.empty() ? well_constrained : good.data();
   if (e == cudaSuccess) e = launch_landmark_quality(h->P, *o, d, h->stream);
-  if (e == cudaSuccess) e = cudaMemcpyAsync(well_constrained, d, NL, cudaMemcpyDeviceToHost, h->stream);
+  if (e == cudaSuccess) e = cudaMemcpyAsync(host, d, NL, cudaMemcpyDeviceToHost, h->stream);
   if (e == cudaSuccess) e = cudaStreamSynchronize(h->stream);
   tmp.release();
+  if (e == cudaSuccess && !h->lm_caller.empty())
+    for (int64_t l = 0; l < NL; ++l) well_constrained[h->lm_caller[l]] = good[l];
   return e == cudaSuccess ? MBA_OK : MBA_ERR_CUDA;
 }
 
@@ -1846,7 +1997,7 @@ mba_status mba_read_state(mba_handle* h, double* kx, double* kv, double* kbg, do
   double* sl = sa + 3 * NK;
   cudaStream_t st = h->stream;
   cudaError_t e = launch_pack_state(h->P, kx ? sx : nullptr, kv ? sv : nullptr, kbg ? sg : nullptr,
-                                    kba ? sa : nullptr, lp ? sl : nullptr, 0, st);
+                                    kba ? sa : nullptr, lp ? sl : nullptr, h->lm_caller_dev, 0, st);
   if (e == cudaSuccess && kx) e = cudaMemcpyAsync(kx, sx, sizeof(double) * 7 * NK, cudaMemcpyDeviceToHost, st);
   if (e == cudaSuccess && kv) e = cudaMemcpyAsync(kv, sv, sizeof(double) * 3 * NK, cudaMemcpyDeviceToHost, st);
   if (e == cudaSuccess && kbg) e = cudaMemcpyAsync(kbg, sg, sizeof(double) * 3 * NK, cudaMemcpyDeviceToHost, st);
@@ -1879,7 +2030,7 @@ mba_status mba_write_state(mba_handle* h, const double* kx, const double* kv, co
   if (e == cudaSuccess && lp && NL) e = cudaMemcpyAsync(sl, lp, sizeof(double) * 3 * NL, cudaMemcpyHostToDevice, st);
   if (e == cudaSuccess)
     e = launch_pack_state(h->P, kx ? sx : nullptr, kv ? sv : nullptr, kbg ? sg : nullptr, kba ? sa : nullptr,
-                          (lp && NL) ? sl : nullptr, 1, st);
+                          (lp && NL) ? sl : nullptr, h->lm_caller_dev, 1, st);
   if (e == cudaSuccess) e = cudaStreamSynchronize(st);
   return cuda_status(e);
 }
@@ -2036,7 +2187,7 @@ mba_status mba_rejected_landmarks(mba_handle* h, uint8_t* flags, int64_t* count)
   int64_t c = 0;
   for (int64_t l = 0; l < NL; ++l) {
     c += off[l] != 0;
-    if (flags) flags[l] = off[l] != 0;
+    if (flags) flags[h->lm_caller.empty() ? l : h->lm_caller[l]] = off[l] != 0;
   }
   if (count) *count = c;
   return MBA_OK;

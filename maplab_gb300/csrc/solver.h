@@ -22,7 +22,8 @@ struct SchurPattern {
   int64_t nslot = 0;      // landmark slots: slot 0 = store keyframe, then one per non-keyframe observation
   int64_t npu = 0;        // upper (i < j) pose-pose 6x6 blocks
   int64_t npair = 0;      // Schur slot pairs (a <= b) within a landmark
-  int64_t* lm_slot_off;   // [nlm+1]
+  int64_t* lm_slot_off;   // [nlm] first slot of each landmark (slots are numbered by store keyframe)
+  int64_t* lm_slot_end;   // [nlm] one past its last slot
   int32_t* slot_kf;       // [nslot]
   int32_t* slot_lm;       // [nslot]
   int32_t* obs_slot;      // [nobs] slot of the observer, -1 for kLocalKeyframe

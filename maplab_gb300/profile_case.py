@@ -42,11 +42,12 @@ def main():
     with ba.BundleAdjuster(m.desc) as g:
         if a.block or a.min_blocks:
             g.set_tuning(visual_block=a.block, visual_min_blocks=a.min_blocks)
-        if a.schur_split or a.pcg_product or a.chain_segment:
-            g.set_tuning(schur_split=a.schur_split, pcg_product=a.pcg_product, chain_segment=a.chain_segment)
         prec = N.MBA_PRECISION_MIXED if a.precision == "mixed" else N.MBA_PRECISION_FP64
         if a.autotune:
             print(json.dumps({"tuning": g.autotune(prec)}))
+        # explicit settings override the autotuner's choice
+        if a.schur_split or a.pcg_product or a.chain_segment:
+            g.set_tuning(schur_split=a.schur_split, pcg_product=a.pcg_product, chain_segment=a.chain_segment)
         if a.what == "visual":
             ms = g.time_visual_kernel(mode=1 if prec == N.MBA_PRECISION_MIXED else 0, iters=a.launches)
             print(json.dumps({"visual_ms_per_launch": ms, "observations": m.desc.num_observations}))

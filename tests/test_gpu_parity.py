@@ -137,6 +137,38 @@ def test_linearize_visual_into_pinned_host_memory(multi, precision):
         np.testing.assert_array_equal(sub[2].numpy(), ref[2])
 
 
+def test_linearize_visual_chunked_into_pinned_host_memory():
+    """FP64 rows into page-locked memory for a map of 32,768 observations or
+    more go in eight chunks evaluated from caller-ordered copies of the
+    observations, each chunk copied out while the next is evaluated.  The
+    rows equal the single-pass rows into pageable memory bit for bit, also
+    with outputs omitted and after the state has changed."""
+    import ctypes
+    import torch
+    m = synth.generate("c2", keyframes_per_mission=200, num_landmarks=20000)
+    n = m.desc.num_observations
+    assert n >= 8 * 4096
+    P = lambda t: ctypes.cast(t.data_ptr(), N.c_double_p) if t is not None else None
+    with ba.BundleAdjuster(m.desc) as g:
+        for step in range(2):
+            ref = g.linearize_visual(N.MBA_PRECISION_FP64)
+            pinned = [torch.full((n, c), np.nan, dtype=torch.float64).pin_memory() for c in (2, 6, 12, 12)]
+            assert ba.lib().mba_linearize_visual(g.handle, N.MBA_PRECISION_FP64, *[P(t) for t in pinned]) == 0
+            for a, b in zip(pinned, ref):
+                np.testing.assert_array_equal(a.numpy(), b)
+            sub = [None, pinned[1], None, pinned[3]]
+            for t in sub:
+                if t is not None:
+                    t.fill_(np.nan)
+            assert ba.lib().mba_linearize_visual(g.handle, N.MBA_PRECISION_FP64, *[P(t) for t in sub]) == 0
+            np.testing.assert_array_equal(sub[1].numpy(), ref[1])
+            np.testing.assert_array_equal(sub[3].numpy(), ref[3])
+            if step == 0:
+                o = N.default_solver_options()
+                o.max_num_iterations = 2
+                g.solve(o)
+
+
 @pytest.mark.parametrize("pipelined, min_blocks, block", [(2, 1, 256), (2, 3, 64), (1, 1, 128), (1, 2, 256), (1, 2, 64)])
 def test_evaluation_kernel_variants_agree(multi, pipelined, min_blocks, block):
     """The pipelined persistent loop and the register-capped variants run the
