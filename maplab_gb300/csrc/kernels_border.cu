@@ -370,7 +370,7 @@ __global__ void __launch_bounds__(64) k_border_schur(SolverLaunch<double> s) {
     }
     for (int64_t sl = s.S.lm_slot_off[l]; sl < s.S.lm_slot_end[l]; ++sl) {
       const int64_t k = s.S.slot_kf[sl];
-      const double* U = s.L.U + kSlotStride * sl;  // V W_slot, 3 x 6
+      const double* U = s.L.U + kSlotStride * (int64_t)s.S.w_u[sl];  // V W_slot, 3 x 6
       double* blk = s.B.BS + 90 * (G * k + ids[b]);
       for (int r = 0; r < 6; ++r)
         for (int c = 0; c < 15; ++c) {

@@ -555,16 +555,17 @@ __global__ void __launch_bounds__(kB) k_schur_lm(SolverLaunch<T> s) {
   for (int a = 0; a < 9; ++a) s.L.V[a * NL + l] = V[a];
 }
 
-// Landmark elimination, part 2: U = V W per slot.
+// Landmark elimination, part 2: U = V W per slot, one thread per U row (U
+// rows are numbered by store keyframe, W rows by landmark: S.u_w maps).
 template <typename T>
 __global__ void __launch_bounds__(kB) k_schur_slot(SolverLaunch<T> s) {
   if (s.ctl->terminated) return;
   const int64_t i = blockIdx.x * (int64_t)blockDim.x + threadIdx.x;
   const int64_t NS = s.S.nslot, NL = s.P.nlm;
   if (i >= NS) return;
-  const int64_t l = s.S.slot_lm[i];
+  const int64_t w = s.S.u_w[i], l = s.S.slot_lm[w];
   T W[18], V[9];
-  load_slot(s.L.Wslot + kSlotStride * i, W);
+  load_slot(s.L.Wslot + kSlotStride * w, W);
 #pragma unroll
   for (int a = 0; a < 9; ++a) V[a] = s.L.V[a * NL + l];
   T U[18];
@@ -574,6 +575,9 @@ __global__ void __launch_bounds__(kB) k_schur_slot(SolverLaunch<T> s) {
     for (int c = 0; c < 6; ++c) U[6 * x + c] = V[3 * x] * W[c] + V[3 * x + 1] * W[6 + c] + V[3 * x + 2] * W[12 + c];
   store_slot(s.L.U + kSlotStride * i, U);
 }
+
+// U row of a pair's b (bitwise-not when b is a itself).
+__device__ __forceinline__ int64_t pair_u(int y) { return y < 0 ? ~y : y; }
 
 // Landmark elimination, part 3: S(k_a, k_b) -= W_a^T U_b for every slot pair.
 // Pairs are sorted by target block; one thread sums a chunk of one target's
@@ -614,14 +618,14 @@ __global__ void __launch_bounds__(kB, sizeof(T) == 4 ? 2 : 1) k_schur_pairs(Solv
     int2 abn = p0 + 1 < p1 ? s.S.pair_rb[p0 + 1] : ab;  // pair indices run one step ahead of the rows
     T Wa[18], Ub[18];
     load_slot(wrow(ab.x), Wa);
-    load_slot(s.L.U + kSlotStride * (int64_t)ab.y, Ub);
+    load_slot(s.L.U + kSlotStride * pair_u(ab.y), Ub);
     for (int64_t p = p0; p < p1; ++p) {
-      const bool sym = diag && s.S.kf_slot[s0 + ab.x] != ab.y;
+      const bool sym = diag && ab.y >= 0;  // a != b
       T Wn[18], Un[18];
       const int2 abnn = p + 2 < p1 ? s.S.pair_rb[p + 2] : abn;
       if (p + 1 < p1) {
         load_slot(wrow(abn.x), Wn);
-        load_slot(s.L.U + kSlotStride * (int64_t)abn.y, Un);
+        load_slot(s.L.U + kSlotStride * pair_u(abn.y), Un);
       }
 #pragma unroll
       for (int r = 0; r < 6; ++r)
@@ -712,19 +716,19 @@ __global__ void __launch_bounds__(kB, sizeof(T) == 4 ? 3 : 1) k_schur_pairs_spli
     int2 abn = p0 + 1 < p1 ? s.S.pair_rb[p0 + 1] : ab;  // pair indices run one step ahead of the rows
     T Ub[9];  // U_b rows 0..2, columns 3h..3h+2
     {
-      const T* u = s.L.U + kSlotStride * (int64_t)ab.y + 3 * h;
+      const T* u = s.L.U + kSlotStride * pair_u(ab.y) + 3 * h;
 #pragma unroll
       for (int k = 0; k < 3; ++k)
 #pragma unroll
         for (int qq = 0; qq < 3; ++qq) Ub[3 * k + qq] = u[6 * k + qq];
     }
     for (int64_t p = p0; p < p1; ++p) {
-      const bool sym = diag && s.S.kf_slot[s0 + ab.x] != ab.y;
+      const bool sym = diag && ab.y >= 0;  // a != b
       const T* wa = staged ? sW + kSlotStride * (int64_t)ab.x : s.L.Wslot + kSlotStride * (int64_t)s.S.kf_slot[s0 + ab.x];
       T Un[9];
       const int2 abnn = p + 2 < p1 ? s.S.pair_rb[p + 2] : abn;
       if (p + 1 < p1) {
-        const T* u = s.L.U + kSlotStride * (int64_t)abn.y + 3 * h;
+        const T* u = s.L.U + kSlotStride * pair_u(abn.y) + 3 * h;
 #pragma unroll
         for (int k = 0; k < 3; ++k)
 #pragma unroll

@@ -1115,9 +1115,9 @@ mba_status mba_create(const mba_problem_desc* d, int32_t device, mba_handle** ou
   // order, then the second, and so on.  Neighbouring landmarks then belong to
   // different store keyframes, so the atomics of neighbouring lanes of the
   // landmark assembly seldom meet on one block, while observations (sorted by
-  // internal landmark below) stay contiguous per lane.  The slots are
-  // numbered in by_kf order instead, so that the partner rows a Schur target
-  // gathers lie close together.  The state, rejection and quality entry
+  // internal landmark below) stay contiguous per lane.  The U rows of the
+  // slots are numbered in by_kf order instead, so that the partner rows a
+  // Schur target gathers lie close together.  The state, rejection and quality entry
   // points translate to the caller's numbering (h->lm_caller: internal ->
   // caller index).
   mba_problem_desc dint;
@@ -1240,8 +1240,7 @@ mba_status mba_create(const mba_problem_desc* d, int32_t device, mba_handle** ou
   slot_kf.reserve(NL + N);
   slot_lm.reserve(NL + N);
   int64_t npair_est = 0;
-  for (int64_t q = 0; q < NL; ++q) {
-    const int64_t l = slot_order[q];
+  for (int64_t l = 0; l < NL; ++l) {
     slot_off[l] = (int64_t)slot_kf.size();
     slot_kf.push_back(d->lm_store_keyframe[l]);
     slot_lm.push_back((int32_t)l);
@@ -1254,6 +1253,18 @@ mba_status mba_create(const mba_problem_desc* d, int32_t device, mba_handle** ou
     slot_end[l] = (int64_t)slot_kf.size();
     const int64_t m = slot_end[l] - slot_off[l];
     if (lm_active[l]) npair_est += m * (m + 1) / 2;
+  }
+  // U rows: the slots again, numbered by store keyframe (slot_order).
+  std::vector<int32_t> w_u(slot_kf.size()), u_w(slot_kf.size());
+  {
+    int32_t u = 0;
+    for (int64_t q = 0; q < NL; ++q) {
+      const int64_t l = slot_order[q];
+      for (int64_t x = slot_off[l]; x < slot_end[l]; ++x) {
+        w_u[x] = u;
+        u_w[u++] = (int32_t)x;
+      }
+    }
   }
   PairMap pm(std::max<int64_t>(1024, N + NE));
   for (int64_t s = 0; s < N; ++s)
@@ -1326,7 +1337,7 @@ mba_status mba_create(const mba_problem_desc* d, int32_t device, mba_handle** ou
       std::vector<int64_t> fill(cnt.begin(), cnt.end() - 1);
       for (int64_t q = 0; q < np; ++q) {
         const int64_t dst = fill[rank[tt[q]]]++;
-        prb[dst] = make_int2(kpos[ta[q]], tb[q]);
+        prb[dst] = make_int2(kpos[ta[q]], ta[q] == tb[q] ? ~w_u[tb[q]] : w_u[tb[q]]);
       }
     }
     tgt_row.resize(ntgt);
@@ -1607,6 +1618,8 @@ mba_status mba_create(const mba_problem_desc* d, int32_t device, mba_handle** ou
   S.npair = (int64_t)prb.size();
   S.lm_slot_off = A.upload(slot_off, st);
   S.lm_slot_end = A.upload(slot_end, st);
+  S.w_u = A.upload(w_u, st);
+  S.u_w = A.upload(u_w, st);
   S.slot_kf = A.upload(slot_kf, st);
   S.slot_lm = A.upload(slot_lm, st);
   S.obs_slot = A.upload(obs_slot, st);

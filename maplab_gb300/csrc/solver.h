@@ -22,15 +22,17 @@ struct SchurPattern {
   int64_t nslot = 0;      // landmark slots: slot 0 = store keyframe, then one per non-keyframe observation
   int64_t npu = 0;        // upper (i < j) pose-pose 6x6 blocks
   int64_t npair = 0;      // Schur slot pairs (a <= b) within a landmark
-  int64_t* lm_slot_off;   // [nlm] first slot of each landmark (slots are numbered by store keyframe)
-  int64_t* lm_slot_end;   // [nlm] one past its last slot
+  int64_t* lm_slot_off;   // [nlm] first W slot of each landmark (W rows numbered by landmark)
+  int64_t* lm_slot_end;   // [nlm] one past its last W slot
+  int32_t* w_u;           // [nslot] U row of each W slot (U rows numbered by store keyframe)
+  int32_t* u_w;           // [nslot] W slot of each U row
   int32_t* slot_kf;       // [nslot]
   int32_t* slot_lm;       // [nslot]
   int32_t* obs_slot;      // [nobs] slot of the observer, -1 for kLocalKeyframe
   int32_t* obs_pblk;      // [nobs] upper block of (store, observer), -1 for kLocalKeyframe
   int64_t nchunk = 0;     // pair chunks (contiguous pair ranges of one target)
-  int2* pair_rb;          // [npair] (a as position in its row's slot list, b global slot), sorted by target;
-                          //   slot_kf[a] <= slot_kf[b]
+  int2* pair_rb;          // [npair] (a as position in its row's W slot list, b as U row, bitwise-not
+                          //   of it when b is a itself), sorted by target; slot_kf[a] <= slot_kf[b]
   int64_t* kf_slot_off;   // [nkf+1] keyframe-major slot lists (a row's W slots are staged from them)
   int32_t* kf_slot;       // [nslot]
   int64_t max_row_slots = 0;
