@@ -1109,17 +1109,21 @@ mba_status mba_create(const mba_problem_desc* d, int32_t device, mba_handle** ou
   }
   cudaStream_t st = h->stream;
 
-  // ---- internal landmark numbering.  by_kf lists the landmarks by store
-  // keyframe (longer tracks first within one keyframe).  The internal order
-  // takes them round robin: the first landmark of every keyframe in keyframe
-  // order, then the second, and so on.  Neighbouring landmarks then belong to
-  // different store keyframes, so the atomics of neighbouring lanes of the
-  // landmark assembly seldom meet on one block, while observations (sorted by
-  // internal landmark below) stay contiguous per lane.  The U rows of the
-  // slots are numbered in by_kf order instead, so that the partner rows a
-  // Schur target gathers lie close together.  The state, rejection and quality entry
-  // points translate to the caller's numbering (h->lm_caller: internal ->
-  // caller index).
+  // ---- internal landmark numbering.  Internal landmark i is the caller's
+  // landmark (i * A) mod N_lm, A coprime to N_lm and near 0.618 N_lm: a
+  // scattering permutation, so that neighbouring landmarks (neighbouring
+  // lanes of the landmark kernels) come from unrelated parts of the map
+  // whatever the caller's order (a map's vertices hold their landmarks, so a
+  // caller may well list them by store keyframe).  Lanes on landmarks of one
+  // store keyframe add into the same blocks at the same time (their atomics
+  // serialize); with neighbours on consecutive store keyframes the assembly
+  // read five times more from DRAM.  Observations are sorted by internal
+  // landmark below, contiguous per lane.  The slots' U
+  // rows are numbered by store keyframe (slot_order: internal landmarks by
+  // store keyframe, longer tracks first), so that the partner rows a Schur
+  // target gathers lie close together.  The state, rejection and quality
+  // entry points translate to the caller's numbering (h->lm_caller:
+  // internal -> caller index).
   mba_problem_desc dint;
   std::vector<int32_t> lm_rank, int_store, int_obs_lm, slot_order(NL);
   std::vector<double> int_lm_p;
@@ -1128,25 +1132,17 @@ mba_status mba_create(const mba_problem_desc* d, int32_t device, mba_handle** ou
     std::vector<int64_t> cnt(NL, 0), end(NK + 1, 0);
     for (int64_t i = 0; i < N; ++i) cnt[d->obs_landmark[i]]++;
     for (int64_t l = 0; l < NL; ++l) end[d->lm_store_keyframe[l] + 1]++;
-    int64_t most = 0;
-    for (int64_t k = 0; k < NK; ++k) {
-      most = std::max(most, end[k + 1]);
-      end[k + 1] += end[k];
-    }
+    for (int64_t k = 0; k < NK; ++k) end[k + 1] += end[k];
     std::vector<int32_t> by_kf(NL);
     std::vector<int64_t> fill(end.begin(), end.end() - 1);
     for (int64_t l = 0; l < NL; ++l) by_kf[fill[d->lm_store_keyframe[l]]++] = (int32_t)l;
     for (int64_t k = 0; k < NK; ++k)
       std::stable_sort(by_kf.begin() + end[k], by_kf.begin() + end[k + 1],
                        [&](int32_t x, int32_t y) { return cnt[x] > cnt[y]; });
-    // round robin = stable counting sort of by_kf by the rank within its keyframe
-    std::vector<int64_t> at(most + 1, 0);
-    for (int64_t k = 0; k < NK; ++k)
-      for (int64_t q = end[k]; q < end[k + 1]; ++q) at[q - end[k] + 1]++;
-    for (int64_t r = 0; r < most; ++r) at[r + 1] += at[r];
+    int64_t A = std::max<int64_t>(1, (int64_t)(0.6180339887498949 * (double)NL));
+    while (std::gcd(A, std::max<int64_t>(NL, 1)) != 1) ++A;
     h->lm_caller.resize(NL);
-    for (int64_t k = 0; k < NK; ++k)
-      for (int64_t q = end[k]; q < end[k + 1]; ++q) h->lm_caller[at[q - end[k]]++] = by_kf[q];
+    for (int64_t l = 0; l < NL; ++l) h->lm_caller[l] = (int32_t)((l * A) % NL);
     lm_rank.resize(NL);
     for (int64_t l = 0; l < NL; ++l) lm_rank[h->lm_caller[l]] = (int32_t)l;
     for (int64_t q = 0; q < NL; ++q) slot_order[q] = lm_rank[by_kf[q]];
