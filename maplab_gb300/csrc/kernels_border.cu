@@ -51,13 +51,6 @@ __device__ __forceinline__ void block_add_b(double v, double* acc) {
 inline unsigned nblk(int64_t n, int b) { return (unsigned)((n + b - 1) / b); }
 inline unsigned gridcap(int64_t n) { return (unsigned)(n <= 0 ? 1 : (n + kB - 1) / kB > 4096 ? 4096 : (n + kB - 1) / kB); }
 
-// x (2x3) * R^T -> rows of x times R^T: out = x R^T.  (helpers on 2 x 3 row-major)
-__device__ __forceinline__ void mul23_33t(const double* x, const M3<double>& R, double* out) {
-  for (int r = 0; r < 2; ++r)
-    for (int c = 0; c < 3; ++c)
-      out[3 * r + c] = x[3 * r] * R.m[3 * c] + x[3 * r + 1] * R.m[3 * c + 1] + x[3 * r + 2] * R.m[3 * c + 2];
-}
-
 // Tangent rows (2 x k) of an ambient quaternion block A_q * 4 Jq(q)^T (the
 // error term's lift), times the parameterization Jacobian: P = Jq (4 x 3)
 // for JplQuaternionParameterization, the yaw column (4 x 1) for

@@ -416,7 +416,7 @@ template <typename T>
 __global__ void __launch_bounds__(kB) k_scale_inplace(DevProblem P, SchurPattern S, LinearSystem<T> L,
                                                       const int* run_if, const int* skip_if) {
   if (gated(run_if, skip_if)) return;
-  const int64_t NL = P.nlm, NS = S.nslot, NK = P.nkf, NE = P.nedge, NPU = S.npu;
+  const int64_t NL = P.nlm, NK = P.nkf, NE = P.nedge, NPU = S.npu;
   const int64_t n1 = 9 * NL, n2 = n1 + 3 * NL, n3 = n2 /* W slots: k_scale_slots */, n4 = n3 + 225 * NK, n5 = n4 + 36 * NPU,
                 n6 = n5 + 225 * NE, n7 = n6 + 15 * NK, n8 = n7 + 2 * P.nsw, n9 = n8 + 30 * P.nsw;
   for (int64_t i = blockIdx.x * (int64_t)blockDim.x + threadIdx.x; i < n9; i += (int64_t)gridDim.x * blockDim.x) {

@@ -778,14 +778,6 @@ mba_status chain_apply_host(mba_handle* h, double radius, const double* r, doubl
   return failed ? MBA_ERR_NOT_SPD : MBA_OK;
 }
 
-void unpermute_soa(const std::vector<double>& sorted_soa, int64_t N, int comps, const std::vector<int64_t>& perm,
-                   double* out) {
-  for (int64_t i = 0; i < N; ++i) {
-    const int64_t o = perm[i];
-    for (int c = 0; c < comps; ++c) out[comps * o + c] = sorted_soa[(size_t)c * N + i];
-  }
-}
-
 // Device address of a page-locked host range [p, p + bytes) of one mapping,
 // or null (pageable or unknown memory, or a range that leaves the mapping).
 void* mapped_host_range(void* p, size_t bytes) {
