@@ -112,6 +112,7 @@ def main(root):
         json.dump(out, f, indent=1)
     print("wrote", os.path.join(here, "imu_integrator.json"))
     sensor_files(root, here)
+    pose_extrinsics_scenarios(root, here)
     sys.path.insert(0, here)
     import error_term_scenarios
     with open(os.path.join(here, "error_term_scenarios.json"), "w") as f:
@@ -133,6 +134,115 @@ def sensor_files(root, here):
     with open(os.path.join(here, "reference_sensors.json"), "w") as f:
         json.dump(out, f, indent=1)
     print("wrote", os.path.join(here, "reference_sensors.json"))
+
+
+# The relative pose term with extrinsics (SixDoFBlockPoseErrorTermWithExtrinsics,
+# the odometry term of the optimization builder) has its own unit test; its
+# enabled cases are read here: the fixture's SetUp values and, per test, the
+# measurement, the blocks held constant and the asserted outcomes.
+POSE_EXTRINSICS_TEST = "algorithms/ceres-error-terms/test/test_six_dof_block_transformation_error_term_with_extrinsics.cc"
+
+
+def _eval_list(expr):
+    """Comma-separated numeric expressions of a comma initializer: numbers,
+    + - * / and sqrt(...), nothing else."""
+    import ast
+
+    def ev(n):
+        if isinstance(n, ast.Constant) and isinstance(n.value, (int, float)):
+            return float(n.value)
+        if isinstance(n, ast.UnaryOp) and isinstance(n.op, (ast.USub, ast.UAdd)):
+            v = ev(n.operand)
+            return -v if isinstance(n.op, ast.USub) else v
+        if isinstance(n, ast.BinOp) and isinstance(n.op, (ast.Add, ast.Sub, ast.Mult, ast.Div)):
+            a, b = ev(n.left), ev(n.right)
+            return {ast.Add: a + b, ast.Sub: a - b, ast.Mult: a * b, ast.Div: a / b}[type(n.op)]
+        if (isinstance(n, ast.Call) and isinstance(n.func, ast.Name) and n.func.id == "sqrt" and len(n.args) == 1):
+            return math.sqrt(ev(n.args[0]))
+        raise ValueError("unsupported expression: " + ast.dump(n))
+
+    return [ev(ast.parse(part.strip(), mode="eval").body) for part in expr.split(",")]
+
+
+def pose_extrinsics_scenarios(root, here):
+    text = re.sub(r"//[^\n]*", "", open(os.path.join(root, POSE_EXTRINSICS_TEST)).read())
+    setup = text[text.index("virtual void SetUp()"):text.index("void addPriorOn_T_B_I")]
+    values = {}
+    for m in re.finditer(r"(prior_\w+)(\.coeffs\(\))?\s*<<\s*([^;]+);", setup):
+        values[m.group(1)] = _eval_list(m.group(3))
+    # The parameter blocks are built from those values (SetUp): the keyframe
+    # blocks as q_G_I coefficients | p_G_I, the extrinsics block as the
+    # coefficients of q_B_I's inverse | p_B_I.
+    assert "pose_G_Ik_ << prior_orientation_G_Ik_.coeffs(), prior_position_G_Ik_" in " ".join(setup.split())
+    assert "orientation_B_I_ << prior_orientation_B_I_.inverse().coeffs()" in " ".join(setup.split())
+    normalized = set(re.findall(r"(\w+)\.coeffs\(\)\.normalize\(\);", setup))
+    for name in normalized:
+        v = values[name]
+        n = math.sqrt(sum(x * x for x in v))
+        values[name] = [x / n for x in v]
+    fixture = {
+        "p_G_Ik": values["prior_position_G_Ik_"], "p_G_Ikp1": values["prior_position_G_Ikp1_"],
+        "p_B_I": values["prior_position_B_I_"],
+        "q_G_Ik": values["prior_orientation_G_Ik_"], "q_G_Ikp1": values["prior_orientation_G_Ikp1_"],
+        "q_B_I": values["prior_orientation_B_I_"],
+        "quaternions": "Hamilton, x y z w (Eigen coeffs)",
+        "covariance": "identity" if "T_Bk_Bkp1_measurement_covariance_matrix_.setIdentity()" in setup else None,
+    }
+    assert fixture["covariance"] == "identity"
+    getters = {"get_T_G_Ik()": "T_G_Ik", "get_T_G_Ikp1()": "T_G_Ikp1", "get_T_B_I()": "T_B_I"}
+    tests = []
+    for m in re.finditer(r"TEST_F\(\s*\w+,\s*(\w+)\)\s*\{", text):
+        name = m.group(1)
+        depth, i = 0, m.end() - 1
+        for j in range(i, len(text)):
+            depth += {"{": 1, "}": -1}.get(text[j], 0)
+            if depth == 0:
+                break
+        body = text[i + 1:j]
+        if name.startswith("DISABLED_"):
+            tests.append({"name": name, "skipped": "disabled in the reference"})
+            continue
+        case = {"name": name, "fixed": [], "expect": []}
+        local = {}
+        for stmt in [s.strip() for s in body.split(";") if s.strip()]:
+            stmt = " ".join(stmt.split())
+            mm = re.fullmatch(r"const aslam::Transformation (\w+) = (.+)", stmt)
+            if mm:
+                factors = []
+                for f in mm.group(2).split(" * "):
+                    inv = f.endswith(".inverse()")
+                    g = f[:-len(".inverse()")] if inv else f
+                    factors.append([getters[g], -1 if inv else 1])
+                local[mm.group(1)] = factors
+                continue
+            mm = re.fullmatch(r"add_T_Bk_Bkp1_Measurement\((.+)\)", stmt)
+            if mm:
+                arg = mm.group(1)
+                case["measurement"] = [] if arg == "aslam::Transformation()" else local[arg]
+                continue
+            mm = re.fullmatch(r"fix_(T_\w+)\(\)", stmt)
+            if mm:
+                case["fixed"].append(mm.group(1))
+                continue
+            if stmt == "solve()":
+                continue
+            mm = re.fullmatch(r"EXPECT_NEAR\(summary_\.(initial_cost|final_cost), ([-+.\deE]+), ([-+.\deE]+)\)", stmt)
+            if mm:
+                case["expect"].append({"what": mm.group(1), "value": float(mm.group(2)), "tol": float(mm.group(3))})
+                continue
+            mm = re.fullmatch(r"EXPECT_TRUE\( EIGEN_MATRIX_NEAR\( (get_T_\w+\(\))\.getTransformationMatrix\(\), "
+                              r"(get_T_\w+\(\))\.getTransformationMatrix\(\), ([-+.\deE]+)\)\)", stmt)
+            if mm:
+                case["expect"].append({"what": "same_transform", "a": getters[mm.group(1)],
+                                       "b": getters[mm.group(2)], "tol": float(mm.group(3))})
+                continue
+            raise ValueError(f"{name}: unsupported statement: {stmt}")
+        tests.append(case)
+    out = {"generator": "tests/golden/make_golden.py", "source": POSE_EXTRINSICS_TEST,
+           "fixture": fixture, "tests": tests}
+    with open(os.path.join(here, "pose_extrinsics_scenarios.json"), "w") as f:
+        json.dump(out, f, indent=1)
+    print("wrote", os.path.join(here, "pose_extrinsics_scenarios.json"))
 
 
 if __name__ == "__main__":
