@@ -11,7 +11,11 @@ algorithms/imu-integrator-rk4/test/test_imu_integrator_cov_phi_test.cc
 15x15 transition and 15x15 covariance at 1e-12) and the closed-form cases of
 test_imu_integrator_basic_test.cc (restated as inputs + expected outputs).
 The numbers are copied verbatim from the reference tests; nothing is
-recomputed here.
+recomputed here.  It also writes reference_sensors.json (maplab's own
+calibration files), error_term_scenarios.json (the visual and inertial
+cost-term tests, via error_term_scenarios.py), pose_extrinsics_scenarios.json
+(the relative pose term with extrinsics) and pose_parameterization_scenario.json
+(JplPoseParameterization's minimization test).
 """
 import json
 import math
@@ -113,6 +117,7 @@ def main(root):
     print("wrote", os.path.join(here, "imu_integrator.json"))
     sensor_files(root, here)
     pose_extrinsics_scenarios(root, here)
+    pose_parameterization_scenario(root, here)
     sys.path.insert(0, here)
     import error_term_scenarios
     with open(os.path.join(here, "error_term_scenarios.json"), "w") as f:
@@ -243,6 +248,36 @@ def pose_extrinsics_scenarios(root, here):
     with open(os.path.join(here, "pose_extrinsics_scenarios.json"), "w") as f:
         json.dump(out, f, indent=1)
     print("wrote", os.path.join(here, "pose_extrinsics_scenarios.json"))
+
+
+# JplPoseParameterization's own test: a pose block pulled onto a reference
+# transformation by a 6-dim error (2 vec(q (x) q_ref^-1) | p - p_ref) under the
+# pose parameterization, with Ceres' default options.
+POSE_PARAM_TEST = "algorithms/ceres-error-terms/test/test_pose_parameterization_test.cc"
+
+
+def pose_parameterization_scenario(root, here):
+    text = re.sub(r"//[^\n]*", "", open(os.path.join(root, POSE_PARAM_TEST)).read())
+    body = text[text.index("TEST(JplPoseParameterization, SimpleMinimization)"):]
+    vals = {}
+    for m in re.finditer(r"pose::(Quaternion|Position3D) ((?:x|reference)_(?:rot|pos))\(([^;]*)\);", body):
+        vals[m.group(2)] = _eval_list(m.group(3))
+    wxyz = lambda q: [q[1], q[2], q[3], q[0]]  # kindr (w, x, y, z) -> Eigen coeffs (x, y, z, w)
+    flat = " ".join(body.split())
+    assert "x_pose << x_rot.toImplementation().coeffs(), x_pos" in flat
+    assert "pose::Transformation reference(reference_pos, reference_rot)" in flat
+    assert "ceres::Solver::Options options; options.minimizer_progress_to_stdout = false; ceres::Solver::Summary" in flat
+    tol_q = float(re.search(r"EXPECT_NEAR_KINDR_QUATERNION\(out_rot, reference_rot, ([-+.\deE]+)\)", flat).group(1))
+    tol_p = float(re.search(r"EXPECT_NEAR_EIGEN\(out_pos, reference_pos, ([-+.\deE]+)\)", flat).group(1))
+    out = {"generator": "tests/golden/make_golden.py", "source": POSE_PARAM_TEST,
+           "name": "JplPoseParameterization.SimpleMinimization",
+           "quaternions": "Hamilton, x y z w (Eigen coeffs)",
+           "x_q": wxyz(vals["x_rot"]), "x_p": vals["x_pos"],
+           "reference_q": wxyz(vals["reference_rot"]), "reference_p": vals["reference_pos"],
+           "options": "Ceres defaults", "tol_rotation": tol_q, "tol_position": tol_p}
+    with open(os.path.join(here, "pose_parameterization_scenario.json"), "w") as f:
+        json.dump(out, f, indent=1)
+    print("wrote", os.path.join(here, "pose_parameterization_scenario.json"))
 
 
 if __name__ == "__main__":

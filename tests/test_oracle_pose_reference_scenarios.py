@@ -130,3 +130,64 @@ def test_reference_pose_extrinsics_case(case):
     # the constant keyframe did not move
     if "T_G_Ik" in case["fixed"]:
         assert np.array_equal(state[0], np.asarray(own.a["kf_q_IM_p_MI"][0]))
+
+
+# JplPoseParameterization's own test (test_pose_parameterization_test.cc,
+# tests/golden/pose_parameterization_scenario.json): a pose block pulled onto
+# a reference transformation by the error (2 vec(q (x) q_ref^-1) | p - p_ref)
+# under the pose parameterization, Ceres' default options.  That error is the
+# absolute 6-DoF term (BlockPosePriorErrorTermV2) with an identity baseframe,
+# identity sensor extrinsics and identity covariance (its rows in the other
+# order and, where w < 0, with the opposite sign: the same cost and minimum),
+# so the case runs as one keyframe with one absolute pose edge.
+PARAM = json.load(open(os.path.join(HERE, "golden", "pose_parameterization_scenario.json")))
+
+
+def _hprod(a, b):
+    ax, ay, az, aw = a
+    bx, by, bz, bw = b
+    return np.array([aw * bx + ax * bw + ay * bz - az * by, aw * by - ax * bz + ay * bw + az * bx,
+                     aw * bz + ax * by - ay * bx + az * bw, aw * bw - ax * bx - ay * by - az * bz])
+
+
+def _disparity_angle(a, b):
+    """Rotation angle between two Hamilton quaternions (either sign)."""
+    d = _hprod(np.asarray(a) / np.linalg.norm(a), np.array([-b[0], -b[1], -b[2], b[3]]) / np.linalg.norm(b))
+    return 2.0 * np.arctan2(np.linalg.norm(d[:3]), abs(d[3]))
+
+
+def test_reference_pose_parameterization_minimization():
+    assert PARAM["source"].endswith("test_pose_parameterization_test.cc")
+    own = U.OwnedDesc(obs_uv=np.zeros((0, 2)), obs_sigma=np.zeros(0), obs_landmark=np.zeros(0),
+                      obs_keyframe=np.zeros(0), obs_camera=np.zeros(0), lm_p_B=np.zeros((0, 3)),
+                      lm_store_keyframe=np.zeros(0), kf_q_IM_p_MI=[list(PARAM["x_q"]) + list(PARAM["x_p"])],
+                      cameras=[U.camera()])
+    a = own.a
+    a["pe_from"] = np.array([0], dtype=np.int32)
+    a["pe_to"] = np.array([0], dtype=np.int32)
+    a["pe_type"] = np.array([N.MBA_POSE_EDGE_ABSOLUTE], dtype=np.int32)
+    a["pe_meas"] = np.ascontiguousarray(np.concatenate([PARAM["reference_q"], PARAM["reference_p"]]))  # T_G_S
+    a["pe_cov"] = np.ascontiguousarray(np.eye(6).ravel())
+    a["pe_ext"] = np.ascontiguousarray([0.0, 0.0, 0.0, 1.0, 0.0, 0.0, 0.0])  # T_S_B = identity
+    d = own.desc
+    d.num_pose_edges = 1
+    d.pose_edge_from = N.ptr(a["pe_from"], ctypes.c_int32)
+    d.pose_edge_to = N.ptr(a["pe_to"], ctypes.c_int32)
+    d.pose_edge_type = N.ptr(a["pe_type"], ctypes.c_int32)
+    d.pose_edge_T_Bk_Bkp1 = N.ptr(a["pe_meas"])
+    d.pose_edge_covariance = N.ptr(a["pe_cov"])
+    d.pose_edge_q_I_B_p_B_I = N.ptr(a["pe_ext"])
+    o = O.OracleProblem(d)
+    opts = N.default_solver_options()
+    opts.linear_solver = N.MBA_LINEAR_SOLVER_DENSE_SCHUR
+    # Ceres' defaults (ceres::Solver::Options)
+    opts.max_num_iterations = 50
+    opts.function_tolerance = 1e-6
+    opts.gradient_tolerance = 1e-10
+    opts.parameter_tolerance = 1e-8
+    opts.initial_trust_region_radius = 1e4
+    s = o.solve(opts)
+    x = o.read_state()["kf_q_IM_p_MI"][0]
+    assert s["initial_cost"] > 1.0
+    assert _disparity_angle(x[:4], PARAM["reference_q"]) <= PARAM["tol_rotation"]
+    assert np.abs(x[4:] - np.asarray(PARAM["reference_p"])).max() <= PARAM["tol_position"]
