@@ -14,8 +14,9 @@ The numbers are copied verbatim from the reference tests; nothing is
 recomputed here.  It also writes reference_sensors.json (maplab's own
 calibration files), error_term_scenarios.json (the visual and inertial
 cost-term tests, via error_term_scenarios.py), pose_extrinsics_scenarios.json
-(the relative pose term with extrinsics) and pose_parameterization_scenario.json
-(JplPoseParameterization's minimization test).
+(the relative pose term with extrinsics), pose_parameterization_scenario.json
+(JplPoseParameterization's minimization test) and camera_scenarios.json
+(aslam's pinhole camera and distortion tests).
 """
 import json
 import math
@@ -118,6 +119,7 @@ def main(root):
     sensor_files(root, here)
     pose_extrinsics_scenarios(root, here)
     pose_parameterization_scenario(root, here)
+    camera_scenarios(root, here)
     sys.path.insert(0, here)
     import error_term_scenarios
     with open(os.path.join(here, "error_term_scenarios.json"), "w") as f:
@@ -278,6 +280,77 @@ def pose_parameterization_scenario(root, here):
     with open(os.path.join(here, "pose_parameterization_scenario.json"), "w") as f:
         json.dump(out, f, indent=1)
     print("wrote", os.path.join(here, "pose_parameterization_scenario.json"))
+
+
+# aslam's camera and distortion tests for the models the visual term uses
+# (pinhole with radtan, equidistant, fisheye = FOV, or no distortion): the
+# test objects' parameters (createTestDistortion, createTestCamera), the
+# Jacobian checks' points, finite-difference steps and tolerances, the manual
+# projection and the projection-status cases.
+CAMERA_DIR = "aslam_cv2/aslam_cv_cameras"
+
+
+def camera_scenarios(root, here):
+    inc = os.path.join(root, CAMERA_DIR, "include", "aslam", "cameras")
+    dist = {}
+    for name, header, n in (("radtan", "distortion-radtan.h", 4), ("equidistant", "distortion-equidistant.h", 4),
+                            ("fov", "distortion-fisheye.h", 1)):
+        text = open(os.path.join(inc, header)).read()
+        body = text[text.index("createTestDistortion()"):]
+        m = re.search(r"Eigen::VectorXd params\((\d+)\);\s*params\s*<<\s*([^;]+);", body)
+        assert int(m.group(1)) == n
+        dist[name] = _eval_list(m.group(2))
+    pin_h = " ".join(open(os.path.join(inc, "camera-pinhole.h")).read().split())
+    m = re.search(r"createTestCameraUnique\(\) \{ Distortion::UniquePtr distortion = DistortionType::createTestDistortion\(\); "
+                  r"PinholeCamera::UniquePtr camera\( new PinholeCamera\(([^)]*), distortion\)\);", pin_h)
+    test_camera = _eval_list(m.group(1))
+    pin_cc = " ".join(open(os.path.join(root, CAMERA_DIR, "src", "camera-pinhole.cc")).read().split())
+    m = re.search(r"PinholeCamera::Ptr PinholeCamera::createTestCamera\(\) \{ PinholeCamera::Ptr camera\(new PinholeCamera\(([^)]*)\)\);",
+                  pin_cc)
+    plain_camera = _eval_list(m.group(1))
+    tdist = " ".join(re.sub(r"//[^\n]*", "", open(os.path.join(root, CAMERA_DIR, "test", "test-distortions.cc")).read()).split())
+    jk = re.search(r"TYPED_TEST\(TestDistortions, JacobianWrtKeypoint\) \{ Eigen::Vector2d keypoint\(([^)]*)\);.*?"
+                   r"TEST_JACOBIAN_FINITE_DIFFERENCE\(Point3dJacobianFunctor, keypoint, ([^,]+), ([^,]+),", tdist)
+    jd = re.search(r"TYPED_TEST\(TestDistortionsNotNull, JacobianWrtDistortion\) \{ Eigen::Vector2d keypoint\(([^)]*)\);.*?"
+                   r"TEST_JACOBIAN_FINITE_DIFFERENCE\(DistortionJacobianFunctor<TypeParam::parameterCount\(\)>, "
+                   r"dist_coeffs, ([^,]+), ([^,]+),", tdist)
+    tcam = " ".join(re.sub(r"//[^\n]*", "", open(os.path.join(root, CAMERA_DIR, "test", "test-cameras.cc")).read()).split())
+    jp = re.search(r"TYPED_TEST\(TestCameras, JacobianWrtPoint3d\) \{ for \(int i=0; i<(\d+); i\+\+\) \{ "
+                   r"Eigen::Vector3d x = this->camera_->createRandomVisiblePoint\(([^)]*)\); "
+                   r"TEST_JACOBIAN_FINITE_DIFFERENCE\(Point3dFunctor, x, ([^,]+), ([^,]+),", tcam)
+    ji = re.search(r"TYPED_TEST\(TestCameras, JacobianWrtIntrinsics\) \{.*?createRandomVisiblePoint\(([^)]*)\);.*?"
+                   r"TEST_JACOBIAN_FINITE_DIFFERENCE\(IntrinsicJacobianFunctor<[^>]*>, intrinsics, ([^,]+), ([^,]+),", tcam)
+    jdc = re.search(r"TYPED_TEST\(TestCameras, JacobianWrtDistortion\) \{.*?createRandomVisiblePoint\(([^)]*)\);.*?"
+                    r"TEST_JACOBIAN_FINITE_DIFFERENCE\(DistortionJacobianFunctor<[^>]*>, dist_coeffs, ([^,]+), ([^,]+) ?,", tcam)
+    mp = re.search(r"TEST\(TestCameraPinhole, ManualProjectionWithoutDistortion\) \{.*?double kx = ([^,]+), ky = ([^,]+), "
+                   r"kz = ([^;]+);.*?EXPECT_TRUE\(EIGEN_MATRIX_NEAR\(keypoint_manual, keypoint, ([^)]+)\)\);", tcam)
+    pr_body = tcam[tcam.index("TEST(TestCameraPinhole, ProjectionResult)"):tcam.index("TEST(CameraComparison, TestEquality)")]
+    status = []
+    for m in re.finditer(r"ret = cam->project3\(Eigen::Vector3d\(([^)]*)\), &keypoint\); "
+                         r"EXPECT_EQ\(ret.getDetailedStatus\(\), aslam::ProjectionResult::Status::(\w+)\);", pr_body):
+        status.append({"point": _eval_list(m.group(1)), "status": m.group(2)})
+    assert len(status) == 4, status
+    f = lambda s: float(s.strip())
+    out = {"generator": "tests/golden/make_golden.py", "source": CAMERA_DIR + "/test/test-cameras.cc, test-distortions.cc",
+           "distortions": dist,
+           "test_camera": {"fu": test_camera[0], "fv": test_camera[1], "cu": test_camera[2], "cv": test_camera[3],
+                           "width": test_camera[4], "height": test_camera[5]},
+           "plain_camera": {"fu": plain_camera[0], "fv": plain_camera[1], "cu": plain_camera[2], "cv": plain_camera[3],
+                            "width": plain_camera[4], "height": plain_camera[5]},
+           "numdiff": "five-point central stencil, h = sqrt(step) |x_j| (sqrt(step) where x_j = 0)",
+           "distortion_jacobian_wrt_keypoint": {"keypoint": _eval_list(jk.group(1)), "step": f(jk.group(2)),
+                                                "tol": f(jk.group(3))},
+           "distortion_jacobian_wrt_parameters": {"keypoint": _eval_list(jd.group(1)), "step": f(jd.group(2)),
+                                                  "tol": f(jd.group(3))},
+           "camera_jacobian_wrt_point": {"points": int(jp.group(1)), "depth": f(jp.group(2)), "step": f(jp.group(3)),
+                                         "tol": f(jp.group(4))},
+           "camera_jacobian_wrt_intrinsics": {"depth": f(ji.group(1)), "step": f(ji.group(2)), "tol": f(ji.group(3))},
+           "camera_jacobian_wrt_distortion": {"depth": f(jdc.group(1)), "step": f(jdc.group(2)), "tol": f(jdc.group(3))},
+           "manual_projection": {"point": [f(mp.group(1)), f(mp.group(2)), f(mp.group(3))], "tol": f(mp.group(4))},
+           "projection_status": status}
+    with open(os.path.join(here, "camera_scenarios.json"), "w") as fh:
+        json.dump(out, fh, indent=1)
+    print("wrote", os.path.join(here, "camera_scenarios.json"))
 
 
 if __name__ == "__main__":
