@@ -15,8 +15,9 @@ recomputed here.  It also writes reference_sensors.json (maplab's own
 calibration files), error_term_scenarios.json (the visual and inertial
 cost-term tests, via error_term_scenarios.py), pose_extrinsics_scenarios.json
 (the relative pose term with extrinsics), pose_parameterization_scenario.json
-(JplPoseParameterization's minimization test) and camera_scenarios.json
-(aslam's pinhole camera and distortion tests).
+(JplPoseParameterization's minimization test), camera_scenarios.json
+(aslam's pinhole camera and distortion tests) and quaternion_math.json
+(maplab-common's JPL rotation-matrix known answer).
 """
 import json
 import math
@@ -120,6 +121,7 @@ def main(root):
     pose_extrinsics_scenarios(root, here)
     pose_parameterization_scenario(root, here)
     camera_scenarios(root, here)
+    quaternion_math_cases(root, here)
     sys.path.insert(0, here)
     import error_term_scenarios
     with open(os.path.join(here, "error_term_scenarios.json"), "w") as f:
@@ -351,6 +353,27 @@ def camera_scenarios(root, here):
     with open(os.path.join(here, "camera_scenarios.json"), "w") as fh:
         json.dump(out, fh, indent=1)
     print("wrote", os.path.join(here, "camera_scenarios.json"))
+
+
+# maplab-common's JPL rotation-matrix known answer (the only case of
+# test-quaternion-math.cc on the visual and inertial terms' path; the others
+# test the inverse map, axis-angle and yaw helpers, which the path does not use).
+QUAT_TEST = "common/maplab-common/test/test-quaternion-math.cc"
+
+
+def quaternion_math_cases(root, here):
+    text = " ".join(re.sub(r"//[^\n]*", "", open(os.path.join(root, QUAT_TEST)).read()).split())
+    m = re.search(r"TEST\(QuaternionMath, toRotationMatrixJPL\) \{ Eigen::Vector4d quat_coeff_xyzw; "
+                  r"quat_coeff_xyzw << ([^;]+); Eigen::Matrix3d expected_rotation_matrix; "
+                  r"expected_rotation_matrix << ([^;]+); Eigen::Matrix3d rotation_matrix; "
+                  r"common::toRotationMatrixJPL\(quat_coeff_xyzw, &rotation_matrix\); "
+                  r"EXPECT_NEAR_EIGEN\(expected_rotation_matrix, rotation_matrix, ([^)]+)\);", text)
+    out = {"generator": "tests/golden/make_golden.py", "source": QUAT_TEST,
+           "toRotationMatrixJPL": {"q_xyzw": _eval_list(m.group(1)), "R_row_major": _eval_list(m.group(2)),
+                                   "tol": float(m.group(3))}}
+    with open(os.path.join(here, "quaternion_math.json"), "w") as fh:
+        json.dump(out, fh, indent=1)
+    print("wrote", os.path.join(here, "quaternion_math.json"))
 
 
 if __name__ == "__main__":

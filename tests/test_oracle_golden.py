@@ -48,3 +48,15 @@ def test_rk4_basic_golden(case):
     if "expected_velocity" in case:
         np.testing.assert_allclose(nxt[7:10], case["expected_velocity"], rtol=0, atol=case["tol"])
         np.testing.assert_allclose(nxt[13:16], case["expected_position"], rtol=0, atol=case["tol"])
+
+
+QUAT = json.load(open(os.path.join(os.path.dirname(__file__), "golden", "quaternion_math.json")))
+
+
+def test_jpl_rotation_matrix_golden():
+    """maplab-common's toRotationMatrixJPL known answer
+    (common/maplab-common/test/test-quaternion-math.cc)."""
+    case = QUAT["toRotationMatrixJPL"]
+    R = np.zeros(9)
+    O.load().oracle_rotation_matrix(N.ptr(O.arr(case["q_xyzw"])), N.ptr(R))
+    assert np.abs(R - np.asarray(case["R_row_major"])).max() <= case["tol"]
