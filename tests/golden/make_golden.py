@@ -42,7 +42,9 @@ def _test_body(text, name):
     return text[i:j]
 
 
-def main(root):
+def main(root, here=None):
+    """Writes every fixture into `here` (default: this file's directory)."""
+    here = here or os.path.dirname(os.path.abspath(__file__))
     base = os.path.join(root, "algorithms", "imu-integrator-rk4", "test")
     src = open(os.path.join(base, "test_imu_integrator_cov_phi_test.cc")).read()
     phi_body = _test_body(src, "ImuIntegratorPhiTest")
@@ -113,7 +115,6 @@ def main(root):
                   "expected_velocity": [0.5 * dt / 2, 0, 0],
                   "expected_position": [0.5 * dt * dt / 3, 0, 0], "tol": 1e-15})
     out = {"generator": "tests/golden/make_golden.py", "cases": cases, "basic": basic}
-    here = os.path.dirname(os.path.abspath(__file__))
     with open(os.path.join(here, "imu_integrator.json"), "w") as f:
         json.dump(out, f, indent=1)
     print("wrote", os.path.join(here, "imu_integrator.json"))
@@ -122,7 +123,7 @@ def main(root):
     pose_parameterization_scenario(root, here)
     camera_scenarios(root, here)
     quaternion_math_cases(root, here)
-    sys.path.insert(0, here)
+    sys.path.insert(0, os.path.dirname(os.path.abspath(__file__)))
     import error_term_scenarios
     with open(os.path.join(here, "error_term_scenarios.json"), "w") as f:
         json.dump(error_term_scenarios.extract(root), f, indent=1)
